@@ -1,0 +1,509 @@
+"""Python mirror of feNG's operator API for the hot path.
+
+Names, argument order and meaning follow the reference so that a driver
+reads like feNG's own tests (tests/withLinearSolver/*.cpp):
+
+    mesh = Mesh2DP1.generate_square(64, jitter=0.1, seed=1)
+    u  = createFiniteElementSpace(mesh, LAGRANGE, 2, "U", "Domaine", 4, zero)
+    uB = createFiniteElementSpace(mesh, LAGRANGE, 2, "U", "Bord", 4, exact)
+    numbering = feMetaNumber(mesh, [uB, u], [uB])
+    diff = createBilinearForm([u], feSysElm_Diffusion(1.0))
+    src  = createBilinearForm([u], feSysElm_Source(SRC_SIN_SIN, [-2 pi^2]))
+    system = createLinearSystem(CUDA, [diff, src], numbering, options)
+    sol = feSolution(system)
+    sol.initializeEssentialBC()
+    stats = solveNewtonRaphson(system, sol, feNLSolverOptions(...))
+
+Every compute call goes through the C ABI of include/feng_cuda.h into the
+CUDA backend; nothing here computes element matrices or solves.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Callable, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, ptr
+
+LAGRANGE = "LAGRANGE"
+VECTOR_LAGRANGE = "VECTOR_LAGRANGE"
+CUDA = "CUDA"
+
+CNC = {"Domaine": 0, "Bord": 1, "PointPression": 2}
+
+# Form kinds (FE_FORM_* in include/feng_cuda.h)
+SOURCE, DIFFUSION, VECTOR_SOURCE, TRANSIENT_VECTOR_MASS = 1, 2, 3, 4
+MIXED_DIVERGENCE, VECTOR_CONVECTIVE_ACCELERATION, DIV_NEWTONIAN_STRESS = 5, 6, 7
+# Device source registry (FE_SRC_*)
+SRC_NONE, SRC_SIN_SIN, SRC_NS_MMS_POLY, SRC_CONST_VEC, SRC_SIN_BODY = 0, 1, 2, 3, 4
+ELEM_P2, ELEM_TAYLOR_HOOD = 1, 2
+
+
+class Mesh2DP1:
+    """Triangle mesh with physical groups "Domaine", "Bord", "PointPression"."""
+
+    def __init__(self, handle):
+        self._h = handle
+        self._lib = _lib.load()
+
+    @classmethod
+    def generate_square(cls, n: int, x0=0.0, x1=1.0, y0=0.0, y1=1.0, jitter=0.1, seed=1):
+        lib = _lib.load()
+        h = C.c_void_p()
+        check(lib.fe_mesh_generate_square(n, x0, x1, y0, y1, jitter, seed, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_msh(cls, path: str):
+        lib = _lib.load()
+        h = C.c_void_p()
+        check(lib.fe_mesh_read_msh(str(path).encode(), C.byref(h)))
+        return cls(h)
+
+    def write_msh(self, path: str):
+        check(self._lib.fe_mesh_write_msh(self._h, str(path).encode()))
+
+    def sizes(self):
+        nv, nt, ne, nb = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        check(self._lib.fe_mesh_sizes(self._h, C.byref(nv), C.byref(nt), C.byref(ne), C.byref(nb)))
+        return nv.value, nt.value, ne.value, nb.value
+
+    def arrays(self):
+        nv, nt, ne, nb = self.sizes()
+        x = np.empty(nv); y = np.empty(nv)
+        tri = np.empty(3 * nt, np.int32); te = np.empty(3 * nt, np.int32)
+        bnd = np.empty(2 * nb, np.int32); pt = np.empty(1, np.int32)
+        check(self._lib.fe_mesh_arrays(self._h, ptr(x), ptr(y), ptr(tri), ptr(te), ptr(bnd), ptr(pt)))
+        return dict(x=x, y=y, tri=tri.reshape(-1, 3), tri_edges=te.reshape(-1, 3),
+                    bnd=bnd.reshape(-1, 2), point=int(pt[0]), n_edges=ne)
+
+    def getNumElements(self):
+        return self.sizes()[1]
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h:
+            self._lib.fe_mesh_destroy(h)
+
+
+@dataclass
+class feSpace:
+    mesh: Mesh2DP1
+    element: str
+    degree: int
+    fieldID: str
+    cncGeoID: str
+    degreeQuadrature: int
+    fct: Optional[Callable] = None
+
+    @property
+    def ncomp(self):
+        return 2 if self.element == VECTOR_LAGRANGE else 1
+
+
+def createFiniteElementSpace(mesh, element, degree, fieldID, cncGeoID, degreeQuadrature, fct=None):
+    """createFiniteElementSpace (src/feSpace.cpp:11-420) for the spaces the
+    backend supports: Lagrange P1/P2 (scalar or 2-vector) on "Domaine" and
+    "Bord", P0 on "PointPression"."""
+    if cncGeoID not in CNC:
+        raise ValueError(f"unknown connectivity {cncGeoID!r}")
+    if element not in (LAGRANGE, VECTOR_LAGRANGE):
+        raise ValueError(f"unsupported element {element!r}")
+    deg = 0 if cncGeoID == "PointPression" else degree
+    return feSpace(mesh, element, deg, fieldID, cncGeoID, degreeQuadrature, fct)
+
+
+class feMetaNumber:
+    """DOF numbering of feMetaNumber (src/feNumber.cpp:677-835)."""
+
+    def __init__(self, mesh, spaces: Sequence[feSpace], essentialSpaces: Sequence[feSpace]):
+        self.mesh = mesh
+        self.spaces = list(spaces)
+        self.essentialSpaces = list(essentialSpaces)
+        self.fieldIDs = []
+        for s in self.spaces:
+            if s.fieldID not in self.fieldIDs:
+                self.fieldIDs.append(s.fieldID)
+        for e in self.essentialSpaces:
+            if not any(e is s for s in self.spaces):
+                raise ValueError("every essential space must be listed among the spaces")
+        arr = (_lib.SpaceDesc * len(self.spaces))()
+        for i, s in enumerate(self.spaces):
+            arr[i] = _lib.SpaceDesc(self.fieldIDs.index(s.fieldID), s.degree, s.ncomp, CNC[s.cncGeoID],
+                                    int(any(s is e for e in self.essentialSpaces)))
+        self._desc = arr
+        dom = [s for s in self.spaces if s.cncGeoID == "Domaine"]
+        self.elem_type = ELEM_TAYLOR_HOOD if any(
+            s.element == VECTOR_LAGRANGE and s.degree == 2 for s in dom) else ELEM_P2
+        qdeg = {s.degreeQuadrature for s in dom}
+        if len(qdeg) != 1:
+            raise ValueError("the domain spaces must share one quadrature degree")
+        self.quad_degree = qdeg.pop()
+        self._setups = {}
+        st = self.setup()
+        self.nInc, self.nDofs = st.nInc, st.nDofs
+
+    def setup(self, pc_block_rows: int = 256) -> "feSetup":
+        """Host tables (numbering, element DOFs, coloring, pattern) for the backend."""
+        if pc_block_rows not in self._setups:
+            self._setups[pc_block_rows] = feSetup(self, pc_block_rows)
+        return self._setups[pc_block_rows]
+
+    def getNbUnknowns(self):
+        return self.nInc
+
+    def getNbDOFs(self):
+        return self.nDofs
+
+
+class feSetup:
+    """Host set-up of the standalone route (fe_setup_* in include/feng_cuda.h);
+    needs no GPU."""
+
+    def __init__(self, numbering: feMetaNumber, pc_block_rows: int = 256):
+        self.lib = _lib.load()
+        self.numbering = numbering
+        h = C.c_void_p()
+        check(self.lib.fe_setup_create(numbering.mesh._h, C.cast(numbering._desc, C.c_void_p),
+                                       len(numbering.spaces), numbering.elem_type,
+                                       numbering.quad_degree, pc_block_rows, C.byref(h)))
+        self._h = h
+        n = [C.c_int64() for _ in range(4)]
+        nc, nl = C.c_int(), C.c_int()
+        check(self.lib.fe_setup_sizes(h, *[C.byref(v) for v in n], C.byref(nc), C.byref(nl)))
+        self.nInc, self.nDofs, self.nnz, self.nElm = (v.value for v in n)
+        self.nColors, self.nloc = nc.value, nl.value
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h:
+            self.lib.fe_setup_destroy(h)
+
+    def pattern(self):
+        ia = np.empty(self.nInc + 1, np.int64)
+        ja = np.empty(self.nnz, np.int32)
+        check(self.lib.fe_setup_get_pattern(self._h, ptr(ia), ptr(ja)))
+        return ia, ja
+
+    def coloring(self):
+        off = np.empty(self.nColors + 1, np.int64)
+        el = np.empty(self.nElm, np.int32)
+        check(self.lib.fe_setup_get_coloring(self._h, ptr(off), ptr(el)))
+        return off, el
+
+    def elementDofs(self):
+        adr = np.empty(self.nElm * self.nloc, np.int64)
+        check(self.lib.fe_setup_get_element_dofs(self._h, ptr(adr)))
+        return adr.reshape(self.nElm, self.nloc)
+
+    def dofInfo(self):
+        x = np.empty(self.nDofs); y = np.empty(self.nDofs)
+        f = np.empty(self.nDofs, np.int32); c = np.empty(self.nDofs, np.int32)
+        v = np.empty(self.nDofs, np.int32)
+        check(self.lib.fe_setup_get_dof_info(self._h, ptr(x), ptr(y), ptr(f), ptr(c), ptr(v)))
+        return x, y, f, c, v
+
+    def blocks(self):
+        b = np.empty(self.nInc, np.int32)
+        check(self.lib.fe_setup_get_blocks(self._h, ptr(b)))
+        return b
+
+
+def quadrature_rule(degree: int):
+    """(r, s, w) of the triangle rule of the given degree."""
+    lib = _lib.load()
+    n = C.c_int()
+    r, s, w = np.empty(16), np.empty(16), np.empty(16)
+    check(lib.fe_quadrature_rule(degree, C.byref(n), ptr(r), ptr(s), ptr(w)))
+    k = n.value
+    return r[:k].copy(), s[:k].copy(), w[:k].copy()
+
+
+@dataclass
+class feSysElm:
+    kind: int
+    coeff: float = 1.0
+    coeff2: float = 0.0
+    source: int = SRC_NONE
+    params: tuple = (0.0, 0.0, 0.0, 0.0)
+
+
+def feSysElm_Diffusion(coeff=1.0):
+    return feSysElm(DIFFUSION, coeff)
+
+
+def feSysElm_Source(source=SRC_SIN_SIN, params=(1.0,), coeff=1.0):
+    return feSysElm(SOURCE, coeff, 0.0, source, tuple(params) + (0.0,) * (4 - len(params)))
+
+
+def feSysElm_VectorSource(source=SRC_NS_MMS_POLY, params=(), coeff=1.0):
+    return feSysElm(VECTOR_SOURCE, coeff, 0.0, source, tuple(params) + (0.0,) * (4 - len(params)))
+
+
+def feSysElm_VectorConvectiveAcceleration(coeff=1.0):
+    return feSysElm(VECTOR_CONVECTIVE_ACCELERATION, coeff)
+
+
+def feSysElm_MixedDivergence(coeff=1.0):
+    return feSysElm(MIXED_DIVERGENCE, coeff)
+
+
+def feSysElm_DivergenceNewtonianStress(coeff=1.0, viscosity=1.0):
+    return feSysElm(DIV_NEWTONIAN_STRESS, coeff, viscosity)
+
+
+def feSysElm_TransientVectorMass(coeff=1.0):
+    return feSysElm(TRANSIENT_VECTOR_MASS, coeff)
+
+
+@dataclass
+class feBilinearForm:
+    spaces: list
+    sysElm: feSysElm
+
+
+def createBilinearForm(spaces, sysElm):
+    return feBilinearForm(list(spaces), sysElm)
+
+
+@dataclass
+class LinearSolverOptions:
+    krylov: str = "fgmres"        # "cg" | "fgmres"
+    restart: int = 50
+    max_iter: int = 10000
+    rel_tol: float = 1e-8         # feLinearSystem::_rel_tol (src/feLinearSystem.h:66)
+    abs_tol: float = 1e-14
+    div_tol: float = 1e6
+    precond: str = "bjacobi-ilu0"  # "none" | "bjacobi-ilu0" | "ilu0" | "jacobi"
+    pc_block_rows: int = 256
+    precision: str = "fp64"       # "fp64" | "mixed"
+
+    def to_c(self, quad_degree: int) -> _lib.Options:
+        pc = {"none": 0, "bjacobi-ilu0": 1, "ilu0": 1, "jacobi": 2}[self.precond]
+        rows = 0 if self.precond == "ilu0" else self.pc_block_rows
+        return _lib.Options(0 if self.krylov == "cg" else 1, self.restart, self.max_iter, self.rel_tol,
+                            self.abs_tol, self.div_tol, pc, rows,
+                            1 if self.precision == "mixed" else 0, quad_degree)
+
+
+class feLinearSystemCUDA:
+    """The CUDA backend behind the feLinearSystem interface
+    (src/feLinearSystem.h:43-169)."""
+
+    def __init__(self, forms: Sequence[feBilinearForm], numbering: feMetaNumber,
+                 options: LinearSolverOptions | None = None):
+        self.lib = _lib.load()
+        self.forms = list(forms)
+        self.numbering = numbering
+        self.options = options or LinearSolverOptions()
+        self.elem_type = numbering.elem_type
+        qdeg = {s.degreeQuadrature for f in self.forms for s in f.spaces}
+        if qdeg != {numbering.quad_degree}:
+            raise ValueError("all forms must use the quadrature rule of the domain spaces")
+        self.quad_degree = numbering.quad_degree
+        rows = 0 if self.options.precond == "ilu0" else self.options.pc_block_rows
+        self.setup = numbering.setup(rows)
+        fa = (_lib.FormDesc * len(self.forms))()
+        for i, f in enumerate(self.forms):
+            se = f.sysElm
+            fa[i] = _lib.FormDesc(se.kind, se.coeff, se.coeff2, se.source, (C.c_double * 4)(*se.params))
+        opts = self.options.to_c(self.quad_degree)
+        h = C.c_void_p()
+        check(self.lib.fe_cuda_system_create(self.setup._h, C.cast(fa, C.c_void_p), len(self.forms),
+                                             C.byref(opts), C.byref(h)))
+        self._h = h
+        n = [C.c_int64() for _ in range(4)]
+        nc = C.c_int()
+        check(self.lib.fe_cuda_system_sizes(h, *[C.byref(v) for v in n], C.byref(nc)))
+        self.nInc, self.nDofs, self.nnz, self.nElm = (v.value for v in n)
+        self.nColors = nc.value
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h:
+            self.lib.fe_cuda_system_destroy(h)
+
+    # -- feLinearSystem operations
+    def getSystemSize(self):
+        return self.nInc
+
+    def setToZero(self):
+        check(self.lib.fe_cuda_set_to_zero(self._h))
+
+    def setMatrixToZero(self):
+        check(self.lib.fe_cuda_set_matrix_to_zero(self._h))
+
+    def setResidualToZero(self):
+        check(self.lib.fe_cuda_set_residual_to_zero(self._h))
+
+    def assembleResiduals(self):
+        check(self.lib.fe_cuda_assemble_residuals(self._h))
+
+    def assembleMatrices(self):
+        check(self.lib.fe_cuda_assemble_matrices(self._h))
+
+    def assemble(self):
+        self.assembleMatrices()
+        self.assembleResiduals()
+
+    def getRHSMaxNorm(self):
+        v = C.c_double()
+        check(self.lib.fe_cuda_get_rhs_max_norm(self._h, C.byref(v)))
+        return v.value
+
+    def solve(self, raise_on_failure=True):
+        dx, rhs, axb, it = C.c_double(), C.c_double(), C.c_double(), C.c_int()
+        s = self.lib.fe_cuda_solve(self._h, C.byref(dx), C.byref(rhs), C.byref(axb), C.byref(it))
+        if raise_on_failure:
+            check(s)
+        return dict(status=s, normDx=dx.value, normRHS=rhs.value, normAxb=axb.value,
+                    nIter=it.value)
+
+    def correctSolution(self):
+        check(self.lib.fe_cuda_correct_solution(self._h))
+
+    # -- state
+    def setSolution(self, u, udot=None):
+        u = np.ascontiguousarray(u, np.float64)
+        ud = None if udot is None else np.ascontiguousarray(udot, np.float64)
+        check(self.lib.fe_cuda_set_solution(self._h, ptr(u), ptr(ud)))
+
+    def getSolution(self):
+        u = np.empty(self.nDofs)
+        check(self.lib.fe_cuda_get_solution(self._h, ptr(u)))
+        return u
+
+    def setTime(self, t, c0=0.0):
+        check(self.lib.fe_cuda_set_time(self._h, t, c0))
+
+    def setBDF(self, order, cn, hist1=None, hist2=None):
+        cn = np.ascontiguousarray(np.resize(np.asarray(cn, np.float64), 3))
+        h1 = None if hist1 is None else np.ascontiguousarray(hist1, np.float64)
+        h2 = None if hist2 is None else np.ascontiguousarray(hist2, np.float64)
+        check(self.lib.fe_cuda_set_bdf(self._h, order, ptr(cn), ptr(h1), ptr(h2)))
+
+    # -- views for checks
+    def getMatrix(self):
+        v = np.empty(self.nnz)
+        check(self.lib.fe_cuda_get_matrix(self._h, ptr(v)))
+        return v
+
+    def getRHS(self):
+        v = np.empty(self.nInc)
+        check(self.lib.fe_cuda_get_rhs(self._h, ptr(v)))
+        return v
+
+    def getDu(self):
+        v = np.empty(self.nInc)
+        check(self.lib.fe_cuda_get_du(self._h, ptr(v)))
+        return v
+
+    def pattern(self):
+        ia = np.empty(self.nInc + 1, np.int64)
+        ja = np.empty(self.nnz, np.int32)
+        check(self.lib.fe_cuda_get_pattern(self._h, ptr(ia), ptr(ja)))
+        return ia, ja
+
+    def coloring(self):
+        off = np.empty(self.nColors + 1, np.int64)
+        el = np.empty(self.nElm, np.int32)
+        check(self.lib.fe_cuda_get_coloring(self._h, ptr(off), ptr(el)))
+        return off, el
+
+    def elementDofs(self):
+        return self.setup.elementDofs()
+
+    def dofInfo(self):
+        return self.setup.dofInfo()[:4]
+
+    def times(self):
+        v = [C.c_double() for _ in range(4)]
+        check(self.lib.fe_cuda_get_times(self._h, *[C.byref(t) for t in v]))
+        return dict(zip(("residual_ms", "matrix_ms", "factor_ms", "solve_ms"), (t.value for t in v)))
+
+    def resetTimes(self):
+        check(self.lib.fe_cuda_reset_times(self._h))
+
+    def synchronize(self):
+        check(self.lib.fe_cuda_synchronize(self._h))
+
+
+def createLinearSystem(kind, forms, numbering, options: LinearSolverOptions | None = None):
+    if kind != CUDA:
+        raise ValueError("only the CUDA backend is provided")
+    return feLinearSystemCUDA(forms, numbering, options)
+
+
+class feSolution:
+    """Host view of the solution vector; the authoritative copy lives on the device."""
+
+    def __init__(self, system: feLinearSystemCUDA):
+        self.system = system
+        self.u = np.zeros(system.nDofs)
+        self.udot = np.zeros(system.nDofs)
+        self.t = 0.0
+        self.c0 = 0.0
+        self.dof_x, self.dof_y, self.dof_field, self.dof_comp = system.dofInfo()
+
+    def initializeEssentialBC(self, t: float = 0.0):
+        """Nodewise essential values (feSolution::initializeEssentialBC,
+        src/feSolution.cpp:246-...): the function of each field's essential
+        space evaluated at the DOF locations (vertices, edge midpoints)."""
+        num = self.system.numbering
+        ess = np.arange(self.system.nInc, self.system.nDofs)
+        for fi, fid in enumerate(num.fieldIDs):
+            spaces = [s for s in num.essentialSpaces if s.fieldID == fid and s.fct is not None]
+            if not spaces:
+                continue
+            sel = ess[self.dof_field[ess] == fi]
+            for s in spaces:
+                vals = s.fct(self.dof_x[sel], self.dof_y[sel])
+                comp = self.dof_comp[sel]
+                out = np.empty(len(sel))
+                for c in range(len(vals)):
+                    m = comp == c
+                    out[m] = np.broadcast_to(vals[c], sel.shape)[m]
+                self.u[sel] = out
+                break
+        self.push()
+
+    def push(self):
+        self.system.setSolution(self.u, self.udot)
+
+    def pull(self):
+        self.u = self.system.getSolution()
+        return self.u
+
+
+@dataclass
+class feNLSolverOptions:
+    tolResidual: float = 1e-10
+    tolCorrection: float = 1e-10
+    tolDivergence: float = 1e4
+    maxIter: int = 20
+    recomputeJacobianEveryNsteps: int = 3
+    residualDecrease: float = 1e-1
+    relResidual: float = 0.0
+    linearRtolMin: float = 0.0
+
+
+def solveNewtonRaphson(system: feLinearSystemCUDA, sol: feSolution | None,
+                       tol: feNLSolverOptions, stationary: bool = True):
+    """solveNewtonRaphson (src/feNonLinearSolver.cpp:38-181) on device data."""
+    if sol is not None:
+        sol.push()
+    o = _lib.NewtonOptions(tol.tolResidual, tol.tolCorrection, tol.tolDivergence, int(tol.maxIter),
+                           tol.recomputeJacobianEveryNsteps, tol.residualDecrease, int(stationary),
+                           tol.relResidual, tol.linearRtolMin)
+    st = _lib.NewtonStats()
+    s = system.lib.fe_cuda_newton(system._h, C.byref(o), C.byref(st))
+    out = {k: getattr(st, k) for k, _ in _lib.NewtonStats._fields_}
+    out["return"] = s
+    if sol is not None:
+        sol.pull()
+    if s not in (0, -5):
+        check(s)
+    return out

@@ -1,0 +1,487 @@
+// Element assembly kernels: residual (FP64) and Jacobian (FP64 or FP32) of
+// the fused weak forms, scattered into CSR through the element-to-nonzero
+// map, one launch per element color (no two elements of a color share a DOF,
+// so the read-modify-write of values/rhs needs no atomics).
+//
+// Mapping: a block holds 32 elements (lane = element) x 6 warps (warp = P2
+// function a of the element).  Thread (e, a) produces the element-matrix rows
+// of the DOFs attached to function a -- one row for a scalar field, the two
+// component rows (a,x) (a,y) for the Taylor-Hood velocity -- plus, for a < 3,
+// the pressure row of P1 function a.  All lanes of a warp read the same
+// reference tensor entries (shared-memory broadcast) and their own element's
+// data (shared-memory columns), so the contraction has no divergence.
+//
+// Arithmetic: for affine (P1) geometry the physical gradients are
+// grad phi = G^T dphi/dr with G[r][k] = d r_r / d x_k constant per element,
+// so every quadrature sum of the reference weak forms factors into constant
+// reference tensors contracted with G, |J| and the element DOF values:
+//   int dphi_a/dx_k dphi_b/dx_l     = |J| sum_rs G[r][k] G[s][l] K[r][s][a][b]
+//   int phi_a phi_c dphi_b/dx_k     = |J| sum_r  G[r][k] T[r][a][c][b]
+//   int psi_j dphi_a/dx_k           = |J| sum_r  G[r][k] D[r][j][a]
+//   int phi_a phi_b                 = |J| M[a][b]
+// The tensors are sums over the same quadrature nodes and weights the
+// reference loops over (feSysElm.cpp:530-583, feVectorSysElm.cpp:112-130,
+// 390-427, 685-747, 1171-1240, 1454-1530), so the results are the same sums
+// regrouped: they agree to rounding.
+#include <cuda_runtime.h>
+
+#include "fe_device.h"
+
+namespace feng {
+
+namespace {
+
+constexpr int EPB = 32;  // elements per block (one per lane)
+constexpr double PI = 3.14159265358979323846;
+
+__device__ __forceinline__ void source_value(int kind, const double *p, double x, double y,
+                                             double f[2])
+{
+  switch(kind) {
+    case SRC_SIN_SIN:
+      f[0] = p[0] * sin(PI * x) * sin(PI * y);
+      f[1] = 0.;
+      break;
+    case SRC_NS_MMS_POLY: {
+      // f = -( -u.grad u - grad p + lap u ) for u=(x^4 y^4, -4/5 x^3 y^5), p = x^2 y^2
+      const double mdpdx0 = -2. * x * y * y, mdpdx1 = -2. * x * x * y;
+      const double lap0 = 12. * (x * x * y * y * y * y + x * x * x * x * y * y);
+      const double lap1 = -4. / 5. * (6. * x * y * y * y * y * y + 20. * x * x * x * y * y * y);
+      const double u0 = x * x * x * x * y * y * y * y, u1 = -4. / 5. * x * x * x * y * y * y * y * y;
+      const double g00 = 4. * x * x * x * y * y * y * y, g01 = -12. * x * x * y * y * y * y * y / 5.;
+      const double g10 = 4. * x * x * x * x * y * y * y, g11 = -4. * x * x * x * y * y * y * y;
+      const double c0 = u0 * g00 + u1 * g10, c1 = u0 * g01 + u1 * g11;
+      f[0] = -(-c0 + mdpdx0 + lap0);
+      f[1] = -(-c1 + mdpdx1 + lap1);
+      break;
+    }
+    case SRC_CONST_VEC:
+      f[0] = p[0];
+      f[1] = p[1];
+      break;
+    case SRC_SIN_BODY:
+      f[0] = p[0] * sin(PI * x) * sin(PI * y);
+      f[1] = 0.;
+      break;
+    default:
+      f[0] = f[1] = 0.;
+  }
+}
+
+template <typename V>
+struct SharedTensors {
+  V K[2][2][6][6];
+  V T[2][6][6][6];
+  V D[2][3][6];
+  V M[6][6];
+};
+
+template <typename V>
+__device__ void load_tensors(SharedTensors<V> &s, const RefTensors *g)
+{
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+  const double *K = &g->K[0][0][0][0], *T = &g->T[0][0][0][0], *D = &g->D[0][0][0], *M = &g->M[0][0];
+  V *sK = &s.K[0][0][0][0], *sT = &s.T[0][0][0][0], *sD = &s.D[0][0][0], *sM = &s.M[0][0];
+  for(int i = tid; i < 144; i += nt) sK[i] = (V)K[i];
+  for(int i = tid; i < 432; i += nt) sT[i] = (V)T[i];
+  for(int i = tid; i < 36; i += nt) sD[i] = (V)D[i];
+  for(int i = tid; i < 36; i += nt) sM[i] = (V)M[i];
+}
+
+// ---------------------------------------------------------------------------
+// Residual, scalar P2 (DIFFUSION + SOURCE).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(EPB * 6) k_residual_p2(DeviceMesh dm, FormCoeffs fc,
+                                                        const RefTensors *__restrict__ gT,
+                                                        const double *__restrict__ u, double t,
+                                                        int64_t nInc, double *__restrict__ rhs,
+                                                        int64_t begin, int64_t end)
+{
+  __shared__ SharedTensors<double> sT;
+  __shared__ double sU[6][EPB];
+  __shared__ double sG[5][EPB];
+  __shared__ double sF[16][EPB];
+  __shared__ int32_t sA[6][EPB];
+  const int lane = threadIdx.x, a = threadIdx.y;
+  const int64_t p = begin + (int64_t)blockIdx.x * EPB + lane;
+  const bool live = p < end;
+  const int64_t nE = dm.nElm;
+  load_tensors(sT, gT);
+  if(live) {
+    int32_t d = dm.adr[(int64_t)a * nE + p];
+    sA[a][lane] = d;
+    sU[a][lane] = u[d];
+    if(a < 5) sG[a][lane] = dm.geo[(int64_t)a * nE + p];
+  }
+  const int nq = gT->nq;
+  if(fc.srcKind != SRC_NONE && live) {
+    const double x0 = dm.xy[0 * nE + p], y0 = dm.xy[1 * nE + p], x1 = dm.xy[2 * nE + p],
+                 y1 = dm.xy[3 * nE + p], x2 = dm.xy[4 * nE + p], y2 = dm.xy[5 * nE + p];
+    for(int q = a; q < nq; q += 6) {
+      const double r = gT->qr[q], s = gT->qs[q];
+      const double x = x0 * (1. - r - s) + x1 * r + x2 * s;
+      const double y = y0 * (1. - r - s) + y1 * r + y2 * s;
+      double f[2];
+      source_value(fc.srcKind, fc.srcParam, x, y, f);
+      sF[q][lane] = f[0];
+    }
+  }
+  __syncthreads();
+  if(!live) return;
+  const double G[2][2] = {{sG[0][lane], sG[1][lane]}, {sG[2][lane], sG[3][lane]}};
+  const double J = sG[4][lane];
+  double be = 0.;
+  if(fc.hasDiff) {
+    // Be_a -= k grad phi_a . grad u  (feSysElm.cpp:560-583)
+    double GG[2][2];
+    for(int r = 0; r < 2; ++r)
+      for(int s2 = 0; s2 < 2; ++s2) GG[r][s2] = G[r][0] * G[s2][0] + G[r][1] * G[s2][1];
+    double acc = 0.;
+    for(int b = 0; b < 6; ++b) {
+      double L = 0.;
+      for(int r = 0; r < 2; ++r)
+        for(int s2 = 0; s2 < 2; ++s2) L += GG[r][s2] * sT.K[r][s2][a][b];
+      acc += L * sU[b][lane];
+    }
+    be -= fc.diff * acc * J;
+  }
+  if(fc.srcKind != SRC_NONE) {
+    // Be_a -= phi_a S jac w  (feSysElm.cpp:16-27)
+    double acc = 0.;
+    for(int q = 0; q < nq; ++q) acc += gT->phi[q][a] * sF[q][lane] * gT->qw[q];
+    be -= fc.srcCoeff * acc * J;
+  }
+  const int32_t d = sA[a][lane];
+  if(d < nInc) rhs[d] += be;
+}
+
+// ---------------------------------------------------------------------------
+// Jacobian, scalar P2 (DIFFUSION).
+// ---------------------------------------------------------------------------
+template <typename V>
+__global__ void __launch_bounds__(EPB * 6) k_matrix_p2(DeviceMesh dm, FormCoeffs fc,
+                                                      const RefTensors *__restrict__ gT,
+                                                      V *__restrict__ values, int64_t begin,
+                                                      int64_t end)
+{
+  __shared__ SharedTensors<V> sT;
+  __shared__ V sG[5][EPB];
+  const int lane = threadIdx.x, a = threadIdx.y;
+  const int64_t p = begin + (int64_t)blockIdx.x * EPB + lane;
+  const bool live = p < end;
+  const int64_t nE = dm.nElm;
+  load_tensors(sT, gT);
+  if(live && a < 5) sG[a][lane] = (V)dm.geo[(int64_t)a * nE + p];
+  __syncthreads();
+  if(!live || !fc.hasDiff) return;
+  const V G[2][2] = {{sG[0][lane], sG[1][lane]}, {sG[2][lane], sG[3][lane]}};
+  const V cJ = (V)fc.diff * sG[4][lane];
+  V GG[2][2];
+  for(int r = 0; r < 2; ++r)
+    for(int s2 = 0; s2 < 2; ++s2) GG[r][s2] = G[r][0] * G[s2][0] + G[r][1] * G[s2][1];
+  for(int b = 0; b < 6; ++b) {
+    V L = 0;
+    for(int r = 0; r < 2; ++r)
+      for(int s2 = 0; s2 < 2; ++s2) L += GG[r][s2] * sT.K[r][s2][a][b];
+    const int32_t pos = dm.map[(int64_t)(a * 6 + b) * nE + p];
+    if(pos >= 0) values[pos] += cJ * L;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Residual, Taylor-Hood P2-P1 (VECTOR_CONVECTIVE_ACCELERATION,
+// DIV_NEWTONIAN_STRESS, MIXED_DIVERGENCE, TRANSIENT_VECTOR_MASS,
+// VECTOR_SOURCE).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(EPB * 6) k_residual_th(DeviceMesh dm, FormCoeffs fc,
+                                                        const RefTensors *__restrict__ gT,
+                                                        const double *__restrict__ u,
+                                                        const double *__restrict__ udot, double t,
+                                                        int64_t nInc, double *__restrict__ rhs,
+                                                        int64_t begin, int64_t end)
+{
+  __shared__ SharedTensors<double> sT;
+  __shared__ double sU[12][EPB];
+  __shared__ double sUd[12][EPB];
+  __shared__ double sP[3][EPB];
+  __shared__ double sG[5][EPB];
+  __shared__ double sF[2][16][EPB];
+  __shared__ int32_t sA[15][EPB];
+  const int lane = threadIdx.x, a = threadIdx.y;
+  const int64_t p = begin + (int64_t)blockIdx.x * EPB + lane;
+  const bool live = p < end;
+  const int64_t nE = dm.nElm;
+  load_tensors(sT, gT);
+  const bool hasSrc = fc.srcKind != SRC_NONE;
+  if(live) {
+    for(int i = a; i < 15; i += 6) {
+      int32_t d = dm.adr[(int64_t)i * nE + p];
+      sA[i][lane] = d;
+      if(i < 12) {
+        sU[i][lane] = u[d];
+        if(fc.hasMass) sUd[i][lane] = udot[d];
+      } else {
+        sP[i - 12][lane] = u[d];
+      }
+    }
+    if(a < 5) sG[a][lane] = dm.geo[(int64_t)a * nE + p];
+  }
+  const int nq = gT->nq;
+  if(hasSrc && live) {
+    const double x0 = dm.xy[0 * nE + p], y0 = dm.xy[1 * nE + p], x1 = dm.xy[2 * nE + p],
+                 y1 = dm.xy[3 * nE + p], x2 = dm.xy[4 * nE + p], y2 = dm.xy[5 * nE + p];
+    for(int q = a; q < nq; q += 6) {
+      const double r = gT->qr[q], s = gT->qs[q];
+      const double x = x0 * (1. - r - s) + x1 * r + x2 * s;
+      const double y = y0 * (1. - r - s) + y1 * r + y2 * s;
+      double f[2];
+      source_value(fc.srcKind, fc.srcParam, x, y, f);
+      sF[0][q][lane] = f[0];
+      sF[1][q][lane] = f[1];
+    }
+  }
+  __syncthreads();
+  if(!live) return;
+  const double G[2][2] = {{sG[0][lane], sG[1][lane]}, {sG[2][lane], sG[3][lane]}};
+  const double J = sG[4][lane];
+  double be[2] = {0., 0.};
+
+  if(fc.hasConv) {
+    // Be_(a,m) -= c (u . grad u)_m phi_a jac w   (feVectorSysElm.cpp:1206-1240)
+    double V0[2][6];
+    for(int c = 0; c < 6; ++c)
+      for(int r = 0; r < 2; ++r) V0[r][c] = sU[2 * c][lane] * G[r][0] + sU[2 * c + 1][lane] * G[r][1];
+    double R[2] = {0., 0.};
+    for(int b = 0; b < 6; ++b) {
+      double W = 0.;
+      for(int c = 0; c < 6; ++c) W += V0[0][c] * sT.T[0][a][c][b] + V0[1][c] * sT.T[1][a][c][b];
+      R[0] += W * sU[2 * b][lane];
+      R[1] += W * sU[2 * b + 1][lane];
+    }
+    be[0] -= fc.conv * R[0] * J;
+    be[1] -= fc.conv * R[1] * J;
+  }
+  if(fc.hasSigma) {
+    // Be_(a,m) -= c (p div phi - mu (grad u + grad u^T) : grad phi) jac w
+    // (feVectorSysElm.cpp:1494-1530)
+    double GG[2][2][2][2];  // [k][l][r][s] = G[r][k] G[s][l]
+    for(int k = 0; k < 2; ++k)
+      for(int l = 0; l < 2; ++l)
+        for(int r = 0; r < 2; ++r)
+          for(int s2 = 0; s2 < 2; ++s2) GG[k][l][r][s2] = G[r][k] * G[s2][l];
+    double visc[2] = {0., 0.};
+    for(int b = 0; b < 6; ++b) {
+      double S[2][2];
+      for(int k = 0; k < 2; ++k)
+        for(int l = 0; l < 2; ++l) {
+          double v = 0.;
+          for(int r = 0; r < 2; ++r)
+            for(int s2 = 0; s2 < 2; ++s2) v += GG[k][l][r][s2] * sT.K[r][s2][a][b];
+          S[k][l] = v;
+        }
+      const double tr = S[0][0] + S[1][1];
+      const double ub0 = sU[2 * b][lane], ub1 = sU[2 * b + 1][lane];
+      // m-th component: U_bm (S_xx+S_yy) + sum_k U_bk S_km
+      visc[0] += ub0 * tr + ub0 * S[0][0] + ub1 * S[1][0];
+      visc[1] += ub1 * tr + ub0 * S[0][1] + ub1 * S[1][1];
+    }
+    double pdiv[2] = {0., 0.};
+    for(int j = 0; j < 3; ++j) {
+      const double pj = sP[j][lane];
+      for(int m = 0; m < 2; ++m) pdiv[m] += pj * (G[0][m] * sT.D[0][j][a] + G[1][m] * sT.D[1][j][a]);
+    }
+    for(int m = 0; m < 2; ++m) be[m] -= fc.sigma * (pdiv[m] - fc.mu * visc[m]) * J;
+  }
+  if(fc.hasMass) {
+    // Be_(a,m) -= c udot . phi jac w   (feVectorSysElm.cpp:410-427)
+    double acc[2] = {0., 0.};
+    for(int b = 0; b < 6; ++b) {
+      acc[0] += sT.M[a][b] * sUd[2 * b][lane];
+      acc[1] += sT.M[a][b] * sUd[2 * b + 1][lane];
+    }
+    be[0] -= fc.mass * acc[0] * J;
+    be[1] -= fc.mass * acc[1] * J;
+  }
+  if(hasSrc) {
+    // Be_(a,m) -= f . phi jac w   (feVectorSysElm.cpp:112-130)
+    double acc[2] = {0., 0.};
+    for(int q = 0; q < nq; ++q) {
+      const double pw = gT->phi[q][a] * gT->qw[q];
+      acc[0] += sF[0][q][lane] * pw;
+      acc[1] += sF[1][q][lane] * pw;
+    }
+    be[0] -= fc.srcCoeff * acc[0] * J;
+    be[1] -= fc.srcCoeff * acc[1] * J;
+  }
+  for(int m = 0; m < 2; ++m) {
+    const int32_t d = sA[2 * a + m][lane];
+    if(d < nInc) rhs[d] += be[m];
+  }
+  if(fc.hasDivu && a < 3) {
+    // Be_pj -= c div u psi_j jac w   (feVectorSysElm.cpp:722-747), j = a
+    double acc = 0.;
+    for(int b = 0; b < 6; ++b)
+      for(int n = 0; n < 2; ++n)
+        acc += sU[2 * b + n][lane] * (G[0][n] * sT.D[0][a][b] + G[1][n] * sT.D[1][a][b]);
+    const int32_t d = sA[12 + a][lane];
+    if(d < nInc) rhs[d] -= fc.divu * acc * J;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Jacobian, Taylor-Hood P2-P1.
+// ---------------------------------------------------------------------------
+template <typename V>
+__global__ void __launch_bounds__(EPB * 6) k_matrix_th(DeviceMesh dm, FormCoeffs fc,
+                                                      const RefTensors *__restrict__ gT,
+                                                      const double *__restrict__ u, double c0,
+                                                      V *__restrict__ values, int64_t begin,
+                                                      int64_t end)
+{
+  __shared__ SharedTensors<V> sT;
+  __shared__ V sU[12][EPB];
+  __shared__ V sG[5][EPB];
+  const int lane = threadIdx.x, a = threadIdx.y;
+  const int64_t p = begin + (int64_t)blockIdx.x * EPB + lane;
+  const bool live = p < end;
+  const int64_t nE = dm.nElm;
+  load_tensors(sT, gT);
+  if(live) {
+    if(fc.hasConv)
+      for(int i = a; i < 12; i += 6) sU[i][lane] = (V)u[dm.adr[(int64_t)i * nE + p]];
+    if(a < 5) sG[a][lane] = (V)dm.geo[(int64_t)a * nE + p];
+  }
+  __syncthreads();
+  if(!live) return;
+  const V G[2][2] = {{sG[0][lane], sG[1][lane]}, {sG[2][lane], sG[3][lane]}};
+  const V J = sG[4][lane];
+
+  // Element rows (a,0) and (a,1): 12 velocity columns + 3 pressure columns.
+  V A[2][12];
+#pragma unroll
+  for(int m = 0; m < 2; ++m)
+#pragma unroll
+    for(int j = 0; j < 12; ++j) A[m][j] = 0;
+
+  if(fc.hasConv) {
+    // A_(a,m),(b,n) += c [ delta_mn phi_a (u0 . grad phi_b) + phi_a phi_b d_n u0_m ]
+    // (vectorDotGradShapeDotShape + shapeDotTensorDotShape, feVectorSpace.cpp:202-290)
+    V V0[2][6];
+    for(int c = 0; c < 6; ++c)
+      for(int r = 0; r < 2; ++r) V0[r][c] = sU[2 * c][lane] * G[r][0] + sU[2 * c + 1][lane] * G[r][1];
+    const V cc = (V)fc.conv * J;
+    for(int b = 0; b < 6; ++b) {
+      V W = 0, Z[2][2] = {{0, 0}, {0, 0}};  // Z[r][m] = sum_c U_cm T[r][a][b][c]
+      for(int c = 0; c < 6; ++c) {
+        W += V0[0][c] * sT.T[0][a][c][b] + V0[1][c] * sT.T[1][a][c][b];
+        const V t0 = sT.T[0][a][b][c], t1 = sT.T[1][a][b][c];
+        const V uc0 = sU[2 * c][lane], uc1 = sU[2 * c + 1][lane];
+        Z[0][0] += uc0 * t0; Z[0][1] += uc1 * t0;
+        Z[1][0] += uc0 * t1; Z[1][1] += uc1 * t1;
+      }
+      for(int m = 0; m < 2; ++m)
+        for(int n = 0; n < 2; ++n) {
+          V v = G[0][n] * Z[0][m] + G[1][n] * Z[1][m];
+          if(m == n) v += W;
+          A[m][2 * b + n] += cc * v;
+        }
+    }
+  }
+  if(fc.hasSigma) {
+    // A_(a,m),(b,n) += -c mu [ delta_mn grad phi_a . grad phi_b + d_n phi_a d_m phi_b ]
+    // (feVectorSysElm.cpp:1454-1492)
+    const V cs = -(V)fc.sigma * (V)fc.mu * J;
+    V GG[2][2][2][2];
+    for(int k = 0; k < 2; ++k)
+      for(int l = 0; l < 2; ++l)
+        for(int r = 0; r < 2; ++r)
+          for(int s2 = 0; s2 < 2; ++s2) GG[k][l][r][s2] = G[r][k] * G[s2][l];
+    for(int b = 0; b < 6; ++b) {
+      V S[2][2];
+      for(int k = 0; k < 2; ++k)
+        for(int l = 0; l < 2; ++l) {
+          V v = 0;
+          for(int r = 0; r < 2; ++r)
+            for(int s2 = 0; s2 < 2; ++s2) v += GG[k][l][r][s2] * sT.K[r][s2][a][b];
+          S[k][l] = v;
+        }
+      const V tr = S[0][0] + S[1][1];
+      for(int m = 0; m < 2; ++m)
+        for(int n = 0; n < 2; ++n) A[m][2 * b + n] += cs * ((m == n ? tr : (V)0) + S[n][m]);
+    }
+  }
+  if(fc.hasMass) {
+    // A_(a,m),(b,n) += c c0 delta_mn phi_a phi_b   (feVectorSysElm.cpp:390-408)
+    const V cm = (V)fc.mass * (V)c0 * J;
+    for(int b = 0; b < 6; ++b) {
+      A[0][2 * b] += cm * sT.M[a][b];
+      A[1][2 * b + 1] += cm * sT.M[a][b];
+    }
+  }
+  // Pressure columns of rows (a,m) and the column (a,m) of the pressure rows:
+  // both are int psi_j d_m phi_a.
+  V Bp[2][3];
+  for(int m = 0; m < 2; ++m)
+    for(int j = 0; j < 3; ++j) Bp[m][j] = (G[0][m] * sT.D[0][j][a] + G[1][m] * sT.D[1][j][a]) * J;
+
+  for(int m = 0; m < 2; ++m) {
+    const int i = 2 * a + m;
+    for(int j = 0; j < 12; ++j) {
+      const int32_t pos = dm.map[(int64_t)(i * 15 + j) * nE + p];
+      if(pos >= 0) values[pos] += A[m][j];
+    }
+    if(fc.hasSigma)
+      for(int j = 0; j < 3; ++j) {
+        const int32_t pos = dm.map[(int64_t)(i * 15 + 12 + j) * nE + p];
+        if(pos >= 0) values[pos] += (V)fc.sigma * Bp[m][j];
+      }
+    if(fc.hasDivu)
+      for(int j = 0; j < 3; ++j) {
+        const int32_t pos = dm.map[(int64_t)((12 + j) * 15 + i) * nE + p];
+        if(pos >= 0) values[pos] += (V)fc.divu * Bp[m][j];
+      }
+  }
+}
+
+int64_t nblocks(int64_t begin, int64_t end) { return (end - begin + EPB - 1) / EPB; }
+
+}  // namespace
+
+void launch_assemble_residual(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
+                              const double *u, const double *udot, double t, int64_t nInc,
+                              double *rhs, int64_t begin, int64_t end, cudaStream_t s)
+{
+  if(end <= begin) return;
+  dim3 block(EPB, 6);
+  if(fc.elemType == 1)
+    k_residual_p2<<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, u, t, nInc, rhs, begin, end);
+  else
+    k_residual_th<<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, u, udot, t, nInc, rhs, begin,
+                                                        end);
+}
+
+void launch_assemble_matrix_f64(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
+                                const double *u, double c0, double *values, int64_t begin,
+                                int64_t end, cudaStream_t s)
+{
+  if(end <= begin) return;
+  dim3 block(EPB, 6);
+  if(fc.elemType == 1)
+    k_matrix_p2<double><<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, values, begin, end);
+  else
+    k_matrix_th<double><<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, u, c0, values, begin, end);
+}
+
+void launch_assemble_matrix_f32(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
+                                const double *u, double c0, float *values, int64_t begin,
+                                int64_t end, cudaStream_t s)
+{
+  if(end <= begin) return;
+  dim3 block(EPB, 6);
+  if(fc.elemType == 1)
+    k_matrix_p2<float><<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, values, begin, end);
+  else
+    k_matrix_th<float><<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, u, c0, values, begin, end);
+}
+
+}  // namespace feng

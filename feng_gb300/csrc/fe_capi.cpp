@@ -1,0 +1,599 @@
+// extern "C" entry points declared in include/feng_cuda.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+
+#include "../../include/feng_cuda.h"
+#include "fe_common.h"
+#include "fe_mesh.h"
+#include "fe_setup.h"
+#include "fe_system.h"
+
+namespace feng {
+namespace {
+thread_local std::string g_err;
+}
+void set_error(const char *fmt, ...)
+{
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+}
+const char *last_error() { return g_err.c_str(); }
+}  // namespace feng
+
+using namespace feng;
+
+struct fe_mesh {
+  Mesh2D m;
+};
+
+struct fe_cuda_system {
+  SystemCUDA sys;
+};
+
+struct fe_setup {
+  Numbering num;
+  ElementTables et;
+  Coloring col;
+  CSRPattern pat;
+  std::vector<int32_t> blockOfRow;
+  std::vector<double> elemXY;
+  QuadRule quad;
+};
+
+#define GUARD_BEGIN try {
+#define GUARD_END                                  \
+  }                                                \
+  catch(const std::bad_alloc &) {                  \
+    set_error("host allocation failed");           \
+    return FE_CUDA_ERROR;                          \
+  }                                                \
+  catch(...) {                                     \
+    set_error("unexpected exception");             \
+    return FE_CUDA_ERROR;                          \
+  }
+
+static int check_options(const fe_cuda_options *o)
+{
+  if(!o) {
+    set_error("null options");
+    return FE_INVALID_ARG;
+  }
+  if(o->krylov < 0 || o->krylov > 1 || o->precond < 0 || o->precond > 2 || o->precision < 0 ||
+     o->precision > 1 || o->restart < 1 || o->restart > 128 || o->max_iter < 1 ||
+     !(o->rel_tol >= 0) || !(o->abs_tol >= 0) || o->pc_block_rows < 0) {
+    set_error("invalid linear solver options");
+    return FE_INVALID_ARG;
+  }
+  return FE_OK;
+}
+
+static SystemOptions to_sys_options(const fe_cuda_options *o)
+{
+  SystemOptions so;
+  so.kry.method = o->krylov;
+  so.kry.restart = o->restart;
+  so.kry.maxIter = o->max_iter;
+  so.kry.rtol = o->rel_tol;
+  so.kry.atol = o->abs_tol;
+  so.kry.dtol = o->div_tol > 0 ? o->div_tol : 1e6;
+  so.kry.precond = o->precond;
+  so.pcBlockRows = o->pc_block_rows;
+  so.precision = o->precision;
+  return so;
+}
+
+static void to_forms(const fe_form_desc *forms, int n, std::vector<FormDesc> &out)
+{
+  out.resize(n);
+  for(int i = 0; i < n; ++i) {
+    out[i].kind = forms[i].kind;
+    out[i].coeff = forms[i].coeff;
+    out[i].coeff2 = forms[i].coeff2;
+    out[i].source = forms[i].source;
+    for(int k = 0; k < 4; ++k) out[i].params[k] = forms[i].params[k];
+  }
+}
+
+extern "C" {
+
+const char *fe_cuda_last_error(void) { return last_error(); }
+int fe_cuda_version(void) { return 1; }
+
+int fe_cuda_device_count(int *count)
+{
+  int c = 0;
+  cudaError_t e = cudaGetDeviceCount(&c);
+  if(count) *count = (e == cudaSuccess) ? c : 0;
+  if(e != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cudaGetDeviceCount: %s", cudaGetErrorString(e));
+    return FE_CUDA_DEVICE_FAIL;
+  }
+  return FE_OK;
+}
+
+int fe_mesh_generate_square(int n, double x0, double x1, double y0, double y1, double jitter,
+                            uint64_t seed, fe_mesh **out)
+{
+  GUARD_BEGIN
+  if(!out) { set_error("null output"); return FE_INVALID_ARG; }
+  auto *m = new fe_mesh();
+  int s = mesh_generate_square(m->m, n, x0, x1, y0, y1, jitter, seed);
+  if(s) { delete m; return s; }
+  *out = m;
+  return FE_OK;
+  GUARD_END
+}
+
+int fe_mesh_read_msh(const char *path, fe_mesh **out)
+{
+  GUARD_BEGIN
+  if(!out || !path) { set_error("null argument"); return FE_INVALID_ARG; }
+  auto *m = new fe_mesh();
+  int s = mesh_read_msh41(m->m, path);
+  if(s) { delete m; return s; }
+  *out = m;
+  return FE_OK;
+  GUARD_END
+}
+
+int fe_mesh_write_msh(const fe_mesh *m, const char *path)
+{
+  GUARD_BEGIN
+  if(!m || !path) { set_error("null argument"); return FE_INVALID_ARG; }
+  return mesh_write_msh41(m->m, path);
+  GUARD_END
+}
+
+int fe_mesh_sizes(const fe_mesh *m, int64_t *nv, int64_t *nt, int64_t *ne, int64_t *nb)
+{
+  if(!m) { set_error("null mesh"); return FE_INVALID_ARG; }
+  if(nv) *nv = m->m.n_vertices();
+  if(nt) *nt = m->m.n_triangles();
+  if(ne) *ne = m->m.n_edges;
+  if(nb) *nb = m->m.n_boundary();
+  return FE_OK;
+}
+
+int fe_mesh_arrays(const fe_mesh *m, double *x, double *y, int32_t *tri, int32_t *tri_edges,
+                   int32_t *bnd, int32_t *point)
+{
+  if(!m) { set_error("null mesh"); return FE_INVALID_ARG; }
+  const Mesh2D &M = m->m;
+  if(x) std::copy(M.x.begin(), M.x.end(), x);
+  if(y) std::copy(M.y.begin(), M.y.end(), y);
+  if(tri) std::copy(M.tri.begin(), M.tri.end(), tri);
+  if(tri_edges) std::copy(M.tri_edges.begin(), M.tri_edges.end(), tri_edges);
+  if(bnd) std::copy(M.bnd.begin(), M.bnd.end(), bnd);
+  if(point) *point = M.point;
+  return FE_OK;
+}
+
+void fe_mesh_destroy(fe_mesh *m) { delete m; }
+
+static int to_spaces(const fe_space_desc *spaces, int n, std::vector<SpaceDesc> &out)
+{
+  if(!spaces || n <= 0) { set_error("no spaces"); return FE_INVALID_ARG; }
+  out.resize(n);
+  for(int i = 0; i < n; ++i) {
+    out[i] = {spaces[i].field, spaces[i].degree, spaces[i].ncomp, spaces[i].cnc, spaces[i].essential};
+    if(out[i].field < 0 || out[i].field > 7 || out[i].cnc < 0 || out[i].cnc > 2) {
+      set_error("invalid space %d", i);
+      return FE_INVALID_ARG;
+    }
+  }
+  return FE_OK;
+}
+
+int fe_setup_create(const fe_mesh *m, const fe_space_desc *spaces, int nspaces, int elem_type,
+                    int quad_degree, int pc_block_rows, fe_setup **out)
+{
+  GUARD_BEGIN
+  if(!m || !out) { set_error("null argument"); return FE_INVALID_ARG; }
+  if(pc_block_rows < 0) { set_error("negative block size"); return FE_INVALID_ARG; }
+  std::vector<SpaceDesc> sp;
+  FE_TRY(to_spaces(spaces, nspaces, sp));
+  std::unique_ptr<fe_setup> S(new fe_setup());
+  const Mesh2D &M = m->m;
+  FE_TRY(build_numbering(M, sp, S->num));
+  // The element's fields: the P2 space on the domain, and for Taylor-Hood the
+  // P1 space on the domain.
+  int fieldU = -1, fieldP = -1;
+  for(const SpaceDesc &d : sp) {
+    if(d.cnc != CNC_DOMAIN) continue;
+    if(d.degree == 2 && fieldU < 0) fieldU = d.field;
+    if(d.degree == 1 && fieldP < 0) fieldP = d.field;
+  }
+  FE_TRY(build_element_tables(M, S->num, elem_type, fieldU,
+                              elem_type == ELEM_TAYLOR_HOOD ? fieldP : -1, S->et));
+  FE_TRY(color_elements(M, S->col));
+  FE_TRY(build_csr_pattern(S->et, S->num.nInc, S->pat));
+  FE_TRY(triangle_rule(quad_degree, S->quad));
+  // Block-Jacobi partition: unknowns grouped by the smallest mesh vertex
+  // they touch, in contiguous vertex ranges, so a block holds the velocity
+  // and pressure unknowns of one patch (velocity rows first, as numbered).
+  const int64_t nInc = S->num.nInc;
+  const int64_t nb = pc_block_rows > 0 ? std::max<int64_t>(1, nInc / pc_block_rows) : 1;
+  const int64_t nv = M.n_vertices();
+  std::vector<int64_t> key(S->num.nDofs, 0);
+  for(int f = 0; f < S->num.nFields; ++f) {
+    const int C = S->num.fieldComp[f];
+    for(int64_t v = 0; v < nv; ++v)
+      for(int c = 0; c < C; ++c) {
+        int64_t d = S->num.vdof[f][v * C + c];
+        if(d >= 0) key[d] = v;
+      }
+    for(int64_t e = 0; e < M.n_edges; ++e)
+      for(int c = 0; c < C; ++c) {
+        int64_t d = S->num.edof[f][e * C + c];
+        if(d >= 0) key[d] = std::min(M.edge_v[2 * e], M.edge_v[2 * e + 1]);
+      }
+  }
+  S->blockOfRow.resize(nInc);
+  for(int64_t i = 0; i < nInc; ++i) S->blockOfRow[i] = (int32_t)((key[i] * nb) / nv);
+  S->elemXY.resize(M.n_triangles() * 6);
+  for(int64_t t = 0; t < M.n_triangles(); ++t)
+    for(int k = 0; k < 3; ++k) {
+      S->elemXY[6 * t + 2 * k] = M.x[M.tri[3 * t + k]];
+      S->elemXY[6 * t + 2 * k + 1] = M.y[M.tri[3 * t + k]];
+    }
+  *out = S.release();
+  return FE_OK;
+  GUARD_END
+}
+
+void fe_setup_destroy(fe_setup *s) { delete s; }
+
+int fe_setup_sizes(const fe_setup *s, int64_t *n_inc, int64_t *n_dofs, int64_t *nnz,
+                   int64_t *n_elm, int *n_colors, int *nloc)
+{
+  if(!s) { set_error("null setup"); return FE_INVALID_ARG; }
+  if(n_inc) *n_inc = s->num.nInc;
+  if(n_dofs) *n_dofs = s->num.nDofs;
+  if(nnz) *nnz = s->pat.nnz();
+  if(n_elm) *n_elm = s->et.nElm;
+  if(n_colors) *n_colors = s->col.nColors;
+  if(nloc) *nloc = s->et.nloc;
+  return FE_OK;
+}
+
+int fe_setup_get_pattern(const fe_setup *s, int64_t *ia, int32_t *ja)
+{
+  if(!s) { set_error("null setup"); return FE_INVALID_ARG; }
+  if(ia) std::copy(s->pat.ia.begin(), s->pat.ia.end(), ia);
+  if(ja) std::copy(s->pat.ja.begin(), s->pat.ja.end(), ja);
+  return FE_OK;
+}
+
+int fe_setup_get_coloring(const fe_setup *s, int64_t *offsets, int32_t *elements)
+{
+  if(!s) { set_error("null setup"); return FE_INVALID_ARG; }
+  if(offsets) std::copy(s->col.offsets.begin(), s->col.offsets.end(), offsets);
+  if(elements) std::copy(s->col.elements.begin(), s->col.elements.end(), elements);
+  return FE_OK;
+}
+
+int fe_setup_get_element_dofs(const fe_setup *s, int64_t *adr)
+{
+  if(!s) { set_error("null setup"); return FE_INVALID_ARG; }
+  if(adr) std::copy(s->et.adr.begin(), s->et.adr.end(), adr);
+  return FE_OK;
+}
+
+int fe_setup_get_dof_info(const fe_setup *s, double *x, double *y, int32_t *field, int32_t *comp,
+                          int32_t *is_vertex)
+{
+  if(!s) { set_error("null setup"); return FE_INVALID_ARG; }
+  const Numbering &n = s->num;
+  if(x) std::copy(n.dof_x.begin(), n.dof_x.end(), x);
+  if(y) std::copy(n.dof_y.begin(), n.dof_y.end(), y);
+  if(field) std::copy(n.dof_field.begin(), n.dof_field.end(), field);
+  if(comp) std::copy(n.dof_comp.begin(), n.dof_comp.end(), comp);
+  if(is_vertex)
+    for(size_t i = 0; i < n.dof_is_vertex.size(); ++i) is_vertex[i] = n.dof_is_vertex[i];
+  return FE_OK;
+}
+
+int fe_setup_get_blocks(const fe_setup *s, int32_t *block_of_row)
+{
+  if(!s) { set_error("null setup"); return FE_INVALID_ARG; }
+  if(block_of_row) std::copy(s->blockOfRow.begin(), s->blockOfRow.end(), block_of_row);
+  return FE_OK;
+}
+
+int fe_quadrature_rule(int degree, int *n, double *r, double *s, double *w)
+{
+  GUARD_BEGIN
+  QuadRule q;
+  FE_TRY(triangle_rule(degree, q));
+  if(n) *n = q.n();
+  for(int k = 0; k < q.n(); ++k) {
+    if(r) r[k] = q.r[k];
+    if(s) s[k] = q.s[k];
+    if(w) w[k] = q.w[k];
+  }
+  return FE_OK;
+  GUARD_END
+}
+
+int fe_cuda_system_create(const fe_setup *setup, const fe_form_desc *forms, int nforms,
+                          const fe_cuda_options *opt, fe_cuda_system **out)
+{
+  GUARD_BEGIN
+  if(!setup || !out || (!forms && nforms > 0)) { set_error("null argument"); return FE_INVALID_ARG; }
+  FE_TRY(check_options(opt));
+  if(opt->quad_degree != setup->quad.degree) {
+    set_error("options ask for quadrature degree %d, the set-up was built with %d",
+              opt->quad_degree, setup->quad.degree);
+    return FE_INVALID_ARG;
+  }
+  std::unique_ptr<fe_cuda_system> S(new fe_cuda_system());
+  SystemTables T;
+  T.elemType = setup->et.type;
+  T.nElm = setup->et.nElm;
+  T.nloc = setup->et.nloc;
+  T.nInc = setup->num.nInc;
+  T.nDofs = setup->num.nDofs;
+  T.adr = setup->et.adr.data();
+  T.elemXY = setup->elemXY.data();
+  T.coloring = &setup->col;
+  T.pattern = &setup->pat;
+  // The set-up's partition targets its own block size; a different size in
+  // the options re-partitions by contiguous index ranges.
+  T.blockOfRow = &setup->blockOfRow;
+  T.quad = setup->quad;
+  std::vector<FormDesc> fd;
+  to_forms(forms, nforms, fd);
+  FE_TRY(S->sys.init(T, fd.data(), nforms, to_sys_options(opt)));
+  *out = S.release();
+  return FE_OK;
+  GUARD_END
+}
+
+int fe_cuda_system_create_from_tables(int elem_type, int64_t n_elm, const int64_t *adr,
+                                      const double *elem_xy, int64_t n_inc, int64_t n_dofs,
+                                      int n_colors, const int64_t *color_offsets,
+                                      const int32_t *color_elements, const int64_t *ia,
+                                      const int32_t *ja, const int32_t *block_of_row,
+                                      const fe_form_desc *forms, int nforms,
+                                      const fe_cuda_options *opt, fe_cuda_system **out)
+{
+  GUARD_BEGIN
+  if(!out || !adr || !elem_xy || (!forms && nforms > 0)) { set_error("null argument"); return FE_INVALID_ARG; }
+  FE_TRY(check_options(opt));
+  std::unique_ptr<fe_cuda_system> S(new fe_cuda_system());
+  const int nloc = elem_type == ELEM_P2 ? 6 : elem_type == ELEM_TAYLOR_HOOD ? 15 : 0;
+  if(!nloc) { set_error("unknown element type %d", elem_type); return FE_INVALID_ARG; }
+  SystemTables T;
+  T.elemType = elem_type;
+  T.nElm = n_elm;
+  T.nloc = nloc;
+  T.nInc = n_inc;
+  T.nDofs = n_dofs;
+  T.adr = adr;
+  T.elemXY = elem_xy;
+  Coloring col;
+  if(color_offsets && color_elements && n_colors > 0) {
+    if(n_colors > 64) { set_error("at most 64 colors"); return FE_BAD_COLORING; }
+    col.nColors = n_colors;
+    col.offsets.assign(color_offsets, color_offsets + n_colors + 1);
+    col.elements.assign(color_elements, color_elements + n_elm);
+    if(col.offsets[0] != 0 || col.offsets[n_colors] != n_elm) { set_error("color offsets do not cover the elements"); return FE_BAD_COLORING; }
+    T.coloring = &col;
+  }
+  CSRPattern pat;
+  if(ia && ja) {
+    pat.n = n_inc;
+    pat.ia.assign(ia, ia + n_inc + 1);
+    if(pat.ia[0] != 0 || pat.ia[n_inc] < n_inc) { set_error("invalid CSR row pointers"); return FE_INVALID_ARG; }
+    for(int64_t r = 0; r < n_inc; ++r)
+      if(pat.ia[r + 1] < pat.ia[r]) { set_error("CSR row pointers decrease at row %lld", (long long)r); return FE_INVALID_ARG; }
+    pat.ja.assign(ja, ja + pat.ia[n_inc]);
+    for(int64_t r = 0; r < n_inc; ++r)
+      for(int64_t k = pat.ia[r]; k < pat.ia[r + 1]; ++k)
+        if(pat.ja[k] < 0 || pat.ja[k] >= n_inc || (k > pat.ia[r] && pat.ja[k] <= pat.ja[k - 1])) {
+          set_error("CSR columns of row %lld are out of range or not strictly ascending", (long long)r);
+          return FE_INVALID_ARG;
+        }
+    T.pattern = &pat;
+  }
+  std::vector<int32_t> blocks;
+  if(block_of_row) {
+    blocks.assign(block_of_row, block_of_row + n_inc);
+    for(int32_t b : blocks)
+      if(b < 0) { set_error("negative block id"); return FE_INVALID_ARG; }
+    T.blockOfRow = &blocks;
+  }
+  FE_TRY(triangle_rule(opt->quad_degree, T.quad));
+  std::vector<FormDesc> fd;
+  to_forms(forms, nforms, fd);
+  FE_TRY(S->sys.init(T, fd.data(), nforms, to_sys_options(opt)));
+  if(T.coloring) FE_TRY(S->sys.validateColoring());
+  *out = S.release();
+  return FE_OK;
+  GUARD_END
+}
+
+void fe_cuda_system_destroy(fe_cuda_system *s) { delete s; }
+
+int fe_cuda_system_sizes(const fe_cuda_system *s, int64_t *n_inc, int64_t *n_dofs, int64_t *nnz,
+                         int64_t *n_elm, int *n_colors)
+{
+  if(!s) { set_error("null system"); return FE_INVALID_ARG; }
+  if(n_inc) *n_inc = s->sys.nInc();
+  if(n_dofs) *n_dofs = s->sys.nDofs();
+  if(nnz) *nnz = s->sys.nnz();
+  if(n_elm) *n_elm = s->sys.nElm();
+  if(n_colors) *n_colors = s->sys.nColors();
+  return FE_OK;
+}
+
+int fe_cuda_get_pattern(const fe_cuda_system *s, int64_t *ia, int32_t *ja)
+{
+  if(!s) { set_error("null system"); return FE_INVALID_ARG; }
+  const CSRPattern &p = s->sys.pattern();
+  if(ia) std::copy(p.ia.begin(), p.ia.end(), ia);
+  if(ja) std::copy(p.ja.begin(), p.ja.end(), ja);
+  return FE_OK;
+}
+
+int fe_cuda_get_coloring(const fe_cuda_system *s, int64_t *offsets, int32_t *elements)
+{
+  if(!s) { set_error("null system"); return FE_INVALID_ARG; }
+  const Coloring &c = s->sys.coloring();
+  if(offsets) std::copy(c.offsets.begin(), c.offsets.end(), offsets);
+  if(elements) std::copy(c.elements.begin(), c.elements.end(), elements);
+  return FE_OK;
+}
+
+int fe_cuda_validate_coloring(const fe_cuda_system *s)
+{
+  if(!s) { set_error("null system"); return FE_INVALID_ARG; }
+  return s->sys.validateColoring();
+}
+
+int fe_cuda_set_solution(fe_cuda_system *s, const double *u, const double *udot)
+{
+  if(!s) { set_error("null system"); return FE_INVALID_ARG; }
+  return s->sys.setSolution(u, udot);
+}
+
+int fe_cuda_get_solution(const fe_cuda_system *s, double *u)
+{
+  if(!s || !u) { set_error("null argument"); return FE_INVALID_ARG; }
+  return s->sys.getSolution(u);
+}
+
+int fe_cuda_set_time(fe_cuda_system *s, double t, double c0)
+{
+  if(!s) { set_error("null system"); return FE_INVALID_ARG; }
+  s->sys.setTime(t, c0);
+  return FE_OK;
+}
+
+int fe_cuda_set_bdf(fe_cuda_system *s, int order, const double *cn, const double *hist1,
+                    const double *hist2)
+{
+  if(!s || !cn) { set_error("null argument"); return FE_INVALID_ARG; }
+  const double *h[3] = {nullptr, hist1, hist2};
+  return s->sys.setBDF(order, cn, h);
+}
+
+int fe_cuda_compute_soldot(fe_cuda_system *s)
+{
+  if(!s) { set_error("null system"); return FE_INVALID_ARG; }
+  return s->sys.computeSolDot();
+}
+
+int fe_cuda_set_to_zero(fe_cuda_system *s) { return s ? s->sys.setToZero() : FE_INVALID_ARG; }
+int fe_cuda_set_matrix_to_zero(fe_cuda_system *s) { return s ? s->sys.setMatrixToZero() : FE_INVALID_ARG; }
+int fe_cuda_set_residual_to_zero(fe_cuda_system *s) { return s ? s->sys.setResidualToZero() : FE_INVALID_ARG; }
+int fe_cuda_assemble_residuals(fe_cuda_system *s) { return s ? s->sys.assembleResiduals() : FE_INVALID_ARG; }
+int fe_cuda_assemble_matrices(fe_cuda_system *s) { return s ? s->sys.assembleMatrices() : FE_INVALID_ARG; }
+
+int fe_cuda_get_rhs_max_norm(fe_cuda_system *s, double *norm)
+{
+  if(!s || !norm) { set_error("null argument"); return FE_INVALID_ARG; }
+  return s->sys.getRHSMaxNorm(norm);
+}
+
+int fe_cuda_solve(fe_cuda_system *s, double *norm_dx, double *norm_rhs, double *norm_axb, int *n_iter)
+{
+  if(!s) { set_error("null system"); return FE_INVALID_ARG; }
+  return s->sys.solve(norm_dx, norm_rhs, norm_axb, n_iter);
+}
+
+int fe_cuda_correct_solution(fe_cuda_system *s) { return s ? s->sys.correctSolution() : FE_INVALID_ARG; }
+
+int fe_cuda_get_matrix(const fe_cuda_system *s, double *values)
+{
+  if(!s || !values) { set_error("null argument"); return FE_INVALID_ARG; }
+  return s->sys.getMatrix(values);
+}
+
+int fe_cuda_get_rhs(const fe_cuda_system *s, double *rhs)
+{
+  if(!s || !rhs) { set_error("null argument"); return FE_INVALID_ARG; }
+  return s->sys.getRHS(rhs);
+}
+
+int fe_cuda_get_du(const fe_cuda_system *s, double *du)
+{
+  if(!s || !du) { set_error("null argument"); return FE_INVALID_ARG; }
+  return s->sys.getDu(du);
+}
+
+int fe_cuda_newton(fe_cuda_system *s, const fe_newton_options *o, fe_newton_stats *st)
+{
+  GUARD_BEGIN
+  if(!s || !o) { set_error("null argument"); return FE_INVALID_ARG; }
+  NewtonOptions no;
+  no.tolResidual = o->tol_residual;
+  no.tolCorrection = o->tol_correction;
+  no.tolDivergence = o->tol_divergence;
+  no.maxIter = o->max_iter;
+  no.recomputeEvery = o->recompute_every > 0 ? o->recompute_every : 3;
+  no.residualDecrease = o->residual_decrease;
+  no.stationary = o->stationary;
+  no.relResidual = o->rel_residual;
+  no.linearRtolMin = o->linear_rtol_min;
+  NewtonStats ns;
+  const PhaseTimes before = s->sys.times;
+  int r = newton_solve(s->sys, no, ns);
+  if(st) {
+    st->iterations = ns.iterations;
+    st->krylov_iterations = ns.krylovIterations;
+    st->matrix_assemblies = ns.matrixAssemblies;
+    st->status = ns.status;
+    st->residual0 = ns.residual0;
+    st->residual = ns.residual;
+    st->correction = ns.correction;
+    st->residual_ms = s->sys.times.residual_ms - before.residual_ms;
+    st->matrix_ms = s->sys.times.matrix_ms - before.matrix_ms;
+    st->factor_ms = s->sys.times.factor_ms - before.factor_ms;
+    st->solve_ms = s->sys.times.solve_ms - before.solve_ms;
+  }
+  return r;
+  GUARD_END
+}
+
+int fe_cuda_get_times(const fe_cuda_system *s, double *residual_ms, double *matrix_ms,
+                      double *factor_ms, double *solve_ms)
+{
+  if(!s) { set_error("null system"); return FE_INVALID_ARG; }
+  if(residual_ms) *residual_ms = s->sys.times.residual_ms;
+  if(matrix_ms) *matrix_ms = s->sys.times.matrix_ms;
+  if(factor_ms) *factor_ms = s->sys.times.factor_ms;
+  if(solve_ms) *solve_ms = s->sys.times.solve_ms;
+  return FE_OK;
+}
+
+int fe_cuda_reset_times(fe_cuda_system *s)
+{
+  if(!s) { set_error("null system"); return FE_INVALID_ARG; }
+  s->sys.times = PhaseTimes();
+  return FE_OK;
+}
+
+int fe_cuda_synchronize(fe_cuda_system *s)
+{
+  if(!s) { set_error("null system"); return FE_INVALID_ARG; }
+  cudaError_t e = cudaStreamSynchronize(s->sys.stream());
+  if(e != cudaSuccess) {
+    set_error("stream synchronize: %s", cudaGetErrorString(e));
+    return FE_CUDA_DEVICE_FAIL;
+  }
+  return FE_OK;
+}
+
+}  // extern "C"

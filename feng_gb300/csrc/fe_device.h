@@ -1,0 +1,88 @@
+// Device-side data of one linear system and the kernel entry points.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace feng {
+
+// Weak forms the fused element kernels know, named after feNG's
+// elementSystemType (feSysElm.h:13-77).
+enum FormKind : int {
+  FORM_SOURCE = 1,                           // feSysElm_Source
+  FORM_DIFFUSION = 2,                        // feSysElm_Diffusion<2>
+  FORM_VECTOR_SOURCE = 3,                    // feSysElm_VectorSource<2>
+  FORM_TRANSIENT_VECTOR_MASS = 4,            // feSysElm_TransientVectorMass<2>
+  FORM_MIXED_DIVERGENCE = 5,                 // feSysElm_MixedDivergence<2>
+  FORM_VECTOR_CONVECTIVE_ACCELERATION = 6,   // feSysElm_VectorConvectiveAcceleration<2>
+  FORM_DIV_NEWTONIAN_STRESS = 7,             // feSysElm_DivergenceNewtonianStress<2>
+};
+
+// Closed registry of non-constant source functions evaluated on the device
+// at quadrature nodes (std::function callbacks cannot run there).
+enum SourceKind : int {
+  SRC_NONE = 0,
+  SRC_SIN_SIN = 1,        // scalar  f = p0 * sin(pi x) sin(pi y)
+  SRC_NS_MMS_POLY = 2,    // vector  manufactured NS source of u=(x^4y^4, -4/5 x^3y^5), p=x^2y^2
+  SRC_CONST_VEC = 3,      // vector  f = (p0, p1)
+  SRC_SIN_BODY = 4,       // vector  f = (p0 sin(pi x) sin(pi y), 0)
+};
+
+// Reference-element tensors of one quadrature rule (all sums over the rule's
+// nodes, weights included):
+//   K[r][s][a][b] = sum_q w dphi_a/dr dphi_b/ds
+//   T[r][a][c][b] = sum_q w phi_a phi_c dphi_b/dr
+//   D[r][j][a]    = sum_q w psi_j dphi_a/dr        (psi: P1, phi: P2)
+//   M[a][b]       = sum_q w phi_a phi_b
+// with r,s in {r,s} reference directions, a,b,c P2 and j P1 functions.
+struct RefTensors {
+  double K[2][2][6][6];
+  double T[2][6][6][6];
+  double D[2][3][6];
+  double M[6][6];
+  int nq;
+  double qw[16], qr[16], qs[16];  // the rule, for non-polynomial sources
+  double phi[16][6];              // P2 functions at the nodes
+};
+
+// Constant coefficients of the fused forms (0 = form absent).
+struct FormCoeffs {
+  int elemType;     // 1 scalar P2, 2 Taylor-Hood P2-P1
+  double diff;      // DIFFUSION coefficient
+  double conv;      // VECTOR_CONVECTIVE_ACCELERATION coefficient
+  double sigma;     // DIV_NEWTONIAN_STRESS coefficient
+  double mu;        // DIV_NEWTONIAN_STRESS viscosity
+  double divu;      // MIXED_DIVERGENCE coefficient
+  double mass;      // TRANSIENT_VECTOR_MASS coefficient
+  int hasSigma, hasDivu, hasConv, hasMass, hasDiff;
+  int srcKind;      // SourceKind of SOURCE / VECTOR_SOURCE
+  double srcParam[4];
+  double srcCoeff;  // multiplies the source (1 when present)
+};
+
+struct DeviceMesh {
+  int64_t nElm = 0;
+  int nloc = 0;
+  int nColors = 0;
+  int64_t colorOff[65];
+  int32_t *adr = nullptr;    // [nloc][nElm]  global DOF per local DOF, color order
+  double *geo = nullptr;     // [5][nElm]     G00 G01 G10 G11 |J|   (G[r][k] = d r / d x_k)
+  double *xy = nullptr;      // [6][nElm]     x0 y0 x1 y1 x2 y2
+  int32_t *map = nullptr;    // [nloc*nloc][nElm] CSR position or -1
+};
+
+// Residual (FP64) of the fused forms on elements [begin,end) of the color
+// order, accumulated into rhs with feNG's sign (rhs = sum of element Be).
+void launch_assemble_residual(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
+                              const double *u, const double *udot, double t, int64_t nInc,
+                              double *rhs, int64_t begin, int64_t end, cudaStream_t s);
+// Jacobian of the fused forms, in double or float.
+void launch_assemble_matrix_f64(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
+                                const double *u, double c0, double *values, int64_t begin,
+                                int64_t end, cudaStream_t s);
+void launch_assemble_matrix_f32(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
+                                const double *u, double c0, float *values, int64_t begin,
+                                int64_t end, cudaStream_t s);
+
+}  // namespace feng

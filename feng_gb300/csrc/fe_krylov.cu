@@ -1,0 +1,906 @@
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "fe_common.h"
+#include "fe_krylov.h"
+
+namespace feng {
+
+#define CK(x)                                                                          \
+  do {                                                                                 \
+    cudaError_t _e = (x);                                                              \
+    if(_e != cudaSuccess) {                                                            \
+      set_error("CUDA error %s at %s:%d", cudaGetErrorString(_e), __FILE__, __LINE__); \
+      return FE_CUDA_FAIL;                                                             \
+    }                                                                                  \
+  } while(0)
+
+namespace {
+
+constexpr int RB = 256;        // threads per reduction block
+constexpr int MAXRED = 1024;   // maximum number of reduction blocks
+constexpr int MAXM = 128;      // maximum restart length
+
+// ---------------------------------------------------------------------------
+// SpMV: y = A x (or y = b - A x), LANES consecutive lanes per row.
+// ---------------------------------------------------------------------------
+template <typename VA, typename VX, typename VY, typename ACC, int LANES, bool RESID>
+__global__ void __launch_bounds__(256) k_spmv(int64_t n, const int32_t *__restrict__ ia,
+                                              const int32_t *__restrict__ ja,
+                                              const VA *__restrict__ a, const VX *__restrict__ x,
+                                              const double *__restrict__ b, VY *__restrict__ y,
+                                              const int *__restrict__ done)
+{
+  if(done && *done) return;
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
+  const int sub = threadIdx.x % LANES;
+  if(row >= n) return;
+  const int32_t beg = ia[row], end = ia[row + 1];
+  ACC acc = 0;
+  for(int32_t k = beg + sub; k < end; k += LANES) acc += (ACC)a[k] * (ACC)x[ja[k]];
+#pragma unroll
+  for(int o = LANES / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, LANES);
+  if(sub == 0) {
+    if(RESID) y[row] = (VY)(b[row] - (double)acc);
+    else y[row] = (VY)acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Reductions with in-kernel finalisation: every block writes a partial, the
+// last block to finish sums the partials in block order (deterministic).
+// ---------------------------------------------------------------------------
+struct RedState {
+  unsigned int counter;
+  double result[4];
+};
+
+__device__ double block_sum(double v, double *sh)
+{
+  for(int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+  if(l == 0) sh[w] = v;
+  __syncthreads();
+  v = 0;
+  if(threadIdx.x < blockDim.x / 32) v = sh[threadIdx.x];
+  if(w == 0)
+    for(int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  return v;  // valid in thread 0
+}
+
+__device__ double block_max(double v, double *sh)
+{
+  for(int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+  if(l == 0) sh[w] = v;
+  __syncthreads();
+  v = 0;
+  if(threadIdx.x < blockDim.x / 32) v = sh[threadIdx.x];
+  if(w == 0)
+    for(int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  __syncthreads();
+  return v;
+}
+
+// Finishes a reduction of K values: writes partials, last block sums them.
+template <int K, bool MAX>
+__device__ void finish_reduction(const double (&v)[K], double *partials, RedState *st,
+                                 double *out)
+{
+  __shared__ double sh[RB / 32];
+  __shared__ bool last;
+  double tot[K];
+#pragma unroll
+  for(int k = 0; k < K; ++k) tot[k] = MAX ? block_max(v[k], sh) : block_sum(v[k], sh);
+  if(threadIdx.x == 0) {
+#pragma unroll
+    for(int k = 0; k < K; ++k) partials[k * MAXRED + blockIdx.x] = tot[k];
+    __threadfence();
+    unsigned int prev = atomicAdd(&st->counter, 1u);
+    last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if(!last) return;
+  __threadfence();
+#pragma unroll
+  for(int k = 0; k < K; ++k) {
+    double s = 0.;
+    for(int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+      double p = ((volatile double *)partials)[k * MAXRED + i];
+      s = MAX ? fmax(s, p) : s + p;
+    }
+    s = MAX ? block_max(s, sh) : block_sum(s, sh);
+    if(threadIdx.x == 0) {
+      st->result[k] = s;
+      if(out) out[k] = s;
+    }
+  }
+  if(threadIdx.x == 0) st->counter = 0;
+}
+
+__global__ void k_dot(int64_t n, const double *__restrict__ x, const double *__restrict__ y,
+                      double *partials, RedState *st, double *out)
+{
+  double v[1] = {0.};
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x)
+    v[0] += x[i] * y[i];
+  finish_reduction<1, false>(v, partials, st, out);
+}
+
+__global__ void k_absmax(int64_t n, const double *__restrict__ x, double *partials, RedState *st,
+                         double *out)
+{
+  double v[1] = {0.};
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x)
+    v[0] = fmax(v[0], fabs(x[i]));
+  finish_reduction<1, true>(v, partials, st, out);
+}
+
+// h[c] (+)= V_c . w for c < ncols; grid (parts, ncols).  Partials per column.
+__global__ void k_mdot_partial(int64_t n, const double *__restrict__ V, int ncols,
+                               const double *__restrict__ w, double *partials,
+                               const int *__restrict__ done)
+{
+  if(*done) return;
+  __shared__ double sh[RB / 32];
+  const int c = blockIdx.y;
+  const double *vc = V + (int64_t)c * n;
+  double v = 0.;
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x)
+    v += vc[i] * w[i];
+  v = block_sum(v, sh);
+  if(threadIdx.x == 0) partials[(int64_t)c * MAXRED + blockIdx.x] = v;
+}
+
+// Sums the partials of each column c (block c) into hcol[c] (and H column).
+__global__ void k_mdot_final(int nparts, double *partials, double *hcur, double *Hcol, int accum,
+                             const int *__restrict__ done)
+{
+  if(*done) return;
+  __shared__ double sh[RB / 32];
+  const int c = blockIdx.x;
+  double s = 0.;
+  for(int i = threadIdx.x; i < nparts; i += blockDim.x) s += partials[(int64_t)c * MAXRED + i];
+  s = block_sum(s, sh);
+  if(threadIdx.x == 0) {
+    hcur[c] = s;
+    Hcol[c] = accum ? Hcol[c] + s : s;
+  }
+}
+
+// w -= sum_c h[c] V_c
+__global__ void k_mupdate(int64_t n, const double *__restrict__ V, int ncols,
+                          const double *__restrict__ h, double *__restrict__ w,
+                          const int *__restrict__ done)
+{
+  if(*done) return;
+  __shared__ double sh[MAXM + 1];
+  for(int c = threadIdx.x; c < ncols; c += blockDim.x) sh[c] = h[c];
+  __syncthreads();
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x) {
+    double acc = w[i];
+    for(int c = 0; c < ncols; ++c) acc -= sh[c] * V[(int64_t)c * n + i];
+    w[i] = acc;
+  }
+}
+
+// Sum of squares of w into st->result[0] (k_scale_from takes the root).
+__global__ void k_norm_to(int64_t n, const double *__restrict__ w, double *partials, RedState *st,
+                          const int *__restrict__ done)
+{
+  if(*done) return;
+  double v[1] = {0.};
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x)
+    v[0] += w[i] * w[i];
+  finish_reduction<1, false>(v, partials, st, nullptr);
+}
+
+// v = w / sqrt(ss), and H[j+1][j] = sqrt(ss).  ss read from st->result[0].
+__global__ void k_scale_from(int64_t n, const double *__restrict__ w, double *__restrict__ v,
+                             const RedState *st, double *Hsub, const int *__restrict__ done)
+{
+  if(*done) return;
+  const double nrm = sqrt(st->result[0]);
+  if(blockIdx.x == 0 && threadIdx.x == 0) *Hsub = nrm;
+  const double inv = nrm > 0 ? 1.0 / nrm : 0.0;
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x)
+    v[i] = w[i] * inv;
+}
+
+template <typename VO>
+__global__ void k_scale_vec(int64_t n, const double *__restrict__ w, VO *__restrict__ v,
+                            const double *__restrict__ s, int invert)
+{
+  const double f = invert ? (*s > 0 ? 1.0 / *s : 0.0) : *s;
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x)
+    v[i] = (VO)(w[i] * f);
+}
+
+__global__ void k_to_f32(int64_t n, const double *__restrict__ x, float *__restrict__ y,
+                         const int *__restrict__ done)
+{
+  if(done && *done) return;
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (float)x[i];
+}
+
+// Givens rotations on Hessenberg column j (device, one thread).  H is stored
+// column-major with leading dimension MAXM+1.
+struct GmresState {
+  double H[MAXM * (MAXM + 1)];
+  double cs[MAXM], sn[MAXM], g[MAXM + 1], y[MAXM];
+  double hcur[MAXM + 1];
+  double beta;    // ||r|| at the start of the cycle
+  int done;       // set once the estimate reaches tol or on breakdown
+  int k;          // number of basis vectors in use
+  double est;     // |g[k]|: residual norm estimate
+  double tol;
+};
+
+__global__ void k_givens(GmresState *gs, int j)
+{
+  if(gs->done) return;
+  double *h = gs->H + (int64_t)j * (MAXM + 1);
+  for(int i = 0; i < j; ++i) {
+    const double t = gs->cs[i] * h[i] + gs->sn[i] * h[i + 1];
+    h[i + 1] = -gs->sn[i] * h[i] + gs->cs[i] * h[i + 1];
+    h[i] = t;
+  }
+  const double a = h[j], b = h[j + 1];
+  const double r = hypot(a, b);
+  double c = 1., s = 0.;
+  if(r > 0) { c = a / r; s = b / r; }
+  gs->cs[j] = c;
+  gs->sn[j] = s;
+  h[j] = r;
+  h[j + 1] = 0.;
+  gs->g[j + 1] = -s * gs->g[j];
+  gs->g[j] = c * gs->g[j];
+  gs->k = j + 1;
+  gs->est = fabs(gs->g[j + 1]);
+  if(!(gs->est > gs->tol) || b == 0.0 || !isfinite(gs->est)) gs->done = 1;
+}
+
+__global__ void k_backsolve(GmresState *gs)
+{
+  const int k = gs->k;
+  for(int i = k - 1; i >= 0; --i) {
+    double s = gs->g[i];
+    for(int c = i + 1; c < k; ++c) s -= gs->H[(int64_t)c * (MAXM + 1) + i] * gs->y[c];
+    const double d = gs->H[(int64_t)i * (MAXM + 1) + i];
+    gs->y[i] = d != 0 ? s / d : 0.;
+  }
+}
+
+template <typename VZ>
+__global__ void k_xupdate(int64_t n, const VZ *__restrict__ Z, const GmresState *gs,
+                          double *__restrict__ x)
+{
+  __shared__ double sy[MAXM];
+  const int k = gs->k;
+  for(int c = threadIdx.x; c < k; c += blockDim.x) sy[c] = gs->y[c];
+  __syncthreads();
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x) {
+    double acc = x[i];
+    for(int c = 0; c < k; ++c) acc += sy[c] * (double)Z[(int64_t)c * n + i];
+    x[i] = acc;
+  }
+}
+
+__global__ void k_gmres_init(GmresState *gs, const RedState *st, double tol)
+{
+  const double beta = sqrt(st->result[0]);
+  gs->g[0] = beta;
+  for(int i = 1; i <= MAXM; ++i) gs->g[i] = 0.;
+  gs->done = (beta <= tol || !isfinite(beta)) ? 1 : 0;
+  gs->k = 0;
+  gs->est = beta;
+  gs->tol = tol;
+}
+
+// ---------------------------------------------------------------------------
+// Block-Jacobi ILU(0): one thread per block, rows in ascending order.
+// Factorisation: IKJ variant restricted to the pattern (Saad Alg. 10.4).
+// ---------------------------------------------------------------------------
+template <typename VF>
+__global__ void k_ilu_factor(int64_t nBlocks, const int32_t *__restrict__ bstart,
+                             const int32_t *__restrict__ perm, const int32_t *__restrict__ lia,
+                             const int32_t *__restrict__ lja, const int32_t *__restrict__ ldiag,
+                             const int32_t *__restrict__ srcPos, const double *__restrict__ v64,
+                             const float *__restrict__ v32, VF *__restrict__ f,
+                             int *__restrict__ status)
+{
+  const int64_t blk = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if(blk >= nBlocks) return;
+  for(int32_t q = bstart[blk]; q < bstart[blk + 1]; ++q) {
+    const int32_t i = perm[q];
+    const int32_t rb = lia[i], re = lia[i + 1], rd = ldiag[i];
+    for(int32_t k = rb; k < re; ++k) f[k] = v64 ? (VF)v64[srcPos[k]] : (VF)v32[srcPos[k]];
+    // eliminate with previous rows k < i (entries before the diagonal)
+    for(int32_t kk = rb; kk < rd; ++kk) {
+      const int32_t kr = lja[kk];
+      const VF piv = f[ldiag[kr]];
+      if(piv == (VF)0) { atomicExch(status, 1); return; }
+      const VF lik = f[kk] / piv;
+      f[kk] = lik;
+      // row i entries j > kr: subtract lik * U(kr, j) where (kr,j) exists
+      int32_t p = ldiag[kr] + 1;
+      const int32_t pe = lia[kr + 1];
+      for(int32_t jj = kk + 1; jj < re && p < pe; ++jj) {
+        const int32_t col = lja[jj];
+        while(p < pe && lja[p] < col) ++p;
+        if(p < pe && lja[p] == col) f[jj] -= lik * f[p];
+      }
+    }
+    const VF d = f[rd];
+    if(d == (VF)0) { atomicExch(status, 1); return; }
+    if(!isfinite((double)d)) { atomicExch(status, 2); return; }
+  }
+}
+
+// z = (LU)^{-1} r on each block.
+template <typename VF, typename VV>
+__global__ void k_ilu_solve(int64_t nBlocks, const int32_t *__restrict__ bstart,
+                            const int32_t *__restrict__ perm, const int32_t *__restrict__ lia,
+                            const int32_t *__restrict__ lja, const int32_t *__restrict__ ldiag,
+                            const VF *__restrict__ f, const VV *__restrict__ r,
+                            VV *__restrict__ z, const int *__restrict__ done)
+{
+  if(done && *done) return;
+  const int64_t blk = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if(blk >= nBlocks) return;
+  const int32_t qb = bstart[blk], qe = bstart[blk + 1];
+  for(int32_t q = qb; q < qe; ++q) {
+    const int32_t i = perm[q];
+    VF s = (VF)r[i];
+    for(int32_t k = lia[i]; k < ldiag[i]; ++k) s -= f[k] * (VF)z[lja[k]];
+    z[i] = (VV)s;
+  }
+  for(int32_t q = qe - 1; q >= qb; --q) {
+    const int32_t i = perm[q];
+    VF s = (VF)z[i];
+    const int32_t d = ldiag[i];
+    for(int32_t k = d + 1; k < lia[i + 1]; ++k) s -= f[k] * (VF)z[lja[k]];
+    z[i] = (VV)(s / f[d]);
+  }
+}
+
+template <typename VV, typename VD>
+__global__ void k_jacobi(int64_t n, const VD *__restrict__ dinv, const VV *__restrict__ r,
+                         VV *__restrict__ z, const int *__restrict__ done)
+{
+  if(done && *done) return;
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x)
+    z[i] = (VV)((VD)r[i] * dinv[i]);
+}
+
+template <typename VA, typename VD>
+__global__ void k_inv_diag(int64_t n, const int32_t *__restrict__ diag, const VA *__restrict__ a,
+                           VD *__restrict__ dinv, int *__restrict__ status)
+{
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x) {
+    const VA d = a[diag[i]];
+    if(d == (VA)0) { atomicExch(status, 1); dinv[i] = 0; }
+    else dinv[i] = (VD)(1.0 / (double)d);
+  }
+}
+
+// CG helpers operating on device scalars (CGState) so that the host need not
+// read back anything inside an iteration.
+struct CGState {
+  double rz, rzOld, pq, rr;
+  double tol;
+  int done;
+  int it;
+};
+
+__global__ void k_cg_xr(int64_t n, CGState *cs, const double *__restrict__ p,
+                        const double *__restrict__ q, double *__restrict__ x,
+                        double *__restrict__ r, double *partials, RedState *st)
+{
+  // alpha = rz / pq ; x += alpha p ; r -= alpha q ; accumulate rr
+  double v[1] = {0.};
+  if(!cs->done) {
+    const double alpha = cs->rz / cs->pq;
+    for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x) {
+      x[i] += alpha * p[i];
+      const double ri = r[i] - alpha * q[i];
+      r[i] = ri;
+      v[0] += ri * ri;
+    }
+  }
+  finish_reduction<1, false>(v, partials, st, nullptr);
+}
+
+__global__ void k_cg_check(CGState *cs, const RedState *st)
+{
+  if(cs->done) return;
+  cs->rr = st->result[0];
+  cs->it++;
+  if(!(sqrt(cs->rr) > cs->tol) || !isfinite(cs->rr)) cs->done = 1;
+}
+
+__global__ void k_cg_p(int64_t n, CGState *cs, const RedState *st, const double *__restrict__ z,
+                       double *__restrict__ p, int first)
+{
+  if(cs->done) return;
+  const double rzNew = st->result[0];
+  const double beta = first ? 0. : rzNew / cs->rz;
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = z[i] + beta * p[i];
+  __syncthreads();
+  // the scalar update happens in k_cg_rz once every block is done
+}
+
+__global__ void k_cg_rz(CGState *cs, const RedState *st)
+{
+  if(cs->done) return;
+  cs->rz = st->result[0];
+}
+
+__global__ void k_cg_pq(CGState *cs, const RedState *st)
+{
+  if(cs->done) return;
+  cs->pq = st->result[0];
+  if(cs->pq == 0.0 || !isfinite(cs->pq)) cs->done = 1;
+}
+
+__global__ void k_dot_if(int64_t n, const double *__restrict__ x, const double *__restrict__ y,
+                         double *partials, RedState *st, const CGState *cs)
+{
+  double v[1] = {0.};
+  if(!cs->done)
+    for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+      v[0] += x[i] * y[i];
+  finish_reduction<1, false>(v, partials, st, nullptr);
+}
+
+__global__ void k_zero(int64_t n, double *x)
+{
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = 0.;
+}
+
+__global__ void k_copy(int64_t n, const double *__restrict__ a, double *__restrict__ b)
+{
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = a[i];
+}
+
+__global__ void k_axpy(int64_t n, double alpha, const double *__restrict__ x, double *__restrict__ y)
+{
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x)
+    y[i] += alpha * x[i];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+namespace {
+struct Ws {
+  RedState *st;
+  GmresState *gs, *hgs;
+  CGState *cg, *hcg;
+};
+}  // namespace
+#define Ws_INIT(k) {(RedState *)(k)->red_state_, (GmresState *)(k)->gmres_, (GmresState *)(k)->h_gmres_, (CGState *)(k)->cg_, (CGState *)(k)->h_cg_}
+Krylov::~Krylov()
+{
+  cudaFree(V_); cudaFree(Z_); cudaFree(Z32_); cudaFree(v32_); cudaFree(w32_);
+  cudaFree(w_); cudaFree(r_); cudaFree(t_); cudaFree(p_); cudaFree(q_);
+  cudaFree(diag_); cudaFree(diag32_); cudaFree(red_); cudaFree(dsum_);
+  cudaFreeHost(hred_);
+  cudaFree(ilu_.blockStart); cudaFree(ilu_.perm); cudaFree(ilu_.lia); cudaFree(ilu_.lja);
+  cudaFree(ilu_.ldiag); cudaFree(ilu_.srcPos); cudaFree(ilu_.vals); cudaFree(ilu_.status);
+  cudaFree(red_state_); cudaFree(gmres_); cudaFree(cg_);
+  cudaFreeHost(h_gmres_); cudaFreeHost(h_cg_);
+}
+
+static int grid_for(int64_t n, int threads, int maxBlocks)
+{
+  int64_t b = (n + threads - 1) / threads;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(b, maxBlocks));
+}
+
+int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, int64_t nBlocksHint,
+                  const KrylovOptions &o, cudaStream_t s)
+{
+  A_ = A;
+  opt = o;
+  s_ = s;
+  n_ = A.n;
+  if(opt.restart < 1 || opt.restart > MAXM) {
+    set_error("restart must be in [1, %d]", MAXM);
+    return FE_INVALID_ARG;
+  }
+  const double avg = n_ > 0 ? (double)A.nnz / n_ : 0;
+  lanes_ = avg > 24 ? 8 : 4;
+  nParts_ = grid_for(n_, RB, MAXRED);
+  const int m = opt.restart;
+  CK(cudaMalloc(&red_, sizeof(double) * MAXRED * (MAXM + 2)));
+  CK(cudaMalloc(&dsum_, sizeof(double) * 8));
+  CK(cudaMallocHost(&hred_, sizeof(double) * 8));
+  CK(cudaMalloc(&w_, sizeof(double) * n_));
+  CK(cudaMalloc(&r_, sizeof(double) * n_));
+  CK(cudaMalloc(&t_, sizeof(double) * n_));
+  CK(cudaMalloc(&p_, sizeof(double) * n_));
+  CK(cudaMalloc(&q_, sizeof(double) * n_));
+  if(opt.method == 1) {
+    CK(cudaMalloc(&V_, sizeof(double) * n_ * (m + 1)));
+    if(opt.mixed) {
+      CK(cudaMalloc(&Z32_, sizeof(float) * n_ * m));
+      CK(cudaMalloc(&v32_, sizeof(float) * n_));
+      CK(cudaMalloc(&w32_, sizeof(float) * n_));
+    } else {
+      CK(cudaMalloc(&Z_, sizeof(double) * n_ * m));
+    }
+  }
+  CK(cudaMalloc(&red_state_, sizeof(RedState)));
+  CK(cudaMemset(red_state_, 0, sizeof(RedState)));
+  CK(cudaMalloc(&gmres_, sizeof(GmresState)));
+  CK(cudaMemset(gmres_, 0, sizeof(GmresState)));
+  CK(cudaMalloc(&cg_, sizeof(CGState)));
+  CK(cudaMemset(cg_, 0, sizeof(CGState)));
+  CK(cudaMallocHost(&h_gmres_, sizeof(GmresState)));
+  CK(cudaMallocHost(&h_cg_, sizeof(CGState)));
+
+  if(opt.precond == 2) {
+    if(opt.mixed) CK(cudaMalloc(&diag32_, sizeof(float) * n_));
+    else CK(cudaMalloc(&diag_, sizeof(double) * n_));
+    CK(cudaMalloc(&ilu_.status, sizeof(int)));
+  } else if(opt.precond == 1) {
+    // Host: gather the block-diagonal part of the pattern.
+    std::vector<int32_t> hia(n_ + 1), hja(A.nnz);
+    CK(cudaMemcpy(hia.data(), A.ia, sizeof(int32_t) * (n_ + 1), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hja.data(), A.ja, sizeof(int32_t) * A.nnz, cudaMemcpyDeviceToHost));
+    std::vector<int32_t> blk(n_);
+    int64_t nb = 1;
+    if((int64_t)blockOfRow.size() == n_) {
+      nb = 0;
+      for(int64_t i = 0; i < n_; ++i) {
+        blk[i] = blockOfRow[i];
+        nb = std::max<int64_t>(nb, blk[i] + 1);
+      }
+    } else {
+      nb = std::max<int64_t>(1, std::min<int64_t>(nBlocksHint, n_));
+      for(int64_t i = 0; i < n_; ++i) blk[i] = (int32_t)((i * nb) / n_);
+    }
+    std::vector<int32_t> bstart(nb + 1, 0), perm(n_);
+    for(int64_t i = 0; i < n_; ++i) bstart[blk[i] + 1]++;
+    for(int64_t b = 0; b < nb; ++b) bstart[b + 1] += bstart[b];
+    std::vector<int32_t> fillp(bstart.begin(), bstart.end() - 1);
+    for(int64_t i = 0; i < n_; ++i) perm[fillp[blk[i]]++] = (int32_t)i;
+    std::vector<int32_t> lia(n_ + 1, 0), lja, ldiag(n_, -1), src;
+    lja.reserve(A.nnz);
+    src.reserve(A.nnz);
+    for(int64_t i = 0; i < n_; ++i) {
+      for(int32_t k = hia[i]; k < hia[i + 1]; ++k) {
+        const int32_t j = hja[k];
+        if(blk[j] != blk[i]) continue;
+        if(j == i) ldiag[i] = (int32_t)lja.size();
+        lja.push_back(j);
+        src.push_back(k);
+      }
+      lia[i + 1] = (int32_t)lja.size();
+      if(ldiag[i] < 0) {
+        set_error("row %lld has no diagonal entry in the pattern", (long long)i);
+        return FE_INVALID_ARG;
+      }
+    }
+    ilu_.nBlocks = nb;
+    ilu_.lnnz = (int64_t)lja.size();
+    CK(cudaMalloc(&ilu_.blockStart, sizeof(int32_t) * (nb + 1)));
+    CK(cudaMalloc(&ilu_.perm, sizeof(int32_t) * n_));
+    CK(cudaMalloc(&ilu_.lia, sizeof(int32_t) * (n_ + 1)));
+    CK(cudaMalloc(&ilu_.lja, sizeof(int32_t) * ilu_.lnnz));
+    CK(cudaMalloc(&ilu_.ldiag, sizeof(int32_t) * n_));
+    CK(cudaMalloc(&ilu_.srcPos, sizeof(int32_t) * ilu_.lnnz));
+    CK(cudaMalloc(&ilu_.vals, (opt.mixed ? sizeof(float) : sizeof(double)) * ilu_.lnnz));
+    CK(cudaMalloc(&ilu_.status, sizeof(int)));
+    CK(cudaMemcpy(ilu_.blockStart, bstart.data(), sizeof(int32_t) * (nb + 1), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ilu_.perm, perm.data(), sizeof(int32_t) * n_, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ilu_.lia, lia.data(), sizeof(int32_t) * (n_ + 1), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ilu_.lja, lja.data(), sizeof(int32_t) * ilu_.lnnz, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ilu_.ldiag, ldiag.data(), sizeof(int32_t) * n_, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ilu_.srcPos, src.data(), sizeof(int32_t) * ilu_.lnnz, cudaMemcpyHostToDevice));
+  }
+  return FE_OK;
+}
+
+int Krylov::factor(const double *values64, const float *values32)
+{
+  factoredOk_ = false;
+  if(opt.precond == 0) { factoredOk_ = true; return FE_OK; }
+  CK(cudaMemsetAsync(ilu_.status, 0, sizeof(int), s_));
+  if(opt.precond == 2) {
+    const int g = grid_for(n_, 256, 4096);
+    if(opt.mixed) k_inv_diag<float, float><<<g, 256, 0, s_>>>(n_, A_.diag, values32, diag32_, ilu_.status);
+    else k_inv_diag<double, double><<<g, 256, 0, s_>>>(n_, A_.diag, values64, diag_, ilu_.status);
+  } else {
+    const int g = grid_for(ilu_.nBlocks, 64, 1 << 20);
+    if(opt.mixed)
+      k_ilu_factor<float><<<g, 64, 0, s_>>>(ilu_.nBlocks, ilu_.blockStart, ilu_.perm, ilu_.lia,
+                                            ilu_.lja, ilu_.ldiag, ilu_.srcPos, nullptr, values32,
+                                            (float *)ilu_.vals, ilu_.status);
+    else
+      k_ilu_factor<double><<<g, 64, 0, s_>>>(ilu_.nBlocks, ilu_.blockStart, ilu_.perm, ilu_.lia,
+                                             ilu_.lja, ilu_.ldiag, ilu_.srcPos, values64, nullptr,
+                                             (double *)ilu_.vals, ilu_.status);
+  }
+  CK(cudaGetLastError());
+  int hs = 0;
+  CK(cudaMemcpyAsync(&hs, ilu_.status, sizeof(int), cudaMemcpyDeviceToHost, s_));
+  CK(cudaStreamSynchronize(s_));
+  if(hs != 0) {
+    set_error(hs == 1 ? "preconditioner build hit a zero pivot" : "preconditioner build produced a non-finite pivot");
+    return FE_PC_FAILED;
+  }
+  factoredOk_ = true;
+  return FE_OK;
+}
+
+void Krylov::precond64(const double *r, double *z, const int *done)
+{
+  if(opt.precond == 0) {
+    cudaMemcpyAsync(z, r, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s_);
+  } else if(opt.precond == 2) {
+    k_jacobi<double, double><<<grid_for(n_, 256, 4096), 256, 0, s_>>>(n_, diag_, r, z, done);
+  } else {
+    k_ilu_solve<double, double><<<grid_for(ilu_.nBlocks, 64, 1 << 20), 64, 0, s_>>>(
+      ilu_.nBlocks, ilu_.blockStart, ilu_.perm, ilu_.lia, ilu_.lja, ilu_.ldiag,
+      (const double *)ilu_.vals, r, z, done);
+  }
+}
+
+void Krylov::precond32(const float *r, float *z, const int *done)
+{
+  if(opt.precond == 0) {
+    cudaMemcpyAsync(z, r, sizeof(float) * n_, cudaMemcpyDeviceToDevice, s_);
+  } else if(opt.precond == 2) {
+    k_jacobi<float, float><<<grid_for(n_, 256, 4096), 256, 0, s_>>>(n_, diag32_, r, z, done);
+  } else {
+    k_ilu_solve<float, float><<<grid_for(ilu_.nBlocks, 64, 1 << 20), 64, 0, s_>>>(
+      ilu_.nBlocks, ilu_.blockStart, ilu_.perm, ilu_.lia, ilu_.lja, ilu_.ldiag,
+      (const float *)ilu_.vals, r, z, done);
+  }
+}
+
+template <typename VA, typename VX, typename VY, typename ACC, bool RESID>
+static void spmv_launch(int lanes, int64_t n, const DeviceCSR &A, const VA *a, const VX *x,
+                        const double *b, VY *y, const int *done, cudaStream_t s)
+{
+  const int64_t threads = n * lanes;
+  const int grid = (int)((threads + 255) / 256);
+  if(lanes == 8)
+    k_spmv<VA, VX, VY, ACC, 8, RESID><<<grid, 256, 0, s>>>(n, A.ia, A.ja, a, x, b, y, done);
+  else
+    k_spmv<VA, VX, VY, ACC, 4, RESID><<<grid, 256, 0, s>>>(n, A.ia, A.ja, a, x, b, y, done);
+}
+
+void Krylov::spmv64(const double *values, const double *x, double *y)
+{
+  spmv_launch<double, double, double, double, false>(lanes_, n_, A_, values, x, nullptr, y,
+                                                     nullptr, s_);
+}
+
+double Krylov::dot(const double *x, const double *y)
+{
+  Ws w = Ws_INIT(this);
+  k_dot<<<nParts_, RB, 0, s_>>>(n_, x, y, red_, w.st, dsum_);
+  cudaMemcpyAsync(hred_, dsum_, sizeof(double), cudaMemcpyDeviceToHost, s_);
+  cudaStreamSynchronize(s_);
+  return hred_[0];
+}
+
+double Krylov::norm2(const double *x) { return sqrt(dot(x, x)); }
+
+double Krylov::norminf(const double *x)
+{
+  Ws w = Ws_INIT(this);
+  k_absmax<<<nParts_, RB, 0, s_>>>(n_, x, red_, w.st, dsum_);
+  cudaMemcpyAsync(hred_, dsum_, sizeof(double), cudaMemcpyDeviceToHost, s_);
+  cudaStreamSynchronize(s_);
+  return hred_[0];
+}
+
+// FGMRES(m), right preconditioned, FP64 throughout (Saad Alg. 9.6).
+int Krylov::solve_fgmres64(const double *vals, const double *b, double *x, double tolAbs, int maxIt,
+                           KrylovStats &st)
+{
+  Ws w = Ws_INIT(this);
+  const int m = opt.restart;
+  const int gv = grid_for(n_, 256, 2048);
+  int total = 0;
+  while(true) {
+    // r = b - A x  -> V_0 = r / ||r||
+    spmv_launch<double, double, double, double, true>(lanes_, n_, A_, vals, x, b, w_, nullptr, s_);
+    cudaMemsetAsync(&w.gs->done, 0, sizeof(int), s_);
+    k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done);
+    k_gmres_init<<<1, 1, 0, s_>>>(w.gs, w.st, tolAbs);
+    k_scale_from<<<gv, 256, 0, s_>>>(n_, w_, V_, w.st, &w.gs->beta, &w.gs->done);
+    const int jmax = std::min(m, maxIt - total);
+    for(int j = 0; j < jmax; ++j) {
+      double *vj = V_ + (int64_t)j * n_, *zj = Z_ + (int64_t)j * n_;
+      precond64(vj, zj, &w.gs->done);
+      spmv_launch<double, double, double, double, false>(lanes_, n_, A_, vals, zj, nullptr, w_,
+                                                         &w.gs->done, s_);
+      double *Hcol = w.gs->H + (int64_t)j * (MAXM + 1);
+      for(int pass = 0; pass < 2; ++pass) {
+        k_mdot_partial<<<dim3(nParts_, j + 1), RB, 0, s_>>>(n_, V_, j + 1, w_, red_, &w.gs->done);
+        k_mdot_final<<<j + 1, RB, 0, s_>>>(nParts_, red_, w.gs->hcur, Hcol, pass, &w.gs->done);
+        k_mupdate<<<gv, 256, 0, s_>>>(n_, V_, j + 1, w.gs->hcur, w_, &w.gs->done);
+      }
+      k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done);
+      k_scale_from<<<gv, 256, 0, s_>>>(n_, w_, V_ + (int64_t)(j + 1) * n_, w.st, Hcol + j + 1,
+                                       &w.gs->done);
+      k_givens<<<1, 1, 0, s_>>>(w.gs, j);
+    }
+    k_backsolve<<<1, 1, 0, s_>>>(w.gs);
+    k_xupdate<double><<<gv, 256, 0, s_>>>(n_, Z_, w.gs, x);
+    cudaMemcpyAsync(w.hgs, w.gs, sizeof(GmresState), cudaMemcpyDeviceToHost, s_);
+    CK(cudaStreamSynchronize(s_));
+    CK(cudaGetLastError());
+    total += w.hgs->k;
+    st.iterations = total;
+    st.rnorm = w.hgs->est;
+    if(!std::isfinite(w.hgs->est)) { set_error("non-finite residual in FGMRES"); return FE_NONFINITE; }
+    if(w.hgs->est <= tolAbs) break;
+    if(total >= maxIt || w.hgs->k == 0) break;
+    if(w.hgs->est > opt.dtol * std::max(st.rnorm0, 1e-300)) { set_error("FGMRES diverged"); return FE_NOT_CONVERGED; }
+  }
+  // Converged on the Arnoldi estimate (as PETSc's default test); report the
+  // true residual alongside.
+  const bool conv = w.hgs->est <= tolAbs;
+  spmv_launch<double, double, double, double, true>(lanes_, n_, A_, vals, x, b, w_, nullptr, s_);
+  st.rnorm = norm2(w_);
+  return conv ? FE_OK : FE_NOT_CONVERGED;
+}
+
+// FGMRES with FP32 matrix, SpMV and preconditioner, FP64 Krylov basis and
+// Gram-Schmidt; every restart recomputes the true residual b - A x with FP64
+// accumulation (iterative refinement).
+int Krylov::solve_fgmres_mixed(const float *vals32, const double *b, double *x, double tolAbs,
+                               int maxIt, KrylovStats &st)
+{
+  Ws w = Ws_INIT(this);
+  const int m = opt.restart;
+  const int gv = grid_for(n_, 256, 2048);
+  int total = 0;
+  while(true) {
+    spmv_launch<float, double, double, double, true>(lanes_, n_, A_, vals32, x, b, w_, nullptr, s_);
+    cudaMemsetAsync(&w.gs->done, 0, sizeof(int), s_);
+    k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done);
+    k_gmres_init<<<1, 1, 0, s_>>>(w.gs, w.st, tolAbs);
+    k_scale_from<<<gv, 256, 0, s_>>>(n_, w_, V_, w.st, &w.gs->beta, &w.gs->done);
+    st.refinements++;
+    const int jmax = std::min(m, maxIt - total);
+    for(int j = 0; j < jmax; ++j) {
+      double *vj = V_ + (int64_t)j * n_;
+      float *zj = Z32_ + (int64_t)j * n_;
+      k_to_f32<<<gv, 256, 0, s_>>>(n_, vj, v32_, &w.gs->done);
+      precond32(v32_, zj, &w.gs->done);
+      spmv_launch<float, float, double, float, false>(lanes_, n_, A_, vals32, zj, nullptr, w_,
+                                                      &w.gs->done, s_);
+      double *Hcol = w.gs->H + (int64_t)j * (MAXM + 1);
+      for(int pass = 0; pass < 2; ++pass) {
+        k_mdot_partial<<<dim3(nParts_, j + 1), RB, 0, s_>>>(n_, V_, j + 1, w_, red_, &w.gs->done);
+        k_mdot_final<<<j + 1, RB, 0, s_>>>(nParts_, red_, w.gs->hcur, Hcol, pass, &w.gs->done);
+        k_mupdate<<<gv, 256, 0, s_>>>(n_, V_, j + 1, w.gs->hcur, w_, &w.gs->done);
+      }
+      k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done);
+      k_scale_from<<<gv, 256, 0, s_>>>(n_, w_, V_ + (int64_t)(j + 1) * n_, w.st, Hcol + j + 1,
+                                       &w.gs->done);
+      k_givens<<<1, 1, 0, s_>>>(w.gs, j);
+    }
+    k_backsolve<<<1, 1, 0, s_>>>(w.gs);
+    k_xupdate<float><<<gv, 256, 0, s_>>>(n_, Z32_, w.gs, x);
+    cudaMemcpyAsync(w.hgs, w.gs, sizeof(GmresState), cudaMemcpyDeviceToHost, s_);
+    CK(cudaStreamSynchronize(s_));
+    CK(cudaGetLastError());
+    total += w.hgs->k;
+    st.iterations = total;
+    if(!std::isfinite(w.hgs->est)) { set_error("non-finite residual in mixed FGMRES"); return FE_NONFINITE; }
+    // Refinement check on the true residual.
+    spmv_launch<float, double, double, double, true>(lanes_, n_, A_, vals32, x, b, w_, nullptr, s_);
+    st.rnorm = norm2(w_);
+    if(st.rnorm <= tolAbs) break;
+    if(total >= maxIt || w.hgs->k == 0) break;
+    if(st.rnorm > opt.dtol * std::max(st.rnorm0, 1e-300)) { set_error("mixed FGMRES diverged"); return FE_NOT_CONVERGED; }
+  }
+  return st.rnorm <= tolAbs * 1.0000001 + 1e-300 ? FE_OK : FE_NOT_CONVERGED;
+}
+
+// Preconditioned CG (Saad Alg. 9.1) with device-resident scalars; the host
+// polls convergence every 8 iterations.
+int Krylov::solve_cg64(const double *vals, const double *b, double *x, double tolAbs, int maxIt,
+                       KrylovStats &st)
+{
+  Ws w = Ws_INIT(this);
+  const int gv = grid_for(n_, 256, 2048);
+  // x = 0, r = b
+  k_zero<<<gv, 256, 0, s_>>>(n_, x);
+  k_copy<<<gv, 256, 0, s_>>>(n_, b, r_);
+  CGState init{};
+  init.tol = tolAbs;
+  init.done = 0;
+  cudaMemcpyAsync(w.cg, &init, sizeof(CGState), cudaMemcpyHostToDevice, s_);
+  // z = M r ; rz = r.z ; p = z
+  precond64(r_, t_, &w.cg->done);
+  k_dot_if<<<nParts_, RB, 0, s_>>>(n_, r_, t_, red_, w.st, w.cg);
+  k_cg_p<<<gv, 256, 0, s_>>>(n_, w.cg, w.st, t_, p_, 1);
+  k_cg_rz<<<1, 1, 0, s_>>>(w.cg, w.st);
+  int it = 0;
+  while(it < maxIt) {
+    const int batch = std::min(8, maxIt - it);
+    for(int k = 0; k < batch; ++k) {
+      spmv_launch<double, double, double, double, false>(lanes_, n_, A_, vals, p_, nullptr, q_,
+                                                         &w.cg->done, s_);
+      k_dot_if<<<nParts_, RB, 0, s_>>>(n_, p_, q_, red_, w.st, w.cg);
+      k_cg_pq<<<1, 1, 0, s_>>>(w.cg, w.st);
+      k_cg_xr<<<nParts_, RB, 0, s_>>>(n_, w.cg, p_, q_, x, r_, red_, w.st);
+      k_cg_check<<<1, 1, 0, s_>>>(w.cg, w.st);
+      precond64(r_, t_, &w.cg->done);
+      k_dot_if<<<nParts_, RB, 0, s_>>>(n_, r_, t_, red_, w.st, w.cg);
+      k_cg_p<<<gv, 256, 0, s_>>>(n_, w.cg, w.st, t_, p_, 0);
+      k_cg_rz<<<1, 1, 0, s_>>>(w.cg, w.st);
+    }
+    it += batch;
+    cudaMemcpyAsync(w.hcg, w.cg, sizeof(CGState), cudaMemcpyDeviceToHost, s_);
+    CK(cudaStreamSynchronize(s_));
+    CK(cudaGetLastError());
+    if(w.hcg->done) break;
+  }
+  st.iterations = w.hcg->it;
+  st.rnorm = sqrt(w.hcg->rr);
+  if(!std::isfinite(st.rnorm)) { set_error("non-finite residual in CG"); return FE_NONFINITE; }
+  return st.rnorm <= tolAbs * 1.0000001 ? FE_OK : FE_NOT_CONVERGED;
+}
+
+int Krylov::solve(const double *values64, const float *values32, const double *b, double *x,
+                  KrylovStats &st)
+{
+  st = KrylovStats();
+  if(!factoredOk_) {
+    set_error("preconditioner not built");
+    return FE_PC_FAILED;
+  }
+  const double bn = norm2(b);
+  st.rnorm0 = bn;
+  if(!std::isfinite(bn)) { set_error("non-finite right-hand side"); return FE_NONFINITE; }
+  const int gv = grid_for(n_, 256, 2048);
+  k_zero<<<gv, 256, 0, s_>>>(n_, x);
+  const double tolAbs = std::max(opt.rtol * bn, opt.atol);
+  if(bn <= opt.atol) { st.rnorm = bn; return FE_OK; }
+  if(opt.method == 0) {
+    if(opt.mixed) { set_error("CG runs in FP64 only"); return FE_INVALID_ARG; }
+    return solve_cg64(values64, b, x, tolAbs, opt.maxIter, st);
+  }
+  if(opt.mixed) return solve_fgmres_mixed(values32, b, x, tolAbs, opt.maxIter, st);
+  return solve_fgmres64(values64, b, x, tolAbs, opt.maxIter, st);
+}
+
+}  // namespace feng

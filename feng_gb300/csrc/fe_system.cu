@@ -1,0 +1,558 @@
+#include "fe_system.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "fe_common.h"
+
+namespace feng {
+
+#define CK(x)                                                                          \
+  do {                                                                                 \
+    cudaError_t _e = (x);                                                              \
+    if(_e != cudaSuccess) {                                                            \
+      set_error("CUDA error %s at %s:%d", cudaGetErrorString(_e), __FILE__, __LINE__); \
+      return FE_CUDA_FAIL;                                                             \
+    }                                                                                  \
+  } while(0)
+
+namespace {
+
+__global__ void k_add(int64_t n, const double *__restrict__ du, double *__restrict__ u)
+{
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x)
+    u[i] += du[i];
+}
+
+__global__ void k_soldot(int64_t n, int order, double c0, double c1, double c2,
+                         const double *__restrict__ u, const double *__restrict__ h1,
+                         const double *__restrict__ h2, double *__restrict__ ud)
+{
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x) {
+    double v = c0 * u[i];
+    if(order >= 1) v += c1 * h1[i];
+    if(order >= 2) v += c2 * h2[i];
+    ud[i] = v;
+  }
+}
+
+__global__ void k_diagpos(int64_t n, const int32_t *__restrict__ ia, const int32_t *__restrict__ ja,
+                          int32_t *__restrict__ diag)
+{
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x) {
+    int32_t d = -1;
+    for(int32_t k = ia[i]; k < ia[i + 1]; ++k)
+      if(ja[k] == i) { d = k; break; }
+    diag[i] = d;
+  }
+}
+
+int gridFor(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 4096)); }
+
+void p2_basis(double r, double s, double phi[6], double dr[6], double ds[6])
+{
+  // feSpaceTriP2 (feSpace_2D.cpp:536-566, 727-737)
+  phi[0] = (1. - r - s) * (1. - 2. * r - 2. * s);
+  phi[1] = r * (2. * r - 1.);
+  phi[2] = s * (2. * s - 1.);
+  phi[3] = 4. * r * (1. - r - s);
+  phi[4] = 4. * r * s;
+  phi[5] = 4. * s * (1. - r - s);
+  dr[0] = 4. * (r + s) - 3.; dr[1] = 4. * r - 1.; dr[2] = 0.;
+  dr[3] = 4. * (1. - 2. * r - s); dr[4] = 4. * s; dr[5] = -4. * s;
+  ds[0] = 4. * (r + s) - 3.; ds[1] = 0.; ds[2] = 4. * s - 1.;
+  ds[3] = -4. * r; ds[4] = 4. * r; ds[5] = 4. * (1. - r - 2. * s);
+}
+
+}  // namespace
+
+void build_ref_tensors(const QuadRule &q, RefTensors &T)
+{
+  std::memset(&T, 0, sizeof(T));
+  T.nq = q.n();
+  for(int k = 0; k < q.n(); ++k) {
+    double phi[6], d[2][6];
+    p2_basis(q.r[k], q.s[k], phi, d[0], d[1]);
+    const double psi[3] = {1. - q.r[k] - q.s[k], q.r[k], q.s[k]};
+    const double w = q.w[k];
+    T.qw[k] = w; T.qr[k] = q.r[k]; T.qs[k] = q.s[k];
+    for(int a = 0; a < 6; ++a) T.phi[k][a] = phi[a];
+    for(int r = 0; r < 2; ++r)
+      for(int s = 0; s < 2; ++s)
+        for(int a = 0; a < 6; ++a)
+          for(int b = 0; b < 6; ++b) T.K[r][s][a][b] += w * d[r][a] * d[s][b];
+    for(int r = 0; r < 2; ++r)
+      for(int a = 0; a < 6; ++a)
+        for(int c = 0; c < 6; ++c)
+          for(int b = 0; b < 6; ++b) T.T[r][a][c][b] += w * phi[a] * phi[c] * d[r][b];
+    for(int r = 0; r < 2; ++r)
+      for(int j = 0; j < 3; ++j)
+        for(int a = 0; a < 6; ++a) T.D[r][j][a] += w * psi[j] * d[r][a];
+    for(int a = 0; a < 6; ++a)
+      for(int b = 0; b < 6; ++b) T.M[a][b] += w * phi[a] * phi[b];
+  }
+}
+
+SystemCUDA::~SystemCUDA()
+{
+  cudaFree(dm_.adr); cudaFree(dm_.geo); cudaFree(dm_.xy); cudaFree(dm_.map);
+  cudaFree(dT_); cudaFree(csr_.ia); cudaFree(csr_.ja); cudaFree(csr_.diag);
+  cudaFree(vals64_); cudaFree(vals32_); cudaFree(rhs_); cudaFree(du_); cudaFree(u_);
+  cudaFree(udot_); cudaFree(hist_[1]); cudaFree(hist_[2]); cudaFree(scratch_);
+  if(ev0_) cudaEventDestroy(ev0_);
+  if(ev1_) cudaEventDestroy(ev1_);
+  if(s_) cudaStreamDestroy(s_);
+}
+
+int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
+                     const SystemOptions &o)
+{
+  opt = o;
+  nInc_ = t.nInc;
+  nDofs_ = t.nDofs;
+  nloc_ = t.nloc;
+  const int64_t nE = t.nElm;
+  if(nE <= 0 || !t.adr || !t.elemXY || nInc_ <= 0 || nDofs_ < nInc_) {
+    set_error("invalid system tables");
+    return FE_INVALID_ARG;
+  }
+  if(t.quad.n() < 1 || t.quad.n() > 16) {
+    set_error("quadrature rule with %d nodes is not supported (1..16)", t.quad.n());
+    return FE_INVALID_ARG;
+  }
+  if((t.elemType == ELEM_P2 && nloc_ != 6) || (t.elemType == ELEM_TAYLOR_HOOD && nloc_ != 15) ||
+     (t.elemType != ELEM_P2 && t.elemType != ELEM_TAYLOR_HOOD)) {
+    set_error("element type %d with %d local DOFs is not supported", t.elemType, nloc_);
+    return FE_INVALID_ARG;
+  }
+  for(int64_t i = 0; i < nE * nloc_; ++i)
+    if(t.adr[i] < 0 || t.adr[i] >= nDofs_) {
+      set_error("element DOF %lld out of range", (long long)t.adr[i]);
+      return FE_INVALID_ARG;
+    }
+
+  // Forms -> fused coefficients.
+  fc_ = FormCoeffs();
+  fc_.elemType = t.elemType;
+  for(int i = 0; i < nforms; ++i) {
+    const FormDesc &f = forms[i];
+    const bool vec = t.elemType == ELEM_TAYLOR_HOOD;
+    switch(f.kind) {
+      case FORM_DIFFUSION:
+        if(vec) { set_error("DIFFUSION needs a scalar P2 element"); return FE_INVALID_ARG; }
+        fc_.hasDiff = 1; fc_.diff += f.coeff; break;
+      case FORM_SOURCE:
+      case FORM_VECTOR_SOURCE:
+        if((f.kind == FORM_SOURCE) == vec) { set_error("source kind does not match the element"); return FE_INVALID_ARG; }
+        if(fc_.srcKind != SRC_NONE) { set_error("only one source form is supported"); return FE_INVALID_ARG; }
+        fc_.srcKind = f.source;
+        fc_.srcCoeff = f.coeff == 0 ? 1.0 : f.coeff;
+        for(int k = 0; k < 4; ++k) fc_.srcParam[k] = f.params[k];
+        break;
+      case FORM_VECTOR_CONVECTIVE_ACCELERATION:
+        if(!vec) { set_error("convective form needs a Taylor-Hood element"); return FE_INVALID_ARG; }
+        fc_.hasConv = 1; fc_.conv += f.coeff; break;
+      case FORM_DIV_NEWTONIAN_STRESS:
+        if(!vec || fc_.hasSigma) { set_error("one DIV_NEWTONIAN_STRESS on a Taylor-Hood element"); return FE_INVALID_ARG; }
+        fc_.hasSigma = 1; fc_.sigma = f.coeff; fc_.mu = f.coeff2; break;
+      case FORM_MIXED_DIVERGENCE:
+        if(!vec) { set_error("MIXED_DIVERGENCE needs a Taylor-Hood element"); return FE_INVALID_ARG; }
+        fc_.hasDivu = 1; fc_.divu += f.coeff; break;
+      case FORM_TRANSIENT_VECTOR_MASS:
+        if(!vec) { set_error("TRANSIENT_VECTOR_MASS needs a Taylor-Hood element"); return FE_INVALID_ARG; }
+        fc_.hasMass = 1; fc_.mass += f.coeff; break;
+      default:
+        set_error("unsupported form kind %d", f.kind);
+        return FE_INVALID_ARG;
+    }
+  }
+  if(fc_.srcKind < 0 || fc_.srcKind > SRC_SIN_BODY) { set_error("unknown source kind"); return FE_INVALID_ARG; }
+
+  // Host tables: coloring, pattern, scatter map.
+  Mesh2D tmpMesh;  // only the triangle connectivity is needed for coloring
+  ElementTables et;
+  et.type = t.elemType; et.nloc = nloc_; et.nElm = nE;
+  et.adr.assign(t.adr, t.adr + nE * nloc_);
+  if(t.elemType == ELEM_P2) et.mask.assign(36, 1);
+  else {
+    et.mask.assign(225, 0);
+    for(int i = 0; i < 15; ++i)
+      for(int j = 0; j < 15; ++j) et.mask[i * 15 + j] = (i < 12 || j < 12) ? 1 : 0;
+  }
+  if(t.coloring && !t.coloring->elements.empty()) {
+    col_ = *t.coloring;
+  } else {
+    // Color on the vertex DOFs of the element (first three local functions
+    // of the scalar field / first component of the vector field).
+    tmpMesh.x.assign(nDofs_, 0.); tmpMesh.y.assign(nDofs_, 0.);
+    tmpMesh.tri.resize(nE * 3);
+    const int stride = t.elemType == ELEM_P2 ? 1 : 2;
+    for(int64_t e = 0; e < nE; ++e)
+      for(int k = 0; k < 3; ++k) tmpMesh.tri[3 * e + k] = (int32_t)t.adr[e * nloc_ + k * stride];
+    FE_TRY(color_elements(tmpMesh, col_));
+  }
+  if(col_.nColors > 64 || (int64_t)col_.elements.size() != nE) {
+    set_error("invalid coloring");
+    return FE_BAD_COLORING;
+  }
+  adrHost_.assign(t.adr, t.adr + nE * nloc_);
+  FE_TRY(validateColoring());
+  if(t.pattern && t.pattern->n == nInc_) pat_ = *t.pattern;
+  else FE_TRY(build_csr_pattern(et, nInc_, pat_));
+  std::vector<int32_t> map;
+  FE_TRY(build_scatter_map(et, col_, pat_, nInc_, map));
+
+  // Color-ordered SoA element data.
+  std::vector<int32_t> adrP((size_t)nloc_ * nE);
+  std::vector<double> geo(5 * nE), xy(6 * nE);
+  for(int64_t p = 0; p < nE; ++p) {
+    const int64_t e = col_.elements[p];
+    for(int i = 0; i < nloc_; ++i) adrP[(size_t)i * nE + p] = (int32_t)t.adr[e * nloc_ + i];
+    const double *c = t.elemXY + 6 * e;
+    // P1 geometry: dx/dr = x1-x0, dx/ds = x2-x0 (feCncGeo::computeElementTransformation,
+    // feCncGeo.cpp:651-670)
+    const double dxdr0 = c[2] - c[0], dxdr1 = c[3] - c[1];
+    const double dxds0 = c[4] - c[0], dxds1 = c[5] - c[1];
+    const double jac = dxdr0 * dxds1 - dxdr1 * dxds0;
+    if(!(std::fabs(jac) > 0)) {
+      set_error("element %lld has a zero Jacobian", (long long)e);
+      return FE_INVALID_ARG;
+    }
+    const double drdx0 = dxds1 / jac, drdx1 = -dxdr1 / jac, drdy0 = -dxds0 / jac, drdy1 = dxdr0 / jac;
+    geo[0 * nE + p] = drdx0;  // G[0][0] = dr/dx
+    geo[1 * nE + p] = drdy0;  // G[0][1] = dr/dy
+    geo[2 * nE + p] = drdx1;  // G[1][0] = ds/dx
+    geo[3 * nE + p] = drdy1;  // G[1][1] = ds/dy
+    geo[4 * nE + p] = jac;
+    for(int k = 0; k < 6; ++k) xy[k * nE + p] = c[k];
+  }
+  dm_.nElm = nE;
+  dm_.nloc = nloc_;
+  dm_.nColors = col_.nColors;
+  for(int c = 0; c <= col_.nColors; ++c) dm_.colorOff[c] = col_.offsets[c];
+
+  CK(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&ev0_));
+  CK(cudaEventCreate(&ev1_));
+  CK(cudaMalloc(&dm_.adr, sizeof(int32_t) * adrP.size()));
+  CK(cudaMalloc(&dm_.geo, sizeof(double) * geo.size()));
+  CK(cudaMalloc(&dm_.xy, sizeof(double) * xy.size()));
+  CK(cudaMalloc(&dm_.map, sizeof(int32_t) * map.size()));
+  CK(cudaMemcpy(dm_.adr, adrP.data(), sizeof(int32_t) * adrP.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dm_.geo, geo.data(), sizeof(double) * geo.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dm_.xy, xy.data(), sizeof(double) * xy.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dm_.map, map.data(), sizeof(int32_t) * map.size(), cudaMemcpyHostToDevice));
+
+  RefTensors hT;
+  build_ref_tensors(t.quad, hT);
+  CK(cudaMalloc(&dT_, sizeof(RefTensors)));
+  CK(cudaMemcpy(dT_, &hT, sizeof(RefTensors), cudaMemcpyHostToDevice));
+
+  const int64_t nnz = pat_.nnz();
+  std::vector<int32_t> ia32(nInc_ + 1);
+  for(int64_t i = 0; i <= nInc_; ++i) ia32[i] = (int32_t)pat_.ia[i];
+  csr_.n = nInc_;
+  csr_.nnz = nnz;
+  CK(cudaMalloc(&csr_.ia, sizeof(int32_t) * (nInc_ + 1)));
+  CK(cudaMalloc(&csr_.ja, sizeof(int32_t) * nnz));
+  CK(cudaMalloc(&csr_.diag, sizeof(int32_t) * nInc_));
+  CK(cudaMemcpy(csr_.ia, ia32.data(), sizeof(int32_t) * (nInc_ + 1), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(csr_.ja, pat_.ja.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice));
+  k_diagpos<<<gridFor(nInc_), 256, 0, s_>>>(nInc_, csr_.ia, csr_.ja, csr_.diag);
+  if(opt.precision == 0) CK(cudaMalloc(&vals64_, sizeof(double) * nnz));
+  else CK(cudaMalloc(&vals32_, sizeof(float) * nnz));
+  CK(cudaMalloc(&rhs_, sizeof(double) * nInc_));
+  CK(cudaMalloc(&du_, sizeof(double) * nInc_));
+  CK(cudaMalloc(&u_, sizeof(double) * nDofs_));
+  CK(cudaMalloc(&udot_, sizeof(double) * nDofs_));
+  CK(cudaMemsetAsync(u_, 0, sizeof(double) * nDofs_, s_));
+  CK(cudaMemsetAsync(udot_, 0, sizeof(double) * nDofs_, s_));
+  CK(cudaMemsetAsync(du_, 0, sizeof(double) * nInc_, s_));
+  CK(cudaMemsetAsync(rhs_, 0, sizeof(double) * nInc_, s_));
+
+  KrylovOptions ko = opt.kry;
+  ko.mixed = opt.precision == 1 ? 1 : 0;
+  std::vector<int32_t> blocks;
+  int64_t nbHint = 1;
+  if(ko.precond == 1) {
+    if(t.blockOfRow && (int64_t)t.blockOfRow->size() == nInc_) blocks = *t.blockOfRow;
+    else if(opt.pcBlockRows > 0) nbHint = std::max<int64_t>(1, nInc_ / opt.pcBlockRows);
+  }
+  CK(cudaStreamSynchronize(s_));
+  FE_TRY(kry_.setup(csr_, blocks, nbHint, ko, s_));
+  return FE_OK;
+}
+
+// Rejects a coloring under which two elements of one color share a DOF (the
+// scatter would race).  Run before any launch.
+int SystemCUDA::validateColoring() const
+{
+  const int64_t nE = (int64_t)adrHost_.size() / std::max(nloc_, 1);
+  if((int64_t)col_.elements.size() != nE || (int64_t)col_.offsets.size() != col_.nColors + 1) {
+    set_error("coloring does not list every element");
+    return FE_BAD_COLORING;
+  }
+  std::vector<int32_t> stamp(nDofs_, -1);
+  std::vector<uint8_t> seen(nE, 0);
+  for(int c = 0; c < col_.nColors; ++c)
+    for(int64_t p = col_.offsets[c]; p < col_.offsets[c + 1]; ++p) {
+      const int64_t e = col_.elements[p];
+      if(e < 0 || e >= nE || seen[e]) {
+        set_error("element %lld missing, repeated or out of range in the coloring", (long long)e);
+        return FE_BAD_COLORING;
+      }
+      seen[e] = 1;
+      for(int i = 0; i < nloc_; ++i) {
+        const int64_t d = adrHost_[e * nloc_ + i];
+        if(stamp[d] == c) {
+          set_error("elements of color %d share DOF %lld", c, (long long)d);
+          return FE_BAD_COLORING;
+        }
+        stamp[d] = c;
+      }
+    }
+  return FE_OK;
+}
+
+int SystemCUDA::begin_phase()
+{
+  if(timing) CK(cudaEventRecord(ev0_, s_));
+  return FE_OK;
+}
+
+float SystemCUDA::end_phase()
+{
+  if(!timing) return 0.f;
+  float ms = 0.f;
+  cudaEventRecord(ev1_, s_);
+  cudaEventSynchronize(ev1_);
+  cudaEventElapsedTime(&ms, ev0_, ev1_);
+  return ms;
+}
+
+int SystemCUDA::setToZero()
+{
+  FE_TRY(setMatrixToZero());
+  return setResidualToZero();
+}
+
+int SystemCUDA::setMatrixToZero()
+{
+  if(vals64_) CK(cudaMemsetAsync(vals64_, 0, sizeof(double) * pat_.nnz(), s_));
+  if(vals32_) CK(cudaMemsetAsync(vals32_, 0, sizeof(float) * pat_.nnz(), s_));
+  matrixValid_ = false;
+  return FE_OK;
+}
+
+int SystemCUDA::setResidualToZero()
+{
+  CK(cudaMemsetAsync(rhs_, 0, sizeof(double) * nInc_, s_));
+  return FE_OK;
+}
+
+int SystemCUDA::assembleResiduals()
+{
+  begin_phase();
+  for(int c = 0; c < dm_.nColors; ++c)
+    launch_assemble_residual(dm_, fc_, dT_, u_, udot_, t_, nInc_, rhs_, dm_.colorOff[c],
+                             dm_.colorOff[c + 1], s_);
+  CK(cudaGetLastError());
+  times.residual_ms += end_phase();
+  times.residual_calls++;
+  return FE_OK;
+}
+
+int SystemCUDA::assembleMatrices()
+{
+  begin_phase();
+  for(int c = 0; c < dm_.nColors; ++c) {
+    if(vals64_)
+      launch_assemble_matrix_f64(dm_, fc_, dT_, u_, c0_, vals64_, dm_.colorOff[c],
+                                 dm_.colorOff[c + 1], s_);
+    else
+      launch_assemble_matrix_f32(dm_, fc_, dT_, u_, c0_, vals32_, dm_.colorOff[c],
+                                 dm_.colorOff[c + 1], s_);
+  }
+  CK(cudaGetLastError());
+  times.matrix_ms += end_phase();
+  times.matrix_calls++;
+  matrixValid_ = true;
+  begin_phase();
+  int s = kry_.factor(vals64_, vals32_);
+  times.factor_ms += end_phase();
+  return s;
+}
+
+int SystemCUDA::getRHSMaxNorm(double *norm)
+{
+  *norm = kry_.norminf(rhs_);
+  if(!std::isfinite(*norm)) {
+    set_error("non-finite residual");
+    return FE_NONFINITE;
+  }
+  return FE_OK;
+}
+
+int SystemCUDA::solve(double *normDx, double *normRHS, double *normAxb, int *nIter)
+{
+  begin_phase();
+  KrylovStats st;
+  int s = kry_.solve(vals64_, vals32_, rhs_, du_, st);
+  times.solve_ms += end_phase();
+  times.solve_calls++;
+  lastSolve = st;
+  if(nIter) *nIter = st.iterations;
+  if(normDx) *normDx = kry_.norminf(du_);
+  if(normRHS) *normRHS = kry_.norminf(rhs_);
+  if(normAxb) *normAxb = st.rnorm;
+  return s;
+}
+
+int SystemCUDA::correctSolution()
+{
+  k_add<<<gridFor(nInc_), 256, 0, s_>>>(nInc_, du_, u_);
+  CK(cudaGetLastError());
+  return FE_OK;
+}
+
+int SystemCUDA::setSolution(const double *hostU, const double *hostUdot)
+{
+  if(hostU) CK(cudaMemcpyAsync(u_, hostU, sizeof(double) * nDofs_, cudaMemcpyHostToDevice, s_));
+  if(hostUdot)
+    CK(cudaMemcpyAsync(udot_, hostUdot, sizeof(double) * nDofs_, cudaMemcpyHostToDevice, s_));
+  CK(cudaStreamSynchronize(s_));
+  return FE_OK;
+}
+
+int SystemCUDA::getSolution(double *hostU) const
+{
+  CK(cudaMemcpyAsync(hostU, u_, sizeof(double) * nDofs_, cudaMemcpyDeviceToHost, s_));
+  CK(cudaStreamSynchronize(s_));
+  return FE_OK;
+}
+
+int SystemCUDA::getSolutionDot(double *hostUdot) const
+{
+  CK(cudaMemcpyAsync(hostUdot, udot_, sizeof(double) * nDofs_, cudaMemcpyDeviceToHost, s_));
+  CK(cudaStreamSynchronize(s_));
+  return FE_OK;
+}
+
+int SystemCUDA::setBDF(int order, const double *cn, const double *const *hostHist)
+{
+  if(order < 0 || order > 2) {
+    set_error("BDF order %d not supported", order);
+    return FE_INVALID_ARG;
+  }
+  bdfOrder_ = order;
+  for(int k = 0; k < 3; ++k) cn_[k] = k <= order ? cn[k] : 0.;
+  for(int k = 1; k <= order; ++k) {
+    if(!hist_[k]) CK(cudaMalloc(&hist_[k], sizeof(double) * nDofs_));
+    if(hostHist && hostHist[k])
+      CK(cudaMemcpyAsync(hist_[k], hostHist[k], sizeof(double) * nDofs_, cudaMemcpyHostToDevice, s_));
+  }
+  c0_ = cn_[0];
+  CK(cudaStreamSynchronize(s_));
+  return FE_OK;
+}
+
+int SystemCUDA::computeSolDot()
+{
+  k_soldot<<<gridFor(nDofs_), 256, 0, s_>>>(nDofs_, bdfOrder_, cn_[0], cn_[1], cn_[2], u_, hist_[1],
+                                             hist_[2], udot_);
+  CK(cudaGetLastError());
+  return FE_OK;
+}
+
+int SystemCUDA::getMatrix(double *hostValues) const
+{
+  const int64_t nnz = pat_.nnz();
+  if(vals64_) {
+    CK(cudaMemcpyAsync(hostValues, vals64_, sizeof(double) * nnz, cudaMemcpyDeviceToHost, s_));
+    CK(cudaStreamSynchronize(s_));
+  } else {
+    std::vector<float> tmp(nnz);
+    CK(cudaMemcpyAsync(tmp.data(), vals32_, sizeof(float) * nnz, cudaMemcpyDeviceToHost, s_));
+    CK(cudaStreamSynchronize(s_));
+    for(int64_t i = 0; i < nnz; ++i) hostValues[i] = tmp[i];
+  }
+  return FE_OK;
+}
+
+int SystemCUDA::getRHS(double *hostRhs) const
+{
+  CK(cudaMemcpyAsync(hostRhs, rhs_, sizeof(double) * nInc_, cudaMemcpyDeviceToHost, s_));
+  CK(cudaStreamSynchronize(s_));
+  return FE_OK;
+}
+
+int SystemCUDA::getDu(double *hostDu) const
+{
+  CK(cudaMemcpyAsync(hostDu, du_, sizeof(double) * nInc_, cudaMemcpyDeviceToHost, s_));
+  CK(cudaStreamSynchronize(s_));
+  return FE_OK;
+}
+
+// Newton-Raphson, restating solveNewtonRaphson (feNonLinearSolver.cpp:38-181)
+// on device-resident data: max-norm tests, Jacobian-reuse heuristic
+// (feNonLinearSolver.cpp:12-31); divergence and failure return a status
+// instead of exiting.
+int newton_solve(SystemCUDA &sys, const NewtonOptions &o, NewtonStats &st)
+{
+  st = NewtonStats();
+  bool recompute = true;
+  int iter = 0;
+  double normResidual = 0, normCorrection = 0, normAxb = 0, previous = 1e22;
+  const double baseRtol = sys.krylov().opt.rtol;
+  while(true) {
+    if(!o.stationary) FE_TRY(sys.computeSolDot());
+    FE_TRY(sys.setToZero());
+    FE_TRY(sys.assembleResiduals());
+    FE_TRY(sys.getRHSMaxNorm(&normResidual));
+    if(iter == 0) st.residual0 = normResidual;
+    st.residual = normResidual;
+    if(iter > 0 && normResidual <= o.tolResidual) break;
+    if(iter > 0 && o.relResidual > 0 && normResidual <= o.relResidual * st.residual0) break;
+    if(iter == 0 && normResidual == 0.0) break;
+    if(recompute) {
+      FE_TRY(sys.assembleMatrices());
+      st.matrixAssemblies++;
+    }
+    if(o.linearRtolMin > 0 && st.residual0 > 0) {
+      // Inexact Newton: solve only as far as the nonlinear residual warrants.
+      const double ratio = normResidual / st.residual0;
+      sys.krylov().opt.rtol = std::max(o.linearRtolMin, std::min(1e-2, 0.1 * ratio));
+    }
+    int nIt = 0;
+    int s = sys.solve(&normCorrection, nullptr, &normAxb, &nIt);
+    sys.krylov().opt.rtol = baseRtol;
+    st.krylovIterations += nIt;
+    if(s != FE_OK && s != FE_NOT_CONVERGED) { st.status = s; return s; }
+    if(s == FE_NOT_CONVERGED && o.linearRtolMin <= 0) { st.status = s; return s; }
+    if(normResidual > o.tolDivergence) {
+      set_error("residual norm %g above divergence tolerance %g", normResidual, o.tolDivergence);
+      st.status = FE_NOT_CONVERGED;
+      return FE_NOT_CONVERGED;
+    }
+    FE_TRY(sys.correctSolution());
+    ++iter;
+    st.iterations = iter;
+    st.correction = normCorrection;
+    // recomputeMatrixHeuristic
+    if(o.stationary) recompute = true;
+    else recompute = (iter % o.recomputeEvery == 0) || (normResidual > o.residualDecrease * previous);
+    previous = normResidual;
+    bool stop = normResidual <= o.tolResidual || normCorrection <= o.tolCorrection || iter > o.maxIter;
+    if(stop) break;
+  }
+  st.converged = (st.residual <= o.tolResidual) || (o.relResidual > 0 && st.residual <= o.relResidual * st.residual0) ||
+                 (st.correction <= o.tolCorrection) || st.residual0 == 0.0;
+  st.status = st.converged ? FE_OK : FE_NOT_CONVERGED;
+  return st.status;
+}
+
+}  // namespace feng

@@ -1,0 +1,158 @@
+// The CUDA linear-system backend: device-resident matrix, right-hand side,
+// solution and the operations of feNG's feLinearSystem interface
+// (src/feLinearSystem.h:43-169), plus the Newton driver that calls them
+// (solveNewtonRaphson, src/feNonLinearSolver.cpp:38-181) and the BDF time
+// derivative (BDFContainer, src/feSolutionContainer.cpp:82-101, 338-349).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+#include "fe_device.h"
+#include "fe_krylov.h"
+#include "fe_setup.h"
+
+namespace feng {
+
+struct FormDesc {
+  int kind;          // FormKind
+  double coeff;      // constant coefficient
+  double coeff2;     // second coefficient (viscosity of DIV_NEWTONIAN_STRESS)
+  int source;        // SourceKind for SOURCE / VECTOR_SOURCE
+  double params[4];  // source parameters
+};
+
+struct SystemOptions {
+  KrylovOptions kry;
+  int pcBlockRows = 256;   // target rows per block-Jacobi block (0: a single block)
+  int precision = 0;       // 0 FP64 matrix, 1 FP32 matrix + mixed Krylov
+};
+
+// Everything the backend needs from the set-up, in the original element order.
+struct SystemTables {
+  int elemType = 0;
+  int64_t nElm = 0;
+  int nloc = 0;
+  int64_t nInc = 0, nDofs = 0;
+  const int64_t *adr = nullptr;       // [nElm*nloc]
+  const double *elemXY = nullptr;     // [nElm*6] x0 y0 x1 y1 x2 y2
+  // optional (computed when null/empty):
+  const Coloring *coloring = nullptr;
+  const CSRPattern *pattern = nullptr;
+  const std::vector<int32_t> *blockOfRow = nullptr;  // block-Jacobi partition of unknowns
+  QuadRule quad;
+};
+
+struct PhaseTimes {
+  double residual_ms = 0, matrix_ms = 0, factor_ms = 0, solve_ms = 0, other_ms = 0;
+  int residual_calls = 0, matrix_calls = 0, solve_calls = 0;
+};
+
+class SystemCUDA {
+ public:
+  ~SystemCUDA();
+  int init(const SystemTables &t, const FormDesc *forms, int nforms, const SystemOptions &opt);
+
+  // feLinearSystem operations
+  int setToZero();
+  int setMatrixToZero();
+  int setResidualToZero();
+  int assembleResiduals();
+  int assembleMatrices();
+  int getRHSMaxNorm(double *norm);
+  int solve(double *normDx, double *normRHS, double *normAxb, int *nIter);
+  int correctSolution();
+
+  // Solution state (device), time and BDF coefficient c0.
+  int setSolution(const double *hostU, const double *hostUdot);
+  int getSolution(double *hostU) const;
+  int getSolutionDot(double *hostUdot) const;
+  void setTime(double t, double c0)
+  {
+    t_ = t;
+    c0_ = c0;
+  }
+  // BDF history: hist[k] = u^{n+1-k}; udot = sum_k cn[k] hist[k] with hist[0] = u.
+  int setBDF(int order, const double *cn, const double *const *hostHist);
+  int computeSolDot();
+
+  int64_t nInc() const { return nInc_; }
+  int64_t nDofs() const { return nDofs_; }
+  int64_t nnz() const { return pat_.nnz(); }
+  int64_t nElm() const { return dm_.nElm; }
+  int nColors() const { return dm_.nColors; }
+  const CSRPattern &pattern() const { return pat_; }
+  const Coloring &coloring() const { return col_; }
+  int getMatrix(double *hostValues) const;  // FP64 copy of the current values
+  int getRHS(double *hostRhs) const;
+  int getDu(double *hostDu) const;
+  int validateColoring() const;
+
+  double *dU() { return u_; }
+  double *dUdot() { return udot_; }
+  double *dRhs() { return rhs_; }
+  double *dDu() { return du_; }
+  cudaStream_t stream() const { return s_; }
+  Krylov &krylov() { return kry_; }
+  PhaseTimes times;
+  KrylovStats lastSolve;
+  SystemOptions opt;
+  int timing = 1;  // record CUDA events around the phases
+
+ private:
+  int64_t nInc_ = 0, nDofs_ = 0;
+  int nloc_ = 0;
+  double t_ = 0, c0_ = 0;
+  Coloring col_;
+  CSRPattern pat_;
+  std::vector<int64_t> adrHost_;      // element table, original element order
+  DeviceMesh dm_;
+  FormCoeffs fc_{};
+  RefTensors *dT_ = nullptr;
+  DeviceCSR csr_;
+  double *vals64_ = nullptr;
+  float *vals32_ = nullptr;
+  double *rhs_ = nullptr, *du_ = nullptr, *u_ = nullptr, *udot_ = nullptr;
+  double *hist_[3] = {nullptr, nullptr, nullptr};
+  double cn_[3] = {0, 0, 0};
+  int bdfOrder_ = 0;
+  double *scratch_ = nullptr;
+  Krylov kry_;
+  cudaStream_t s_ = nullptr;
+  cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+  bool hostTmp_ = false;
+  bool matrixValid_ = false;
+  int begin_phase();
+  float end_phase();
+};
+
+// Reference-element tensors of a quadrature rule (host, FP64).
+void build_ref_tensors(const QuadRule &q, RefTensors &T);
+
+struct NewtonOptions {
+  double tolResidual = 1e-10;     // feNLSolverOptions (feNonLinearSolver.h:12-40)
+  double tolCorrection = 1e-10;
+  double tolDivergence = 1e4;
+  int maxIter = 20;
+  int recomputeEvery = 3;
+  double residualDecrease = 0.1;
+  int stationary = 1;
+  double relResidual = 0.0;       // extra stop: ||R||inf <= relResidual * ||R0||inf (0: off)
+  double linearRtolMin = 0.0;     // >0: adaptive linear tolerance max(min, 0.1*||R||/||R0||)
+};
+
+struct NewtonStats {
+  int iterations = 0;
+  int krylovIterations = 0;
+  int matrixAssemblies = 0;
+  double residual0 = 0, residual = 0, correction = 0;
+  int status = 0;
+  int converged = 0;
+};
+
+int newton_solve(SystemCUDA &sys, const NewtonOptions &o, NewtonStats &st);
+
+}  // namespace feng

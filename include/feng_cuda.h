@@ -1,0 +1,242 @@
+/*
+ * feng_cuda.h -- C ABI of the GB300 (sm_103a) backend for feNG's element
+ * assembly + Krylov solve hot path.
+ *
+ * Plain C types only: caller-owned host arrays in, opaque handles out, every
+ * function returns an int status (0 = OK, < 0 = error, mirroring feStatus in
+ * feNG's src/feMessage.h:44-62).  fe_cuda_last_error() gives the message of
+ * the last failure on the calling thread.  Handles are not thread-safe.
+ *
+ * Two ways in:
+ *  1. The drop-in route.  A feLinearSystemCUDA subclass of feNG's
+ *     feLinearSystem (src/feLinearSystem.h:43-169) flattens its
+ *     feBilinearForm list into fe_form_desc, its element addressing into an
+ *     element-to-DOF table, and passes feNG's own CSR pattern and coloring:
+ *     fe_cuda_system_create_from_tables().
+ *  2. The standalone route.  The library builds mesh, numbering, pattern and
+ *     coloring itself with the same algorithms (fe_mesh_*, fe_cuda_system_create).
+ * Either way the per-Newton-iteration calls are the feLinearSystem
+ * operations below.
+ */
+#ifndef FENG_CUDA_H
+#define FENG_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes: feStatus FE_STATUS_OK / FE_STATUS_ERROR and refinements */
+#define FE_CUDA_OK 0
+#define FE_CUDA_ERROR (-1)
+#define FE_CUDA_READ_ERROR (-2)
+#define FE_CUDA_INVALID_ARG (-3)
+#define FE_CUDA_DEVICE_FAIL (-4)
+#define FE_CUDA_NOT_CONVERGED (-5)
+#define FE_CUDA_PC_FAILED (-6)
+#define FE_CUDA_NONFINITE (-7)
+#define FE_CUDA_BAD_COLORING (-8)
+
+/* ---- weak forms (feSysElm elementSystemType, src/feSysElm.h:13-77) */
+#define FE_FORM_SOURCE 1
+#define FE_FORM_DIFFUSION 2
+#define FE_FORM_VECTOR_SOURCE 3
+#define FE_FORM_TRANSIENT_VECTOR_MASS 4
+#define FE_FORM_MIXED_DIVERGENCE 5
+#define FE_FORM_VECTOR_CONVECTIVE_ACCELERATION 6
+#define FE_FORM_DIV_NEWTONIAN_STRESS 7
+
+/* ---- device-evaluated source functions (feFunction callbacks cannot run on
+ * the device; src/feFunction.h:44-56) */
+#define FE_SRC_NONE 0
+#define FE_SRC_SIN_SIN 1      /* p0 sin(pi x) sin(pi y)                         */
+#define FE_SRC_NS_MMS_POLY 2  /* NS manufactured source, tests/withLinearSolver/navier_stokes.cpp:33-51 */
+#define FE_SRC_CONST_VEC 3    /* (p0, p1)                                        */
+#define FE_SRC_SIN_BODY 4     /* (p0 sin(pi x) sin(pi y), 0)                     */
+
+/* ---- element types of the fused kernels */
+#define FE_ELEM_P2 1            /* scalar Lagrange P2 triangle, 6 local DOFs          */
+#define FE_ELEM_TAYLOR_HOOD 2   /* vector P2 (interleaved x,y) + P1, 12 + 3 local DOFs */
+
+/* ---- connectivities a space lives on (feMesh physical names) */
+#define FE_CNC_DOMAIN 0    /* "Domaine"       */
+#define FE_CNC_BOUNDARY 1  /* "Bord"          */
+#define FE_CNC_POINT 2     /* "PointPression" */
+
+typedef struct fe_mesh fe_mesh;
+typedef struct fe_cuda_system fe_cuda_system;
+
+/* One bilinear/linear form: createBilinearForm(spaces, new feSysElm_*(coeffs)),
+ * src/feBilinearForm.cpp:6-73.  Coefficients are constants
+ * (feConstantFunction, src/feFunction.h:113-118). */
+typedef struct fe_form_desc {
+  int32_t kind;       /* FE_FORM_* */
+  double coeff;       /* scalar coefficient */
+  double coeff2;      /* viscosity of FE_FORM_DIV_NEWTONIAN_STRESS */
+  int32_t source;     /* FE_SRC_* for the source forms */
+  double params[4];   /* source parameters */
+} fe_form_desc;
+
+/* One FE space: createFiniteElementSpace(..., LAGRANGE/VECTOR_LAGRANGE, degree,
+ * field, cnc), src/feSpace.cpp:11-420; essential = listed in essentialSpaces
+ * of feMetaNumber, src/feNumber.cpp:677. */
+typedef struct fe_space_desc {
+  int32_t field;      /* field index, in order of first appearance */
+  int32_t degree;     /* 0 (point), 1, 2 */
+  int32_t ncomp;      /* 1 or 2 */
+  int32_t cnc;        /* FE_CNC_* */
+  int32_t essential;  /* 0 / 1 */
+} fe_space_desc;
+
+/* Linear solver options (feLinearSystem tolerances, src/feLinearSystem.h:66-69;
+ * KSP/PC choice of the PETSc backend, src/feLinearSystemPETSc.cpp:337-352). */
+typedef struct fe_cuda_options {
+  int32_t krylov;         /* 0 CG, 1 FGMRES */
+  int32_t restart;        /* FGMRES restart length (<= 128) */
+  int32_t max_iter;
+  double rel_tol;         /* ||b - A x||_2 <= max(rel_tol ||b||_2, abs_tol) */
+  double abs_tol;
+  double div_tol;
+  int32_t precond;        /* 0 none, 1 block-Jacobi ILU(0), 2 Jacobi */
+  int32_t pc_block_rows;  /* target rows per block-Jacobi block; 0 = one block (plain ILU(0)) */
+  int32_t precision;      /* 0 FP64; 1 FP32 matrix, SpMV, preconditioner inside FP64 refinement */
+  int32_t quad_degree;    /* triangle rule degree: 1, 2, 4, 5, 8 */
+} fe_cuda_options;
+
+/* Newton options (feNLSolverOptions, src/feNonLinearSolver.h:12-40) plus the
+ * relative stop ||R||inf <= rel_residual ||R0||inf used for benchmarking. */
+typedef struct fe_newton_options {
+  double tol_residual;
+  double tol_correction;
+  double tol_divergence;
+  int32_t max_iter;
+  int32_t recompute_every;
+  double residual_decrease;
+  int32_t stationary;
+  double rel_residual;
+  double linear_rtol_min;   /* > 0: inexact Newton, linear rtol = max(this, 0.1 ||R||/||R0||) */
+} fe_newton_options;
+
+typedef struct fe_newton_stats {
+  int32_t iterations;
+  int32_t krylov_iterations;
+  int32_t matrix_assemblies;
+  int32_t status;
+  double residual0;
+  double residual;
+  double correction;
+  double residual_ms;  /* device time of the phases, CUDA events */
+  double matrix_ms;
+  double factor_ms;
+  double solve_ms;
+} fe_newton_stats;
+
+/* ---- library */
+const char *fe_cuda_last_error(void);
+int fe_cuda_version(void);
+int fe_cuda_device_count(int *count);
+
+/* ---- mesh (feMesh2DP1, src/feMesh.h:357-497; reader src/feMeshRead.cpp:645) */
+int fe_mesh_generate_square(int n, double x0, double x1, double y0, double y1, double jitter,
+                            uint64_t seed, fe_mesh **out);
+int fe_mesh_read_msh(const char *path, fe_mesh **out);
+int fe_mesh_write_msh(const fe_mesh *m, const char *path);
+int fe_mesh_sizes(const fe_mesh *m, int64_t *n_vertices, int64_t *n_triangles, int64_t *n_edges,
+                  int64_t *n_boundary);
+/* Any output may be NULL.  x,y [nv]; tri [3 nt]; tri_edges [3 nt]; bnd [2 nb]; point [1]. */
+int fe_mesh_arrays(const fe_mesh *m, double *x, double *y, int32_t *tri, int32_t *tri_edges,
+                   int32_t *bnd, int32_t *point);
+void fe_mesh_destroy(fe_mesh *m);
+
+/* ---- host set-up of the standalone route (no device needed):
+ * DOF numbering (feMetaNumber, src/feNumber.cpp:677-835), element-to-DOF
+ * tables of elem_type (the P2 space on "Domaine" is the scalar / velocity
+ * field, the P1 space on "Domaine" the pressure), element coloring
+ * (feCncGeo::colorElements(1), src/feCncGeo.cpp:735), CSR pattern
+ * (feEZCompressedRowStorage, src/feCompressedRowStorage.cpp:15-135),
+ * quadrature rule (getGQTPts, src/feQuadratureTri.cpp:874) and a
+ * block-Jacobi partition with about pc_block_rows unknowns per block. */
+typedef struct fe_setup fe_setup;
+int fe_setup_create(const fe_mesh *m, const fe_space_desc *spaces, int nspaces, int elem_type,
+                    int quad_degree, int pc_block_rows, fe_setup **out);
+void fe_setup_destroy(fe_setup *s);
+int fe_setup_sizes(const fe_setup *s, int64_t *n_inc, int64_t *n_dofs, int64_t *nnz,
+                   int64_t *n_elm, int *n_colors, int *nloc);
+/* Outputs may be NULL.  ia [n_inc+1], ja [nnz]. */
+int fe_setup_get_pattern(const fe_setup *s, int64_t *ia, int32_t *ja);
+/* offsets [n_colors+1], elements [n_elm]. */
+int fe_setup_get_coloring(const fe_setup *s, int64_t *offsets, int32_t *elements);
+/* adr [n_elm*nloc], original element order. */
+int fe_setup_get_element_dofs(const fe_setup *s, int64_t *adr);
+/* DOF locations: x, y, field, component, is_vertex [n_dofs]. */
+int fe_setup_get_dof_info(const fe_setup *s, double *x, double *y, int32_t *field, int32_t *comp,
+                          int32_t *is_vertex);
+/* block_of_row [n_inc]. */
+int fe_setup_get_blocks(const fe_setup *s, int32_t *block_of_row);
+/* Quadrature rule: n points (<= 16), r, s, w [n]. */
+int fe_quadrature_rule(int degree, int *n, double *r, double *s, double *w);
+
+/* ---- system creation */
+/* Standalone route: device system from a host set-up. */
+int fe_cuda_system_create(const fe_setup *setup, const fe_form_desc *forms, int nforms,
+                          const fe_cuda_options *opt, fe_cuda_system **out);
+/* Drop-in route: the caller's tables.  adr [n_elm * nloc] global DOFs per
+ * element in the fused layout; elem_xy [n_elm * 6] vertex coordinates;
+ * color_offsets [n_colors+1] / color_elements [n_elm] (may be NULL);
+ * ia [n_inc+1] / ja [nnz] the caller's pattern (may be NULL);
+ * block_of_row [n_inc] block-Jacobi partition (may be NULL). */
+int fe_cuda_system_create_from_tables(int elem_type, int64_t n_elm, const int64_t *adr,
+                                      const double *elem_xy, int64_t n_inc, int64_t n_dofs,
+                                      int n_colors, const int64_t *color_offsets,
+                                      const int32_t *color_elements, const int64_t *ia,
+                                      const int32_t *ja, const int32_t *block_of_row,
+                                      const fe_form_desc *forms, int nforms,
+                                      const fe_cuda_options *opt, fe_cuda_system **out);
+void fe_cuda_system_destroy(fe_cuda_system *s);
+
+int fe_cuda_system_sizes(const fe_cuda_system *s, int64_t *n_inc, int64_t *n_dofs, int64_t *nnz,
+                         int64_t *n_elm, int *n_colors);
+int fe_cuda_get_pattern(const fe_cuda_system *s, int64_t *ia, int32_t *ja);
+int fe_cuda_get_coloring(const fe_cuda_system *s, int64_t *offsets, int32_t *elements);
+/* Rejects a coloring in which two elements of one color share a vertex DOF. */
+int fe_cuda_validate_coloring(const fe_cuda_system *s);
+
+/* ---- state (feSolution: _sol / _dsoldt, src/feSolution.h) */
+int fe_cuda_set_solution(fe_cuda_system *s, const double *u, const double *udot);
+int fe_cuda_get_solution(const fe_cuda_system *s, double *u);
+int fe_cuda_set_time(fe_cuda_system *s, double t, double c0);
+/* BDF history for the time derivative (BDFContainer, src/feSolutionContainer.cpp:82-101,338-349):
+ * udot = cn[0] u + cn[1] hist1 + cn[2] hist2.  hist1/hist2 may be NULL to keep the device copy. */
+int fe_cuda_set_bdf(fe_cuda_system *s, int order, const double *cn, const double *hist1,
+                    const double *hist2);
+int fe_cuda_compute_soldot(fe_cuda_system *s);
+
+/* ---- feLinearSystem operations (src/feLinearSystem.h:96-145) */
+int fe_cuda_set_to_zero(fe_cuda_system *s);
+int fe_cuda_set_matrix_to_zero(fe_cuda_system *s);
+int fe_cuda_set_residual_to_zero(fe_cuda_system *s);
+int fe_cuda_assemble_residuals(fe_cuda_system *s);
+int fe_cuda_assemble_matrices(fe_cuda_system *s);
+int fe_cuda_get_rhs_max_norm(fe_cuda_system *s, double *norm);
+/* Returns FE_CUDA_OK when converged (solve() -> true). */
+int fe_cuda_solve(fe_cuda_system *s, double *norm_dx, double *norm_rhs, double *norm_axb,
+                  int *n_iter);
+int fe_cuda_correct_solution(fe_cuda_system *s);
+int fe_cuda_get_matrix(const fe_cuda_system *s, double *values);
+int fe_cuda_get_rhs(const fe_cuda_system *s, double *rhs);
+int fe_cuda_get_du(const fe_cuda_system *s, double *du);
+
+/* ---- Newton driver (solveNewtonRaphson, src/feNonLinearSolver.cpp:38-181) */
+int fe_cuda_newton(fe_cuda_system *s, const fe_newton_options *o, fe_newton_stats *st);
+/* Phase timers since creation or the last reset. */
+int fe_cuda_get_times(const fe_cuda_system *s, double *residual_ms, double *matrix_ms,
+                      double *factor_ms, double *solve_ms);
+int fe_cuda_reset_times(fe_cuda_system *s);
+int fe_cuda_synchronize(fe_cuda_system *s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FENG_CUDA_H */
