@@ -38,13 +38,15 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int32_t *__restri
   if(done && *done) return;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
   const int sub = threadIdx.x % LANES;
-  if(row >= n) return;
-  const int32_t beg = ia[row], end = ia[row + 1];
+  // Rows past n keep their lanes alive (zero work) so the shuffles below
+  // always run with the full warp.
+  const bool live = row < n;
+  const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
   ACC acc = 0;
   for(int32_t k = beg + sub; k < end; k += LANES) acc += (ACC)a[k] * (ACC)x[ja[k]];
 #pragma unroll
   for(int o = LANES / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, LANES);
-  if(sub == 0) {
+  if(live && sub == 0) {
     if(RESID) y[row] = (VY)(b[row] - (double)acc);
     else y[row] = (VY)acc;
   }

@@ -1,0 +1,32 @@
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+GOLDEN = ROOT / "tests" / "golden"
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
+
+
+@pytest.fixture(scope="session", autouse=True)
+def built_library():
+    """Builds the in-tree CUDA library once (nvcc cross-compiles without a GPU)."""
+    from feng_gb300 import build
+    build.build()
+    return build.LIB
+
+
+def load_golden(name):
+    with np.load(GOLDEN / f"{name}.npz") as z:
+        return {k: z[k] for k in z.files}
+
+
+def golden_names():
+    return sorted(p.stem for p in GOLDEN.glob("*.npz"))

@@ -1,0 +1,75 @@
+"""Host set-up against the reference library's own outputs (golden fixtures
+made by tests/golden/make_golden.py): mesh generator determinism, DOF
+numbering / element tables, coloring and CSR pattern bit-exact, quadrature
+rules to rounding."""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from helpers import golden_mesh, problem_spaces
+from feng_gb300.api import quadrature_rule
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_mesh_generator_reproduces_fixture(name):
+    g = load_golden(name)
+    a = golden_mesh(g).arrays()
+    assert np.array_equal(a["tri"], g["tri"])
+    assert np.array_equal(a["bnd"], g["bnd"])
+    np.testing.assert_allclose(a["x"], g["x"], rtol=0, atol=1e-15)
+    np.testing.assert_allclose(a["y"], g["y"], rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_numbering_pattern_coloring_bit_exact(name):
+    g = load_golden(name)
+    num, _ = problem_spaces(str(g["problem"]), golden_mesh(g), float(g["re"]))
+    st = num.setup()
+    assert (num.nInc, num.nDofs) == (int(g["nInc"]), int(g["nDofs"]))
+    assert np.array_equal(st.elementDofs().ravel(), g["adr"])
+    ia, ja = st.pattern()
+    assert np.array_equal(ia, g["ia"]) and np.array_equal(ja, g["ja"])
+    off, el = st.coloring()
+    assert np.array_equal(off, g["color_offsets"]) and np.array_equal(el, g["color_elements"])
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_quadrature_matches_reference_rule(name):
+    g = load_golden(name)
+    r, s, w = quadrature_rule(int(g["quad_degree"]))
+    np.testing.assert_allclose(np.stack([r, s, w], 1), g["quad"], rtol=0, atol=4e-16)
+
+
+@pytest.mark.parametrize("deg", [1, 2, 4, 5, 8])
+def test_quadrature_exactness(deg):
+    from math import factorial
+    r, s, w = quadrature_rule(deg)
+    for i in range(deg + 1):
+        for j in range(deg + 1 - i):
+            exact = factorial(i) * factorial(j) / factorial(i + j + 2)
+            assert abs(np.sum(w * r**i * s**j) - exact) < 1e-15
+
+
+def test_coloring_is_vertex_disjoint_and_reference_sized():
+    import feng_gb300 as fe
+    m = fe.Mesh2DP1.generate_square(64, jitter=0.1, seed=1)
+    num, _ = problem_spaces("diffusion", m)
+    st = num.setup()
+    off, el = st.coloring()
+    tri = m.arrays()["tri"]
+    assert st.nColors == 7  # as the reference finds on jittered structured meshes
+    for c in range(st.nColors):
+        v = tri[el[off[c]:off[c + 1]]].ravel()
+        assert len(np.unique(v)) == len(v)
+    assert sorted(el.tolist()) == list(range(len(tri)))
+
+
+def test_true_problem_sizes():
+    """DOF counts of the 2D configurations (P2: (2n+1)^2 nodes)."""
+    import feng_gb300 as fe
+    m = fe.Mesh2DP1.generate_square(64, jitter=0.1, seed=1)
+    num, _ = problem_spaces("diffusion", m)
+    assert num.nDofs == 16641
+    m = fe.Mesh2DP1.generate_square(32, -0.5, 1.5, -0.5, 1.5, jitter=0.1, seed=1)
+    num, _ = problem_spaces("ns_kovasznay", m)
+    assert num.nDofs == 2 * 65 * 65 + 33 * 33
