@@ -241,6 +241,25 @@ int fe_setup_create(const fe_mesh *m, const fe_space_desc *spaces, int nspaces, 
   }
   S->blockOfRow.resize(nInc);
   for(int64_t i = 0; i < nInc; ++i) S->blockOfRow[i] = (int32_t)((key[i] * nb) / nv);
+  // Saddle-point rows (the pressure field, whose diagonal no form fills)
+  // get a nonzero ILU(0) pivot only through eliminated velocity unknowns of
+  // the same block.  A pressure row with no velocity unknown in its block
+  // (next to essential velocities at a block border) joins the block of its
+  // first coupled velocity unknown.
+  if(elem_type == ELEM_TAYLOR_HOOD && nb > 1) {
+    for(int64_t i = 0; i < nInc; ++i) {
+      if(S->num.dof_field[i] != fieldP) continue;
+      int64_t firstU = -1;
+      bool inBlock = false;
+      for(int64_t k = S->pat.ia[i]; k < S->pat.ia[i + 1]; ++k) {
+        const int32_t j = S->pat.ja[k];
+        if(S->num.dof_field[j] != fieldU) continue;
+        if(firstU < 0) firstU = j;
+        if(S->blockOfRow[j] == S->blockOfRow[i]) { inBlock = true; break; }
+      }
+      if(!inBlock && firstU >= 0) S->blockOfRow[i] = S->blockOfRow[firstU];
+    }
+  }
   S->elemXY.resize(M.n_triangles() * 6);
   for(int64_t t = 0; t < M.n_triangles(); ++t)
     for(int k = 0; k < 3; ++k) {

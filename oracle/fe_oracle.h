@@ -1,0 +1,91 @@
+/* CPU oracle for the assembly + Krylov hot path.  TEST INFRASTRUCTURE ONLY:
+ * the parity tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+ * use it as the checker; the product never calls it.
+ *
+ * It restates, in plain C, the reference algorithms the GPU path replaces:
+ *   element kernels per quadrature node   feSysElm.cpp:16-27, 530-583;
+ *                                         feVectorSysElm.cpp:112-130, 390-427,
+ *                                         685-747, 1171-1240, 1454-1530
+ *   physical gradients                    feSpace.cpp:669-768, feCncGeo.cpp:651-670
+ *   colored scatter (sorted local indices + linear scan of the CSR row)
+ *                                         feLinearSystemMklPardiso.cpp:501-749
+ *   Newton-Raphson                        feNonLinearSolver.cpp:38-181
+ * and the published Krylov algorithms (Saad, Iterative Methods for Sparse
+ * Linear Systems, 2nd ed.): ILU(0) Alg. 10.4, PCG Alg. 9.1, FGMRES Alg. 9.6.
+ * Its pins: the golden fixtures produced by the reference library itself
+ * (tests/golden), checked by the CPU tests.
+ */
+#ifndef FE_ORACLE_H
+#define FE_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Forms (same ids as FE_FORM_* of include/feng_cuda.h). */
+typedef struct fo_forms {
+  int elem_type;   /* 1 scalar P2, 2 Taylor-Hood */
+  int has_diff; double diff;
+  int has_conv; double conv;
+  int has_sigma; double sigma, mu;
+  int has_divu; double divu;
+  int has_mass; double mass;
+  int src_kind; double src_coeff; double src_param[4];
+} fo_forms;
+
+typedef struct fo_problem {
+  int elem_type;
+  int64_t n_elm;
+  int nloc;
+  int64_t n_inc, n_dofs;
+  const int64_t *adr;        /* [n_elm*nloc] */
+  const double *elem_xy;     /* [n_elm*6] */
+  int n_colors;
+  const int64_t *color_offsets;
+  const int32_t *color_elements;
+  const int64_t *ia;         /* [n_inc+1] */
+  const int32_t *ja;         /* [nnz] */
+  int nq;
+  const double *qr, *qs, *qw;
+  fo_forms forms;
+} fo_problem;
+
+/* rhs (n_inc) and values (nnz) are accumulated (caller zeroes them).
+ * elem_begin/elem_end select a range of the color order (for sampling). */
+int fo_assemble_residual(const fo_problem *p, const double *u, const double *udot, double *rhs,
+                         int64_t elem_begin, int64_t elem_end, int nthreads);
+int fo_assemble_matrix(const fo_problem *p, const double *u, double c0, double *values,
+                       int64_t elem_begin, int64_t elem_end, int nthreads);
+
+/* Sparse helpers on the n_inc x n_inc CSR system. */
+void fo_spmv(int64_t n, const int64_t *ia, const int32_t *ja, const double *a, const double *x,
+             double *y, int nthreads);
+
+/* Preconditioners.  kind: 0 none, 1 block-Jacobi ILU(0) (block_of_row may be
+ * NULL for one block), 2 Jacobi, 3 block-triangular Schur for Taylor-Hood
+ * (velocity block: block-Jacobi ILU(0); pressure: lumped mass / viscosity). */
+typedef struct fo_precond fo_precond;
+fo_precond *fo_precond_create(int kind, int64_t n, const int64_t *ia, const int32_t *ja,
+                              const int32_t *block_of_row, const int32_t *is_pressure,
+                              const double *pmass_lumped, double viscosity);
+int fo_precond_factor(fo_precond *pc, const double *values);
+void fo_precond_apply(fo_precond *pc, const double *r, double *z);
+void fo_precond_destroy(fo_precond *pc);
+
+typedef struct fo_krylov_stats {
+  int iterations;
+  int converged;
+  double rnorm0, rnorm;
+} fo_krylov_stats;
+
+/* method 0 CG, 1 FGMRES(restart).  x starts at zero.  Converged when
+ * ||b - A x||_2 <= max(rtol ||b||_2, atol). */
+int fo_krylov_solve(int method, int restart, int max_iter, double rtol, double atol, int64_t n,
+                    const int64_t *ia, const int32_t *ja, const double *a, fo_precond *pc,
+                    const double *b, double *x, fo_krylov_stats *st, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,151 @@
+"""ctypes binding of the CPU oracle (oracle/fe_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg, never by the product.  Built by
+``make -C oracle port`` into oracle/_ref/libfeoracle.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_ref" / "libfeoracle.so"
+
+
+class Forms(C.Structure):
+    _fields_ = [("elem_type", C.c_int), ("has_diff", C.c_int), ("diff", C.c_double),
+                ("has_conv", C.c_int), ("conv", C.c_double), ("has_sigma", C.c_int),
+                ("sigma", C.c_double), ("mu", C.c_double), ("has_divu", C.c_int),
+                ("divu", C.c_double), ("has_mass", C.c_int), ("mass", C.c_double),
+                ("src_kind", C.c_int), ("src_coeff", C.c_double), ("src_param", C.c_double * 4)]
+
+
+class Problem(C.Structure):
+    _fields_ = [("elem_type", C.c_int), ("n_elm", C.c_int64), ("nloc", C.c_int),
+                ("n_inc", C.c_int64), ("n_dofs", C.c_int64), ("adr", C.c_void_p),
+                ("elem_xy", C.c_void_p), ("n_colors", C.c_int), ("color_offsets", C.c_void_p),
+                ("color_elements", C.c_void_p), ("ia", C.c_void_p), ("ja", C.c_void_p),
+                ("nq", C.c_int), ("qr", C.c_void_p), ("qs", C.c_void_p), ("qw", C.c_void_p),
+                ("forms", Forms)]
+
+
+class KStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("rnorm0", C.c_double),
+                ("rnorm", C.c_double)]
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            subprocess.run(["make", "-C", str(HERE), "port"], check=True, capture_output=True)
+        lib = C.CDLL(str(LIB))
+        P = C.c_void_p
+        lib.fo_assemble_residual.argtypes = [P, P, P, P, C.c_int64, C.c_int64, C.c_int]
+        lib.fo_assemble_matrix.argtypes = [P, P, C.c_double, P, C.c_int64, C.c_int64, C.c_int]
+        lib.fo_spmv.argtypes = [C.c_int64, P, P, P, P, P, C.c_int]
+        lib.fo_precond_create.restype = P
+        lib.fo_precond_create.argtypes = [C.c_int, C.c_int64, P, P, P, P, P, C.c_double]
+        lib.fo_precond_factor.argtypes = [P, P]
+        lib.fo_precond_apply.argtypes = [P, P, P]
+        lib.fo_precond_destroy.argtypes = [P]
+        lib.fo_krylov_solve.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                        C.c_int64, P, P, P, P, P, P, C.POINTER(KStats), C.c_int]
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def forms_from(elem_type, sysElms):
+    """Fused coefficients of a list of feSysElm descriptors (feng_gb300.api)."""
+    f = Forms()
+    f.elem_type = elem_type
+    for s in sysElms:
+        k = s.kind
+        if k == 2:
+            f.has_diff, f.diff = 1, f.diff + s.coeff
+        elif k in (1, 3):
+            f.src_kind, f.src_coeff = s.source, (s.coeff or 1.0)
+            for i in range(4):
+                f.src_param[i] = s.params[i]
+        elif k == 6:
+            f.has_conv, f.conv = 1, f.conv + s.coeff
+        elif k == 7:
+            f.has_sigma, f.sigma, f.mu = 1, s.coeff, s.coeff2
+        elif k == 5:
+            f.has_divu, f.divu = 1, f.divu + s.coeff
+        elif k == 4:
+            f.has_mass, f.mass = 1, f.mass + s.coeff
+    return f
+
+
+class OracleProblem:
+    """Element tables + pattern + coloring + quadrature + forms, held for the C oracle."""
+
+    def __init__(self, elem_type, adr, elem_xy, n_inc, n_dofs, color_offsets, color_elements,
+                 ia, ja, quad, sysElms):
+        self.lib = load()
+        self.keep = dict(
+            adr=np.ascontiguousarray(adr, np.int64).ravel(),
+            xy=np.ascontiguousarray(elem_xy, np.float64).ravel(),
+            off=np.ascontiguousarray(color_offsets, np.int64),
+            el=np.ascontiguousarray(color_elements, np.int32),
+            ia=np.ascontiguousarray(ia, np.int64), ja=np.ascontiguousarray(ja, np.int32),
+            qr=np.ascontiguousarray(quad[0], np.float64), qs=np.ascontiguousarray(quad[1], np.float64),
+            qw=np.ascontiguousarray(quad[2], np.float64))
+        k = self.keep
+        nloc = 6 if elem_type == 1 else 15
+        self.n_inc, self.n_dofs, self.nnz = int(n_inc), int(n_dofs), len(k["ja"])
+        self.n_elm = len(k["adr"]) // nloc
+        self.p = Problem(elem_type, self.n_elm, nloc, self.n_inc, self.n_dofs, _p(k["adr"]), _p(k["xy"]),
+                         len(k["off"]) - 1, _p(k["off"]), _p(k["el"]), _p(k["ia"]), _p(k["ja"]),
+                         len(k["qw"]), _p(k["qr"]), _p(k["qs"]), _p(k["qw"]), forms_from(elem_type, sysElms))
+
+    def residual(self, u, udot=None, begin=0, end=None, nthreads=None):
+        rhs = np.zeros(self.n_inc)
+        self.lib.fo_assemble_residual(C.byref(self.p), _p(np.ascontiguousarray(u)),
+                                      _p(None if udot is None else np.ascontiguousarray(udot)), _p(rhs),
+                                      begin, self.n_elm if end is None else end,
+                                      nthreads or os.cpu_count())
+        return rhs
+
+    def matrix(self, u, c0=0.0, begin=0, end=None, nthreads=None):
+        vals = np.zeros(self.nnz)
+        self.lib.fo_assemble_matrix(C.byref(self.p), _p(np.ascontiguousarray(u)), c0, _p(vals), begin,
+                                    self.n_elm if end is None else end, nthreads or os.cpu_count())
+        return vals
+
+    def solve(self, values, b, method=1, restart=50, max_iter=5000, rtol=1e-8, atol=1e-14,
+              pc_kind=1, block_of_row=None, is_pressure=None, pmass=None, viscosity=1.0,
+              nthreads=None):
+        k = self.keep
+        blk = None if block_of_row is None else np.ascontiguousarray(block_of_row, np.int32)
+        isp = None if is_pressure is None else np.ascontiguousarray(is_pressure, np.int32)
+        pm = None if pmass is None else np.ascontiguousarray(pmass, np.float64)
+        pc = self.lib.fo_precond_create(pc_kind, self.n_inc, _p(k["ia"]), _p(k["ja"]), _p(blk), _p(isp),
+                                        _p(pm), viscosity)
+        try:
+            vals = np.ascontiguousarray(values, np.float64)
+            s = self.lib.fo_precond_factor(pc, _p(vals))
+            if s != 0:
+                raise RuntimeError("oracle preconditioner: zero pivot")
+            x = np.zeros(self.n_inc)
+            st = KStats()
+            self.lib.fo_krylov_solve(method, restart, max_iter, rtol, atol, self.n_inc, _p(k["ia"]),
+                                     _p(k["ja"]), _p(vals), pc, _p(np.ascontiguousarray(b)), _p(x),
+                                     C.byref(st), nthreads or os.cpu_count())
+            return x, dict(iterations=st.iterations, converged=bool(st.converged), rnorm0=st.rnorm0,
+                           rnorm=st.rnorm)
+        finally:
+            self.lib.fo_precond_destroy(pc)
