@@ -40,7 +40,7 @@ class Options(C.Structure):
     _fields_ = [("krylov", C.c_int32), ("restart", C.c_int32), ("max_iter", C.c_int32),
                 ("rel_tol", C.c_double), ("abs_tol", C.c_double), ("div_tol", C.c_double),
                 ("precond", C.c_int32), ("pc_block_rows", C.c_int32), ("precision", C.c_int32),
-                ("quad_degree", C.c_int32)]
+                ("quad_degree", C.c_int32), ("mg_inner", C.c_int32), ("mg_smooth", C.c_int32)]
 
 
 class NewtonOptions(C.Structure):
@@ -109,6 +109,7 @@ SIGNATURES = {
     "fe_cuda_assemble_residuals": (C.c_int, [P]),
     "fe_cuda_assemble_matrices": (C.c_int, [P]),
     "fe_cuda_get_rhs_max_norm": (C.c_int, [P, C.POINTER(C.c_double)]),
+    "fe_cuda_set_tolerances": (C.c_int, [P, C.c_double, C.c_double, C.c_int]),
     "fe_cuda_solve": (C.c_int, [P, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                 C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "fe_cuda_correct_solution": (C.c_int, [P]),

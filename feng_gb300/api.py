@@ -277,16 +277,19 @@ class LinearSolverOptions:
     rel_tol: float = 1e-8         # feLinearSystem::_rel_tol (src/feLinearSystem.h:66)
     abs_tol: float = 1e-14
     div_tol: float = 1e6
-    precond: str = "bjacobi-ilu0"  # "none" | "bjacobi-ilu0" | "ilu0" | "jacobi"
+    precond: str = "amg"           # "none" | "bjacobi-ilu0" | "ilu0" | "jacobi" | "amg"
     pc_block_rows: int = 256
     precision: str = "fp64"       # "fp64" | "mixed"
+    mg_inner: int = 0             # multigrid: inner AMG-CG steps per velocity component
+    mg_smooth: int = 2            # multigrid: Chebyshev smoother degree
 
     def to_c(self, quad_degree: int) -> _lib.Options:
-        pc = {"none": 0, "bjacobi-ilu0": 1, "ilu0": 1, "jacobi": 2}[self.precond]
+        pc = {"none": 0, "bjacobi-ilu0": 1, "ilu0": 1, "jacobi": 2, "amg": 3}[self.precond]
         rows = 0 if self.precond == "ilu0" else self.pc_block_rows
         return _lib.Options(0 if self.krylov == "cg" else 1, self.restart, self.max_iter, self.rel_tol,
                             self.abs_tol, self.div_tol, pc, rows,
-                            1 if self.precision == "mixed" else 0, quad_degree)
+                            1 if self.precision == "mixed" else 0, quad_degree, self.mg_inner,
+                            self.mg_smooth)
 
 
 class feLinearSystemCUDA:
@@ -353,6 +356,14 @@ class feLinearSystemCUDA:
         v = C.c_double()
         check(self.lib.fe_cuda_get_rhs_max_norm(self._h, C.byref(v)))
         return v.value
+
+    def setTolerances(self, rel_tol=None, abs_tol=None, max_iter=None):
+        """setRelativeTol / setAbsoluteTol / setMaxIter (src/feLinearSystem.h:86-89)."""
+        o = self.options
+        o.rel_tol = o.rel_tol if rel_tol is None else rel_tol
+        o.abs_tol = o.abs_tol if abs_tol is None else abs_tol
+        o.max_iter = o.max_iter if max_iter is None else max_iter
+        check(self.lib.fe_cuda_set_tolerances(self._h, o.rel_tol, o.abs_tol, o.max_iter))
 
     def solve(self, raise_on_failure=True):
         dx, rhs, axb, it = C.c_double(), C.c_double(), C.c_double(), C.c_int()

@@ -1,0 +1,280 @@
+// Device V-cycle of the smoothed-aggregation hierarchy (see fe_amg.h).
+// Each level: Chebyshev smoothing on D^-1 A (polynomial, SpMV-only),
+// residual, restriction, coarse correction, prolongation, Chebyshev again;
+// the coarsest level is a dense inverse applied as a mat-vec.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "fe_amg.h"
+#include "fe_common.h"
+
+namespace feng {
+
+#define CKA(x)                                                                         \
+  do {                                                                                 \
+    cudaError_t _e = (x);                                                              \
+    if(_e != cudaSuccess) {                                                            \
+      set_error("CUDA error %s at %s:%d", cudaGetErrorString(_e), __FILE__, __LINE__); \
+      return FE_CUDA_FAIL;                                                             \
+    }                                                                                  \
+  } while(0)
+
+namespace {
+
+int grid(int64_t n, int per = 256) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + per - 1) / per, 1 << 20)); }
+
+// y = A x (MODE 0), y = b - A x (MODE 1), y += A x (MODE 2)
+template <typename V, int LANES, int MODE>
+__global__ void __launch_bounds__(256) k_csr(int64_t n, const int32_t *__restrict__ ia,
+                                             const int32_t *__restrict__ ja, const V *__restrict__ a,
+                                             const V *__restrict__ x, const V *__restrict__ b,
+                                             V *__restrict__ y)
+{
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
+  const int sub = threadIdx.x % LANES;
+  const bool live = row < n;
+  const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
+  V acc = 0;
+  for(int32_t k = beg + sub; k < end; k += LANES) acc += a[k] * x[ja[k]];
+#pragma unroll
+  for(int o = LANES / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, LANES);
+  if(live && sub == 0) {
+    if(MODE == 0) y[row] = acc;
+    else if(MODE == 1) y[row] = b[row] - acc;
+    else y[row] += acc;
+  }
+}
+
+template <typename V, int MODE>
+void csr(int lanes, int64_t n, const int32_t *ia, const int32_t *ja, const V *a, const V *x, const V *b,
+         V *y, cudaStream_t s)
+{
+  const int g = grid(n * lanes);
+  if(lanes == 8) k_csr<V, 8, MODE><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y);
+  else if(lanes == 16) k_csr<V, 16, MODE><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y);
+  else k_csr<V, 4, MODE><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y);
+}
+
+// Chebyshev start (x = 0): r = D^-1 b, d = r / theta, x = 0.
+template <typename V>
+__global__ void k_cheb_start(int64_t n, const V *__restrict__ dinv, const V *__restrict__ b, V *__restrict__ r,
+                             V *__restrict__ d, V *__restrict__ x, V inv_theta)
+{
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const V ri = dinv[i] * b[i];
+    r[i] = ri;
+    d[i] = ri * inv_theta;
+    x[i] = 0;
+  }
+}
+
+// Chebyshev start from a nonzero x: r = D^-1 (b - A x), d = r / theta.
+template <typename V, int LANES>
+__global__ void __launch_bounds__(256) k_cheb_restart(int64_t n, const int32_t *__restrict__ ia,
+                                                      const int32_t *__restrict__ ja, const V *__restrict__ a,
+                                                      const V *__restrict__ dinv, const V *__restrict__ b,
+                                                      const V *__restrict__ x, V *__restrict__ r,
+                                                      V *__restrict__ d, V inv_theta)
+{
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
+  const int sub = threadIdx.x % LANES;
+  const bool live = row < n;
+  const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
+  V acc = 0;
+  for(int32_t k = beg + sub; k < end; k += LANES) acc += a[k] * x[ja[k]];
+#pragma unroll
+  for(int o = LANES / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, LANES);
+  if(live && sub == 0) {
+    const V ri = dinv[row] * (b[row] - acc);
+    r[row] = ri;
+    d[row] = ri * inv_theta;
+  }
+}
+
+// One Chebyshev step: x += d; r -= D^-1 A d; dn = c1 d + c2 r.
+template <typename V, int LANES>
+__global__ void __launch_bounds__(256) k_cheb_step(int64_t n, const int32_t *__restrict__ ia,
+                                                   const int32_t *__restrict__ ja, const V *__restrict__ a,
+                                                   const V *__restrict__ dinv, const V *__restrict__ d,
+                                                   V *__restrict__ dn, V *__restrict__ r,
+                                                   V *__restrict__ x, V c1, V c2)
+{
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
+  const int sub = threadIdx.x % LANES;
+  const bool live = row < n;
+  const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
+  V acc = 0;
+  for(int32_t k = beg + sub; k < end; k += LANES) acc += a[k] * d[ja[k]];
+#pragma unroll
+  for(int o = LANES / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, LANES);
+  if(live && sub == 0) {
+    const V di = d[row];
+    x[row] += di;
+    const V ri = r[row] - dinv[row] * acc;
+    r[row] = ri;
+    dn[row] = c1 * di + c2 * ri;
+  }
+}
+
+// x = Minv b for the coarsest level (dense, row-major), one warp per row.
+template <typename V>
+__global__ void k_dense(int64_t n, const V *__restrict__ M, const V *__restrict__ b, V *__restrict__ x)
+{
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x % 32;
+  const bool live = row < n;
+  V acc = 0;
+  if(live)
+    for(int64_t k = lane; k < n; k += 32) acc += M[row * n + k] * b[k];
+  for(int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if(live && lane == 0) x[row] = acc;
+}
+
+template <typename V>
+int upload_vec(void **dst, const std::vector<double> &src)
+{
+  std::vector<V> tmp(src.begin(), src.end());
+  CKA(cudaMalloc(dst, sizeof(V) * std::max<size_t>(1, tmp.size())));
+  CKA(cudaMemcpy(*dst, tmp.data(), sizeof(V) * tmp.size(), cudaMemcpyHostToDevice));
+  return FE_OK;
+}
+
+int upload_idx(int32_t **dst, const std::vector<int64_t> &src)
+{
+  std::vector<int32_t> tmp(src.begin(), src.end());
+  CKA(cudaMalloc(dst, sizeof(int32_t) * std::max<size_t>(1, tmp.size())));
+  CKA(cudaMemcpy(*dst, tmp.data(), sizeof(int32_t) * tmp.size(), cudaMemcpyHostToDevice));
+  return FE_OK;
+}
+
+int upload_idx(int32_t **dst, const std::vector<int32_t> &src)
+{
+  CKA(cudaMalloc(dst, sizeof(int32_t) * std::max<size_t>(1, src.size())));
+  CKA(cudaMemcpy(*dst, src.data(), sizeof(int32_t) * src.size(), cudaMemcpyHostToDevice));
+  return FE_OK;
+}
+
+int lanes_for(const HostCSR &M)
+{
+  const double avg = M.n ? (double)M.nnz() / M.n : 0;
+  return avg > 24 ? 16 : avg > 10 ? 8 : 4;
+}
+
+}  // namespace
+
+AMGDevice::~AMGDevice()
+{
+  for(Lev &L : lv_) {
+    cudaFree(L.Aia); cudaFree(L.Aja); cudaFree(L.Pia); cudaFree(L.Pja); cudaFree(L.Ria); cudaFree(L.Rja);
+    cudaFree(L.Aa); cudaFree(L.Pa); cudaFree(L.Ra); cudaFree(L.dinv);
+    cudaFree(L.x); cudaFree(L.b); cudaFree(L.r); cudaFree(L.d0); cudaFree(L.d1);
+  }
+  cudaFree(coarseInv_);
+}
+
+int AMGDevice::upload(const AMGHierarchy &H, const AMGParams &p, int fp32, cudaStream_t s)
+{
+  p_ = p;
+  fp32_ = fp32;
+  s_ = s;
+  const size_t vs = fp32 ? sizeof(float) : sizeof(double);
+  lv_.resize(H.levels.size());
+  n0_ = H.levels.empty() ? 0 : H.levels[0].A.n;
+  diagSum_ = 0;
+  for(int64_t i = 0; i < n0_; ++i) diagSum_ += 1.0 / H.levels[0].dinv[i];
+  for(size_t l = 0; l < H.levels.size(); ++l) {
+    const AMGLevel &h = H.levels[l];
+    Lev &L = lv_[l];
+    L.n = h.A.n;
+    L.lmax = h.lmax;
+    L.lanesA = lanes_for(h.A);
+    FE_TRY(upload_idx(&L.Aia, h.A.ia));
+    FE_TRY(upload_idx(&L.Aja, h.A.ja));
+    FE_TRY(fp32 ? upload_vec<float>(&L.Aa, h.A.a) : upload_vec<double>(&L.Aa, h.A.a));
+    FE_TRY(fp32 ? upload_vec<float>(&L.dinv, h.dinv) : upload_vec<double>(&L.dinv, h.dinv));
+    for(void **v : {&L.x, &L.b, &L.r, &L.d0, &L.d1}) CKA(cudaMalloc(v, vs * std::max<int64_t>(1, L.n)));
+    if(l + 1 < H.levels.size()) {
+      L.nc = h.P.m;
+      L.lanesP = lanes_for(h.P);
+      L.lanesR = lanes_for(h.R);
+      FE_TRY(upload_idx(&L.Pia, h.P.ia));
+      FE_TRY(upload_idx(&L.Pja, h.P.ja));
+      FE_TRY(fp32 ? upload_vec<float>(&L.Pa, h.P.a) : upload_vec<double>(&L.Pa, h.P.a));
+      FE_TRY(upload_idx(&L.Ria, h.R.ia));
+      FE_TRY(upload_idx(&L.Rja, h.R.ja));
+      FE_TRY(fp32 ? upload_vec<float>(&L.Ra, h.R.a) : upload_vec<double>(&L.Ra, h.R.a));
+    }
+  }
+  nCoarse_ = lv_.empty() ? 0 : lv_.back().n;
+  FE_TRY(fp32 ? upload_vec<float>(&coarseInv_, H.coarseInv) : upload_vec<double>(&coarseInv_, H.coarseInv));
+  return FE_OK;
+}
+
+template <typename V>
+static void chebyshev(int lanes, int64_t n, const int32_t *ia, const int32_t *ja, const V *a, const V *dinv,
+                      const V *b, V *x, V *r, V *d0, V *d1, double lmax, const AMGParams &p, bool zeroStart,
+                      cudaStream_t s)
+{
+  // Chebyshev iteration on D^-1 A over [low, high] * lmax (Saad, Alg. 12.1).
+  const double lo = p.chebyLow * lmax, hi = p.chebyHigh * lmax;
+  const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+  double rho = 1.0 / sigma;
+  const int g = grid(n * lanes);
+  if(zeroStart) {
+    k_cheb_start<V><<<grid(n), 256, 0, s>>>(n, dinv, b, r, d0, x, (V)(1.0 / theta));
+  } else {
+    if(lanes == 16) k_cheb_restart<V, 16><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta));
+    else if(lanes == 8) k_cheb_restart<V, 8><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta));
+    else k_cheb_restart<V, 4><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta));
+  }
+  V *d = d0, *dn = d1;
+  for(int k = 0; k < p.chebyDegree; ++k) {
+    const double rhoN = 1.0 / (2.0 * sigma - rho);
+    const V c1 = (V)(rhoN * rho), c2 = (V)(2.0 * rhoN / delta);
+    if(lanes == 16) k_cheb_step<V, 16><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2);
+    else if(lanes == 8) k_cheb_step<V, 8><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2);
+    else k_cheb_step<V, 4><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2);
+    rho = rhoN;
+    std::swap(d, dn);
+  }
+}
+
+template <typename V>
+void AMGDevice::vcycle_t(int l, const V *b, V *x)
+{
+  Lev &L = lv_[l];
+  if(l == (int)lv_.size() - 1) {
+    k_dense<V><<<grid(L.n * 32), 256, 0, s_>>>(L.n, (const V *)coarseInv_, b, x);
+    return;
+  }
+  Lev &C = lv_[l + 1];
+  const V *A = (const V *)L.Aa;
+  chebyshev<V>(L.lanesA, L.n, L.Aia, L.Aja, A, (const V *)L.dinv, b, x, (V *)L.r, (V *)L.d0, (V *)L.d1,
+               L.lmax, p_, true, s_);
+  // residual r = b - A x, restrict into the coarse right-hand side
+  csr<V, 1>(L.lanesA, L.n, L.Aia, L.Aja, A, x, b, (V *)L.r, s_);
+  csr<V, 0>(L.lanesR, C.n, L.Ria, L.Rja, (const V *)L.Ra, (const V *)L.r, nullptr, (V *)C.b, s_);
+  vcycle_t<V>(l + 1, (const V *)C.b, (V *)C.x);
+  csr<V, 2>(L.lanesP, L.n, L.Pia, L.Pja, (const V *)L.Pa, (const V *)C.x, nullptr, x, s_);
+  chebyshev<V>(L.lanesA, L.n, L.Aia, L.Aja, A, (const V *)L.dinv, b, x, (V *)L.r, (V *)L.d0, (V *)L.d1,
+               L.lmax, p_, false, s_);
+}
+
+void AMGDevice::vcycle64(const double *b, double *x) { vcycle_t<double>(0, b, x); }
+void AMGDevice::vcycle32(const float *b, float *x) { vcycle_t<float>(0, b, x); }
+
+void AMGDevice::spmv64(const double *x, double *y)
+{
+  const Lev &L = lv_[0];
+  csr<double, 0>(L.lanesA, L.n, L.Aia, L.Aja, (const double *)L.Aa, x, nullptr, y, s_);
+}
+
+void AMGDevice::spmv32(const float *x, float *y)
+{
+  const Lev &L = lv_[0];
+  csr<float, 0>(L.lanesA, L.n, L.Aia, L.Aja, (const float *)L.Aa, x, nullptr, y, s_);
+}
+
+}  // namespace feng

@@ -1,0 +1,87 @@
+// Smoothed-aggregation algebraic multigrid (Vanek, Mandel, Brezina, "Algebraic
+// multigrid by smoothed aggregation for second and fourth order elliptic
+// problems", Computing 56, 1996) for scalar SPD operators: host set-up once
+// per mesh, V-cycles with Chebyshev smoothing on the device.
+//
+// Used as the velocity-block solve of the block-triangular saddle-point
+// preconditioner and as the preconditioner of scalar diffusion.  The
+// reference has no counterpart (its solves are PETSc/MKL library calls); it
+// is the device replacement that makes the Krylov solve converge in a
+// mesh-independent number of iterations.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+namespace feng {
+
+struct HostCSR {
+  int64_t n = 0, m = 0;  // rows, columns
+  std::vector<int64_t> ia;
+  std::vector<int32_t> ja;
+  std::vector<double> a;
+  int64_t nnz() const { return ia.empty() ? 0 : ia.back(); }
+};
+
+struct AMGLevel {
+  HostCSR A, P, R;
+  std::vector<double> dinv;
+  double lmax = 0;  // spectral radius estimate of D^-1 A
+};
+
+struct AMGHierarchy {
+  std::vector<AMGLevel> levels;  // last level: only A (coarsest)
+  std::vector<double> coarseInv; // dense inverse of the coarsest A, row-major
+};
+
+struct AMGParams {
+  double theta = 0.08;     // strength of connection
+  int maxLevels = 12;
+  int64_t coarseSize = 1200;
+  int chebyDegree = 2;
+  double chebyLow = 0.15;  // smoothing interval [low, high] * lmax
+  double chebyHigh = 1.05;
+};
+
+int amg_build(const HostCSR &A, const AMGParams &p, AMGHierarchy &H);
+
+template <typename V>
+struct DevLevelT;
+
+// Device hierarchy and V-cycle, in FP64 or FP32.
+class AMGDevice {
+ public:
+  ~AMGDevice();
+  int upload(const AMGHierarchy &H, const AMGParams &p, int fp32, cudaStream_t s);
+  // x = V-cycle(b) for the finest operator (x overwritten).
+  void vcycle64(const double *b, double *x);
+  void vcycle32(const float *b, float *x);
+  // y = A x with the finest operator.
+  void spmv64(const double *x, double *y);
+  void spmv32(const float *x, float *y);
+  int64_t n() const { return n0_; }
+  int levels() const { return (int)lv_.size(); }
+  double finestDiagSum() const { return diagSum_; }
+
+ private:
+  struct Lev {
+    int64_t n = 0, nc = 0;
+    int32_t *Aia = nullptr, *Aja = nullptr, *Pia = nullptr, *Pja = nullptr, *Ria = nullptr, *Rja = nullptr;
+    void *Aa = nullptr, *Pa = nullptr, *Ra = nullptr, *dinv = nullptr;
+    void *x = nullptr, *b = nullptr, *r = nullptr, *d0 = nullptr, *d1 = nullptr;
+    double lmax = 0;
+    int lanesA = 4, lanesP = 4, lanesR = 4;
+  };
+  template <typename V> void vcycle_t(int l, const V *b, V *x);
+  std::vector<Lev> lv_;
+  void *coarseInv_ = nullptr;
+  int64_t nCoarse_ = 0, n0_ = 0;
+  int fp32_ = 0;
+  AMGParams p_;
+  double diagSum_ = 0;
+  cudaStream_t s_ = 0;
+};
+
+}  // namespace feng

@@ -68,7 +68,7 @@ static int check_options(const fe_cuda_options *o)
     set_error("null options");
     return FE_INVALID_ARG;
   }
-  if(o->krylov < 0 || o->krylov > 1 || o->precond < 0 || o->precond > 2 || o->precision < 0 ||
+  if(o->krylov < 0 || o->krylov > 1 || o->precond < 0 || o->precond > 3 || o->precision < 0 ||
      o->precision > 1 || o->restart < 1 || o->restart > 128 || o->max_iter < 1 ||
      !(o->rel_tol >= 0) || !(o->abs_tol >= 0) || o->pc_block_rows < 0) {
     set_error("invalid linear solver options");
@@ -89,6 +89,8 @@ static SystemOptions to_sys_options(const fe_cuda_options *o)
   so.kry.precond = o->precond;
   so.pcBlockRows = o->pc_block_rows;
   so.precision = o->precision;
+  so.mgInner = o->mg_inner;
+  so.mgSmooth = o->mg_smooth > 0 ? o->mg_smooth : 2;
   return so;
 }
 
@@ -524,6 +526,18 @@ int fe_cuda_get_rhs_max_norm(fe_cuda_system *s, double *norm)
 {
   if(!s || !norm) { set_error("null argument"); return FE_INVALID_ARG; }
   return s->sys.getRHSMaxNorm(norm);
+}
+
+int fe_cuda_set_tolerances(fe_cuda_system *s, double rel_tol, double abs_tol, int max_iter)
+{
+  if(!s || !(rel_tol >= 0) || !(abs_tol >= 0) || max_iter < 1) {
+    set_error("invalid tolerances");
+    return FE_INVALID_ARG;
+  }
+  s->sys.krylov().opt.rtol = rel_tol;
+  s->sys.krylov().opt.atol = abs_tol;
+  s->sys.krylov().opt.maxIter = max_iter;
+  return FE_OK;
 }
 
 int fe_cuda_solve(fe_cuda_system *s, double *norm_dx, double *norm_rhs, double *norm_axb, int *n_iter)

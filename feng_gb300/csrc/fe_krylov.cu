@@ -519,7 +519,8 @@ Krylov::~Krylov()
   cudaFree(ilu_.blockStart); cudaFree(ilu_.perm); cudaFree(ilu_.lia); cudaFree(ilu_.lja);
   cudaFree(ilu_.ldiag); cudaFree(ilu_.srcPos); cudaFree(ilu_.vals); cudaFree(ilu_.status);
   cudaFree(red_state_); cudaFree(gmres_); cudaFree(cg_);
-  cudaFreeHost(h_gmres_); cudaFreeHost(h_cg_);
+  cudaFreeHost(h_gmres_); cudaFreeHost(h_cg_); cudaFreeHost(hflag_);
+  delete mg_;
 }
 
 static int grid_for(int64_t n, int threads, int maxBlocks)
@@ -528,8 +529,18 @@ static int grid_for(int64_t n, int threads, int maxBlocks)
   return (int)std::max<int64_t>(1, std::min<int64_t>(b, maxBlocks));
 }
 
+// Stops launching the iterations of a restart cycle once the device has set
+// its done flag (read every 4 iterations; skipped kernels would no-op anyway).
+bool Krylov::poll_done(const int *dflag, int j)
+{
+  if((j & 3) != 3) return false;
+  cudaMemcpyAsync(hflag_, dflag, sizeof(int), cudaMemcpyDeviceToHost, s_);
+  cudaStreamSynchronize(s_);
+  return *hflag_ != 0;
+}
+
 int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, int64_t nBlocksHint,
-                  const KrylovOptions &o, cudaStream_t s)
+                  const KrylovOptions &o, cudaStream_t s, const PrecondInfo *pinfo)
 {
   A_ = A;
   opt = o;
@@ -569,8 +580,15 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
   CK(cudaMemset(cg_, 0, sizeof(CGState)));
   CK(cudaMallocHost(&h_gmres_, sizeof(GmresState)));
   CK(cudaMallocHost(&h_cg_, sizeof(CGState)));
+  CK(cudaMallocHost(&hflag_, sizeof(int)));
 
-  if(opt.precond == 2) {
+  if(opt.precond == 3 || opt.precond == 4) {
+    if(!pinfo) {
+      set_error("multigrid preconditioner without set-up information");
+      return FE_INVALID_ARG;
+    }
+    FE_TRY(setup_mg(*pinfo));
+  } else if(opt.precond == 2) {
     if(opt.mixed) CK(cudaMalloc(&diag32_, sizeof(float) * n_));
     else CK(cudaMalloc(&diag_, sizeof(double) * n_));
     CK(cudaMalloc(&ilu_.status, sizeof(int)));
@@ -636,7 +654,14 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
 int Krylov::factor(const double *values64, const float *values32)
 {
   factoredOk_ = false;
+  cur64_ = values64;
+  cur32_ = values32;
   if(opt.precond == 0) { factoredOk_ = true; return FE_OK; }
+  if(opt.precond == 3 || opt.precond == 4) {
+    FE_TRY(factor_mg(values64, values32));
+    factoredOk_ = true;
+    return FE_OK;
+  }
   CK(cudaMemsetAsync(ilu_.status, 0, sizeof(int), s_));
   if(opt.precond == 2) {
     const int g = grid_for(n_, 256, 4096);
@@ -669,6 +694,8 @@ void Krylov::precond64(const double *r, double *z, const int *done)
 {
   if(opt.precond == 0) {
     cudaMemcpyAsync(z, r, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s_);
+  } else if(opt.precond >= 3) {
+    apply_mg<double>(cur64_, r, z, done);
   } else if(opt.precond == 2) {
     k_jacobi<double, double><<<grid_for(n_, 256, 4096), 256, 0, s_>>>(n_, diag_, r, z, done);
   } else {
@@ -682,6 +709,8 @@ void Krylov::precond32(const float *r, float *z, const int *done)
 {
   if(opt.precond == 0) {
     cudaMemcpyAsync(z, r, sizeof(float) * n_, cudaMemcpyDeviceToDevice, s_);
+  } else if(opt.precond >= 3) {
+    apply_mg<float>(cur32_, r, z, done);
   } else if(opt.precond == 2) {
     k_jacobi<float, float><<<grid_for(n_, 256, 4096), 256, 0, s_>>>(n_, diag32_, r, z, done);
   } else {
@@ -760,6 +789,7 @@ int Krylov::solve_fgmres64(const double *vals, const double *b, double *x, doubl
       k_scale_from<<<gv, 256, 0, s_>>>(n_, w_, V_ + (int64_t)(j + 1) * n_, w.st, Hcol + j + 1,
                                        &w.gs->done);
       k_givens<<<1, 1, 0, s_>>>(w.gs, j);
+      if(poll_done(&w.gs->done, j)) break;
     }
     k_backsolve<<<1, 1, 0, s_>>>(w.gs);
     k_xupdate<double><<<gv, 256, 0, s_>>>(n_, Z_, w.gs, x);
@@ -817,6 +847,7 @@ int Krylov::solve_fgmres_mixed(const float *vals32, const double *b, double *x, 
       k_scale_from<<<gv, 256, 0, s_>>>(n_, w_, V_ + (int64_t)(j + 1) * n_, w.st, Hcol + j + 1,
                                        &w.gs->done);
       k_givens<<<1, 1, 0, s_>>>(w.gs, j);
+      if(poll_done(&w.gs->done, j)) break;
     }
     k_backsolve<<<1, 1, 0, s_>>>(w.gs);
     k_xupdate<float><<<gv, 256, 0, s_>>>(n_, Z32_, w.gs, x);

@@ -39,6 +39,25 @@ struct DeviceBlockILU {
   int *status = nullptr;          // device flag: 0 ok, 1 zero pivot, 2 non-finite
 };
 
+// Host description of the multigrid-based preconditioners:
+//  kind 3 (scalar field):  z = M^-1 r with M = s K, K the P2 stiffness
+//                          matrix on the unknown nodes (AMG V-cycle);
+//  kind 4 (Taylor-Hood):   block upper-triangular saddle-point
+//                          preconditioner  [A  G; 0  S]^-1  with
+//                          A^-1 ~ (s K)^-1 per velocity component (AMG) and
+//                          S^-1 ~ (mu / c_div) M_p^-1 (lumped pressure mass).
+// s is measured from the diagonal of the current Jacobian at each factor().
+struct HostCSR;
+struct PrecondInfo {
+  const HostCSR *lap = nullptr;          // scalar stiffness on the nodes
+  std::vector<int32_t> nodeDofX, nodeDofY;  // unknown DOF of each node (per component)
+  std::vector<int32_t> pRows;            // pressure unknowns (kind 4)
+  std::vector<double> pMass;             // lumped pressure mass of pRows
+  double sigma = 1, divu = 1;            // DIV_NEWTONIAN_STRESS / MIXED_DIVERGENCE coefficients
+  int innerIterations = 0;               // inner AMG-preconditioned CG steps per component (0: one V-cycle)
+  int chebyDegree = 2;                   // Chebyshev smoother degree
+};
+
 struct KrylovOptions {
   int method = 1;          // 0 CG, 1 FGMRES
   int restart = 50;
@@ -46,7 +65,7 @@ struct KrylovOptions {
   double rtol = 1e-8;      // relative to ||b||_2 (PETSc default test)
   double atol = 1e-14;
   double dtol = 1e6;
-  int precond = 1;         // 0 none, 1 block-Jacobi ILU(0), 2 Jacobi
+  int precond = 1;         // 0 none, 1 block-Jacobi ILU(0), 2 Jacobi, 3 AMG, 4 saddle-point AMG
   int mixed = 0;           // 1: FP32 matrix/preconditioner/SpMV inside FP64 refinement
   int refineMax = 20;      // outer refinement steps in mixed mode
   double innerRtol = 1e-4; // inner FP32 solve tolerance in mixed mode
@@ -64,7 +83,7 @@ class Krylov {
   ~Krylov();
   // Allocates the workspace for systems of size n with the given pattern.
   int setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, int64_t nBlocksHint,
-            const KrylovOptions &opt, cudaStream_t s);
+            const KrylovOptions &opt, cudaStream_t s, const PrecondInfo *pinfo = nullptr);
   // Factors the preconditioner from the current matrix values.
   int factor(const double *values64, const float *values32);
   // Solves A x = b (x initial guess is zero).  Returns a Status.
@@ -108,6 +127,16 @@ class Krylov {
   // Device-resident solver state (opaque here, defined in fe_krylov.cu).
   void *red_state_ = nullptr, *gmres_ = nullptr, *cg_ = nullptr;
   void *h_gmres_ = nullptr, *h_cg_ = nullptr;
+  // Multigrid preconditioners (kinds 3, 4).
+  struct MG;
+  MG *mg_ = nullptr;
+  const double *cur64_ = nullptr;  // matrix values of the last factor()
+  const float *cur32_ = nullptr;
+  int *hflag_ = nullptr;           // pinned copy of the device done flag
+  bool poll_done(const int *dflag, int j);
+  int setup_mg(const PrecondInfo &pi);
+  int factor_mg(const double *values64, const float *values32);
+  template <typename V> void apply_mg(const V *vals, const V *r, V *z, const int *skip);
 };
 
 }  // namespace feng

@@ -1,0 +1,525 @@
+// Multigrid-based preconditioners of the Krylov solver (kinds 3 and 4 in
+// fe_krylov.h): AMG V-cycles on the scalar P2 stiffness matrix, used directly
+// for a scalar field or per velocity component inside the block
+// upper-triangular saddle-point preconditioner
+//     P = [ A  G ]      z_p = S^-1 r_p,   S^-1 ~ (mu / c_div) M_p^-1 (lumped)
+//         [ 0  S ]      z_u = A^-1 (r_u - G z_p),  A^-1 ~ (s K)^-1 per component
+// (Elman, Silvester, Wathen, "Finite Elements and Fast Iterative Solvers",
+// 2nd ed., ch. 9: block preconditioning of the Oseen problem).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "fe_amg.h"
+#include "fe_common.h"
+#include "fe_krylov.h"
+
+namespace feng {
+
+#define CKM(x)                                                                         \
+  do {                                                                                 \
+    cudaError_t _e = (x);                                                              \
+    if(_e != cudaSuccess) {                                                            \
+      set_error("CUDA error %s at %s:%d", cudaGetErrorString(_e), __FILE__, __LINE__); \
+      return FE_CUDA_FAIL;                                                             \
+    }                                                                                  \
+  } while(0)
+
+struct Krylov::MG {
+  AMGDevice amg;
+  int kind = 0;
+  int64_t nNodes = 0, nP = 0;
+  int32_t *dofX = nullptr, *dofY = nullptr, *pRows = nullptr;
+  int32_t *upIa = nullptr, *upPos = nullptr, *upCol = nullptr;  // G block, rows = velocity slot 2k+c
+  int32_t *dnIa = nullptr, *dnPos = nullptr, *dnCol = nullptr;  // D block, rows = pressure rows
+  int32_t *slotOf = nullptr;                                     // velocity DOF -> slot 2k+c (-1 otherwise)
+  double cMc = 0, cSc = 0;  // constant pressure mode: c^T M c and c^T S c (deflation)
+  double *pMassDev = nullptr, *tP = nullptr;
+  int32_t *diagX = nullptr;                                        // CSR position of diag of x rows
+  double *pScale64 = nullptr;
+  float *pScale32 = nullptr;
+  void *bx = nullptr, *by = nullptr, *zx = nullptr, *zy = nullptr;
+  double *dsum = nullptr;
+  double lapDiagSum = 0, s = 1, sigma = 1, divu = 1;
+  std::vector<double> pMass;
+  int fp32 = 0;
+  // Inner preconditioned CG on K (AMG V-cycle preconditioner), `inner`
+  // iterations per component; 0 = a single V-cycle.
+  int inner = 0;
+  void *ir = nullptr, *iz = nullptr, *ip = nullptr, *iq = nullptr;
+  double *part = nullptr;  // [2][1024] partial sums
+  double *scal = nullptr;  // rz, pq
+  ~MG()
+  {
+    cudaFree(dofX); cudaFree(dofY); cudaFree(pRows); cudaFree(upIa); cudaFree(upPos); cudaFree(upCol);
+    cudaFree(diagX); cudaFree(pScale64); cudaFree(pScale32); cudaFree(bx); cudaFree(by); cudaFree(zx);
+    cudaFree(zy); cudaFree(dsum); cudaFree(ir); cudaFree(iz); cudaFree(ip); cudaFree(iq);
+    cudaFree(part); cudaFree(scal); cudaFree(dnIa); cudaFree(dnPos); cudaFree(dnCol); cudaFree(slotOf);
+    cudaFree(pMassDev); cudaFree(tP);
+  }
+  template <typename V> void solveK(const V *b, V *x, cudaStream_t st);
+};
+
+namespace {
+
+constexpr int NPART = 512;
+
+template <typename V>
+__global__ void k_dot_part(int64_t n, const V *__restrict__ a, const V *__restrict__ b, double *part)
+{
+  __shared__ double sh[256];
+  double s = 0.;
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s += (double)a[i] * (double)b[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for(int o = 128; o > 0; o >>= 1) {
+    if(threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if(threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void k_dot_fin(int nparts, const double *__restrict__ part, double *out)
+{
+  __shared__ double sh[256];
+  double s = 0.;
+  for(int i = threadIdx.x; i < nparts; i += blockDim.x) s += part[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for(int o = 128; o > 0; o >>= 1) {
+    if(threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if(threadIdx.x == 0) *out = sh[0];
+}
+
+// x += alpha p, r -= alpha q with alpha = rz / pq (device scalars); a zero
+// or non-finite pq leaves x, r unchanged.
+template <typename V>
+__global__ void k_pcg_xr(int64_t n, const double *__restrict__ scal, const V *__restrict__ p,
+                         const V *__restrict__ q, V *__restrict__ x, V *__restrict__ r)
+{
+  const double pq = scal[1];
+  const double alpha = (pq != 0. && isfinite(pq)) ? scal[0] / pq : 0.;
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += (V)alpha * p[i];
+    r[i] -= (V)alpha * q[i];
+  }
+}
+
+// p = z + beta p with beta = rz_new / rz (scal[2] / scal[0]); then rz = rz_new.
+template <typename V>
+__global__ void k_pcg_p(int64_t n, const double *__restrict__ scal, const V *__restrict__ z, V *__restrict__ p,
+                        int first)
+{
+  const double beta = (first || scal[0] == 0.) ? 0. : scal[2] / scal[0];
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = z[i] + (V)beta * p[i];
+}
+
+__global__ void k_pcg_shift(double *scal) { scal[0] = scal[2]; }
+
+template <typename V>
+__global__ void k_copy_v(int64_t n, const V *__restrict__ a, V *__restrict__ b)
+{
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = a[i];
+}
+
+__global__ void k_zero_d(int64_t n, double *x)
+{
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) x[i] = 0.;
+}
+
+}  // namespace
+
+// x = K^-1 b approximately: one V-cycle, or `inner` steps of CG preconditioned
+// by the V-cycle (Saad Alg. 9.1), all scalars kept on the device.
+template <typename V>
+void Krylov::MG::solveK(const V *b, V *x, cudaStream_t st)
+{
+  const int64_t n = nNodes;
+  auto vc = [&](const V *in, V *out) {
+    if constexpr(sizeof(V) == 8) amg.vcycle64(in, out);
+    else amg.vcycle32(in, out);
+  };
+  auto spmv = [&](const V *in, V *out) {
+    if constexpr(sizeof(V) == 8) amg.spmv64(in, out);
+    else amg.spmv32(in, out);
+  };
+  if(inner <= 0) {
+    vc(b, x);
+    return;
+  }
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 4096));
+  const int gp = (int)std::min<int64_t>(NPART, std::max<int64_t>(1, (n + 255) / 256));
+  V *r = (V *)ir, *z = (V *)iz, *p = (V *)ip, *q = (V *)iq;
+  k_copy_v<V><<<g, 256, 0, st>>>(n, b, r);
+  // x = 0 (written through r's type)
+  if constexpr(sizeof(V) == 8) k_zero_d<<<g, 256, 0, st>>>(n, (double *)x);
+  else cudaMemsetAsync(x, 0, sizeof(float) * n, st);
+  vc(r, z);
+  k_dot_part<V><<<gp, 256, 0, st>>>(n, r, z, part);
+  k_dot_fin<<<1, 256, 0, st>>>(gp, part, scal + 0);
+  k_pcg_p<V><<<g, 256, 0, st>>>(n, scal, z, p, 1);
+  for(int it = 0; it < inner; ++it) {
+    spmv(p, q);
+    k_dot_part<V><<<gp, 256, 0, st>>>(n, p, q, part);
+    k_dot_fin<<<1, 256, 0, st>>>(gp, part, scal + 1);
+    k_pcg_xr<V><<<g, 256, 0, st>>>(n, scal, p, q, x, r);
+    if(it + 1 == inner) break;
+    vc(r, z);
+    k_dot_part<V><<<gp, 256, 0, st>>>(n, r, z, part);
+    k_dot_fin<<<1, 256, 0, st>>>(gp, part, scal + 2);
+    k_pcg_p<V><<<g, 256, 0, st>>>(n, scal, z, p, 0);
+    k_pcg_shift<<<1, 1, 0, st>>>(scal);
+  }
+}
+
+namespace {
+
+int grid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 1 << 16)); }
+
+template <typename VA>
+__global__ void k_diag_sum(int64_t n, const int32_t *__restrict__ pos, const VA *__restrict__ a,
+                           double *out)
+{
+  __shared__ double sh[256];
+  double s = 0.;
+  for(int64_t i = threadIdx.x; i < n; i += blockDim.x) s += (double)a[pos[i]];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for(int o = 128; o > 0; o >>= 1) {
+    if(threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if(threadIdx.x == 0) *out = sh[0];
+}
+
+template <typename V>
+__global__ void k_scale_copy(int64_t n, const V *__restrict__ r, V *__restrict__ z, V f,
+                             const int *__restrict__ skip)
+{
+  if(skip && *skip) return;
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    z[i] = r[i] * f;
+}
+
+// Pressure block with the constant mode deflated:
+//   z_p = pscale_p (r_p - (c^T r) m_p / c^T M c) + (c^T r) / c^T S c,
+// c = 1 on the pressure unknowns, (c^T r) read from *cr.
+template <typename V, typename S>
+__global__ void k_pressure(int64_t nP, const int32_t *__restrict__ rows, const S *__restrict__ sc,
+                           const double *__restrict__ mass, const double *__restrict__ cr, double cMc,
+                           double cSc, const V *__restrict__ r, V *__restrict__ z,
+                           const int *__restrict__ skip)
+{
+  if(skip && *skip) return;
+  const double c = cr ? *cr : 0.;
+  const double shift = cMc > 0 ? c / cMc : 0., lift = cSc != 0. ? c / cSc : 0.;
+  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nP; k += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t i = rows[k];
+    const double rp = (double)r[i] - (cr ? shift * mass[k] : 0.);
+    z[i] = (V)((double)sc[k] * rp + lift);
+  }
+}
+
+// partial sums of r over the pressure rows
+template <typename V>
+__global__ void k_psum_part(int64_t nP, const int32_t *__restrict__ rows, const V *__restrict__ r, double *part)
+{
+  __shared__ double sh[256];
+  double s = 0.;
+  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nP; k += (int64_t)gridDim.x * blockDim.x)
+    s += (double)r[rows[k]];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for(int o = 128; o > 0; o >>= 1) {
+    if(threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if(threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// partial sums of a double array
+__global__ void k_tsum(int64_t n, const double *__restrict__ t, double *part)
+{
+  __shared__ double sh[256];
+  double s = 0.;
+  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    s += t[k];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for(int o = 128; o > 0; o >>= 1) {
+    if(threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if(threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// g = G c: row sums of the G block per velocity slot.
+template <typename V>
+__global__ void k_gsum(int64_t nN, const int32_t *__restrict__ upIa, const int32_t *__restrict__ upPos,
+                       const V *__restrict__ a, V *__restrict__ bx, V *__restrict__ by)
+{
+  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nN; k += (int64_t)gridDim.x * blockDim.x)
+    for(int c = 0; c < 2; ++c) {
+      double s = 0.;
+      for(int32_t e = upIa[2 * k + c]; e < upIa[2 * k + c + 1]; ++e) s += (double)a[upPos[e]];
+      if(c == 0) bx[k] = (V)s;
+      else by[k] = (V)s;
+    }
+}
+
+// t_p = (D w)_p with w given per slot by (wx, wy).
+template <typename V>
+__global__ void k_dw(int64_t nP, const int32_t *__restrict__ dnIa, const int32_t *__restrict__ dnPos,
+                     const int32_t *__restrict__ dnCol, const int32_t *__restrict__ slotOf,
+                     const V *__restrict__ a, const V *__restrict__ wx, const V *__restrict__ wy,
+                     double *__restrict__ t)
+{
+  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nP; k += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.;
+    for(int32_t e = dnIa[k]; e < dnIa[k + 1]; ++e) {
+      const int32_t sl = slotOf[dnCol[e]];
+      const double w = (sl & 1) ? (double)wy[sl >> 1] : (double)wx[sl >> 1];
+      s += (double)a[dnPos[e]] * w;
+    }
+    t[k] = s;
+  }
+}
+
+// b_c[k] = r_u - G z_p on velocity component c of node k.
+template <typename V>
+__global__ void k_vel_rhs(int64_t nN, const int32_t *__restrict__ dofX, const int32_t *__restrict__ dofY,
+                          const int32_t *__restrict__ upIa, const int32_t *__restrict__ upPos,
+                          const int32_t *__restrict__ upCol, const V *__restrict__ a,
+                          const V *__restrict__ r, const V *__restrict__ z, V *__restrict__ bx,
+                          V *__restrict__ by, const int *__restrict__ skip)
+{
+  if(skip && *skip) return;
+  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nN; k += (int64_t)gridDim.x * blockDim.x) {
+    for(int c = 0; c < 2; ++c) {
+      const int32_t d = c == 0 ? dofX[k] : dofY[k];
+      V t = r[d];
+      const int64_t slot = 2 * k + c;
+      if(upIa)
+        for(int32_t e = upIa[slot]; e < upIa[slot + 1]; ++e) t -= a[upPos[e]] * z[upCol[e]];
+      if(c == 0) bx[k] = t;
+      else by[k] = t;
+    }
+  }
+}
+
+template <typename V>
+__global__ void k_vel_out(int64_t nN, const int32_t *__restrict__ dofX, const int32_t *__restrict__ dofY,
+                          const V *__restrict__ zx, const V *__restrict__ zy, V f, V *__restrict__ z,
+                          const int *__restrict__ skip)
+{
+  if(skip && *skip) return;
+  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nN; k += (int64_t)gridDim.x * blockDim.x) {
+    z[dofX[k]] = zx[k] * f;
+    if(dofY) z[dofY[k]] = zy[k] * f;
+  }
+}
+
+template <typename T>
+int up(T **dst, const std::vector<T> &v)
+{
+  CKM(cudaMalloc(dst, sizeof(T) * std::max<size_t>(1, v.size())));
+  CKM(cudaMemcpy(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  return FE_OK;
+}
+
+}  // namespace
+
+int Krylov::setup_mg(const PrecondInfo &pi)
+{
+  if(!pi.lap || pi.lap->n <= 0) {
+    set_error("multigrid preconditioner needs the scalar stiffness matrix");
+    return FE_INVALID_ARG;
+  }
+  mg_ = new MG();
+  MG &M = *mg_;
+  M.kind = opt.precond;
+  M.fp32 = opt.mixed;
+  M.sigma = pi.sigma;
+  M.divu = pi.divu;
+  M.nNodes = pi.lap->n;
+  if((int64_t)pi.nodeDofX.size() != M.nNodes ||
+     (M.kind == 4 && (int64_t)pi.nodeDofY.size() != M.nNodes)) {
+    set_error("node maps do not match the stiffness matrix");
+    return FE_INVALID_ARG;
+  }
+  AMGParams ap;
+  ap.chebyDegree = pi.chebyDegree;
+  M.inner = pi.innerIterations;
+  AMGHierarchy H;
+  FE_TRY(amg_build(*pi.lap, ap, H));
+  FE_TRY(M.amg.upload(H, ap, M.fp32, s_));
+  M.lapDiagSum = M.amg.finestDiagSum();
+  FE_TRY(up(&M.dofX, pi.nodeDofX));
+  if(M.kind == 4) FE_TRY(up(&M.dofY, pi.nodeDofY));
+  const size_t vs = M.fp32 ? sizeof(float) : sizeof(double);
+  for(void **v : {&M.bx, &M.by, &M.zx, &M.zy, &M.ir, &M.iz, &M.ip, &M.iq})
+    CKM(cudaMalloc(v, vs * M.nNodes));
+  CKM(cudaMalloc(&M.dsum, sizeof(double)));
+  CKM(cudaMalloc(&M.part, sizeof(double) * NPART));
+  CKM(cudaMalloc(&M.scal, sizeof(double) * 4));
+  CKM(cudaMemset(M.scal, 0, sizeof(double) * 4));
+  // Host pattern for the diagonal positions and the G block.
+  std::vector<int32_t> hia(n_ + 1), hja(A_.nnz);
+  CKM(cudaMemcpy(hia.data(), A_.ia, sizeof(int32_t) * (n_ + 1), cudaMemcpyDeviceToHost));
+  CKM(cudaMemcpy(hja.data(), A_.ja, sizeof(int32_t) * A_.nnz, cudaMemcpyDeviceToHost));
+  std::vector<int32_t> diagX(M.nNodes, -1);
+  for(int64_t k = 0; k < M.nNodes; ++k) {
+    const int32_t d = pi.nodeDofX[k];
+    if(d < 0 || d >= n_) { set_error("node DOF out of range"); return FE_INVALID_ARG; }
+    for(int32_t e = hia[d]; e < hia[d + 1]; ++e)
+      if(hja[e] == d) diagX[k] = e;
+    if(diagX[k] < 0) { set_error("missing diagonal"); return FE_INVALID_ARG; }
+  }
+  FE_TRY(up(&M.diagX, diagX));
+  if(M.kind == 4) {
+    M.nP = (int64_t)pi.pRows.size();
+    M.pMass = pi.pMass;
+    std::vector<uint8_t> isP(n_, 0);
+    for(int32_t p : pi.pRows) {
+      if(p < 0 || p >= n_) { set_error("pressure row out of range"); return FE_INVALID_ARG; }
+      isP[p] = 1;
+    }
+    std::vector<int32_t> ia2(2 * M.nNodes + 1, 0), pos, col;
+    for(int64_t k = 0; k < M.nNodes; ++k)
+      for(int c = 0; c < 2; ++c) {
+        const int32_t d = c == 0 ? pi.nodeDofX[k] : pi.nodeDofY[k];
+        if(d < 0 || d >= n_) { set_error("node DOF out of range"); return FE_INVALID_ARG; }
+        for(int32_t e = hia[d]; e < hia[d + 1]; ++e)
+          if(isP[hja[e]]) { pos.push_back(e); col.push_back(hja[e]); }
+        ia2[2 * k + c + 1] = (int32_t)pos.size();
+      }
+    FE_TRY(up(&M.upIa, ia2));
+    FE_TRY(up(&M.upPos, pos));
+    FE_TRY(up(&M.upCol, col));
+    FE_TRY(up(&M.pRows, pi.pRows));
+    // D block (pressure rows -> velocity columns) and the slot of each velocity DOF.
+    std::vector<int32_t> slot(n_, -1);
+    for(int64_t k = 0; k < M.nNodes; ++k) {
+      slot[pi.nodeDofX[k]] = (int32_t)(2 * k);
+      slot[pi.nodeDofY[k]] = (int32_t)(2 * k + 1);
+    }
+    std::vector<int32_t> dia(M.nP + 1, 0), dpos, dcol;
+    for(int64_t k = 0; k < M.nP; ++k) {
+      const int32_t p = pi.pRows[k];
+      for(int32_t e = hia[p]; e < hia[p + 1]; ++e)
+        if(slot[hja[e]] >= 0) { dpos.push_back(e); dcol.push_back(hja[e]); }
+      dia[k + 1] = (int32_t)dpos.size();
+    }
+    FE_TRY(up(&M.dnIa, dia));
+    FE_TRY(up(&M.dnPos, dpos));
+    FE_TRY(up(&M.dnCol, dcol));
+    FE_TRY(up(&M.slotOf, slot));
+    FE_TRY(up(&M.pMassDev, pi.pMass));
+    CKM(cudaMalloc(&M.tP, sizeof(double) * std::max<int64_t>(1, M.nP)));
+    M.cMc = 0.;
+    for(double m : pi.pMass) M.cMc += m;
+    CKM(cudaMalloc(&M.pScale64, sizeof(double) * std::max<int64_t>(1, M.nP)));
+    CKM(cudaMalloc(&M.pScale32, sizeof(float) * std::max<int64_t>(1, M.nP)));
+  }
+  return FE_OK;
+}
+
+int Krylov::factor_mg(const double *values64, const float *values32)
+{
+  MG &M = *mg_;
+  if(values64) k_diag_sum<double><<<1, 256, 0, s_>>>(M.nNodes, M.diagX, values64, M.dsum);
+  else k_diag_sum<float><<<1, 256, 0, s_>>>(M.nNodes, M.diagX, values32, M.dsum);
+  double sum = 0.;
+  CKM(cudaMemcpyAsync(&sum, M.dsum, sizeof(double), cudaMemcpyDeviceToHost, s_));
+  CKM(cudaStreamSynchronize(s_));
+  if(!(std::isfinite(sum)) || sum == 0.) {
+    set_error("preconditioner scale: zero or non-finite diagonal");
+    return FE_PC_FAILED;
+  }
+  // A_xx ~ s K; for the symmetric-gradient viscous operator the diagonal of
+  // one component block is about 1.5 times the Laplacian's, so
+  // mu ~ -s / (1.5 sigma) and S^-1 ~ (mu / c_div) M_p^-1.
+  M.s = sum / M.lapDiagSum;
+  if(M.kind == 4) {
+    std::vector<double> sc(M.nP);
+    std::vector<float> sc32(M.nP);
+    for(int64_t k = 0; k < M.nP; ++k) {
+      sc[k] = -M.s / (1.5 * M.sigma * M.divu * M.pMass[k]);
+      sc32[k] = (float)sc[k];
+    }
+    CKM(cudaMemcpyAsync(M.pScale64, sc.data(), sizeof(double) * M.nP, cudaMemcpyHostToDevice, s_));
+    CKM(cudaMemcpyAsync(M.pScale32, sc32.data(), sizeof(float) * M.nP, cudaMemcpyHostToDevice, s_));
+    // Constant pressure mode c: with the pressure fixed at a single point the
+    // true Schur complement is nearly singular along c, far below the mass
+    // estimate.  c^T S c = -(D^T c) . A^-1 (G c) is estimated once per
+    // Jacobian with the velocity solve A^-1 ~ (s K)^-1.
+    const int g = grid(M.nNodes);
+    double sum2 = 0.;
+    if(values64) {
+      k_gsum<double><<<g, 256, 0, s_>>>(M.nNodes, M.upIa, M.upPos, values64, (double *)M.bx, (double *)M.by);
+      M.solveK<double>((const double *)M.bx, (double *)M.zx, s_);
+      M.solveK<double>((const double *)M.by, (double *)M.zy, s_);
+      k_dw<double><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values64,
+                                                (const double *)M.zx, (const double *)M.zy, M.tP);
+    } else {
+      k_gsum<float><<<g, 256, 0, s_>>>(M.nNodes, M.upIa, M.upPos, values32, (float *)M.bx, (float *)M.by);
+      M.solveK<float>((const float *)M.bx, (float *)M.zx, s_);
+      M.solveK<float>((const float *)M.by, (float *)M.zy, s_);
+      k_dw<float><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values32,
+                                               (const float *)M.zx, (const float *)M.zy, M.tP);
+    }
+    const int gp = (int)std::min<int64_t>(NPART, std::max<int64_t>(1, (M.nP + 255) / 256));
+    k_tsum<<<gp, 256, 0, s_>>>(M.nP, M.tP, M.part);
+    k_dot_fin<<<1, 256, 0, s_>>>(gp, M.part, M.dsum);
+    CKM(cudaMemcpyAsync(&sum2, M.dsum, sizeof(double), cudaMemcpyDeviceToHost, s_));
+    CKM(cudaStreamSynchronize(s_));
+    M.cSc = -sum2 / M.s;
+    if(!std::isfinite(M.cSc) || M.cSc == 0.) M.cSc = 0.;  // no deflation
+  }
+  return FE_OK;
+}
+
+template <typename V>
+void Krylov::apply_mg(const V *vals, const V *r, V *z, const int *skip)
+{
+  MG &M = *mg_;
+  const V f = (V)(1.0 / M.s);
+  if(M.kind == 3) {
+    // z = (s K)^-1 r on the unknown rows (the nodes are the unknowns)
+    k_vel_rhs<V><<<grid(M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofX, nullptr, nullptr, nullptr,
+                                                  vals, r, z, (V *)M.bx, (V *)M.by, skip);
+  } else {
+    const double *cr = nullptr;
+    if(M.cSc != 0.) {
+      const int gp = (int)std::min<int64_t>(NPART, std::max<int64_t>(1, (M.nP + 255) / 256));
+      k_psum_part<V><<<gp, 256, 0, s_>>>(M.nP, M.pRows, r, M.part);
+      k_dot_fin<<<1, 256, 0, s_>>>(gp, M.part, M.scal + 3);
+      cr = M.scal + 3;
+    }
+    if constexpr(sizeof(V) == 8)
+      k_pressure<V, double><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.pRows, M.pScale64, M.pMassDev, cr, M.cMc,
+                                                        M.cSc, r, z, skip);
+    else
+      k_pressure<V, float><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.pRows, M.pScale32, M.pMassDev, cr, M.cMc,
+                                                       M.cSc, r, z, skip);
+    k_vel_rhs<V><<<grid(M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, M.upIa, M.upPos, M.upCol,
+                                                  vals, r, z, (V *)M.bx, (V *)M.by, skip);
+  }
+  // The component solves run unconditionally; when `skip` is set their
+  // output is discarded by the skipped scatter below.
+  M.solveK<V>((const V *)M.bx, (V *)M.zx, s_);
+  if(M.kind == 4) M.solveK<V>((const V *)M.by, (V *)M.zy, s_);
+  k_vel_out<V><<<grid(M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.kind == 4 ? M.dofY : nullptr,
+                                                (const V *)M.zx, (const V *)M.zy, f, z, skip);
+}
+
+template void Krylov::apply_mg<double>(const double *, const double *, double *, const int *);
+template void Krylov::apply_mg<float>(const float *, const float *, float *, const int *);
+
+}  // namespace feng

@@ -283,7 +283,94 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
     else if(opt.pcBlockRows > 0) nbHint = std::max<int64_t>(1, nInc_ / opt.pcBlockRows);
   }
   CK(cudaStreamSynchronize(s_));
-  FE_TRY(kry_.setup(csr_, blocks, nbHint, ko, s_));
+  PrecondInfo pinfo;
+  HostCSR lap;
+  if(ko.precond == 3 || ko.precond == 4) {
+    ko.precond = t.elemType == ELEM_P2 ? 3 : 4;
+    FE_TRY(build_precond_info(t, hT, lap, pinfo));
+    pinfo.innerIterations = opt.mgInner;
+    pinfo.chebyDegree = std::max(1, std::min(6, opt.mgSmooth));
+  }
+  FE_TRY(kry_.setup(csr_, blocks, nbHint, ko, s_, &pinfo));
+  return FE_OK;
+}
+
+// Scalar P2 stiffness matrix on the unknown nodes (the scalar field's
+// unknowns, or the velocity nodes whose two components are unknowns), the
+// pressure unknowns and their lumped mass int psi_j = |J|/3 * 1/2.
+int SystemCUDA::build_precond_info(const SystemTables &t, const RefTensors &T, HostCSR &lap,
+                                   PrecondInfo &pi)
+{
+  const int64_t nE = t.nElm;
+  const int nl = nloc_;
+  const bool th = t.elemType == ELEM_TAYLOR_HOOD;
+  std::vector<int32_t> nodeOf(nDofs_, -1);
+  int64_t nN = 0;
+  for(int64_t e = 0; e < nE; ++e)
+    for(int a = 0; a < 6; ++a) {
+      const int64_t dx = t.adr[e * nl + (th ? 2 * a : a)];
+      if(dx >= nInc_ || nodeOf[dx] >= 0) continue;
+      if(th && t.adr[e * nl + 2 * a + 1] >= nInc_) {
+        set_error("a velocity node with one essential component is not supported by the multigrid preconditioner");
+        return FE_INVALID_ARG;
+      }
+      nodeOf[dx] = (int32_t)nN++;
+      pi.nodeDofX.push_back((int32_t)dx);
+      if(th) pi.nodeDofY.push_back((int32_t)t.adr[e * nl + 2 * a + 1]);
+    }
+  std::vector<std::pair<int64_t, double>> coo;  // (row*nN + col, value)
+  coo.reserve(nE * 36);
+  std::vector<double> pm(nDofs_, 0.);
+  for(int64_t e = 0; e < nE; ++e) {
+    const double *c = t.elemXY + 6 * e;
+    const double dxdr0 = c[2] - c[0], dxdr1 = c[3] - c[1], dxds0 = c[4] - c[0], dxds1 = c[5] - c[1];
+    const double jac = dxdr0 * dxds1 - dxdr1 * dxds0;
+    const double G[2][2] = {{dxds1 / jac, -dxds0 / jac}, {-dxdr1 / jac, dxdr0 / jac}};
+    double GG[2][2];
+    for(int r = 0; r < 2; ++r)
+      for(int s = 0; s < 2; ++s) GG[r][s] = G[r][0] * G[s][0] + G[r][1] * G[s][1];
+    int32_t nd[6];
+    for(int a = 0; a < 6; ++a) {
+      const int64_t dx = t.adr[e * nl + (th ? 2 * a : a)];
+      nd[a] = dx < nInc_ ? nodeOf[dx] : -1;
+    }
+    for(int a = 0; a < 6; ++a) {
+      if(nd[a] < 0) continue;
+      for(int b = 0; b < 6; ++b) {
+        if(nd[b] < 0) continue;
+        double v = 0.;
+        for(int r = 0; r < 2; ++r)
+          for(int s = 0; s < 2; ++s) v += GG[r][s] * T.K[r][s][a][b];
+        coo.push_back({(int64_t)nd[a] * nN + nd[b], std::fabs(jac) * v});
+      }
+    }
+    if(th)
+      for(int j = 0; j < 3; ++j) pm[t.adr[e * nl + 12 + j]] += std::fabs(jac) / 6.0;
+  }
+  std::sort(coo.begin(), coo.end(),
+            [](const std::pair<int64_t, double> &x, const std::pair<int64_t, double> &y) { return x.first < y.first; });
+  lap = HostCSR();
+  lap.n = lap.m = nN;
+  lap.ia.assign(nN + 1, 0);
+  for(size_t k = 0; k < coo.size();) {
+    const int64_t key = coo[k].first;
+    double v = 0.;
+    while(k < coo.size() && coo[k].first == key) v += coo[k++].second;
+    lap.ja.push_back((int32_t)(key % nN));
+    lap.a.push_back(v);
+    lap.ia[key / nN + 1] = (int64_t)lap.ja.size();
+  }
+  for(int64_t i = 0; i < nN; ++i) lap.ia[i + 1] = std::max(lap.ia[i + 1], lap.ia[i]);
+  pi.lap = &lap;
+  if(th) {
+    for(int64_t d = 0; d < nInc_; ++d)
+      if(pm[d] > 0) {
+        pi.pRows.push_back((int32_t)d);
+        pi.pMass.push_back(pm[d]);
+      }
+    pi.sigma = fc_.hasSigma ? fc_.sigma : 1.0;
+    pi.divu = fc_.hasDivu ? fc_.divu : 1.0;
+  }
   return FE_OK;
 }
 

@@ -11,6 +11,7 @@
 #include <memory>
 #include <vector>
 
+#include "fe_amg.h"
 #include "fe_device.h"
 #include "fe_krylov.h"
 #include "fe_setup.h"
@@ -29,6 +30,8 @@ struct SystemOptions {
   KrylovOptions kry;
   int pcBlockRows = 256;   // target rows per block-Jacobi block (0: a single block)
   int precision = 0;       // 0 FP64 matrix, 1 FP32 matrix + mixed Krylov
+  int mgInner = 0;         // multigrid: inner CG steps per component (0: one V-cycle)
+  int mgSmooth = 2;        // multigrid: Chebyshev degree
 };
 
 // Everything the backend needs from the set-up, in the original element order.
@@ -127,6 +130,7 @@ class SystemCUDA {
   bool matrixValid_ = false;
   int begin_phase();
   float end_phase();
+  int build_precond_info(const SystemTables &t, const RefTensors &T, HostCSR &lap, PrecondInfo &pi);
 };
 
 // Reference-element tensors of a quadrature rule (host, FP64).

@@ -98,10 +98,16 @@ typedef struct fe_cuda_options {
   double rel_tol;         /* ||b - A x||_2 <= max(rel_tol ||b||_2, abs_tol) */
   double abs_tol;
   double div_tol;
-  int32_t precond;        /* 0 none, 1 block-Jacobi ILU(0), 2 Jacobi */
+  int32_t precond;        /* 0 none, 1 block-Jacobi ILU(0), 2 Jacobi, 3 multigrid: AMG on the
+                             scalar P2 stiffness (scalar field) or block-triangular
+                             saddle-point preconditioner with AMG velocity blocks and
+                             lumped pressure mass Schur complement (Taylor-Hood) */
   int32_t pc_block_rows;  /* target rows per block-Jacobi block; 0 = one block (plain ILU(0)) */
   int32_t precision;      /* 0 FP64; 1 FP32 matrix, SpMV, preconditioner inside FP64 refinement */
   int32_t quad_degree;    /* triangle rule degree: 1, 2, 4, 5, 8 */
+  int32_t mg_inner;       /* multigrid: inner AMG-preconditioned CG steps per velocity
+                             component (0 = a single V-cycle) */
+  int32_t mg_smooth;      /* multigrid: Chebyshev smoother degree (1..6) */
 } fe_cuda_options;
 
 /* Newton options (feNLSolverOptions, src/feNonLinearSolver.h:12-40) plus the
@@ -219,6 +225,8 @@ int fe_cuda_set_residual_to_zero(fe_cuda_system *s);
 int fe_cuda_assemble_residuals(fe_cuda_system *s);
 int fe_cuda_assemble_matrices(fe_cuda_system *s);
 int fe_cuda_get_rhs_max_norm(fe_cuda_system *s, double *norm);
+/* setRelativeTol / setAbsoluteTol / setMaxIter (src/feLinearSystem.h:86-89). */
+int fe_cuda_set_tolerances(fe_cuda_system *s, double rel_tol, double abs_tol, int max_iter);
 /* Returns FE_CUDA_OK when converged (solve() -> true). */
 int fe_cuda_solve(fe_cuda_system *s, double *norm_dx, double *norm_rhs, double *norm_axb,
                   int *n_iter);

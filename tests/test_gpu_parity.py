@@ -64,6 +64,21 @@ def test_newton_converges_to_reference_solution(name, precision):
     assert rel_err(sol.u, g["usol"]) <= TOL_SOL
 
 
+@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_newton_multigrid_preconditioner(name, precision):
+    g = load_golden(name)
+    num, forms = problem_spaces(str(g["problem"]), golden_mesh(g), float(g["re"]))
+    krylov = "cg" if str(g["problem"]) == "diffusion" and precision == "fp64" else "fgmres"
+    opts = fe.LinearSolverOptions(krylov=krylov, precond="amg", precision=precision, rel_tol=1e-12)
+    sys = fe.createLinearSystem(fe.CUDA, forms, num, opts)
+    sol = fe.feSolution(sys)
+    sol.initializeEssentialBC()
+    st = fe.solveNewtonRaphson(sys, sol, fe.feNLSolverOptions(tolResidual=1e-12, tolCorrection=1e-14, maxIter=30))
+    assert st["return"] == 0, st
+    assert rel_err(sol.u, g["usol"]) <= TOL_SOL
+
+
 def test_kovasznay_block_jacobi_fgmres():
     g = load_golden("kovasznay_th_8")
     num, forms = problem_spaces("ns_kovasznay", golden_mesh(g), 40.0)
