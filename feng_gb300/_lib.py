@@ -121,6 +121,13 @@ SIGNATURES = {
                                     C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "fe_cuda_reset_times": (C.c_int, [P]),
     "fe_cuda_synchronize": (C.c_int, [P]),
+    "fe_cuda_bench_phase": (C.c_int, [P, C.c_int, C.c_int, C.c_int64, C.POINTER(C.c_double)]),
+    "fe_cuda_launch_count": (C.c_int, [C.POINTER(C.c_int64)]),
+    "fe_cuda_save_solution": (C.c_int, [P]),
+    "fe_cuda_restore_solution": (C.c_int, [P]),
+    "fe_cuda_event_record": (C.c_int, [P, C.c_int]),
+    "fe_cuda_event_elapsed": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    "fe_cuda_set_device": (C.c_int, [C.c_int]),
 }
 
 _lib = None

@@ -30,8 +30,9 @@ template <typename V, int LANES, int MODE>
 __global__ void __launch_bounds__(256) k_csr(int64_t n, const int32_t *__restrict__ ia,
                                              const int32_t *__restrict__ ja, const V *__restrict__ a,
                                              const V *__restrict__ x, const V *__restrict__ b,
-                                             V *__restrict__ y)
+                                             V *__restrict__ y, const int *__restrict__ skip)
 {
+  if(skip && *skip) return;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
   const int sub = threadIdx.x % LANES;
   const bool live = row < n;
@@ -49,19 +50,20 @@ __global__ void __launch_bounds__(256) k_csr(int64_t n, const int32_t *__restric
 
 template <typename V, int MODE>
 void csr(int lanes, int64_t n, const int32_t *ia, const int32_t *ja, const V *a, const V *x, const V *b,
-         V *y, cudaStream_t s)
+         V *y, cudaStream_t s, const int *skip)
 {
   const int g = grid(n * lanes);
-  if(lanes == 8) k_csr<V, 8, MODE><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y);
-  else if(lanes == 16) k_csr<V, 16, MODE><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y);
-  else k_csr<V, 4, MODE><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y);
+  if(lanes == 8) (k_csr<V, 8, MODE><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y, skip), ::feng::count_launch());
+  else if(lanes == 16) (k_csr<V, 16, MODE><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y, skip), ::feng::count_launch());
+  else (k_csr<V, 4, MODE><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y, skip), ::feng::count_launch());
 }
 
 // Chebyshev start (x = 0): r = D^-1 b, d = r / theta, x = 0.
 template <typename V>
 __global__ void k_cheb_start(int64_t n, const V *__restrict__ dinv, const V *__restrict__ b, V *__restrict__ r,
-                             V *__restrict__ d, V *__restrict__ x, V inv_theta)
+                             V *__restrict__ d, V *__restrict__ x, V inv_theta, const int *__restrict__ skip)
 {
+  if(skip && *skip) return;
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const V ri = dinv[i] * b[i];
     r[i] = ri;
@@ -76,8 +78,9 @@ __global__ void __launch_bounds__(256) k_cheb_restart(int64_t n, const int32_t *
                                                       const int32_t *__restrict__ ja, const V *__restrict__ a,
                                                       const V *__restrict__ dinv, const V *__restrict__ b,
                                                       const V *__restrict__ x, V *__restrict__ r,
-                                                      V *__restrict__ d, V inv_theta)
+                                                      V *__restrict__ d, V inv_theta, const int *__restrict__ skip)
 {
+  if(skip && *skip) return;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
   const int sub = threadIdx.x % LANES;
   const bool live = row < n;
@@ -99,8 +102,9 @@ __global__ void __launch_bounds__(256) k_cheb_step(int64_t n, const int32_t *__r
                                                    const int32_t *__restrict__ ja, const V *__restrict__ a,
                                                    const V *__restrict__ dinv, const V *__restrict__ d,
                                                    V *__restrict__ dn, V *__restrict__ r,
-                                                   V *__restrict__ x, V c1, V c2)
+                                                   V *__restrict__ x, V c1, V c2, const int *__restrict__ skip)
 {
+  if(skip && *skip) return;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
   const int sub = threadIdx.x % LANES;
   const bool live = row < n;
@@ -120,8 +124,10 @@ __global__ void __launch_bounds__(256) k_cheb_step(int64_t n, const int32_t *__r
 
 // x = Minv b for the coarsest level (dense, row-major), one warp per row.
 template <typename V>
-__global__ void k_dense(int64_t n, const V *__restrict__ M, const V *__restrict__ b, V *__restrict__ x)
+__global__ void k_dense(int64_t n, const V *__restrict__ M, const V *__restrict__ b, V *__restrict__ x,
+                        const int *__restrict__ skip)
 {
+  if(skip && *skip) return;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
   const int lane = threadIdx.x % 32;
   const bool live = row < n;
@@ -215,7 +221,7 @@ int AMGDevice::upload(const AMGHierarchy &H, const AMGParams &p, int fp32, cudaS
 template <typename V>
 static void chebyshev(int lanes, int64_t n, const int32_t *ia, const int32_t *ja, const V *a, const V *dinv,
                       const V *b, V *x, V *r, V *d0, V *d1, double lmax, const AMGParams &p, bool zeroStart,
-                      cudaStream_t s)
+                      cudaStream_t s, const int *skip)
 {
   // Chebyshev iteration on D^-1 A over [low, high] * lmax (Saad, Alg. 12.1).
   const double lo = p.chebyLow * lmax, hi = p.chebyHigh * lmax;
@@ -223,19 +229,19 @@ static void chebyshev(int lanes, int64_t n, const int32_t *ia, const int32_t *ja
   double rho = 1.0 / sigma;
   const int g = grid(n * lanes);
   if(zeroStart) {
-    k_cheb_start<V><<<grid(n), 256, 0, s>>>(n, dinv, b, r, d0, x, (V)(1.0 / theta));
+    (k_cheb_start<V><<<grid(n), 256, 0, s>>>(n, dinv, b, r, d0, x, (V)(1.0 / theta), skip), ::feng::count_launch());
   } else {
-    if(lanes == 16) k_cheb_restart<V, 16><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta));
-    else if(lanes == 8) k_cheb_restart<V, 8><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta));
-    else k_cheb_restart<V, 4><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta));
+    if(lanes == 16) (k_cheb_restart<V, 16><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip), ::feng::count_launch());
+    else if(lanes == 8) (k_cheb_restart<V, 8><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip), ::feng::count_launch());
+    else (k_cheb_restart<V, 4><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip), ::feng::count_launch());
   }
   V *d = d0, *dn = d1;
   for(int k = 0; k < p.chebyDegree; ++k) {
     const double rhoN = 1.0 / (2.0 * sigma - rho);
     const V c1 = (V)(rhoN * rho), c2 = (V)(2.0 * rhoN / delta);
-    if(lanes == 16) k_cheb_step<V, 16><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2);
-    else if(lanes == 8) k_cheb_step<V, 8><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2);
-    else k_cheb_step<V, 4><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2);
+    if(lanes == 16) (k_cheb_step<V, 16><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2, skip), ::feng::count_launch());
+    else if(lanes == 8) (k_cheb_step<V, 8><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2, skip), ::feng::count_launch());
+    else (k_cheb_step<V, 4><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2, skip), ::feng::count_launch());
     rho = rhoN;
     std::swap(d, dn);
   }
@@ -246,20 +252,20 @@ void AMGDevice::vcycle_t(int l, const V *b, V *x)
 {
   Lev &L = lv_[l];
   if(l == (int)lv_.size() - 1) {
-    k_dense<V><<<grid(L.n * 32), 256, 0, s_>>>(L.n, (const V *)coarseInv_, b, x);
+    (k_dense<V><<<grid(L.n * 32), 256, 0, s_>>>(L.n, (const V *)coarseInv_, b, x, skip_), ::feng::count_launch());
     return;
   }
   Lev &C = lv_[l + 1];
   const V *A = (const V *)L.Aa;
   chebyshev<V>(L.lanesA, L.n, L.Aia, L.Aja, A, (const V *)L.dinv, b, x, (V *)L.r, (V *)L.d0, (V *)L.d1,
-               L.lmax, p_, true, s_);
+               L.lmax, p_, true, s_, skip_);
   // residual r = b - A x, restrict into the coarse right-hand side
-  csr<V, 1>(L.lanesA, L.n, L.Aia, L.Aja, A, x, b, (V *)L.r, s_);
-  csr<V, 0>(L.lanesR, C.n, L.Ria, L.Rja, (const V *)L.Ra, (const V *)L.r, nullptr, (V *)C.b, s_);
+  csr<V, 1>(L.lanesA, L.n, L.Aia, L.Aja, A, x, b, (V *)L.r, s_, skip_);
+  csr<V, 0>(L.lanesR, C.n, L.Ria, L.Rja, (const V *)L.Ra, (const V *)L.r, nullptr, (V *)C.b, s_, skip_);
   vcycle_t<V>(l + 1, (const V *)C.b, (V *)C.x);
-  csr<V, 2>(L.lanesP, L.n, L.Pia, L.Pja, (const V *)L.Pa, (const V *)C.x, nullptr, x, s_);
+  csr<V, 2>(L.lanesP, L.n, L.Pia, L.Pja, (const V *)L.Pa, (const V *)C.x, nullptr, x, s_, skip_);
   chebyshev<V>(L.lanesA, L.n, L.Aia, L.Aja, A, (const V *)L.dinv, b, x, (V *)L.r, (V *)L.d0, (V *)L.d1,
-               L.lmax, p_, false, s_);
+               L.lmax, p_, false, s_, skip_);
 }
 
 void AMGDevice::vcycle64(const double *b, double *x) { vcycle_t<double>(0, b, x); }
@@ -268,13 +274,13 @@ void AMGDevice::vcycle32(const float *b, float *x) { vcycle_t<float>(0, b, x); }
 void AMGDevice::spmv64(const double *x, double *y)
 {
   const Lev &L = lv_[0];
-  csr<double, 0>(L.lanesA, L.n, L.Aia, L.Aja, (const double *)L.Aa, x, nullptr, y, s_);
+  csr<double, 0>(L.lanesA, L.n, L.Aia, L.Aja, (const double *)L.Aa, x, nullptr, y, s_, skip_);
 }
 
 void AMGDevice::spmv32(const float *x, float *y)
 {
   const Lev &L = lv_[0];
-  csr<float, 0>(L.lanesA, L.n, L.Aia, L.Aja, (const float *)L.Aa, x, nullptr, y, s_);
+  csr<float, 0>(L.lanesA, L.n, L.Aia, L.Aja, (const float *)L.Aa, x, nullptr, y, s_, skip_);
 }
 
 }  // namespace feng

@@ -82,6 +82,12 @@ class AMGDevice {
   AMGParams p_;
   double diagSum_ = 0;
   cudaStream_t s_ = 0;
+  const int *skip_ = nullptr;
+
+ public:
+  // Device flag: when set (nonzero) every kernel of the V-cycle returns at
+  // once (a converged Krylov cycle replayed from a CUDA graph).
+  void setSkip(const int *skip) { skip_ = skip; }
 };
 
 }  // namespace feng

@@ -25,6 +25,7 @@
 // regrouped: they agree to rounding.
 #include <cuda_runtime.h>
 
+#include "fe_common.h"
 #include "fe_device.h"
 
 namespace feng {
@@ -454,10 +455,10 @@ void launch_assemble_residual(const DeviceMesh &dm, const FormCoeffs &fc, const 
   if(end <= begin) return;
   dim3 block(EPB, 6);
   if(fc.elemType == 1)
-    k_residual_p2<<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, u, t, nInc, rhs, begin, end);
+    (k_residual_p2<<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, u, t, nInc, rhs, begin, end), ::feng::count_launch());
   else
-    k_residual_th<<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, u, udot, t, nInc, rhs, begin,
-                                                        end);
+    (k_residual_th<<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, u, udot, t, nInc, rhs, begin,
+                                                        end), ::feng::count_launch());
 }
 
 void launch_assemble_matrix_f64(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
@@ -467,9 +468,9 @@ void launch_assemble_matrix_f64(const DeviceMesh &dm, const FormCoeffs &fc, cons
   if(end <= begin) return;
   dim3 block(EPB, 6);
   if(fc.elemType == 1)
-    k_matrix_p2<double><<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, values, begin, end);
+    (k_matrix_p2<double><<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, values, begin, end), ::feng::count_launch());
   else
-    k_matrix_th<double><<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, u, c0, values, begin, end);
+    (k_matrix_th<double><<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, u, c0, values, begin, end), ::feng::count_launch());
 }
 
 void launch_assemble_matrix_f32(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
@@ -479,9 +480,9 @@ void launch_assemble_matrix_f32(const DeviceMesh &dm, const FormCoeffs &fc, cons
   if(end <= begin) return;
   dim3 block(EPB, 6);
   if(fc.elemType == 1)
-    k_matrix_p2<float><<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, values, begin, end);
+    (k_matrix_p2<float><<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, values, begin, end), ::feng::count_launch());
   else
-    k_matrix_th<float><<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, u, c0, values, begin, end);
+    (k_matrix_th<float><<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, u, c0, values, begin, end), ::feng::count_launch());
 }
 
 }  // namespace feng

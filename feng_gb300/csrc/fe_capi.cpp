@@ -28,6 +28,8 @@ void set_error(const char *fmt, ...)
   g_err = buf;
 }
 const char *last_error() { return g_err.c_str(); }
+std::atomic<long long> g_launches{0};
+thread_local int g_capturing = 0;
 }  // namespace feng
 
 using namespace feng;
@@ -38,6 +40,14 @@ struct fe_mesh {
 
 struct fe_cuda_system {
   SystemCUDA sys;
+  double *saved = nullptr;
+  cudaEvent_t ev[8] = {};
+  ~fe_cuda_system()
+  {
+    cudaFree(saved);
+    for(auto e : ev)
+      if(e) cudaEventDestroy(e);
+  }
 };
 
 struct fe_setup {
@@ -615,6 +625,85 @@ int fe_cuda_reset_times(fe_cuda_system *s)
 {
   if(!s) { set_error("null system"); return FE_INVALID_ARG; }
   s->sys.times = PhaseTimes();
+  return FE_OK;
+}
+
+int fe_cuda_bench_phase(fe_cuda_system *s, int which, int reps, int64_t flush_bytes, double *avg_ms)
+{
+  if(!s || !avg_ms || flush_bytes < 0) { set_error("invalid argument"); return FE_INVALID_ARG; }
+  return s->sys.benchPhase(which, reps, (size_t)flush_bytes, avg_ms);
+}
+
+int fe_cuda_save_solution(fe_cuda_system *s)
+{
+  if(!s) { set_error("null system"); return FE_INVALID_ARG; }
+  const size_t bytes = sizeof(double) * s->sys.nDofs();
+  if(!s->saved && cudaMalloc(&s->saved, bytes) != cudaSuccess) {
+    set_error("device allocation failed");
+    return FE_CUDA_DEVICE_FAIL;
+  }
+  if(cudaMemcpyAsync(s->saved, s->sys.dU(), bytes, cudaMemcpyDeviceToDevice, s->sys.stream()) != cudaSuccess) {
+    set_error("device copy failed");
+    return FE_CUDA_DEVICE_FAIL;
+  }
+  return FE_OK;
+}
+
+int fe_cuda_restore_solution(fe_cuda_system *s)
+{
+  if(!s || !s->saved) { set_error("no saved solution"); return FE_INVALID_ARG; }
+  if(cudaMemcpyAsync(s->sys.dU(), s->saved, sizeof(double) * s->sys.nDofs(), cudaMemcpyDeviceToDevice,
+                     s->sys.stream()) != cudaSuccess) {
+    set_error("device copy failed");
+    return FE_CUDA_DEVICE_FAIL;
+  }
+  return FE_OK;
+}
+
+int fe_cuda_event_record(fe_cuda_system *s, int slot)
+{
+  if(!s || slot < 0 || slot > 7) { set_error("invalid event slot"); return FE_INVALID_ARG; }
+  if(!s->ev[slot] && cudaEventCreate(&s->ev[slot]) != cudaSuccess) {
+    set_error("event creation failed");
+    return FE_CUDA_DEVICE_FAIL;
+  }
+  if(cudaEventRecord(s->ev[slot], s->sys.stream()) != cudaSuccess) {
+    set_error("event record failed");
+    return FE_CUDA_DEVICE_FAIL;
+  }
+  return FE_OK;
+}
+
+int fe_cuda_event_elapsed(fe_cuda_system *s, int slot0, int slot1, double *ms)
+{
+  if(!s || !ms || slot0 < 0 || slot0 > 7 || slot1 < 0 || slot1 > 7 || !s->ev[slot0] || !s->ev[slot1]) {
+    set_error("invalid event slots");
+    return FE_INVALID_ARG;
+  }
+  float f = 0.f;
+  if(cudaEventSynchronize(s->ev[slot1]) != cudaSuccess ||
+     cudaEventElapsedTime(&f, s->ev[slot0], s->ev[slot1]) != cudaSuccess) {
+    set_error("event timing failed");
+    return FE_CUDA_DEVICE_FAIL;
+  }
+  *ms = f;
+  return FE_OK;
+}
+
+int fe_cuda_set_device(int device)
+{
+  if(cudaSetDevice(device) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cudaSetDevice(%d) failed", device);
+    return FE_CUDA_DEVICE_FAIL;
+  }
+  return FE_OK;
+}
+
+int fe_cuda_launch_count(int64_t *count)
+{
+  if(!count) { set_error("null argument"); return FE_INVALID_ARG; }
+  *count = g_launches.load();
   return FE_OK;
 }
 

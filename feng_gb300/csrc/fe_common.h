@@ -3,6 +3,7 @@
 // 0 is success, negative values are errors.
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -25,6 +26,15 @@ enum Status : int {
 // Last error message of the calling thread (read through fe_last_error()).
 void set_error(const char *fmt, ...);
 const char *last_error();
+
+// Count of the library's kernel launches (graph replays add their kernel
+// nodes); launches recorded while a stream is being captured are not counted.
+extern std::atomic<long long> g_launches;
+extern thread_local int g_capturing;
+inline void count_launch()
+{
+  if(!g_capturing) g_launches.fetch_add(1, std::memory_order_relaxed);
+}
 
 #define FE_TRY(expr)                   \
   do {                                 \

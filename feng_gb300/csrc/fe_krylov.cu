@@ -241,15 +241,17 @@ __global__ void k_to_f32(int64_t n, const double *__restrict__ x, float *__restr
 
 // Givens rotations on Hessenberg column j (device, one thread).  H is stored
 // column-major with leading dimension MAXM+1.
-struct GmresState {
-  double H[MAXM * (MAXM + 1)];
-  double cs[MAXM], sn[MAXM], g[MAXM + 1], y[MAXM];
-  double hcur[MAXM + 1];
-  double beta;    // ||r|| at the start of the cycle
+struct GmresHead {
   int done;       // set once the estimate reaches tol or on breakdown
   int k;          // number of basis vectors in use
   double est;     // |g[k]|: residual norm estimate
   double tol;
+  double beta;    // ||r|| at the start of the cycle
+};
+struct GmresState : GmresHead {
+  double H[MAXM * (MAXM + 1)];
+  double cs[MAXM], sn[MAXM], g[MAXM + 1], y[MAXM];
+  double hcur[MAXM + 1];
 };
 
 __global__ void k_givens(GmresState *gs, int j)
@@ -303,15 +305,15 @@ __global__ void k_xupdate(int64_t n, const VZ *__restrict__ Z, const GmresState 
   }
 }
 
-__global__ void k_gmres_init(GmresState *gs, const RedState *st, double tol)
+__global__ void k_gmres_init(GmresState *gs, const RedState *st)
 {
   const double beta = sqrt(st->result[0]);
+  const double tol = gs->tol;
   gs->g[0] = beta;
   for(int i = 1; i <= MAXM; ++i) gs->g[i] = 0.;
   gs->done = (beta <= tol || !isfinite(beta)) ? 1 : 0;
   gs->k = 0;
   gs->est = beta;
-  gs->tol = tol;
 }
 
 // ---------------------------------------------------------------------------
@@ -519,7 +521,8 @@ Krylov::~Krylov()
   cudaFree(ilu_.blockStart); cudaFree(ilu_.perm); cudaFree(ilu_.lia); cudaFree(ilu_.lja);
   cudaFree(ilu_.ldiag); cudaFree(ilu_.srcPos); cudaFree(ilu_.vals); cudaFree(ilu_.status);
   cudaFree(red_state_); cudaFree(gmres_); cudaFree(cg_);
-  cudaFreeHost(h_gmres_); cudaFreeHost(h_cg_); cudaFreeHost(hflag_);
+  cudaFreeHost(h_gmres_); cudaFreeHost(h_cg_); cudaFreeHost(hflag_); cudaFreeHost(htol_);
+  for(auto &g : graphs_) cudaGraphExecDestroy(g.second);
   delete mg_;
 }
 
@@ -564,14 +567,11 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
   CK(cudaMalloc(&q_, sizeof(double) * n_));
   if(opt.method == 1) {
     CK(cudaMalloc(&V_, sizeof(double) * n_ * (m + 1)));
-    if(opt.mixed) {
-      CK(cudaMalloc(&Z32_, sizeof(float) * n_ * m));
-      CK(cudaMalloc(&v32_, sizeof(float) * n_));
-      CK(cudaMalloc(&w32_, sizeof(float) * n_));
-    } else {
-      CK(cudaMalloc(&Z_, sizeof(double) * n_ * m));
-    }
+    if(opt.mixed) CK(cudaMalloc(&Z32_, sizeof(float) * n_ * m));
+    else CK(cudaMalloc(&Z_, sizeof(double) * n_ * m));
   }
+  CK(cudaMalloc(&v32_, sizeof(float) * n_));
+  CK(cudaMalloc(&w32_, sizeof(float) * n_));
   CK(cudaMalloc(&red_state_, sizeof(RedState)));
   CK(cudaMemset(red_state_, 0, sizeof(RedState)));
   CK(cudaMalloc(&gmres_, sizeof(GmresState)));
@@ -581,6 +581,7 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
   CK(cudaMallocHost(&h_gmres_, sizeof(GmresState)));
   CK(cudaMallocHost(&h_cg_, sizeof(CGState)));
   CK(cudaMallocHost(&hflag_, sizeof(int)));
+  CK(cudaMallocHost(&htol_, sizeof(double)));
 
   if(opt.precond == 3 || opt.precond == 4) {
     if(!pinfo) {
@@ -665,18 +666,18 @@ int Krylov::factor(const double *values64, const float *values32)
   CK(cudaMemsetAsync(ilu_.status, 0, sizeof(int), s_));
   if(opt.precond == 2) {
     const int g = grid_for(n_, 256, 4096);
-    if(opt.mixed) k_inv_diag<float, float><<<g, 256, 0, s_>>>(n_, A_.diag, values32, diag32_, ilu_.status);
-    else k_inv_diag<double, double><<<g, 256, 0, s_>>>(n_, A_.diag, values64, diag_, ilu_.status);
+    if(opt.mixed) (k_inv_diag<float, float><<<g, 256, 0, s_>>>(n_, A_.diag, values32, diag32_, ilu_.status), ::feng::count_launch());
+    else (k_inv_diag<double, double><<<g, 256, 0, s_>>>(n_, A_.diag, values64, diag_, ilu_.status), ::feng::count_launch());
   } else {
     const int g = grid_for(ilu_.nBlocks, 64, 1 << 20);
     if(opt.mixed)
-      k_ilu_factor<float><<<g, 64, 0, s_>>>(ilu_.nBlocks, ilu_.blockStart, ilu_.perm, ilu_.lia,
+      (k_ilu_factor<float><<<g, 64, 0, s_>>>(ilu_.nBlocks, ilu_.blockStart, ilu_.perm, ilu_.lia,
                                             ilu_.lja, ilu_.ldiag, ilu_.srcPos, nullptr, values32,
-                                            (float *)ilu_.vals, ilu_.status);
+                                            (float *)ilu_.vals, ilu_.status), ::feng::count_launch());
     else
-      k_ilu_factor<double><<<g, 64, 0, s_>>>(ilu_.nBlocks, ilu_.blockStart, ilu_.perm, ilu_.lia,
+      (k_ilu_factor<double><<<g, 64, 0, s_>>>(ilu_.nBlocks, ilu_.blockStart, ilu_.perm, ilu_.lia,
                                              ilu_.lja, ilu_.ldiag, ilu_.srcPos, values64, nullptr,
-                                             (double *)ilu_.vals, ilu_.status);
+                                             (double *)ilu_.vals, ilu_.status), ::feng::count_launch());
   }
   CK(cudaGetLastError());
   int hs = 0;
@@ -697,11 +698,11 @@ void Krylov::precond64(const double *r, double *z, const int *done)
   } else if(opt.precond >= 3) {
     apply_mg<double>(cur64_, r, z, done);
   } else if(opt.precond == 2) {
-    k_jacobi<double, double><<<grid_for(n_, 256, 4096), 256, 0, s_>>>(n_, diag_, r, z, done);
+    (k_jacobi<double, double><<<grid_for(n_, 256, 4096), 256, 0, s_>>>(n_, diag_, r, z, done), ::feng::count_launch());
   } else {
-    k_ilu_solve<double, double><<<grid_for(ilu_.nBlocks, 64, 1 << 20), 64, 0, s_>>>(
+    (k_ilu_solve<double, double><<<grid_for(ilu_.nBlocks, 64, 1 << 20), 64, 0, s_>>>(
       ilu_.nBlocks, ilu_.blockStart, ilu_.perm, ilu_.lia, ilu_.lja, ilu_.ldiag,
-      (const double *)ilu_.vals, r, z, done);
+      (const double *)ilu_.vals, r, z, done), ::feng::count_launch());
   }
 }
 
@@ -712,11 +713,11 @@ void Krylov::precond32(const float *r, float *z, const int *done)
   } else if(opt.precond >= 3) {
     apply_mg<float>(cur32_, r, z, done);
   } else if(opt.precond == 2) {
-    k_jacobi<float, float><<<grid_for(n_, 256, 4096), 256, 0, s_>>>(n_, diag32_, r, z, done);
+    (k_jacobi<float, float><<<grid_for(n_, 256, 4096), 256, 0, s_>>>(n_, diag32_, r, z, done), ::feng::count_launch());
   } else {
-    k_ilu_solve<float, float><<<grid_for(ilu_.nBlocks, 64, 1 << 20), 64, 0, s_>>>(
+    (k_ilu_solve<float, float><<<grid_for(ilu_.nBlocks, 64, 1 << 20), 64, 0, s_>>>(
       ilu_.nBlocks, ilu_.blockStart, ilu_.perm, ilu_.lia, ilu_.lja, ilu_.ldiag,
-      (const float *)ilu_.vals, r, z, done);
+      (const float *)ilu_.vals, r, z, done), ::feng::count_launch());
   }
 }
 
@@ -727,9 +728,9 @@ static void spmv_launch(int lanes, int64_t n, const DeviceCSR &A, const VA *a, c
   const int64_t threads = n * lanes;
   const int grid = (int)((threads + 255) / 256);
   if(lanes == 8)
-    k_spmv<VA, VX, VY, ACC, 8, RESID><<<grid, 256, 0, s>>>(n, A.ia, A.ja, a, x, b, y, done);
+    (k_spmv<VA, VX, VY, ACC, 8, RESID><<<grid, 256, 0, s>>>(n, A.ia, A.ja, a, x, b, y, done), ::feng::count_launch());
   else
-    k_spmv<VA, VX, VY, ACC, 4, RESID><<<grid, 256, 0, s>>>(n, A.ia, A.ja, a, x, b, y, done);
+    (k_spmv<VA, VX, VY, ACC, 4, RESID><<<grid, 256, 0, s>>>(n, A.ia, A.ja, a, x, b, y, done), ::feng::count_launch());
 }
 
 void Krylov::spmv64(const double *values, const double *x, double *y)
@@ -738,10 +739,33 @@ void Krylov::spmv64(const double *values, const double *x, double *y)
                                                      nullptr, s_);
 }
 
+void Krylov::spmv32(const float *values, const double *x, double *y)
+{
+  const int gv = grid_for(n_, 256, 2048);
+  (k_to_f32<<<gv, 256, 0, s_>>>(n_, x, v32_, nullptr), ::feng::count_launch());
+  spmv_launch<float, float, double, float, false>(lanes_, n_, A_, values, v32_, nullptr, y, nullptr, s_);
+}
+
+int Krylov::applyPrecond(const double *r, double *z)
+{
+  if(!factoredOk_) {
+    set_error("preconditioner not built");
+    return FE_PC_FAILED;
+  }
+  if(opt.mixed) {
+    const int gv = grid_for(n_, 256, 2048);
+    (k_to_f32<<<gv, 256, 0, s_>>>(n_, r, v32_, nullptr), ::feng::count_launch());
+    precond32(v32_, Z32_ ? Z32_ : w32_, nullptr);
+  } else {
+    precond64(r, z, nullptr);
+  }
+  return FE_OK;
+}
+
 double Krylov::dot(const double *x, const double *y)
 {
   Ws w = Ws_INIT(this);
-  k_dot<<<nParts_, RB, 0, s_>>>(n_, x, y, red_, w.st, dsum_);
+  (k_dot<<<nParts_, RB, 0, s_>>>(n_, x, y, red_, w.st, dsum_), ::feng::count_launch());
   cudaMemcpyAsync(hred_, dsum_, sizeof(double), cudaMemcpyDeviceToHost, s_);
   cudaStreamSynchronize(s_);
   return hred_[0];
@@ -752,61 +776,127 @@ double Krylov::norm2(const double *x) { return sqrt(dot(x, x)); }
 double Krylov::norminf(const double *x)
 {
   Ws w = Ws_INIT(this);
-  k_absmax<<<nParts_, RB, 0, s_>>>(n_, x, red_, w.st, dsum_);
+  (k_absmax<<<nParts_, RB, 0, s_>>>(n_, x, red_, w.st, dsum_), ::feng::count_launch());
   cudaMemcpyAsync(hred_, dsum_, sizeof(double), cudaMemcpyDeviceToHost, s_);
   cudaStreamSynchronize(s_);
   return hred_[0];
 }
 
 // FGMRES(m), right preconditioned, FP64 throughout (Saad Alg. 9.6).
+// One FGMRES(m) restart cycle (Saad Alg. 9.6): r = b - A x, V_0 = r/||r||,
+// then up to jmax Arnoldi steps with right preconditioning z_j = M^-1 v_j,
+// classical Gram-Schmidt applied twice, Givens rotations on the device.
+// Every kernel after convergence is skipped through the device done flag,
+// so the same launch sequence can be replayed from a CUDA graph.
+void Krylov::launch_cycle(bool mixed, const void *vals, const double *b, double *x, int jmax, bool poll)
+{
+  Ws w = Ws_INIT(this);
+  const int gv = grid_for(n_, 256, 2048);
+  if(mixed)
+    spmv_launch<float, double, double, double, true>(lanes_, n_, A_, (const float *)vals, x, b, w_, nullptr, s_);
+  else
+    spmv_launch<double, double, double, double, true>(lanes_, n_, A_, (const double *)vals, x, b, w_, nullptr, s_);
+  cudaMemsetAsync(&w.gs->done, 0, sizeof(int), s_);
+  cudaMemcpyAsync(&w.gs->tol, htol_, sizeof(double), cudaMemcpyHostToDevice, s_);
+  (k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done), ::feng::count_launch());
+  (k_gmres_init<<<1, 1, 0, s_>>>(w.gs, w.st), ::feng::count_launch());
+  (k_scale_from<<<gv, 256, 0, s_>>>(n_, w_, V_, w.st, &w.gs->beta, &w.gs->done), ::feng::count_launch());
+  for(int j = 0; j < jmax; ++j) {
+    double *vj = V_ + (int64_t)j * n_;
+    if(mixed) {
+      float *zj = Z32_ + (int64_t)j * n_;
+      (k_to_f32<<<gv, 256, 0, s_>>>(n_, vj, v32_, &w.gs->done), ::feng::count_launch());
+      precond32(v32_, zj, &w.gs->done);
+      spmv_launch<float, float, double, float, false>(lanes_, n_, A_, (const float *)vals, zj, nullptr, w_,
+                                                      &w.gs->done, s_);
+    } else {
+      double *zj = Z_ + (int64_t)j * n_;
+      precond64(vj, zj, &w.gs->done);
+      spmv_launch<double, double, double, double, false>(lanes_, n_, A_, (const double *)vals, zj, nullptr,
+                                                         w_, &w.gs->done, s_);
+    }
+    double *Hcol = w.gs->H + (int64_t)j * (MAXM + 1);
+    for(int pass = 0; pass < 2; ++pass) {
+      (k_mdot_partial<<<dim3(nParts_, j + 1), RB, 0, s_>>>(n_, V_, j + 1, w_, red_, &w.gs->done), ::feng::count_launch());
+      (k_mdot_final<<<j + 1, RB, 0, s_>>>(nParts_, red_, w.gs->hcur, Hcol, pass, &w.gs->done), ::feng::count_launch());
+      (k_mupdate<<<gv, 256, 0, s_>>>(n_, V_, j + 1, w.gs->hcur, w_, &w.gs->done), ::feng::count_launch());
+    }
+    (k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done), ::feng::count_launch());
+    (k_scale_from<<<gv, 256, 0, s_>>>(n_, w_, V_ + (int64_t)(j + 1) * n_, w.st, Hcol + j + 1, &w.gs->done), ::feng::count_launch());
+    (k_givens<<<1, 1, 0, s_>>>(w.gs, j), ::feng::count_launch());
+    if(poll && poll_done(&w.gs->done, j)) break;
+  }
+  (k_backsolve<<<1, 1, 0, s_>>>(w.gs), ::feng::count_launch());
+  if(mixed) (k_xupdate<float><<<gv, 256, 0, s_>>>(n_, Z32_, w.gs, x), ::feng::count_launch());
+  else (k_xupdate<double><<<gv, 256, 0, s_>>>(n_, Z_, w.gs, x), ::feng::count_launch());
+  cudaMemcpyAsync(h_gmres_, w.gs, sizeof(GmresHead), cudaMemcpyDeviceToHost, s_);
+}
+
+// Runs one full restart cycle, from a CUDA graph when the cycle has its full
+// length (the graph is captured once per operand set and replayed).
+int Krylov::run_cycle(bool mixed, const void *vals, const double *b, double *x, int jmax)
+{
+  const int m = opt.restart;
+  if(useGraphs_ && jmax == m) {
+    GraphKey key{mixed, vals, b, x};
+    cudaGraphExec_t exec = nullptr;
+    for(auto &g : graphs_)
+      if(g.first.mixed == key.mixed && g.first.vals == key.vals && g.first.b == key.b && g.first.x == key.x)
+        exec = g.second;
+    size_t nKernels = 0;
+    if(!exec) {
+      cudaGraph_t graph;
+      CK(cudaStreamBeginCapture(s_, cudaStreamCaptureModeThreadLocal));
+      ++g_capturing;
+      launch_cycle(mixed, vals, b, x, m, false);
+      --g_capturing;
+      CK(cudaStreamEndCapture(s_, &graph));
+      CK(cudaGraphInstantiate(&exec, graph, 0));
+      size_t nn = 0;
+      CK(cudaGraphGetNodes(graph, nullptr, &nn));
+      std::vector<cudaGraphNode_t> nodes(nn);
+      CK(cudaGraphGetNodes(graph, nodes.data(), &nn));
+      for(auto nd : nodes) {
+        cudaGraphNodeType t;
+        CK(cudaGraphNodeGetType(nd, &t));
+        if(t == cudaGraphNodeTypeKernel) ++nKernels;
+      }
+      cudaGraphDestroy(graph);
+      graphs_.push_back({key, exec});
+      graphKernels_.push_back(nKernels);
+    } else {
+      for(size_t i = 0; i < graphs_.size(); ++i)
+        if(graphs_[i].second == exec) nKernels = graphKernels_[i];
+    }
+    CK(cudaGraphLaunch(exec, s_));
+    g_launches.fetch_add((long long)nKernels, std::memory_order_relaxed);
+  } else {
+    launch_cycle(mixed, vals, b, x, jmax, true);
+  }
+  CK(cudaStreamSynchronize(s_));
+  CK(cudaGetLastError());
+  return FE_OK;
+}
+
 int Krylov::solve_fgmres64(const double *vals, const double *b, double *x, double tolAbs, int maxIt,
                            KrylovStats &st)
 {
-  Ws w = Ws_INIT(this);
-  const int m = opt.restart;
-  const int gv = grid_for(n_, 256, 2048);
+  const GmresHead *hd = (const GmresHead *)h_gmres_;
   int total = 0;
+  *htol_ = tolAbs;
   while(true) {
-    // r = b - A x  -> V_0 = r / ||r||
-    spmv_launch<double, double, double, double, true>(lanes_, n_, A_, vals, x, b, w_, nullptr, s_);
-    cudaMemsetAsync(&w.gs->done, 0, sizeof(int), s_);
-    k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done);
-    k_gmres_init<<<1, 1, 0, s_>>>(w.gs, w.st, tolAbs);
-    k_scale_from<<<gv, 256, 0, s_>>>(n_, w_, V_, w.st, &w.gs->beta, &w.gs->done);
-    const int jmax = std::min(m, maxIt - total);
-    for(int j = 0; j < jmax; ++j) {
-      double *vj = V_ + (int64_t)j * n_, *zj = Z_ + (int64_t)j * n_;
-      precond64(vj, zj, &w.gs->done);
-      spmv_launch<double, double, double, double, false>(lanes_, n_, A_, vals, zj, nullptr, w_,
-                                                         &w.gs->done, s_);
-      double *Hcol = w.gs->H + (int64_t)j * (MAXM + 1);
-      for(int pass = 0; pass < 2; ++pass) {
-        k_mdot_partial<<<dim3(nParts_, j + 1), RB, 0, s_>>>(n_, V_, j + 1, w_, red_, &w.gs->done);
-        k_mdot_final<<<j + 1, RB, 0, s_>>>(nParts_, red_, w.gs->hcur, Hcol, pass, &w.gs->done);
-        k_mupdate<<<gv, 256, 0, s_>>>(n_, V_, j + 1, w.gs->hcur, w_, &w.gs->done);
-      }
-      k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done);
-      k_scale_from<<<gv, 256, 0, s_>>>(n_, w_, V_ + (int64_t)(j + 1) * n_, w.st, Hcol + j + 1,
-                                       &w.gs->done);
-      k_givens<<<1, 1, 0, s_>>>(w.gs, j);
-      if(poll_done(&w.gs->done, j)) break;
-    }
-    k_backsolve<<<1, 1, 0, s_>>>(w.gs);
-    k_xupdate<double><<<gv, 256, 0, s_>>>(n_, Z_, w.gs, x);
-    cudaMemcpyAsync(w.hgs, w.gs, sizeof(GmresState), cudaMemcpyDeviceToHost, s_);
-    CK(cudaStreamSynchronize(s_));
-    CK(cudaGetLastError());
-    total += w.hgs->k;
+    FE_TRY(run_cycle(false, vals, b, x, std::min(opt.restart, maxIt - total)));
+    total += hd->k;
     st.iterations = total;
-    st.rnorm = w.hgs->est;
-    if(!std::isfinite(w.hgs->est)) { set_error("non-finite residual in FGMRES"); return FE_NONFINITE; }
-    if(w.hgs->est <= tolAbs) break;
-    if(total >= maxIt || w.hgs->k == 0) break;
-    if(w.hgs->est > opt.dtol * std::max(st.rnorm0, 1e-300)) { set_error("FGMRES diverged"); return FE_NOT_CONVERGED; }
+    st.rnorm = hd->est;
+    if(!std::isfinite(hd->est)) { set_error("non-finite residual in FGMRES"); return FE_NONFINITE; }
+    if(hd->est <= tolAbs) break;
+    if(total >= maxIt || hd->k == 0) break;
+    if(hd->est > opt.dtol * std::max(st.rnorm0, 1e-300)) { set_error("FGMRES diverged"); return FE_NOT_CONVERGED; }
   }
   // Converged on the Arnoldi estimate (as PETSc's default test); report the
   // true residual alongside.
-  const bool conv = w.hgs->est <= tolAbs;
+  const bool conv = hd->est <= tolAbs;
   spmv_launch<double, double, double, double, true>(lanes_, n_, A_, vals, x, b, w_, nullptr, s_);
   st.rnorm = norm2(w_);
   return conv ? FE_OK : FE_NOT_CONVERGED;
@@ -818,50 +908,20 @@ int Krylov::solve_fgmres64(const double *vals, const double *b, double *x, doubl
 int Krylov::solve_fgmres_mixed(const float *vals32, const double *b, double *x, double tolAbs,
                                int maxIt, KrylovStats &st)
 {
-  Ws w = Ws_INIT(this);
-  const int m = opt.restart;
-  const int gv = grid_for(n_, 256, 2048);
+  const GmresHead *hd = (const GmresHead *)h_gmres_;
   int total = 0;
+  *htol_ = tolAbs;
   while(true) {
-    spmv_launch<float, double, double, double, true>(lanes_, n_, A_, vals32, x, b, w_, nullptr, s_);
-    cudaMemsetAsync(&w.gs->done, 0, sizeof(int), s_);
-    k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done);
-    k_gmres_init<<<1, 1, 0, s_>>>(w.gs, w.st, tolAbs);
-    k_scale_from<<<gv, 256, 0, s_>>>(n_, w_, V_, w.st, &w.gs->beta, &w.gs->done);
+    FE_TRY(run_cycle(true, vals32, b, x, std::min(opt.restart, maxIt - total)));
     st.refinements++;
-    const int jmax = std::min(m, maxIt - total);
-    for(int j = 0; j < jmax; ++j) {
-      double *vj = V_ + (int64_t)j * n_;
-      float *zj = Z32_ + (int64_t)j * n_;
-      k_to_f32<<<gv, 256, 0, s_>>>(n_, vj, v32_, &w.gs->done);
-      precond32(v32_, zj, &w.gs->done);
-      spmv_launch<float, float, double, float, false>(lanes_, n_, A_, vals32, zj, nullptr, w_,
-                                                      &w.gs->done, s_);
-      double *Hcol = w.gs->H + (int64_t)j * (MAXM + 1);
-      for(int pass = 0; pass < 2; ++pass) {
-        k_mdot_partial<<<dim3(nParts_, j + 1), RB, 0, s_>>>(n_, V_, j + 1, w_, red_, &w.gs->done);
-        k_mdot_final<<<j + 1, RB, 0, s_>>>(nParts_, red_, w.gs->hcur, Hcol, pass, &w.gs->done);
-        k_mupdate<<<gv, 256, 0, s_>>>(n_, V_, j + 1, w.gs->hcur, w_, &w.gs->done);
-      }
-      k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done);
-      k_scale_from<<<gv, 256, 0, s_>>>(n_, w_, V_ + (int64_t)(j + 1) * n_, w.st, Hcol + j + 1,
-                                       &w.gs->done);
-      k_givens<<<1, 1, 0, s_>>>(w.gs, j);
-      if(poll_done(&w.gs->done, j)) break;
-    }
-    k_backsolve<<<1, 1, 0, s_>>>(w.gs);
-    k_xupdate<float><<<gv, 256, 0, s_>>>(n_, Z32_, w.gs, x);
-    cudaMemcpyAsync(w.hgs, w.gs, sizeof(GmresState), cudaMemcpyDeviceToHost, s_);
-    CK(cudaStreamSynchronize(s_));
-    CK(cudaGetLastError());
-    total += w.hgs->k;
+    total += hd->k;
     st.iterations = total;
-    if(!std::isfinite(w.hgs->est)) { set_error("non-finite residual in mixed FGMRES"); return FE_NONFINITE; }
+    if(!std::isfinite(hd->est)) { set_error("non-finite residual in mixed FGMRES"); return FE_NONFINITE; }
     // Refinement check on the true residual.
     spmv_launch<float, double, double, double, true>(lanes_, n_, A_, vals32, x, b, w_, nullptr, s_);
     st.rnorm = norm2(w_);
     if(st.rnorm <= tolAbs) break;
-    if(total >= maxIt || w.hgs->k == 0) break;
+    if(total >= maxIt || hd->k == 0) break;
     if(st.rnorm > opt.dtol * std::max(st.rnorm0, 1e-300)) { set_error("mixed FGMRES diverged"); return FE_NOT_CONVERGED; }
   }
   return st.rnorm <= tolAbs * 1.0000001 + 1e-300 ? FE_OK : FE_NOT_CONVERGED;
@@ -875,31 +935,31 @@ int Krylov::solve_cg64(const double *vals, const double *b, double *x, double to
   Ws w = Ws_INIT(this);
   const int gv = grid_for(n_, 256, 2048);
   // x = 0, r = b
-  k_zero<<<gv, 256, 0, s_>>>(n_, x);
-  k_copy<<<gv, 256, 0, s_>>>(n_, b, r_);
+  (k_zero<<<gv, 256, 0, s_>>>(n_, x), ::feng::count_launch());
+  (k_copy<<<gv, 256, 0, s_>>>(n_, b, r_), ::feng::count_launch());
   CGState init{};
   init.tol = tolAbs;
   init.done = 0;
   cudaMemcpyAsync(w.cg, &init, sizeof(CGState), cudaMemcpyHostToDevice, s_);
   // z = M r ; rz = r.z ; p = z
   precond64(r_, t_, &w.cg->done);
-  k_dot_if<<<nParts_, RB, 0, s_>>>(n_, r_, t_, red_, w.st, w.cg);
-  k_cg_p<<<gv, 256, 0, s_>>>(n_, w.cg, w.st, t_, p_, 1);
-  k_cg_rz<<<1, 1, 0, s_>>>(w.cg, w.st);
+  (k_dot_if<<<nParts_, RB, 0, s_>>>(n_, r_, t_, red_, w.st, w.cg), ::feng::count_launch());
+  (k_cg_p<<<gv, 256, 0, s_>>>(n_, w.cg, w.st, t_, p_, 1), ::feng::count_launch());
+  (k_cg_rz<<<1, 1, 0, s_>>>(w.cg, w.st), ::feng::count_launch());
   int it = 0;
   while(it < maxIt) {
     const int batch = std::min(8, maxIt - it);
     for(int k = 0; k < batch; ++k) {
       spmv_launch<double, double, double, double, false>(lanes_, n_, A_, vals, p_, nullptr, q_,
                                                          &w.cg->done, s_);
-      k_dot_if<<<nParts_, RB, 0, s_>>>(n_, p_, q_, red_, w.st, w.cg);
-      k_cg_pq<<<1, 1, 0, s_>>>(w.cg, w.st);
-      k_cg_xr<<<nParts_, RB, 0, s_>>>(n_, w.cg, p_, q_, x, r_, red_, w.st);
-      k_cg_check<<<1, 1, 0, s_>>>(w.cg, w.st);
+      (k_dot_if<<<nParts_, RB, 0, s_>>>(n_, p_, q_, red_, w.st, w.cg), ::feng::count_launch());
+      (k_cg_pq<<<1, 1, 0, s_>>>(w.cg, w.st), ::feng::count_launch());
+      (k_cg_xr<<<nParts_, RB, 0, s_>>>(n_, w.cg, p_, q_, x, r_, red_, w.st), ::feng::count_launch());
+      (k_cg_check<<<1, 1, 0, s_>>>(w.cg, w.st), ::feng::count_launch());
       precond64(r_, t_, &w.cg->done);
-      k_dot_if<<<nParts_, RB, 0, s_>>>(n_, r_, t_, red_, w.st, w.cg);
-      k_cg_p<<<gv, 256, 0, s_>>>(n_, w.cg, w.st, t_, p_, 0);
-      k_cg_rz<<<1, 1, 0, s_>>>(w.cg, w.st);
+      (k_dot_if<<<nParts_, RB, 0, s_>>>(n_, r_, t_, red_, w.st, w.cg), ::feng::count_launch());
+      (k_cg_p<<<gv, 256, 0, s_>>>(n_, w.cg, w.st, t_, p_, 0), ::feng::count_launch());
+      (k_cg_rz<<<1, 1, 0, s_>>>(w.cg, w.st), ::feng::count_launch());
     }
     it += batch;
     cudaMemcpyAsync(w.hcg, w.cg, sizeof(CGState), cudaMemcpyDeviceToHost, s_);
@@ -925,7 +985,7 @@ int Krylov::solve(const double *values64, const float *values32, const double *b
   st.rnorm0 = bn;
   if(!std::isfinite(bn)) { set_error("non-finite right-hand side"); return FE_NONFINITE; }
   const int gv = grid_for(n_, 256, 2048);
-  k_zero<<<gv, 256, 0, s_>>>(n_, x);
+  (k_zero<<<gv, 256, 0, s_>>>(n_, x), ::feng::count_launch());
   const double tolAbs = std::max(opt.rtol * bn, opt.atol);
   if(bn <= opt.atol) { st.rnorm = bn; return FE_OK; }
   if(opt.method == 0) {

@@ -91,6 +91,10 @@ class Krylov {
             KrylovStats &st);
   // y = A x (FP64 values, FP64 vectors) on this object's stream.
   void spmv64(const double *values, const double *x, double *y);
+  // The inner-loop FP32 product: x rounded to FP32, FP32 accumulation.
+  void spmv32(const float *values, const double *x, double *y);
+  // One preconditioner application z = M^-1 r (the FP32 path rounds r).
+  int applyPrecond(const double *r, double *z);
   double norm2(const double *x);
   double norminf(const double *x);
   KrylovOptions opt;
@@ -133,7 +137,21 @@ class Krylov {
   const double *cur64_ = nullptr;  // matrix values of the last factor()
   const float *cur32_ = nullptr;
   int *hflag_ = nullptr;           // pinned copy of the device done flag
+  double *htol_ = nullptr;         // pinned absolute tolerance read by the cycle
   bool poll_done(const int *dflag, int j);
+  void launch_cycle(bool mixed, const void *vals, const double *b, double *x, int jmax, bool poll);
+  int run_cycle(bool mixed, const void *vals, const double *b, double *x, int jmax);
+  struct GraphKey {
+    bool mixed;
+    const void *vals;
+    const double *b;
+    double *x;
+  };
+  std::vector<std::pair<GraphKey, cudaGraphExec_t>> graphs_;
+  std::vector<size_t> graphKernels_;  // kernel nodes of each graph
+
+ public:
+  bool useGraphs_ = true;  // replay full restart cycles from CUDA graphs
   int setup_mg(const PrecondInfo &pi);
   int factor_mg(const double *values64, const float *values32);
   template <typename V> void apply_mg(const V *vals, const V *r, V *z, const int *skip);

@@ -36,6 +36,8 @@ struct Krylov::MG {
   int32_t *slotOf = nullptr;                                     // velocity DOF -> slot 2k+c (-1 otherwise)
   double cMc = 0, cSc = 0;  // constant pressure mode: c^T M c and c^T S c (deflation)
   double *pMassDev = nullptr, *tP = nullptr;
+  double *consts = nullptr;   // device: 1/s, c^T S c, c^T M c
+  double hconst[3] = {1, 0, 0};
   int32_t *diagX = nullptr;                                        // CSR position of diag of x rows
   double *pScale64 = nullptr;
   float *pScale32 = nullptr;
@@ -56,7 +58,7 @@ struct Krylov::MG {
     cudaFree(diagX); cudaFree(pScale64); cudaFree(pScale32); cudaFree(bx); cudaFree(by); cudaFree(zx);
     cudaFree(zy); cudaFree(dsum); cudaFree(ir); cudaFree(iz); cudaFree(ip); cudaFree(iq);
     cudaFree(part); cudaFree(scal); cudaFree(dnIa); cudaFree(dnPos); cudaFree(dnCol); cudaFree(slotOf);
-    cudaFree(pMassDev); cudaFree(tP);
+    cudaFree(pMassDev); cudaFree(tP); cudaFree(consts);
   }
   template <typename V> void solveK(const V *b, V *x, cudaStream_t st);
 };
@@ -156,25 +158,25 @@ void Krylov::MG::solveK(const V *b, V *x, cudaStream_t st)
   const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 4096));
   const int gp = (int)std::min<int64_t>(NPART, std::max<int64_t>(1, (n + 255) / 256));
   V *r = (V *)ir, *z = (V *)iz, *p = (V *)ip, *q = (V *)iq;
-  k_copy_v<V><<<g, 256, 0, st>>>(n, b, r);
+  (k_copy_v<V><<<g, 256, 0, st>>>(n, b, r), ::feng::count_launch());
   // x = 0 (written through r's type)
-  if constexpr(sizeof(V) == 8) k_zero_d<<<g, 256, 0, st>>>(n, (double *)x);
+  if constexpr(sizeof(V) == 8) (k_zero_d<<<g, 256, 0, st>>>(n, (double *)x), ::feng::count_launch());
   else cudaMemsetAsync(x, 0, sizeof(float) * n, st);
   vc(r, z);
-  k_dot_part<V><<<gp, 256, 0, st>>>(n, r, z, part);
-  k_dot_fin<<<1, 256, 0, st>>>(gp, part, scal + 0);
-  k_pcg_p<V><<<g, 256, 0, st>>>(n, scal, z, p, 1);
+  (k_dot_part<V><<<gp, 256, 0, st>>>(n, r, z, part), ::feng::count_launch());
+  (k_dot_fin<<<1, 256, 0, st>>>(gp, part, scal + 0), ::feng::count_launch());
+  (k_pcg_p<V><<<g, 256, 0, st>>>(n, scal, z, p, 1), ::feng::count_launch());
   for(int it = 0; it < inner; ++it) {
     spmv(p, q);
-    k_dot_part<V><<<gp, 256, 0, st>>>(n, p, q, part);
-    k_dot_fin<<<1, 256, 0, st>>>(gp, part, scal + 1);
-    k_pcg_xr<V><<<g, 256, 0, st>>>(n, scal, p, q, x, r);
+    (k_dot_part<V><<<gp, 256, 0, st>>>(n, p, q, part), ::feng::count_launch());
+    (k_dot_fin<<<1, 256, 0, st>>>(gp, part, scal + 1), ::feng::count_launch());
+    (k_pcg_xr<V><<<g, 256, 0, st>>>(n, scal, p, q, x, r), ::feng::count_launch());
     if(it + 1 == inner) break;
     vc(r, z);
-    k_dot_part<V><<<gp, 256, 0, st>>>(n, r, z, part);
-    k_dot_fin<<<1, 256, 0, st>>>(gp, part, scal + 2);
-    k_pcg_p<V><<<g, 256, 0, st>>>(n, scal, z, p, 0);
-    k_pcg_shift<<<1, 1, 0, st>>>(scal);
+    (k_dot_part<V><<<gp, 256, 0, st>>>(n, r, z, part), ::feng::count_launch());
+    (k_dot_fin<<<1, 256, 0, st>>>(gp, part, scal + 2), ::feng::count_launch());
+    (k_pcg_p<V><<<g, 256, 0, st>>>(n, scal, z, p, 0), ::feng::count_launch());
+    (k_pcg_shift<<<1, 1, 0, st>>>(scal), ::feng::count_launch());
   }
 }
 
@@ -212,16 +214,16 @@ __global__ void k_scale_copy(int64_t n, const V *__restrict__ r, V *__restrict__
 // c = 1 on the pressure unknowns, (c^T r) read from *cr.
 template <typename V, typename S>
 __global__ void k_pressure(int64_t nP, const int32_t *__restrict__ rows, const S *__restrict__ sc,
-                           const double *__restrict__ mass, const double *__restrict__ cr, double cMc,
-                           double cSc, const V *__restrict__ r, V *__restrict__ z,
+                           const double *__restrict__ mass, const double *__restrict__ cr,
+                           const double *__restrict__ consts, const V *__restrict__ r, V *__restrict__ z,
                            const int *__restrict__ skip)
 {
   if(skip && *skip) return;
-  const double c = cr ? *cr : 0.;
+  const double c = *cr, cSc = consts[1], cMc = consts[2];
   const double shift = cMc > 0 ? c / cMc : 0., lift = cSc != 0. ? c / cSc : 0.;
   for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nP; k += (int64_t)gridDim.x * blockDim.x) {
     const int32_t i = rows[k];
-    const double rp = (double)r[i] - (cr ? shift * mass[k] : 0.);
+    const double rp = (double)r[i] - shift * mass[k];
     z[i] = (V)((double)sc[k] * rp + lift);
   }
 }
@@ -315,10 +317,11 @@ __global__ void k_vel_rhs(int64_t nN, const int32_t *__restrict__ dofX, const in
 
 template <typename V>
 __global__ void k_vel_out(int64_t nN, const int32_t *__restrict__ dofX, const int32_t *__restrict__ dofY,
-                          const V *__restrict__ zx, const V *__restrict__ zy, V f, V *__restrict__ z,
-                          const int *__restrict__ skip)
+                          const V *__restrict__ zx, const V *__restrict__ zy, const double *__restrict__ consts,
+                          V *__restrict__ z, const int *__restrict__ skip)
 {
   if(skip && *skip) return;
+  const V f = (V)consts[0];
   for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nN; k += (int64_t)gridDim.x * blockDim.x) {
     z[dofX[k]] = zx[k] * f;
     if(dofY) z[dofY[k]] = zy[k] * f;
@@ -368,6 +371,7 @@ int Krylov::setup_mg(const PrecondInfo &pi)
   CKM(cudaMalloc(&M.dsum, sizeof(double)));
   CKM(cudaMalloc(&M.part, sizeof(double) * NPART));
   CKM(cudaMalloc(&M.scal, sizeof(double) * 4));
+  CKM(cudaMalloc(&M.consts, sizeof(double) * 3));
   CKM(cudaMemset(M.scal, 0, sizeof(double) * 4));
   // Host pattern for the diagonal positions and the G block.
   std::vector<int32_t> hia(n_ + 1), hja(A_.nnz);
@@ -433,8 +437,9 @@ int Krylov::setup_mg(const PrecondInfo &pi)
 int Krylov::factor_mg(const double *values64, const float *values32)
 {
   MG &M = *mg_;
-  if(values64) k_diag_sum<double><<<1, 256, 0, s_>>>(M.nNodes, M.diagX, values64, M.dsum);
-  else k_diag_sum<float><<<1, 256, 0, s_>>>(M.nNodes, M.diagX, values32, M.dsum);
+  M.amg.setSkip(nullptr);
+  if(values64) (k_diag_sum<double><<<1, 256, 0, s_>>>(M.nNodes, M.diagX, values64, M.dsum), ::feng::count_launch());
+  else (k_diag_sum<float><<<1, 256, 0, s_>>>(M.nNodes, M.diagX, values32, M.dsum), ::feng::count_launch());
   double sum = 0.;
   CKM(cudaMemcpyAsync(&sum, M.dsum, sizeof(double), cudaMemcpyDeviceToHost, s_));
   CKM(cudaStreamSynchronize(s_));
@@ -462,26 +467,32 @@ int Krylov::factor_mg(const double *values64, const float *values32)
     const int g = grid(M.nNodes);
     double sum2 = 0.;
     if(values64) {
-      k_gsum<double><<<g, 256, 0, s_>>>(M.nNodes, M.upIa, M.upPos, values64, (double *)M.bx, (double *)M.by);
+      (k_gsum<double><<<g, 256, 0, s_>>>(M.nNodes, M.upIa, M.upPos, values64, (double *)M.bx, (double *)M.by), ::feng::count_launch());
       M.solveK<double>((const double *)M.bx, (double *)M.zx, s_);
       M.solveK<double>((const double *)M.by, (double *)M.zy, s_);
-      k_dw<double><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values64,
-                                                (const double *)M.zx, (const double *)M.zy, M.tP);
+      (k_dw<double><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values64,
+                                                (const double *)M.zx, (const double *)M.zy, M.tP), ::feng::count_launch());
     } else {
-      k_gsum<float><<<g, 256, 0, s_>>>(M.nNodes, M.upIa, M.upPos, values32, (float *)M.bx, (float *)M.by);
+      (k_gsum<float><<<g, 256, 0, s_>>>(M.nNodes, M.upIa, M.upPos, values32, (float *)M.bx, (float *)M.by), ::feng::count_launch());
       M.solveK<float>((const float *)M.bx, (float *)M.zx, s_);
       M.solveK<float>((const float *)M.by, (float *)M.zy, s_);
-      k_dw<float><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values32,
-                                               (const float *)M.zx, (const float *)M.zy, M.tP);
+      (k_dw<float><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values32,
+                                               (const float *)M.zx, (const float *)M.zy, M.tP), ::feng::count_launch());
     }
     const int gp = (int)std::min<int64_t>(NPART, std::max<int64_t>(1, (M.nP + 255) / 256));
-    k_tsum<<<gp, 256, 0, s_>>>(M.nP, M.tP, M.part);
-    k_dot_fin<<<1, 256, 0, s_>>>(gp, M.part, M.dsum);
+    (k_tsum<<<gp, 256, 0, s_>>>(M.nP, M.tP, M.part), ::feng::count_launch());
+    (k_dot_fin<<<1, 256, 0, s_>>>(gp, M.part, M.dsum), ::feng::count_launch());
     CKM(cudaMemcpyAsync(&sum2, M.dsum, sizeof(double), cudaMemcpyDeviceToHost, s_));
     CKM(cudaStreamSynchronize(s_));
     M.cSc = -sum2 / M.s;
     if(!std::isfinite(M.cSc) || M.cSc == 0.) M.cSc = 0.;  // no deflation
   }
+  // Scalars read by the (graph-replayed) apply kernels.
+  M.hconst[0] = 1.0 / M.s;
+  M.hconst[1] = M.cSc;
+  M.hconst[2] = M.cMc;
+  CKM(cudaMemcpyAsync(M.consts, M.hconst, sizeof(double) * 3, cudaMemcpyHostToDevice, s_));
+  CKM(cudaStreamSynchronize(s_));
   return FE_OK;
 }
 
@@ -489,34 +500,31 @@ template <typename V>
 void Krylov::apply_mg(const V *vals, const V *r, V *z, const int *skip)
 {
   MG &M = *mg_;
-  const V f = (V)(1.0 / M.s);
+  M.amg.setSkip(skip);
   if(M.kind == 3) {
     // z = (s K)^-1 r on the unknown rows (the nodes are the unknowns)
-    k_vel_rhs<V><<<grid(M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofX, nullptr, nullptr, nullptr,
-                                                  vals, r, z, (V *)M.bx, (V *)M.by, skip);
+    (k_vel_rhs<V><<<grid(M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofX, nullptr, nullptr, nullptr,
+                                                  vals, r, z, (V *)M.bx, (V *)M.by, skip), ::feng::count_launch());
   } else {
-    const double *cr = nullptr;
-    if(M.cSc != 0.) {
-      const int gp = (int)std::min<int64_t>(NPART, std::max<int64_t>(1, (M.nP + 255) / 256));
-      k_psum_part<V><<<gp, 256, 0, s_>>>(M.nP, M.pRows, r, M.part);
-      k_dot_fin<<<1, 256, 0, s_>>>(gp, M.part, M.scal + 3);
-      cr = M.scal + 3;
-    }
+    const int gp = (int)std::min<int64_t>(NPART, std::max<int64_t>(1, (M.nP + 255) / 256));
+    (k_psum_part<V><<<gp, 256, 0, s_>>>(M.nP, M.pRows, r, M.part), ::feng::count_launch());
+    (k_dot_fin<<<1, 256, 0, s_>>>(gp, M.part, M.scal + 3), ::feng::count_launch());
+    const double *cr = M.scal + 3;
     if constexpr(sizeof(V) == 8)
-      k_pressure<V, double><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.pRows, M.pScale64, M.pMassDev, cr, M.cMc,
-                                                        M.cSc, r, z, skip);
+      (k_pressure<V, double><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.pRows, M.pScale64, M.pMassDev, cr, M.consts,
+                                                        r, z, skip), ::feng::count_launch());
     else
-      k_pressure<V, float><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.pRows, M.pScale32, M.pMassDev, cr, M.cMc,
-                                                       M.cSc, r, z, skip);
-    k_vel_rhs<V><<<grid(M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, M.upIa, M.upPos, M.upCol,
-                                                  vals, r, z, (V *)M.bx, (V *)M.by, skip);
+      (k_pressure<V, float><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.pRows, M.pScale32, M.pMassDev, cr, M.consts,
+                                                       r, z, skip), ::feng::count_launch());
+    (k_vel_rhs<V><<<grid(M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, M.upIa, M.upPos, M.upCol,
+                                                  vals, r, z, (V *)M.bx, (V *)M.by, skip), ::feng::count_launch());
   }
   // The component solves run unconditionally; when `skip` is set their
   // output is discarded by the skipped scatter below.
   M.solveK<V>((const V *)M.bx, (V *)M.zx, s_);
   if(M.kind == 4) M.solveK<V>((const V *)M.by, (V *)M.zy, s_);
-  k_vel_out<V><<<grid(M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.kind == 4 ? M.dofY : nullptr,
-                                                (const V *)M.zx, (const V *)M.zy, f, z, skip);
+  (k_vel_out<V><<<grid(M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.kind == 4 ? M.dofY : nullptr,
+                                                (const V *)M.zx, (const V *)M.zy, M.consts, z, skip), ::feng::count_launch());
 }
 
 template void Krylov::apply_mg<double>(const double *, const double *, double *, const int *);

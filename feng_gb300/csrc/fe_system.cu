@@ -262,7 +262,7 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
   CK(cudaMalloc(&csr_.diag, sizeof(int32_t) * nInc_));
   CK(cudaMemcpy(csr_.ia, ia32.data(), sizeof(int32_t) * (nInc_ + 1), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(csr_.ja, pat_.ja.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice));
-  k_diagpos<<<gridFor(nInc_), 256, 0, s_>>>(nInc_, csr_.ia, csr_.ja, csr_.diag);
+  (k_diagpos<<<gridFor(nInc_), 256, 0, s_>>>(nInc_, csr_.ia, csr_.ja, csr_.diag), ::feng::count_launch());
   if(opt.precision == 0) CK(cudaMalloc(&vals64_, sizeof(double) * nnz));
   else CK(cudaMalloc(&vals32_, sizeof(float) * nnz));
   CK(cudaMalloc(&rhs_, sizeof(double) * nInc_));
@@ -501,7 +501,7 @@ int SystemCUDA::solve(double *normDx, double *normRHS, double *normAxb, int *nIt
 
 int SystemCUDA::correctSolution()
 {
-  k_add<<<gridFor(nInc_), 256, 0, s_>>>(nInc_, du_, u_);
+  (k_add<<<gridFor(nInc_), 256, 0, s_>>>(nInc_, du_, u_), ::feng::count_launch());
   CK(cudaGetLastError());
   return FE_OK;
 }
@@ -549,10 +549,67 @@ int SystemCUDA::setBDF(int order, const double *cn, const double *const *hostHis
 
 int SystemCUDA::computeSolDot()
 {
-  k_soldot<<<gridFor(nDofs_), 256, 0, s_>>>(nDofs_, bdfOrder_, cn_[0], cn_[1], cn_[2], u_, hist_[1],
-                                             hist_[2], udot_);
+  (k_soldot<<<gridFor(nDofs_), 256, 0, s_>>>(nDofs_, bdfOrder_, cn_[0], cn_[1], cn_[2], u_, hist_[1],
+                                             hist_[2], udot_), ::feng::count_launch());
   CK(cudaGetLastError());
   return FE_OK;
+}
+
+int SystemCUDA::benchPhase(int which, int reps, size_t flushBytes, double *avgMs)
+{
+  if(which < 0 || which > 3 || reps < 1) {
+    set_error("invalid benchmark request");
+    return FE_INVALID_ARG;
+  }
+  void *flush = nullptr;
+  if(flushBytes) CK(cudaMalloc(&flush, flushBytes));
+  double *x = nullptr, *y = nullptr;
+  CK(cudaMalloc(&x, sizeof(double) * nInc_));
+  CK(cudaMalloc(&y, sizeof(double) * nInc_));
+  CK(cudaMemsetAsync(x, 0, sizeof(double) * nInc_, s_));
+  CK(cudaMemcpyAsync(x, rhs_, sizeof(double) * nInc_, cudaMemcpyDeviceToDevice, s_));
+  const int savedTiming = timing;
+  timing = 0;
+  double total = 0.;
+  int status = FE_OK;
+  for(int r = 0; r < reps && status == FE_OK; ++r) {
+    if(flush) CK(cudaMemsetAsync(flush, r & 0xff, flushBytes, s_));
+    CK(cudaEventRecord(ev0_, s_));
+    switch(which) {
+      case 0:
+        for(int c = 0; c < dm_.nColors; ++c)
+          launch_assemble_residual(dm_, fc_, dT_, u_, udot_, t_, nInc_, y, dm_.colorOff[c],
+                                   dm_.colorOff[c + 1], s_);
+        break;
+      case 1:
+        for(int c = 0; c < dm_.nColors; ++c) {
+          if(vals64_)
+            launch_assemble_matrix_f64(dm_, fc_, dT_, u_, c0_, vals64_, dm_.colorOff[c], dm_.colorOff[c + 1], s_);
+          else
+            launch_assemble_matrix_f32(dm_, fc_, dT_, u_, c0_, vals32_, dm_.colorOff[c], dm_.colorOff[c + 1], s_);
+        }
+        break;
+      case 2:
+        if(vals64_) kry_.spmv64(vals64_, x, y);
+        else kry_.spmv32(vals32_, x, y);
+        break;
+      case 3:
+        status = kry_.applyPrecond(x, y);
+        break;
+    }
+    CK(cudaEventRecord(ev1_, s_));
+    CK(cudaEventSynchronize(ev1_));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ev0_, ev1_));
+    total += ms;
+  }
+  timing = savedTiming;
+  CK(cudaGetLastError());
+  cudaFree(flush);
+  cudaFree(x);
+  cudaFree(y);
+  *avgMs = total / reps;
+  return status;
 }
 
 int SystemCUDA::getMatrix(double *hostValues) const

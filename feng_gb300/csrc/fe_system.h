@@ -93,6 +93,11 @@ class SystemCUDA {
   int getRHS(double *hostRhs) const;
   int getDu(double *hostDu) const;
   int validateColoring() const;
+  // Times `reps` runs of one phase with CUDA events on the system stream, each
+  // preceded by an L2 flush (a write of flushBytes): which = 0 residual
+  // assembly, 1 matrix assembly, 2 SpMV with the system matrix, 3 one
+  // preconditioner application.  Returns the mean milliseconds per run.
+  int benchPhase(int which, int reps, size_t flushBytes, double *avgMs);
 
   double *dU() { return u_; }
   double *dUdot() { return udot_; }

@@ -241,6 +241,24 @@ int fe_cuda_newton(fe_cuda_system *s, const fe_newton_options *o, fe_newton_stat
 int fe_cuda_get_times(const fe_cuda_system *s, double *residual_ms, double *matrix_ms,
                       double *factor_ms, double *solve_ms);
 int fe_cuda_reset_times(fe_cuda_system *s);
+/* Mean device milliseconds of one phase over `reps` runs timed with CUDA
+ * events on the system stream, each run preceded by an L2 flush (a write of
+ * flush_bytes): which = 0 residual assembly (all colors), 1 matrix assembly
+ * (all colors), 2 SpMV with the system matrix, 3 one preconditioner
+ * application.  Uses the current solution state. */
+int fe_cuda_bench_phase(fe_cuda_system *s, int which, int reps, int64_t flush_bytes, double *avg_ms);
+/* Kernel launches of the library since load (graph replays count their
+ * kernel nodes). */
+int fe_cuda_launch_count(int64_t *count);
+/* Device-side copy of the solution vector: save / restore (no host traffic). */
+int fe_cuda_save_solution(fe_cuda_system *s);
+int fe_cuda_restore_solution(fe_cuda_system *s);
+/* CUDA events on the system stream: record event `slot` (0..7); elapsed
+ * milliseconds between two recorded slots (synchronizes on the later one). */
+int fe_cuda_event_record(fe_cuda_system *s, int slot);
+int fe_cuda_event_elapsed(fe_cuda_system *s, int slot0, int slot1, double *ms);
+/* Selects the CUDA device of the calling thread (one process per GPU). */
+int fe_cuda_set_device(int device);
 int fe_cuda_synchronize(fe_cuda_system *s);
 
 #ifdef __cplusplus
