@@ -2,6 +2,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -547,6 +548,9 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
 {
   A_ = A;
   opt = o;
+  // FENG_CUDA_GRAPHS=0 launches the restart cycles kernel by kernel (the same
+  // kernels, in the same order) -- for profilers that cannot replay graphs.
+  if(const char *e = std::getenv("FENG_CUDA_GRAPHS")) useGraphs_ = std::strcmp(e, "0") != 0;
   s_ = s;
   n_ = A.n;
   if(opt.restart < 1 || opt.restart > MAXM) {
