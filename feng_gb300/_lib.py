@@ -128,6 +128,7 @@ SIGNATURES = {
     "fe_cuda_event_record": (C.c_int, [P, C.c_int]),
     "fe_cuda_event_elapsed": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_double)]),
     "fe_cuda_set_device": (C.c_int, [C.c_int]),
+    "fe_cuda_max_norm_noalloc": (C.c_int, [P, C.c_int64, P, C.POINTER(C.c_double)]),
 }
 
 _lib = None

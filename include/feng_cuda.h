@@ -261,6 +261,21 @@ int fe_cuda_event_elapsed(fe_cuda_system *s, int slot0, int slot1, double *ms);
 int fe_cuda_set_device(int device);
 int fe_cuda_synchronize(fe_cuda_system *s);
 
+/* ---- allocation-free variant (no counterpart in the reference)
+ * Max-norm max_i |x_i| of a caller-owned device vector, for callers that may
+ * not allocate device memory (a host framework that owns every device byte
+ * through its own pool, a loop that cannot afford cudaMalloc's implicit
+ * synchronization).  Same reduction as fe_cuda_get_rhs_max_norm, but its
+ * scratch is a static device array of the library (about 8 KB per GPU, held
+ * until the process exits): nothing is allocated or freed.  n may be at most
+ * FE_NOALLOC_MAX_N; larger n is rejected with FE_CUDA_INVALID_ARG.  `stream`
+ * is a cudaStream_t (NULL: the legacy default stream); the call waits for it
+ * and writes the result to host memory.  The first call on each device looks
+ * up the scratch's device address (make it before any stream capture).  All
+ * calls share the one scratch array: calls that overlap on the GPU race. */
+#define FE_NOALLOC_MAX_N 4194304
+int fe_cuda_max_norm_noalloc(const double *x, int64_t n, void *stream, double *result);
+
 #ifdef __cplusplus
 }
 #endif
