@@ -40,7 +40,6 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 RE = 40.0
-DOMAIN = (-0.5, 1.5, -0.5, 1.5)
 METRIC = "newton_step_s"
 UNIT = "s"
 
@@ -95,19 +94,8 @@ class Dist:
 
 
 def build_problem(n):
-    import feng_gb300 as fe
-    from feng_gb300 import exact
-    m = fe.Mesh2DP1.generate_square(n, *DOMAIN, jitter=0.1, seed=1)
-    uex, pex = exact.kovasznay_velocity(RE), exact.kovasznay_pressure(RE)
-    u = fe.createFiniteElementSpace(m, fe.VECTOR_LAGRANGE, 2, "U", "Domaine", 8, uex)
-    uB = fe.createFiniteElementSpace(m, fe.VECTOR_LAGRANGE, 2, "U", "Bord", 8, uex)
-    p = fe.createFiniteElementSpace(m, fe.LAGRANGE, 1, "P", "Domaine", 8, pex)
-    pP = fe.createFiniteElementSpace(m, fe.LAGRANGE, 1, "P", "PointPression", 8, pex)
-    num = fe.feMetaNumber(m, [u, uB, p, pP], [uB, pP])
-    forms = [fe.createBilinearForm([u], fe.feSysElm_VectorConvectiveAcceleration(-1.0)),
-             fe.createBilinearForm([p, u], fe.feSysElm_MixedDivergence(1.0)),
-             fe.createBilinearForm([u, p], fe.feSysElm_DivergenceNewtonianStress(1.0, 1.0 / RE))]
-    return m, num, forms
+    from feng_gb300 import kovasznay
+    return kovasznay.build(n, RE)
 
 
 class Clocks:
@@ -151,21 +139,13 @@ def measured_peaks():
 
 
 def make_system(num, forms, precision):
-    import feng_gb300 as fe
-    opts = fe.LinearSolverOptions(precond="amg", rel_tol=1e-8, max_iter=3000,
-                                  precision="mixed" if precision == "mixed" else "fp64")
-    sys_ = fe.createLinearSystem(fe.CUDA, forms, num, opts)
-    sol = fe.feSolution(sys_)
-    sol.initializeEssentialBC()
-    return sys_, sol
+    from feng_gb300 import kovasznay
+    return kovasznay.make_system(num, forms, precision)
 
 
 def newton_opts(precision):
-    import feng_gb300 as fe
-    if precision == "mixed":
-        return fe.feNLSolverOptions(tolResidual=0.0, tolCorrection=0.0, maxIter=30, relResidual=1e-8,
-                                    linearRtolMin=1e-6)
-    return fe.feNLSolverOptions(tolResidual=0.0, tolCorrection=0.0, maxIter=30, relResidual=1e-8)
+    from feng_gb300 import kovasznay
+    return kovasznay.newton_options(precision)
 
 
 def run_newton(sys_, nl):
@@ -204,20 +184,24 @@ def timed_steps(sys_, nl, steps, warmup, dist):
 
 def e2e_steps(sys_, nl, steps):
     """Same metric through the public API with host buffers: every step
-    uploads the initial state from pinned host memory and reads the solution
-    back."""
+    uploads the initial state from pinned host memory, runs the Newton solve
+    and reads the solution back into pinned host memory."""
+    import torch
     import feng_gb300 as fe
-    from feng_gb300._lib import check, ptr
+    from feng_gb300._lib import check
     lib = sys_.lib
-    u0 = sys_.getSolution()
-    hostbuf = np.empty(sys_.nDofs)
-    # pinned host copies would need torch or cudaHostAlloc; the solution
-    # vectors are small (4.7 MB) and pageable copies are what a C caller makes.
+    # The initial state saved before the timed device steps (with its
+    # boundary values), fetched to the host outside the timed region.
+    check(lib.fe_cuda_restore_solution(sys_._h))
+    u0 = torch.from_numpy(sys_.getSolution()).pin_memory()
+    hostbuf = torch.empty(sys_.nDofs, dtype=torch.float64).pin_memory()
+    pu0, pout = C.c_void_p(u0.data_ptr()), C.c_void_p(hostbuf.data_ptr())
+    sys_.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
-        check(lib.fe_cuda_set_solution(sys_._h, ptr(u0), None))
+        check(lib.fe_cuda_set_solution(sys_._h, pu0, None))
         fe.solveNewtonRaphson(sys_, None, nl)
-        check(lib.fe_cuda_get_solution(sys_._h, ptr(hostbuf)))
+        check(lib.fe_cuda_get_solution(sys_._h, pout))
     dt = (time.perf_counter() - t0) / steps
     return dt, sys_.nDofs * 8, sys_.nDofs * 8
 

@@ -48,7 +48,21 @@ class NewtonOptions(C.Structure):
                 ("tol_divergence", C.c_double), ("max_iter", C.c_int32),
                 ("recompute_every", C.c_int32), ("residual_decrease", C.c_double),
                 ("stationary", C.c_int32), ("rel_residual", C.c_double),
-                ("linear_rtol_min", C.c_double)]
+                ("linear_rtol_min", C.c_double), ("residual_scale", C.c_double)]
+
+
+class TransientOptions(C.Structure):
+    _fields_ = [("dt", C.c_double), ("t0", C.c_double), ("guess", C.c_int32), ("train_from", C.c_int32),
+                ("use_from", C.c_int32), ("train_iters", C.c_int32), ("batch", C.c_int64),
+                ("lr", C.c_double), ("seed", C.c_uint64)]
+
+
+class StepStats(C.Structure):
+    _fields_ = [("step", C.c_int32), ("newton_iterations", C.c_int32), ("krylov_iterations", C.c_int32),
+                ("status", C.c_int32), ("guess_used", C.c_int32), ("t", C.c_double),
+                ("residual_ref", C.c_double), ("residual_guess", C.c_double),
+                ("residual_extrap", C.c_double), ("residual", C.c_double), ("step_ms", C.c_double),
+                ("guess_ms", C.c_double), ("train_ms", C.c_double), ("train_loss", C.c_double)]
 
 
 class NewtonStats(C.Structure):
@@ -129,6 +143,18 @@ SIGNATURES = {
     "fe_cuda_event_elapsed": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_double)]),
     "fe_cuda_set_device": (C.c_int, [C.c_int]),
     "fe_cuda_max_norm_noalloc": (C.c_int, [P, C.c_int64, P, C.POINTER(C.c_double)]),
+    "fe_cuda_transient_create": (C.c_int, [P, C.POINTER(TransientOptions), C.POINTER(NewtonOptions),
+                                           C.POINTER(P)]),
+    "fe_cuda_transient_steps": (C.c_int, [P, C.c_int, P]),
+    "fe_cuda_transient_destroy": (None, [P]),
+    "fe_mlp_sizes": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                               C.POINTER(C.c_int), C.POINTER(C.c_int64)]),
+    "fe_mlp_create": (C.c_int, [C.c_uint64, C.c_int64, C.POINTER(P)]),
+    "fe_mlp_destroy": (None, [P]),
+    "fe_mlp_set_params": (C.c_int, [P, P]),
+    "fe_mlp_get_params": (C.c_int, [P, P]),
+    "fe_mlp_forward": (C.c_int, [P, P, C.c_int64, P]),
+    "fe_mlp_train_step": (C.c_int, [P, P, P, P, C.c_int64, C.c_double, P, C.POINTER(C.c_double)]),
 }
 
 _lib = None

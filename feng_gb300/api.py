@@ -499,6 +499,7 @@ class feNLSolverOptions:
     residualDecrease: float = 1e-1
     relResidual: float = 0.0
     linearRtolMin: float = 0.0
+    residualScale: float = 0.0
 
 
 def solveNewtonRaphson(system: feLinearSystemCUDA, sol: feSolution | None,
@@ -508,7 +509,7 @@ def solveNewtonRaphson(system: feLinearSystemCUDA, sol: feSolution | None,
         sol.push()
     o = _lib.NewtonOptions(tol.tolResidual, tol.tolCorrection, tol.tolDivergence, int(tol.maxIter),
                            tol.recomputeJacobianEveryNsteps, tol.residualDecrease, int(stationary),
-                           tol.relResidual, tol.linearRtolMin)
+                           tol.relResidual, tol.linearRtolMin, tol.residualScale)
     st = _lib.NewtonStats()
     s = system.lib.fe_cuda_newton(system._h, C.byref(o), C.byref(st))
     out = {k: getattr(st, k) for k, _ in _lib.NewtonStats._fields_}
@@ -518,3 +519,102 @@ def solveNewtonRaphson(system: feLinearSystemCUDA, sol: feSolution | None,
     if s not in (0, -5):
         check(s)
     return out
+
+
+# ---- time integration (src/feTimeIntegration.h) --------------------------------
+
+BDF2 = "BDF2"
+GUESS = {"previous": 0, "extrapolate": 1, "learned": 2}
+
+
+class BDF2Integrator:
+    """BDF2Integrator (src/feTimeIntegration.cpp:449-547) on device-resident
+    history: the first step starts with a BDF1 substep of 0.1 dt
+    (startWithBDF1, :383-435), then variable-step BDF2.  ``guess`` picks the
+    Newton initial guess of each step: "previous" (the reference's),
+    "extrapolate" (linear in time) or "learned" (extrapolation plus an online
+    trained per-node MLP correction, used only where its FP64 residual is
+    smaller).  Each Newton solve stops at ||R||inf <= relResidual * ||R(u^n)||inf
+    (plus the absolute tests of ``nlOptions``)."""
+
+    def __init__(self, system: feLinearSystemCUDA, sol: feSolution | None, nlOptions: feNLSolverOptions,
+                 t0: float, t1: float, nTimeSteps: int, guess: str = "extrapolate", trainFrom: int = 20,
+                 useFrom: int = 25, trainIters: int = 8, batch: int = 16384, lr: float = 1e-3, seed: int = 1):
+        self.system, self.sol = system, sol
+        self.dt = (t1 - t0) / nTimeSteps
+        if sol is not None:
+            sol.push()
+        o = _lib.TransientOptions(self.dt, t0, GUESS[guess], trainFrom, useFrom, trainIters, batch, lr, seed)
+        n = _lib.NewtonOptions(nlOptions.tolResidual, nlOptions.tolCorrection, nlOptions.tolDivergence,
+                               int(nlOptions.maxIter), nlOptions.recomputeJacobianEveryNsteps,
+                               nlOptions.residualDecrease, 0, nlOptions.relResidual, nlOptions.linearRtolMin, 0.0)
+        h = C.c_void_p()
+        check(system.lib.fe_cuda_transient_create(system._h, C.byref(o), C.byref(n), C.byref(h)))
+        self._h = h
+
+    def makeSteps(self, nSteps: int):
+        """Advances nSteps steps; returns one statistics dict per step."""
+        st = (_lib.StepStats * max(nSteps, 1))()
+        check(self.system.lib.fe_cuda_transient_steps(self._h, nSteps, C.cast(st, C.c_void_p)))
+        if self.sol is not None:
+            self.sol.pull()
+        return [{k: getattr(s, k) for k, _ in _lib.StepStats._fields_} for s in st[:nSteps]]
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h:
+            self.system.lib.fe_cuda_transient_destroy(h)
+
+
+def createTimeIntegrator(scheme: str, nlOptions: feNLSolverOptions, system: feLinearSystemCUDA,
+                         sol: feSolution | None, t0: float, t1: float, nTimeSteps: int, **kw):
+    """createTimeIntegrator (src/feTimeIntegration.cpp) for the BDF2 scheme."""
+    if scheme != BDF2:
+        raise ValueError("only the BDF2 scheme runs on the device")
+    return BDF2Integrator(system, sol, nlOptions, t0, t1, nTimeSteps, **kw)
+
+
+class MLP:
+    """The learned-guess network alone (device kernels, host buffers)."""
+
+    def __init__(self, seed: int = 1, max_batch: int = 4096):
+        self.lib = _lib.load()
+        d = [C.c_int() for _ in range(4)]
+        npar = C.c_int64()
+        check(self.lib.fe_mlp_sizes(*[C.byref(v) for v in d], C.byref(npar)))
+        self.dims = tuple(v.value for v in d)
+        self.nparams = npar.value
+        h = C.c_void_p()
+        check(self.lib.fe_mlp_create(seed, max_batch, C.byref(h)))
+        self._h = h
+
+    def params(self) -> np.ndarray:
+        p = np.empty(self.nparams, np.float32)
+        check(self.lib.fe_mlp_get_params(self._h, ptr(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        check(self.lib.fe_mlp_set_params(self._h, ptr(p)))
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.empty((x.shape[0], self.dims[3]), np.float32)
+        check(self.lib.fe_mlp_forward(self._h, ptr(x), x.shape[0], ptr(y)))
+        return y
+
+    def train_step(self, x, t, mask, lr):
+        """Gradient and loss of the batch, then one Adam step; returns (loss, grad)."""
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        mask = np.ascontiguousarray(mask, np.float32)
+        g = np.empty(self.nparams, np.float32)
+        loss = C.c_double()
+        check(self.lib.fe_mlp_train_step(self._h, ptr(x), ptr(t), ptr(mask), x.shape[0], lr, ptr(g),
+                                         C.byref(loss)))
+        return loss.value, g
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h:
+            self.lib.fe_mlp_destroy(h)

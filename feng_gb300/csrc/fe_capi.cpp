@@ -13,6 +13,7 @@
 #include "fe_mesh.h"
 #include "fe_setup.h"
 #include "fe_system.h"
+#include "fe_transient.h"
 
 namespace feng {
 namespace {
@@ -590,6 +591,7 @@ int fe_cuda_newton(fe_cuda_system *s, const fe_newton_options *o, fe_newton_stat
   no.stationary = o->stationary;
   no.relResidual = o->rel_residual;
   no.linearRtolMin = o->linear_rtol_min;
+  no.residualScale = o->residual_scale;
   NewtonStats ns;
   const PhaseTimes before = s->sys.times;
   int r = newton_solve(s->sys, no, ns);
@@ -719,3 +721,85 @@ int fe_cuda_synchronize(fe_cuda_system *s)
 }
 
 }  // extern "C"
+
+// ---- BDF2 time integration with extrapolated / learned initial guesses ------
+
+struct fe_transient {
+  fe_cuda_system *sys = nullptr;
+  Transient tr;
+};
+
+static NewtonOptions newton_options_of(const fe_newton_options *o)
+{
+  NewtonOptions no;
+  no.tolResidual = o->tol_residual;
+  no.tolCorrection = o->tol_correction;
+  no.tolDivergence = o->tol_divergence;
+  no.maxIter = o->max_iter;
+  no.recomputeEvery = o->recompute_every > 0 ? o->recompute_every : 3;
+  no.residualDecrease = o->residual_decrease;
+  no.stationary = 0;
+  no.relResidual = o->rel_residual;
+  no.linearRtolMin = o->linear_rtol_min;
+  no.residualScale = 0.0;  // set per step by the integrator
+  return no;
+}
+
+extern "C" int fe_cuda_transient_create(fe_cuda_system *s, const fe_transient_options *o,
+                                        const fe_newton_options *n, fe_transient **out)
+{
+  GUARD_BEGIN
+  if(!s || !o || !n || !out) { set_error("null argument"); return FE_INVALID_ARG; }
+  TransientOptions to;
+  to.dt = o->dt;
+  to.t0 = o->t0;
+  to.guess = o->guess;
+  to.trainFrom = o->train_from;
+  to.useFrom = o->use_from;
+  to.trainIters = o->train_iters;
+  to.batch = o->batch;
+  to.lr = o->lr;
+  to.seed = o->seed;
+  auto *t = new fe_transient();
+  t->sys = s;
+  const int r = t->tr.init(&s->sys, to, newton_options_of(n));
+  if(r != FE_OK) {
+    delete t;
+    return r;
+  }
+  *out = t;
+  return FE_OK;
+  GUARD_END
+}
+
+extern "C" int fe_cuda_transient_steps(fe_transient *t, int nsteps, fe_step_stats *stats)
+{
+  GUARD_BEGIN
+  if(!t || nsteps < 0) { set_error("null handle or negative step count"); return FE_INVALID_ARG; }
+  for(int k = 0; k < nsteps; ++k) {
+    StepStats st;
+    const int r = t->tr.step(st);
+    if(stats) {
+      fe_step_stats &o = stats[k];
+      o.step = st.step;
+      o.newton_iterations = st.newtonIterations;
+      o.krylov_iterations = st.krylovIterations;
+      o.status = r != FE_OK ? r : st.status;
+      o.guess_used = st.guessUsed;
+      o.t = st.t;
+      o.residual_ref = st.residualRef;
+      o.residual_guess = st.residualGuess;
+      o.residual_extrap = st.residualExtrap;
+      o.residual = st.residual;
+      o.step_ms = st.stepMs;
+      o.guess_ms = st.guessMs;
+      o.train_ms = st.trainMs;
+      o.train_loss = st.trainLoss;
+    }
+    if(r != FE_OK) return r;
+  }
+  return FE_OK;
+  GUARD_END
+}
+
+extern "C" void fe_cuda_transient_destroy(fe_transient *t) { delete t; }

@@ -200,6 +200,8 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
     return FE_BAD_COLORING;
   }
   adrHost_.assign(t.adr, t.adr + nE * nloc_);
+  elemXYHost_.assign(t.elemXY, t.elemXY + nE * 6);
+  elemType_ = t.elemType;
   FE_TRY(validateColoring());
   if(t.pattern && t.pattern->n == nInc_) pat_ = *t.pattern;
   else FE_TRY(build_csr_pattern(et, nInc_, pat_));
@@ -547,6 +549,20 @@ int SystemCUDA::setBDF(int order, const double *cn, const double *const *hostHis
   return FE_OK;
 }
 
+int SystemCUDA::setBDFCoefficients(int order, const double *cn)
+{
+  if(order < 0 || order > 2) {
+    set_error("BDF order %d not supported", order);
+    return FE_INVALID_ARG;
+  }
+  bdfOrder_ = order;
+  for(int k = 0; k < 3; ++k) cn_[k] = k <= order ? cn[k] : 0.;
+  for(int k = 1; k <= order; ++k)
+    if(!hist_[k]) CK(cudaMalloc(&hist_[k], sizeof(double) * nDofs_));
+  c0_ = cn_[0];
+  return FE_OK;
+}
+
 int SystemCUDA::computeSolDot()
 {
   (k_soldot<<<gridFor(nDofs_), 256, 0, s_>>>(nDofs_, bdfOrder_, cn_[0], cn_[1], cn_[2], u_, hist_[1],
@@ -654,21 +670,25 @@ int newton_solve(SystemCUDA &sys, const NewtonOptions &o, NewtonStats &st)
   const double baseRtol = sys.krylov().opt.rtol;
   while(true) {
     if(!o.stationary) FE_TRY(sys.computeSolDot());
-    FE_TRY(sys.setToZero());
+    // As feLinearSystemMklPardiso::setToZero (:967-971): a reused Jacobian
+    // (and its preconditioner) is kept.
+    if(recompute) FE_TRY(sys.setToZero());
+    else FE_TRY(sys.setResidualToZero());
     FE_TRY(sys.assembleResiduals());
     FE_TRY(sys.getRHSMaxNorm(&normResidual));
     if(iter == 0) st.residual0 = normResidual;
     st.residual = normResidual;
     if(iter > 0 && normResidual <= o.tolResidual) break;
-    if(iter > 0 && o.relResidual > 0 && normResidual <= o.relResidual * st.residual0) break;
+    const double scale = o.residualScale > 0 ? o.residualScale : st.residual0;
+    if(iter > 0 && o.relResidual > 0 && normResidual <= o.relResidual * scale) break;
     if(iter == 0 && normResidual == 0.0) break;
     if(recompute) {
       FE_TRY(sys.assembleMatrices());
       st.matrixAssemblies++;
     }
-    if(o.linearRtolMin > 0 && st.residual0 > 0) {
+    if(o.linearRtolMin > 0 && scale > 0) {
       // Inexact Newton: solve only as far as the nonlinear residual warrants.
-      const double ratio = normResidual / st.residual0;
+      const double ratio = normResidual / scale;
       sys.krylov().opt.rtol = std::max(o.linearRtolMin, std::min(1e-2, 0.1 * ratio));
     }
     int nIt = 0;
@@ -693,7 +713,8 @@ int newton_solve(SystemCUDA &sys, const NewtonOptions &o, NewtonStats &st)
     bool stop = normResidual <= o.tolResidual || normCorrection <= o.tolCorrection || iter > o.maxIter;
     if(stop) break;
   }
-  st.converged = (st.residual <= o.tolResidual) || (o.relResidual > 0 && st.residual <= o.relResidual * st.residual0) ||
+  const double scale = o.residualScale > 0 ? o.residualScale : st.residual0;
+  st.converged = (st.residual <= o.tolResidual) || (o.relResidual > 0 && st.residual <= o.relResidual * scale) ||
                  (st.correction <= o.tolCorrection) || st.residual0 == 0.0;
   st.status = st.converged ? FE_OK : FE_NOT_CONVERGED;
   return st.status;

@@ -80,7 +80,12 @@ class SystemCUDA {
   }
   // BDF history: hist[k] = u^{n+1-k}; udot = sum_k cn[k] hist[k] with hist[0] = u.
   int setBDF(int order, const double *cn, const double *const *hostHist);
+  // Coefficients only (device history kept; buffers allocated on first use).
+  int setBDFCoefficients(int order, const double *cn);
   int computeSolDot();
+  // Device history u^{n+1-k} (k = 1, 2), owned by the system.
+  double *dHist(int k) { return k >= 1 && k <= 2 ? hist_[k] : nullptr; }
+  double time() const { return t_; }
 
   int64_t nInc() const { return nInc_; }
   int64_t nDofs() const { return nDofs_; }
@@ -98,6 +103,12 @@ class SystemCUDA {
   // assembly, 1 matrix assembly, 2 SpMV with the system matrix, 3 one
   // preconditioner application.  Returns the mean milliseconds per run.
   int benchPhase(int which, int reps, size_t flushBytes, double *avgMs);
+
+  // Host copies of the set-up tables (original element order).
+  const std::vector<int64_t> &elementTable() const { return adrHost_; }
+  const std::vector<double> &elementXY() const { return elemXYHost_; }
+  int elemType() const { return elemType_; }
+  int nloc() const { return nloc_; }
 
   double *dU() { return u_; }
   double *dUdot() { return udot_; }
@@ -117,6 +128,8 @@ class SystemCUDA {
   Coloring col_;
   CSRPattern pat_;
   std::vector<int64_t> adrHost_;      // element table, original element order
+  std::vector<double> elemXYHost_;    // vertex coordinates per element
+  int elemType_ = 0;
   DeviceMesh dm_;
   FormCoeffs fc_{};
   RefTensors *dT_ = nullptr;
@@ -151,6 +164,7 @@ struct NewtonOptions {
   int stationary = 1;
   double relResidual = 0.0;       // extra stop: ||R||inf <= relResidual * ||R0||inf (0: off)
   double linearRtolMin = 0.0;     // >0: adaptive linear tolerance max(min, 0.1*||R||/||R0||)
+  double residualScale = 0.0;     // >0: replaces ||R0||inf in the two relative tests above
 };
 
 struct NewtonStats {

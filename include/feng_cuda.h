@@ -122,6 +122,9 @@ typedef struct fe_newton_options {
   int32_t stationary;
   double rel_residual;
   double linear_rtol_min;   /* > 0: inexact Newton, linear rtol = max(this, 0.1 ||R||/||R0||) */
+  double residual_scale;    /* > 0: replaces ||R0||inf in the two relative tests above (time
+                               steps: the residual of the previous step's solution, so that
+                               the stop does not depend on the initial guess) */
 } fe_newton_options;
 
 typedef struct fe_newton_stats {
@@ -260,6 +263,77 @@ int fe_cuda_event_elapsed(fe_cuda_system *s, int slot0, int slot1, double *ms);
 /* Selects the CUDA device of the calling thread (one process per GPU). */
 int fe_cuda_set_device(int device);
 int fe_cuda_synchronize(fe_cuda_system *s);
+
+/* ---- BDF2 time integration on device-resident history (BDF2Integrator::makeSteps,
+ * src/feTimeIntegration.cpp:449-547, started as startWithBDF1, :383-435; BDF
+ * coefficients and history rotation, src/feSolutionContainer.cpp:82-101,291-304).
+ * The system's current solution (fe_cuda_set_solution) is the initial
+ * condition, with its essential values; the forms must include
+ * FE_FORM_TRANSIENT_VECTOR_MASS.  Each step's Newton solve stops when
+ * ||R||inf <= rel_residual * ||R(u^n)||inf at the new time level (and on the
+ * absolute tests), whatever its initial guess:
+ *   FE_GUESS_PREVIOUS     u^n, as the reference;
+ *   FE_GUESS_EXTRAPOLATE  u^n + dt_n/dt_{n-1} (u^n - u^{n-1});
+ *   FE_GUESS_LEARNED      the extrapolation plus the correction of a per-node
+ *                         MLP (16 -> 64 -> 64 -> 4, tanh, FP32; inputs: the last
+ *                         three solutions and 6 geometry features) trained online
+ *                         with device forward/backward/Adam kernels on the
+ *                         corrections of converged steps from step train_from;
+ *                         from step use_from the extrapolation and the learned
+ *                         guess are both evaluated with the FP64 residual and the
+ *                         smaller one is used (no counterpart in the reference). */
+#define FE_GUESS_PREVIOUS 0
+#define FE_GUESS_EXTRAPOLATE 1
+#define FE_GUESS_LEARNED 2
+typedef struct fe_transient fe_transient;
+typedef struct fe_transient_options {
+  double dt;
+  double t0;
+  int32_t guess;         /* FE_GUESS_* */
+  int32_t train_from;    /* first step that trains the network */
+  int32_t use_from;      /* first step that may use the learned guess */
+  int32_t train_iters;   /* Adam steps per time step */
+  int64_t batch;         /* nodes per Adam step */
+  double lr;             /* Adam learning rate */
+  uint64_t seed;         /* weights and minibatch sampling */
+} fe_transient_options;
+typedef struct fe_step_stats {
+  int32_t step;
+  int32_t newton_iterations;
+  int32_t krylov_iterations;
+  int32_t status;
+  int32_t guess_used;      /* FE_GUESS_* */
+  double t;
+  double residual_ref;     /* ||R(u^n)||inf at the new time level */
+  double residual_guess;   /* ||R||inf at the guess used */
+  double residual_extrap;  /* ||R||inf at the extrapolation (0 if not formed) */
+  double residual;         /* final ||R||inf */
+  double step_ms;          /* device time of the whole step */
+  double guess_ms;         /* ... up to the end of the guess */
+  double train_ms;         /* ... of the training after the step */
+  double train_loss;       /* loss of the last Adam step (-1: no training) */
+} fe_step_stats;
+int fe_cuda_transient_create(fe_cuda_system *s, const fe_transient_options *o,
+                             const fe_newton_options *newton, fe_transient **out);
+/* Advances nsteps steps; stats [nsteps] may be NULL. */
+int fe_cuda_transient_steps(fe_transient *t, int nsteps, fe_step_stats *stats);
+void fe_cuda_transient_destroy(fe_transient *t);
+
+/* ---- the learned-guess MLP alone, through host buffers (tests and tools; same
+ * kernels as the integrator; no counterpart in the reference).  Parameters are
+ * packed W1 [64x16], b1 [64], W2 [64x64], b2 [64], W3 [4x64], b3 [4] (row-major);
+ * loss = sum mask (y - t)^2 / (4 n). */
+typedef struct fe_mlp fe_mlp;
+int fe_mlp_sizes(int *nin, int *h1, int *h2, int *nout, int64_t *nparams);
+int fe_mlp_create(uint64_t seed, int64_t max_batch, fe_mlp **out);
+void fe_mlp_destroy(fe_mlp *m);
+int fe_mlp_set_params(fe_mlp *m, const float *params);
+int fe_mlp_get_params(fe_mlp *m, float *params_out);
+int fe_mlp_forward(fe_mlp *m, const float *x, int64_t n, float *y);
+/* Loss and gradient of the batch (x [n x 16], t and mask [n x 4]) before one
+ * Adam step with learning rate lr (beta 0.9 / 0.999, eps 1e-8). */
+int fe_mlp_train_step(fe_mlp *m, const float *x, const float *t, const float *mask, int64_t n,
+                      double lr, float *grad, double *loss);
 
 /* ---- allocation-free variant (no counterpart in the reference)
  * Max-norm max_i |x_i| of a caller-owned device vector, for callers that may

@@ -59,6 +59,13 @@ def load():
         lib.fo_precond_destroy.argtypes = [P]
         lib.fo_krylov_solve.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                         C.c_int64, P, P, P, P, P, P, C.POINTER(KStats), C.c_int]
+        lib.mo_param_count.restype = C.c_int64
+        lib.mo_param_count.argtypes = [C.c_int] * 4
+        lib.mo_forward.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int64, P]
+        lib.mo_loss_grad.restype = C.c_double
+        lib.mo_loss_grad.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, C.c_int64, P]
+        lib.mo_adam.argtypes = [P, P, P, P, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_double,
+                                C.c_int]
         _lib = lib
     return _lib
 
@@ -149,3 +156,37 @@ class OracleProblem:
                            rnorm=st.rnorm)
         finally:
             self.lib.fo_precond_destroy(pc)
+
+
+# ---- learned-guess MLP (oracle/mlp_oracle.c) ----------------------------------
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def mlp_param_count(dims):
+    return int(load().mo_param_count(*dims))
+
+
+def mlp_forward(params, dims, x):
+    """FP64 forward pass; dims = (nin, h1, h2, nout), x [n, nin] -> y [n, nout]."""
+    params, x = _f64(params), _f64(x)
+    y = np.zeros((x.shape[0], dims[3]))
+    load().mo_forward(_p(params), *dims, _p(x), x.shape[0], _p(y))
+    return y
+
+
+def mlp_loss_grad(params, dims, x, t, mask=None):
+    """Masked mean-squared loss and its gradient (packed like the parameters)."""
+    params, x, t = _f64(params), _f64(x), _f64(t)
+    mask = None if mask is None else _f64(mask)
+    g = np.zeros(mlp_param_count(dims))
+    loss = load().mo_loss_grad(_p(params), *dims, _p(x), _p(t), _p(mask), x.shape[0], _p(g))
+    return loss, g
+
+
+def mlp_adam(params, m, v, grad, lr, step, beta1=0.9, beta2=0.999, eps=1e-8):
+    """One Adam step in place on FP64 copies; returns (params, m, v)."""
+    params, m, v, grad = _f64(params).copy(), _f64(m).copy(), _f64(v).copy(), _f64(grad)
+    load().mo_adam(_p(params), _p(m), _p(v), _p(grad), params.size, lr, beta1, beta2, eps, step)
+    return params, m, v

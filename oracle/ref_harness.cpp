@@ -12,7 +12,7 @@
 // the CSR row) and solves with the vendored Eigen SparseLU.
 //
 // usage: ref_harness <mesh.msh> <problem> <outdir> [Re] [seed]
-//   problem: diffusion | ns_kovasznay | ns_mms
+//   problem: diffusion | ns_kovasznay | ns_mms | ns_cavity_bdf2 (then [dt] [steps])
 // writes raw little-endian arrays (see write_* calls) and meta.txt.
 #include <Eigen/Sparse>
 #include <Eigen/SparseLU>
@@ -39,6 +39,9 @@ class feLinearSystemRef : public feLinearSystem {
   CSR *crs;
   std::vector<double> values, rhs, du;
   double lastAxb = 0;
+  Eigen::SparseMatrix<double> A;
+  Eigen::SparseLU<Eigen::SparseMatrix<double>> lu;
+  bool factored = false;
 
   feLinearSystemRef(std::vector<feBilinearForm *> forms, const feMetaNumber *numbering)
     : feLinearSystem(forms, numbering)
@@ -63,7 +66,13 @@ class feLinearSystemRef : public feLinearSystem {
     for(double v : du) m = std::max(m, std::fabs(v));
     *norm = m;
   }
-  void setToZero() override { setMatrixToZero(); setResidualToZero(); }
+  // As feLinearSystemMklPardiso::setToZero (:967-971): the matrix is kept
+  // when the Newton driver reuses the Jacobian.
+  void setToZero() override
+  {
+    if(_recomputeMatrix) setMatrixToZero();
+    setResidualToZero();
+  }
   void setMatrixToZero() override { std::fill(values.begin(), values.end(), 0.); }
   void setResidualToZero() override { std::fill(rhs.begin(), rhs.end(), 0.); }
   void assemble(const feSolution *sol, const bool onlyTransient) override
@@ -136,18 +145,22 @@ class feLinearSystemRef : public feLinearSystem {
   void permute() override {}
   bool solve(double *normDx, double *normResidual, double *normAxb, int *nIter) override
   {
+    // As feLinearSystemMklPardiso::solve (:893-965): factor only when the
+    // matrix was recomputed, otherwise solve with the previous factors.
     const auto &ia = crs->ia();
     const auto &ja = crs->ja();
-    std::vector<Eigen::Triplet<double>> trip;
-    trip.reserve(values.size());
-    for(feInt r = 0; r < nInc; ++r)
-      for(feInt k = ia[r]; k < ia[r + 1]; ++k) trip.emplace_back(r, ja[k], values[k]);
-    Eigen::SparseMatrix<double> A(nInc, nInc);
-    A.setFromTriplets(trip.begin(), trip.end());
-    A.makeCompressed();
-    Eigen::SparseLU<Eigen::SparseMatrix<double>> lu;
-    lu.compute(A);
-    if(lu.info() != Eigen::Success) return false;
+    if(_recomputeMatrix || !factored) {
+      std::vector<Eigen::Triplet<double>> trip;
+      trip.reserve(values.size());
+      for(feInt r = 0; r < nInc; ++r)
+        for(feInt k = ia[r]; k < ia[r + 1]; ++k) trip.emplace_back(r, ja[k], values[k]);
+      A = Eigen::SparseMatrix<double>(nInc, nInc);
+      A.setFromTriplets(trip.begin(), trip.end());
+      A.makeCompressed();
+      lu.compute(A);
+      if(lu.info() != Eigen::Success) return false;
+      factored = true;
+    }
     Eigen::Map<Eigen::VectorXd> b(rhs.data(), nInc);
     Eigen::VectorXd x = lu.solve(b);
     for(feInt i = 0; i < nInc; ++i) du[i] = x[i];
@@ -191,6 +204,15 @@ void write_raw(const std::string &path, const std::vector<T> &v)
 }
 
 double g_re = 40.0;
+double g_dt = 0.01;
+int g_steps = 6;
+
+// Lid-driven cavity: u = (1, 0) on the lid y = 1, zero elsewhere.
+void cavity_lid(const feFunctionArguments &a, const std::vector<double> &, std::vector<double> &r)
+{
+  r[0] = std::fabs(a.pos[1] - 1.0) <= 1e-12 ? 1.0 : 0.0;
+  r[1] = 0.0;
+}
 
 double sinsin(const feFunctionArguments &a, const std::vector<double> &)
 {
@@ -242,18 +264,22 @@ void mms_src(const feFunctionArguments &a, const std::vector<double> &, std::vec
 int main(int argc, char **argv)
 {
   if(argc < 4) {
-    fprintf(stderr, "usage: %s mesh.msh diffusion|ns_kovasznay|ns_mms outdir [Re] [seed]\n", argv[0]);
+    fprintf(stderr, "usage: %s mesh.msh diffusion|ns_kovasznay|ns_mms|ns_cavity_bdf2 outdir [Re] [seed] [dt] [steps]\n", argv[0]);
     return 2;
   }
   const std::string meshFile = argv[1], problem = argv[2], out = argv[3];
   if(argc > 4) g_re = atof(argv[4]);
   const unsigned long seed = argc > 5 ? strtoul(argv[5], nullptr, 10) : 1;
-  setVerbose(0);
+  if(argc > 6) g_dt = atof(argv[6]);
+  if(argc > 7) g_steps = atoi(argv[7]);
+  setVerbose(getenv("FE_HARNESS_VERBOSE") ? atoi(getenv("FE_HARNESS_VERBOSE")) : 0);
 
   feMesh2DP1 mesh(meshFile);
   feFunction fSinSin(sinsin), fSrc(sinsin_src), fKovP(kov_p), fMmsP(mms_p);
   feVectorFunction fKovU(kov_u), fMmsU(mms_u), fMmsSrc(mms_src);
   feConstantFunction fMu(1.0 / g_re);
+  feVectorFunction fLid(cavity_lid);
+  const bool cavity = problem == "ns_cavity_bdf2";
 
   std::vector<feSpace *> spaces, essential, domainSpaces;
   std::vector<feBilinearForm *> forms;
@@ -269,8 +295,8 @@ int main(int argc, char **argv)
     degQ = 8;
     const bool kov = problem == "ns_kovasznay";
     feSpace *u = nullptr, *uB = nullptr, *p = nullptr, *pP = nullptr;
-    const feVectorFunction *uex = kov ? &fKovU : &fMmsU;
-    const feFunction *pex = kov ? &fKovP : &fMmsP;
+    const feVectorFunction *uex = cavity ? &fLid : kov ? &fKovU : &fMmsU;
+    const feFunction *pex = cavity ? &scalarConstant::zero : kov ? &fKovP : &fMmsP;
     feCheck(createFiniteElementSpace(u, &mesh, elementType::VECTOR_LAGRANGE, 2, "U", "Domaine", degQ, uex));
     feCheck(createFiniteElementSpace(uB, &mesh, elementType::VECTOR_LAGRANGE, 2, "U", "Bord", degQ, uex));
     feCheck(createFiniteElementSpace(p, &mesh, elementType::LAGRANGE, 1, "P", "Domaine", degQ, pex));
@@ -291,11 +317,19 @@ int main(int argc, char **argv)
     feSpace *u = domainSpaces[0], *p = domainSpaces[1];
     const bool kov = problem == "ns_kovasznay";
     feBilinearForm *conv = nullptr, *divU = nullptr, *sigma = nullptr, *src = nullptr;
-    feCheck(createBilinearForm(conv, {u}, new feSysElm_VectorConvectiveAcceleration<2>(&scalarConstant::minusOne)));
+    // Sign convention of the steady tests (navier_stokes.cpp:83-90), or of
+    // the unsteady ones (vectorFEunsteady.cpp:562-584) for the cavity.
+    const feConstantFunction *cConv = cavity ? &scalarConstant::one : &scalarConstant::minusOne;
+    const feConstantFunction *cSigma = cavity ? &scalarConstant::minusOne : &scalarConstant::one;
+    feCheck(createBilinearForm(conv, {u}, new feSysElm_VectorConvectiveAcceleration<2>(cConv)));
     feCheck(createBilinearForm(divU, {p, u}, new feSysElm_MixedDivergence<2>(&scalarConstant::one)));
-    feCheck(createBilinearForm(sigma, {u, p}, new feSysElm_DivergenceNewtonianStress<2>(&scalarConstant::one, kov ? &fMu : &scalarConstant::one)));
+    feCheck(createBilinearForm(sigma, {u, p}, new feSysElm_DivergenceNewtonianStress<2>(cSigma, (kov || cavity) ? &fMu : &scalarConstant::one)));
     forms = {conv, divU, sigma};
-    if(!kov) {
+    if(cavity) {
+      feBilinearForm *mass = nullptr;
+      feCheck(createBilinearForm(mass, {u}, new feSysElm_TransientVectorMass<2>(&scalarConstant::one)));
+      forms.insert(forms.begin(), mass);
+    } else if(!kov) {
       feCheck(createBilinearForm(src, {u}, new feSysElm_VectorSource<2>(&fMmsSrc)));
       forms.push_back(src);
     }
@@ -331,6 +365,36 @@ int main(int argc, char **argv)
     const auto &r = s->getRQuadraturePoints();
     const auto &q = s->getSQuadraturePoints();
     for(size_t k = 0; k < w.size(); ++k) { quad.push_back(r[k]); quad.push_back(q[k]); quad.push_back(w[k]); }
+  }
+
+  if(cavity) {
+    // BDF2 from rest (BDF1 starter of 0.1 dt, the reference's default) with
+    // tight absolute Newton tolerances; writes the solution after every step.
+    const int nSteps = g_steps;
+    TimeIntegrator *ti = nullptr;
+    std::vector<feNorm *> norms;
+    feNLSolverOptions NL{1e-11, 1e-13, 1e12, 30, 3, 1e-1};
+    feCheck(createTimeIntegrator(ti, timeIntegratorScheme::BDF2, NL, sys, &sol, &mesh, norms, {nullptr, 1, ""},
+                                 0.0, nSteps * g_dt, nSteps));
+    feCheck(ti->makeSteps(nSteps));
+    std::vector<double> traj = sol.getSolution();
+    write_raw(out + "/ia.i64", ia);
+    write_raw(out + "/ja.i64", ja);
+    write_raw(out + "/adr.i64", adr);
+    write_raw(out + "/color_offsets.i64", colOff);
+    write_raw(out + "/color_elements.i32", colEl);
+    write_raw(out + "/traj.f64", traj);
+    write_raw(out + "/quad.f64", quad);
+    FILE *f = fopen((out + "/meta.txt").c_str(), "w");
+    fprintf(f, "problem %s\nnInc %ld\nnDofs %ld\nnnz %zu\nnElm %d\nnColors %d\nnloc %zu\nquad_degree %d\nre %.17g\nseed %lu\ndt %.17g\nsteps %d\n",
+            problem.c_str(), (long)nInc, (long)nDofs, ja.size(), nElm, cnc->getNbColor(),
+            adr.size() / nElm, degQ, g_re, seed, g_dt, nSteps);
+    fclose(f);
+    delete ti;
+    delete sys;
+    for(auto *fm : forms) delete fm;
+    for(auto *s : spaces) delete s;
+    return 0;
   }
 
   // Assembly state: essential values from the exact solution, unknowns

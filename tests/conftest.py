@@ -28,5 +28,12 @@ def load_golden(name):
         return {k: z[k] for k in z.files}
 
 
-def golden_names():
-    return sorted(p.stem for p in GOLDEN.glob("*.npz"))
+def golden_names(transient=False):
+    """Fixture names: the steady cases (assembly state + Newton solution), or
+    the BDF2 runs with transient=True."""
+    out = []
+    for p in sorted(GOLDEN.glob("*.npz")):
+        with np.load(p) as z:
+            if ("steps" in z.files) == transient:
+                out.append(p.stem)
+    return out

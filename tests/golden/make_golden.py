@@ -5,8 +5,9 @@ Needs the reference checkout (default /root/reference) and a C++ compiler:
 it builds oracle/_ref/ref_harness with oracle/Makefile, writes each seeded
 mesh with this package's generator (the same file the backend reads), runs
 the reference's spaces, numbering, coloring, CSR pattern, element kernels
-and a Newton solve on it, and stores the arrays as compressed .npz files
-next to this script.
+and a Newton solve (or a BDF2 run of the lid-driven cavity with the
+reference's BDF2Integrator) on it, and stores the arrays as compressed .npz
+files next to this script.
 
     python tests/golden/make_golden.py [--ref /root/reference]
 """
@@ -32,6 +33,10 @@ CASES = [
     ("diffusion_p2_16", "diffusion", 16, (0.0, 1.0, 0.0, 1.0), 40.0, 2),
     ("kovasznay_th_8", "ns_kovasznay", 8, (-0.5, 1.5, -0.5, 1.5), 40.0, 1),
     ("ns_mms_th_8", "ns_mms", 8, (0.0, 1.0, 0.0, 1.0), 40.0, 3),
+]
+# BDF2 lid-driven cavity from rest: name, n, Re, seed, dt, steps
+TRANSIENT = [
+    ("cavity_bdf2_8", 8, 100.0, 5, 0.01, 6),
 ]
 
 
@@ -64,6 +69,29 @@ def main():
                 u0=np.fromfile(td / "u0.f64"), values0=np.fromfile(td / "values0.f64"),
                 rhs0=np.fromfile(td / "rhs0.f64"), usol=np.fromfile(td / "usol.f64"),
                 quad=np.fromfile(td / "quad.f64").reshape(-1, 3),
+            )
+            np.savez_compressed(HERE / f"{name}.npz", **out)
+            print(name, meta["nInc"], meta["nDofs"], len(out["ja"]))
+    for name, n, re, seed, dt, steps in TRANSIENT:
+        with tempfile.TemporaryDirectory() as td:
+            td = Path(td)
+            mesh = fe.Mesh2DP1.generate_square(n, 0.0, 1.0, 0.0, 1.0, jitter=0.1, seed=seed)
+            mesh.write_msh(td / "mesh.msh")
+            subprocess.run([str(harness), str(td / "mesh.msh"), "ns_cavity_bdf2", str(td), str(re), str(seed),
+                            repr(dt), str(steps)], check=True)
+            meta = dict(l.split(maxsplit=1) for l in (td / "meta.txt").read_text().splitlines())
+            arr = mesh.arrays()
+            out = dict(
+                problem=np.array("ns_cavity_bdf2"), n=np.int64(n), domain=np.array((0.0, 1.0, 0.0, 1.0)),
+                re=np.float64(re), seed=np.int64(seed), jitter=np.float64(0.1), dt=np.float64(dt),
+                steps=np.int64(steps), nInc=np.int64(meta["nInc"]), nDofs=np.int64(meta["nDofs"]),
+                quad_degree=np.int64(meta["quad_degree"]),
+                x=arr["x"], y=arr["y"], tri=arr["tri"], bnd=arr["bnd"],
+                ia=np.fromfile(td / "ia.i64", np.int64), ja=np.fromfile(td / "ja.i64", np.int64),
+                adr=np.fromfile(td / "adr.i64", np.int64),
+                color_offsets=np.fromfile(td / "color_offsets.i64", np.int64),
+                color_elements=np.fromfile(td / "color_elements.i32", np.int32),
+                usol=np.fromfile(td / "traj.f64"), quad=np.fromfile(td / "quad.f64").reshape(-1, 3),
             )
             np.savez_compressed(HERE / f"{name}.npz", **out)
             print(name, meta["nInc"], meta["nDofs"], len(out["ja"]))

@@ -15,6 +15,8 @@ def problem_spaces(problem, mesh, re=40.0):
         forms = [fe.createBilinearForm([u], fe.feSysElm_Diffusion(1.0)),
                  fe.createBilinearForm([u], fe.feSysElm_Source(fe.api.SRC_SIN_SIN, (-2 * np.pi ** 2,)))]
         return num, forms
+    if problem == "ns_cavity_bdf2":
+        return cavity_spaces(mesh, re)
     kov = problem == "ns_kovasznay"
     uex = exact.kovasznay_velocity(re) if kov else exact.ns_mms_velocity
     pex = exact.kovasznay_pressure(re) if kov else exact.ns_mms_pressure
@@ -28,6 +30,23 @@ def problem_spaces(problem, mesh, re=40.0):
              fe.createBilinearForm([u, p], fe.feSysElm_DivergenceNewtonianStress(1.0, 1.0 / re if kov else 1.0))]
     if not kov:
         forms.append(fe.createBilinearForm([u], fe.feSysElm_VectorSource(fe.api.SRC_NS_MMS_POLY)))
+    return num, forms
+
+
+def cavity_spaces(mesh, re):
+    """Lid-driven cavity with the transient forms and the sign convention of
+    the reference's unsteady Navier-Stokes test
+    (tests/withLinearSolver/vectorFEunsteady.cpp:560-584)."""
+    lid = exact.cavity_lid()
+    u = fe.createFiniteElementSpace(mesh, fe.VECTOR_LAGRANGE, 2, "U", "Domaine", 8, lid)
+    uB = fe.createFiniteElementSpace(mesh, fe.VECTOR_LAGRANGE, 2, "U", "Bord", 8, lid)
+    p = fe.createFiniteElementSpace(mesh, fe.LAGRANGE, 1, "P", "Domaine", 8, exact.zero_scalar)
+    pP = fe.createFiniteElementSpace(mesh, fe.LAGRANGE, 1, "P", "PointPression", 8, exact.zero_scalar)
+    num = fe.feMetaNumber(mesh, [u, uB, p, pP], [uB, pP])
+    forms = [fe.createBilinearForm([u], fe.feSysElm_TransientVectorMass(1.0)),
+             fe.createBilinearForm([u], fe.feSysElm_VectorConvectiveAcceleration(1.0)),
+             fe.createBilinearForm([p, u], fe.feSysElm_MixedDivergence(1.0)),
+             fe.createBilinearForm([u, p], fe.feSysElm_DivergenceNewtonianStress(-1.0, 1.0 / re))]
     return num, forms
 
 

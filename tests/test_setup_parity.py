@@ -10,7 +10,10 @@ from helpers import golden_mesh, problem_spaces
 from feng_gb300.api import quadrature_rule
 
 
-@pytest.mark.parametrize("name", golden_names())
+ALL = golden_names() + golden_names(transient=True)
+
+
+@pytest.mark.parametrize("name", ALL)
 def test_mesh_generator_reproduces_fixture(name):
     g = load_golden(name)
     a = golden_mesh(g).arrays()
@@ -20,7 +23,7 @@ def test_mesh_generator_reproduces_fixture(name):
     np.testing.assert_allclose(a["y"], g["y"], rtol=0, atol=1e-15)
 
 
-@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("name", ALL)
 def test_numbering_pattern_coloring_bit_exact(name):
     g = load_golden(name)
     num, _ = problem_spaces(str(g["problem"]), golden_mesh(g), float(g["re"]))
