@@ -25,8 +25,54 @@ namespace {
 
 int grid(int64_t n, int per = 256) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + per - 1) / per, 1 << 20)); }
 
+// Vectors hold NV interleaved components per row (NV = 2: both velocity
+// components of a node share one pass over the matrix).
+template <typename V, int NV>
+struct Vals {
+  V v[NV];
+};
+
+template <typename V, int NV>
+__device__ __forceinline__ Vals<V, NV> ldv(const V *__restrict__ p, int64_t i)
+{
+  Vals<V, NV> r;
+  if constexpr(NV == 2 && sizeof(V) == 4) {
+    const float2 t = *reinterpret_cast<const float2 *>(p + 2 * i);
+    r.v[0] = t.x;
+    r.v[1] = t.y;
+  } else if constexpr(NV == 2 && sizeof(V) == 8) {
+    const double2 t = *reinterpret_cast<const double2 *>(p + 2 * i);
+    r.v[0] = t.x;
+    r.v[1] = t.y;
+  } else {
+#pragma unroll
+    for(int c = 0; c < NV; ++c) r.v[c] = p[i * NV + c];
+  }
+  return r;
+}
+
+// Row dot products acc[c] = sum_k a[k] x[ja[k]][c] over LANES lanes per row
+// (result valid in lane 0 of the row).
+template <typename V, int LANES, int NV>
+__device__ __forceinline__ void row_dot(int32_t beg, int32_t end, int sub, const int32_t *__restrict__ ja,
+                                        const V *__restrict__ a, const V *__restrict__ x, V (&acc)[NV])
+{
+#pragma unroll
+  for(int c = 0; c < NV; ++c) acc[c] = 0;
+  for(int32_t k = beg + sub; k < end; k += LANES) {
+    const V ak = a[k];
+    const Vals<V, NV> xv = ldv<V, NV>(x, ja[k]);
+#pragma unroll
+    for(int c = 0; c < NV; ++c) acc[c] += ak * xv.v[c];
+  }
+#pragma unroll
+  for(int c = 0; c < NV; ++c)
+#pragma unroll
+    for(int o = LANES / 2; o > 0; o >>= 1) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], o, LANES);
+}
+
 // y = A x (MODE 0), y = b - A x (MODE 1), y += A x (MODE 2)
-template <typename V, int LANES, int MODE>
+template <typename V, int LANES, int MODE, int NV>
 __global__ void __launch_bounds__(256) k_csr(int64_t n, const int32_t *__restrict__ ia,
                                              const int32_t *__restrict__ ja, const V *__restrict__ a,
                                              const V *__restrict__ x, const V *__restrict__ b,
@@ -37,35 +83,37 @@ __global__ void __launch_bounds__(256) k_csr(int64_t n, const int32_t *__restric
   const int sub = threadIdx.x % LANES;
   const bool live = row < n;
   const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
-  V acc = 0;
-  for(int32_t k = beg + sub; k < end; k += LANES) acc += a[k] * x[ja[k]];
-#pragma unroll
-  for(int o = LANES / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, LANES);
+  V acc[NV];
+  row_dot<V, LANES, NV>(beg, end, sub, ja, a, x, acc);
   if(live && sub == 0) {
-    if(MODE == 0) y[row] = acc;
-    else if(MODE == 1) y[row] = b[row] - acc;
-    else y[row] += acc;
+#pragma unroll
+    for(int c = 0; c < NV; ++c) {
+      const int64_t o = row * NV + c;
+      if(MODE == 0) y[o] = acc[c];
+      else if(MODE == 1) y[o] = b[o] - acc[c];
+      else y[o] += acc[c];
+    }
   }
 }
 
-template <typename V, int MODE>
+template <typename V, int MODE, int NV>
 void csr(int lanes, int64_t n, const int32_t *ia, const int32_t *ja, const V *a, const V *x, const V *b,
          V *y, cudaStream_t s, const int *skip)
 {
   const int g = grid(n * lanes);
-  if(lanes == 8) (k_csr<V, 8, MODE><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y, skip), ::feng::count_launch());
-  else if(lanes == 16) (k_csr<V, 16, MODE><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y, skip), ::feng::count_launch());
-  else (k_csr<V, 4, MODE><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y, skip), ::feng::count_launch());
+  if(lanes == 8) (k_csr<V, 8, MODE, NV><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y, skip), ::feng::count_launch());
+  else if(lanes == 16) (k_csr<V, 16, MODE, NV><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y, skip), ::feng::count_launch());
+  else (k_csr<V, 4, MODE, NV><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y, skip), ::feng::count_launch());
 }
 
 // Chebyshev start (x = 0): r = D^-1 b, d = r / theta, x = 0.
-template <typename V>
+template <typename V, int NV>
 __global__ void k_cheb_start(int64_t n, const V *__restrict__ dinv, const V *__restrict__ b, V *__restrict__ r,
                              V *__restrict__ d, V *__restrict__ x, V inv_theta, const int *__restrict__ skip)
 {
   if(skip && *skip) return;
-  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const V ri = dinv[i] * b[i];
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * NV; i += (int64_t)gridDim.x * blockDim.x) {
+    const V ri = dinv[i / NV] * b[i];
     r[i] = ri;
     d[i] = ri * inv_theta;
     x[i] = 0;
@@ -73,7 +121,7 @@ __global__ void k_cheb_start(int64_t n, const V *__restrict__ dinv, const V *__r
 }
 
 // Chebyshev start from a nonzero x: r = D^-1 (b - A x), d = r / theta.
-template <typename V, int LANES>
+template <typename V, int LANES, int NV>
 __global__ void __launch_bounds__(256) k_cheb_restart(int64_t n, const int32_t *__restrict__ ia,
                                                       const int32_t *__restrict__ ja, const V *__restrict__ a,
                                                       const V *__restrict__ dinv, const V *__restrict__ b,
@@ -85,19 +133,22 @@ __global__ void __launch_bounds__(256) k_cheb_restart(int64_t n, const int32_t *
   const int sub = threadIdx.x % LANES;
   const bool live = row < n;
   const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
-  V acc = 0;
-  for(int32_t k = beg + sub; k < end; k += LANES) acc += a[k] * x[ja[k]];
-#pragma unroll
-  for(int o = LANES / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, LANES);
+  V acc[NV];
+  row_dot<V, LANES, NV>(beg, end, sub, ja, a, x, acc);
   if(live && sub == 0) {
-    const V ri = dinv[row] * (b[row] - acc);
-    r[row] = ri;
-    d[row] = ri * inv_theta;
+    const V di = dinv[row];
+#pragma unroll
+    for(int c = 0; c < NV; ++c) {
+      const int64_t o = row * NV + c;
+      const V ri = di * (b[o] - acc[c]);
+      r[o] = ri;
+      d[o] = ri * inv_theta;
+    }
   }
 }
 
 // One Chebyshev step: x += d; r -= D^-1 A d; dn = c1 d + c2 r.
-template <typename V, int LANES>
+template <typename V, int LANES, int NV>
 __global__ void __launch_bounds__(256) k_cheb_step(int64_t n, const int32_t *__restrict__ ia,
                                                    const int32_t *__restrict__ ja, const V *__restrict__ a,
                                                    const V *__restrict__ dinv, const V *__restrict__ d,
@@ -109,21 +160,24 @@ __global__ void __launch_bounds__(256) k_cheb_step(int64_t n, const int32_t *__r
   const int sub = threadIdx.x % LANES;
   const bool live = row < n;
   const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
-  V acc = 0;
-  for(int32_t k = beg + sub; k < end; k += LANES) acc += a[k] * d[ja[k]];
-#pragma unroll
-  for(int o = LANES / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, LANES);
+  V acc[NV];
+  row_dot<V, LANES, NV>(beg, end, sub, ja, a, d, acc);
   if(live && sub == 0) {
-    const V di = d[row];
-    x[row] += di;
-    const V ri = r[row] - dinv[row] * acc;
-    r[row] = ri;
-    dn[row] = c1 * di + c2 * ri;
+    const V dv = dinv[row];
+#pragma unroll
+    for(int c = 0; c < NV; ++c) {
+      const int64_t o = row * NV + c;
+      const V di = d[o];
+      x[o] += di;
+      const V ri = r[o] - dv * acc[c];
+      r[o] = ri;
+      dn[o] = c1 * di + c2 * ri;
+    }
   }
 }
 
 // x = Minv b for the coarsest level (dense, row-major), one warp per row.
-template <typename V>
+template <typename V, int NV>
 __global__ void k_dense(int64_t n, const V *__restrict__ M, const V *__restrict__ b, V *__restrict__ x,
                         const int *__restrict__ skip)
 {
@@ -131,11 +185,21 @@ __global__ void k_dense(int64_t n, const V *__restrict__ M, const V *__restrict_
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
   const int lane = threadIdx.x % 32;
   const bool live = row < n;
-  V acc = 0;
+  V acc[NV];
+#pragma unroll
+  for(int c = 0; c < NV; ++c) acc[c] = 0;
   if(live)
-    for(int64_t k = lane; k < n; k += 32) acc += M[row * n + k] * b[k];
-  for(int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  if(live && lane == 0) x[row] = acc;
+    for(int64_t k = lane; k < n; k += 32) {
+      const V m = M[row * n + k];
+#pragma unroll
+      for(int c = 0; c < NV; ++c) acc[c] += m * b[k * NV + c];
+    }
+#pragma unroll
+  for(int c = 0; c < NV; ++c)
+    for(int o = 16; o > 0; o >>= 1) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], o);
+  if(live && lane == 0)
+#pragma unroll
+    for(int c = 0; c < NV; ++c) x[row * NV + c] = acc[c];
 }
 
 template <typename V>
@@ -200,7 +264,8 @@ int AMGDevice::upload(const AMGHierarchy &H, const AMGParams &p, int fp32, cudaS
     FE_TRY(upload_idx(&L.Aja, h.A.ja));
     FE_TRY(fp32 ? upload_vec<float>(&L.Aa, h.A.a) : upload_vec<double>(&L.Aa, h.A.a));
     FE_TRY(fp32 ? upload_vec<float>(&L.dinv, h.dinv) : upload_vec<double>(&L.dinv, h.dinv));
-    for(void **v : {&L.x, &L.b, &L.r, &L.d0, &L.d1}) CKA(cudaMalloc(v, vs * std::max<int64_t>(1, L.n)));
+    // room for two interleaved components (vcycle2)
+    for(void **v : {&L.x, &L.b, &L.r, &L.d0, &L.d1}) CKA(cudaMalloc(v, 2 * vs * std::max<int64_t>(1, L.n)));
     if(l + 1 < H.levels.size()) {
       L.nc = h.P.m;
       L.lanesP = lanes_for(h.P);
@@ -218,7 +283,7 @@ int AMGDevice::upload(const AMGHierarchy &H, const AMGParams &p, int fp32, cudaS
   return FE_OK;
 }
 
-template <typename V>
+template <typename V, int NV>
 static void chebyshev(int lanes, int64_t n, const int32_t *ia, const int32_t *ja, const V *a, const V *dinv,
                       const V *b, V *x, V *r, V *d0, V *d1, double lmax, const AMGParams &p, bool zeroStart,
                       cudaStream_t s, const int *skip)
@@ -229,58 +294,61 @@ static void chebyshev(int lanes, int64_t n, const int32_t *ia, const int32_t *ja
   double rho = 1.0 / sigma;
   const int g = grid(n * lanes);
   if(zeroStart) {
-    (k_cheb_start<V><<<grid(n), 256, 0, s>>>(n, dinv, b, r, d0, x, (V)(1.0 / theta), skip), ::feng::count_launch());
+    (k_cheb_start<V, NV><<<grid(n * NV), 256, 0, s>>>(n, dinv, b, r, d0, x, (V)(1.0 / theta), skip),
+     ::feng::count_launch());
   } else {
-    if(lanes == 16) (k_cheb_restart<V, 16><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip), ::feng::count_launch());
-    else if(lanes == 8) (k_cheb_restart<V, 8><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip), ::feng::count_launch());
-    else (k_cheb_restart<V, 4><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip), ::feng::count_launch());
+    if(lanes == 16) (k_cheb_restart<V, 16, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip), ::feng::count_launch());
+    else if(lanes == 8) (k_cheb_restart<V, 8, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip), ::feng::count_launch());
+    else (k_cheb_restart<V, 4, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip), ::feng::count_launch());
   }
   V *d = d0, *dn = d1;
   for(int k = 0; k < p.chebyDegree; ++k) {
     const double rhoN = 1.0 / (2.0 * sigma - rho);
     const V c1 = (V)(rhoN * rho), c2 = (V)(2.0 * rhoN / delta);
-    if(lanes == 16) (k_cheb_step<V, 16><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2, skip), ::feng::count_launch());
-    else if(lanes == 8) (k_cheb_step<V, 8><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2, skip), ::feng::count_launch());
-    else (k_cheb_step<V, 4><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2, skip), ::feng::count_launch());
+    if(lanes == 16) (k_cheb_step<V, 16, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2, skip), ::feng::count_launch());
+    else if(lanes == 8) (k_cheb_step<V, 8, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2, skip), ::feng::count_launch());
+    else (k_cheb_step<V, 4, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2, skip), ::feng::count_launch());
     rho = rhoN;
     std::swap(d, dn);
   }
 }
 
-template <typename V>
+template <typename V, int NV>
 void AMGDevice::vcycle_t(int l, const V *b, V *x)
 {
   Lev &L = lv_[l];
   if(l == (int)lv_.size() - 1) {
-    (k_dense<V><<<grid(L.n * 32), 256, 0, s_>>>(L.n, (const V *)coarseInv_, b, x, skip_), ::feng::count_launch());
+    (k_dense<V, NV><<<grid(L.n * 32), 256, 0, s_>>>(L.n, (const V *)coarseInv_, b, x, skip_), ::feng::count_launch());
     return;
   }
   Lev &C = lv_[l + 1];
   const V *A = (const V *)L.Aa;
-  chebyshev<V>(L.lanesA, L.n, L.Aia, L.Aja, A, (const V *)L.dinv, b, x, (V *)L.r, (V *)L.d0, (V *)L.d1,
-               L.lmax, p_, true, s_, skip_);
+  chebyshev<V, NV>(L.lanesA, L.n, L.Aia, L.Aja, A, (const V *)L.dinv, b, x, (V *)L.r, (V *)L.d0, (V *)L.d1,
+                   L.lmax, p_, true, s_, skip_);
   // residual r = b - A x, restrict into the coarse right-hand side
-  csr<V, 1>(L.lanesA, L.n, L.Aia, L.Aja, A, x, b, (V *)L.r, s_, skip_);
-  csr<V, 0>(L.lanesR, C.n, L.Ria, L.Rja, (const V *)L.Ra, (const V *)L.r, nullptr, (V *)C.b, s_, skip_);
-  vcycle_t<V>(l + 1, (const V *)C.b, (V *)C.x);
-  csr<V, 2>(L.lanesP, L.n, L.Pia, L.Pja, (const V *)L.Pa, (const V *)C.x, nullptr, x, s_, skip_);
-  chebyshev<V>(L.lanesA, L.n, L.Aia, L.Aja, A, (const V *)L.dinv, b, x, (V *)L.r, (V *)L.d0, (V *)L.d1,
-               L.lmax, p_, false, s_, skip_);
+  csr<V, 1, NV>(L.lanesA, L.n, L.Aia, L.Aja, A, x, b, (V *)L.r, s_, skip_);
+  csr<V, 0, NV>(L.lanesR, C.n, L.Ria, L.Rja, (const V *)L.Ra, (const V *)L.r, nullptr, (V *)C.b, s_, skip_);
+  vcycle_t<V, NV>(l + 1, (const V *)C.b, (V *)C.x);
+  csr<V, 2, NV>(L.lanesP, L.n, L.Pia, L.Pja, (const V *)L.Pa, (const V *)C.x, nullptr, x, s_, skip_);
+  chebyshev<V, NV>(L.lanesA, L.n, L.Aia, L.Aja, A, (const V *)L.dinv, b, x, (V *)L.r, (V *)L.d0, (V *)L.d1,
+                   L.lmax, p_, false, s_, skip_);
 }
 
-void AMGDevice::vcycle64(const double *b, double *x) { vcycle_t<double>(0, b, x); }
-void AMGDevice::vcycle32(const float *b, float *x) { vcycle_t<float>(0, b, x); }
+void AMGDevice::vcycle64(const double *b, double *x) { vcycle_t<double, 1>(0, b, x); }
+void AMGDevice::vcycle32(const float *b, float *x) { vcycle_t<float, 1>(0, b, x); }
+void AMGDevice::vcycle2_64(const double *b, double *x) { vcycle_t<double, 2>(0, b, x); }
+void AMGDevice::vcycle2_32(const float *b, float *x) { vcycle_t<float, 2>(0, b, x); }
 
 void AMGDevice::spmv64(const double *x, double *y)
 {
   const Lev &L = lv_[0];
-  csr<double, 0>(L.lanesA, L.n, L.Aia, L.Aja, (const double *)L.Aa, x, nullptr, y, s_, skip_);
+  csr<double, 0, 1>(L.lanesA, L.n, L.Aia, L.Aja, (const double *)L.Aa, x, nullptr, y, s_, skip_);
 }
 
 void AMGDevice::spmv32(const float *x, float *y)
 {
   const Lev &L = lv_[0];
-  csr<float, 0>(L.lanesA, L.n, L.Aia, L.Aja, (const float *)L.Aa, x, nullptr, y, s_, skip_);
+  csr<float, 0, 1>(L.lanesA, L.n, L.Aia, L.Aja, (const float *)L.Aa, x, nullptr, y, s_, skip_);
 }
 
 }  // namespace feng

@@ -58,6 +58,10 @@ class AMGDevice {
   // x = V-cycle(b) for the finest operator (x overwritten).
   void vcycle64(const double *b, double *x);
   void vcycle32(const float *b, float *x);
+  // The same V-cycle on two right-hand sides stored interleaved
+  // (b[2 i + c], component c of row i): one pass over each operator.
+  void vcycle2_64(const double *b, double *x);
+  void vcycle2_32(const float *b, float *x);
   // y = A x with the finest operator.
   void spmv64(const double *x, double *y);
   void spmv32(const float *x, float *y);
@@ -74,7 +78,7 @@ class AMGDevice {
     double lmax = 0;
     int lanesA = 4, lanesP = 4, lanesR = 4;
   };
-  template <typename V> void vcycle_t(int l, const V *b, V *x);
+  template <typename V, int NV> void vcycle_t(int l, const V *b, V *x);
   std::vector<Lev> lv_;
   void *coarseInv_ = nullptr;
   int64_t nCoarse_ = 0, n0_ = 0;

@@ -306,6 +306,122 @@ __global__ void k_xupdate(int64_t n, const VZ *__restrict__ Z, const GmresState 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Classical Gram-Schmidt passes on the FP32 Krylov basis of the mixed cycle
+// (V column-major with leading dimension n, columns c < ncols <= CMAX):
+//   MODE 0: h_c = V_c . w
+//   MODE 1: w -= V hprev, then h_c = V_c . w   (the second CGS pass)
+//   MODE 2: w -= V hprev, then ss = w . w
+// One read of V and w per pass, FP32 products, per-block partial sums in
+// FP64; the last block sums the partials in block order (deterministic) and
+// writes hcur / Hcol (MODE 0: Hcol = h, MODE 1: Hcol += h) or ss into
+// st->result[0].  The FP64 pipe of the GB300 is too slow for these loops.
+// ---------------------------------------------------------------------------
+template <int CMAX, int MODE>
+__global__ void __launch_bounds__(RB) k_gs32(int64_t n, const float *__restrict__ V, int ncols,
+                                             const double *__restrict__ hprev, float *__restrict__ w,
+                                             double *partials, RedState *st, double *hcur, double *Hcol,
+                                             const int *__restrict__ done)
+{
+  if(*done) return;
+  constexpr int NACC = MODE == 2 ? 1 : CMAX;
+  __shared__ float hs[CMAX];
+  __shared__ float red[RB / 32][NACC];
+  __shared__ bool last;
+  if(MODE > 0) {
+    for(int c = threadIdx.x; c < CMAX; c += RB) hs[c] = c < ncols ? (float)hprev[c] : 0.f;
+    __syncthreads();
+  }
+  float acc[NACC];
+#pragma unroll
+  for(int c = 0; c < NACC; ++c) acc[c] = 0.f;
+  for(int64_t i = (int64_t)blockIdx.x * RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) {
+    float wi = w[i];
+    if(MODE == 0) {
+#pragma unroll
+      for(int c = 0; c < CMAX; ++c)
+        if(c < ncols) acc[c] = fmaf(V[(int64_t)c * n + i], wi, acc[c]);
+    } else {
+      float v[CMAX];
+#pragma unroll
+      for(int c = 0; c < CMAX; ++c)
+        if(c < ncols) {
+          v[c] = V[(int64_t)c * n + i];
+          wi = fmaf(-hs[c], v[c], wi);
+        }
+      w[i] = wi;
+      if(MODE == 1) {
+#pragma unroll
+        for(int c = 0; c < CMAX; ++c)
+          if(c < ncols) acc[c] = fmaf(v[c], wi, acc[c]);
+      } else {
+        acc[0] = fmaf(wi, wi, acc[0]);
+      }
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nr = MODE == 2 ? 1 : ncols;
+#pragma unroll
+  for(int c = 0; c < NACC; ++c) {
+    if(c < nr) {
+      float v = acc[c];
+      for(int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if(lane == 0) red[warp][c] = v;
+    }
+  }
+  __syncthreads();
+  for(int c = threadIdx.x; c < nr; c += RB) {
+    double sum = 0.;
+    for(int k = 0; k < RB / 32; ++k) sum += (double)red[k][c];
+    partials[(int64_t)c * MAXRED + blockIdx.x] = sum;
+    __threadfence();
+  }
+  __syncthreads();
+  if(threadIdx.x == 0) last = atomicAdd(&st->counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if(!last) return;
+  __threadfence();
+  for(int c = warp; c < nr; c += RB / 32) {
+    double sum = 0.;
+    for(int b = lane; b < (int)gridDim.x; b += 32) sum += ((volatile double *)partials)[(int64_t)c * MAXRED + b];
+    for(int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if(lane == 0) {
+      if(MODE == 2) {
+        st->result[0] = sum;
+      } else {
+        hcur[c] = sum;
+        Hcol[c] = MODE == 0 ? sum : Hcol[c] + sum;
+      }
+    }
+  }
+  __syncthreads();
+  if(threadIdx.x == 0) st->counter = 0;
+}
+
+// v = w / sqrt(ss) in FP32 and H[j+1][j] = sqrt(ss); ss in st->result[0].
+__global__ void k_scale32(int64_t n, const float *__restrict__ w, float *__restrict__ v, const RedState *st,
+                          double *Hsub, const int *__restrict__ done)
+{
+  if(*done) return;
+  const double nrm = sqrt(st->result[0]);
+  if(blockIdx.x == 0 && threadIdx.x == 0) *Hsub = nrm;
+  const float inv = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v[i] = w[i] * inv;
+}
+
+// V_0 = r / ||r|| rounded to FP32 (start of a mixed cycle), beta = ||r||.
+__global__ void k_scale_r32(int64_t n, const double *__restrict__ r, float *__restrict__ v, const RedState *st,
+                            double *beta, const int *__restrict__ done)
+{
+  if(*done) return;
+  const double nrm = sqrt(st->result[0]);
+  if(blockIdx.x == 0 && threadIdx.x == 0) *beta = nrm;
+  const double inv = nrm > 0 ? 1.0 / nrm : 0.0;
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v[i] = (float)(r[i] * inv);
+}
+
 __global__ void k_gmres_init(GmresState *gs, const RedState *st)
 {
   const double beta = sqrt(st->result[0]);
@@ -515,7 +631,7 @@ struct Ws {
 #define Ws_INIT(k) {(RedState *)(k)->red_state_, (GmresState *)(k)->gmres_, (GmresState *)(k)->h_gmres_, (CGState *)(k)->cg_, (CGState *)(k)->h_cg_}
 Krylov::~Krylov()
 {
-  cudaFree(V_); cudaFree(Z_); cudaFree(Z32_); cudaFree(v32_); cudaFree(w32_);
+  cudaFree(V_); cudaFree(Z_); cudaFree(Z32_); cudaFree(V32_); cudaFree(v32_); cudaFree(w32_);
   cudaFree(w_); cudaFree(r_); cudaFree(t_); cudaFree(p_); cudaFree(q_);
   cudaFree(diag_); cudaFree(diag32_); cudaFree(red_); cudaFree(dsum_);
   cudaFreeHost(hred_);
@@ -570,10 +686,19 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
   CK(cudaMalloc(&p_, sizeof(double) * n_));
   CK(cudaMalloc(&q_, sizeof(double) * n_));
   if(opt.method == 1) {
-    CK(cudaMalloc(&V_, sizeof(double) * n_ * (m + 1)));
-    if(opt.mixed) CK(cudaMalloc(&Z32_, sizeof(float) * n_ * m));
-    else CK(cudaMalloc(&Z_, sizeof(double) * n_ * m));
+    if(opt.mixed) {
+      if(m > 64) {
+        set_error("mixed-precision FGMRES supports restart lengths up to 64 (got %d)", m);
+        return FE_INVALID_ARG;
+      }
+      CK(cudaMalloc(&V32_, sizeof(float) * n_ * (m + 1)));
+      CK(cudaMalloc(&Z32_, sizeof(float) * n_ * m));
+    } else {
+      CK(cudaMalloc(&V_, sizeof(double) * n_ * (m + 1)));
+      CK(cudaMalloc(&Z_, sizeof(double) * n_ * m));
+    }
   }
+  gsParts_ = grid_for(n_, RB * 4, 4 * 152);
   CK(cudaMalloc(&v32_, sizeof(float) * n_));
   CK(cudaMalloc(&w32_, sizeof(float) * n_));
   CK(cudaMalloc(&red_state_, sizeof(RedState)));
@@ -786,6 +911,27 @@ double Krylov::norminf(const double *x)
   return hred_[0];
 }
 
+// One FP32 Gram-Schmidt pass (k_gs32) over the first ncols basis vectors.
+void Krylov::gs32(int mode, int ncols, const double *hprev, double *hcur, double *Hcol, const int *done)
+{
+  RedState *st = (RedState *)red_state_;
+  const int g = gsParts_;
+#define FE_GS_LAUNCH(C)                                                                                         \
+  do {                                                                                                          \
+    if(mode == 0)                                                                                               \
+      (k_gs32<C, 0><<<g, RB, 0, s_>>>(n_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done), ::feng::count_launch()); \
+    else if(mode == 1)                                                                                          \
+      (k_gs32<C, 1><<<g, RB, 0, s_>>>(n_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done), ::feng::count_launch()); \
+    else                                                                                                        \
+      (k_gs32<C, 2><<<g, RB, 0, s_>>>(n_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done), ::feng::count_launch()); \
+  } while(0)
+  if(ncols <= 8) FE_GS_LAUNCH(8);
+  else if(ncols <= 16) FE_GS_LAUNCH(16);
+  else if(ncols <= 32) FE_GS_LAUNCH(32);
+  else FE_GS_LAUNCH(64);
+#undef FE_GS_LAUNCH
+}
+
 // FGMRES(m), right preconditioned, FP64 throughout (Saad Alg. 9.6).
 // One FGMRES(m) restart cycle (Saad Alg. 9.6): r = b - A x, V_0 = r/||r||,
 // then up to jmax Arnoldi steps with right preconditioning z_j = M^-1 v_j,
@@ -796,10 +942,11 @@ void Krylov::launch_cycle(bool mixed, const void *vals, const double *b, double 
 {
   Ws w = Ws_INIT(this);
   const int gv = grid_for(n_, 256, 2048);
-  if(mixed)
-    spmv_launch<float, double, double, double, true>(lanes_, n_, A_, (const float *)vals, x, b, w_, nullptr, s_);
-  else
-    spmv_launch<double, double, double, double, true>(lanes_, n_, A_, (const double *)vals, x, b, w_, nullptr, s_);
+  if(mixed) {
+    launch_cycle_mixed((const float *)vals, b, x, jmax, poll);
+    return;
+  }
+  spmv_launch<double, double, double, double, true>(lanes_, n_, A_, (const double *)vals, x, b, w_, nullptr, s_);
   cudaMemsetAsync(&w.gs->done, 0, sizeof(int), s_);
   cudaMemcpyAsync(&w.gs->tol, htol_, sizeof(double), cudaMemcpyHostToDevice, s_);
   (k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done), ::feng::count_launch());
@@ -807,13 +954,7 @@ void Krylov::launch_cycle(bool mixed, const void *vals, const double *b, double 
   (k_scale_from<<<gv, 256, 0, s_>>>(n_, w_, V_, w.st, &w.gs->beta, &w.gs->done), ::feng::count_launch());
   for(int j = 0; j < jmax; ++j) {
     double *vj = V_ + (int64_t)j * n_;
-    if(mixed) {
-      float *zj = Z32_ + (int64_t)j * n_;
-      (k_to_f32<<<gv, 256, 0, s_>>>(n_, vj, v32_, &w.gs->done), ::feng::count_launch());
-      precond32(v32_, zj, &w.gs->done);
-      spmv_launch<float, float, double, float, false>(lanes_, n_, A_, (const float *)vals, zj, nullptr, w_,
-                                                      &w.gs->done, s_);
-    } else {
+    {
       double *zj = Z_ + (int64_t)j * n_;
       precond64(vj, zj, &w.gs->done);
       spmv_launch<double, double, double, double, false>(lanes_, n_, A_, (const double *)vals, zj, nullptr,
@@ -831,8 +972,41 @@ void Krylov::launch_cycle(bool mixed, const void *vals, const double *b, double 
     if(poll && poll_done(&w.gs->done, j)) break;
   }
   (k_backsolve<<<1, 1, 0, s_>>>(w.gs), ::feng::count_launch());
-  if(mixed) (k_xupdate<float><<<gv, 256, 0, s_>>>(n_, Z32_, w.gs, x), ::feng::count_launch());
-  else (k_xupdate<double><<<gv, 256, 0, s_>>>(n_, Z_, w.gs, x), ::feng::count_launch());
+  (k_xupdate<double><<<gv, 256, 0, s_>>>(n_, Z_, w.gs, x), ::feng::count_launch());
+  cudaMemcpyAsync(h_gmres_, w.gs, sizeof(GmresHead), cudaMemcpyDeviceToHost, s_);
+}
+
+// One mixed-precision restart cycle: the residual b - A x with FP64
+// accumulation (iterative refinement), then Arnoldi on an FP32 basis: FP32
+// preconditioner and SpMV, classical Gram-Schmidt twice in FP32 with FP64
+// partial sums (three fused passes over the basis), FP64 Hessenberg and
+// Givens rotations, FP64 solution update.
+void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, int jmax, bool poll)
+{
+  Ws w = Ws_INIT(this);
+  const int gv = grid_for(n_, 256, 2048);
+  spmv_launch<float, double, double, double, true>(lanes_, n_, A_, vals, x, b, w_, nullptr, s_);
+  cudaMemsetAsync(&w.gs->done, 0, sizeof(int), s_);
+  cudaMemcpyAsync(&w.gs->tol, htol_, sizeof(double), cudaMemcpyHostToDevice, s_);
+  (k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done), ::feng::count_launch());
+  (k_gmres_init<<<1, 1, 0, s_>>>(w.gs, w.st), ::feng::count_launch());
+  (k_scale_r32<<<gv, 256, 0, s_>>>(n_, w_, V32_, w.st, &w.gs->beta, &w.gs->done), ::feng::count_launch());
+  for(int j = 0; j < jmax; ++j) {
+    const float *vj = V32_ + (int64_t)j * n_;
+    float *zj = Z32_ + (int64_t)j * n_;
+    precond32(vj, zj, &w.gs->done);
+    spmv_launch<float, float, float, float, false>(lanes_, n_, A_, vals, zj, nullptr, w32_, &w.gs->done, s_);
+    double *Hcol = w.gs->H + (int64_t)j * (MAXM + 1);
+    gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done);
+    gs32(1, j + 1, w.gs->hcur, w.gs->hcur, Hcol, &w.gs->done);
+    gs32(2, j + 1, w.gs->hcur, nullptr, nullptr, &w.gs->done);
+    (k_scale32<<<gv, 256, 0, s_>>>(n_, w32_, V32_ + (int64_t)(j + 1) * n_, w.st, Hcol + j + 1, &w.gs->done),
+     ::feng::count_launch());
+    (k_givens<<<1, 1, 0, s_>>>(w.gs, j), ::feng::count_launch());
+    if(poll && poll_done(&w.gs->done, j)) break;
+  }
+  (k_backsolve<<<1, 1, 0, s_>>>(w.gs), ::feng::count_launch());
+  (k_xupdate<float><<<gv, 256, 0, s_>>>(n_, Z32_, w.gs, x), ::feng::count_launch());
   cudaMemcpyAsync(h_gmres_, w.gs, sizeof(GmresHead), cudaMemcpyDeviceToHost, s_);
 }
 

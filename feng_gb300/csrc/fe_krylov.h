@@ -119,6 +119,9 @@ class Krylov {
   double *V_ = nullptr;   // (m+1) x n  Krylov basis, FP64
   double *Z_ = nullptr;   // m x n      preconditioned directions (FP64 path)
   float *Z32_ = nullptr;  // m x n      preconditioned directions (mixed path)
+  float *V32_ = nullptr;  // (m+1) x n  Krylov basis of the mixed path, FP32
+  int gsParts_ = 0;       // blocks of the FP32 Gram-Schmidt passes
+  void gs32(int mode, int ncols, const double *hprev, double *hcur, double *Hcol, const int *done);
   float *v32_ = nullptr, *w32_ = nullptr;
   double *w_ = nullptr, *r_ = nullptr, *t_ = nullptr, *p_ = nullptr, *q_ = nullptr;
   double *diag_ = nullptr;    // inverse diagonal (Jacobi)
@@ -140,6 +143,7 @@ class Krylov {
   double *htol_ = nullptr;         // pinned absolute tolerance read by the cycle
   bool poll_done(const int *dflag, int j);
   void launch_cycle(bool mixed, const void *vals, const double *b, double *x, int jmax, bool poll);
+  void launch_cycle_mixed(const float *vals, const double *b, double *x, int jmax, bool poll);
   int run_cycle(bool mixed, const void *vals, const double *b, double *x, int jmax);
   struct GraphKey {
     bool mixed;

@@ -42,6 +42,7 @@ struct Krylov::MG {
   double *pScale64 = nullptr;
   float *pScale32 = nullptr;
   void *bx = nullptr, *by = nullptr, *zx = nullptr, *zy = nullptr;
+  void *bxy = nullptr, *zxy = nullptr;  // both components interleaved (paired V-cycle)
   double *dsum = nullptr;
   double lapDiagSum = 0, s = 1, sigma = 1, divu = 1;
   std::vector<double> pMass;
@@ -58,7 +59,7 @@ struct Krylov::MG {
     cudaFree(diagX); cudaFree(pScale64); cudaFree(pScale32); cudaFree(bx); cudaFree(by); cudaFree(zx);
     cudaFree(zy); cudaFree(dsum); cudaFree(ir); cudaFree(iz); cudaFree(ip); cudaFree(iq);
     cudaFree(part); cudaFree(scal); cudaFree(dnIa); cudaFree(dnPos); cudaFree(dnCol); cudaFree(slotOf);
-    cudaFree(pMassDev); cudaFree(tP); cudaFree(consts);
+    cudaFree(pMassDev); cudaFree(tP); cudaFree(consts); cudaFree(bxy); cudaFree(zxy);
   }
   template <typename V> void solveK(const V *b, V *x, cudaStream_t st);
 };
@@ -315,6 +316,37 @@ __global__ void k_vel_rhs(int64_t nN, const int32_t *__restrict__ dofX, const in
   }
 }
 
+// The same right-hand side, both components interleaved: bxy[2 k + c].
+template <typename V>
+__global__ void k_vel_rhs_pair(int64_t nN, const int32_t *__restrict__ dofX, const int32_t *__restrict__ dofY,
+                               const int32_t *__restrict__ upIa, const int32_t *__restrict__ upPos,
+                               const int32_t *__restrict__ upCol, const V *__restrict__ a,
+                               const V *__restrict__ r, const V *__restrict__ z, V *__restrict__ bxy,
+                               const int *__restrict__ skip)
+{
+  if(skip && *skip) return;
+  for(int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 2 * nN; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = q >> 1;
+    const int c = (int)(q & 1);
+    V t = r[c == 0 ? dofX[k] : dofY[k]];
+    for(int32_t e = upIa[q]; e < upIa[q + 1]; ++e) t -= a[upPos[e]] * z[upCol[e]];
+    bxy[q] = t;
+  }
+}
+
+template <typename V>
+__global__ void k_vel_out_pair(int64_t nN, const int32_t *__restrict__ dofX, const int32_t *__restrict__ dofY,
+                               const V *__restrict__ zxy, const double *__restrict__ consts, V *__restrict__ z,
+                               const int *__restrict__ skip)
+{
+  if(skip && *skip) return;
+  const V f = (V)consts[0];
+  for(int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 2 * nN; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = q >> 1;
+    z[(q & 1) == 0 ? dofX[k] : dofY[k]] = zxy[q] * f;
+  }
+}
+
 template <typename V>
 __global__ void k_vel_out(int64_t nN, const int32_t *__restrict__ dofX, const int32_t *__restrict__ dofY,
                           const V *__restrict__ zx, const V *__restrict__ zy, const double *__restrict__ consts,
@@ -368,6 +400,7 @@ int Krylov::setup_mg(const PrecondInfo &pi)
   const size_t vs = M.fp32 ? sizeof(float) : sizeof(double);
   for(void **v : {&M.bx, &M.by, &M.zx, &M.zy, &M.ir, &M.iz, &M.ip, &M.iq})
     CKM(cudaMalloc(v, vs * M.nNodes));
+  for(void **v : {&M.bxy, &M.zxy}) CKM(cudaMalloc(v, 2 * vs * M.nNodes));
   CKM(cudaMalloc(&M.dsum, sizeof(double)));
   CKM(cudaMalloc(&M.part, sizeof(double) * NPART));
   CKM(cudaMalloc(&M.scal, sizeof(double) * 4));
@@ -516,6 +549,17 @@ void Krylov::apply_mg(const V *vals, const V *r, V *z, const int *skip)
     else
       (k_pressure<V, float><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.pRows, M.pScale32, M.pMassDev, cr, M.consts,
                                                        r, z, skip), ::feng::count_launch());
+    if(M.inner <= 0) {
+      // Both velocity components through one paired V-cycle (one pass over
+      // each level operator for the two right-hand sides).
+      (k_vel_rhs_pair<V><<<grid(2 * M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, M.upIa, M.upPos, M.upCol,
+                                                               vals, r, z, (V *)M.bxy, skip), ::feng::count_launch());
+      if constexpr(sizeof(V) == 8) M.amg.vcycle2_64((const double *)M.bxy, (double *)M.zxy);
+      else M.amg.vcycle2_32((const float *)M.bxy, (float *)M.zxy);
+      (k_vel_out_pair<V><<<grid(2 * M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, (const V *)M.zxy, M.consts,
+                                                              z, skip), ::feng::count_launch());
+      return;
+    }
     (k_vel_rhs<V><<<grid(M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, M.upIa, M.upPos, M.upCol,
                                                   vals, r, z, (V *)M.bx, (V *)M.by, skip), ::feng::count_launch());
   }
