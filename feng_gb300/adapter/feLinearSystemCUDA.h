@@ -69,7 +69,7 @@ public:
     o.precision = 0;
     o.quad_degree = quadratureDegree;
     o.mg_inner = 0;
-    o.mg_smooth = 2;
+    o.mg_smooth = 1;
     return o;
   }
 

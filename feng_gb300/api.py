@@ -281,7 +281,7 @@ class LinearSolverOptions:
     pc_block_rows: int = 256
     precision: str = "fp64"       # "fp64" | "mixed"
     mg_inner: int = 0             # multigrid: inner AMG-CG steps per velocity component
-    mg_smooth: int = 2            # multigrid: Chebyshev smoother degree
+    mg_smooth: int = 1            # multigrid: Chebyshev smoother degree
 
     def to_c(self, quad_degree: int) -> _lib.Options:
         pc = {"none": 0, "bjacobi-ilu0": 1, "ilu0": 1, "jacobi": 2, "amg": 3}[self.precond]

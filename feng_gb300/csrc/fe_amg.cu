@@ -71,7 +71,8 @@ __device__ __forceinline__ void row_dot(int32_t beg, int32_t end, int sub, const
     for(int o = LANES / 2; o > 0; o >>= 1) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], o, LANES);
 }
 
-// y = A x (MODE 0), y = b - A x (MODE 1), y += A x (MODE 2)
+// y = A x (MODE 0), y = b - A x (MODE 1), y += A x (MODE 2),
+// y = A (b .* x) with b a per-row scale of x (MODE 3)
 template <typename V, int LANES, int MODE, int NV>
 __global__ void __launch_bounds__(256) k_csr(int64_t n, const int32_t *__restrict__ ia,
                                              const int32_t *__restrict__ ja, const V *__restrict__ a,
@@ -84,12 +85,28 @@ __global__ void __launch_bounds__(256) k_csr(int64_t n, const int32_t *__restric
   const bool live = row < n;
   const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
   V acc[NV];
-  row_dot<V, LANES, NV>(beg, end, sub, ja, a, x, acc);
+  if(MODE == 3) {
+#pragma unroll
+    for(int c = 0; c < NV; ++c) acc[c] = 0;
+    for(int32_t k = beg + sub; k < end; k += LANES) {
+      const int32_t j = ja[k];
+      const V ak = a[k] * b[j];
+      const Vals<V, NV> xv = ldv<V, NV>(x, j);
+#pragma unroll
+      for(int c = 0; c < NV; ++c) acc[c] += ak * xv.v[c];
+    }
+#pragma unroll
+    for(int c = 0; c < NV; ++c)
+#pragma unroll
+      for(int o = LANES / 2; o > 0; o >>= 1) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], o, LANES);
+  } else {
+    row_dot<V, LANES, NV>(beg, end, sub, ja, a, x, acc);
+  }
   if(live && sub == 0) {
 #pragma unroll
     for(int c = 0; c < NV; ++c) {
       const int64_t o = row * NV + c;
-      if(MODE == 0) y[o] = acc[c];
+      if(MODE == 0 || MODE == 3) y[o] = acc[c];
       else if(MODE == 1) y[o] = b[o] - acc[c];
       else y[o] += acc[c];
     }
@@ -238,7 +255,7 @@ AMGDevice::~AMGDevice()
 {
   for(Lev &L : lv_) {
     cudaFree(L.Aia); cudaFree(L.Aja); cudaFree(L.Pia); cudaFree(L.Pja); cudaFree(L.Ria); cudaFree(L.Rja);
-    cudaFree(L.Aa); cudaFree(L.Pa); cudaFree(L.Ra); cudaFree(L.dinv);
+    cudaFree(L.Aa); cudaFree(L.Pa); cudaFree(L.Ra); cudaFree(L.dinv); cudaFree(L.diag);
     cudaFree(L.x); cudaFree(L.b); cudaFree(L.r); cudaFree(L.d0); cudaFree(L.d1);
   }
   cudaFree(coarseInv_);
@@ -264,6 +281,9 @@ int AMGDevice::upload(const AMGHierarchy &H, const AMGParams &p, int fp32, cudaS
     FE_TRY(upload_idx(&L.Aja, h.A.ja));
     FE_TRY(fp32 ? upload_vec<float>(&L.Aa, h.A.a) : upload_vec<double>(&L.Aa, h.A.a));
     FE_TRY(fp32 ? upload_vec<float>(&L.dinv, h.dinv) : upload_vec<double>(&L.dinv, h.dinv));
+    std::vector<double> dg(h.dinv.size());
+    for(size_t i = 0; i < dg.size(); ++i) dg[i] = 1.0 / h.dinv[i];
+    FE_TRY(fp32 ? upload_vec<float>(&L.diag, dg) : upload_vec<double>(&L.diag, dg));
     // room for two interleaved components (vcycle2)
     for(void **v : {&L.x, &L.b, &L.r, &L.d0, &L.d1}) CKA(cudaMalloc(v, 2 * vs * std::max<int64_t>(1, L.n)));
     if(l + 1 < H.levels.size()) {
@@ -325,9 +345,10 @@ void AMGDevice::vcycle_t(int l, const V *b, V *x)
   const V *A = (const V *)L.Aa;
   chebyshev<V, NV>(L.lanesA, L.n, L.Aia, L.Aja, A, (const V *)L.dinv, b, x, (V *)L.r, (V *)L.d0, (V *)L.d1,
                    L.lmax, p_, true, s_, skip_);
-  // residual r = b - A x, restrict into the coarse right-hand side
-  csr<V, 1, NV>(L.lanesA, L.n, L.Aia, L.Aja, A, x, b, (V *)L.r, s_, skip_);
-  csr<V, 0, NV>(L.lanesR, C.n, L.Ria, L.Rja, (const V *)L.Ra, (const V *)L.r, nullptr, (V *)C.b, s_, skip_);
+  // Chebyshev keeps r = D^-1 (b - A x): restrict the residual D r directly
+  // (no extra pass over A).
+  csr<V, 3, NV>(L.lanesR, C.n, L.Ria, L.Rja, (const V *)L.Ra, (const V *)L.r, (const V *)L.diag, (V *)C.b, s_,
+                skip_);
   vcycle_t<V, NV>(l + 1, (const V *)C.b, (V *)C.x);
   csr<V, 2, NV>(L.lanesP, L.n, L.Pia, L.Pja, (const V *)L.Pa, (const V *)C.x, nullptr, x, s_, skip_);
   chebyshev<V, NV>(L.lanesA, L.n, L.Aia, L.Aja, A, (const V *)L.dinv, b, x, (V *)L.r, (V *)L.d0, (V *)L.d1,

@@ -73,7 +73,7 @@ class AMGDevice {
   struct Lev {
     int64_t n = 0, nc = 0;
     int32_t *Aia = nullptr, *Aja = nullptr, *Pia = nullptr, *Pja = nullptr, *Ria = nullptr, *Rja = nullptr;
-    void *Aa = nullptr, *Pa = nullptr, *Ra = nullptr, *dinv = nullptr;
+    void *Aa = nullptr, *Pa = nullptr, *Ra = nullptr, *dinv = nullptr, *diag = nullptr;
     void *x = nullptr, *b = nullptr, *r = nullptr, *d0 = nullptr, *d1 = nullptr;
     double lmax = 0;
     int lanesA = 4, lanesP = 4, lanesR = 4;

@@ -101,7 +101,7 @@ static SystemOptions to_sys_options(const fe_cuda_options *o)
   so.pcBlockRows = o->pc_block_rows;
   so.precision = o->precision;
   so.mgInner = o->mg_inner;
-  so.mgSmooth = o->mg_smooth > 0 ? o->mg_smooth : 2;
+  so.mgSmooth = o->mg_smooth > 0 ? o->mg_smooth : 1;
   return so;
 }
 

@@ -59,6 +59,7 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int32_t *__restri
 // ---------------------------------------------------------------------------
 struct RedState {
   unsigned int counter;
+  float finv;  // 1 / ||w|| of the last FP32 Gram-Schmidt norm pass
   double result[4];
 };
 
@@ -291,7 +292,7 @@ __global__ void k_backsolve(GmresState *gs)
 }
 
 template <typename VZ>
-__global__ void k_xupdate(int64_t n, const VZ *__restrict__ Z, const GmresState *gs,
+__global__ void k_xupdate(int64_t n, int64_t ld, const VZ *__restrict__ Z, const GmresState *gs,
                           double *__restrict__ x)
 {
   __shared__ double sy[MAXM];
@@ -301,7 +302,7 @@ __global__ void k_xupdate(int64_t n, const VZ *__restrict__ Z, const GmresState 
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
       i += (int64_t)gridDim.x * blockDim.x) {
     double acc = x[i];
-    for(int c = 0; c < k; ++c) acc += sy[c] * (double)Z[(int64_t)c * n + i];
+    for(int c = 0; c < k; ++c) acc += sy[c] * (double)Z[(int64_t)c * ld + i];
     x[i] = acc;
   }
 }
@@ -317,12 +318,24 @@ __global__ void k_xupdate(int64_t n, const VZ *__restrict__ Z, const GmresState 
 // writes hcur / Hcol (MODE 0: Hcol = h, MODE 1: Hcol += h) or ss into
 // st->result[0].  The FP64 pipe of the GB300 is too slow for these loops.
 // ---------------------------------------------------------------------------
+// A second read of a line this thread has just read (served by L1): a
+// separate load, so that the compiler does not keep the first read in
+// registers (which costs occupancy).
+__device__ __forceinline__ float4 ld4_l1(const float4 *p)
+{
+  float4 r;
+  asm volatile("ld.global.ca.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w) : "l"(p));
+  return r;
+}
+
 template <int CMAX, int MODE>
-__global__ void __launch_bounds__(RB) k_gs32(int64_t n, const float *__restrict__ V, int ncols,
+__global__ void __launch_bounds__(RB) k_gs32(int64_t n4, int64_t ld, const float *__restrict__ V, int ncols,
                                              const double *__restrict__ hprev, float *__restrict__ w,
                                              double *partials, RedState *st, double *hcur, double *Hcol,
                                              const int *__restrict__ done)
 {
+  // Rows are taken four at a time (16-byte loads); the basis columns have a
+  // leading dimension ld that is a multiple of 4 and rows n..ld-1 hold zeros.
   if(*done) return;
   constexpr int NACC = MODE == 2 ? 1 : CMAX;
   __shared__ float hs[CMAX];
@@ -335,28 +348,33 @@ __global__ void __launch_bounds__(RB) k_gs32(int64_t n, const float *__restrict_
   float acc[NACC];
 #pragma unroll
   for(int c = 0; c < NACC; ++c) acc[c] = 0.f;
-  for(int64_t i = (int64_t)blockIdx.x * RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) {
-    float wi = w[i];
-    if(MODE == 0) {
-#pragma unroll
-      for(int c = 0; c < CMAX; ++c)
-        if(c < ncols) acc[c] = fmaf(V[(int64_t)c * n + i], wi, acc[c]);
-    } else {
-      float v[CMAX];
+  float4 *w4 = reinterpret_cast<float4 *>(w);
+  for(int64_t g = (int64_t)blockIdx.x * RB + threadIdx.x; g < n4; g += (int64_t)gridDim.x * RB) {
+    float4 wv = w4[g];
+    if(MODE > 0) {
 #pragma unroll
       for(int c = 0; c < CMAX; ++c)
         if(c < ncols) {
-          v[c] = V[(int64_t)c * n + i];
-          wi = fmaf(-hs[c], v[c], wi);
+          const float4 v = reinterpret_cast<const float4 *>(V + (int64_t)c * ld)[g];
+          const float h = hs[c];
+          wv.x = fmaf(-h, v.x, wv.x);
+          wv.y = fmaf(-h, v.y, wv.y);
+          wv.z = fmaf(-h, v.z, wv.z);
+          wv.w = fmaf(-h, v.w, wv.w);
         }
-      w[i] = wi;
-      if(MODE == 1) {
+      w4[g] = wv;
+    }
+    if(MODE < 2) {
+      // (MODE 1 reads the columns again: the same lines, from L1.)
 #pragma unroll
-        for(int c = 0; c < CMAX; ++c)
-          if(c < ncols) acc[c] = fmaf(v[c], wi, acc[c]);
-      } else {
-        acc[0] = fmaf(wi, wi, acc[0]);
-      }
+      for(int c = 0; c < CMAX; ++c)
+        if(c < ncols) {
+          const float4 *pv = reinterpret_cast<const float4 *>(V + (int64_t)c * ld) + g;
+          const float4 v = MODE == 1 ? ld4_l1(pv) : *pv;
+          acc[c] = fmaf(v.x, wv.x, fmaf(v.y, wv.y, fmaf(v.z, wv.z, fmaf(v.w, wv.w, acc[c]))));
+        }
+    } else {
+      acc[0] = fmaf(wv.x, wv.x, fmaf(wv.y, wv.y, fmaf(wv.z, wv.z, fmaf(wv.w, wv.w, acc[0]))));
     }
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -387,7 +405,11 @@ __global__ void __launch_bounds__(RB) k_gs32(int64_t n, const float *__restrict_
     for(int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
     if(lane == 0) {
       if(MODE == 2) {
+        // ||w||: H[j+1][j] (through Hcol) and the FP32 scale of the next basis vector.
+        const double nrm = sqrt(sum);
         st->result[0] = sum;
+        *Hcol = nrm;
+        st->finv = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
       } else {
         hcur[c] = sum;
         Hcol[c] = MODE == 0 ? sum : Hcol[c] + sum;
@@ -398,16 +420,22 @@ __global__ void __launch_bounds__(RB) k_gs32(int64_t n, const float *__restrict_
   if(threadIdx.x == 0) st->counter = 0;
 }
 
-// v = w / sqrt(ss) in FP32 and H[j+1][j] = sqrt(ss); ss in st->result[0].
-__global__ void k_scale32(int64_t n, const float *__restrict__ w, float *__restrict__ v, const RedState *st,
-                          double *Hsub, const int *__restrict__ done)
+// v = w * (1 / ||w||) in FP32, 4 rows per thread; the scale comes from k_gs32<., 2>.
+__global__ void k_scale32(int64_t n4, const float *__restrict__ w, float *__restrict__ v, const RedState *st,
+                          const int *__restrict__ done)
 {
   if(*done) return;
-  const double nrm = sqrt(st->result[0]);
-  if(blockIdx.x == 0 && threadIdx.x == 0) *Hsub = nrm;
-  const float inv = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
-  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    v[i] = w[i] * inv;
+  const float inv = st->finv;
+  const float4 *w4 = reinterpret_cast<const float4 *>(w);
+  float4 *v4 = reinterpret_cast<float4 *>(v);
+  for(int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n4; g += (int64_t)gridDim.x * blockDim.x) {
+    float4 t = w4[g];
+    t.x *= inv;
+    t.y *= inv;
+    t.z *= inv;
+    t.w *= inv;
+    v4[g] = t;
+  }
 }
 
 // V_0 = r / ||r|| rounded to FP32 (start of a mixed cycle), beta = ||r||.
@@ -691,16 +719,21 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
         set_error("mixed-precision FGMRES supports restart lengths up to 64 (got %d)", m);
         return FE_INVALID_ARG;
       }
-      CK(cudaMalloc(&V32_, sizeof(float) * n_ * (m + 1)));
-      CK(cudaMalloc(&Z32_, sizeof(float) * n_ * m));
+      // Leading dimension a multiple of 64 floats; rows n..ld-1 stay zero.
+      ld32_ = (n_ + 63) / 64 * 64;
+      CK(cudaMalloc(&V32_, sizeof(float) * ld32_ * (m + 1)));
+      CK(cudaMalloc(&Z32_, sizeof(float) * ld32_ * m));
+      CK(cudaMemset(V32_, 0, sizeof(float) * ld32_ * (m + 1)));
+      CK(cudaMemset(Z32_, 0, sizeof(float) * ld32_ * m));
     } else {
       CK(cudaMalloc(&V_, sizeof(double) * n_ * (m + 1)));
       CK(cudaMalloc(&Z_, sizeof(double) * n_ * m));
     }
   }
-  gsParts_ = grid_for(n_, RB * 4, 4 * 152);
+  gsParts_ = grid_for((n_ + 3) / 4, RB * 2, 4 * 152);
   CK(cudaMalloc(&v32_, sizeof(float) * n_));
-  CK(cudaMalloc(&w32_, sizeof(float) * n_));
+  CK(cudaMalloc(&w32_, sizeof(float) * ((n_ + 63) / 64 * 64)));
+  CK(cudaMemset(w32_, 0, sizeof(float) * ((n_ + 63) / 64 * 64)));
   CK(cudaMalloc(&red_state_, sizeof(RedState)));
   CK(cudaMemset(red_state_, 0, sizeof(RedState)));
   CK(cudaMalloc(&gmres_, sizeof(GmresState)));
@@ -916,14 +949,15 @@ void Krylov::gs32(int mode, int ncols, const double *hprev, double *hcur, double
 {
   RedState *st = (RedState *)red_state_;
   const int g = gsParts_;
+  const int64_t n4 = ld32_ / 4;
 #define FE_GS_LAUNCH(C)                                                                                         \
   do {                                                                                                          \
     if(mode == 0)                                                                                               \
-      (k_gs32<C, 0><<<g, RB, 0, s_>>>(n_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done), ::feng::count_launch()); \
+      (k_gs32<C, 0><<<g, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done), ::feng::count_launch()); \
     else if(mode == 1)                                                                                          \
-      (k_gs32<C, 1><<<g, RB, 0, s_>>>(n_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done), ::feng::count_launch()); \
+      (k_gs32<C, 1><<<g, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done), ::feng::count_launch()); \
     else                                                                                                        \
-      (k_gs32<C, 2><<<g, RB, 0, s_>>>(n_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done), ::feng::count_launch()); \
+      (k_gs32<C, 2><<<g, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done), ::feng::count_launch()); \
   } while(0)
   if(ncols <= 8) FE_GS_LAUNCH(8);
   else if(ncols <= 16) FE_GS_LAUNCH(16);
@@ -972,7 +1006,7 @@ void Krylov::launch_cycle(bool mixed, const void *vals, const double *b, double 
     if(poll && poll_done(&w.gs->done, j)) break;
   }
   (k_backsolve<<<1, 1, 0, s_>>>(w.gs), ::feng::count_launch());
-  (k_xupdate<double><<<gv, 256, 0, s_>>>(n_, Z_, w.gs, x), ::feng::count_launch());
+  (k_xupdate<double><<<gv, 256, 0, s_>>>(n_, n_, Z_, w.gs, x), ::feng::count_launch());
   cudaMemcpyAsync(h_gmres_, w.gs, sizeof(GmresHead), cudaMemcpyDeviceToHost, s_);
 }
 
@@ -991,22 +1025,23 @@ void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, i
   (k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done), ::feng::count_launch());
   (k_gmres_init<<<1, 1, 0, s_>>>(w.gs, w.st), ::feng::count_launch());
   (k_scale_r32<<<gv, 256, 0, s_>>>(n_, w_, V32_, w.st, &w.gs->beta, &w.gs->done), ::feng::count_launch());
+  const int g4 = grid_for(ld32_ / 4, 256, 4 * 152);
   for(int j = 0; j < jmax; ++j) {
-    const float *vj = V32_ + (int64_t)j * n_;
-    float *zj = Z32_ + (int64_t)j * n_;
+    const float *vj = V32_ + (int64_t)j * ld32_;
+    float *zj = Z32_ + (int64_t)j * ld32_;
     precond32(vj, zj, &w.gs->done);
     spmv_launch<float, float, float, float, false>(lanes_, n_, A_, vals, zj, nullptr, w32_, &w.gs->done, s_);
     double *Hcol = w.gs->H + (int64_t)j * (MAXM + 1);
     gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done);
     gs32(1, j + 1, w.gs->hcur, w.gs->hcur, Hcol, &w.gs->done);
-    gs32(2, j + 1, w.gs->hcur, nullptr, nullptr, &w.gs->done);
-    (k_scale32<<<gv, 256, 0, s_>>>(n_, w32_, V32_ + (int64_t)(j + 1) * n_, w.st, Hcol + j + 1, &w.gs->done),
+    gs32(2, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done);
+    (k_scale32<<<g4, 256, 0, s_>>>(ld32_ / 4, w32_, V32_ + (int64_t)(j + 1) * ld32_, w.st, &w.gs->done),
      ::feng::count_launch());
     (k_givens<<<1, 1, 0, s_>>>(w.gs, j), ::feng::count_launch());
     if(poll && poll_done(&w.gs->done, j)) break;
   }
   (k_backsolve<<<1, 1, 0, s_>>>(w.gs), ::feng::count_launch());
-  (k_xupdate<float><<<gv, 256, 0, s_>>>(n_, Z32_, w.gs, x), ::feng::count_launch());
+  (k_xupdate<float><<<gv, 256, 0, s_>>>(n_, ld32_, Z32_, w.gs, x), ::feng::count_launch());
   cudaMemcpyAsync(h_gmres_, w.gs, sizeof(GmresHead), cudaMemcpyDeviceToHost, s_);
 }
 

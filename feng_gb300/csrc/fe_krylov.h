@@ -121,6 +121,7 @@ class Krylov {
   float *Z32_ = nullptr;  // m x n      preconditioned directions (mixed path)
   float *V32_ = nullptr;  // (m+1) x n  Krylov basis of the mixed path, FP32
   int gsParts_ = 0;       // blocks of the FP32 Gram-Schmidt passes
+  int64_t ld32_ = 0;      // leading dimension of V32_ / Z32_ (multiple of 64)
   void gs32(int mode, int ncols, const double *hprev, double *hcur, double *Hcol, const int *done);
   float *v32_ = nullptr, *w32_ = nullptr;
   double *w_ = nullptr, *r_ = nullptr, *t_ = nullptr, *p_ = nullptr, *q_ = nullptr;

@@ -31,7 +31,7 @@ struct SystemOptions {
   int pcBlockRows = 256;   // target rows per block-Jacobi block (0: a single block)
   int precision = 0;       // 0 FP64 matrix, 1 FP32 matrix + mixed Krylov
   int mgInner = 0;         // multigrid: inner CG steps per component (0: one V-cycle)
-  int mgSmooth = 2;        // multigrid: Chebyshev degree
+  int mgSmooth = 1;        // multigrid: Chebyshev degree
 };
 
 // Everything the backend needs from the set-up, in the original element order.

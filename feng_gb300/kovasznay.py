@@ -41,11 +41,12 @@ def build(n: int, re: float = 40.0, jitter: float = 0.1, seed: int = 1):
     return m, num, forms
 
 
-def make_system(num, forms, precision: str, precond: str = "amg"):
-    """Linear system (FP64 or mixed) with the boundary values set."""
+def make_system(num, forms, precision: str, precond: str = "amg", **solver):
+    """Linear system (FP64 or mixed) with the boundary values set; extra
+    keywords go to LinearSolverOptions (restart, mg_smooth, ...)."""
     from . import api as fe
     opts = fe.LinearSolverOptions(precond=precond, rel_tol=1e-8, max_iter=3000,
-                                  precision="mixed" if precision == "mixed" else "fp64")
+                                  precision="mixed" if precision == "mixed" else "fp64", **solver)
     sys_ = fe.createLinearSystem(fe.CUDA, forms, num, opts)
     sol = fe.feSolution(sys_)
     sol.initializeEssentialBC()
@@ -71,12 +72,15 @@ def main(argv=None):
     ap.add_argument("--solves", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=0)
     ap.add_argument("--max-iter", type=int, default=30, help="Newton iterations at most (feNLSolverOptions.maxIter)")
+    ap.add_argument("--restart", type=int, default=50, help="FGMRES restart length")
+    ap.add_argument("--mg-smooth", type=int, default=1, help="Chebyshev smoother degree of the multigrid")
     args = ap.parse_args(argv)
 
     from . import api as fe
     from ._lib import check
     _, num, forms = build(args.n, args.re)
-    sys_, _ = make_system(num, forms, args.precision, args.precond)
+    sys_, _ = make_system(num, forms, args.precision, args.precond, restart=args.restart,
+                          mg_smooth=args.mg_smooth)
     nl = newton_options(args.precision)
     nl.maxIter = args.max_iter
     lib = sys_.lib
@@ -93,7 +97,8 @@ def main(argv=None):
                          "krylov_iterations": st["krylov_iterations"],
                          "rel_residual": st["residual"] / st["residual0"] if st["residual0"] else 0.0})
     print(json.dumps({"case": f"kovasznay_re{args.re:g}_{args.n}x{args.n}", "precision": args.precision,
-                      "precond": args.precond, "unknowns": sys_.nInc, "nnz": sys_.nnz, "solves": runs}))
+                      "precond": args.precond, "restart": args.restart, "mg_smooth": args.mg_smooth,
+                      "unknowns": sys_.nInc, "nnz": sys_.nnz, "solves": runs}))
 
 
 if __name__ == "__main__":
