@@ -137,6 +137,7 @@ SIGNATURES = {
     "fe_cuda_synchronize": (C.c_int, [P]),
     "fe_cuda_bench_phase": (C.c_int, [P, C.c_int, C.c_int, C.c_int64, C.POINTER(C.c_double)]),
     "fe_cuda_launch_count": (C.c_int, [C.POINTER(C.c_int64)]),
+    "fe_cuda_smoother_bytes": (C.c_int, [P, C.POINTER(C.c_int64)]),
     "fe_cuda_save_solution": (C.c_int, [P]),
     "fe_cuda_restore_solution": (C.c_int, [P]),
     "fe_cuda_event_record": (C.c_int, [P, C.c_int]),

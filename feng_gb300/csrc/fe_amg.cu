@@ -52,23 +52,39 @@ __device__ __forceinline__ Vals<V, NV> ldv(const V *__restrict__ p, int64_t i)
 }
 
 // Row dot products acc[c] = sum_k a[k] x[ja[k]][c] over LANES lanes per row
-// (result valid in lane 0 of the row).
+// (butterfly reduction: the sums are valid in every lane of the row).  The
+// row is walked UNR segments of LANES entries at a time: the column indices
+// and values of all UNR segments are loaded first (streaming: each matrix
+// entry is used once per product), then the gathers of x.
 template <typename V, int LANES, int NV>
 __device__ __forceinline__ void row_dot(int32_t beg, int32_t end, int sub, const int32_t *__restrict__ ja,
                                         const V *__restrict__ a, const V *__restrict__ x, V (&acc)[NV])
 {
+  constexpr int UNR = LANES >= 8 ? 4 : 2;
 #pragma unroll
   for(int c = 0; c < NV; ++c) acc[c] = 0;
-  for(int32_t k = beg + sub; k < end; k += LANES) {
-    const V ak = a[k];
-    const Vals<V, NV> xv = ldv<V, NV>(x, ja[k]);
+  for(int32_t k0 = beg + sub; k0 < end; k0 += LANES * UNR) {
+    int32_t j[UNR];
+    V av[UNR];
 #pragma unroll
-    for(int c = 0; c < NV; ++c) acc[c] += ak * xv.v[c];
+    for(int u = 0; u < UNR; ++u) {
+      const int32_t k = k0 + u * LANES;
+      const bool ok = k < end;
+      j[u] = ok ? __ldcs(ja + k) : -1;
+      av[u] = ok ? __ldcs(a + k) : (V)0;
+    }
+#pragma unroll
+    for(int u = 0; u < UNR; ++u)
+      if(j[u] >= 0) {
+        const Vals<V, NV> xv = ldv<V, NV>(x, j[u]);
+#pragma unroll
+        for(int c = 0; c < NV; ++c) acc[c] += av[u] * xv.v[c];
+      }
   }
 #pragma unroll
   for(int c = 0; c < NV; ++c)
 #pragma unroll
-    for(int o = LANES / 2; o > 0; o >>= 1) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], o, LANES);
+    for(int o = LANES / 2; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o, LANES);
 }
 
 // y = A x (MODE 0), y = b - A x (MODE 1), y += A x (MODE 2),
@@ -179,17 +195,19 @@ __global__ void __launch_bounds__(256) k_cheb_step(int64_t n, const int32_t *__r
   const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
   V acc[NV];
   row_dot<V, LANES, NV>(beg, end, sub, ja, a, d, acc);
-  if(live && sub == 0) {
+  if(live && sub < NV) {
+    // lane c of the row updates component c
     const V dv = dinv[row];
+    V ac = acc[0];
 #pragma unroll
-    for(int c = 0; c < NV; ++c) {
-      const int64_t o = row * NV + c;
-      const V di = d[o];
-      x[o] += di;
-      const V ri = r[o] - dv * acc[c];
-      r[o] = ri;
-      dn[o] = c1 * di + c2 * ri;
-    }
+    for(int c = 1; c < NV; ++c)
+      if(sub == c) ac = acc[c];
+    const int64_t o = row * NV + sub;
+    const V di = d[o];
+    x[o] += di;
+    const V ri = r[o] - dv * ac;
+    r[o] = ri;
+    dn[o] = c1 * di + c2 * ri;
   }
 }
 
@@ -299,6 +317,7 @@ int AMGDevice::upload(const AMGHierarchy &H, const AMGParams &p, int fp32, cudaS
     }
   }
   nCoarse_ = lv_.empty() ? 0 : lv_.back().n;
+  nnz0_ = H.levels.empty() ? 0 : H.levels[0].A.nnz();
   FE_TRY(fp32 ? upload_vec<float>(&coarseInv_, H.coarseInv) : upload_vec<double>(&coarseInv_, H.coarseInv));
   return FE_OK;
 }
@@ -359,6 +378,33 @@ void AMGDevice::vcycle64(const double *b, double *x) { vcycle_t<double, 1>(0, b,
 void AMGDevice::vcycle32(const float *b, float *x) { vcycle_t<float, 1>(0, b, x); }
 void AMGDevice::vcycle2_64(const double *b, double *x) { vcycle_t<double, 2>(0, b, x); }
 void AMGDevice::vcycle2_32(const float *b, float *x) { vcycle_t<float, 2>(0, b, x); }
+
+void AMGDevice::fineStep2()
+{
+  const Lev &L = lv_[0];
+  const int g = grid(L.n * L.lanesA);
+  auto go = [&](auto tag) {
+    using V = decltype(tag);
+    const V *a = (const V *)L.Aa, *dinv = (const V *)L.dinv;
+    V *d = (V *)L.d0, *dn = (V *)L.d1, *r = (V *)L.r, *x = (V *)L.x;
+    const V c1 = (V)0.5, c2 = (V)0.5;
+    if(L.lanesA == 16) (k_cheb_step<V, 16, 2><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, a, dinv, d, dn, r, x, c1, c2, skip_), ::feng::count_launch());
+    else if(L.lanesA == 8) (k_cheb_step<V, 8, 2><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, a, dinv, d, dn, r, x, c1, c2, skip_), ::feng::count_launch());
+    else (k_cheb_step<V, 4, 2><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, a, dinv, d, dn, r, x, c1, c2, skip_), ::feng::count_launch());
+  };
+  if(fp32_) go(float());
+  else go(double());
+}
+
+int64_t AMGDevice::fineStep2Bytes() const
+{
+  if(lv_.empty()) return 0;
+  const Lev &L = lv_[0];
+  const int64_t vs = fp32_ ? 4 : 8;
+  // values + columns, row pointers, dinv, and per component: d read, x
+  // read+write, r read+write, dn write
+  return nnz0_ * (vs + 4) + (L.n + 1) * 4 + L.n * vs + 2 * L.n * vs * 6;
+}
 
 void AMGDevice::spmv64(const double *x, double *y)
 {

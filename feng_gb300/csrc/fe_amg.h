@@ -65,6 +65,12 @@ class AMGDevice {
   // y = A x with the finest operator.
   void spmv64(const double *x, double *y);
   void spmv32(const float *x, float *y);
+  // One Chebyshev step of the finest level on two interleaved components
+  // (the level's own work vectors): the dominant kernel of the V-cycle.
+  void fineStep2();
+  // Algorithmic bytes of fineStep2: the level operator once (values,
+  // columns, row pointers) and every vector entry it reads or writes once.
+  int64_t fineStep2Bytes() const;
   int64_t n() const { return n0_; }
   int levels() const { return (int)lv_.size(); }
   double finestDiagSum() const { return diagSum_; }
@@ -81,7 +87,7 @@ class AMGDevice {
   template <typename V, int NV> void vcycle_t(int l, const V *b, V *x);
   std::vector<Lev> lv_;
   void *coarseInv_ = nullptr;
-  int64_t nCoarse_ = 0, n0_ = 0;
+  int64_t nCoarse_ = 0, n0_ = 0, nnz0_ = 0;
   int fp32_ = 0;
   AMGParams p_;
   double diagSum_ = 0;

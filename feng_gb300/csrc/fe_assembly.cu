@@ -330,6 +330,176 @@ __global__ void __launch_bounds__(EPB * 6) k_residual_th(DeviceMesh dm, FormCoef
 }
 
 // ---------------------------------------------------------------------------
+// Residual, Taylor-Hood, by quadrature with a 7-node rule exact to degree 5
+// (used when the form's own rule is also exact to degree 5, so that both
+// compute the exact integrals of these polynomial integrands and agree to
+// rounding).  The quadrature-node fluxes are computed once per element
+// (threads of the element split the nodes) and projected onto each test
+// function: about a quarter of the FP64 work of the tensor contraction.
+// Sources keep the form's own rule (their integrands are not polynomial).
+//   Be_(a,m) = sum_q [ Fphi_m phi_a + sum_r H_rm dphi_a/dr ]
+//   Fphi_m   = w |J| ( -c_conv (u . grad) u_m - c_mass udot_m )
+//   H_rm     = sum_k G[r][k] w |J| ( -sigma ( p delta_km - mu (d_k u_m + d_m u_k) ) )
+//   Be_pj    = sum_q w |J| ( -c_div div u ) psi_j
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(EPB * 6) k_residual_th_q(DeviceMesh dm, FormCoeffs fc,
+                                                          const RefTensors *__restrict__ gT,
+                                                          const double *__restrict__ u,
+                                                          const double *__restrict__ udot, double t,
+                                                          int64_t nInc, double *__restrict__ rhs,
+                                                          int64_t begin, int64_t end)
+{
+  __shared__ double sU[12][EPB];
+  __shared__ double sUd[12][EPB];
+  __shared__ double sP[3][EPB];
+  __shared__ double sG[5][EPB];
+  __shared__ double sQ[7][7][EPB];
+  __shared__ double sF[2][16][EPB];
+  __shared__ int32_t sA[15][EPB];
+  const int lane = threadIdx.x, a = threadIdx.y;
+  const int64_t p = begin + (int64_t)blockIdx.x * EPB + lane;
+  const bool live = p < end;
+  const int64_t nE = dm.nElm;
+  const bool hasSrc = fc.srcKind != SRC_NONE;
+  if(live) {
+    for(int i = a; i < 15; i += 6) {
+      int32_t d = dm.adr[(int64_t)i * nE + p];
+      sA[i][lane] = d;
+      if(i < 12) {
+        sU[i][lane] = u[d];
+        sUd[i][lane] = fc.hasMass ? udot[d] : 0.;
+      } else {
+        sP[i - 12][lane] = u[d];
+      }
+    }
+    if(a < 5) sG[a][lane] = dm.geo[(int64_t)a * nE + p];
+  }
+  const int nq = gT->nq;
+  if(hasSrc && live) {
+    const double x0 = dm.xy[0 * nE + p], y0 = dm.xy[1 * nE + p], x1 = dm.xy[2 * nE + p],
+                 y1 = dm.xy[3 * nE + p], x2 = dm.xy[4 * nE + p], y2 = dm.xy[5 * nE + p];
+    for(int q = a; q < nq; q += 6) {
+      const double r = gT->qr[q], s = gT->qs[q];
+      const double x = x0 * (1. - r - s) + x1 * r + x2 * s;
+      const double y = y0 * (1. - r - s) + y1 * r + y2 * s;
+      double f[2];
+      source_value(fc.srcKind, fc.srcParam, x, y, f);
+      sF[0][q][lane] = f[0];
+      sF[1][q][lane] = f[1];
+    }
+  }
+  __syncthreads();
+  if(live) {
+    const double G[2][2] = {{sG[0][lane], sG[1][lane]}, {sG[2][lane], sG[3][lane]}};
+    const double J = sG[4][lane];
+    for(int q = a; q < 7; q += 6) {
+      double uq[2] = {0., 0.}, ur[2] = {0., 0.}, us[2] = {0., 0.}, udq[2] = {0., 0.};
+      for(int b = 0; b < 6; ++b) {
+        const double ph = gT->phi5[q][b], dr = gT->dr5[q][b], ds = gT->ds5[q][b];
+        for(int m = 0; m < 2; ++m) {
+          const double v = sU[2 * b + m][lane];
+          uq[m] += ph * v;
+          ur[m] += dr * v;
+          us[m] += ds * v;
+          udq[m] += ph * sUd[2 * b + m][lane];
+        }
+      }
+      double gu[2][2];  // gu[k][m] = d_k u_m
+      for(int k = 0; k < 2; ++k)
+        for(int m = 0; m < 2; ++m) gu[k][m] = G[0][k] * ur[m] + G[1][k] * us[m];
+      const double pq = gT->psi5[q][0] * sP[0][lane] + gT->psi5[q][1] * sP[1][lane] + gT->psi5[q][2] * sP[2][lane];
+      const double wJ = gT->w5[q] * J;
+      for(int m = 0; m < 2; ++m) {
+        double f = 0.;
+        if(fc.hasConv) f -= fc.conv * (uq[0] * gu[0][m] + uq[1] * gu[1][m]);
+        if(fc.hasMass) f -= fc.mass * udq[m];
+        sQ[q][m][lane] = wJ * f;
+      }
+      double Fg[2][2] = {{0., 0.}, {0., 0.}};  // coefficient of d_k phi_a, component m
+      if(fc.hasSigma)
+        for(int k = 0; k < 2; ++k)
+          for(int m = 0; m < 2; ++m)
+            Fg[k][m] = -fc.sigma * wJ * ((k == m ? pq : 0.) - fc.mu * (gu[k][m] + gu[m][k]));
+      for(int r = 0; r < 2; ++r)
+        for(int m = 0; m < 2; ++m) sQ[q][2 + 2 * r + m][lane] = G[r][0] * Fg[0][m] + G[r][1] * Fg[1][m];
+      sQ[q][6][lane] = fc.hasDivu ? -fc.divu * wJ * (gu[0][0] + gu[1][1]) : 0.;
+    }
+  }
+  __syncthreads();
+  if(!live) return;
+  const double J = sG[4][lane];
+  double be[2] = {0., 0.};
+  for(int q = 0; q < 7; ++q) {
+    const double ph = gT->phi5[q][a], dr = gT->dr5[q][a], ds = gT->ds5[q][a];
+    for(int m = 0; m < 2; ++m) be[m] += sQ[q][m][lane] * ph + sQ[q][2 + m][lane] * dr + sQ[q][4 + m][lane] * ds;
+  }
+  if(hasSrc) {
+    // Be_(a,m) -= f . phi jac w   (feVectorSysElm.cpp:112-130), the form's own rule
+    double acc[2] = {0., 0.};
+    for(int q = 0; q < nq; ++q) {
+      const double pw = gT->phi[q][a] * gT->qw[q];
+      acc[0] += sF[0][q][lane] * pw;
+      acc[1] += sF[1][q][lane] * pw;
+    }
+    be[0] -= fc.srcCoeff * acc[0] * J;
+    be[1] -= fc.srcCoeff * acc[1] * J;
+  }
+  for(int m = 0; m < 2; ++m) {
+    const int32_t d = sA[2 * a + m][lane];
+    if(d < nInc) rhs[d] += be[m];
+  }
+  if(fc.hasDivu && a < 3) {
+    double acc = 0.;
+    for(int q = 0; q < 7; ++q) acc += sQ[q][6][lane] * gT->psi5[q][a];
+    const int32_t d = sA[12 + a][lane];
+    if(d < nInc) rhs[d] += acc;
+  }
+}
+
+// Local entry k = a*18 + j of the staged rows (2a+m) of a Taylor-Hood
+// element matrix -> index of the element-to-nonzero map (i = 2a+m; j < 12
+// velocity column j, 12 <= j < 15 pressure column j-12, 15 <= j < 18 the
+// entry of pressure row j-15 in column i).
+__device__ __forceinline__ int th_map_index(int k, int m)
+{
+  const int a = k / 18, j = k % 18, i = 2 * a + m;
+  return j < 15 ? i * 15 + j : (12 + j - 15) * 15 + i;
+}
+
+template <typename V>
+__device__ __forceinline__ void scatter_staged(const int32_t *__restrict__ map, int64_t nE, int64_t p0, int64_t end,
+                                               int hasSigma, int hasDivu, int m, const V (*sAdd)[EPB],
+                                               V *__restrict__ values)
+{
+  const int tid = threadIdx.y * EPB + threadIdx.x;
+  constexpr int NT = EPB * 6, TOTAL = 108 * EPB, BATCH = 6;
+  for(int base = tid; base < TOTAL; base += NT * BATCH) {
+    int32_t pos[BATCH];
+    V add[BATCH];
+#pragma unroll
+    for(int q = 0; q < BATCH; ++q) {
+      const int idx = base + q * NT;
+      pos[q] = -1;
+      add[q] = 0;
+      if(idx < TOTAL) {
+        const int e = idx % EPB, k = idx / EPB, j = k % 18;
+        const bool on = (j < 12) || (j < 15 ? hasSigma : hasDivu);
+        if(on && p0 + e < end) {
+          pos[q] = __ldg(map + (int64_t)th_map_index(k, m) * nE + p0 + e);
+          add[q] = sAdd[k][e];
+        }
+      }
+    }
+    V old[BATCH];
+#pragma unroll
+    for(int q = 0; q < BATCH; ++q) old[q] = pos[q] >= 0 ? values[pos[q]] : (V)0;
+#pragma unroll
+    for(int q = 0; q < BATCH; ++q)
+      if(pos[q] >= 0) values[pos[q]] = old[q] + add[q];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Jacobian, Taylor-Hood P2-P1.
 // ---------------------------------------------------------------------------
 template <typename V>
@@ -342,6 +512,7 @@ __global__ void __launch_bounds__(EPB * 6) k_matrix_th(DeviceMesh dm, FormCoeffs
   __shared__ SharedTensors<V> sT;
   __shared__ V sU[12][EPB];
   __shared__ V sG[5][EPB];
+  __shared__ V sAdd[108][EPB];
   const int lane = threadIdx.x, a = threadIdx.y;
   const int64_t p = begin + (int64_t)blockIdx.x * EPB + lane;
   const bool live = p < end;
@@ -351,9 +522,12 @@ __global__ void __launch_bounds__(EPB * 6) k_matrix_th(DeviceMesh dm, FormCoeffs
     if(fc.hasConv)
       for(int i = a; i < 12; i += 6) sU[i][lane] = (V)u[dm.adr[(int64_t)i * nE + p]];
     if(a < 5) sG[a][lane] = (V)dm.geo[(int64_t)a * nE + p];
+  } else {
+    // Past the end of the color: zero data, entries never scattered.
+    for(int i = a; i < 12; i += 6) sU[i][lane] = 0;
+    if(a < 5) sG[a][lane] = 0;
   }
   __syncthreads();
-  if(!live) return;
   const V G[2][2] = {{sG[0][lane], sG[1][lane]}, {sG[2][lane], sG[3][lane]}};
   const V J = sG[4][lane];
 
@@ -425,22 +599,25 @@ __global__ void __launch_bounds__(EPB * 6) k_matrix_th(DeviceMesh dm, FormCoeffs
   for(int m = 0; m < 2; ++m)
     for(int j = 0; j < 3; ++j) Bp[m][j] = (G[0][m] * sT.D[0][j][a] + G[1][m] * sT.D[1][j][a]) * J;
 
+  // Stage the element's 216 structurally nonzero entries in shared memory
+  // (thread (e, a): rows 2a+m, velocity + pressure columns, and the
+  // pressure-row entries in columns 2a+m), then scatter them block-wide: consecutive
+  // threads take consecutive elements of one entry, so the map reads are
+  // coalesced and every thread keeps several read-modify-writes in flight.
+  // (two passes, one row component m at a time, to bound shared memory)
+#pragma unroll
   for(int m = 0; m < 2; ++m) {
-    const int i = 2 * a + m;
-    for(int j = 0; j < 12; ++j) {
-      const int32_t pos = dm.map[(int64_t)(i * 15 + j) * nE + p];
-      if(pos >= 0) values[pos] += A[m][j];
+    if(m) __syncthreads();
+#pragma unroll
+    for(int j = 0; j < 12; ++j) sAdd[a * 18 + j][lane] = A[m][j];
+#pragma unroll
+    for(int j = 0; j < 3; ++j) {
+      sAdd[a * 18 + 12 + j][lane] = fc.hasSigma ? (V)fc.sigma * Bp[m][j] : (V)0;
+      sAdd[a * 18 + 15 + j][lane] = fc.hasDivu ? (V)fc.divu * Bp[m][j] : (V)0;
     }
-    if(fc.hasSigma)
-      for(int j = 0; j < 3; ++j) {
-        const int32_t pos = dm.map[(int64_t)(i * 15 + 12 + j) * nE + p];
-        if(pos >= 0) values[pos] += (V)fc.sigma * Bp[m][j];
-      }
-    if(fc.hasDivu)
-      for(int j = 0; j < 3; ++j) {
-        const int32_t pos = dm.map[(int64_t)((12 + j) * 15 + i) * nE + p];
-        if(pos >= 0) values[pos] += (V)fc.divu * Bp[m][j];
-      }
+    __syncthreads();
+    scatter_staged<V>(dm.map, nE, begin + (int64_t)blockIdx.x * EPB, end, fc.hasSigma, fc.hasDivu, m, sAdd,
+                      values);
   }
 }
 
@@ -450,12 +627,15 @@ int64_t nblocks(int64_t begin, int64_t end) { return (end - begin + EPB - 1) / E
 
 void launch_assemble_residual(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
                               const double *u, const double *udot, double t, int64_t nInc,
-                              double *rhs, int64_t begin, int64_t end, cudaStream_t s)
+                              double *rhs, int64_t begin, int64_t end, cudaStream_t s, int exact5)
 {
   if(end <= begin) return;
   dim3 block(EPB, 6);
   if(fc.elemType == 1)
     (k_residual_p2<<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, u, t, nInc, rhs, begin, end), ::feng::count_launch());
+  else if(exact5)
+    (k_residual_th_q<<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, u, udot, t, nInc, rhs, begin,
+                                                          end), ::feng::count_launch());
   else
     (k_residual_th<<<nblocks(begin, end), block, 0, s>>>(dm, fc, dT, u, udot, t, nInc, rhs, begin,
                                                         end), ::feng::count_launch());

@@ -630,6 +630,21 @@ int fe_cuda_reset_times(fe_cuda_system *s)
   return FE_OK;
 }
 
+int fe_cuda_smoother_bytes(fe_cuda_system *s, int64_t *bytes)
+{
+  GUARD_BEGIN
+  if(!s || !bytes) { set_error("null argument"); return FE_INVALID_ARG; }
+  // One step also computes the figure; run it on the system stream.
+  const int r = s->sys.krylov().smootherStep(bytes);
+  if(r != FE_OK) return r;
+  if(cudaStreamSynchronize(s->sys.stream()) != cudaSuccess) {
+    set_error("fe_cuda_smoother_bytes: device error");
+    return FE_CUDA_DEVICE_FAIL;
+  }
+  return FE_OK;
+  GUARD_END
+}
+
 int fe_cuda_bench_phase(fe_cuda_system *s, int which, int reps, int64_t flush_bytes, double *avg_ms)
 {
   if(!s || !avg_ms || flush_bytes < 0) { set_error("invalid argument"); return FE_INVALID_ARG; }

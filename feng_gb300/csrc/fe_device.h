@@ -44,6 +44,11 @@ struct RefTensors {
   int nq;
   double qw[16], qr[16], qs[16];  // the rule, for non-polynomial sources
   double phi[16][6];              // P2 functions at the nodes
+  // A 7-node rule exact to degree 5 (every polynomial integrand of the
+  // residual on affine triangles has degree <= 5).  Used when the rule above
+  // is itself exact to degree 5 (exact5), so both give the exact integrals.
+  int exact5;
+  double w5[7], phi5[7][6], dr5[7][6], ds5[7][6], psi5[7][3];
 };
 
 // Constant coefficients of the fused forms (0 = form absent).
@@ -74,9 +79,11 @@ struct DeviceMesh {
 
 // Residual (FP64) of the fused forms on elements [begin,end) of the color
 // order, accumulated into rhs with feNG's sign (rhs = sum of element Be).
+// exact5: the rule integrates degree 5 exactly (RefTensors::exact5), so the
+// Taylor-Hood residual may use the 7-node quadrature kernel.
 void launch_assemble_residual(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
                               const double *u, const double *udot, double t, int64_t nInc,
-                              double *rhs, int64_t begin, int64_t end, cudaStream_t s);
+                              double *rhs, int64_t begin, int64_t end, cudaStream_t s, int exact5);
 // Jacobian of the fused forms, in double or float.
 void launch_assemble_matrix_f64(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
                                 const double *u, double c0, double *values, int64_t begin,

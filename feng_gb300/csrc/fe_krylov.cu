@@ -43,8 +43,24 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int32_t *__restri
   // always run with the full warp.
   const bool live = row < n;
   const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
+  // UNR segments of LANES entries per step: the column indices and values
+  // (streamed, used once) are loaded before the gathers of x.
+  constexpr int UNR = LANES >= 8 ? 4 : 2;
   ACC acc = 0;
-  for(int32_t k = beg + sub; k < end; k += LANES) acc += (ACC)a[k] * (ACC)x[ja[k]];
+  for(int32_t k0 = beg + sub; k0 < end; k0 += LANES * UNR) {
+    int32_t j[UNR];
+    VA av[UNR];
+#pragma unroll
+    for(int u = 0; u < UNR; ++u) {
+      const int32_t k = k0 + u * LANES;
+      const bool ok = k < end;
+      j[u] = ok ? __ldcs(ja + k) : -1;
+      av[u] = ok ? __ldcs(a + k) : (VA)0;
+    }
+#pragma unroll
+    for(int u = 0; u < UNR; ++u)
+      if(j[u] >= 0) acc += (ACC)av[u] * (ACC)x[j[u]];
+  }
 #pragma unroll
   for(int o = LANES / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, LANES);
   if(live && sub == 0) {
@@ -730,7 +746,8 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
       CK(cudaMalloc(&Z_, sizeof(double) * n_ * m));
     }
   }
-  gsParts_ = grid_for((n_ + 3) / 4, RB * 2, 4 * 152);
+  // one group of 4 rows per thread: the whole pass is one wave of loads
+  gsParts_ = grid_for((n_ + 3) / 4, RB, MAXRED);
   CK(cudaMalloc(&v32_, sizeof(float) * n_));
   CK(cudaMalloc(&w32_, sizeof(float) * ((n_ + 63) / 64 * 64)));
   CK(cudaMemset(w32_, 0, sizeof(float) * ((n_ + 63) / 64 * 64)));

@@ -158,6 +158,9 @@ class Krylov {
  public:
   bool useGraphs_ = true;  // replay full restart cycles from CUDA graphs
   int setup_mg(const PrecondInfo &pi);
+  // The multigrid's finest-level smoother step alone (benchmarking); bytes:
+  // its algorithmic bytes, 0 when there is no multigrid.
+  int smootherStep(int64_t *bytes);
   int factor_mg(const double *values64, const float *values32);
   template <typename V> void apply_mg(const V *vals, const V *r, V *z, const int *skip);
 };

@@ -529,6 +529,19 @@ int Krylov::factor_mg(const double *values64, const float *values32)
   return FE_OK;
 }
 
+int Krylov::smootherStep(int64_t *bytes)
+{
+  if(!mg_) {
+    if(bytes) *bytes = 0;
+    set_error("no multigrid preconditioner");
+    return FE_INVALID_ARG;
+  }
+  mg_->amg.setSkip(nullptr);
+  mg_->amg.fineStep2();
+  if(bytes) *bytes = mg_->amg.fineStep2Bytes();
+  return FE_OK;
+}
+
 template <typename V>
 void Krylov::apply_mg(const V *vals, const V *r, V *z, const int *skip)
 {

@@ -95,6 +95,39 @@ void build_ref_tensors(const QuadRule &q, RefTensors &T)
     for(int a = 0; a < 6; ++a)
       for(int b = 0; b < 6; ++b) T.M[a][b] += w * phi[a] * phi[b];
   }
+  // Is the rule exact to degree 5?  int_T r^i s^j = i! j! / (i + j + 2)!
+  // on the reference triangle.
+  auto fact = [](int k) {
+    double f = 1.;
+    for(int i = 2; i <= k; ++i) f *= i;
+    return f;
+  };
+  T.exact5 = 1;
+  for(int i = 0; i <= 5; ++i)
+    for(int j = 0; i + j <= 5; ++j) {
+      double sum = 0.;
+      for(int k = 0; k < q.n(); ++k) sum += q.w[k] * std::pow(q.r[k], i) * std::pow(q.s[k], j);
+      const double exact = fact(i) * fact(j) / fact(i + j + 2);
+      if(std::fabs(sum - exact) > 1e-13 * exact) T.exact5 = 0;
+    }
+  QuadRule q5;
+  if(triangle_rule(5, q5) != FE_OK || q5.n() != 7) {
+    T.exact5 = 0;
+    return;
+  }
+  for(int k = 0; k < 7; ++k) {
+    double phi[6], d[2][6];
+    p2_basis(q5.r[k], q5.s[k], phi, d[0], d[1]);
+    T.w5[k] = q5.w[k];
+    for(int a = 0; a < 6; ++a) {
+      T.phi5[k][a] = phi[a];
+      T.dr5[k][a] = d[0][a];
+      T.ds5[k][a] = d[1][a];
+    }
+    T.psi5[k][0] = 1. - q5.r[k] - q5.s[k];
+    T.psi5[k][1] = q5.r[k];
+    T.psi5[k][2] = q5.s[k];
+  }
 }
 
 SystemCUDA::~SystemCUDA()
@@ -251,6 +284,7 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
 
   RefTensors hT;
   build_ref_tensors(t.quad, hT);
+  exact5_ = hT.exact5;
   CK(cudaMalloc(&dT_, sizeof(RefTensors)));
   CK(cudaMemcpy(dT_, &hT, sizeof(RefTensors), cudaMemcpyHostToDevice));
 
@@ -448,7 +482,7 @@ int SystemCUDA::assembleResiduals()
   begin_phase();
   for(int c = 0; c < dm_.nColors; ++c)
     launch_assemble_residual(dm_, fc_, dT_, u_, udot_, t_, nInc_, rhs_, dm_.colorOff[c],
-                             dm_.colorOff[c + 1], s_);
+                             dm_.colorOff[c + 1], s_, exact5_);
   CK(cudaGetLastError());
   times.residual_ms += end_phase();
   times.residual_calls++;
@@ -573,7 +607,7 @@ int SystemCUDA::computeSolDot()
 
 int SystemCUDA::benchPhase(int which, int reps, size_t flushBytes, double *avgMs)
 {
-  if(which < 0 || which > 3 || reps < 1) {
+  if(which < 0 || which > 4 || reps < 1) {
     set_error("invalid benchmark request");
     return FE_INVALID_ARG;
   }
@@ -595,7 +629,7 @@ int SystemCUDA::benchPhase(int which, int reps, size_t flushBytes, double *avgMs
       case 0:
         for(int c = 0; c < dm_.nColors; ++c)
           launch_assemble_residual(dm_, fc_, dT_, u_, udot_, t_, nInc_, y, dm_.colorOff[c],
-                                   dm_.colorOff[c + 1], s_);
+                                   dm_.colorOff[c + 1], s_, exact5_);
         break;
       case 1:
         for(int c = 0; c < dm_.nColors; ++c) {
@@ -611,6 +645,9 @@ int SystemCUDA::benchPhase(int which, int reps, size_t flushBytes, double *avgMs
         break;
       case 3:
         status = kry_.applyPrecond(x, y);
+        break;
+      case 4:
+        status = kry_.smootherStep(nullptr);
         break;
     }
     CK(cudaEventRecord(ev1_, s_));

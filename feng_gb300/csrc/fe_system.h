@@ -101,7 +101,8 @@ class SystemCUDA {
   // Times `reps` runs of one phase with CUDA events on the system stream, each
   // preceded by an L2 flush (a write of flushBytes): which = 0 residual
   // assembly, 1 matrix assembly, 2 SpMV with the system matrix, 3 one
-  // preconditioner application.  Returns the mean milliseconds per run.
+  // preconditioner application, 4 one finest-level multigrid smoother step
+  // (two components).  Returns the mean milliseconds per run.
   int benchPhase(int which, int reps, size_t flushBytes, double *avgMs);
 
   // Host copies of the set-up tables (original element order).
@@ -130,6 +131,7 @@ class SystemCUDA {
   std::vector<int64_t> adrHost_;      // element table, original element order
   std::vector<double> elemXYHost_;    // vertex coordinates per element
   int elemType_ = 0;
+  int exact5_ = 0;   // the rule integrates degree 5 exactly (quadrature residual kernel)
   DeviceMesh dm_;
   FormCoeffs fc_{};
   RefTensors *dT_ = nullptr;

@@ -248,8 +248,12 @@ int fe_cuda_reset_times(fe_cuda_system *s);
  * events on the system stream, each run preceded by an L2 flush (a write of
  * flush_bytes): which = 0 residual assembly (all colors), 1 matrix assembly
  * (all colors), 2 SpMV with the system matrix, 3 one preconditioner
- * application.  Uses the current solution state. */
+ * application, 4 one finest-level step of the multigrid smoother (both
+ * velocity components).  Uses the current solution state. */
 int fe_cuda_bench_phase(fe_cuda_system *s, int which, int reps, int64_t flush_bytes, double *avg_ms);
+/* Algorithmic bytes of one run of phase 4 (finest multigrid operator read
+ * once, each vector entry read or written once). */
+int fe_cuda_smoother_bytes(fe_cuda_system *s, int64_t *bytes);
 /* Kernel launches of the library since load (graph replays count their
  * kernel nodes). */
 int fe_cuda_launch_count(int64_t *count);
