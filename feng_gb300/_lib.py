@@ -40,7 +40,8 @@ class Options(C.Structure):
     _fields_ = [("krylov", C.c_int32), ("restart", C.c_int32), ("max_iter", C.c_int32),
                 ("rel_tol", C.c_double), ("abs_tol", C.c_double), ("div_tol", C.c_double),
                 ("precond", C.c_int32), ("pc_block_rows", C.c_int32), ("precision", C.c_int32),
-                ("quad_degree", C.c_int32), ("mg_inner", C.c_int32), ("mg_smooth", C.c_int32)]
+                ("quad_degree", C.c_int32), ("mg_inner", C.c_int32), ("mg_smooth", C.c_int32),
+                ("gs_passes", C.c_int32)]
 
 
 class NewtonOptions(C.Structure):

@@ -70,6 +70,7 @@ public:
     o.quad_degree = quadratureDegree;
     o.mg_inner = 0;
     o.mg_smooth = 1;
+    o.gs_passes = 1;
     return o;
   }
 

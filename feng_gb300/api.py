@@ -282,6 +282,7 @@ class LinearSolverOptions:
     precision: str = "fp64"       # "fp64" | "mixed"
     mg_inner: int = 0             # multigrid: inner AMG-CG steps per velocity component
     mg_smooth: int = 1            # multigrid: Chebyshev smoother degree
+    gs_passes: int = 1            # mixed FGMRES: classical Gram-Schmidt passes (1 or 2)
 
     def to_c(self, quad_degree: int) -> _lib.Options:
         pc = {"none": 0, "bjacobi-ilu0": 1, "ilu0": 1, "jacobi": 2, "amg": 3}[self.precond]
@@ -289,7 +290,7 @@ class LinearSolverOptions:
         return _lib.Options(0 if self.krylov == "cg" else 1, self.restart, self.max_iter, self.rel_tol,
                             self.abs_tol, self.div_tol, pc, rows,
                             1 if self.precision == "mixed" else 0, quad_degree, self.mg_inner,
-                            self.mg_smooth)
+                            self.mg_smooth, self.gs_passes)
 
 
 class feLinearSystemCUDA:

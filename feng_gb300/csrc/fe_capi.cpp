@@ -102,6 +102,7 @@ static SystemOptions to_sys_options(const fe_cuda_options *o)
   so.precision = o->precision;
   so.mgInner = o->mg_inner;
   so.mgSmooth = o->mg_smooth > 0 ? o->mg_smooth : 1;
+  so.kry.gsPasses = o->gs_passes == 2 ? 2 : 1;
   return so;
 }
 

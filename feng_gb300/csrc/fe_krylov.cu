@@ -129,9 +129,11 @@ __device__ void finish_reduction(const double (&v)[K], double *partials, RedStat
   __threadfence();
 #pragma unroll
   for(int k = 0; k < K; ++k) {
+    // L2-coherent loads (the partials come from other blocks), independent
+    // so that they overlap.
     double s = 0.;
     for(int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
-      double p = ((volatile double *)partials)[k * MAXRED + i];
+      const double p = __ldcg(partials + k * MAXRED + i);
       s = MAX ? fmax(s, p) : s + p;
     }
     s = MAX ? block_max(s, sh) : block_sum(s, sh);
@@ -416,8 +418,16 @@ __global__ void __launch_bounds__(RB) k_gs32(int64_t n4, int64_t ld, const float
   if(!last) return;
   __threadfence();
   for(int c = warp; c < nr; c += RB / 32) {
-    double sum = 0.;
-    for(int b = lane; b < (int)gridDim.x; b += 32) sum += ((volatile double *)partials)[(int64_t)c * MAXRED + b];
+    // L2-coherent loads (written by other blocks), eight independent chains.
+    const double *pc = partials + (int64_t)c * MAXRED;
+    double s8[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
+    const int nb = (int)gridDim.x;
+    for(int b0 = lane; b0 < nb; b0 += 256) {
+#pragma unroll
+      for(int q = 0; q < 8; ++q)
+        if(b0 + 32 * q < nb) s8[q] += __ldcg(pc + b0 + 32 * q);
+    }
+    double sum = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
     for(int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
     if(lane == 0) {
       if(MODE == 2) {
@@ -430,6 +440,67 @@ __global__ void __launch_bounds__(RB) k_gs32(int64_t n4, int64_t ld, const float
         hcur[c] = sum;
         Hcol[c] = MODE == 0 ? sum : Hcol[c] + sum;
       }
+    }
+  }
+  __syncthreads();
+  if(threadIdx.x == 0) st->counter = 0;
+}
+
+// h_c = V_c . w for c < ncols, column-blocked: a block stages a chunk of w
+// (GS_CH groups of 4 rows) in shared memory and each warp streams whole
+// chunk-long runs of its columns (c = warp, warp + 8, ...), so every warp
+// reads long contiguous stretches of one basis vector.  Per-block partial
+// sums in FP64; the last block sums them in block order.
+constexpr int GS_CH = 1024;  // float4 groups per block (16 KB of w)
+__global__ void __launch_bounds__(RB) k_gs_dots(int64_t n4, int64_t ld, const float *__restrict__ V, int ncols,
+                                                const float *__restrict__ w, double *partials, RedState *st,
+                                                double *hcur, double *Hcol, const int *__restrict__ done)
+{
+  if(*done) return;
+  __shared__ float4 sw[GS_CH];
+  __shared__ bool last;
+  const int64_t g0 = (int64_t)blockIdx.x * GS_CH;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const float4 *w4 = reinterpret_cast<const float4 *>(w);
+  for(int i = threadIdx.x; i < GS_CH; i += RB) sw[i] = g0 + i < n4 ? w4[g0 + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  __syncthreads();
+  const int64_t lim = n4 - g0;  // groups of this chunk that exist
+  for(int c = warp; c < ncols; c += RB / 32) {
+    const float4 *vc = reinterpret_cast<const float4 *>(V + (int64_t)c * ld) + g0;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 8
+    for(int i = lane; i < GS_CH; i += 32) {
+      if(i < lim) {
+        const float4 v = __ldcs(vc + i);
+        const float4 x = sw[i];
+        float &a = acc[(i >> 5) & 3];
+        a = fmaf(v.x, x.x, fmaf(v.y, x.y, fmaf(v.z, x.z, fmaf(v.w, x.w, a))));
+      }
+    }
+    float sum = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+    for(int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if(lane == 0) partials[(int64_t)c * MAXRED + blockIdx.x] = (double)sum;
+  }
+  __threadfence();
+  __syncthreads();
+  if(threadIdx.x == 0) last = atomicAdd(&st->counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if(!last) return;
+  __threadfence();
+  for(int c = warp; c < ncols; c += RB / 32) {
+    const double *pc = partials + (int64_t)c * MAXRED;
+    double s8[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
+    const int nb = (int)gridDim.x;
+    for(int b0 = lane; b0 < nb; b0 += 256) {
+#pragma unroll
+      for(int q = 0; q < 8; ++q)
+        if(b0 + 32 * q < nb) s8[q] += __ldcg(pc + b0 + 32 * q);
+    }
+    double sum = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
+    for(int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if(lane == 0) {
+      hcur[c] = sum;
+      Hcol[c] = sum;
     }
   }
   __syncthreads();
@@ -976,6 +1047,11 @@ void Krylov::gs32(int mode, int ncols, const double *hprev, double *hcur, double
     else                                                                                                        \
       (k_gs32<C, 2><<<g, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done), ::feng::count_launch()); \
   } while(0)
+  if(mode == 0) {
+    const int gb = (int)std::max<int64_t>(1, (n4 + GS_CH - 1) / GS_CH);
+    (k_gs_dots<<<gb, RB, 0, s_>>>(n4, ld32_, V32_, ncols, w32_, red_, st, hcur, Hcol, done), ::feng::count_launch());
+    return;
+  }
   if(ncols <= 8) FE_GS_LAUNCH(8);
   else if(ncols <= 16) FE_GS_LAUNCH(16);
   else if(ncols <= 32) FE_GS_LAUNCH(32);
@@ -1029,9 +1105,10 @@ void Krylov::launch_cycle(bool mixed, const void *vals, const double *b, double 
 
 // One mixed-precision restart cycle: the residual b - A x with FP64
 // accumulation (iterative refinement), then Arnoldi on an FP32 basis: FP32
-// preconditioner and SpMV, classical Gram-Schmidt twice in FP32 with FP64
-// partial sums (three fused passes over the basis), FP64 Hessenberg and
-// Givens rotations, FP64 solution update.
+// preconditioner and SpMV, classical Gram-Schmidt in FP32 with FP64 partial
+// sums (a dot pass, then a fused update + norm pass; gsPasses = 2 adds the
+// fused update + dot pass of the second orthogonalisation), FP64 Hessenberg
+// and Givens rotations, FP64 solution update.
 void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, int jmax, bool poll)
 {
   Ws w = Ws_INIT(this);
@@ -1050,7 +1127,7 @@ void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, i
     spmv_launch<float, float, float, float, false>(lanes_, n_, A_, vals, zj, nullptr, w32_, &w.gs->done, s_);
     double *Hcol = w.gs->H + (int64_t)j * (MAXM + 1);
     gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done);
-    gs32(1, j + 1, w.gs->hcur, w.gs->hcur, Hcol, &w.gs->done);
+    if(opt.gsPasses > 1) gs32(1, j + 1, w.gs->hcur, w.gs->hcur, Hcol, &w.gs->done);
     gs32(2, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done);
     (k_scale32<<<g4, 256, 0, s_>>>(ld32_ / 4, w32_, V32_ + (int64_t)(j + 1) * ld32_, w.st, &w.gs->done),
      ::feng::count_launch());

@@ -7,7 +7,9 @@
 // (feLinearSystemMklPardiso.cpp:893-965).  The algorithms follow Saad,
 // "Iterative Methods for Sparse Linear Systems", 2nd ed.: ILU(0) (Alg. 10.4),
 // preconditioned CG (Alg. 9.1), flexible GMRES (Alg. 9.6) with classical
-// Gram-Schmidt applied twice for the Arnoldi step.
+// Gram-Schmidt applied twice for the Arnoldi step (FP64 path; the mixed
+// path's FP32 Arnoldi uses one pass by default, its FP64 restart residual
+// corrects any loss of orthogonality).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -69,6 +71,7 @@ struct KrylovOptions {
   int mixed = 0;           // 1: FP32 matrix/preconditioner/SpMV inside FP64 refinement
   int refineMax = 20;      // outer refinement steps in mixed mode
   double innerRtol = 1e-4; // inner FP32 solve tolerance in mixed mode
+  int gsPasses = 1;        // classical Gram-Schmidt passes of the mixed FGMRES (1 or 2)
 };
 
 struct KrylovStats {

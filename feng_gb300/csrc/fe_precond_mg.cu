@@ -32,6 +32,8 @@ struct Krylov::MG {
   int64_t nNodes = 0, nP = 0;
   int32_t *dofX = nullptr, *dofY = nullptr, *pRows = nullptr;
   int32_t *upIa = nullptr, *upPos = nullptr, *upCol = nullptr;  // G block, rows = velocity slot 2k+c
+  void *gVals = nullptr;  // the G block's values, gathered contiguous at each factor()
+  int64_t nG = 0;
   int32_t *dnIa = nullptr, *dnPos = nullptr, *dnCol = nullptr;  // D block, rows = pressure rows
   int32_t *slotOf = nullptr;                                     // velocity DOF -> slot 2k+c (-1 otherwise)
   double cMc = 0, cSc = 0;  // constant pressure mode: c^T M c and c^T S c (deflation)
@@ -59,7 +61,7 @@ struct Krylov::MG {
     cudaFree(diagX); cudaFree(pScale64); cudaFree(pScale32); cudaFree(bx); cudaFree(by); cudaFree(zx);
     cudaFree(zy); cudaFree(dsum); cudaFree(ir); cudaFree(iz); cudaFree(ip); cudaFree(iq);
     cudaFree(part); cudaFree(scal); cudaFree(dnIa); cudaFree(dnPos); cudaFree(dnCol); cudaFree(slotOf);
-    cudaFree(pMassDev); cudaFree(tP); cudaFree(consts); cudaFree(bxy); cudaFree(zxy);
+    cudaFree(pMassDev); cudaFree(tP); cudaFree(consts); cudaFree(bxy); cudaFree(zxy); cudaFree(gVals);
   }
   template <typename V> void solveK(const V *b, V *x, cudaStream_t st);
 };
@@ -316,6 +318,13 @@ __global__ void k_vel_rhs(int64_t nN, const int32_t *__restrict__ dofX, const in
   }
 }
 
+template <typename V>
+__global__ void k_gather_vals(int64_t n, const int32_t *__restrict__ pos, const V *__restrict__ a, V *__restrict__ out)
+{
+  for(int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = a[pos[e]];
+}
+
 // The same right-hand side, both components interleaved: bxy[2 k + c].
 template <typename V>
 __global__ void k_vel_rhs_pair(int64_t nN, const int32_t *__restrict__ dofX, const int32_t *__restrict__ dofY,
@@ -329,7 +338,7 @@ __global__ void k_vel_rhs_pair(int64_t nN, const int32_t *__restrict__ dofX, con
     const int64_t k = q >> 1;
     const int c = (int)(q & 1);
     V t = r[c == 0 ? dofX[k] : dofY[k]];
-    for(int32_t e = upIa[q]; e < upIa[q + 1]; ++e) t -= a[upPos[e]] * z[upCol[e]];
+    for(int32_t e = upIa[q]; e < upIa[q + 1]; ++e) t -= (upPos ? a[upPos[e]] : a[e]) * z[upCol[e]];
     bxy[q] = t;
   }
 }
@@ -438,6 +447,8 @@ int Krylov::setup_mg(const PrecondInfo &pi)
       }
     FE_TRY(up(&M.upIa, ia2));
     FE_TRY(up(&M.upPos, pos));
+    M.nG = (int64_t)pos.size();
+    CKM(cudaMalloc(&M.gVals, sizeof(double) * std::max<int64_t>(1, M.nG)));
     FE_TRY(up(&M.upCol, col));
     FE_TRY(up(&M.pRows, pi.pRows));
     // D block (pressure rows -> velocity columns) and the slot of each velocity DOF.
@@ -485,6 +496,11 @@ int Krylov::factor_mg(const double *values64, const float *values32)
   // mu ~ -s / (1.5 sigma) and S^-1 ~ (mu / c_div) M_p^-1.
   M.s = sum / M.lapDiagSum;
   if(M.kind == 4) {
+    // Contiguous copy of the G block's values for the apply kernels.
+    if(values64)
+      (k_gather_vals<double><<<grid(M.nG), 256, 0, s_>>>(M.nG, M.upPos, values64, (double *)M.gVals), ::feng::count_launch());
+    else
+      (k_gather_vals<float><<<grid(M.nG), 256, 0, s_>>>(M.nG, M.upPos, values32, (float *)M.gVals), ::feng::count_launch());
     std::vector<double> sc(M.nP);
     std::vector<float> sc32(M.nP);
     for(int64_t k = 0; k < M.nP; ++k) {
@@ -565,8 +581,9 @@ void Krylov::apply_mg(const V *vals, const V *r, V *z, const int *skip)
     if(M.inner <= 0) {
       // Both velocity components through one paired V-cycle (one pass over
       // each level operator for the two right-hand sides).
-      (k_vel_rhs_pair<V><<<grid(2 * M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, M.upIa, M.upPos, M.upCol,
-                                                               vals, r, z, (V *)M.bxy, skip), ::feng::count_launch());
+      (k_vel_rhs_pair<V><<<grid(2 * M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, M.upIa, nullptr, M.upCol,
+                                                               (const V *)M.gVals, r, z, (V *)M.bxy, skip),
+       ::feng::count_launch());
       if constexpr(sizeof(V) == 8) M.amg.vcycle2_64((const double *)M.bxy, (double *)M.zxy);
       else M.amg.vcycle2_32((const float *)M.bxy, (float *)M.zxy);
       (k_vel_out_pair<V><<<grid(2 * M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, (const V *)M.zxy, M.consts,

@@ -74,13 +74,14 @@ def main(argv=None):
     ap.add_argument("--max-iter", type=int, default=30, help="Newton iterations at most (feNLSolverOptions.maxIter)")
     ap.add_argument("--restart", type=int, default=50, help="FGMRES restart length")
     ap.add_argument("--mg-smooth", type=int, default=1, help="Chebyshev smoother degree of the multigrid")
+    ap.add_argument("--gs-passes", type=int, default=1, help="Gram-Schmidt passes of the mixed FGMRES (1 or 2)")
     args = ap.parse_args(argv)
 
     from . import api as fe
     from ._lib import check
     _, num, forms = build(args.n, args.re)
     sys_, _ = make_system(num, forms, args.precision, args.precond, restart=args.restart,
-                          mg_smooth=args.mg_smooth)
+                          mg_smooth=args.mg_smooth, gs_passes=args.gs_passes)
     nl = newton_options(args.precision)
     nl.maxIter = args.max_iter
     lib = sys_.lib
@@ -97,7 +98,7 @@ def main(argv=None):
                          "krylov_iterations": st["krylov_iterations"],
                          "rel_residual": st["residual"] / st["residual0"] if st["residual0"] else 0.0})
     print(json.dumps({"case": f"kovasznay_re{args.re:g}_{args.n}x{args.n}", "precision": args.precision,
-                      "precond": args.precond, "restart": args.restart, "mg_smooth": args.mg_smooth,
+                      "precond": args.precond, "restart": args.restart, "mg_smooth": args.mg_smooth, "gs_passes": args.gs_passes,
                       "unknowns": sys_.nInc, "nnz": sys_.nnz, "solves": runs}))
 
 
