@@ -274,16 +274,33 @@ struct GmresState : GmresHead {
   double hcur[MAXM + 1];
 };
 
+// One warp: the column and the previous rotations are staged in shared
+// memory, the (inherently sequential) rotation chain runs on lane 0 out of
+// registers and shared memory, and the column is written back by the warp.
 __global__ void k_givens(GmresState *gs, int j)
 {
   if(gs->done) return;
+  __shared__ double sh[MAXM + 1], scs[MAXM], ssn[MAXM];
   double *h = gs->H + (int64_t)j * (MAXM + 1);
-  for(int i = 0; i < j; ++i) {
-    const double t = gs->cs[i] * h[i] + gs->sn[i] * h[i + 1];
-    h[i + 1] = -gs->sn[i] * h[i] + gs->cs[i] * h[i + 1];
-    h[i] = t;
+  for(int i = threadIdx.x; i <= j + 1; i += blockDim.x) sh[i] = h[i];
+  for(int i = threadIdx.x; i < j; i += blockDim.x) {
+    scs[i] = gs->cs[i];
+    ssn[i] = gs->sn[i];
   }
-  const double a = h[j], b = h[j + 1];
+  __syncwarp();
+  if(threadIdx.x == 0) {
+    double hi = sh[0];
+    for(int i = 0; i < j; ++i) {
+      const double c = scs[i], s = ssn[i], hn = sh[i + 1];
+      sh[i] = c * hi + s * hn;
+      hi = -s * hi + c * hn;
+    }
+    sh[j] = hi;
+  }
+  __syncwarp();
+  for(int i = threadIdx.x; i < j; i += blockDim.x) h[i] = sh[i];
+  if(threadIdx.x != 0) return;
+  const double a = sh[j], b = sh[j + 1];
   const double r = hypot(a, b);
   double c = 1., s = 0.;
   if(r > 0) { c = a / r; s = b / r; }
@@ -298,15 +315,35 @@ __global__ void k_givens(GmresState *gs, int j)
   if(!(gs->est > gs->tol) || b == 0.0 || !isfinite(gs->est)) gs->done = 1;
 }
 
+// y = R^-1 g with R the upper triangle of H (k x k): one block, R staged in
+// shared memory; row i's dot with the solved tail is a block reduction.
 __global__ void k_backsolve(GmresState *gs)
 {
+  // dynamic: the column-major upper triangle of the restart length m
+  // (m (m + 1) / 2 doubles), sized at launch
+  extern __shared__ double sR[];
+  __shared__ double sy[MAXM], sg[MAXM], red[32];
   const int k = gs->k;
+  auto idx = [](int i, int c) { return c * (c + 1) / 2 + i; };  // i <= c
+  for(int c = threadIdx.x; c < k; c += blockDim.x) sg[c] = gs->g[c];
+  for(int c = 0; c < k; ++c)
+    for(int i = threadIdx.x; i <= c; i += blockDim.x) sR[idx(i, c)] = gs->H[(int64_t)c * (MAXM + 1) + i];
+  __syncthreads();
   for(int i = k - 1; i >= 0; --i) {
-    double s = gs->g[i];
-    for(int c = i + 1; c < k; ++c) s -= gs->H[(int64_t)c * (MAXM + 1) + i] * gs->y[c];
-    const double d = gs->H[(int64_t)i * (MAXM + 1) + i];
-    gs->y[i] = d != 0 ? s / d : 0.;
+    double p = 0.;
+    for(int c = i + 1 + threadIdx.x; c < k; c += blockDim.x) p += sR[idx(i, c)] * sy[c];
+    for(int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+    if((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = p;
+    __syncthreads();
+    if(threadIdx.x == 0) {
+      double s = sg[i];
+      for(int w = 0; w < (int)(blockDim.x >> 5); ++w) s -= red[w];
+      const double d = sR[idx(i, i)];
+      sy[i] = d != 0 ? s / d : 0.;
+    }
+    __syncthreads();
   }
+  for(int c = threadIdx.x; c < k; c += blockDim.x) gs->y[c] = sy[c];
 }
 
 template <typename VZ>
@@ -347,7 +384,7 @@ __device__ __forceinline__ float4 ld4_l1(const float4 *p)
 }
 
 template <int CMAX, int MODE>
-__global__ void __launch_bounds__(RB) k_gs32(int64_t n4, int64_t ld, const float *__restrict__ V, int ncols,
+__global__ void __launch_bounds__(RB, 3) k_gs32(int64_t n4, int64_t ld, const float *__restrict__ V, int ncols,
                                              const double *__restrict__ hprev, float *__restrict__ w,
                                              double *partials, RedState *st, double *hcur, double *Hcol,
                                              const int *__restrict__ done)
@@ -451,7 +488,7 @@ __global__ void __launch_bounds__(RB) k_gs32(int64_t n4, int64_t ld, const float
 // chunk-long runs of its columns (c = warp, warp + 8, ...), so every warp
 // reads long contiguous stretches of one basis vector.  Per-block partial
 // sums in FP64; the last block sums them in block order.
-constexpr int GS_CH = 1024;  // float4 groups per block (16 KB of w)
+constexpr int GS_CH = 256;   // float4 groups per block (4 KB of w): ~4 blocks per SM
 __global__ void __launch_bounds__(RB) k_gs_dots(int64_t n4, int64_t ld, const float *__restrict__ V, int ncols,
                                                 const float *__restrict__ w, double *partials, RedState *st,
                                                 double *hcur, double *Hcol, const int *__restrict__ done)
@@ -764,6 +801,8 @@ static int grid_for(int64_t n, int threads, int maxBlocks)
   return (int)std::max<int64_t>(1, std::min<int64_t>(b, maxBlocks));
 }
 
+static size_t backsolveSmem(int m) { return sizeof(double) * (size_t)m * (m + 1) / 2; }
+
 // Stops launching the iterations of a restart cycle once the device has set
 // its done flag (read every 4 iterations; skipped kernels would no-op anyway).
 bool Krylov::poll_done(const int *dflag, int j)
@@ -788,6 +827,7 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
     set_error("restart must be in [1, %d]", MAXM);
     return FE_INVALID_ARG;
   }
+  CK(cudaFuncSetAttribute(k_backsolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)backsolveSmem(MAXM)));
   const double avg = n_ > 0 ? (double)A.nnz / n_ : 0;
   lanes_ = avg > 24 ? 8 : 4;
   nParts_ = grid_for(n_, RB, MAXRED);
@@ -1095,10 +1135,10 @@ void Krylov::launch_cycle(bool mixed, const void *vals, const double *b, double 
     }
     (k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done), ::feng::count_launch());
     (k_scale_from<<<gv, 256, 0, s_>>>(n_, w_, V_ + (int64_t)(j + 1) * n_, w.st, Hcol + j + 1, &w.gs->done), ::feng::count_launch());
-    (k_givens<<<1, 1, 0, s_>>>(w.gs, j), ::feng::count_launch());
+    (k_givens<<<1, 32, 0, s_>>>(w.gs, j), ::feng::count_launch());
     if(poll && poll_done(&w.gs->done, j)) break;
   }
-  (k_backsolve<<<1, 1, 0, s_>>>(w.gs), ::feng::count_launch());
+  (k_backsolve<<<1, 128, backsolveSmem(opt.restart), s_>>>(w.gs), ::feng::count_launch());
   (k_xupdate<double><<<gv, 256, 0, s_>>>(n_, n_, Z_, w.gs, x), ::feng::count_launch());
   cudaMemcpyAsync(h_gmres_, w.gs, sizeof(GmresHead), cudaMemcpyDeviceToHost, s_);
 }
@@ -1131,10 +1171,10 @@ void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, i
     gs32(2, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done);
     (k_scale32<<<g4, 256, 0, s_>>>(ld32_ / 4, w32_, V32_ + (int64_t)(j + 1) * ld32_, w.st, &w.gs->done),
      ::feng::count_launch());
-    (k_givens<<<1, 1, 0, s_>>>(w.gs, j), ::feng::count_launch());
+    (k_givens<<<1, 32, 0, s_>>>(w.gs, j), ::feng::count_launch());
     if(poll && poll_done(&w.gs->done, j)) break;
   }
-  (k_backsolve<<<1, 1, 0, s_>>>(w.gs), ::feng::count_launch());
+  (k_backsolve<<<1, 128, backsolveSmem(opt.restart), s_>>>(w.gs), ::feng::count_launch());
   (k_xupdate<float><<<gv, 256, 0, s_>>>(n_, ld32_, Z32_, w.gs, x), ::feng::count_launch());
   cudaMemcpyAsync(h_gmres_, w.gs, sizeof(GmresHead), cudaMemcpyDeviceToHost, s_);
 }
