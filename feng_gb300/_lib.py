@@ -145,6 +145,10 @@ SIGNATURES = {
     "fe_cuda_event_elapsed": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_double)]),
     "fe_cuda_set_device": (C.c_int, [C.c_int]),
     "fe_cuda_max_norm_noalloc": (C.c_int, [P, C.c_int64, P, C.POINTER(C.c_double)]),
+    "fe_cuda_set_constrained_rows": (C.c_int, [P, P, C.c_int64]),
+    "fe_cuda_constrain_essential_components": (C.c_int, [P]),
+    "fe_cuda_set_periodic_pairs": (C.c_int, [P, P, P, C.c_int64]),
+    "fe_cuda_apply_periodicity": (C.c_int, [P]),
     "fe_cuda_transient_create": (C.c_int, [P, C.POINTER(TransientOptions), C.POINTER(NewtonOptions),
                                            C.POINTER(P)]),
     "fe_cuda_transient_steps": (C.c_int, [P, C.c_int, P]),

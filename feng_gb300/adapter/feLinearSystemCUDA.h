@@ -39,6 +39,7 @@ class feLinearSystemCUDA : public feLinearSystem
 
   fe_cuda_system *_sys = nullptr;
   feInt _nInc = 0, _nDofs = 0, _nnz = 0;
+  bool _constrainInit = false, _periodicInit = false;
   int _nIterLast = 0;
 
   static void check(int status, const char *what)
@@ -159,8 +160,46 @@ public:
   }
 
   // Partially essential vector spaces and periodicity are not offloaded.
-  void constrainEssentialComponents(const feSolution *) override {}
-  void applyPeriodicity() override {}
+  // Rows of the essential components of vector spaces, gathered once as
+  // feLinearSystemMklPardiso::constrainEssentialComponents does
+  // (src/feLinearSystemMklPardiso.cpp:994-1050), then constrained on the device.
+  void constrainEssentialComponents(const feSolution *sol) override
+  {
+    if(!_constrainInit) {
+      _constrainInit = true;
+      std::vector<int64_t> rows;
+      std::vector<feInt> adr;
+      for(const auto &space : sol->_spaces) {
+        const int nc = space->getNumComponents(), nf = space->getNumFunctions(), ne = space->getNumElements();
+        if(nc <= 1) continue;
+        adr.resize(nf);
+        for(int i = 0; i < nc; ++i) {
+          if(!space->isEssentialComponent(i)) continue;
+          for(int e = 0; e < ne; ++e) {
+            space->initializeAddressingVector(e, adr);
+            for(int j = 0; j < nf; ++j)
+              if(j % nc == i && adr[j] < _nInc) rows.push_back((int64_t)adr[j]);
+          }
+        }
+      }
+      check(fe_cuda_set_constrained_rows(_sys, rows.data(), (int64_t)rows.size()), "fe_cuda_set_constrained_rows");
+    }
+    check(fe_cuda_constrain_essential_components(_sys), "fe_cuda_constrain_essential_components");
+  }
+  // Periodic slave rows (feLinearSystemMklPardiso::applyPeriodicity, :1119-1149).
+  void applyPeriodicity() override
+  {
+    if(!_periodicInit) {
+      _periodicInit = true;
+      std::vector<int64_t> m, sl;
+      for(const auto &pr : _numbering->PeriodicDOF()) {
+        m.push_back(pr.first);
+        sl.push_back(pr.second);
+      }
+      check(fe_cuda_set_periodic_pairs(_sys, m.data(), sl.data(), (int64_t)m.size()), "fe_cuda_set_periodic_pairs");
+    }
+    check(fe_cuda_apply_periodicity(_sys), "fe_cuda_apply_periodicity");
+  }
   void permute() override {}
 
   bool solve(double *normDx, double *normResidual, double *normAxb, int *nIter) override

@@ -325,6 +325,25 @@ class feLinearSystemCUDA:
         self.nInc, self.nDofs, self.nnz, self.nElm = (v.value for v in n)
         self.nColors = nc.value
 
+    # feLinearSystem::constrainEssentialComponents / applyPeriodicity
+    # (src/feLinearSystemMklPardiso.cpp:994-1149)
+    def setConstrainedRows(self, rows):
+        rows = np.ascontiguousarray(rows, np.int64)
+        check(self.lib.fe_cuda_set_constrained_rows(self._h, ptr(rows), len(rows)))
+
+    def constrainEssentialComponents(self):
+        check(self.lib.fe_cuda_constrain_essential_components(self._h))
+
+    def setPeriodicPairs(self, master, slave):
+        master = np.ascontiguousarray(master, np.int64)
+        slave = np.ascontiguousarray(slave, np.int64)
+        if master.shape != slave.shape:
+            raise ValueError("master and slave lists differ in length")
+        check(self.lib.fe_cuda_set_periodic_pairs(self._h, ptr(master), ptr(slave), len(master)))
+
+    def applyPeriodicity(self):
+        check(self.lib.fe_cuda_apply_periodicity(self._h))
+
     def __del__(self):
         h, self._h = getattr(self, "_h", None), None
         if h:

@@ -819,3 +819,38 @@ extern "C" int fe_cuda_transient_steps(fe_transient *t, int nsteps, fe_step_stat
 }
 
 extern "C" void fe_cuda_transient_destroy(fe_transient *t) { delete t; }
+
+// ---- partially essential components and periodicity (feLinearSystem::
+// constrainEssentialComponents / applyPeriodicity) -----------------------------
+
+extern "C" int fe_cuda_set_constrained_rows(fe_cuda_system *s, const int64_t *rows, int64_t n)
+{
+  GUARD_BEGIN
+  if(!s || (n > 0 && !rows) || n < 0) { set_error("null argument or negative count"); return FE_INVALID_ARG; }
+  return s->sys.setConstrainedRows(rows, n);
+  GUARD_END
+}
+
+extern "C" int fe_cuda_constrain_essential_components(fe_cuda_system *s)
+{
+  GUARD_BEGIN
+  if(!s) { set_error("null argument"); return FE_INVALID_ARG; }
+  return s->sys.constrainEssentialComponents();
+  GUARD_END
+}
+
+extern "C" int fe_cuda_set_periodic_pairs(fe_cuda_system *s, const int64_t *master, const int64_t *slave, int64_t n)
+{
+  GUARD_BEGIN
+  if(!s || (n > 0 && (!master || !slave)) || n < 0) { set_error("null argument or negative count"); return FE_INVALID_ARG; }
+  return s->sys.setPeriodicPairs(master, slave, n);
+  GUARD_END
+}
+
+extern "C" int fe_cuda_apply_periodicity(fe_cuda_system *s)
+{
+  GUARD_BEGIN
+  if(!s) { set_error("null argument"); return FE_INVALID_ARG; }
+  return s->sys.applyPeriodicity();
+  GUARD_END
+}

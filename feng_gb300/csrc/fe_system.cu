@@ -136,6 +136,7 @@ SystemCUDA::~SystemCUDA()
   cudaFree(dT_); cudaFree(csr_.ia); cudaFree(csr_.ja); cudaFree(csr_.diag);
   cudaFree(vals64_); cudaFree(vals32_); cudaFree(rhs_); cudaFree(du_); cudaFree(u_);
   cudaFree(udot_); cudaFree(hist_[1]); cudaFree(hist_[2]); cudaFree(scratch_);
+  cudaFree(conRows_); cudaFree(conColPos_); cudaFree(perMaster_); cudaFree(perSlave_);
   if(ev0_) cudaEventDestroy(ev0_);
   if(ev1_) cudaEventDestroy(ev1_);
   if(s_) cudaStreamDestroy(s_);
@@ -504,10 +505,146 @@ int SystemCUDA::assembleMatrices()
   times.matrix_ms += end_phase();
   times.matrix_calls++;
   matrixValid_ = true;
+  constrained_ = false;
+  periodic_ = false;
+  // The preconditioner is built at the next solve (after the constraints
+  // that feLinearSystem callers apply between assembly and solve).
+  factorPending_ = true;
+  return FE_OK;
+}
+
+int SystemCUDA::factorIfPending()
+{
+  if(!factorPending_) return FE_OK;
   begin_phase();
   int s = kry_.factor(vals64_, vals32_);
   times.factor_ms += end_phase();
+  if(s == FE_OK) factorPending_ = false;
   return s;
+}
+
+namespace {
+// Zero the column occurrences of the constrained rows (colPos), then the rows
+// themselves with 1 on the diagonal, and their right-hand side entries
+// (feLinearSystemMklPardiso::constrainEssentialComponents, :1082-1112).
+template <typename V>
+__global__ void k_constrain_cols(int64_t nPos, const int64_t *__restrict__ colPos, V *__restrict__ values)
+{
+  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nPos; k += (int64_t)gridDim.x * blockDim.x)
+    values[colPos[k]] = (V)0;
+}
+template <typename V>
+__global__ void k_constrain_rows(int64_t nRows, const int64_t *__restrict__ rows, const int32_t *__restrict__ ia,
+                                 const int32_t *__restrict__ ja, V *__restrict__ values, double *__restrict__ rhs,
+                                 int matrix)
+{
+  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nRows; k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = rows[k];
+    if(matrix)
+      for(int32_t e = ia[r]; e < ia[r + 1]; ++e) values[e] = ja[e] == r ? (V)1 : (V)0;
+    rhs[r] = 0.;
+  }
+}
+// Slave rows become u_slave - u_master = 0 (feLinearSystemMklPardiso::applyPeriodicity, :1119-1149).
+template <typename V>
+__global__ void k_periodic_rows(int64_t nPairs, const int64_t *__restrict__ master, const int64_t *__restrict__ slave,
+                                const int32_t *__restrict__ ia, const int32_t *__restrict__ ja,
+                                V *__restrict__ values, double *__restrict__ rhs, int matrix)
+{
+  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nPairs; k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t sl = slave[k], ms = master[k];
+    if(matrix)
+      for(int32_t e = ia[sl]; e < ia[sl + 1]; ++e) values[e] = ja[e] == sl ? (V)1 : (ja[e] == ms ? (V)-1 : (V)0);
+    rhs[sl] = 0.;
+  }
+}
+}  // namespace
+
+int SystemCUDA::setConstrainedRows(const int64_t *rows, int64_t n)
+{
+  std::vector<int64_t> r;
+  for(int64_t i = 0; i < n; ++i)
+    if(rows[i] >= 0 && rows[i] < nInc_) r.push_back(rows[i]);
+  std::sort(r.begin(), r.end());
+  r.erase(std::unique(r.begin(), r.end()), r.end());
+  std::vector<uint8_t> isC(nInc_, 0);
+  for(int64_t v : r) isC[v] = 1;
+  std::vector<int64_t> pos;
+  for(int64_t k = 0; k < (int64_t)pat_.ja.size(); ++k)
+    if(isC[pat_.ja[k]]) pos.push_back(k);
+  cudaFree(conRows_);
+  cudaFree(conColPos_);
+  conRows_ = conColPos_ = nullptr;
+  nCon_ = (int64_t)r.size();
+  nConPos_ = (int64_t)pos.size();
+  if(nCon_) {
+    CK(cudaMalloc(&conRows_, sizeof(int64_t) * nCon_));
+    CK(cudaMemcpy(conRows_, r.data(), sizeof(int64_t) * nCon_, cudaMemcpyHostToDevice));
+  }
+  if(nConPos_) {
+    CK(cudaMalloc(&conColPos_, sizeof(int64_t) * nConPos_));
+    CK(cudaMemcpy(conColPos_, pos.data(), sizeof(int64_t) * nConPos_, cudaMemcpyHostToDevice));
+  }
+  return FE_OK;
+}
+
+int SystemCUDA::constrainEssentialComponents()
+{
+  if(!nCon_) return FE_OK;
+  const int matrix = !constrained_;  // a matrix already constrained since its assembly keeps its rows
+  auto go = [&](auto *vals) {
+    if(matrix && nConPos_)
+      (k_constrain_cols<<<gridFor(nConPos_), 256, 0, s_>>>(nConPos_, conColPos_, vals), ::feng::count_launch());
+    (k_constrain_rows<<<gridFor(nCon_), 256, 0, s_>>>(nCon_, conRows_, csr_.ia, csr_.ja, vals, rhs_, matrix),
+     ::feng::count_launch());
+  };
+  if(vals64_) go(vals64_);
+  else go(vals32_);
+  CK(cudaGetLastError());
+  if(matrix) {
+    constrained_ = true;
+    factorPending_ = true;
+  }
+  return FE_OK;
+}
+
+int SystemCUDA::setPeriodicPairs(const int64_t *master, const int64_t *slave, int64_t n)
+{
+  std::vector<int64_t> m, sl;
+  for(int64_t i = 0; i < n; ++i)
+    if(master[i] >= 0 && master[i] < nInc_ && slave[i] >= 0 && slave[i] < nInc_) {
+      m.push_back(master[i]);
+      sl.push_back(slave[i]);
+    }
+  cudaFree(perMaster_);
+  cudaFree(perSlave_);
+  perMaster_ = perSlave_ = nullptr;
+  nPer_ = (int64_t)m.size();
+  if(nPer_) {
+    CK(cudaMalloc(&perMaster_, sizeof(int64_t) * nPer_));
+    CK(cudaMalloc(&perSlave_, sizeof(int64_t) * nPer_));
+    CK(cudaMemcpy(perMaster_, m.data(), sizeof(int64_t) * nPer_, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(perSlave_, sl.data(), sizeof(int64_t) * nPer_, cudaMemcpyHostToDevice));
+  }
+  return FE_OK;
+}
+
+int SystemCUDA::applyPeriodicity()
+{
+  if(!nPer_) return FE_OK;
+  const int matrix = !periodic_;
+  if(vals64_)
+    (k_periodic_rows<<<gridFor(nPer_), 256, 0, s_>>>(nPer_, perMaster_, perSlave_, csr_.ia, csr_.ja, vals64_, rhs_,
+                                                     matrix), ::feng::count_launch());
+  else
+    (k_periodic_rows<<<gridFor(nPer_), 256, 0, s_>>>(nPer_, perMaster_, perSlave_, csr_.ia, csr_.ja, vals32_, rhs_,
+                                                     matrix), ::feng::count_launch());
+  CK(cudaGetLastError());
+  if(matrix) {
+    periodic_ = true;
+    factorPending_ = true;
+  }
+  return FE_OK;
 }
 
 int SystemCUDA::getRHSMaxNorm(double *norm)
@@ -522,6 +659,7 @@ int SystemCUDA::getRHSMaxNorm(double *norm)
 
 int SystemCUDA::solve(double *normDx, double *normRHS, double *normAxb, int *nIter)
 {
+  FE_TRY(factorIfPending());
   begin_phase();
   KrylovStats st;
   int s = kry_.solve(vals64_, vals32_, rhs_, du_, st);
@@ -618,6 +756,7 @@ int SystemCUDA::benchPhase(int which, int reps, size_t flushBytes, double *avgMs
   CK(cudaMalloc(&y, sizeof(double) * nInc_));
   CK(cudaMemsetAsync(x, 0, sizeof(double) * nInc_, s_));
   CK(cudaMemcpyAsync(x, rhs_, sizeof(double) * nInc_, cudaMemcpyDeviceToDevice, s_));
+  if(which >= 3) FE_TRY(factorIfPending());
   const int savedTiming = timing;
   timing = 0;
   double total = 0.;
@@ -723,6 +862,8 @@ int newton_solve(SystemCUDA &sys, const NewtonOptions &o, NewtonStats &st)
       FE_TRY(sys.assembleMatrices());
       st.matrixAssemblies++;
     }
+    FE_TRY(sys.constrainEssentialComponents());
+    FE_TRY(sys.applyPeriodicity());
     if(o.linearRtolMin > 0 && scale > 0) {
       // Inexact Newton: solve only as far as the nonlinear residual warrants.
       const double ratio = normResidual / scale;

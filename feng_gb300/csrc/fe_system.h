@@ -66,6 +66,15 @@ class SystemCUDA {
   int assembleResiduals();
   int assembleMatrices();
   int getRHSMaxNorm(double *norm);
+  // Partially essential vector components and periodic DOFs
+  // (feLinearSystemMklPardiso.cpp:994-1149): rows/columns set once, applied
+  // after each assembly (idempotent on an already constrained matrix).
+  int setConstrainedRows(const int64_t *rows, int64_t n);
+  int constrainEssentialComponents();
+  int setPeriodicPairs(const int64_t *master, const int64_t *slave, int64_t n);
+  int applyPeriodicity();
+  // Builds the preconditioner of the current matrix if it changed.
+  int factorIfPending();
   int solve(double *normDx, double *normRHS, double *normAxb, int *nIter);
   int correctSolution();
 
@@ -148,6 +157,10 @@ class SystemCUDA {
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
   bool hostTmp_ = false;
   bool matrixValid_ = false;
+  bool factorPending_ = false;
+  bool constrained_ = false, periodic_ = false;
+  int64_t *conRows_ = nullptr, *conColPos_ = nullptr, *perMaster_ = nullptr, *perSlave_ = nullptr;
+  int64_t nCon_ = 0, nConPos_ = 0, nPer_ = 0;
   int begin_phase();
   float end_phase();
   int build_precond_info(const SystemTables &t, const RefTensors &T, HostCSR &lap, PrecondInfo &pi);

@@ -269,6 +269,19 @@ int fe_cuda_event_elapsed(fe_cuda_system *s, int slot0, int slot1, double *ms);
 int fe_cuda_set_device(int device);
 int fe_cuda_synchronize(fe_cuda_system *s);
 
+/* ---- partially essential vector components and periodic DOFs
+ * (feLinearSystemMklPardiso::constrainEssentialComponents, src/feLinearSystemMklPardiso.cpp:994-1117;
+ *  applyPeriodicity, :1119-1149).  The rows (unknowns of the essential components of vector
+ * spaces) and the (master, slave) pairs are set once; each apply then zeroes the constrained
+ * rows and their column occurrences with 1 on the diagonal and 0 in the right-hand side, and
+ * turns each slave row into u_slave - u_master = 0.  Entries >= the unknown count are ignored.
+ * fe_cuda_newton applies both after every assembly.  The preconditioner is rebuilt at the
+ * next solve. */
+int fe_cuda_set_constrained_rows(fe_cuda_system *s, const int64_t *rows, int64_t n);
+int fe_cuda_constrain_essential_components(fe_cuda_system *s);
+int fe_cuda_set_periodic_pairs(fe_cuda_system *s, const int64_t *master, const int64_t *slave, int64_t n);
+int fe_cuda_apply_periodicity(fe_cuda_system *s);
+
 /* ---- BDF2 time integration on device-resident history (BDF2Integrator::makeSteps,
  * src/feTimeIntegration.cpp:449-547, started as startWithBDF1, :383-435; BDF
  * coefficients and history rotation, src/feSolutionContainer.cpp:82-101,291-304).

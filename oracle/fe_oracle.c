@@ -582,3 +582,37 @@ int fo_krylov_solve(int method, int m, int max_iter, double rtol, double atol, i
   free(V); free(Z); free(w); free(H); free(cs); free(sn); free(g); free(y); free(h);
   return st->converged ? 0 : -5;
 }
+
+/* ---- essential components and periodicity: restatement of
+ * feLinearSystemMklPardiso::constrainEssentialComponents
+ * (src/feLinearSystemMklPardiso.cpp:1082-1112: columns of every constrained
+ * row zeroed, then the row zeroed with 1 on its diagonal, rhs 0) and
+ * applyPeriodicity (:1119-1149: slave row = [1 at slave, -1 at master],
+ * rhs 0).  Rows / pairs with an index >= n are ignored, as there. */
+void fo_constrain(int64_t n, const int64_t *ia, const int32_t *ja, double *values, double *rhs,
+                  const int64_t *rows, int64_t nrows)
+{
+  const int64_t nnz = ia[n];
+  unsigned char *isc = calloc((size_t)n, 1);
+  for(int64_t i = 0; i < nrows; ++i)
+    if(rows[i] >= 0 && rows[i] < n) isc[rows[i]] = 1;
+  for(int64_t k = 0; k < nnz; ++k)
+    if(isc[ja[k]]) values[k] = 0.;
+  for(int64_t r = 0; r < n; ++r) {
+    if(!isc[r]) continue;
+    for(int64_t k = ia[r]; k < ia[r + 1]; ++k) values[k] = ja[k] == r ? 1. : 0.;
+    rhs[r] = 0.;
+  }
+  free(isc);
+}
+
+void fo_periodicity(int64_t n, const int64_t *ia, const int32_t *ja, double *values, double *rhs,
+                    const int64_t *master, const int64_t *slave, int64_t npairs)
+{
+  for(int64_t p = 0; p < npairs; ++p) {
+    const int64_t m = master[p], s = slave[p];
+    if(m < 0 || s < 0 || m >= n || s >= n) continue;
+    for(int64_t k = ia[s]; k < ia[s + 1]; ++k) values[k] = ja[k] == s ? 1. : (ja[k] == m ? -1. : 0.);
+    rhs[s] = 0.;
+  }
+}

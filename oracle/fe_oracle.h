@@ -85,6 +85,12 @@ int fo_krylov_solve(int method, int restart, int max_iter, double rtol, double a
                     const int64_t *ia, const int32_t *ja, const double *a, fo_precond *pc,
                     const double *b, double *x, fo_krylov_stats *st, int nthreads);
 
+/* Essential components / periodicity (feLinearSystemMklPardiso.cpp:994-1149). */
+void fo_constrain(int64_t n, const int64_t *ia, const int32_t *ja, double *values, double *rhs,
+                  const int64_t *rows, int64_t nrows);
+void fo_periodicity(int64_t n, const int64_t *ia, const int32_t *ja, double *values, double *rhs,
+                    const int64_t *master, const int64_t *slave, int64_t npairs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,6 +59,8 @@ def load():
         lib.fo_precond_destroy.argtypes = [P]
         lib.fo_krylov_solve.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                         C.c_int64, P, P, P, P, P, P, C.POINTER(KStats), C.c_int]
+        lib.fo_constrain.argtypes = [C.c_int64, P, P, P, P, P, C.c_int64]
+        lib.fo_periodicity.argtypes = [C.c_int64, P, P, P, P, P, P, C.c_int64]
         lib.mo_param_count.restype = C.c_int64
         lib.mo_param_count.argtypes = [C.c_int] * 4
         lib.mo_forward.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int64, P]
@@ -190,3 +192,21 @@ def mlp_adam(params, m, v, grad, lr, step, beta1=0.9, beta2=0.999, eps=1e-8):
     params, m, v, grad = _f64(params).copy(), _f64(m).copy(), _f64(v).copy(), _f64(grad)
     load().mo_adam(_p(params), _p(m), _p(v), _p(grad), params.size, lr, beta1, beta2, eps, step)
     return params, m, v
+
+
+# ---- essential components / periodicity (oracle/fe_oracle.c) -------------------
+
+def constrain(ia, ja, values, rhs, rows=(), master=(), slave=()):
+    """Copies of (values, rhs) after constrainEssentialComponents and
+    applyPeriodicity as the MKL backend does them."""
+    ia = np.ascontiguousarray(ia, np.int64)
+    ja = np.ascontiguousarray(ja, np.int32)
+    v = np.array(values, dtype=np.float64, copy=True)
+    r = np.array(rhs, dtype=np.float64, copy=True)
+    n = len(ia) - 1
+    rows = np.ascontiguousarray(rows, np.int64)
+    load().fo_constrain(n, _p(ia), _p(ja), _p(v), _p(r), _p(rows), len(rows))
+    m = np.ascontiguousarray(master, np.int64)
+    s = np.ascontiguousarray(slave, np.int64)
+    load().fo_periodicity(n, _p(ia), _p(ja), _p(v), _p(r), _p(m), _p(s), len(m))
+    return v, r
