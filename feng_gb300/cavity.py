@@ -40,12 +40,13 @@ def build(n: int, re: float, jitter: float = 0.1, seed: int = 1):
     return m, num, forms
 
 
-def run(n: int, re: float, dt: float, steps: int, guess: str, precision: str = "mixed", **learn):
-    """BDF2 steps from rest; returns (system, per-step statistics)."""
+def run(n: int, re: float, dt: float, steps: int, guess: str, precision: str = "mixed", solver=None, **learn):
+    """BDF2 steps from rest; returns (system, per-step statistics).  solver:
+    extra LinearSolverOptions keywords."""
     from . import api as fe
     _, num, forms = build(n, re)
     opts = fe.LinearSolverOptions(precond="amg", rel_tol=1e-8, max_iter=3000,
-                                  precision="mixed" if precision == "mixed" else "fp64")
+                                  precision="mixed" if precision == "mixed" else "fp64", **(solver or {}))
     sys_ = fe.createLinearSystem(fe.CUDA, forms, num, opts)
     sol = fe.feSolution(sys_)
     sol.initializeEssentialBC()
@@ -67,6 +68,10 @@ def summarize(stats, first: int):
             "guess_residual_ratio": statistics.mean(s["residual_guess"] / s["residual_ref"] for s in late
                                                     if s["residual_ref"] > 0),
             "learned_used": sum(s["guess_used"] == 2 for s in late),
+            "extrap_residual_ratio": statistics.mean(s["residual_extrap"] / s["residual_ref"] for s in late
+                                                     if s["residual_ref"] > 0 and s["residual_extrap"] > 0)
+            if any(s["residual_extrap"] > 0 for s in late) else None,
+            "train_loss": late[-1]["train_loss"],
             "train_ms": statistics.mean(s["train_ms"] for s in late)}
 
 
@@ -81,9 +86,16 @@ def main(argv=None):
     ap.add_argument("--train-from", type=int, default=10)
     ap.add_argument("--use-from", type=int, default=15)
     ap.add_argument("--summary-from", type=int, default=20)
+    ap.add_argument("--gs-passes", type=int, default=1, help="Gram-Schmidt passes of the mixed FGMRES")
+    ap.add_argument("--restart", type=int, default=50)
+    ap.add_argument("--train-iters", type=int, default=8, help="Adam steps per time step")
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--batch", type=int, default=16384)
     args = ap.parse_args(argv)
-    learn = dict(trainFrom=args.train_from, useFrom=args.use_from) if args.guess == "learned" else {}
-    _, stats = run(args.n, args.re, args.dt, args.steps, args.guess, args.precision, **learn)
+    learn = dict(trainFrom=args.train_from, useFrom=args.use_from, trainIters=args.train_iters, lr=args.lr,
+                 batch=args.batch) if args.guess == "learned" else {}
+    _, stats = run(args.n, args.re, args.dt, args.steps, args.guess, args.precision,
+                   solver=dict(gs_passes=args.gs_passes, restart=args.restart), **learn)
     print(json.dumps({"case": f"cavity_re{args.re:g}_{args.n}x{args.n}_dt{args.dt:g}", "guess": args.guess,
                       "precision": args.precision, "summary": summarize(stats, args.summary_from),
                       "steps": stats}))

@@ -75,7 +75,8 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int32_t *__restri
 // ---------------------------------------------------------------------------
 struct RedState {
   unsigned int counter;
-  float finv;  // 1 / ||w|| of the last FP32 Gram-Schmidt norm pass
+  float finv;   // 1 / ||w|| of the last FP32 Gram-Schmidt norm pass
+  int reorth;   // the last Gram-Schmidt pass asks for a second one
   double result[4];
 };
 
@@ -387,11 +388,15 @@ template <int CMAX, int MODE>
 __global__ void __launch_bounds__(RB, 3) k_gs32(int64_t n4, int64_t ld, const float *__restrict__ V, int ncols,
                                              const double *__restrict__ hprev, float *__restrict__ w,
                                              double *partials, RedState *st, double *hcur, double *Hcol,
-                                             const int *__restrict__ done)
+                                             const int *__restrict__ done, int pass)
 {
   // Rows are taken four at a time (16-byte loads); the basis columns have a
   // leading dimension ld that is a multiple of 4 and rows n..ld-1 hold zeros.
-  if(*done) return;
+  // MODE 2, pass 0: decides whether a second pass is needed (the update kept
+  // less than a tenth of ||w||, i.e. severe cancellation: the test of
+  // Daniel, Gragg, Kaufman and Stewart with eta = 0.1; ||w||^2 from the dot
+  // pass); pass 1 runs only when it was asked for.
+  if(*done || (MODE == 2 && pass == 1 && !st->reorth)) return;
   constexpr int NACC = MODE == 2 ? 1 : CMAX;
   __shared__ float hs[CMAX];
   __shared__ float red[RB / 32][NACC];
@@ -473,6 +478,7 @@ __global__ void __launch_bounds__(RB, 3) k_gs32(int64_t n4, int64_t ld, const fl
         st->result[0] = sum;
         *Hcol = nrm;
         st->finv = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
+        if(pass == 0) st->reorth = sum < 1e-2 * st->result[2] ? 1 : 0;
       } else {
         hcur[c] = sum;
         Hcol[c] = MODE == 0 ? sum : Hcol[c] + sum;
@@ -491,40 +497,67 @@ __global__ void __launch_bounds__(RB, 3) k_gs32(int64_t n4, int64_t ld, const fl
 constexpr int GS_CH = 256;   // float4 groups per block (4 KB of w): ~4 blocks per SM
 __global__ void __launch_bounds__(RB) k_gs_dots(int64_t n4, int64_t ld, const float *__restrict__ V, int ncols,
                                                 const float *__restrict__ w, double *partials, RedState *st,
-                                                double *hcur, double *Hcol, const int *__restrict__ done)
+                                                double *hcur, double *Hcol, const int *__restrict__ done,
+                                                int second)
 {
-  if(*done) return;
+  // second = 1: the reorthogonalisation pass, run only when the previous
+  // update asked for it; its coefficients are added to the Hessenberg column.
+  if(*done || (second && !st->reorth)) return;
   __shared__ float4 sw[GS_CH];
+  __shared__ float colAcc[MAXM + 1];  // per-column sums of this block's chunks
+  __shared__ float wred[RB / 32];
   __shared__ bool last;
-  const int64_t g0 = (int64_t)blockIdx.x * GS_CH;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for(int c = threadIdx.x; c <= ncols; c += RB) colAcc[c] = 0.f;
+  float wq = 0.f;  // this thread's share of ||w||^2
   const float4 *w4 = reinterpret_cast<const float4 *>(w);
-  for(int i = threadIdx.x; i < GS_CH; i += RB) sw[i] = g0 + i < n4 ? w4[g0 + i] : make_float4(0.f, 0.f, 0.f, 0.f);
-  __syncthreads();
-  const int64_t lim = n4 - g0;  // groups of this chunk that exist
-  for(int c = warp; c < ncols; c += RB / 32) {
-    const float4 *vc = reinterpret_cast<const float4 *>(V + (int64_t)c * ld) + g0;
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 8
-    for(int i = lane; i < GS_CH; i += 32) {
-      if(i < lim) {
-        const float4 v = __ldcs(vc + i);
-        const float4 x = sw[i];
-        float &a = acc[(i >> 5) & 3];
-        a = fmaf(v.x, x.x, fmaf(v.y, x.y, fmaf(v.z, x.z, fmaf(v.w, x.w, a))));
-      }
+  const int64_t nChunks = (n4 + GS_CH - 1) / GS_CH;
+  // The grid is capped (one partial per block and column): blocks take
+  // chunks blockIdx.x, blockIdx.x + gridDim.x, ...
+  for(int64_t ch = blockIdx.x; ch < nChunks; ch += gridDim.x) {
+    const int64_t g0 = ch * GS_CH;
+    __syncthreads();  // previous chunk's sw no longer read
+    for(int i = threadIdx.x; i < GS_CH; i += RB) {
+      const float4 x = g0 + i < n4 ? w4[g0 + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+      sw[i] = x;
+      wq = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, wq))));
     }
-    float sum = (acc[0] + acc[1]) + (acc[2] + acc[3]);
-    for(int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-    if(lane == 0) partials[(int64_t)c * MAXRED + blockIdx.x] = (double)sum;
+    __syncthreads();
+    const int64_t lim = n4 - g0;  // groups of this chunk that exist
+    for(int c = warp; c < ncols; c += RB / 32) {
+      const float4 *vc = reinterpret_cast<const float4 *>(V + (int64_t)c * ld) + g0;
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 8
+      for(int i = lane; i < GS_CH; i += 32) {
+        if(i < lim) {
+          const float4 v = __ldcs(vc + i);
+          const float4 x = sw[i];
+          float &a = acc[(i >> 5) & 3];
+          a = fmaf(v.x, x.x, fmaf(v.y, x.y, fmaf(v.z, x.z, fmaf(v.w, x.w, a))));
+        }
+      }
+      float sum = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+      for(int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      if(lane == 0) colAcc[c] += sum;  // column c belongs to this warp only
+    }
   }
+  for(int o = 16; o > 0; o >>= 1) wq += __shfl_xor_sync(0xffffffffu, wq, o);
+  if(lane == 0) wred[warp] = wq;
+  __syncthreads();
+  if(threadIdx.x == 0) {
+    float t = 0.f;
+    for(int k = 0; k < RB / 32; ++k) t += wred[k];
+    colAcc[ncols] = t;  // ||w||^2 for the reorthogonalisation test of the update pass
+  }
+  __syncthreads();
+  for(int c = threadIdx.x; c <= ncols; c += RB) partials[(int64_t)c * MAXRED + blockIdx.x] = (double)colAcc[c];
   __threadfence();
   __syncthreads();
   if(threadIdx.x == 0) last = atomicAdd(&st->counter, 1u) == gridDim.x - 1;
   __syncthreads();
   if(!last) return;
   __threadfence();
-  for(int c = warp; c < ncols; c += RB / 32) {
+  for(int c = warp; c <= ncols; c += RB / 32) {
     const double *pc = partials + (int64_t)c * MAXRED;
     double s8[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
     const int nb = (int)gridDim.x;
@@ -536,8 +569,12 @@ __global__ void __launch_bounds__(RB) k_gs_dots(int64_t n4, int64_t ld, const fl
     double sum = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
     for(int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
     if(lane == 0) {
-      hcur[c] = sum;
-      Hcol[c] = sum;
+      if(c == ncols) {
+        st->result[2] = sum;
+      } else {
+        hcur[c] = sum;
+        Hcol[c] = second ? Hcol[c] + sum : sum;
+      }
     }
   }
   __syncthreads();
@@ -1073,7 +1110,7 @@ double Krylov::norminf(const double *x)
 }
 
 // One FP32 Gram-Schmidt pass (k_gs32) over the first ncols basis vectors.
-void Krylov::gs32(int mode, int ncols, const double *hprev, double *hcur, double *Hcol, const int *done)
+void Krylov::gs32(int mode, int ncols, const double *hprev, double *hcur, double *Hcol, const int *done, int pass)
 {
   RedState *st = (RedState *)red_state_;
   const int g = gsParts_;
@@ -1081,15 +1118,16 @@ void Krylov::gs32(int mode, int ncols, const double *hprev, double *hcur, double
 #define FE_GS_LAUNCH(C)                                                                                         \
   do {                                                                                                          \
     if(mode == 0)                                                                                               \
-      (k_gs32<C, 0><<<g, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done), ::feng::count_launch()); \
+      (k_gs32<C, 0><<<g, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done, pass), ::feng::count_launch()); \
     else if(mode == 1)                                                                                          \
-      (k_gs32<C, 1><<<g, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done), ::feng::count_launch()); \
+      (k_gs32<C, 1><<<g, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done, pass), ::feng::count_launch()); \
     else                                                                                                        \
-      (k_gs32<C, 2><<<g, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done), ::feng::count_launch()); \
+      (k_gs32<C, 2><<<g, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done, pass), ::feng::count_launch()); \
   } while(0)
   if(mode == 0) {
-    const int gb = (int)std::max<int64_t>(1, (n4 + GS_CH - 1) / GS_CH);
-    (k_gs_dots<<<gb, RB, 0, s_>>>(n4, ld32_, V32_, ncols, w32_, red_, st, hcur, Hcol, done), ::feng::count_launch());
+    const int gb = (int)std::max<int64_t>(1, std::min<int64_t>((n4 + GS_CH - 1) / GS_CH, MAXRED));
+    (k_gs_dots<<<gb, RB, 0, s_>>>(n4, ld32_, V32_, ncols, w32_, red_, st, hcur, Hcol, done, pass),
+     ::feng::count_launch());
     return;
   }
   if(ncols <= 8) FE_GS_LAUNCH(8);
@@ -1166,9 +1204,19 @@ void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, i
     precond32(vj, zj, &w.gs->done);
     spmv_launch<float, float, float, float, false>(lanes_, n_, A_, vals, zj, nullptr, w32_, &w.gs->done, s_);
     double *Hcol = w.gs->H + (int64_t)j * (MAXM + 1);
-    gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done);
-    if(opt.gsPasses > 1) gs32(1, j + 1, w.gs->hcur, w.gs->hcur, Hcol, &w.gs->done);
-    gs32(2, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done);
+    if(opt.gsPasses > 1) {
+      // always twice: dots, fused update + dots, update + norm
+      gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 0);
+      gs32(1, j + 1, w.gs->hcur, w.gs->hcur, Hcol, &w.gs->done, 0);
+      gs32(2, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done, 2);
+    } else {
+      // once, and a second time only when the update kept less than a
+      // tenth of ||w|| (decided on the device, so the replayed graph is fixed)
+      gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 0);
+      gs32(2, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done, 0);
+      gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 1);
+      gs32(2, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done, 1);
+    }
     (k_scale32<<<g4, 256, 0, s_>>>(ld32_ / 4, w32_, V32_ + (int64_t)(j + 1) * ld32_, w.st, &w.gs->done),
      ::feng::count_launch());
     (k_givens<<<1, 32, 0, s_>>>(w.gs, j), ::feng::count_launch());

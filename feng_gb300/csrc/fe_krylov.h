@@ -52,6 +52,8 @@ struct DeviceBlockILU {
 struct HostCSR;
 struct PrecondInfo {
   const HostCSR *lap = nullptr;          // scalar stiffness on the nodes
+  const HostCSR *massV = nullptr;        // scalar P2 mass on the nodes (same pattern as lap)
+  const HostCSR *lapP = nullptr;         // P1 stiffness on the pressure unknowns (kind 4)
   std::vector<int32_t> nodeDofX, nodeDofY;  // unknown DOF of each node (per component)
   std::vector<int32_t> pRows;            // pressure unknowns (kind 4)
   std::vector<double> pMass;             // lumped pressure mass of pRows
@@ -71,7 +73,7 @@ struct KrylovOptions {
   int mixed = 0;           // 1: FP32 matrix/preconditioner/SpMV inside FP64 refinement
   int refineMax = 20;      // outer refinement steps in mixed mode
   double innerRtol = 1e-4; // inner FP32 solve tolerance in mixed mode
-  int gsPasses = 1;        // classical Gram-Schmidt passes of the mixed FGMRES (1 or 2)
+  int gsPasses = 1;        // mixed FGMRES Gram-Schmidt: 1 = once + second pass when needed, 2 = always twice
 };
 
 struct KrylovStats {
@@ -125,7 +127,9 @@ class Krylov {
   float *V32_ = nullptr;  // (m+1) x n  Krylov basis of the mixed path, FP32
   int gsParts_ = 0;       // blocks of the FP32 Gram-Schmidt passes
   int64_t ld32_ = 0;      // leading dimension of V32_ / Z32_ (multiple of 64)
-  void gs32(int mode, int ncols, const double *hprev, double *hcur, double *Hcol, const int *done);
+  // pass: 0 first pass (the update + norm decides on reorthogonalisation),
+  // 1 the conditional second pass, 2 the last pass of an unconditional CGS2
+  void gs32(int mode, int ncols, const double *hprev, double *hcur, double *Hcol, const int *done, int pass);
   float *v32_ = nullptr, *w32_ = nullptr;
   double *w_ = nullptr, *r_ = nullptr, *t_ = nullptr, *p_ = nullptr, *q_ = nullptr;
   double *diag_ = nullptr;    // inverse diagonal (Jacobi)
@@ -161,6 +165,12 @@ class Krylov {
  public:
   bool useGraphs_ = true;  // replay full restart cycles from CUDA graphs
   int setup_mg(const PrecondInfo &pi);
+  // Time-dependent saddle-point problems (velocity block ~ c0 M + mu K):
+  // rebuilds the velocity multigrid on K + (c0/mu) M and adds the
+  // Cahouet-Chabard term c0 L_p^-1 (pressure Laplacian multigrid) to the
+  // Schur complement approximation mu M_p^-1.  c0 = 0 restores the steady
+  // preconditioner.  Replayed cycle graphs are rebuilt.
+  int setTransientShift(double c0, double mu);
   // The multigrid's finest-level smoother step alone (benchmarking); bytes:
   // its algorithmic bytes, 0 when there is no multigrid.
   int smootherStep(int64_t *bytes);

@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <memory>
 
 #include "fe_amg.h"
 #include "fe_common.h"
@@ -27,7 +28,14 @@ namespace feng {
   } while(0)
 
 struct Krylov::MG {
-  AMGDevice amg;
+  std::unique_ptr<AMGDevice> amg = std::make_unique<AMGDevice>();
+  // Time-dependent problems: the stiffness and mass kept for re-set-ups,
+  // the pressure Laplacian multigrid and the Cahouet-Chabard coefficient.
+  HostCSR lapH, massH, lapPH;
+  std::unique_ptr<AMGDevice> amgP;
+  AMGParams params;
+  double cc = 0.;
+  void *pr = nullptr, *pz = nullptr;
   int kind = 0;
   int64_t nNodes = 0, nP = 0;
   int32_t *dofX = nullptr, *dofY = nullptr, *pRows = nullptr;
@@ -39,7 +47,7 @@ struct Krylov::MG {
   double cMc = 0, cSc = 0;  // constant pressure mode: c^T M c and c^T S c (deflation)
   double *pMassDev = nullptr, *tP = nullptr;
   double *consts = nullptr;   // device: 1/s, c^T S c, c^T M c
-  double hconst[3] = {1, 0, 0};
+  double hconst[4] = {1, 0, 0, 0};
   int32_t *diagX = nullptr;                                        // CSR position of diag of x rows
   double *pScale64 = nullptr;
   float *pScale32 = nullptr;
@@ -62,6 +70,7 @@ struct Krylov::MG {
     cudaFree(zy); cudaFree(dsum); cudaFree(ir); cudaFree(iz); cudaFree(ip); cudaFree(iq);
     cudaFree(part); cudaFree(scal); cudaFree(dnIa); cudaFree(dnPos); cudaFree(dnCol); cudaFree(slotOf);
     cudaFree(pMassDev); cudaFree(tP); cudaFree(consts); cudaFree(bxy); cudaFree(zxy); cudaFree(gVals);
+    cudaFree(pr); cudaFree(pz);
   }
   template <typename V> void solveK(const V *b, V *x, cudaStream_t st);
 };
@@ -147,12 +156,12 @@ void Krylov::MG::solveK(const V *b, V *x, cudaStream_t st)
 {
   const int64_t n = nNodes;
   auto vc = [&](const V *in, V *out) {
-    if constexpr(sizeof(V) == 8) amg.vcycle64(in, out);
-    else amg.vcycle32(in, out);
+    if constexpr(sizeof(V) == 8) amg->vcycle64(in, out);
+    else amg->vcycle32(in, out);
   };
   auto spmv = [&](const V *in, V *out) {
-    if constexpr(sizeof(V) == 8) amg.spmv64(in, out);
-    else amg.spmv32(in, out);
+    if constexpr(sizeof(V) == 8) amg->spmv64(in, out);
+    else amg->spmv32(in, out);
   };
   if(inner <= 0) {
     vc(b, x);
@@ -325,6 +334,31 @@ __global__ void k_gather_vals(int64_t n, const int32_t *__restrict__ pos, const 
     out[e] = a[pos[e]];
 }
 
+// Cahouet-Chabard term: pr = r_p - (c^T r / c^T M c) m_p (the same deflated
+// pressure residual as k_pressure) in the P1 Laplacian's row order, and
+// z_p += cc * pz afterwards.
+template <typename V>
+__global__ void k_p_gather(int64_t nP, const int32_t *__restrict__ rows, const double *__restrict__ mass,
+                           const double *__restrict__ cr, const double *__restrict__ consts, const V *__restrict__ r,
+                           V *__restrict__ pr, const int *__restrict__ skip)
+{
+  if(skip && *skip) return;
+  const double cMc = consts[2];
+  const double shift = cMc > 0 ? *cr / cMc : 0.;
+  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nP; k += (int64_t)gridDim.x * blockDim.x)
+    pr[k] = (V)((double)r[rows[k]] - shift * mass[k]);
+}
+
+template <typename V>
+__global__ void k_p_add(int64_t nP, const int32_t *__restrict__ rows, const V *__restrict__ pz,
+                        const double *__restrict__ consts, V *__restrict__ z, const int *__restrict__ skip)
+{
+  if(skip && *skip) return;
+  const V cc = (V)consts[3];
+  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nP; k += (int64_t)gridDim.x * blockDim.x)
+    z[rows[k]] += cc * pz[k];
+}
+
 // The same right-hand side, both components interleaved: bxy[2 k + c].
 template <typename V>
 __global__ void k_vel_rhs_pair(int64_t nN, const int32_t *__restrict__ dofX, const int32_t *__restrict__ dofY,
@@ -399,11 +433,17 @@ int Krylov::setup_mg(const PrecondInfo &pi)
   }
   AMGParams ap;
   ap.chebyDegree = pi.chebyDegree;
+  M.params = ap;
   M.inner = pi.innerIterations;
+  if(M.kind == 4) {
+    M.lapH = *pi.lap;
+    if(pi.massV) M.massH = *pi.massV;
+    if(pi.lapP) M.lapPH = *pi.lapP;
+  }
   AMGHierarchy H;
   FE_TRY(amg_build(*pi.lap, ap, H));
-  FE_TRY(M.amg.upload(H, ap, M.fp32, s_));
-  M.lapDiagSum = M.amg.finestDiagSum();
+  FE_TRY(M.amg->upload(H, ap, M.fp32, s_));
+  M.lapDiagSum = M.amg->finestDiagSum();
   FE_TRY(up(&M.dofX, pi.nodeDofX));
   if(M.kind == 4) FE_TRY(up(&M.dofY, pi.nodeDofY));
   const size_t vs = M.fp32 ? sizeof(float) : sizeof(double);
@@ -413,7 +453,7 @@ int Krylov::setup_mg(const PrecondInfo &pi)
   CKM(cudaMalloc(&M.dsum, sizeof(double)));
   CKM(cudaMalloc(&M.part, sizeof(double) * NPART));
   CKM(cudaMalloc(&M.scal, sizeof(double) * 4));
-  CKM(cudaMalloc(&M.consts, sizeof(double) * 3));
+  CKM(cudaMalloc(&M.consts, sizeof(double) * 4));
   CKM(cudaMemset(M.scal, 0, sizeof(double) * 4));
   // Host pattern for the diagonal positions and the G block.
   std::vector<int32_t> hia(n_ + 1), hja(A_.nnz);
@@ -481,7 +521,7 @@ int Krylov::setup_mg(const PrecondInfo &pi)
 int Krylov::factor_mg(const double *values64, const float *values32)
 {
   MG &M = *mg_;
-  M.amg.setSkip(nullptr);
+  M.amg->setSkip(nullptr);
   if(values64) (k_diag_sum<double><<<1, 256, 0, s_>>>(M.nNodes, M.diagX, values64, M.dsum), ::feng::count_launch());
   else (k_diag_sum<float><<<1, 256, 0, s_>>>(M.nNodes, M.diagX, values32, M.dsum), ::feng::count_launch());
   double sum = 0.;
@@ -540,8 +580,52 @@ int Krylov::factor_mg(const double *values64, const float *values32)
   M.hconst[0] = 1.0 / M.s;
   M.hconst[1] = M.cSc;
   M.hconst[2] = M.cMc;
-  CKM(cudaMemcpyAsync(M.consts, M.hconst, sizeof(double) * 3, cudaMemcpyHostToDevice, s_));
+  M.hconst[3] = M.cc;
+  CKM(cudaMemcpyAsync(M.consts, M.hconst, sizeof(double) * 4, cudaMemcpyHostToDevice, s_));
   CKM(cudaStreamSynchronize(s_));
+  return FE_OK;
+}
+
+int Krylov::setTransientShift(double c0, double mu)
+{
+  if(!mg_ || mg_->kind != 4) return FE_OK;
+  MG &M = *mg_;
+  if(!(c0 >= 0.) || !(mu > 0.)) {
+    set_error("transient shift needs c0 >= 0 and a positive viscosity");
+    return FE_INVALID_ARG;
+  }
+  if(M.massH.a.size() != M.lapH.a.size() || M.lapPH.n != M.nP) {
+    set_error("transient shift: preconditioner operators missing");
+    return FE_INVALID_ARG;
+  }
+  // Velocity multigrid on K + (c0 / mu) M (same pattern).
+  HostCSR L = M.lapH;
+  const double alpha = c0 / mu;
+  for(size_t k = 0; k < L.a.size(); ++k) L.a[k] += alpha * M.massH.a[k];
+  AMGHierarchy H;
+  FE_TRY(amg_build(L, M.params, H));
+  auto amg = std::make_unique<AMGDevice>();
+  FE_TRY(amg->upload(H, M.params, M.fp32, s_));
+  M.amg = std::move(amg);
+  M.lapDiagSum = M.amg->finestDiagSum();
+  // Pressure Laplacian multigrid (built once) and the Cahouet-Chabard weight.
+  if(c0 > 0. && !M.amgP) {
+    AMGHierarchy HP;
+    FE_TRY(amg_build(M.lapPH, M.params, HP));
+    auto ap = std::make_unique<AMGDevice>();
+    FE_TRY(ap->upload(HP, M.params, M.fp32, s_));
+    M.amgP = std::move(ap);
+    const size_t vs = M.fp32 ? sizeof(float) : sizeof(double);
+    CKM(cudaMalloc(&M.pr, vs * std::max<int64_t>(1, M.nP)));
+    CKM(cudaMalloc(&M.pz, vs * std::max<int64_t>(1, M.nP)));
+  }
+  M.cc = c0;
+  if(c0 == 0.) M.amgP.reset();
+  // The replayed cycles hold pointers into the old hierarchy.
+  for(auto &g : graphs_) cudaGraphExecDestroy(g.second);
+  graphs_.clear();
+  graphKernels_.clear();
+  factoredOk_ = false;  // rebuilt (scale, deflation) at the next factor
   return FE_OK;
 }
 
@@ -552,9 +636,9 @@ int Krylov::smootherStep(int64_t *bytes)
     set_error("no multigrid preconditioner");
     return FE_INVALID_ARG;
   }
-  mg_->amg.setSkip(nullptr);
-  mg_->amg.fineStep2();
-  if(bytes) *bytes = mg_->amg.fineStep2Bytes();
+  mg_->amg->setSkip(nullptr);
+  mg_->amg->fineStep2();
+  if(bytes) *bytes = mg_->amg->fineStep2Bytes();
   return FE_OK;
 }
 
@@ -562,7 +646,7 @@ template <typename V>
 void Krylov::apply_mg(const V *vals, const V *r, V *z, const int *skip)
 {
   MG &M = *mg_;
-  M.amg.setSkip(skip);
+  M.amg->setSkip(skip);
   if(M.kind == 3) {
     // z = (s K)^-1 r on the unknown rows (the nodes are the unknowns)
     (k_vel_rhs<V><<<grid(M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofX, nullptr, nullptr, nullptr,
@@ -578,14 +662,24 @@ void Krylov::apply_mg(const V *vals, const V *r, V *z, const int *skip)
     else
       (k_pressure<V, float><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.pRows, M.pScale32, M.pMassDev, cr, M.consts,
                                                        r, z, skip), ::feng::count_launch());
+    if(M.amgP) {
+      // + c0 L_p^-1 r_p (Cahouet-Chabard); its V-cycle skips with the cycle
+      M.amgP->setSkip(skip);
+      (k_p_gather<V><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.pRows, M.pMassDev, cr, M.consts, r, (V *)M.pr, skip),
+       ::feng::count_launch());
+      if constexpr(sizeof(V) == 8) M.amgP->vcycle64((const double *)M.pr, (double *)M.pz);
+      else M.amgP->vcycle32((const float *)M.pr, (float *)M.pz);
+      (k_p_add<V><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.pRows, (const V *)M.pz, M.consts, z, skip),
+       ::feng::count_launch());
+    }
     if(M.inner <= 0) {
       // Both velocity components through one paired V-cycle (one pass over
       // each level operator for the two right-hand sides).
       (k_vel_rhs_pair<V><<<grid(2 * M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, M.upIa, nullptr, M.upCol,
                                                                (const V *)M.gVals, r, z, (V *)M.bxy, skip),
        ::feng::count_launch());
-      if constexpr(sizeof(V) == 8) M.amg.vcycle2_64((const double *)M.bxy, (double *)M.zxy);
-      else M.amg.vcycle2_32((const float *)M.bxy, (float *)M.zxy);
+      if constexpr(sizeof(V) == 8) M.amg->vcycle2_64((const double *)M.bxy, (double *)M.zxy);
+      else M.amg->vcycle2_32((const float *)M.bxy, (float *)M.zxy);
       (k_vel_out_pair<V><<<grid(2 * M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, (const V *)M.zxy, M.consts,
                                                               z, skip), ::feng::count_launch());
       return;

@@ -355,9 +355,16 @@ int SystemCUDA::build_precond_info(const SystemTables &t, const RefTensors &T, H
       pi.nodeDofX.push_back((int32_t)dx);
       if(th) pi.nodeDofY.push_back((int32_t)t.adr[e * nl + 2 * a + 1]);
     }
-  std::vector<std::pair<int64_t, double>> coo;  // (row*nN + col, value)
+  struct Entry {
+    int64_t key;  // row * nN + col
+    double k, m;  // stiffness and mass
+  };
+  std::vector<Entry> coo;
   coo.reserve(nE * 36);
   std::vector<double> pm(nDofs_, 0.);
+  // pressure unknown -> index (the P1 Laplacian's rows), by first appearance
+  std::vector<int32_t> pIdx(th ? nDofs_ : 0, -1);
+  std::vector<std::pair<int64_t, double>> cooP;
   for(int64_t e = 0; e < nE; ++e) {
     const double *c = t.elemXY + 6 * e;
     const double dxdr0 = c[2] - c[0], dxdr1 = c[3] - c[1], dxds0 = c[4] - c[0], dxds1 = c[5] - c[1];
@@ -378,32 +385,82 @@ int SystemCUDA::build_precond_info(const SystemTables &t, const RefTensors &T, H
         double v = 0.;
         for(int r = 0; r < 2; ++r)
           for(int s = 0; s < 2; ++s) v += GG[r][s] * T.K[r][s][a][b];
-        coo.push_back({(int64_t)nd[a] * nN + nd[b], std::fabs(jac) * v});
+        coo.push_back({(int64_t)nd[a] * nN + nd[b], std::fabs(jac) * v, std::fabs(jac) * T.M[a][b]});
       }
     }
-    if(th)
+    if(th) {
       for(int j = 0; j < 3; ++j) pm[t.adr[e * nl + 12 + j]] += std::fabs(jac) / 6.0;
+      // P1 stiffness |J|/2 grad psi_i . grad psi_j on the pressure unknowns
+      const double dr[3] = {-1., 1., 0.}, ds[3] = {-1., 0., 1.};
+      int32_t pk[3];
+      for(int j = 0; j < 3; ++j) {
+        const int64_t d = t.adr[e * nl + 12 + j];
+        pk[j] = -1;
+        if(d < nInc_) {
+          if(pIdx[d] < 0) pIdx[d] = nPLap_++;
+          pk[j] = pIdx[d];
+        }
+      }
+      for(int i = 0; i < 3; ++i) {
+        if(pk[i] < 0) continue;
+        const double gix = G[0][0] * dr[i] + G[1][0] * ds[i], giy = G[0][1] * dr[i] + G[1][1] * ds[i];
+        for(int j = 0; j < 3; ++j) {
+          if(pk[j] < 0) continue;
+          const double gjx = G[0][0] * dr[j] + G[1][0] * ds[j], gjy = G[0][1] * dr[j] + G[1][1] * ds[j];
+          cooP.push_back({(int64_t)pk[i] << 32 | (uint32_t)pk[j], 0.5 * std::fabs(jac) * (gix * gjx + giy * gjy)});
+        }
+      }
+    }
   }
-  std::sort(coo.begin(), coo.end(),
-            [](const std::pair<int64_t, double> &x, const std::pair<int64_t, double> &y) { return x.first < y.first; });
+  std::sort(coo.begin(), coo.end(), [](const Entry &x, const Entry &y) { return x.key < y.key; });
   lap = HostCSR();
   lap.n = lap.m = nN;
   lap.ia.assign(nN + 1, 0);
+  massV_ = HostCSR();
+  massV_.n = massV_.m = nN;
   for(size_t k = 0; k < coo.size();) {
-    const int64_t key = coo[k].first;
-    double v = 0.;
-    while(k < coo.size() && coo[k].first == key) v += coo[k++].second;
+    const int64_t key = coo[k].key;
+    double v = 0., mv = 0.;
+    while(k < coo.size() && coo[k].key == key) {
+      v += coo[k].k;
+      mv += coo[k].m;
+      ++k;
+    }
     lap.ja.push_back((int32_t)(key % nN));
     lap.a.push_back(v);
+    massV_.a.push_back(mv);
     lap.ia[key / nN + 1] = (int64_t)lap.ja.size();
   }
   for(int64_t i = 0; i < nN; ++i) lap.ia[i + 1] = std::max(lap.ia[i + 1], lap.ia[i]);
+  massV_.ia = lap.ia;
+  massV_.ja = lap.ja;
   pi.lap = &lap;
+  pi.massV = &massV_;
+  if(th && nPLap_ > 0) {
+    std::sort(cooP.begin(), cooP.end(),
+              [](const std::pair<int64_t, double> &x, const std::pair<int64_t, double> &y) { return x.first < y.first; });
+    lapP_ = HostCSR();
+    lapP_.n = lapP_.m = nPLap_;
+    lapP_.ia.assign(nPLap_ + 1, 0);
+    for(size_t k = 0; k < cooP.size();) {
+      const int64_t key = cooP[k].first;
+      double v = 0.;
+      while(k < cooP.size() && cooP[k].first == key) v += cooP[k++].second;
+      lapP_.ja.push_back((int32_t)(key & 0xffffffff));
+      lapP_.a.push_back(v);
+      lapP_.ia[(key >> 32) + 1] = (int64_t)lapP_.ja.size();
+    }
+    for(int64_t i = 0; i < nPLap_; ++i) lapP_.ia[i + 1] = std::max(lapP_.ia[i + 1], lapP_.ia[i]);
+    pi.lapP = &lapP_;
+  }
   if(th) {
+    // pressure unknowns in the order of the P1 Laplacian's rows
+    pi.pRows.assign(nPLap_, -1);
+    pi.pMass.assign(nPLap_, 0.);
     for(int64_t d = 0; d < nInc_; ++d)
-      if(pm[d] > 0) {
-        pi.pRows.push_back((int32_t)d);
-        pi.pMass.push_back(pm[d]);
+      if(pIdx[d] >= 0) {
+        pi.pRows[pIdx[d]] = (int32_t)d;
+        pi.pMass[pIdx[d]] = pm[d];
       }
     pi.sigma = fc_.hasSigma ? fc_.sigma : 1.0;
     pi.divu = fc_.hasDivu ? fc_.divu : 1.0;
@@ -559,6 +616,16 @@ __global__ void k_periodic_rows(int64_t nPairs, const int64_t *__restrict__ mast
   }
 }
 }  // namespace
+
+int SystemCUDA::setTransientShift(double c0)
+{
+  if(!fc_.hasMass || !fc_.hasSigma) return FE_OK;
+  const double c0eff = fc_.mass * c0, mueff = std::fabs(fc_.sigma) * fc_.mu;
+  if(!(c0eff >= 0.) || !(mueff > 0.)) return FE_OK;
+  FE_TRY(kry_.setTransientShift(c0eff, mueff));
+  factorPending_ = true;
+  return FE_OK;
+}
 
 int SystemCUDA::setConstrainedRows(const int64_t *rows, int64_t n)
 {

@@ -75,6 +75,10 @@ class SystemCUDA {
   int applyPeriodicity();
   // Builds the preconditioner of the current matrix if it changed.
   int factorIfPending();
+  // BDF time stepping with c0 = dudt coefficient of the current step: adapts
+  // the multigrid saddle-point preconditioner (Krylov::setTransientShift)
+  // with c0 times the mass coefficient and the form's viscosity.
+  int setTransientShift(double c0);
   int solve(double *normDx, double *normRHS, double *normAxb, int *nIter);
   int correctSolution();
 
@@ -161,6 +165,8 @@ class SystemCUDA {
   bool constrained_ = false, periodic_ = false;
   int64_t *conRows_ = nullptr, *conColPos_ = nullptr, *perMaster_ = nullptr, *perSlave_ = nullptr;
   int64_t nCon_ = 0, nConPos_ = 0, nPer_ = 0;
+  HostCSR massV_, lapP_;   // preconditioner operators kept for transient re-set-ups
+  int32_t nPLap_ = 0;
   int begin_phase();
   float end_phase();
   int build_precond_info(const SystemTables &t, const RefTensors &T, HostCSR &lap, PrecondInfo &pi);

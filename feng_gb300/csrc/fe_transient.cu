@@ -185,6 +185,9 @@ int Transient::init(SystemCUDA *sys, const TransientOptions &o, const NewtonOpti
   CKT(cudaEventCreate(&e3_));
   const double cn[3] = {1.0 / o.dt, -1.0 / o.dt, 0.0};
   FE_TRY(sys->setBDFCoefficients(2, cn));  // allocates the device history
+  // Preconditioner for the time-dependent saddle point: the BDF2 coefficient
+  // of u^{n+1} at constant steps, 1.5 / dt (the two starter solves differ).
+  FE_TRY(sys->setTransientShift(1.5 / o.dt));
   CKT(cudaMemsetAsync(sys->dHist(1), 0, sizeof(double) * nDofs, s));
   CKT(cudaMemsetAsync(sys->dHist(2), 0, sizeof(double) * nDofs, s));
   CKT(cudaMemsetAsync(h3_, 0, sizeof(double) * nDofs, s));

@@ -108,7 +108,8 @@ typedef struct fe_cuda_options {
   int32_t mg_inner;       /* multigrid: inner AMG-preconditioned CG steps per velocity
                              component (0 = a single V-cycle) */
   int32_t mg_smooth;      /* multigrid: Chebyshev smoother degree (1..6; 0 = default 1) */
-  int32_t gs_passes;      /* mixed FGMRES: classical Gram-Schmidt passes, 1 or 2 (0 = default 1) */
+  int32_t gs_passes;      /* mixed FGMRES Gram-Schmidt: 1 = one pass, a second when the update keeps
+                             less than a tenth of the norm; 2 = always two (0 = default 1) */
 } fe_cuda_options;
 
 /* Newton options (feNLSolverOptions, src/feNonLinearSolver.h:12-40) plus the

@@ -89,3 +89,21 @@ def test_kovasznay_block_jacobi_fgmres():
     st = fe.solveNewtonRaphson(sys, sol, fe.feNLSolverOptions(tolResidual=1e-12, maxIter=30))
     assert st["return"] == 0
     assert rel_err(sol.u, g["usol"]) <= TOL_SOL
+
+
+def test_mixed_krylov_at_large_size_matches_fp64():
+    """Mixed FGMRES on more than 4 M rows' worth of Gram-Schmidt chunks
+    (1024 blocks of partial sums are exceeded, so the dot pass loops over
+    chunks): a Kovasznay 400 x 400 Newton solve converges like the FP64 one."""
+    from feng_gb300 import kovasznay
+    _, num, forms = kovasznay.build(400, 40.0)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        sys, _ = kovasznay.make_system(num, forms, prec)
+        st = fe.solveNewtonRaphson(sys, None, kovasznay.newton_options(prec))
+        assert st["return"] == 0, (prec, st)
+        assert st["residual"] <= 1e-8 * st["residual0"]
+        out[prec] = sys.getSolution()
+    # both stop at ||R|| <= 1e-8 ||R0||; at this size that bounds the
+    # difference of the two solutions near 1e-5 relative (max norm)
+    assert rel_err(out["mixed"], out["fp64"]) <= 1e-5
