@@ -264,7 +264,9 @@ int upload_idx(int32_t **dst, const std::vector<int32_t> &src)
 int lanes_for(const HostCSR &M)
 {
   const double avg = M.n ? (double)M.nnz() / M.n : 0;
-  return avg > 24 ? 16 : avg > 10 ? 8 : 4;
+  // 4 lanes per row on the P2 stiffness (~11 entries per row): 21 us per
+  // finest smoother step against 27 us with 8 lanes
+  return avg > 24 ? 16 : avg > 12 ? 8 : 4;
 }
 
 }  // namespace
