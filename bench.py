@@ -403,10 +403,10 @@ def main():
     # The dominant kernel of the Newton step (the Krylov solve is ~97% of it):
     # the finest-level step of the velocity multigrid smoother.
     top = kern["mixed"]["smoother_step"]
-    roof = {"kernel": "k_cheb_step<float,8,2> (finest AMG level, both velocity components)", "bound": "hbm",
+    roof = {"kernel": "k_cheb_step<float,4,2> (finest AMG level, both velocity components)", "bound": "hbm",
             "achieved": top["gbs"], "peak": peak, "unit": "GB/s", "frac": top["gbs"] / peak,
             "peak_source": peak_kind, "bytes_per_launch": top["bytes"], "ms_per_launch": top["ms"],
-            "traffic": ncu_traffic("k_cheb_step<float,8,2>")}
+            "traffic": ncu_traffic("k_cheb_step<float,4,2>")}
     asm = kern["mixed"]["matrix_assembly"]
     roof_asm = {"kernel": "k_matrix_th<float> (Jacobian assembly, all colors)", "bound": "hbm",
                 "achieved": asm["gbs"], "peak": peak, "unit": "GB/s", "frac": asm["gbs"] / peak,

@@ -94,11 +94,12 @@ __global__ void k_features(int64_t nNodes, const int32_t *__restrict__ nd, const
   }
 }
 
-// um = ue + s * y on the node's unknowns (pressure at vertex nodes only).
+// um = ue + scale * s * y on the node's unknowns (pressure at vertex nodes only).
 __global__ void k_apply(int64_t nNodes, int64_t nInc, const int32_t *__restrict__ nd, const float *__restrict__ Y,
-                        const float *__restrict__ sig, const double *__restrict__ ue, double *__restrict__ um)
+                        const float *__restrict__ sig, float scale, const double *__restrict__ ue,
+                        double *__restrict__ um)
 {
-  const float su = safe_scale(sig[0]), sp = safe_scale(sig[1]);
+  const float su = scale * safe_scale(sig[0]), sp = scale * safe_scale(sig[1]);
   for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nNodes; k += (int64_t)gridDim.x * blockDim.x) {
     const int32_t u = nd[4 * k], v = nd[4 * k + 1], p = nd[4 * k + 2];
     if(u < nInc) um[u] = ue[u] + (double)(su * Y[k * NO]);
@@ -396,20 +397,37 @@ int Transient::step(StepStats &st)
       CKT(cudaGetLastError());
     }
     if(learn && trained_ > 0 && st.step >= o_.useFrom) {
+      // The learned correction is tried at full, half and quarter length
+      // (each candidate judged by the FP64 residual); the extrapolation is
+      // kept when no candidate beats it.
       FE_TRY(mlp_.forward(X_, nNodes_, Y_));
-      CKT(cudaMemcpyAsync(um_, ue_, bytes, cudaMemcpyDeviceToDevice, s));
-      (k_apply<<<grid_of(nNodes_), 256, 0, s>>>(nNodes_, nInc, nodeDof_, Y_, sig_, ue_, um_), ::feng::count_launch());
-      CKT(cudaGetLastError());
-      double rm = 0., re = 0.;
-      CKT(cudaMemcpyAsync(sys_->dU(), um_, bytes, cudaMemcpyDeviceToDevice, s));
-      FE_TRY(residualNorm(&rm));
+      double re = 0., best = 0.;
       CKT(cudaMemcpyAsync(sys_->dU(), ue_, bytes, cudaMemcpyDeviceToDevice, s));
       FE_TRY(residualNorm(&re));
       st.residualExtrap = re;
-      if(rm < re) {
+      best = re;
+      float bestScale = 0.f;
+      for(float scale : {1.f, 0.5f, 0.25f}) {
+        CKT(cudaMemcpyAsync(um_, ue_, bytes, cudaMemcpyDeviceToDevice, s));
+        (k_apply<<<grid_of(nNodes_), 256, 0, s>>>(nNodes_, nInc, nodeDof_, Y_, sig_, scale, ue_, um_),
+         ::feng::count_launch());
+        CKT(cudaGetLastError());
+        double rm = 0.;
         CKT(cudaMemcpyAsync(sys_->dU(), um_, bytes, cudaMemcpyDeviceToDevice, s));
+        FE_TRY(residualNorm(&rm));
+        if(rm < best) {
+          best = rm;
+          bestScale = scale;
+        }
+      }
+      CKT(cudaMemcpyAsync(um_, ue_, bytes, cudaMemcpyDeviceToDevice, s));
+      if(bestScale > 0.f) {
+        (k_apply<<<grid_of(nNodes_), 256, 0, s>>>(nNodes_, nInc, nodeDof_, Y_, sig_, bestScale, ue_, um_),
+         ::feng::count_launch());
+        CKT(cudaGetLastError());
         used = GUESS_LEARNED;
       }
+      CKT(cudaMemcpyAsync(sys_->dU(), um_, bytes, cudaMemcpyDeviceToDevice, s));
     } else if(canExtrap) {
       CKT(cudaMemcpyAsync(sys_->dU(), ue_, bytes, cudaMemcpyDeviceToDevice, s));
     }

@@ -11,10 +11,12 @@
 //   learned       the extrapolation plus a per-node correction predicted by
 //                 an MLP (fe_mlp.h) from the last three solutions and the
 //                 local geometry, trained online on the corrections that the
-//                 converged steps reveal.  Both candidates are evaluated with
-//                 the full FP64 residual and the smaller one is used, so the
-//                 extrapolation is the fallback and the converged answer does
-//                 not depend on the network.
+//                 converged steps reveal.  The correction is tried at full,
+//                 half and quarter length; those candidates and the plain
+//                 extrapolation are evaluated with the full FP64 residual and
+//                 the smallest start is used, so the extrapolation is the
+//                 fallback and the converged answer does not depend on the
+//                 network.
 // The Newton stop is relative to the residual of u^n at the new time level
 // (fixed before any guess is formed), so a better guess can only save work.
 #pragma once
