@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(EPB * 6) k_residual_p2(DeviceMesh dm, FormCoef
     be -= fc.srcCoeff * acc * J;
   }
   const int32_t d = sA[a][lane];
-  if(d < nInc) rhs[d] += be;
+  if(d < nInc) atomicAdd(rhs + d, be);  // one contribution per DOF and color
 }
 
 // ---------------------------------------------------------------------------
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(EPB * 6) k_matrix_p2(DeviceMesh dm, FormCoeffs
     for(int r = 0; r < 2; ++r)
       for(int s2 = 0; s2 < 2; ++s2) L += GG[r][s2] * sT.K[r][s2][a][b];
     const int32_t pos = dm.map[(int64_t)(a * 6 + b) * nE + p];
-    if(pos >= 0) values[pos] += cJ * L;
+    if(pos >= 0) atomicAdd(values + pos, cJ * L);  // one contribution per entry and color
   }
 }
 
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(EPB * 6) k_residual_th(DeviceMesh dm, FormCoef
   }
   for(int m = 0; m < 2; ++m) {
     const int32_t d = sA[2 * a + m][lane];
-    if(d < nInc) rhs[d] += be[m];
+    if(d < nInc) atomicAdd(rhs + d, be[m]);  // one contribution per DOF and color
   }
   if(fc.hasDivu && a < 3) {
     // Be_pj -= c div u psi_j jac w   (feVectorSysElm.cpp:722-747), j = a
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(EPB * 6) k_residual_th(DeviceMesh dm, FormCoef
       for(int n = 0; n < 2; ++n)
         acc += sU[2 * b + n][lane] * (G[0][n] * sT.D[0][a][b] + G[1][n] * sT.D[1][a][b]);
     const int32_t d = sA[12 + a][lane];
-    if(d < nInc) rhs[d] -= fc.divu * acc * J;
+    if(d < nInc) atomicAdd(rhs + d, -fc.divu * acc * J);
   }
 }
 
@@ -446,13 +446,13 @@ __global__ void __launch_bounds__(EPB * 6) k_residual_th_q(DeviceMesh dm, FormCo
   }
   for(int m = 0; m < 2; ++m) {
     const int32_t d = sA[2 * a + m][lane];
-    if(d < nInc) rhs[d] += be[m];
+    if(d < nInc) atomicAdd(rhs + d, be[m]);  // one contribution per DOF and color
   }
   if(fc.hasDivu && a < 3) {
     double acc = 0.;
     for(int q = 0; q < 7; ++q) acc += sQ[q][6][lane] * gT->psi5[q][a];
     const int32_t d = sA[12 + a][lane];
-    if(d < nInc) rhs[d] += acc;
+    if(d < nInc) atomicAdd(rhs + d, acc);
   }
 }
 
@@ -490,12 +490,12 @@ __device__ __forceinline__ void scatter_staged(const int32_t *__restrict__ map, 
         }
       }
     }
-    V old[BATCH];
-#pragma unroll
-    for(int q = 0; q < BATCH; ++q) old[q] = pos[q] >= 0 ? values[pos[q]] : (V)0;
+    // Within one color every CSR entry receives at most one contribution, so
+    // the reduction in L2 (no round trip to the SM) gives the same bits as
+    // a read-modify-write.
 #pragma unroll
     for(int q = 0; q < BATCH; ++q)
-      if(pos[q] >= 0) values[pos[q]] = old[q] + add[q];
+      if(pos[q] >= 0) atomicAdd(values + pos[q], add[q]);
   }
 }
 
