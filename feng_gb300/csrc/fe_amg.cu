@@ -211,6 +211,61 @@ __global__ void __launch_bounds__(256) k_cheb_step(int64_t n, const int32_t *__r
   }
 }
 
+// Start from x = 0 fused with the first step: with d = D^-1 b / theta
+// (formed on the fly for the neighbours), x = d, r = D^-1 b - D^-1 A d,
+// dn = c1 d + c2 r.
+template <typename V, int LANES, int NV>
+__global__ void __launch_bounds__(256) k_cheb_first(int64_t n, const int32_t *__restrict__ ia,
+                                                    const int32_t *__restrict__ ja, const V *__restrict__ a,
+                                                    const V *__restrict__ dinv, const V *__restrict__ b,
+                                                    V *__restrict__ dn, V *__restrict__ r, V *__restrict__ x,
+                                                    V inv_theta, V c1, V c2, const int *__restrict__ skip)
+{
+  if(skip && *skip) return;
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
+  const int sub = threadIdx.x % LANES;
+  const bool live = row < n;
+  const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
+  V acc[NV];
+#pragma unroll
+  for(int c = 0; c < NV; ++c) acc[c] = 0;
+  for(int32_t k = beg + sub; k < end; k += LANES) {
+    const int32_t j = __ldcs(ja + k);
+    const V ak = __ldcs(a + k) * dinv[j];
+    const Vals<V, NV> bv = ldv<V, NV>(b, j);
+#pragma unroll
+    for(int c = 0; c < NV; ++c) acc[c] += ak * bv.v[c];
+  }
+#pragma unroll
+  for(int c = 0; c < NV; ++c)
+#pragma unroll
+    for(int o = LANES / 2; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o, LANES);
+  if(live && sub < NV) {
+    const V dv = dinv[row];
+    V ac = acc[0];
+#pragma unroll
+    for(int c = 1; c < NV; ++c)
+      if(sub == c) ac = acc[c];
+    const int64_t o = row * NV + sub;
+    const V r0 = dv * b[o];
+    const V di = r0 * inv_theta;
+    x[o] = di;
+    const V ri = r0 - dv * ac * inv_theta;
+    r[o] = ri;
+    dn[o] = c1 * di + c2 * ri;
+  }
+}
+
+// Last step of a smoothing whose residual is not needed afterwards: x += d
+// only (the step's product with A would be discarded).
+template <typename V>
+__global__ void k_cheb_last(int64_t m, const V *__restrict__ d, V *__restrict__ x, const int *__restrict__ skip)
+{
+  if(skip && *skip) return;
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += d[i];
+}
+
 // x = Minv b for the coarsest level (dense, row-major), one warp per row.
 template <typename V, int NV>
 __global__ void k_dense(int64_t n, const V *__restrict__ M, const V *__restrict__ b, V *__restrict__ x,
@@ -324,17 +379,33 @@ int AMGDevice::upload(const AMGHierarchy &H, const AMGParams &p, int fp32, cudaS
   return FE_OK;
 }
 
+// needResidual: r = D^-1 (b - A x) must hold for the final x (the
+// pre-smoothing, whose residual is restricted); otherwise the last step only
+// moves x.
 template <typename V, int NV>
 static void chebyshev(int lanes, int64_t n, const int32_t *ia, const int32_t *ja, const V *a, const V *dinv,
                       const V *b, V *x, V *r, V *d0, V *d1, double lmax, const AMGParams &p, bool zeroStart,
-                      cudaStream_t s, const int *skip)
+                      bool needResidual, cudaStream_t s, const int *skip)
 {
   // Chebyshev iteration on D^-1 A over [low, high] * lmax (Saad, Alg. 12.1).
   const double lo = p.chebyLow * lmax, hi = p.chebyHigh * lmax;
   const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
   double rho = 1.0 / sigma;
   const int g = grid(n * lanes);
-  if(zeroStart) {
+  int k0 = 0;
+  V *d = d0, *dn = d1;
+  if(zeroStart && (needResidual || p.chebyDegree > 1)) {
+    // start + first step in one pass
+    const double rhoN = 1.0 / (2.0 * sigma - rho);
+    const V c1 = (V)(rhoN * rho), c2 = (V)(2.0 * rhoN / delta);
+    const V it = (V)(1.0 / theta);
+    if(lanes == 16) (k_cheb_first<V, 16, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, dn, r, x, it, c1, c2, skip), ::feng::count_launch());
+    else if(lanes == 8) (k_cheb_first<V, 8, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, dn, r, x, it, c1, c2, skip), ::feng::count_launch());
+    else (k_cheb_first<V, 4, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, dn, r, x, it, c1, c2, skip), ::feng::count_launch());
+    rho = rhoN;
+    std::swap(d, dn);
+    k0 = 1;
+  } else if(zeroStart) {
     (k_cheb_start<V, NV><<<grid(n * NV), 256, 0, s>>>(n, dinv, b, r, d0, x, (V)(1.0 / theta), skip),
      ::feng::count_launch());
   } else {
@@ -342,8 +413,11 @@ static void chebyshev(int lanes, int64_t n, const int32_t *ia, const int32_t *ja
     else if(lanes == 8) (k_cheb_restart<V, 8, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip), ::feng::count_launch());
     else (k_cheb_restart<V, 4, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip), ::feng::count_launch());
   }
-  V *d = d0, *dn = d1;
-  for(int k = 0; k < p.chebyDegree; ++k) {
+  for(int k = k0; k < p.chebyDegree; ++k) {
+    if(!needResidual && k == p.chebyDegree - 1) {
+      (k_cheb_last<V><<<grid(n * NV), 256, 0, s>>>(n * NV, d, x, skip), ::feng::count_launch());
+      break;
+    }
     const double rhoN = 1.0 / (2.0 * sigma - rho);
     const V c1 = (V)(rhoN * rho), c2 = (V)(2.0 * rhoN / delta);
     if(lanes == 16) (k_cheb_step<V, 16, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2, skip), ::feng::count_launch());
@@ -365,7 +439,7 @@ void AMGDevice::vcycle_t(int l, const V *b, V *x)
   Lev &C = lv_[l + 1];
   const V *A = (const V *)L.Aa;
   chebyshev<V, NV>(L.lanesA, L.n, L.Aia, L.Aja, A, (const V *)L.dinv, b, x, (V *)L.r, (V *)L.d0, (V *)L.d1,
-                   L.lmax, p_, true, s_, skip_);
+                   L.lmax, p_, true, true, s_, skip_);
   // Chebyshev keeps r = D^-1 (b - A x): restrict the residual D r directly
   // (no extra pass over A).
   csr<V, 3, NV>(L.lanesR, C.n, L.Ria, L.Rja, (const V *)L.Ra, (const V *)L.r, (const V *)L.diag, (V *)C.b, s_,
@@ -373,7 +447,7 @@ void AMGDevice::vcycle_t(int l, const V *b, V *x)
   vcycle_t<V, NV>(l + 1, (const V *)C.b, (V *)C.x);
   csr<V, 2, NV>(L.lanesP, L.n, L.Pia, L.Pja, (const V *)L.Pa, (const V *)C.x, nullptr, x, s_, skip_);
   chebyshev<V, NV>(L.lanesA, L.n, L.Aia, L.Aja, A, (const V *)L.dinv, b, x, (V *)L.r, (V *)L.d0, (V *)L.d1,
-                   L.lmax, p_, false, s_, skip_);
+                   L.lmax, p_, false, false, s_, skip_);
 }
 
 void AMGDevice::vcycle64(const double *b, double *x) { vcycle_t<double, 1>(0, b, x); }
