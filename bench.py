@@ -222,10 +222,15 @@ def algorithmic_bytes(sys_, nvert, precision):
     mat = sys_.nnz * sA + sys_.nElm * nl * 4 + nvert * 2 * 8 + sys_.nDofs * 8
     sx = 4 if precision == "mixed" else 8
     spmv = sys_.nnz * (sA + 4) + (sys_.nInc + 1) * 4 + sys_.nInc * (sx + 8)
-    sm = C.c_int64()
     from feng_gb300._lib import check
-    check(sys_.lib.fe_cuda_smoother_bytes(sys_._h, C.byref(sm)))
-    return {"residual_assembly": res, "matrix_assembly": mat, "spmv": spmv, "smoother_step": sm.value}
+    out = {"residual_assembly": res, "matrix_assembly": mat, "spmv": spmv}
+    for which, name in ((4, "smoother_step"), (5, "gs_dots"), (6, "gs_update")):
+        if which > 4 and precision != "mixed":
+            continue
+        b = C.c_int64()
+        check(sys_.lib.fe_cuda_phase_bytes(sys_._h, which, C.byref(b)))
+        out[name] = b.value
+    return out
 
 
 def ncu_traffic(kernel):
@@ -238,11 +243,16 @@ def ncu_traffic(kernel):
     return None if d is None else d.get("dram_bytes_per_launch")
 
 
-def phase_bench(sys_, reps=20):
+def phase_bench(sys_, mixed, reps=20):
+    """Device-timed phases (L2 flushed before each run): assembly, SpMV, one
+    preconditioner application, the finest-level pre-smoothing pass, and for
+    the mixed path the two Gram-Schmidt passes at restart/2 = 25 columns
+    (the mean column count of a 50-step cycle)."""
     from feng_gb300._lib import check
     out = {}
-    for which, name in ((0, "residual_assembly"), (1, "matrix_assembly"), (2, "spmv"), (3, "preconditioner"),
-                        (4, "smoother_step")):
+    phases = [(0, "residual_assembly"), (1, "matrix_assembly"), (2, "spmv"), (3, "preconditioner"),
+              (4, "smoother_step")] + ([(5, "gs_dots"), (6, "gs_update")] if mixed else [])
+    for which, name in phases:
         ms = C.c_double()
         check(sys_.lib.fe_cuda_bench_phase(sys_._h, which, reps, 256 << 20, C.byref(ms)))
         out[name] = ms.value
@@ -392,7 +402,7 @@ def main():
     peak, peak_kind = measured_peaks()
     kern = {}
     for name, sys_, prec in (("fp64", plain, "fp64"), ("mixed", mixed, "mixed")):
-        ph = phase_bench(sys_)
+        ph = phase_bench(sys_, prec == "mixed")
         by = algorithmic_bytes(sys_, nvert, prec)
         kern[name] = {k: {"ms": ph[k], "bytes": by.get(k),
                           "gbs": (by[k] / (ph[k] / 1e3) / 1e9) if k in by else None} for k in ph}
@@ -400,20 +410,27 @@ def main():
     ph = ph_mixed
     shares = {"assembly": ph["residual_ms"] + ph["matrix_ms"], "krylov_solve": ph["solve_ms"],
               "preconditioner_build": ph["factor_ms"]}
-    # The dominant kernel of the Newton step (the Krylov solve is ~97% of it):
-    # the finest-level step of the velocity multigrid smoother.
-    top = kern["mixed"]["smoother_step"]
-    roof = {"kernel": "k_cheb_step<float,4,2> (finest AMG level, both velocity components)", "bound": "hbm",
-            "achieved": top["gbs"], "peak": peak, "unit": "GB/s", "frac": top["gbs"] / peak,
-            "peak_source": peak_kind, "bytes_per_launch": top["bytes"], "ms_per_launch": top["ms"],
-            "traffic": ncu_traffic("k_cheb_step<float,4,2>")}
+    # The dominant kernel of the Newton step (the Krylov solve is ~97% of it,
+    # and its largest kernel by time is the Gram-Schmidt dot pass): k_gs_dots
+    # at the mean column count of a restart cycle.
+    def roofline(key, kernel, traffic_key):
+        k = kern["mixed"][key]
+        return {"kernel": kernel, "bound": "hbm", "achieved": k["gbs"], "peak": peak, "unit": "GB/s",
+                "frac": k["gbs"] / peak, "peak_source": peak_kind, "bytes_per_launch": k["bytes"],
+                "ms_per_launch": k["ms"], "traffic": ncu_traffic(traffic_key)}
+    roof = roofline("gs_dots", "k_gs_dots (FP32 Gram-Schmidt dot pass, 25 basis vectors)", "k_gs_dots@25")
+    roof_gsu = roofline("gs_update", "k_gs32<32,2> (FP32 Gram-Schmidt update + norm, 25 basis vectors)",
+                        "k_gs32<32,2>@25")
+    roof_sm = roofline("smoother_step", "k_cheb_first<float,4,2> (finest AMG level, both velocity components)",
+                       "k_cheb_first<float,4,2>")
     asm = kern["mixed"]["matrix_assembly"]
     roof_asm = {"kernel": "k_matrix_th<float> (Jacobian assembly, all colors)", "bound": "hbm",
                 "achieved": asm["gbs"], "peak": peak, "unit": "GB/s", "frac": asm["gbs"] / peak,
                 "peak_source": peak_kind, "traffic": ncu_traffic("k_matrix_th<float>")}
     sp = kern["mixed"]["spmv"]
     roof_spmv = {"kernel": "k_spmv<float> (FGMRES inner SpMV)", "bound": "hbm", "achieved": sp["gbs"],
-                 "peak": peak, "unit": "GB/s", "frac": sp["gbs"] / peak, "peak_source": peak_kind}
+                 "peak": peak, "unit": "GB/s", "frac": sp["gbs"] / peak, "peak_source": peak_kind,
+                 "traffic": ncu_traffic("k_spmv<float,float,float,float,8,0>")}
 
     nits_p = round(statistics.mean(s["iterations"] for s in st_plain), 2)
     kits_p = round(statistics.mean(s["krylov_iterations"] for s in st_plain), 1)
@@ -433,7 +450,8 @@ def main():
         "speedup_mixed_vs_fp64": plain_s / value,
         "phase_share_ms": shares,
         "kernels": kern,
-        "roofline": roof, "roofline_assembly": roof_asm, "roofline_spmv": roof_spmv,
+        "roofline": roof, "roofline_gs_update": roof_gsu, "roofline_smoother": roof_sm,
+        "roofline_assembly": roof_asm, "roofline_spmv": roof_spmv,
         "e2e": {"value": e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": l_mixed,
         "gpu_launches_plain_fp64": l_plain,

@@ -88,6 +88,7 @@ SIGNATURES = {
                                           C.c_double, C.c_uint64, C.POINTER(P)]),
     "fe_mesh_read_msh": (C.c_int, [C.c_char_p, C.POINTER(P)]),
     "fe_mesh_write_msh": (C.c_int, [P, C.c_char_p]),
+    "fe_mesh_from_arrays": (C.c_int, [C.c_int64, P, P, C.c_int64, P, C.c_int64, P, C.c_int32, C.POINTER(P)]),
     "fe_mesh_sizes": (C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                 C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "fe_mesh_arrays": (C.c_int, [P, P, P, P, P, P, P]),
@@ -116,6 +117,8 @@ SIGNATURES = {
     "fe_cuda_set_solution": (C.c_int, [P, P, P]),
     "fe_cuda_get_solution": (C.c_int, [P, P]),
     "fe_cuda_set_time": (C.c_int, [P, C.c_double, C.c_double]),
+    "fe_cuda_norm_points": (C.c_int, [P, P, P, P]),
+    "fe_cuda_l2_error": (C.c_int, [P, C.c_int, P, P]),
     "fe_cuda_set_bdf": (C.c_int, [P, C.c_int, P, P, P]),
     "fe_cuda_compute_soldot": (C.c_int, [P]),
     "fe_cuda_set_to_zero": (C.c_int, [P]),
@@ -139,6 +142,7 @@ SIGNATURES = {
     "fe_cuda_bench_phase": (C.c_int, [P, C.c_int, C.c_int, C.c_int64, C.POINTER(C.c_double)]),
     "fe_cuda_launch_count": (C.c_int, [C.POINTER(C.c_int64)]),
     "fe_cuda_smoother_bytes": (C.c_int, [P, C.POINTER(C.c_int64)]),
+    "fe_cuda_phase_bytes": (C.c_int, [P, C.c_int, C.POINTER(C.c_int64)]),
     "fe_cuda_save_solution": (C.c_int, [P]),
     "fe_cuda_restore_solution": (C.c_int, [P]),
     "fe_cuda_event_record": (C.c_int, [P, C.c_int]),

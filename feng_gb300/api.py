@@ -63,6 +63,18 @@ class Mesh2DP1:
         check(lib.fe_mesh_read_msh(str(path).encode(), C.byref(h)))
         return cls(h)
 
+    @classmethod
+    def from_arrays(cls, x, y, tri, bnd, point=-1):
+        """Mesh from vertex coordinates, counter-clockwise triangles ("Domaine"),
+        boundary lines ("Bord") and the "PointPression" vertex (-1: none)."""
+        lib = _lib.load()
+        x = np.ascontiguousarray(x, np.float64); y = np.ascontiguousarray(y, np.float64)
+        tri = np.ascontiguousarray(tri, np.int32).reshape(-1); bnd = np.ascontiguousarray(bnd, np.int32).reshape(-1)
+        h = C.c_void_p()
+        check(lib.fe_mesh_from_arrays(len(x), ptr(x), ptr(y), len(tri) // 3, ptr(tri), len(bnd) // 2, ptr(bnd),
+                                      int(point), C.byref(h)))
+        return cls(h)
+
     def write_msh(self, path: str):
         check(self._lib.fe_mesh_write_msh(self._h, str(path).encode()))
 
@@ -507,6 +519,72 @@ class feSolution:
     def pull(self):
         self.u = self.system.getSolution()
         return self.u
+
+
+# ---- error norms (src/feNorm.h, src/feNorm.cpp) ---------------------------------
+
+L2_ERROR, VECTOR_L2_ERROR = "L2_ERROR", "VECTOR_L2_ERROR"
+
+
+class feNorm:
+    """L2_ERROR / VECTOR_L2_ERROR of feNorm (src/feNorm.cpp:152-163, 323-391,
+    1399-1443): the exact solution is evaluated on the host at the nodes of
+    the system's quadrature rule on every element (once per compute, as the
+    reference's feFunction calls), the error integral runs on the device from
+    the device solution."""
+
+    def __init__(self, normType, spaces, sol: feSolution, scalarSolution=None, vectorSolution=None):
+        if normType not in (L2_ERROR, VECTOR_L2_ERROR):
+            raise ValueError(f"unsupported norm {normType!r}")
+        space = spaces[0]
+        vector = space.element == VECTOR_LAGRANGE
+        if (normType == VECTOR_L2_ERROR) != vector:
+            raise ValueError("VECTOR_L2_ERROR needs a vector space, L2_ERROR a scalar one")
+        fct = vectorSolution if vector else scalarSolution
+        if fct is None:
+            raise ValueError("the error norm needs the exact solution")
+        self.system = sol.system
+        taylor_hood = self.system.elem_type == ELEM_TAYLOR_HOOD
+        if taylor_hood:
+            if vector and space.degree == 2:
+                self.field = 0
+            elif not vector and space.degree == 1:
+                self.field = 1
+            else:
+                raise ValueError("Taylor-Hood systems hold a P2 vector field and a P1 scalar field")
+        elif not vector and space.degree == 2:
+            self.field = 0
+        else:
+            raise ValueError("scalar P2 systems hold one P2 scalar field")
+        self.ncomp = 2 if vector else 1
+        self.fct = fct
+        self.sol = sol
+
+    def points(self):
+        """Quadrature nodes (x, y) of every element, shape (nElm, nq)."""
+        lib, h = self.system.lib, self.system._h
+        nq = C.c_int()
+        check(lib.fe_cuda_norm_points(h, C.byref(nq), None, None))
+        x = np.empty(self.system.nElm * nq.value)
+        y = np.empty_like(x)
+        check(lib.fe_cuda_norm_points(h, C.byref(nq), ptr(x), ptr(y)))
+        return x.reshape(-1, nq.value), y.reshape(-1, nq.value)
+
+    def compute(self) -> float:
+        x, y = self.points()
+        vals = self.fct(x.ravel(), y.ravel())
+        ex = np.empty((x.size, self.ncomp))
+        for c in range(self.ncomp):
+            ex[:, c] = np.broadcast_to(vals[c], x.size)
+        ex = np.ascontiguousarray(ex)
+        err = C.c_double()
+        check(self.system.lib.fe_cuda_l2_error(self.system._h, self.field, ptr(ex), C.byref(err)))
+        return err.value
+
+
+def createNorm(normType, spaces, sol, scalarSolution=None, vectorSolution=None):
+    """createNorm (src/feNorm.cpp:7-...) for the L2 error norms."""
+    return feNorm(normType, spaces, sol, scalarSolution, vectorSolution)
 
 
 @dataclass

@@ -88,7 +88,7 @@ __device__ __forceinline__ void row_dot(int32_t beg, int32_t end, int sub, const
 }
 
 // y = A x (MODE 0), y = b - A x (MODE 1), y += A x (MODE 2),
-// y = A (b .* x) with b a per-row scale of x (MODE 3)
+// y = A (b .* x) with b a per-row scale of x (MODE 3), y = b + A x (MODE 4)
 template <typename V, int LANES, int MODE, int NV>
 __global__ void __launch_bounds__(256) k_csr(int64_t n, const int32_t *__restrict__ ia,
                                              const int32_t *__restrict__ ja, const V *__restrict__ a,
@@ -124,6 +124,7 @@ __global__ void __launch_bounds__(256) k_csr(int64_t n, const int32_t *__restric
       const int64_t o = row * NV + c;
       if(MODE == 0 || MODE == 3) y[o] = acc[c];
       else if(MODE == 1) y[o] = b[o] - acc[c];
+      else if(MODE == 4) y[o] = b[o] + acc[c];
       else y[o] += acc[c];
     }
   }
@@ -253,6 +254,33 @@ __global__ void __launch_bounds__(256) k_cheb_first(int64_t n, const int32_t *__
     const V ri = r0 - dv * ac * inv_theta;
     r[o] = ri;
     dn[o] = c1 * di + c2 * ri;
+  }
+}
+
+// Degree-1 post-smoothing from the prolongated y = x + P xc:
+// x = y + D^-1 (b - A y) / theta (x and y distinct).
+template <typename V, int LANES, int NV>
+__global__ void __launch_bounds__(256) k_cheb_post(int64_t n, const int32_t *__restrict__ ia,
+                                                   const int32_t *__restrict__ ja, const V *__restrict__ a,
+                                                   const V *__restrict__ dinv, const V *__restrict__ b,
+                                                   const V *__restrict__ y, V *__restrict__ x, V inv_theta,
+                                                   const int *__restrict__ skip)
+{
+  if(skip && *skip) return;
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
+  const int sub = threadIdx.x % LANES;
+  const bool live = row < n;
+  const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
+  V acc[NV];
+  row_dot<V, LANES, NV>(beg, end, sub, ja, a, y, acc);
+  if(live && sub < NV) {
+    V ac = acc[0];
+#pragma unroll
+    for(int c = 1; c < NV; ++c)
+      if(sub == c) ac = acc[c];
+    const int64_t o = row * NV + sub;
+    const V ri = dinv[row] * (b[o] - ac);
+    x[o] = y[o] + ri * inv_theta;
   }
 }
 
@@ -445,6 +473,20 @@ void AMGDevice::vcycle_t(int l, const V *b, V *x)
   csr<V, 3, NV>(L.lanesR, C.n, L.Ria, L.Rja, (const V *)L.Ra, (const V *)L.r, (const V *)L.diag, (V *)C.b, s_,
                 skip_);
   vcycle_t<V, NV>(l + 1, (const V *)C.b, (V *)C.x);
+  if(p_.chebyDegree == 1) {
+    // y = x + P xc into this level's free scratch, then one pass
+    // x = y + D^-1 (b - A y) / theta (the restart and the step in one)
+    V *y = (V *)L.d1;
+    csr<V, 4, NV>(L.lanesP, L.n, L.Pia, L.Pja, (const V *)L.Pa, (const V *)C.x, x, y, s_, skip_);
+    const double lo = p_.chebyLow * L.lmax, hi = p_.chebyHigh * L.lmax, theta = 0.5 * (hi + lo);
+    const V it = (V)(1.0 / theta);
+    const int g = grid(L.n * L.lanesA);
+    const V *dinv = (const V *)L.dinv;
+    if(L.lanesA == 16) (k_cheb_post<V, 16, NV><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_), ::feng::count_launch());
+    else if(L.lanesA == 8) (k_cheb_post<V, 8, NV><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_), ::feng::count_launch());
+    else (k_cheb_post<V, 4, NV><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_), ::feng::count_launch());
+    return;
+  }
   csr<V, 2, NV>(L.lanesP, L.n, L.Pia, L.Pja, (const V *)L.Pa, (const V *)C.x, nullptr, x, s_, skip_);
   chebyshev<V, NV>(L.lanesA, L.n, L.Aia, L.Aja, A, (const V *)L.dinv, b, x, (V *)L.r, (V *)L.d0, (V *)L.d1,
                    L.lmax, p_, false, false, s_, skip_);
@@ -457,16 +499,19 @@ void AMGDevice::vcycle2_32(const float *b, float *x) { vcycle_t<float, 2>(0, b, 
 
 void AMGDevice::fineStep2()
 {
+  // The finest-level pre-smoothing pass of a V-cycle (k_cheb_first) on the
+  // level's scratch vectors: b = d0 (finite values of earlier cycles), x, r,
+  // dn = d1 written.
   const Lev &L = lv_[0];
   const int g = grid(L.n * L.lanesA);
   auto go = [&](auto tag) {
     using V = decltype(tag);
-    const V *a = (const V *)L.Aa, *dinv = (const V *)L.dinv;
-    V *d = (V *)L.d0, *dn = (V *)L.d1, *r = (V *)L.r, *x = (V *)L.x;
-    const V c1 = (V)0.5, c2 = (V)0.5;
-    if(L.lanesA == 16) (k_cheb_step<V, 16, 2><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, a, dinv, d, dn, r, x, c1, c2, skip_), ::feng::count_launch());
-    else if(L.lanesA == 8) (k_cheb_step<V, 8, 2><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, a, dinv, d, dn, r, x, c1, c2, skip_), ::feng::count_launch());
-    else (k_cheb_step<V, 4, 2><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, a, dinv, d, dn, r, x, c1, c2, skip_), ::feng::count_launch());
+    const V *a = (const V *)L.Aa, *dinv = (const V *)L.dinv, *b = (const V *)L.d0;
+    V *dn = (V *)L.d1, *r = (V *)L.r, *x = (V *)L.x;
+    const V it = (V)0.5, c1 = (V)0.5, c2 = (V)0.5;
+    if(L.lanesA == 16) (k_cheb_first<V, 16, 2><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, a, dinv, b, dn, r, x, it, c1, c2, skip_), ::feng::count_launch());
+    else if(L.lanesA == 8) (k_cheb_first<V, 8, 2><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, a, dinv, b, dn, r, x, it, c1, c2, skip_), ::feng::count_launch());
+    else (k_cheb_first<V, 4, 2><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, a, dinv, b, dn, r, x, it, c1, c2, skip_), ::feng::count_launch());
   };
   if(fp32_) go(float());
   else go(double());
@@ -477,9 +522,9 @@ int64_t AMGDevice::fineStep2Bytes() const
   if(lv_.empty()) return 0;
   const Lev &L = lv_[0];
   const int64_t vs = fp32_ ? 4 : 8;
-  // values + columns, row pointers, dinv, and per component: d read, x
-  // read+write, r read+write, dn write
-  return nnz0_ * (vs + 4) + (L.n + 1) * 4 + L.n * vs + 2 * L.n * vs * 6;
+  // values + columns, row pointers, dinv, and per component: b read, x, r,
+  // dn written
+  return nnz0_ * (vs + 4) + (L.n + 1) * 4 + L.n * vs + 2 * L.n * vs * 4;
 }
 
 void AMGDevice::spmv64(const double *x, double *y)

@@ -65,8 +65,9 @@ class AMGDevice {
   // y = A x with the finest operator.
   void spmv64(const double *x, double *y);
   void spmv32(const float *x, float *y);
-  // One Chebyshev step of the finest level on two interleaved components
-  // (the level's own work vectors): the dominant kernel of the V-cycle.
+  // The finest-level pre-smoothing pass (zero start + first Chebyshev step
+  // in one kernel) on two interleaved components, on the level's own work
+  // vectors: one of the two finest-level kernels of every V-cycle.
   void fineStep2();
   // Algorithmic bytes of fineStep2: the level operator once (values,
   // columns, row pointers) and every vector entry it reads or writes once.

@@ -161,6 +161,32 @@ int fe_mesh_read_msh(const char *path, fe_mesh **out)
   GUARD_END
 }
 
+int fe_mesh_from_arrays(int64_t nv, const double *x, const double *y, int64_t nt, const int32_t *tri,
+                        int64_t nb, const int32_t *bnd, int32_t point, fe_mesh **out)
+{
+  GUARD_BEGIN
+  if(!out || !x || !y || !tri || nv <= 0 || nt <= 0 || nb < 0 || (nb > 0 && !bnd)) {
+    set_error("null or empty argument");
+    return FE_INVALID_ARG;
+  }
+  for(int64_t i = 0; i < 3 * nt; ++i)
+    if(tri[i] < 0 || tri[i] >= nv) { set_error("triangle vertex %d out of range", tri[i]); return FE_INVALID_ARG; }
+  for(int64_t i = 0; i < 2 * nb; ++i)
+    if(bnd[i] < 0 || bnd[i] >= nv) { set_error("boundary vertex %d out of range", bnd[i]); return FE_INVALID_ARG; }
+  if(point < -1 || point >= nv) { set_error("point vertex %d out of range", point); return FE_INVALID_ARG; }
+  auto *m = new fe_mesh();
+  m->m.x.assign(x, x + nv);
+  m->m.y.assign(y, y + nv);
+  m->m.tri.assign(tri, tri + 3 * nt);
+  m->m.bnd.assign(bnd, bnd + 2 * nb);
+  m->m.point = point;
+  int s = m->m.build_topology();
+  if(s) { delete m; return s; }
+  *out = m;
+  return FE_OK;
+  GUARD_END
+}
+
 int fe_mesh_write_msh(const fe_mesh *m, const char *path)
 {
   GUARD_BEGIN
@@ -507,6 +533,18 @@ int fe_cuda_get_solution(const fe_cuda_system *s, double *u)
   return s->sys.getSolution(u);
 }
 
+int fe_cuda_norm_points(fe_cuda_system *s, int *nq, double *x, double *y)
+{
+  if(!s || !nq) { set_error("null argument"); return FE_INVALID_ARG; }
+  return s->sys.normPoints(nq, x, y);
+}
+
+int fe_cuda_l2_error(fe_cuda_system *s, int field, const double *exact, double *error)
+{
+  if(!s || !exact || !error) { set_error("null argument"); return FE_INVALID_ARG; }
+  return s->sys.l2Error(field, exact, error);
+}
+
 int fe_cuda_set_time(fe_cuda_system *s, double t, double c0)
 {
   if(!s) { set_error("null system"); return FE_INVALID_ARG; }
@@ -640,6 +678,23 @@ int fe_cuda_smoother_bytes(fe_cuda_system *s, int64_t *bytes)
   if(r != FE_OK) return r;
   if(cudaStreamSynchronize(s->sys.stream()) != cudaSuccess) {
     set_error("fe_cuda_smoother_bytes: device error");
+    return FE_CUDA_DEVICE_FAIL;
+  }
+  return FE_OK;
+  GUARD_END
+}
+
+int fe_cuda_phase_bytes(fe_cuda_system *s, int which, int64_t *bytes)
+{
+  GUARD_BEGIN
+  if(!s || !bytes) { set_error("null argument"); return FE_INVALID_ARG; }
+  if(which == 4) return fe_cuda_smoother_bytes(s, bytes);
+  if(which != 5 && which != 6) { set_error("no byte count for phase %d", which); return FE_INVALID_ARG; }
+  Krylov &k = s->sys.krylov();
+  const int r = k.gsStep(which == 5 ? 0 : 2, std::max(1, k.opt.restart / 2), bytes);
+  if(r != FE_OK) return r;
+  if(cudaStreamSynchronize(s->sys.stream()) != cudaSuccess) {
+    set_error("fe_cuda_phase_bytes: device error");
     return FE_CUDA_DEVICE_FAIL;
   }
   return FE_OK;

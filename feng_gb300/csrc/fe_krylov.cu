@@ -820,7 +820,7 @@ struct Ws {
 #define Ws_INIT(k) {(RedState *)(k)->red_state_, (GmresState *)(k)->gmres_, (GmresState *)(k)->h_gmres_, (CGState *)(k)->cg_, (CGState *)(k)->h_cg_}
 Krylov::~Krylov()
 {
-  cudaFree(V_); cudaFree(Z_); cudaFree(Z32_); cudaFree(V32_); cudaFree(v32_); cudaFree(w32_);
+  cudaFree(V_); cudaFree(Z_); cudaFree(Z32_); cudaFree(V32_); cudaFree(v32_); cudaFree(w32_); cudaFree(zeroFlag_);
   cudaFree(w_); cudaFree(r_); cudaFree(t_); cudaFree(p_); cudaFree(q_);
   cudaFree(diag_); cudaFree(diag32_); cudaFree(red_); cudaFree(dsum_);
   cudaFreeHost(hred_);
@@ -1110,6 +1110,23 @@ double Krylov::norminf(const double *x)
   cudaMemcpyAsync(hred_, dsum_, sizeof(double), cudaMemcpyDeviceToHost, s_);
   cudaStreamSynchronize(s_);
   return hred_[0];
+}
+
+int Krylov::gsStep(int mode, int ncols, int64_t *bytes)
+{
+  if(!V32_ || (mode != 0 && mode != 2) || ncols < 1 || ncols > opt.restart) {
+    set_error("no mixed FP32 basis, or an invalid Gram-Schmidt request");
+    return FE_INVALID_ARG;
+  }
+  if(!zeroFlag_) {
+    CK(cudaMalloc(&zeroFlag_, sizeof(int)));
+    CK(cudaMemsetAsync(zeroFlag_, 0, sizeof(int), s_));
+  }
+  Ws w = Ws_INIT(this);
+  if(mode == 0) gs32(0, ncols, nullptr, w.gs->hcur, w.gs->H, zeroFlag_, 0);
+  else gs32(2, ncols, w.gs->hcur, nullptr, w.gs->H + ncols, zeroFlag_, 0);
+  if(bytes) *bytes = (int64_t)(ncols + (mode == 0 ? 1 : 2)) * ld32_ * (int64_t)sizeof(float);
+  return FE_OK;
 }
 
 // One FP32 Gram-Schmidt pass (k_gs32) over the first ncols basis vectors.

@@ -125,6 +125,7 @@ class Krylov {
   double *Z_ = nullptr;   // m x n      preconditioned directions (FP64 path)
   float *Z32_ = nullptr;  // m x n      preconditioned directions (mixed path)
   float *V32_ = nullptr;  // (m+1) x n  Krylov basis of the mixed path, FP32
+  int *zeroFlag_ = nullptr;  // a device 0 ("not done") for gsStep
   int gsParts_ = 0;       // blocks of the FP32 Gram-Schmidt passes
   int64_t ld32_ = 0;      // leading dimension of V32_ / Z32_ (multiple of 64)
   // pass: 0 first pass (the update + norm decides on reorthogonalisation),
@@ -174,6 +175,10 @@ class Krylov {
   // The multigrid's finest-level smoother step alone (benchmarking); bytes:
   // its algorithmic bytes, 0 when there is no multigrid.
   int smootherStep(int64_t *bytes);
+  // One pass of the mixed FGMRES Gram-Schmidt on the current FP32 basis with
+  // ncols columns (benchmark phases): mode 0 the dot pass (k_gs_dots), mode
+  // 2 the update + norm pass (k_gs32<., 2>).  bytes: algorithmic bytes.
+  int gsStep(int mode, int ncols, int64_t *bytes);
   int factor_mg(const double *values64, const float *values32);
   template <typename V> void apply_mg(const V *vals, const V *r, V *z, const int *skip);
 };

@@ -51,6 +51,74 @@ __global__ void k_diagpos(int64_t n, const int32_t *__restrict__ ia, const int32
   }
 }
 
+// Nodes of the rule on every element: x = sum_j psi_j(r_k, s_k) x_j (P1
+// geometry), index e * nq + k in the system's element order.
+__global__ void k_norm_points(int64_t nElm, const double *__restrict__ xy, const RefTensors *__restrict__ T,
+                              double *__restrict__ px, double *__restrict__ py)
+{
+  const int nq = T->nq;
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nElm * nq;
+      i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = i / nq;
+    const int k = (int)(i - e * nq);
+    const double r = T->qr[k], s = T->qs[k], t = 1. - r - s;
+    px[i] = t * xy[0 * nElm + e] + r * xy[2 * nElm + e] + s * xy[4 * nElm + e];
+    py[i] = t * xy[1 * nElm + e] + r * xy[3 * nElm + e] + s * xy[5 * nElm + e];
+  }
+}
+
+// Squared L2 error of one field on every element:
+//   sum_k sum_c |ex - u_h|^2 |J| w_k
+// with u_h interpolated from the element's DOFs.  layout: 0 scalar P2
+// (local DOF a), 1 vector P2 of Taylor-Hood (local 2a + c), 2 P1 pressure
+// of Taylor-Hood (local 12 + j).
+__global__ void k_l2_err(int64_t nElm, int layout, const int32_t *__restrict__ adr, const double *__restrict__ geo,
+                         const RefTensors *__restrict__ T, const double *__restrict__ u,
+                         const double *__restrict__ ex, double *__restrict__ part)
+{
+  const int nq = T->nq;
+  const int ncomp = layout == 1 ? 2 : 1;
+  for(int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nElm; e += (int64_t)gridDim.x * blockDim.x) {
+    double ue[12];
+    const int nl = layout == 0 ? 6 : layout == 1 ? 12 : 3;
+    const int off = layout == 2 ? 12 : 0;
+    for(int i = 0; i < nl; ++i) ue[i] = u[adr[(int64_t)(off + i) * nElm + e]];
+    double sum = 0.;
+    for(int k = 0; k < nq; ++k) {
+      double c2 = 0.;
+      for(int c = 0; c < ncomp; ++c) {
+        double uh = 0.;
+        if(layout == 2) {
+          const double r = T->qr[k], s = T->qs[k];
+          uh = (1. - r - s) * ue[0] + r * ue[1] + s * ue[2];
+        } else {
+          for(int a = 0; a < 6; ++a) uh += T->phi[k][a] * ue[ncomp * a + c];
+        }
+        const double d = ex[(e * nq + k) * ncomp + c] - uh;
+        c2 += d * d;
+      }
+      sum += c2 * geo[4 * nElm + e] * T->qw[k];
+    }
+    part[e] = sum;
+  }
+}
+
+// One block: out = sum of v[0..n) in a fixed order (strided serial sums,
+// then a tree), so repeated calls give the same bits.
+__global__ void k_sum_fixed(int64_t n, const double *__restrict__ v, double *__restrict__ out)
+{
+  __shared__ double sh[1024];
+  double acc = 0.;
+  for(int64_t i = threadIdx.x; i < n; i += blockDim.x) acc += v[i];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for(int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if(threadIdx.x == 0) *out = sh[0];
+}
+
 int gridFor(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 4096)); }
 
 void p2_basis(double r, double s, double phi[6], double dr[6], double ds[6])
@@ -286,6 +354,7 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
   RefTensors hT;
   build_ref_tensors(t.quad, hT);
   exact5_ = hT.exact5;
+  nq_ = hT.nq;
   CK(cudaMalloc(&dT_, sizeof(RefTensors)));
   CK(cudaMemcpy(dT_, &hT, sizeof(RefTensors), cudaMemcpyHostToDevice));
 
@@ -465,6 +534,64 @@ int SystemCUDA::build_precond_info(const SystemTables &t, const RefTensors &T, H
     pi.sigma = fc_.hasSigma ? fc_.sigma : 1.0;
     pi.divu = fc_.hasDivu ? fc_.divu : 1.0;
   }
+  return FE_OK;
+}
+
+int SystemCUDA::normPoints(int *nq, double *hostX, double *hostY)
+{
+  if(!nq) {
+    set_error("null argument");
+    return FE_INVALID_ARG;
+  }
+  *nq = nq_;
+  if(!hostX && !hostY) return FE_OK;
+  const int64_t m = dm_.nElm * nq_;
+  double *p = nullptr;
+  CK(cudaMalloc(&p, sizeof(double) * 2 * std::max<int64_t>(m, 1)));
+  (k_norm_points<<<gridFor(m), 256, 0, s_>>>(dm_.nElm, dm_.xy, dT_, p, p + m), ::feng::count_launch());
+  cudaError_t e = cudaGetLastError();
+  if(e == cudaSuccess && hostX) e = cudaMemcpyAsync(hostX, p, sizeof(double) * m, cudaMemcpyDeviceToHost, s_);
+  if(e == cudaSuccess && hostY) e = cudaMemcpyAsync(hostY, p + m, sizeof(double) * m, cudaMemcpyDeviceToHost, s_);
+  if(e == cudaSuccess) e = cudaStreamSynchronize(s_);
+  cudaFree(p);
+  CK(e);
+  return FE_OK;
+}
+
+int SystemCUDA::l2Error(int field, const double *hostExact, double *err)
+{
+  if(!hostExact || !err) {
+    set_error("null argument");
+    return FE_INVALID_ARG;
+  }
+  int layout;
+  if(elemType_ == 1 && field == 0) layout = 0;
+  else if(elemType_ == 2 && field == 0) layout = 1;
+  else if(elemType_ == 2 && field == 1) layout = 2;
+  else {
+    set_error("field %d does not exist in this system", field);
+    return FE_INVALID_ARG;
+  }
+  const int ncomp = layout == 1 ? 2 : 1;
+  const int64_t m = dm_.nElm * nq_ * ncomp;
+  double *ex = nullptr;
+  CK(cudaMalloc(&ex, sizeof(double) * (std::max<int64_t>(m, 1) + dm_.nElm + 1)));
+  double *part = ex + std::max<int64_t>(m, 1), *out = part + dm_.nElm;
+  cudaError_t e = cudaMemcpyAsync(ex, hostExact, sizeof(double) * m, cudaMemcpyHostToDevice, s_);
+  if(e == cudaSuccess) {
+    (k_l2_err<<<gridFor(dm_.nElm), 256, 0, s_>>>(dm_.nElm, layout, dm_.adr, dm_.geo, dT_, u_, ex, part),
+     ::feng::count_launch());
+    (k_sum_fixed<<<1, 1024, 0, s_>>>(dm_.nElm, part, out), ::feng::count_launch());
+    e = cudaGetLastError();
+  }
+  double sum = 0.;
+  if(e == cudaSuccess) e = cudaMemcpyAsync(&sum, out, sizeof(double), cudaMemcpyDeviceToHost, s_);
+  if(e == cudaSuccess) e = cudaStreamSynchronize(s_);
+  cudaFree(ex);
+  CK(e);
+  // Negative weights can leave a tiny negative sum (src/feNorm.cpp:383-387).
+  if(sum < 0 && std::fabs(sum) < 1e-14) sum = std::fabs(sum);
+  *err = std::sqrt(sum);
   return FE_OK;
 }
 
@@ -812,7 +939,7 @@ int SystemCUDA::computeSolDot()
 
 int SystemCUDA::benchPhase(int which, int reps, size_t flushBytes, double *avgMs)
 {
-  if(which < 0 || which > 4 || reps < 1) {
+  if(which < 0 || which > 6 || reps < 1) {
     set_error("invalid benchmark request");
     return FE_INVALID_ARG;
   }
@@ -854,6 +981,10 @@ int SystemCUDA::benchPhase(int which, int reps, size_t flushBytes, double *avgMs
         break;
       case 4:
         status = kry_.smootherStep(nullptr);
+        break;
+      case 5:
+      case 6:
+        status = kry_.gsStep(which == 5 ? 0 : 2, std::max(1, kry_.opt.restart / 2), nullptr);
         break;
     }
     CK(cudaEventRecord(ev1_, s_));

@@ -111,6 +111,15 @@ class SystemCUDA {
   int getRHS(double *hostRhs) const;
   int getDu(double *hostDu) const;
   int validateColoring() const;
+  // Error norms of feNorm (src/feNorm.cpp:323-391, 1399-1443) on the
+  // system's quadrature rule: normPoints gives the rule's nodes on every
+  // element (system element order, nq per element) where the caller
+  // evaluates its exact solution; l2Error returns sqrt(sum_e sum_k
+  // sum_c |u_ex - u_h|^2 |J| w_k) for field 0 (the P2 field, 1 or 2
+  // components) or field 1 (the P1 pressure of Taylor-Hood), exact values
+  // host-side [nElm][nq][ncomp].
+  int normPoints(int *nq, double *hostX, double *hostY);
+  int l2Error(int field, const double *hostExact, double *err);
   // Times `reps` runs of one phase with CUDA events on the system stream, each
   // preceded by an L2 flush (a write of flushBytes): which = 0 residual
   // assembly, 1 matrix assembly, 2 SpMV with the system matrix, 3 one
@@ -148,6 +157,7 @@ class SystemCUDA {
   DeviceMesh dm_;
   FormCoeffs fc_{};
   RefTensors *dT_ = nullptr;
+  int nq_ = 0;  // nodes of the system's quadrature rule
   DeviceCSR csr_;
   double *vals64_ = nullptr;
   float *vals32_ = nullptr;

@@ -153,6 +153,13 @@ int fe_mesh_generate_square(int n, double x0, double x1, double y0, double y1, d
                             uint64_t seed, fe_mesh **out);
 int fe_mesh_read_msh(const char *path, fe_mesh **out);
 int fe_mesh_write_msh(const fe_mesh *m, const char *path);
+/* A mesh from caller arrays (0-based): vertices x, y; counter-clockwise
+ * triangles of "Domaine"; boundary lines of "Bord" (oriented like the
+ * triangle edge they lie on); the "PointPression" vertex or -1.  Same result
+ * as reading a msh file that holds these entities in this order. */
+int fe_mesh_from_arrays(int64_t n_vertices, const double *x, const double *y, int64_t n_triangles,
+                        const int32_t *tri, int64_t n_boundary, const int32_t *bnd, int32_t point,
+                        fe_mesh **out);
 int fe_mesh_sizes(const fe_mesh *m, int64_t *n_vertices, int64_t *n_triangles, int64_t *n_edges,
                   int64_t *n_boundary);
 /* Any output may be NULL.  x,y [nv]; tri [3 nt]; tri_edges [3 nt]; bnd [2 nb]; point [1]. */
@@ -223,6 +230,19 @@ int fe_cuda_set_bdf(fe_cuda_system *s, int order, const double *cn, const double
                     const double *hist2);
 int fe_cuda_compute_soldot(fe_cuda_system *s);
 
+/* ---- error norms (feNorm L2_ERROR / VECTOR_L2_ERROR, src/feNorm.cpp:152-163,323-391,1399-1443)
+ * on the quadrature rule of the system's forms.  fe_cuda_norm_points gives the
+ * rule's nodes on every element (nq per element, the system's element order;
+ * x, y: n_elm * nq doubles, or NULL to query nq only): the caller evaluates
+ * its exact solution there (feNorm's feFunction calls) and passes the values
+ * to fe_cuda_l2_error as [n_elm][nq][ncomp].  field 0: the P2 field (scalar
+ * P2 systems: 1 component; Taylor-Hood: the velocity, 2 components), field 1:
+ * the P1 pressure of Taylor-Hood (1 component).  error = sqrt(sum over
+ * elements, nodes and components of |exact - u_h|^2 |J| w), computed on the
+ * device from the current solution. */
+int fe_cuda_norm_points(fe_cuda_system *s, int *nq, double *x, double *y);
+int fe_cuda_l2_error(fe_cuda_system *s, int field, const double *exact, double *error);
+
 /* ---- feLinearSystem operations (src/feLinearSystem.h:96-145) */
 int fe_cuda_set_to_zero(fe_cuda_system *s);
 int fe_cuda_set_matrix_to_zero(fe_cuda_system *s);
@@ -250,12 +270,19 @@ int fe_cuda_reset_times(fe_cuda_system *s);
  * events on the system stream, each run preceded by an L2 flush (a write of
  * flush_bytes): which = 0 residual assembly (all colors), 1 matrix assembly
  * (all colors), 2 SpMV with the system matrix, 3 one preconditioner
- * application, 4 one finest-level step of the multigrid smoother (both
- * velocity components).  Uses the current solution state. */
+ * application, 4 one finest-level multigrid pre-smoothing pass (zero start
+ * fused with the first Chebyshev step, both velocity components), 5 one
+ * Gram-Schmidt dot pass of the mixed FGMRES over restart/2 basis vectors,
+ * 6 one Gram-Schmidt update + norm pass over restart/2 basis vectors.
+ * Phases 5 and 6 need a mixed-precision system that has solved once.  Uses
+ * the current solution state. */
 int fe_cuda_bench_phase(fe_cuda_system *s, int which, int reps, int64_t flush_bytes, double *avg_ms);
 /* Algorithmic bytes of one run of phase 4 (finest multigrid operator read
  * once, each vector entry read or written once). */
 int fe_cuda_smoother_bytes(fe_cuda_system *s, int64_t *bytes);
+/* Algorithmic bytes of one run of phase 4, 5 or 6 (every operand read or
+ * written once). */
+int fe_cuda_phase_bytes(fe_cuda_system *s, int which, int64_t *bytes);
 /* Kernel launches of the library since load (graph replays count their
  * kernel nodes). */
 int fe_cuda_launch_count(int64_t *count);

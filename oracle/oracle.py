@@ -210,3 +210,67 @@ def constrain(ia, ja, values, rhs, rows=(), master=(), slave=()):
     s = np.ascontiguousarray(slave, np.int64)
     load().fo_periodicity(n, _p(ia), _p(ja), _p(v), _p(r), _p(m), _p(s), len(m))
     return v, r
+
+
+# ---- error norms and a direct Newton solve (convergence golden outputs) -------
+
+def _p2_shape(r, s):
+    """feSpaceTriP2 shape functions (src/feSpace_2D.cpp:536-566): vertex
+    functions 0-2, then edge functions of edges (0,1), (1,2), (2,0)."""
+    t = 1.0 - r - s
+    return np.stack([t * (1 - 2 * r - 2 * s), r * (2 * r - 1), s * (2 * s - 1), 4 * r * t, 4 * r * s, 4 * s * t], -1)
+
+
+def l2_error(elem_type, adr, elem_xy, u, quad, fct, field):
+    """feNorm L2_ERROR / VECTOR_L2_ERROR with p = 2 (src/feNorm.cpp:323-391,
+    1399-1443): over the elements in mesh order and the rule's nodes,
+    sum |u_ex - u_h|^2 J w, u_h from the element's DOFs (scalar P2: local a;
+    Taylor-Hood velocity: local 2a + c; Taylor-Hood pressure: local 12 + j),
+    positions from the P1 geometry, J the element's Jacobian determinant;
+    returns the square root."""
+    r, s, w = (np.asarray(v, np.float64) for v in quad)
+    xy = np.asarray(elem_xy, np.float64).reshape(-1, 6)
+    adr = np.asarray(adr, np.int64)
+    x0, y0, x1, y1, x2, y2 = xy.T
+    det = (x1 - x0) * (y2 - y0) - (x2 - x0) * (y1 - y0)
+    psi = np.stack([1 - r - s, r, s], -1)                       # nq x 3
+    px = np.outer(x0, psi[:, 0]) + np.outer(x1, psi[:, 1]) + np.outer(x2, psi[:, 2])
+    py = np.outer(y0, psi[:, 0]) + np.outer(y1, psi[:, 1]) + np.outer(y2, psi[:, 2])
+    ex = fct(px, py)
+    u = np.asarray(u, np.float64)
+    if elem_type == 1 and field == 0:
+        uh = [u[adr[:, :6]] @ _p2_shape(r, s).T]
+    elif elem_type == 2 and field == 0:
+        phi = _p2_shape(r, s)
+        uh = [u[adr[:, c:12:2]] @ phi.T for c in range(2)]
+    elif elem_type == 2 and field == 1:
+        uh = [u[adr[:, 12:15]] @ psi.T]
+    else:
+        raise ValueError("no such field")
+    e2 = sum((np.broadcast_to(ex[c], px.shape) - uh[c]) ** 2 for c in range(len(uh)))
+    per_elem = (e2 * w[None, :]).sum(1) * det
+    res = float(per_elem.sum())
+    if res < 0 and abs(res) < 1e-14:
+        res = abs(res)
+    return np.sqrt(res)
+
+
+def newton_direct(op, u, tol_residual=1e-10, tol_correction=1e-10, max_iter=20):
+    """Newton iterations on the oracle's residual and Jacobian with a direct
+    sparse solve (scipy SuperLU), in feNG's convention: A du = rhs (rhs = sum
+    of element Be), u[:nInc] += du; stops on the absolute max-norms of the
+    residual or the correction (src/feNonLinearSolver.cpp:38-181)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    k = op.keep
+    u = np.array(u, np.float64)
+    for it in range(max_iter):
+        rhs = op.residual(u)
+        if np.max(np.abs(rhs)) <= tol_residual:
+            return u, it
+        a = sp.csr_matrix((op.matrix(u), k["ja"], k["ia"]), shape=(op.n_inc, op.n_inc))
+        du = spl.spsolve(a.tocsc(), rhs)
+        u[:op.n_inc] += du
+        if np.max(np.abs(du)) <= tol_correction:
+            return u, it + 1
+    return u, max_iter

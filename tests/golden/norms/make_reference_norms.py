@@ -1,0 +1,65 @@
+"""Builds tests/golden/norms/reference_l2.npz from the reference checkout:
+
+* the meshes of two of its convergence tests, read with this package's msh
+  4.1 reader and stored as arrays (vertices, triangles, boundary lines,
+  pressure point):
+    - data/mmsMeshes/square1-4.msh (tests/withLinearSolver/scalarFE.cpp:772)
+    - data/square1-4.msh            (tests/withLinearSolver/navier_stokes.cpp:149)
+* the L2 errors those tests print in their golden output files:
+    - tests/withLinearSolver/scalarFE_diffusion.output, block "P2 field 0"
+      (P2 diffusion, u = sin(pi x) sin(pi y), quadrature degree 8)
+    - tests/withLinearSolver/navier_stokes_MMS.output, "Divergence
+      formulation" blocks (Taylor-Hood P2-P1 MMS, velocity and pressure).
+
+Run where the reference exists:  python tests/golden/norms/make_reference_norms.py [REF_ROOT]
+"""
+import re
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parents[2]))
+
+import feng_gb300 as fe  # noqa: E402
+
+
+def parse_block(text, header):
+    """(nElm, error) rows of the table that follows `header`."""
+    lines = text.splitlines()
+    i = lines.index(header)
+    rows = []
+    for ln in lines[i + 2:]:
+        parts = ln.split()
+        if len(parts) != 3:
+            break
+        rows.append((int(parts[0]), float(parts[1])))
+    return np.array([r[0] for r in rows]), np.array([r[1] for r in rows])
+
+
+def main(ref=Path("/root/reference")):
+    out = {}
+    for key, sub in (("diff", "data/mmsMeshes/square"), ("ns", "data/square")):
+        for i in range(1, 5):
+            m = fe.Mesh2DP1.from_msh(ref / f"{sub}{i}.msh")
+            a = m.arrays()
+            out[f"{key}{i}_x"], out[f"{key}{i}_y"] = a["x"], a["y"]
+            out[f"{key}{i}_tri"], out[f"{key}{i}_bnd"] = a["tri"], a["bnd"]
+            out[f"{key}{i}_point"] = np.int32(a["point"])
+    t = (ref / "tests/withLinearSolver/scalarFE_diffusion.output").read_text()
+    out["diff_nelm"], out["diff_err_u"] = parse_block(t, "Diffusion - Error on u - Lagrange elements P2 field 0")
+    t = (ref / "tests/withLinearSolver/navier_stokes_MMS.output").read_text()
+    blocks = [m.start() for m in re.finditer("Navier-Stokes MMS - Divergence formulation - Error on u", t)]
+    assert len(blocks) == 1
+    out["ns_nelm"], out["ns_err_u"] = parse_block(t, "Navier-Stokes MMS - Divergence formulation - Error on u")
+    _, out["ns_err_p"] = parse_block(t, "Navier-Stokes MMS - Divergence formulation - Error on p")
+    for key in ("diff", "ns"):
+        for i in range(1, 5):
+            assert len(out[f"{key}{i}_tri"]) == out[f"{key}_nelm"][i - 1]
+    np.savez_compressed(HERE / "reference_l2.npz", **out)
+    print({k: v for k, v in out.items() if "err" in k or "nelm" in k})
+
+
+if __name__ == "__main__":
+    main(*(Path(a) for a in sys.argv[1:]))

@@ -57,3 +57,64 @@ def golden_mesh(g):
 
 def rel_err(a, b):
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def reference_l2():
+    """Meshes and golden L2 errors of the reference's convergence tests
+    (tests/golden/norms/make_reference_norms.py)."""
+    from pathlib import Path
+    p = Path(__file__).resolve().parent / "golden" / "norms" / "reference_l2.npz"
+    with np.load(p) as z:
+        return {k: z[k] for k in z.files}
+
+
+def convergence_case(g, key, i):
+    """One mesh of the reference's convergence tests with its spaces and
+    forms: key "diff" = P2 diffusion of u = sin(pi x) sin(pi y) on
+    data/mmsMeshes/square<i>.msh (tests/withLinearSolver/scalarFE.cpp:37-56,
+    802), key "ns" = Taylor-Hood Navier-Stokes MMS, divergence formulation,
+    velocity and pressure essential on "Bord", on data/square<i>.msh
+    (tests/withLinearSolver/navier_stokes.cpp:63-92, 355).  Quadrature degree
+    8.  Returns (mesh, numbering, forms, norm spaces, exact functions)."""
+    mesh = fe.Mesh2DP1.from_arrays(g[f"{key}{i}_x"], g[f"{key}{i}_y"], g[f"{key}{i}_tri"], g[f"{key}{i}_bnd"],
+                                   int(g[f"{key}{i}_point"]))
+    if key == "diff":
+        uB = fe.createFiniteElementSpace(mesh, fe.LAGRANGE, 2, "U", "Bord", 8, exact.sin_sin)
+        u = fe.createFiniteElementSpace(mesh, fe.LAGRANGE, 2, "U", "Domaine", 8, exact.zero_scalar)
+        num = fe.feMetaNumber(mesh, [uB, u], [uB])
+        forms = [fe.createBilinearForm([u], fe.feSysElm_Diffusion(1.0)),
+                 fe.createBilinearForm([u], fe.feSysElm_Source(fe.api.SRC_SIN_SIN, (-2 * np.pi ** 2,)))]
+        return mesh, num, forms, [u], [exact.sin_sin]
+    u = fe.createFiniteElementSpace(mesh, fe.VECTOR_LAGRANGE, 2, "U", "Domaine", 8, exact.ns_mms_velocity)
+    uB = fe.createFiniteElementSpace(mesh, fe.VECTOR_LAGRANGE, 2, "U", "Bord", 8, exact.ns_mms_velocity)
+    p = fe.createFiniteElementSpace(mesh, fe.LAGRANGE, 1, "P", "Domaine", 8, exact.ns_mms_pressure)
+    pB = fe.createFiniteElementSpace(mesh, fe.LAGRANGE, 1, "P", "Bord", 8, exact.ns_mms_pressure)
+    num = fe.feMetaNumber(mesh, [u, uB, p, pB], [uB, pB])
+    forms = [fe.createBilinearForm([u], fe.feSysElm_VectorConvectiveAcceleration(-1.0)),
+             fe.createBilinearForm([p, u], fe.feSysElm_MixedDivergence(1.0)),
+             fe.createBilinearForm([u], fe.feSysElm_VectorSource(fe.api.SRC_NS_MMS_POLY)),
+             fe.createBilinearForm([u, p], fe.feSysElm_DivergenceNewtonianStress(1.0, 1.0))]
+    return mesh, num, forms, [u, p], [exact.ns_mms_velocity, exact.ns_mms_pressure]
+
+
+def essential_state(num, fcts_by_field):
+    """Zero unknowns and the exact values on the essential DOFs (nodewise,
+    as feSolution::initializeEssentialBC)."""
+    st = num.setup(256)
+    x, y, fld, comp, _ = st.dofInfo()
+    u = np.zeros(st.nDofs)
+    ess = np.arange(st.nInc, st.nDofs)
+    for f, fct in enumerate(fcts_by_field):
+        sel = ess[fld[ess] == f]
+        vals = fct(x[sel], y[sel])
+        for c in range(len(vals)):
+            m = comp[sel] == c
+            u[sel[m]] = np.broadcast_to(vals[c], sel.shape)[m]
+    return u
+
+
+def element_xy(mesh):
+    arr = mesh.arrays()
+    tri = arr["tri"]
+    return np.stack([arr["x"][tri[:, 0]], arr["y"][tri[:, 0]], arr["x"][tri[:, 1]], arr["y"][tri[:, 1]],
+                     arr["x"][tri[:, 2]], arr["y"][tri[:, 2]]], 1)

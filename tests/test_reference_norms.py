@@ -1,0 +1,66 @@
+"""The oracle against the reference's own golden convergence outputs: P2
+diffusion (tests/withLinearSolver/scalarFE_diffusion.output) and Taylor-Hood
+Navier-Stokes MMS (navier_stokes_MMS.output, divergence formulation) on the
+reference's meshes, solved with the oracle's residual and Jacobian and a
+direct sparse solve, errors by the oracle's restatement of feNorm.
+
+The golden files print 7 significant digits (%e); as the reference's test
+(compareOutputFiles), the errors must print the same."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from helpers import convergence_case, element_xy, essential_state, reference_l2
+
+from feng_gb300.api import quadrature_rule
+from oracle.oracle import OracleProblem, l2_error, newton_direct
+
+
+
+def printed(v):
+    return f"{float(v):.6e}"
+
+
+def _oracle_errors(key, i):
+    g = reference_l2()
+    mesh, num, forms, spaces, fcts = convergence_case(g, key, i)
+    st = num.setup(256)
+    ia, ja = st.pattern()
+    off, el = st.coloring()
+    adr, xy = st.elementDofs(), element_xy(mesh)
+    quad = quadrature_rule(8)
+    op = OracleProblem(num.elem_type, adr, xy, st.nInc, st.nDofs, off, el, ia, ja, quad,
+                       [f.sysElm for f in forms])
+    u, its = newton_direct(op, essential_state(num, fcts))
+    assert its < 20
+    return g, [l2_error(num.elem_type, adr, xy, u, quad, fct, field) for field, fct in enumerate(fcts)]
+
+
+@pytest.mark.parametrize("i", [1, 2, 3, 4])
+def test_oracle_diffusion_p2_errors_match_reference_output(i):
+    g, (e,) = _oracle_errors("diff", i)
+    assert printed(e) == printed(g["diff_err_u"][i - 1])
+
+
+@pytest.mark.parametrize("i", [1, 2, 3, 4])
+def test_oracle_navier_stokes_mms_errors_match_reference_output(i):
+    g, (eu, ep) = _oracle_errors("ns", i)
+    assert printed(eu) == printed(g["ns_err_u"][i - 1])
+    assert printed(ep) == printed(g["ns_err_p"][i - 1])
+
+
+def test_fixture_meshes_read_back_from_the_reference_files():
+    """Where the reference checkout exists: the fixture arrays are what this
+    package's msh reader makes of the reference's mesh files."""
+    import feng_gb300 as fe
+    ref = Path("/root/reference/data")
+    if not ref.exists():
+        pytest.skip("reference checkout absent")
+    g = reference_l2()
+    for key, sub in (("diff", "mmsMeshes/square"), ("ns", "square")):
+        for i in range(1, 5):
+            a = fe.Mesh2DP1.from_msh(ref / f"{sub}{i}.msh").arrays()
+            np.testing.assert_array_equal(a["x"], g[f"{key}{i}_x"])
+            np.testing.assert_array_equal(a["tri"], g[f"{key}{i}_tri"])
+            np.testing.assert_array_equal(a["bnd"], g[f"{key}{i}_bnd"])
