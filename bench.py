@@ -419,14 +419,14 @@ def main():
                 "frac": k["gbs"] / peak, "peak_source": peak_kind, "bytes_per_launch": k["bytes"],
                 "ms_per_launch": k["ms"], "traffic": ncu_traffic(traffic_key)}
     roof = roofline("gs_dots", "k_gs_dots (FP32 Gram-Schmidt dot pass, 25 basis vectors)", "k_gs_dots@25")
-    roof_gsu = roofline("gs_update", "k_gs32<32,2> (FP32 Gram-Schmidt update + norm, 25 basis vectors)",
-                        "k_gs32<32,2>@25")
+    roof_gsu = roofline("gs_update", "k_gs_upd<32,true> (FP32 Gram-Schmidt update + norm, 25 basis vectors)",
+                        "k_gs_upd<32,true>@25")
     roof_sm = roofline("smoother_step", "k_cheb_first<float,4,2> (finest AMG level, both velocity components)",
                        "k_cheb_first<float,4,2>")
     asm = kern["mixed"]["matrix_assembly"]
-    roof_asm = {"kernel": "k_matrix_th<float> (Jacobian assembly, all colors)", "bound": "hbm",
+    roof_asm = {"kernel": "k_pack_th + k_matrix_th_rows<float> (row-owned Jacobian assembly)", "bound": "hbm",
                 "achieved": asm["gbs"], "peak": peak, "unit": "GB/s", "frac": asm["gbs"] / peak,
-                "peak_source": peak_kind, "traffic": ncu_traffic("k_matrix_th<float>")}
+                "peak_source": peak_kind, "traffic": ncu_traffic("k_matrix_th_rows<float>")}
     sp = kern["mixed"]["spmv"]
     roof_spmv = {"kernel": "k_spmv<float> (FGMRES inner SpMV)", "bound": "hbm", "achieved": sp["gbs"],
                  "peak": peak, "unit": "GB/s", "frac": sp["gbs"] / peak, "peak_source": peak_kind,

@@ -294,7 +294,8 @@ class LinearSolverOptions:
     precision: str = "fp64"       # "fp64" | "mixed"
     mg_inner: int = 0             # multigrid: inner AMG-CG steps per velocity component
     mg_smooth: int = 1            # multigrid: Chebyshev smoother degree
-    gs_passes: int = 1            # mixed FGMRES Gram-Schmidt: 1 adaptive (second pass when needed), 2 always twice
+    gs_passes: int = 1            # mixed FGMRES Gram-Schmidt: 1 adaptive (second pass when needed), 2 always twice,
+                                  # 3 adaptive with the norm of the update by Pythagoras
 
     def to_c(self, quad_degree: int) -> _lib.Options:
         pc = {"none": 0, "bjacobi-ilu0": 1, "ilu0": 1, "jacobi": 2, "amg": 3}[self.precond]

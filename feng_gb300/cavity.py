@@ -86,7 +86,8 @@ def main(argv=None):
     ap.add_argument("--train-from", type=int, default=10)
     ap.add_argument("--use-from", type=int, default=15)
     ap.add_argument("--summary-from", type=int, default=20)
-    ap.add_argument("--gs-passes", type=int, default=1, help="Gram-Schmidt passes of the mixed FGMRES")
+    ap.add_argument("--gs-passes", type=int, default=1,
+                    help="mixed FGMRES Gram-Schmidt: 1 adaptive, 2 always twice, 3 adaptive with the Pythagoras norm")
     ap.add_argument("--restart", type=int, default=50)
     ap.add_argument("--train-iters", type=int, default=8, help="Adam steps per time step")
     ap.add_argument("--lr", type=float, default=1e-3)

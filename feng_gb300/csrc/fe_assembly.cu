@@ -1,7 +1,16 @@
 // Element assembly kernels: residual (FP64) and Jacobian (FP64 or FP32) of
-// the fused weak forms, scattered into CSR through the element-to-nonzero
-// map, one launch per element color (no two elements of a color share a DOF,
-// so the read-modify-write of values/rhs needs no atomics).
+// the fused weak forms.
+//
+// Colored kernels (residuals; scalar P2 Jacobian): one launch per element
+// color, entries scattered into CSR through the element-to-nonzero map as
+// L2 reductions; no two elements of a color share a DOF, so every entry
+// receives one contribution per color and the sums are the colored
+// read-modify-write's, in color order.
+//
+// Row-owned kernel (Taylor-Hood Jacobian, k_matrix_th_rows): one thread per
+// CSR row sums the element-matrix rows of the elements holding that DOF, in
+// color order, in shared memory; each block writes its contiguous range of
+// CSR values once (no atomics, no map, no separate zeroing pass).
 //
 // Mapping: a block holds 32 elements (lane = element) x 6 warps (warp = P2
 // function a of the element).  Thread (e, a) produces the element-matrix rows
@@ -24,6 +33,8 @@
 // 390-427, 685-747, 1171-1240, 1454-1530), so the results are the same sums
 // regrouped: they agree to rounding.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "fe_common.h"
 #include "fe_device.h"
@@ -623,7 +634,174 @@ __global__ void __launch_bounds__(EPB * 6) k_matrix_th(DeviceMesh dm, FormCoeffs
 
 int64_t nblocks(int64_t begin, int64_t end) { return (end - begin + EPB - 1) / EPB; }
 
+// ---------------------------------------------------------------------------
+// Row-owned Jacobian, Taylor-Hood.
+// ---------------------------------------------------------------------------
+template <typename V>
+__global__ void k_pack_th(DeviceMesh dm, int hasConv, const double *__restrict__ u, V *__restrict__ pack)
+{
+  const int64_t nE = dm.nElm;
+  for(int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < nE; p += (int64_t)gridDim.x * blockDim.x) {
+    V *o = pack + p * ROWASM_PACK;
+#pragma unroll
+    for(int i = 0; i < 12; ++i) o[i] = hasConv ? (V)u[dm.adr[(int64_t)i * nE + p]] : (V)0;
+#pragma unroll
+    for(int k = 0; k < 5; ++k) o[12 + k] = (V)dm.geo[(int64_t)k * nE + p];
+  }
+}
+
+// Thread = CSR row.  Entry (p, li): li < 12 is velocity row (a = li / 2,
+// component m = li % 2) of element p, whose 12 velocity and 3 pressure
+// columns are the element-matrix row of k_matrix_th; li >= 12 is pressure
+// row j = li - 12, whose 12 velocity columns are divu * int psi_j d_m phi_a.
+// The arithmetic is k_matrix_th's, restricted to one row.
+template <typename V>
+__global__ void __launch_bounds__(256) k_matrix_th_rows(RowAsm ra, FormCoeffs fc, const RefTensors *__restrict__ gT,
+                                                        double c0, V *__restrict__ values, int accumulate)
+{
+  extern __shared__ __align__(16) unsigned char rowsmem[];
+  V *sv = reinterpret_cast<V *>(rowsmem);
+  __shared__ SharedTensors<V> sT;
+  load_tensors(sT, gT);
+  const int32_t r0 = ra.blockRows[blockIdx.x], r1 = ra.blockRows[blockIdx.x + 1];
+  const int32_t base = ra.ia[r0], L = ra.ia[r1] - base;
+  for(int i = threadIdx.x; i < L; i += blockDim.x) sv[i] = accumulate ? values[base + i] : (V)0;
+  __syncthreads();
+  const int32_t r = r0 + (int32_t)threadIdx.x;
+  if(r < r1) {
+    V *row = sv + (ra.ia[r] - base);
+    const V *pk = reinterpret_cast<const V *>(ra.pack);
+    for(int32_t k = ra.rowPtr[r]; k < ra.rowPtr[r + 1]; ++k) {
+      const int32_t ent = ra.rowEnt[k];
+      const int64_t p = ent >> 4;
+      const int li = ent & 15;
+      uint8_t off[16];
+      *reinterpret_cast<uint4 *>(off) = reinterpret_cast<const uint4 *>(ra.offs)[k];
+      const V *e = pk + p * ROWASM_PACK;
+      const V G[2][2] = {{e[12], e[13]}, {e[14], e[15]}};
+      const V J = e[16];
+      if(li < 12) {
+        const int a = li >> 1, m = li & 1;
+        V A[12];
+#pragma unroll
+        for(int j = 0; j < 12; ++j) A[j] = 0;
+        if(fc.hasConv) {
+          V U[12];
+#pragma unroll
+          for(int i = 0; i < 12; ++i) U[i] = e[i];
+          V V0[2][6];
+#pragma unroll
+          for(int c = 0; c < 6; ++c)
+#pragma unroll
+            for(int q = 0; q < 2; ++q) V0[q][c] = U[2 * c] * G[q][0] + U[2 * c + 1] * G[q][1];
+          const V cc = (V)fc.conv * J;
+#pragma unroll
+          for(int b = 0; b < 6; ++b) {
+            V W = 0, Z0 = 0, Z1 = 0;  // Z_q = sum_c U_cm T[q][a][b][c]
+#pragma unroll
+            for(int c = 0; c < 6; ++c) {
+              W += V0[0][c] * sT.T[0][a][c][b] + V0[1][c] * sT.T[1][a][c][b];
+              const V t0 = sT.T[0][a][b][c], t1 = sT.T[1][a][b][c];
+              const V ucm = U[2 * c + m];
+              Z0 += ucm * t0;
+              Z1 += ucm * t1;
+            }
+#pragma unroll
+            for(int n = 0; n < 2; ++n) {
+              V v = G[0][n] * Z0 + G[1][n] * Z1;
+              if(m == n) v += W;
+              A[2 * b + n] += cc * v;
+            }
+          }
+        }
+        if(fc.hasSigma) {
+          const V cs = -(V)fc.sigma * (V)fc.mu * J;
+          V GG[2][2][2][2];
+#pragma unroll
+          for(int kk = 0; kk < 2; ++kk)
+#pragma unroll
+            for(int l = 0; l < 2; ++l)
+#pragma unroll
+              for(int q = 0; q < 2; ++q)
+#pragma unroll
+                for(int s2 = 0; s2 < 2; ++s2) GG[kk][l][q][s2] = G[q][kk] * G[s2][l];
+#pragma unroll
+          for(int b = 0; b < 6; ++b) {
+            V S[2][2];
+#pragma unroll
+            for(int kk = 0; kk < 2; ++kk)
+#pragma unroll
+              for(int l = 0; l < 2; ++l) {
+                V v = 0;
+#pragma unroll
+                for(int q = 0; q < 2; ++q)
+#pragma unroll
+                  for(int s2 = 0; s2 < 2; ++s2) v += GG[kk][l][q][s2] * sT.K[q][s2][a][b];
+                S[kk][l] = v;
+              }
+            const V tr = S[0][0] + S[1][1];
+#pragma unroll
+            for(int n = 0; n < 2; ++n) A[2 * b + n] += cs * ((m == n ? tr : (V)0) + S[n][m]);
+          }
+        }
+        if(fc.hasMass) {
+          const V cm = (V)fc.mass * (V)c0 * J;
+#pragma unroll
+          for(int b = 0; b < 6; ++b) A[2 * b + m] += cm * sT.M[a][b];
+        }
+#pragma unroll
+        for(int j = 0; j < 12; ++j)
+          if(off[j] != 255) row[off[j]] += A[j];
+#pragma unroll
+        for(int j = 0; j < 3; ++j) {
+          const V bp = (G[0][m] * sT.D[0][j][a] + G[1][m] * sT.D[1][j][a]) * J;
+          if(off[12 + j] != 255) row[off[12 + j]] += fc.hasSigma ? (V)fc.sigma * bp : (V)0;
+        }
+      } else {
+        const int j = li - 12;
+#pragma unroll
+        for(int a = 0; a < 6; ++a)
+#pragma unroll
+          for(int m = 0; m < 2; ++m) {
+            const V bp = (G[0][m] * sT.D[0][j][a] + G[1][m] * sT.D[1][j][a]) * J;
+            if(off[2 * a + m] != 255) row[off[2 * a + m]] += fc.hasDivu ? (V)fc.divu * bp : (V)0;
+          }
+      }
+    }
+  }
+  __syncthreads();
+  for(int i = threadIdx.x; i < L; i += blockDim.x) values[base + i] = sv[i];
+}
+
+int pack_grid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 8192)); }
+
 }  // namespace
+
+void launch_pack_th_f32(const DeviceMesh &dm, const FormCoeffs &fc, const double *u, float *pack, cudaStream_t s)
+{
+  (k_pack_th<float><<<pack_grid(dm.nElm), 256, 0, s>>>(dm, fc.hasConv, u, pack), ::feng::count_launch());
+}
+
+void launch_pack_th_f64(const DeviceMesh &dm, const FormCoeffs &fc, const double *u, double *pack, cudaStream_t s)
+{
+  (k_pack_th<double><<<pack_grid(dm.nElm), 256, 0, s>>>(dm, fc.hasConv, u, pack), ::feng::count_launch());
+}
+
+void launch_matrix_th_rows_f32(const RowAsm &ra, const FormCoeffs &fc, const RefTensors *dT, double c0,
+                               float *values, int accumulate, cudaStream_t s)
+{
+  if(ra.nBlocks < 1) return;
+  (k_matrix_th_rows<float><<<ra.nBlocks, 256, ra.capBytes, s>>>(ra, fc, dT, c0, values, accumulate),
+   ::feng::count_launch());
+}
+
+void launch_matrix_th_rows_f64(const RowAsm &ra, const FormCoeffs &fc, const RefTensors *dT, double c0,
+                               double *values, int accumulate, cudaStream_t s)
+{
+  if(ra.nBlocks < 1) return;
+  (k_matrix_th_rows<double><<<ra.nBlocks, 256, ra.capBytes, s>>>(ra, fc, dT, c0, values, accumulate),
+   ::feng::count_launch());
+}
 
 void launch_assemble_residual(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
                               const double *u, const double *udot, double t, int64_t nInc,

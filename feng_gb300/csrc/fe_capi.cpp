@@ -102,7 +102,7 @@ static SystemOptions to_sys_options(const fe_cuda_options *o)
   so.precision = o->precision;
   so.mgInner = o->mg_inner;
   so.mgSmooth = o->mg_smooth > 0 ? o->mg_smooth : 1;
-  so.kry.gsPasses = o->gs_passes == 2 ? 2 : 1;
+  so.kry.gsPasses = o->gs_passes == 2 || o->gs_passes == 3 ? o->gs_passes : 1;
   return so;
 }
 
@@ -691,7 +691,7 @@ int fe_cuda_phase_bytes(fe_cuda_system *s, int which, int64_t *bytes)
   if(which == 4) return fe_cuda_smoother_bytes(s, bytes);
   if(which != 5 && which != 6) { set_error("no byte count for phase %d", which); return FE_INVALID_ARG; }
   Krylov &k = s->sys.krylov();
-  const int r = k.gsStep(which == 5 ? 0 : 2, std::max(1, k.opt.restart / 2), bytes);
+  const int r = k.gsStep(which == 5 ? 0 : 4, std::max(1, k.opt.restart / 2), bytes);
   if(r != FE_OK) return r;
   if(cudaStreamSynchronize(s->sys.stream()) != cudaSuccess) {
     set_error("fe_cuda_phase_bytes: device error");

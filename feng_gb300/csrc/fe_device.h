@@ -77,6 +77,34 @@ struct DeviceMesh {
   int32_t *map = nullptr;    // [nloc*nloc][nElm] CSR position or -1
 };
 
+// Row-owned Jacobian assembly of Taylor-Hood systems: one thread builds one
+// CSR row from the (element, local row) entries whose DOF is that row, in
+// color order of the elements, inside a shared-memory copy of its block's
+// contiguous range of CSR values, which the block then writes once.  No
+// atomics, no element-to-nonzero map; each value is the same sum, in the
+// same order, as the colored scatter.
+struct RowAsm {
+  int nBlocks = 0;
+  int capBytes = 0;               // dynamic shared memory of a block
+  int32_t *blockRows = nullptr;   // [nBlocks + 1] first row of each block
+  int32_t *rowPtr = nullptr;      // [nInc + 1] entries of each row
+  int32_t *rowEnt = nullptr;      // [nEnt] p * 16 + local row (p: color-order element)
+  uint8_t *offs = nullptr;        // [nEnt][16] column offset in the row of each local column (255: none)
+  void *pack = nullptr;           // [nElm][20] per element: u at the 12 velocity DOFs, G (4), J
+  const int32_t *ia = nullptr;    // CSR row pointers
+};
+constexpr int ROWASM_PACK = 20;
+
+// Per-element data of the row-owned assembly (RowAsm::pack), from u.
+void launch_pack_th_f32(const DeviceMesh &dm, const FormCoeffs &fc, const double *u, float *pack, cudaStream_t s);
+void launch_pack_th_f64(const DeviceMesh &dm, const FormCoeffs &fc, const double *u, double *pack, cudaStream_t s);
+// Row-owned Taylor-Hood Jacobian; accumulate = 0 overwrites the values
+// (the matrix was zeroed), 1 adds to them.
+void launch_matrix_th_rows_f32(const RowAsm &ra, const FormCoeffs &fc, const RefTensors *dT, double c0,
+                               float *values, int accumulate, cudaStream_t s);
+void launch_matrix_th_rows_f64(const RowAsm &ra, const FormCoeffs &fc, const RefTensors *dT, double c0,
+                               double *values, int accumulate, cudaStream_t s);
+
 // Residual (FP64) of the fused forms on elements [begin,end) of the color
 // order, accumulated into rhs with feNG's sign (rhs = sum of element Be).
 // exact5: the rule integrates degree 5 exactly (RefTensors::exact5), so the

@@ -489,71 +489,83 @@ __global__ void __launch_bounds__(RB, 3) k_gs32(int64_t n4, int64_t ld, const fl
   if(threadIdx.x == 0) st->counter = 0;
 }
 
-// h_c = V_c . w for c < ncols, column-blocked: a block stages a chunk of w
-// (GS_CH groups of 4 rows) in shared memory and each warp streams whole
-// chunk-long runs of its columns (c = warp, warp + 8, ...), so every warp
-// reads long contiguous stretches of one basis vector.  Per-block partial
-// sums in FP64; the last block sums them in block order.
-constexpr int GS_CH = 256;   // float4 groups per block (4 KB of w): ~4 blocks per SM
+// h_c = V_c . w for c < ncols and ||w||^2.  Grid: x = blocks of rows (each
+// thread takes groups of 4 rows, grid-stride), y = groups of eight columns,
+// so every thread keeps eight FP32 accumulators and issues its eight basis
+// loads together; the ||w||^2 column belongs to y = 0.  Per warp a butterfly
+// sums the eight accumulators over the lanes (the last three steps as a
+// reduce-scatter: lane l ends with column l % 8), the warps are summed in
+// FP64, one partial per row block and column; the last block sums the
+// partials in row-block order.
+// pyth (first pass only): the last block also forms ||w - V h||^2 =
+// ||w||^2 - ||h||^2 (Pythagoras, V orthonormal) and, unless that kept less
+// than a hundredth of ||w||^2 (severe cancellation: the
+// Daniel-Gragg-Kaufman-Stewart test with eta = 0.1), takes it as the norm of
+// the update: H[j+1][j] = its root (through Hcol[ncols]), st->finv its
+// inverse; otherwise st->reorth asks for the second pass.
+// second = 1: the reorthogonalisation pass, run only when it was asked for;
+// its coefficients are added to the Hessenberg column.
 __global__ void __launch_bounds__(RB) k_gs_dots(int64_t n4, int64_t ld, const float *__restrict__ V, int ncols,
                                                 const float *__restrict__ w, double *partials, RedState *st,
                                                 double *hcur, double *Hcol, const int *__restrict__ done,
-                                                int second)
+                                                int second, int pyth)
 {
-  // second = 1: the reorthogonalisation pass, run only when the previous
-  // update asked for it; its coefficients are added to the Hessenberg column.
   if(*done || (second && !st->reorth)) return;
-  __shared__ float4 sw[GS_CH];
-  __shared__ float colAcc[MAXM + 1];  // per-column sums of this block's chunks
-  __shared__ float wred[RB / 32];
+  __shared__ float red[RB / 32][9];
+  __shared__ double hsum[MAXM + 1];
   __shared__ bool last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for(int c = threadIdx.x; c <= ncols; c += RB) colAcc[c] = 0.f;
-  float wq = 0.f;  // this thread's share of ||w||^2
+  const int c0 = blockIdx.y * 8;
+  const bool wcol = blockIdx.y == 0;
+  float acc[8];
+#pragma unroll
+  for(int u = 0; u < 8; ++u) acc[u] = 0.f;
+  float wq = 0.f;
   const float4 *w4 = reinterpret_cast<const float4 *>(w);
-  const int64_t nChunks = (n4 + GS_CH - 1) / GS_CH;
-  // The grid is capped (one partial per block and column): blocks take
-  // chunks blockIdx.x, blockIdx.x + gridDim.x, ...
-  for(int64_t ch = blockIdx.x; ch < nChunks; ch += gridDim.x) {
-    const int64_t g0 = ch * GS_CH;
-    __syncthreads();  // previous chunk's sw no longer read
-    for(int i = threadIdx.x; i < GS_CH; i += RB) {
-      const float4 x = g0 + i < n4 ? w4[g0 + i] : make_float4(0.f, 0.f, 0.f, 0.f);
-      sw[i] = x;
-      wq = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, wq))));
-    }
-    __syncthreads();
-    const int64_t lim = n4 - g0;  // groups of this chunk that exist
-    for(int c = warp; c < ncols; c += RB / 32) {
-      const float4 *vc = reinterpret_cast<const float4 *>(V + (int64_t)c * ld) + g0;
-      float acc[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 8
-      for(int i = lane; i < GS_CH; i += 32) {
-        if(i < lim) {
-          const float4 v = __ldcs(vc + i);
-          const float4 x = sw[i];
-          float &a = acc[(i >> 5) & 3];
-          a = fmaf(v.x, x.x, fmaf(v.y, x.y, fmaf(v.z, x.z, fmaf(v.w, x.w, a))));
-        }
-      }
-      float sum = (acc[0] + acc[1]) + (acc[2] + acc[3]);
-      for(int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-      if(lane == 0) colAcc[c] += sum;  // column c belongs to this warp only
+  const float4 *V4 = reinterpret_cast<const float4 *>(V);
+  const int64_t ld4 = ld / 4;
+  for(int64_t g = (int64_t)blockIdx.x * RB + threadIdx.x; g < n4; g += (int64_t)gridDim.x * RB) {
+    const float4 x = w4[g];
+    if(wcol) wq = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, wq))));
+    float4 v[8];
+#pragma unroll
+    for(int u = 0; u < 8; ++u)
+      v[u] = c0 + u < ncols ? __ldcs(V4 + (int64_t)(c0 + u) * ld4 + g) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for(int u = 0; u < 8; ++u)
+      acc[u] = fmaf(v[u].x, x.x, fmaf(v[u].y, x.y, fmaf(v[u].z, x.z, fmaf(v[u].w, x.w, acc[u]))));
+  }
+  // lanes l, l^8, l^16, l^24 first, then a reduce-scatter over the low bits
+#pragma unroll
+  for(int h = 16; h >= 8; h >>= 1)
+#pragma unroll
+    for(int u = 0; u < 8; ++u) acc[u] += __shfl_xor_sync(0xffffffffu, acc[u], h);
+#pragma unroll
+  for(int h = 4; h > 0; h >>= 1) {
+    const bool hi = lane & h;
+#pragma unroll
+    for(int i = 0; i < h; ++i) {
+      const float keep = hi ? acc[i + h] : acc[i];
+      const float send = hi ? acc[i] : acc[i + h];
+      acc[i] = keep + __shfl_xor_sync(0xffffffffu, send, h);
     }
   }
   for(int o = 16; o > 0; o >>= 1) wq += __shfl_xor_sync(0xffffffffu, wq, o);
-  if(lane == 0) wred[warp] = wq;
+  if(lane < 8) red[warp][lane] = acc[0];
+  if(lane == 0) red[warp][8] = wq;
   __syncthreads();
-  if(threadIdx.x == 0) {
-    float t = 0.f;
-    for(int k = 0; k < RB / 32; ++k) t += wred[k];
-    colAcc[ncols] = t;  // ||w||^2 for the reorthogonalisation test of the update pass
+  if(threadIdx.x < 9) {
+    const int t = threadIdx.x;
+    const int col = t < 8 ? c0 + t : ncols;
+    if((t < 8 && col < ncols) || (t == 8 && wcol)) {
+      double sum = 0.;
+      for(int k = 0; k < RB / 32; ++k) sum += (double)red[k][t];
+      partials[(int64_t)col * MAXRED + blockIdx.x] = sum;
+    }
   }
-  __syncthreads();
-  for(int c = threadIdx.x; c <= ncols; c += RB) partials[(int64_t)c * MAXRED + blockIdx.x] = (double)colAcc[c];
   __threadfence();
   __syncthreads();
-  if(threadIdx.x == 0) last = atomicAdd(&st->counter, 1u) == gridDim.x - 1;
+  if(threadIdx.x == 0) last = atomicAdd(&st->counter, 1u) == gridDim.x * gridDim.y - 1;
   __syncthreads();
   if(!last) return;
   __threadfence();
@@ -569,6 +581,7 @@ __global__ void __launch_bounds__(RB) k_gs_dots(int64_t n4, int64_t ld, const fl
     double sum = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
     for(int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
     if(lane == 0) {
+      hsum[c] = sum;
       if(c == ncols) {
         st->result[2] = sum;
       } else {
@@ -578,14 +591,127 @@ __global__ void __launch_bounds__(RB) k_gs_dots(int64_t n4, int64_t ld, const fl
     }
   }
   __syncthreads();
-  if(threadIdx.x == 0) st->counter = 0;
+  if(threadIdx.x == 0) {
+    st->counter = 0;
+    if(pyth && !second) {
+      const double ww = hsum[ncols];
+      double hh = 0.;
+      for(int c = 0; c < ncols; ++c) hh += hsum[c] * hsum[c];
+      const double est = ww - hh;
+      if(est > 1e-2 * ww) {
+        const double nrm = sqrt(est);
+        Hcol[ncols] = nrm;
+        st->finv = (float)(1.0 / nrm);
+        st->reorth = 0;
+      } else {
+        st->reorth = 1;
+      }
+    }
+  }
+}
+
+// The update pass w - V h over c < ncols.
+// NORM: the result goes back to w and its squared norm is reduced (one FP64
+// partial per block, the last block sums them in block order): H[j+1][j] =
+// the norm (through Hnext), st->finv its inverse; on the first pass
+// (second = 0) st->reorth asks for a second pass when the update kept less
+// than a tenth of ||w|| (||w||^2 in st->result[2] from the dot pass); the
+// second pass runs only when it was asked for.
+// !NORM (after a dot pass that took the norm by Pythagoras): unless a second
+// pass was asked for, the result times st->finv is the next basis vector
+// (vnext); otherwise it goes back to w.
+template <int CMAX, bool NORM>
+__global__ void __launch_bounds__(RB, 4) k_gs_upd(int64_t n4, int64_t ld, const float *__restrict__ V, int ncols,
+                                                  const double *__restrict__ hprev, float *__restrict__ w,
+                                                  float *__restrict__ vnext, RedState *st, double *partials,
+                                                  double *Hnext, const int *__restrict__ done, int second)
+{
+  if(*done || (NORM && second && !st->reorth)) return;
+  __shared__ float hs[CMAX];
+  __shared__ double wred[RB / 32];
+  __shared__ bool last;
+  for(int c = threadIdx.x; c < CMAX; c += RB) hs[c] = c < ncols ? (float)hprev[c] : 0.f;
+  __syncthreads();
+  const bool again = NORM || st->reorth != 0;
+  const float inv = NORM ? 1.f : st->finv;
+  float4 *w4 = reinterpret_cast<float4 *>(w);
+  float4 *o4 = reinterpret_cast<float4 *>(again ? w : vnext);
+  const float4 *V4 = reinterpret_cast<const float4 *>(V);
+  const int64_t ld4 = ld / 4;
+  float q = 0.f;
+  for(int64_t g = (int64_t)blockIdx.x * RB + threadIdx.x; g < n4; g += (int64_t)gridDim.x * RB) {
+    float4 wv = w4[g];
+    // one batch of eight column loads in flight at a time (unrolled
+    // batches would hoist every load and spill)
+#pragma unroll 1
+    for(int c0 = 0; c0 < CMAX; c0 += 8) {
+      if(c0 < ncols) {
+        float4 v[8];
+#pragma unroll
+        for(int u = 0; u < 8; ++u)
+          v[u] = c0 + u < ncols ? __ldcs(V4 + (int64_t)(c0 + u) * ld4 + g) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for(int u = 0; u < 8; ++u) {
+          const float h = hs[c0 + u];
+          wv.x = fmaf(-h, v[u].x, wv.x);
+          wv.y = fmaf(-h, v[u].y, wv.y);
+          wv.z = fmaf(-h, v[u].z, wv.z);
+          wv.w = fmaf(-h, v[u].w, wv.w);
+        }
+      }
+    }
+    if(NORM) {
+      q = fmaf(wv.x, wv.x, fmaf(wv.y, wv.y, fmaf(wv.z, wv.z, fmaf(wv.w, wv.w, q))));
+    } else if(!again) {
+      wv.x *= inv;
+      wv.y *= inv;
+      wv.z *= inv;
+      wv.w *= inv;
+    }
+    o4[g] = wv;
+  }
+  if(!NORM) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for(int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+  if(lane == 0) wred[warp] = (double)q;
+  __syncthreads();
+  if(threadIdx.x == 0) {
+    double sum = 0.;
+    for(int k = 0; k < RB / 32; ++k) sum += wred[k];
+    partials[blockIdx.x] = sum;
+    __threadfence();
+    last = atomicAdd(&st->counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if(!last) return;
+  __threadfence();
+  if(warp == 0) {
+    double s8[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
+    const int nb = (int)gridDim.x;
+    for(int b0 = lane; b0 < nb; b0 += 256) {
+#pragma unroll
+      for(int k = 0; k < 8; ++k)
+        if(b0 + 32 * k < nb) s8[k] += __ldcg(partials + b0 + 32 * k);
+    }
+    double sum = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
+    for(int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if(lane == 0) {
+      const double nrm = sqrt(sum);
+      st->result[0] = sum;
+      *Hnext = nrm;
+      st->finv = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
+      if(!second) st->reorth = sum < 1e-2 * st->result[2] ? 1 : 0;
+      st->counter = 0;
+    }
+  }
 }
 
 // v = w * (1 / ||w||) in FP32, 4 rows per thread; the scale comes from k_gs32<., 2>.
+// gated: only after a second Gram-Schmidt pass (otherwise k_gs_upd wrote v).
 __global__ void k_scale32(int64_t n4, const float *__restrict__ w, float *__restrict__ v, const RedState *st,
-                          const int *__restrict__ done)
+                          const int *__restrict__ done, int gated)
 {
-  if(*done) return;
+  if(*done || (gated && !st->reorth)) return;
   const float inv = st->finv;
   const float4 *w4 = reinterpret_cast<const float4 *>(w);
   float4 *v4 = reinterpret_cast<float4 *>(v);
@@ -896,7 +1022,14 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
     }
   }
   // one group of 4 rows per thread: the whole pass is one wave of loads
-  gsParts_ = grid_for((n_ + 3) / 4, RB, MAXRED);
+  {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    nSM_ = std::max(1, sms);
+  }
+  // whole waves of the update passes (three blocks per SM)
+  gsParts_ = grid_for((n_ + 3) / 4, RB, std::min(MAXRED, 3 * nSM_));
   CK(cudaMalloc(&v32_, sizeof(float) * n_));
   CK(cudaMalloc(&w32_, sizeof(float) * ((n_ + 63) / 64 * 64)));
   CK(cudaMemset(w32_, 0, sizeof(float) * ((n_ + 63) / 64 * 64)));
@@ -1114,7 +1247,7 @@ double Krylov::norminf(const double *x)
 
 int Krylov::gsStep(int mode, int ncols, int64_t *bytes)
 {
-  if(!V32_ || (mode != 0 && mode != 2) || ncols < 1 || ncols > opt.restart) {
+  if(!V32_ || (mode != 0 && mode != 4) || ncols < 1 || ncols > opt.restart) {
     set_error("no mixed FP32 basis, or an invalid Gram-Schmidt request");
     return FE_INVALID_ARG;
   }
@@ -1124,29 +1257,45 @@ int Krylov::gsStep(int mode, int ncols, int64_t *bytes)
   }
   Ws w = Ws_INIT(this);
   if(mode == 0) gs32(0, ncols, nullptr, w.gs->hcur, w.gs->H, zeroFlag_, 0);
-  else gs32(2, ncols, w.gs->hcur, nullptr, w.gs->H + ncols, zeroFlag_, 0);
+  else gs32(4, ncols, w.gs->hcur, nullptr, w.gs->H + ncols, zeroFlag_, 0);
+  // dots: ncols columns and w read; update: ncols columns and w read, w
+  // written
   if(bytes) *bytes = (int64_t)(ncols + (mode == 0 ? 1 : 2)) * ld32_ * (int64_t)sizeof(float);
   return FE_OK;
 }
 
-// One FP32 Gram-Schmidt pass (k_gs32) over the first ncols basis vectors.
+// One FP32 Gram-Schmidt pass over the first ncols basis vectors: mode 0 the
+// dot pass (k_gs_dots), 5 the dot pass with the Pythagoras norm, 1 update +
+// dots, 2 update + norm (k_gs32), 3 the update that writes the next basis
+// vector, 4 update + norm (k_gs_upd).
 void Krylov::gs32(int mode, int ncols, const double *hprev, double *hcur, double *Hcol, const int *done, int pass)
 {
   RedState *st = (RedState *)red_state_;
   const int g = gsParts_;
   const int64_t n4 = ld32_ / 4;
+  const int gu = (int)std::max<int64_t>(1, std::min<int64_t>((n4 + RB - 1) / RB, 4 * nSM_));
 #define FE_GS_LAUNCH(C)                                                                                         \
   do {                                                                                                          \
     if(mode == 0)                                                                                               \
       (k_gs32<C, 0><<<g, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done, pass), ::feng::count_launch()); \
     else if(mode == 1)                                                                                          \
       (k_gs32<C, 1><<<g, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done, pass), ::feng::count_launch()); \
-    else                                                                                                        \
+    else if(mode == 2)                                                                                          \
       (k_gs32<C, 2><<<g, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done, pass), ::feng::count_launch()); \
+    else if(mode == 3)                                                                                          \
+      (k_gs_upd<C, false><<<gu, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, V32_ + (int64_t)ncols * ld32_, st, red_, nullptr, done, 0), ::feng::count_launch()); \
+    else                                                                                                        \
+      (k_gs_upd<C, true><<<gu, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, nullptr, st, red_, Hcol, done, pass), ::feng::count_launch()); \
   } while(0)
-  if(mode == 0) {
-    const int gb = (int)std::max<int64_t>(1, std::min<int64_t>((n4 + GS_CH - 1) / GS_CH, MAXRED));
-    (k_gs_dots<<<gb, RB, 0, s_>>>(n4, ld32_, V32_, ncols, w32_, red_, st, hcur, Hcol, done, pass),
+  if(mode == 0 || mode == 5) {
+    // mode 5: the dot pass that also takes the norm of the update by Pythagoras
+    // about four blocks per SM in all: each block loops over several row
+    // groups (fewer partials, one counter increment per block)
+    const int gy = (ncols + 7) / 8;
+    const int64_t gx = std::max<int64_t>(
+        1, std::min<int64_t>({(n4 + RB - 1) / RB, (int64_t)MAXRED, (int64_t)(4 * nSM_ + gy - 1) / gy}));
+    const dim3 gb((unsigned)gx, (unsigned)gy);
+    (k_gs_dots<<<gb, RB, 0, s_>>>(n4, ld32_, V32_, ncols, w32_, red_, st, hcur, Hcol, done, pass, mode == 5 ? 1 : 0),
      ::feng::count_launch());
     return;
   }
@@ -1224,20 +1373,32 @@ void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, i
     precond32(vj, zj, &w.gs->done);
     spmv_launch<float, float, float, float, false>(lanes_, n_, A_, vals, zj, nullptr, w32_, &w.gs->done, s_);
     double *Hcol = w.gs->H + (int64_t)j * (MAXM + 1);
-    if(opt.gsPasses > 1) {
+    if(opt.gsPasses == 2) {
       // always twice: dots, fused update + dots, update + norm
       gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 0);
       gs32(1, j + 1, w.gs->hcur, w.gs->hcur, Hcol, &w.gs->done, 0);
       gs32(2, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done, 2);
-    } else {
-      // once, and a second time only when the update kept less than a
-      // tenth of ||w|| (decided on the device, so the replayed graph is fixed)
-      gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 0);
-      gs32(2, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done, 0);
+    } else if(opt.gsPasses == 3) {
+      // once, the norm of the update by Pythagoras from the dot pass and the
+      // next basis vector written by the update pass; a second time only
+      // when the update kept less than a tenth of ||w|| (decided on the
+      // device, so the replayed graph is fixed): the update goes back to w,
+      // the second dot pass, update + norm pass and scale pass run.
+      gs32(5, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 0);
+      gs32(3, j + 1, w.gs->hcur, nullptr, nullptr, &w.gs->done, 0);
       gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 1);
-      gs32(2, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done, 1);
+      gs32(4, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done, 1);
+    } else {
+      // once (dot pass, update + norm pass), and a second time only when
+      // the update kept less than a tenth of ||w|| (decided on the device,
+      // so the replayed graph is fixed)
+      gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 0);
+      gs32(4, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done, 0);
+      gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 1);
+      gs32(4, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done, 1);
     }
-    (k_scale32<<<g4, 256, 0, s_>>>(ld32_ / 4, w32_, V32_ + (int64_t)(j + 1) * ld32_, w.st, &w.gs->done),
+    (k_scale32<<<g4, 256, 0, s_>>>(ld32_ / 4, w32_, V32_ + (int64_t)(j + 1) * ld32_, w.st, &w.gs->done,
+                                   opt.gsPasses == 3 ? 1 : 0),
      ::feng::count_launch());
     (k_givens<<<1, 32, 0, s_>>>(w.gs, j), ::feng::count_launch());
     if(poll && poll_done(&w.gs->done, j)) break;

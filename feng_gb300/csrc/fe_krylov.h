@@ -73,7 +73,8 @@ struct KrylovOptions {
   int mixed = 0;           // 1: FP32 matrix/preconditioner/SpMV inside FP64 refinement
   int refineMax = 20;      // outer refinement steps in mixed mode
   double innerRtol = 1e-4; // inner FP32 solve tolerance in mixed mode
-  int gsPasses = 1;        // mixed FGMRES Gram-Schmidt: 1 = once + second pass when needed, 2 = always twice
+  int gsPasses = 1;        // mixed FGMRES Gram-Schmidt: 1 = once + second pass when needed, 2 = always
+                           // twice, 3 = as 1 with the norm of the update by Pythagoras from the dot pass
 };
 
 struct KrylovStats {
@@ -126,7 +127,8 @@ class Krylov {
   float *Z32_ = nullptr;  // m x n      preconditioned directions (mixed path)
   float *V32_ = nullptr;  // (m+1) x n  Krylov basis of the mixed path, FP32
   int *zeroFlag_ = nullptr;  // a device 0 ("not done") for gsStep
-  int gsParts_ = 0;       // blocks of the FP32 Gram-Schmidt passes
+  int gsParts_ = 0;       // blocks of the FP32 Gram-Schmidt update passes
+  int nSM_ = 1;           // multiprocessors of the device
   int64_t ld32_ = 0;      // leading dimension of V32_ / Z32_ (multiple of 64)
   // pass: 0 first pass (the update + norm decides on reorthogonalisation),
   // 1 the conditional second pass, 2 the last pass of an unconditional CGS2
@@ -177,7 +179,7 @@ class Krylov {
   int smootherStep(int64_t *bytes);
   // One pass of the mixed FGMRES Gram-Schmidt on the current FP32 basis with
   // ncols columns (benchmark phases): mode 0 the dot pass (k_gs_dots), mode
-  // 2 the update + norm pass (k_gs32<., 2>).  bytes: algorithmic bytes.
+  // 4 the update + norm pass (k_gs_upd).  bytes: algorithmic bytes.
   int gsStep(int mode, int ncols, int64_t *bytes);
   int factor_mg(const double *values64, const float *values32);
   template <typename V> void apply_mg(const V *vals, const V *r, V *z, const int *skip);

@@ -121,7 +121,8 @@ class SystemCUDA {
   int normPoints(int *nq, double *hostX, double *hostY);
   int l2Error(int field, const double *hostExact, double *err);
   // Times `reps` runs of one phase with CUDA events on the system stream, each
-  // preceded by an L2 flush (a write of flushBytes): which = 0 residual
+  // preceded by an L2 flush (a write of flushBytes, then a read of it, so
+  // that no dirty lines remain to be written back): which = 0 residual
   // assembly, 1 matrix assembly, 2 SpMV with the system matrix, 3 one
   // preconditioner application, 4 one finest-level multigrid smoother step
   // (two components).  Returns the mean milliseconds per run.
@@ -158,6 +159,16 @@ class SystemCUDA {
   FormCoeffs fc_{};
   RefTensors *dT_ = nullptr;
   int nq_ = 0;  // nodes of the system's quadrature rule
+  // Row-owned Taylor-Hood Jacobian (used when every row is shorter than 255).
+  RowAsm ra_;
+  bool useRows_ = false;
+  // setMatrixToZero is deferred: the next row-owned assembly overwrites the
+  // values instead of adding to them; any other use of the values zeroes
+  // them first.
+  mutable bool zeroPending_ = false;
+  int ensureMatrixZeroed() const;
+  int launch_matrix();  // the Jacobian launches of assembleMatrices
+  int build_row_assembly(const std::vector<int32_t> &adrP, const std::vector<int32_t> &map);
   DeviceCSR csr_;
   double *vals64_ = nullptr;
   float *vals32_ = nullptr;

@@ -18,6 +18,7 @@ kernel (for per-kernel profiler launch lists).
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import time
 
@@ -74,7 +75,13 @@ def main(argv=None):
     ap.add_argument("--max-iter", type=int, default=30, help="Newton iterations at most (feNLSolverOptions.maxIter)")
     ap.add_argument("--restart", type=int, default=50, help="FGMRES restart length")
     ap.add_argument("--mg-smooth", type=int, default=1, help="Chebyshev smoother degree of the multigrid")
-    ap.add_argument("--gs-passes", type=int, default=1, help="Gram-Schmidt passes of the mixed FGMRES (1 or 2)")
+    ap.add_argument("--gs-passes", type=int, default=1,
+                    help="mixed FGMRES Gram-Schmidt: 1 adaptive, 2 always twice, 3 adaptive with the Pythagoras norm")
+    ap.add_argument("--phases", default="",
+                    help="after the solves, time these benchmark phases (comma list of fe_cuda_bench_phase "
+                         "numbers: 0 residual, 1 Jacobian, 2 SpMV, 3 preconditioner, 4 finest smoother pass, "
+                         "5 Gram-Schmidt dots, 6 Gram-Schmidt update)")
+    ap.add_argument("--phase-reps", type=int, default=20)
     args = ap.parse_args(argv)
 
     from . import api as fe
@@ -97,9 +104,22 @@ def main(argv=None):
             runs.append({"seconds": time.perf_counter() - t0, "newton_iterations": st["iterations"],
                          "krylov_iterations": st["krylov_iterations"],
                          "rel_residual": st["residual"] / st["residual0"] if st["residual0"] else 0.0})
+    phases = {}
+    for w in [int(v) for v in args.phases.split(",") if v.strip()]:
+        # device time per run with the L2 flushed before each run; bytes:
+        # algorithmic bytes where the library defines them (phases 4-6)
+        ms = C.c_double()
+        check(lib.fe_cuda_bench_phase(sys_._h, w, args.phase_reps, 256 << 20, C.byref(ms)))
+        ph = {"us": ms.value * 1e3}
+        if w >= 4:
+            by = C.c_int64()
+            check(lib.fe_cuda_phase_bytes(sys_._h, w, C.byref(by)))
+            ph["bytes"] = by.value
+            ph["gbs"] = by.value / (ms.value * 1e-3) / 1e9
+        phases[str(w)] = ph
     print(json.dumps({"case": f"kovasznay_re{args.re:g}_{args.n}x{args.n}", "precision": args.precision,
                       "precond": args.precond, "restart": args.restart, "mg_smooth": args.mg_smooth, "gs_passes": args.gs_passes,
-                      "unknowns": sys_.nInc, "nnz": sys_.nnz, "solves": runs}))
+                      "unknowns": sys_.nInc, "nnz": sys_.nnz, "solves": runs, "phases": phases}))
 
 
 if __name__ == "__main__":

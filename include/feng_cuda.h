@@ -109,7 +109,9 @@ typedef struct fe_cuda_options {
                              component (0 = a single V-cycle) */
   int32_t mg_smooth;      /* multigrid: Chebyshev smoother degree (1..6; 0 = default 1) */
   int32_t gs_passes;      /* mixed FGMRES Gram-Schmidt: 1 = one pass, a second when the update keeps
-                             less than a tenth of the norm; 2 = always two (0 = default 1) */
+                             less than a tenth of the norm; 2 = always two; 3 = as 1, the norm of
+                             the update taken as ||w||^2 - ||h||^2 from the dot pass and the next
+                             basis vector written by the update pass (0 = default 1) */
 } fe_cuda_options;
 
 /* Newton options (feNLSolverOptions, src/feNonLinearSolver.h:12-40) plus the
@@ -267,9 +269,9 @@ int fe_cuda_get_times(const fe_cuda_system *s, double *residual_ms, double *matr
                       double *factor_ms, double *solve_ms);
 int fe_cuda_reset_times(fe_cuda_system *s);
 /* Mean device milliseconds of one phase over `reps` runs timed with CUDA
- * events on the system stream, each run preceded by an L2 flush (a write of
- * flush_bytes): which = 0 residual assembly (all colors), 1 matrix assembly
- * (all colors), 2 SpMV with the system matrix, 3 one preconditioner
+ * events on the system stream, each run preceded by an L2 flush (a write, then a read, of
+ * flush_bytes): which = 0 residual assembly (all colors), 1 Jacobian assembly
+ * (a zeroed matrix, then the Jacobian), 2 SpMV with the system matrix, 3 one preconditioner
  * application, 4 one finest-level multigrid pre-smoothing pass (zero start
  * fused with the first Chebyshev step, both velocity components), 5 one
  * Gram-Schmidt dot pass of the mixed FGMRES over restart/2 basis vectors,
