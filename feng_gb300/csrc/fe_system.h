@@ -159,7 +159,8 @@ class SystemCUDA {
   FormCoeffs fc_{};
   RefTensors *dT_ = nullptr;
   int nq_ = 0;  // nodes of the system's quadrature rule
-  // Row-owned Taylor-Hood Jacobian (used when every row is shorter than 255).
+  // Row-owned Taylor-Hood FP32 Jacobian (used when every row is shorter
+  // than 255).
   RowAsm ra_;
   bool useRows_ = false;
   // setMatrixToZero is deferred: the next row-owned assembly overwrites the
