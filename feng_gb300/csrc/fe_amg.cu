@@ -259,12 +259,17 @@ __global__ void __launch_bounds__(256) k_cheb_first(int64_t n, const int32_t *__
 
 // Degree-1 post-smoothing from the prolongated y = x + P xc:
 // x = y + D^-1 (b - A y) / theta (x and y distinct).
-template <typename V, int LANES, int NV>
+// OUT (the finest level of a paired V-cycle whose result goes straight to
+// the caller's vector): component c of row i is written, times *scale, to
+// out[dof[c][i]] instead of x.
+template <typename V, int LANES, int NV, bool OUT>
 __global__ void __launch_bounds__(256) k_cheb_post(int64_t n, const int32_t *__restrict__ ia,
                                                    const int32_t *__restrict__ ja, const V *__restrict__ a,
                                                    const V *__restrict__ dinv, const V *__restrict__ b,
                                                    const V *__restrict__ y, V *__restrict__ x, V inv_theta,
-                                                   const int *__restrict__ skip)
+                                                   const int *__restrict__ skip, const int32_t *__restrict__ dofX,
+                                                   const int32_t *__restrict__ dofY, const double *__restrict__ scale,
+                                                   V *__restrict__ out)
 {
   if(skip && *skip) return;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
@@ -280,7 +285,87 @@ __global__ void __launch_bounds__(256) k_cheb_post(int64_t n, const int32_t *__r
       if(sub == c) ac = acc[c];
     const int64_t o = row * NV + sub;
     const V ri = dinv[row] * (b[o] - ac);
-    x[o] = y[o] + ri * inv_theta;
+    const V xo = y[o] + ri * inv_theta;
+    if(OUT) out[sub == 0 ? dofX[row] : dofY[row]] = xo * (V)*scale;
+    else x[o] = xo;
+  }
+}
+
+// k_cheb_first on the sliced-ELL copy of A: thread = row, both components.
+template <typename V, int NV>
+__global__ void __launch_bounds__(256) k_cheb_first_sell(int64_t n, const int32_t *__restrict__ sp,
+                                                         const int32_t *__restrict__ sc, const V *__restrict__ sv,
+                                                         const V *__restrict__ dinv, const V *__restrict__ b,
+                                                         V *__restrict__ dn, V *__restrict__ r, V *__restrict__ x,
+                                                         V inv_theta, V c1, V c2, const int *__restrict__ skip)
+{
+  if(skip && *skip) return;
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if(row >= n) return;
+  const int64_t sl = row >> 5;
+  const int lane = (int)(row & 31);
+  const int32_t base = sp[sl], len = (sp[sl + 1] - base) >> 5;
+  V acc[NV];
+#pragma unroll
+  for(int c = 0; c < NV; ++c) acc[c] = 0;
+#pragma unroll 4
+  for(int32_t k = 0; k < len; ++k) {
+    const int32_t e = base + (k << 5) + lane;
+    const int32_t j = __ldcs(sc + e);
+    const V ak = __ldcs(sv + e) * dinv[j];
+    const Vals<V, NV> bv = ldv<V, NV>(b, j);
+#pragma unroll
+    for(int c = 0; c < NV; ++c) acc[c] += ak * bv.v[c];
+  }
+  const V dv = dinv[row];
+#pragma unroll
+  for(int c = 0; c < NV; ++c) {
+    const int64_t o = row * NV + c;
+    const V r0 = dv * b[o];
+    const V di = r0 * inv_theta;
+    x[o] = di;
+    const V ri = r0 - dv * acc[c] * inv_theta;
+    r[o] = ri;
+    dn[o] = c1 * di + c2 * ri;
+  }
+}
+
+// k_cheb_post on the sliced-ELL copy of A: thread = row, both components.
+template <typename V, int NV, bool OUT>
+__global__ void __launch_bounds__(256) k_cheb_post_sell(int64_t n, const int32_t *__restrict__ sp,
+                                                        const int32_t *__restrict__ sc, const V *__restrict__ sv,
+                                                        const V *__restrict__ dinv, const V *__restrict__ b,
+                                                        const V *__restrict__ y, V *__restrict__ x, V inv_theta,
+                                                        const int *__restrict__ skip, const int32_t *__restrict__ dofX,
+                                                        const int32_t *__restrict__ dofY,
+                                                        const double *__restrict__ scale, V *__restrict__ out)
+{
+  if(skip && *skip) return;
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if(row >= n) return;
+  const int64_t sl = row >> 5;
+  const int lane = (int)(row & 31);
+  const int32_t base = sp[sl], len = (sp[sl + 1] - base) >> 5;
+  V acc[NV];
+#pragma unroll
+  for(int c = 0; c < NV; ++c) acc[c] = 0;
+#pragma unroll 4
+  for(int32_t k = 0; k < len; ++k) {
+    const int32_t e = base + (k << 5) + lane;
+    const int32_t j = __ldcs(sc + e);
+    const V ak = __ldcs(sv + e);
+    const Vals<V, NV> yv = ldv<V, NV>(y, j);
+#pragma unroll
+    for(int c = 0; c < NV; ++c) acc[c] += ak * yv.v[c];
+  }
+  const V dv = dinv[row];
+#pragma unroll
+  for(int c = 0; c < NV; ++c) {
+    const int64_t o = row * NV + c;
+    const V ri = dv * (b[o] - acc[c]);
+    const V xo = y[o] + ri * inv_theta;
+    if(OUT) out[c == 0 ? dofX[row] : dofY[row]] = xo * (V)*scale;
+    else x[o] = xo;
   }
 }
 
@@ -344,6 +429,46 @@ int upload_idx(int32_t **dst, const std::vector<int32_t> &src)
   return FE_OK;
 }
 
+// The sliced-ELL copy of A (AMGDevice::Lev::sellPtr).
+template <typename V>
+int upload_sell(const HostCSR &A, int32_t **sellPtr, int32_t **sellCol, void **sellVal)
+{
+  const int64_t n = A.n, ns = (n + 31) / 32;
+  std::vector<int32_t> ptr(ns + 1, 0);
+  for(int64_t sl = 0; sl < ns; ++sl) {
+    int64_t len = 0;
+    for(int64_t r = sl * 32; r < std::min<int64_t>(n, sl * 32 + 32); ++r) len = std::max<int64_t>(len, A.ia[r + 1] - A.ia[r]);
+    if(ptr[sl] + 32 * len >= (int64_t)INT32_MAX) return FE_OK;  // keep the CSR kernels
+    ptr[sl + 1] = (int32_t)(ptr[sl] + 32 * len);
+  }
+  std::vector<int32_t> col(std::max<int32_t>(ptr[ns], 1));
+  std::vector<V> val(col.size(), (V)0);
+  for(int64_t sl = 0; sl < ns; ++sl) {
+    const int32_t len = (ptr[sl + 1] - ptr[sl]) / 32;
+    for(int lane = 0; lane < 32; ++lane) {
+      const int64_t r = sl * 32 + lane;
+      for(int32_t k = 0; k < len; ++k) {
+        const int64_t e = ptr[sl] + (int64_t)k * 32 + lane;
+        const int64_t src = r < n ? A.ia[r] + k : -1;
+        if(r < n && src < A.ia[r + 1]) {
+          col[e] = (int32_t)A.ja[src];
+          val[e] = (V)A.a[src];
+        } else {
+          col[e] = (int32_t)std::min<int64_t>(r, n - 1);  // padding: value 0 on an existing column
+          val[e] = (V)0;
+        }
+      }
+    }
+  }
+  CKA(cudaMalloc(sellPtr, sizeof(int32_t) * ptr.size()));
+  CKA(cudaMalloc(sellCol, sizeof(int32_t) * col.size()));
+  CKA(cudaMalloc(sellVal, sizeof(V) * val.size()));
+  CKA(cudaMemcpy(*sellPtr, ptr.data(), sizeof(int32_t) * ptr.size(), cudaMemcpyHostToDevice));
+  CKA(cudaMemcpy(*sellCol, col.data(), sizeof(int32_t) * col.size(), cudaMemcpyHostToDevice));
+  CKA(cudaMemcpy(*sellVal, val.data(), sizeof(V) * val.size(), cudaMemcpyHostToDevice));
+  return FE_OK;
+}
+
 int lanes_for(const HostCSR &M)
 {
   const double avg = M.n ? (double)M.nnz() / M.n : 0;
@@ -360,6 +485,7 @@ AMGDevice::~AMGDevice()
     cudaFree(L.Aia); cudaFree(L.Aja); cudaFree(L.Pia); cudaFree(L.Pja); cudaFree(L.Ria); cudaFree(L.Rja);
     cudaFree(L.Aa); cudaFree(L.Pa); cudaFree(L.Ra); cudaFree(L.dinv); cudaFree(L.diag);
     cudaFree(L.x); cudaFree(L.b); cudaFree(L.r); cudaFree(L.d0); cudaFree(L.d1);
+    cudaFree(L.sellPtr); cudaFree(L.sellCol); cudaFree(L.sellVal);
   }
   cudaFree(coarseInv_);
 }
@@ -383,6 +509,9 @@ int AMGDevice::upload(const AMGHierarchy &H, const AMGParams &p, int fp32, cudaS
     FE_TRY(upload_idx(&L.Aia, h.A.ia));
     FE_TRY(upload_idx(&L.Aja, h.A.ja));
     FE_TRY(fp32 ? upload_vec<float>(&L.Aa, h.A.a) : upload_vec<double>(&L.Aa, h.A.a));
+    if(l == 0 && h.A.n >= 32 * 152)
+      FE_TRY(fp32 ? upload_sell<float>(h.A, &L.sellPtr, &L.sellCol, &L.sellVal)
+                  : upload_sell<double>(h.A, &L.sellPtr, &L.sellCol, &L.sellVal));
     FE_TRY(fp32 ? upload_vec<float>(&L.dinv, h.dinv) : upload_vec<double>(&L.dinv, h.dinv));
     std::vector<double> dg(h.dinv.size());
     for(size_t i = 0; i < dg.size(); ++i) dg[i] = 1.0 / h.dinv[i];
@@ -411,9 +540,10 @@ int AMGDevice::upload(const AMGHierarchy &H, const AMGParams &p, int fp32, cudaS
 // pre-smoothing, whose residual is restricted); otherwise the last step only
 // moves x.
 template <typename V, int NV>
-static void chebyshev(int lanes, int64_t n, const int32_t *ia, const int32_t *ja, const V *a, const V *dinv,
-                      const V *b, V *x, V *r, V *d0, V *d1, double lmax, const AMGParams &p, bool zeroStart,
-                      bool needResidual, cudaStream_t s, const int *skip)
+static void chebyshev(int lanes, int64_t n, const int32_t *ia, const int32_t *ja, const V *a, const int32_t *sp,
+                      const int32_t *sc, const V *sv, const V *dinv, const V *b, V *x, V *r, V *d0, V *d1,
+                      double lmax, const AMGParams &p, bool zeroStart, bool needResidual, cudaStream_t s,
+                      const int *skip)
 {
   // Chebyshev iteration on D^-1 A over [low, high] * lmax (Saad, Alg. 12.1).
   const double lo = p.chebyLow * lmax, hi = p.chebyHigh * lmax;
@@ -427,7 +557,8 @@ static void chebyshev(int lanes, int64_t n, const int32_t *ia, const int32_t *ja
     const double rhoN = 1.0 / (2.0 * sigma - rho);
     const V c1 = (V)(rhoN * rho), c2 = (V)(2.0 * rhoN / delta);
     const V it = (V)(1.0 / theta);
-    if(lanes == 16) (k_cheb_first<V, 16, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, dn, r, x, it, c1, c2, skip), ::feng::count_launch());
+    if(sp) (k_cheb_first_sell<V, NV><<<grid(n), 256, 0, s>>>(n, sp, sc, sv, dinv, b, dn, r, x, it, c1, c2, skip), ::feng::count_launch());
+    else if(lanes == 16) (k_cheb_first<V, 16, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, dn, r, x, it, c1, c2, skip), ::feng::count_launch());
     else if(lanes == 8) (k_cheb_first<V, 8, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, dn, r, x, it, c1, c2, skip), ::feng::count_launch());
     else (k_cheb_first<V, 4, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, dn, r, x, it, c1, c2, skip), ::feng::count_launch());
     rho = rhoN;
@@ -466,8 +597,8 @@ void AMGDevice::vcycle_t(int l, const V *b, V *x)
   }
   Lev &C = lv_[l + 1];
   const V *A = (const V *)L.Aa;
-  chebyshev<V, NV>(L.lanesA, L.n, L.Aia, L.Aja, A, (const V *)L.dinv, b, x, (V *)L.r, (V *)L.d0, (V *)L.d1,
-                   L.lmax, p_, true, true, s_, skip_);
+  chebyshev<V, NV>(L.lanesA, L.n, L.Aia, L.Aja, A, L.sellPtr, L.sellCol, (const V *)L.sellVal, (const V *)L.dinv, b,
+                   x, (V *)L.r, (V *)L.d0, (V *)L.d1, L.lmax, p_, true, true, s_, skip_);
   // Chebyshev keeps r = D^-1 (b - A x): restrict the residual D r directly
   // (no extra pass over A).
   csr<V, 3, NV>(L.lanesR, C.n, L.Ria, L.Rja, (const V *)L.Ra, (const V *)L.r, (const V *)L.diag, (V *)C.b, s_,
@@ -482,20 +613,59 @@ void AMGDevice::vcycle_t(int l, const V *b, V *x)
     const V it = (V)(1.0 / theta);
     const int g = grid(L.n * L.lanesA);
     const V *dinv = (const V *)L.dinv;
-    if(L.lanesA == 16) (k_cheb_post<V, 16, NV><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_), ::feng::count_launch());
-    else if(L.lanesA == 8) (k_cheb_post<V, 8, NV><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_), ::feng::count_launch());
-    else (k_cheb_post<V, 4, NV><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_), ::feng::count_launch());
+    if(L.sellPtr) {
+      const V *sv = (const V *)L.sellVal;
+      if(l == 0 && NV == 2 && out_.z) {
+        (k_cheb_post_sell<V, NV, true><<<grid(L.n), 256, 0, s_>>>(L.n, L.sellPtr, L.sellCol, sv, dinv, b, y, x, it, skip_,
+                                                                 out_.dofX, out_.dofY, out_.scale, (V *)out_.z),
+         ::feng::count_launch());
+        outWritten_ = true;
+      } else {
+        (k_cheb_post_sell<V, NV, false><<<grid(L.n), 256, 0, s_>>>(L.n, L.sellPtr, L.sellCol, sv, dinv, b, y, x, it,
+                                                                  skip_, nullptr, nullptr, nullptr, nullptr),
+         ::feng::count_launch());
+      }
+      return;
+    }
+    if(l == 0 && NV == 2 && out_.z) {
+      const int32_t *dx = out_.dofX, *dy = out_.dofY;
+      const double *sc = out_.scale;
+      V *z = (V *)out_.z;
+      if(L.lanesA == 16) (k_cheb_post<V, 16, NV, true><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, dx, dy, sc, z), ::feng::count_launch());
+      else if(L.lanesA == 8) (k_cheb_post<V, 8, NV, true><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, dx, dy, sc, z), ::feng::count_launch());
+      else (k_cheb_post<V, 4, NV, true><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, dx, dy, sc, z), ::feng::count_launch());
+      outWritten_ = true;
+      return;
+    }
+    if(L.lanesA == 16) (k_cheb_post<V, 16, NV, false><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, nullptr, nullptr, nullptr, nullptr), ::feng::count_launch());
+    else if(L.lanesA == 8) (k_cheb_post<V, 8, NV, false><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, nullptr, nullptr, nullptr, nullptr), ::feng::count_launch());
+    else (k_cheb_post<V, 4, NV, false><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, nullptr, nullptr, nullptr, nullptr), ::feng::count_launch());
     return;
   }
   csr<V, 2, NV>(L.lanesP, L.n, L.Pia, L.Pja, (const V *)L.Pa, (const V *)C.x, nullptr, x, s_, skip_);
-  chebyshev<V, NV>(L.lanesA, L.n, L.Aia, L.Aja, A, (const V *)L.dinv, b, x, (V *)L.r, (V *)L.d0, (V *)L.d1,
-                   L.lmax, p_, false, false, s_, skip_);
+  chebyshev<V, NV>(L.lanesA, L.n, L.Aia, L.Aja, A, L.sellPtr, L.sellCol, (const V *)L.sellVal, (const V *)L.dinv, b,
+                   x, (V *)L.r, (V *)L.d0, (V *)L.d1, L.lmax, p_, false, false, s_, skip_);
 }
 
 void AMGDevice::vcycle64(const double *b, double *x) { vcycle_t<double, 1>(0, b, x); }
 void AMGDevice::vcycle32(const float *b, float *x) { vcycle_t<float, 1>(0, b, x); }
-void AMGDevice::vcycle2_64(const double *b, double *x) { vcycle_t<double, 2>(0, b, x); }
-void AMGDevice::vcycle2_32(const float *b, float *x) { vcycle_t<float, 2>(0, b, x); }
+bool AMGDevice::vcycle2_64(const double *b, double *x, const OutMap *om)
+{
+  out_ = om ? *om : OutMap();
+  outWritten_ = false;
+  vcycle_t<double, 2>(0, b, x);
+  out_ = OutMap();
+  return outWritten_;
+}
+
+bool AMGDevice::vcycle2_32(const float *b, float *x, const OutMap *om)
+{
+  out_ = om ? *om : OutMap();
+  outWritten_ = false;
+  vcycle_t<float, 2>(0, b, x);
+  out_ = OutMap();
+  return outWritten_;
+}
 
 void AMGDevice::fineStep2()
 {
@@ -509,7 +679,10 @@ void AMGDevice::fineStep2()
     const V *a = (const V *)L.Aa, *dinv = (const V *)L.dinv, *b = (const V *)L.d0;
     V *dn = (V *)L.d1, *r = (V *)L.r, *x = (V *)L.x;
     const V it = (V)0.5, c1 = (V)0.5, c2 = (V)0.5;
-    if(L.lanesA == 16) (k_cheb_first<V, 16, 2><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, a, dinv, b, dn, r, x, it, c1, c2, skip_), ::feng::count_launch());
+    if(L.sellPtr)
+      (k_cheb_first_sell<V, 2><<<grid(L.n), 256, 0, s_>>>(L.n, L.sellPtr, L.sellCol, (const V *)L.sellVal, dinv, b, dn,
+                                                          r, x, it, c1, c2, skip_), ::feng::count_launch());
+    else if(L.lanesA == 16) (k_cheb_first<V, 16, 2><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, a, dinv, b, dn, r, x, it, c1, c2, skip_), ::feng::count_launch());
     else if(L.lanesA == 8) (k_cheb_first<V, 8, 2><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, a, dinv, b, dn, r, x, it, c1, c2, skip_), ::feng::count_launch());
     else (k_cheb_first<V, 4, 2><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, a, dinv, b, dn, r, x, it, c1, c2, skip_), ::feng::count_launch());
   };

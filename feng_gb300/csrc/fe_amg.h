@@ -60,8 +60,18 @@ class AMGDevice {
   void vcycle32(const float *b, float *x);
   // The same V-cycle on two right-hand sides stored interleaved
   // (b[2 i + c], component c of row i): one pass over each operator.
-  void vcycle2_64(const double *b, double *x);
-  void vcycle2_32(const float *b, float *x);
+  // The caller's vector for the result of a paired V-cycle: component c of
+  // finest row i goes, times *scale, to z[dofX[i]] (c = 0) or z[dofY[i]].
+  struct OutMap {
+    const int32_t *dofX = nullptr, *dofY = nullptr;
+    const double *scale = nullptr;
+    void *z = nullptr;
+  };
+  // Both components at once (x, b interleaved).  With om, the finest
+  // post-smoothing pass writes the result through om when it can (then
+  // returns true; x does not hold the result), otherwise x holds it.
+  bool vcycle2_64(const double *b, double *x, const OutMap *om = nullptr);
+  bool vcycle2_32(const float *b, float *x, const OutMap *om = nullptr);
   // y = A x with the finest operator.
   void spmv64(const double *x, double *y);
   void spmv32(const float *x, float *y);
@@ -84,8 +94,17 @@ class AMGDevice {
     void *x = nullptr, *b = nullptr, *r = nullptr, *d0 = nullptr, *d1 = nullptr;
     double lmax = 0;
     int lanesA = 4, lanesP = 4, lanesR = 4;
+    // Sliced-ELL copy of A (slices of 32 rows, each padded to its longest
+    // row with the row's own column and value 0, entries column-major in
+    // the slice): one thread per row, every load a full line.  Built for
+    // the finest level only.
+    int32_t *sellPtr = nullptr;  // [nSlices + 1] first entry of each slice
+    int32_t *sellCol = nullptr;
+    void *sellVal = nullptr;
   };
   template <typename V, int NV> void vcycle_t(int l, const V *b, V *x);
+  OutMap out_;
+  bool outWritten_ = false;
   std::vector<Lev> lv_;
   void *coarseInv_ = nullptr;
   int64_t nCoarse_ = 0, n0_ = 0, nnz0_ = 0;

@@ -467,6 +467,213 @@ __global__ void __launch_bounds__(EPB * 6) k_residual_th_q(DeviceMesh dm, FormCo
   }
 }
 
+// ---------------------------------------------------------------------------
+// Double-float arithmetic: a value is hi + lo, two floats (~44-bit
+// significand) computed on the FP32 pipes.  Knuth's error-free sum
+// (TwoSum, The Art of Computer Programming vol. 2, 4.2.2), Dekker's product
+// ("A floating-point technique for extending the available precision",
+// Numer. Math. 18, 1971) with the error of hi * hi from a fused
+// multiply-add, and the pair addition of Dekker (the same paper) as in
+// Bailey's double-double library, whose error is relative to the operands (u^2 |x| + u^2 |y|,
+// u = 2^-24): enough for element sums, which do not cancel to the size of
+// a converged residual (that cancellation happens in the FP64 sums across
+// elements).  Every operation is an explicit round-to-nearest intrinsic so
+// that no multiply and add are contracted into one.
+// ---------------------------------------------------------------------------
+struct dfl {
+  float hi, lo;
+};
+
+__device__ __forceinline__ dfl df_from(double x)
+{
+  const float h = __double2float_rn(x);
+  return {h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ double df_to(dfl a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ dfl df_zero() { return {0.f, 0.f}; }
+__device__ __forceinline__ dfl df_neg(dfl a) { return {-a.hi, -a.lo}; }
+// s + e with |a| >= |b|
+__device__ __forceinline__ dfl df_fast2(float a, float b)
+{
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ dfl df_add(dfl x, dfl y)
+{
+  const float s = __fadd_rn(x.hi, y.hi);
+  const float v = __fsub_rn(s, x.hi);
+  float e = __fadd_rn(__fsub_rn(x.hi, __fsub_rn(s, v)), __fsub_rn(y.hi, v));
+  e = __fadd_rn(e, __fadd_rn(x.lo, y.lo));
+  return df_fast2(s, e);
+}
+__device__ __forceinline__ dfl df_sub(dfl x, dfl y) { return df_add(x, df_neg(y)); }
+__device__ __forceinline__ dfl df_mul(dfl x, dfl y)
+{
+  const float p = __fmul_rn(x.hi, y.hi);
+  float e = __fmaf_rn(x.hi, y.hi, -p);
+  e = __fmaf_rn(x.hi, y.lo, e);
+  e = __fmaf_rn(x.lo, y.hi, e);
+  return df_fast2(p, e);
+}
+__device__ __forceinline__ dfl df_fma(dfl a, dfl b, dfl c) { return df_add(df_mul(a, b), c); }
+
+// k_residual_th_q in double-float: the same 7-node quadrature, the same
+// sums in the same order; sources (non-polynomial) and the scatter in FP64.
+// Block: 32 elements x 7 warps.  Quadrature node q is warp q; then warps
+// 0-5 form the two velocity rows of P2 function a = warp, warp 6 the three
+// pressure rows.  Inputs are already float pairs (no FP64 arithmetic but
+// the source and the final scatter).
+__global__ void __launch_bounds__(EPB * 7) k_residual_th_df(DeviceMesh dm, FormCoeffs fc,
+                                                           const RefTensors *__restrict__ gT,
+                                                           const float2 *__restrict__ up,
+                                                           const float2 *__restrict__ udp, double t,
+                                                           int64_t nInc, double *__restrict__ rhs,
+                                                           int64_t begin, int64_t end)
+{
+  __shared__ dfl sU[12][EPB];
+  __shared__ dfl sUd[12][EPB];
+  __shared__ dfl sP[3][EPB];
+  __shared__ dfl sG[5][EPB];
+  __shared__ dfl sQ[7][7][EPB];
+  __shared__ double sF[2][16][EPB];
+  __shared__ int32_t sA[15][EPB];
+  const int lane = threadIdx.x, a = threadIdx.y;
+  const int64_t p = begin + (int64_t)blockIdx.x * EPB + lane;
+  const bool live = p < end;
+  const int64_t nE = dm.nElm;
+  const bool hasSrc = fc.srcKind != SRC_NONE;
+  if(live) {
+    for(int i = a; i < 15; i += 7) {
+      int32_t d = dm.adr[(int64_t)i * nE + p];
+      sA[i][lane] = d;
+      const float2 v = up[d];
+      if(i < 12) {
+        sU[i][lane] = {v.x, v.y};
+        if(fc.hasMass) {
+          const float2 w = udp[d];
+          sUd[i][lane] = {w.x, w.y};
+        } else {
+          sUd[i][lane] = df_zero();
+        }
+      } else {
+        sP[i - 12][lane] = {v.x, v.y};
+      }
+    }
+    if(a < 5) {
+      const float2 g = dm.geoPair[(int64_t)a * nE + p];
+      sG[a][lane] = {g.x, g.y};
+    }
+  }
+  const int nq = gT->nq;
+  if(hasSrc && live) {
+    const double x0 = dm.xy[0 * nE + p], y0 = dm.xy[1 * nE + p], x1 = dm.xy[2 * nE + p],
+                 y1 = dm.xy[3 * nE + p], x2 = dm.xy[4 * nE + p], y2 = dm.xy[5 * nE + p];
+    for(int q = a; q < nq; q += 7) {
+      const double r = gT->qr[q], s = gT->qs[q];
+      const double x = x0 * (1. - r - s) + x1 * r + x2 * s;
+      const double y = y0 * (1. - r - s) + y1 * r + y2 * s;
+      double f[2];
+      source_value(fc.srcKind, fc.srcParam, x, y, f);
+      sF[0][q][lane] = f[0];
+      sF[1][q][lane] = f[1];
+    }
+  }
+  __syncthreads();
+  if(live) {
+    const dfl G[2][2] = {{sG[0][lane], sG[1][lane]}, {sG[2][lane], sG[3][lane]}};
+    const dfl J = sG[4][lane];
+    const dfl conv = {fc.pair[0][0], fc.pair[0][1]}, mass = {fc.pair[1][0], fc.pair[1][1]},
+              sig = {fc.pair[2][0], fc.pair[2][1]}, mu = {fc.pair[3][0], fc.pair[3][1]},
+              divu = {fc.pair[4][0], fc.pair[4][1]};
+    const int q = a;  // one quadrature node per warp
+    dfl uq[2] = {df_zero(), df_zero()}, ur[2] = {df_zero(), df_zero()}, us[2] = {df_zero(), df_zero()},
+        udq[2] = {df_zero(), df_zero()};
+    for(int b = 0; b < 6; ++b) {
+      const dfl ph = {gT->phi5h[q][b], gT->phi5l[q][b]}, dr = {gT->dr5h[q][b], gT->dr5l[q][b]},
+                ds = {gT->ds5h[q][b], gT->ds5l[q][b]};
+      for(int m = 0; m < 2; ++m) {
+        const dfl v = sU[2 * b + m][lane];
+        uq[m] = df_fma(ph, v, uq[m]);
+        ur[m] = df_fma(dr, v, ur[m]);
+        us[m] = df_fma(ds, v, us[m]);
+        if(fc.hasMass) udq[m] = df_fma(ph, sUd[2 * b + m][lane], udq[m]);
+      }
+    }
+    dfl gu[2][2];  // gu[k][m] = d_k u_m
+    for(int k = 0; k < 2; ++k)
+      for(int m = 0; m < 2; ++m) gu[k][m] = df_add(df_mul(G[0][k], ur[m]), df_mul(G[1][k], us[m]));
+    dfl pq = df_zero();
+    for(int j = 0; j < 3; ++j) pq = df_fma({gT->psi5h[q][j], gT->psi5l[q][j]}, sP[j][lane], pq);
+    const dfl wJ = df_mul({gT->w5h[q], gT->w5l[q]}, J);
+    for(int m = 0; m < 2; ++m) {
+      dfl f = df_zero();
+      if(fc.hasConv) f = df_sub(f, df_mul(conv, df_add(df_mul(uq[0], gu[0][m]), df_mul(uq[1], gu[1][m]))));
+      if(fc.hasMass) f = df_sub(f, df_mul(mass, udq[m]));
+      sQ[q][m][lane] = df_mul(wJ, f);
+    }
+    dfl Fg[2][2] = {{df_zero(), df_zero()}, {df_zero(), df_zero()}};  // coefficient of d_k phi_a, component m
+    if(fc.hasSigma) {
+      const dfl sw = df_neg(df_mul(sig, wJ));
+      for(int k = 0; k < 2; ++k)
+        for(int m = 0; m < 2; ++m) {
+          const dfl in = df_sub(k == m ? pq : df_zero(), df_mul(mu, df_add(gu[k][m], gu[m][k])));
+          Fg[k][m] = df_mul(sw, in);
+        }
+    }
+    for(int r = 0; r < 2; ++r)
+      for(int m = 0; m < 2; ++m)
+        sQ[q][2 + 2 * r + m][lane] = df_add(df_mul(G[r][0], Fg[0][m]), df_mul(G[r][1], Fg[1][m]));
+    sQ[q][6][lane] = fc.hasDivu ? df_neg(df_mul(df_mul(divu, wJ), df_add(gu[0][0], gu[1][1]))) : df_zero();
+  }
+  __syncthreads();
+  if(!live) return;
+  if(a == 6) {
+    // the three pressure rows
+    if(!fc.hasDivu) return;
+    for(int j = 0; j < 3; ++j) {
+      dfl acc = df_zero();
+      for(int q = 0; q < 7; ++q) acc = df_fma(sQ[q][6][lane], {gT->psi5h[q][j], gT->psi5l[q][j]}, acc);
+      const int32_t d = sA[12 + j][lane];
+      if(d < nInc) atomicAdd(rhs + d, df_to(acc));
+    }
+    return;
+  }
+  dfl be[2] = {df_zero(), df_zero()};
+  for(int q = 0; q < 7; ++q) {
+    const dfl ph = {gT->phi5h[q][a], gT->phi5l[q][a]}, dr = {gT->dr5h[q][a], gT->dr5l[q][a]},
+              ds = {gT->ds5h[q][a], gT->ds5l[q][a]};
+    for(int m = 0; m < 2; ++m)
+      be[m] = df_add(be[m], df_add(df_add(df_mul(sQ[q][m][lane], ph), df_mul(sQ[q][2 + m][lane], dr)),
+                                   df_mul(sQ[q][4 + m][lane], ds)));
+  }
+  double bd[2] = {df_to(be[0]), df_to(be[1])};
+  if(hasSrc) {
+    // Be_(a,m) -= f . phi jac w   (feVectorSysElm.cpp:112-130), the form's own rule, in FP64
+    const double J = dm.geo[(int64_t)4 * nE + p];
+    double acc[2] = {0., 0.};
+    for(int q = 0; q < nq; ++q) {
+      const double pw = gT->phi[q][a] * gT->qw[q];
+      acc[0] += sF[0][q][lane] * pw;
+      acc[1] += sF[1][q][lane] * pw;
+    }
+    bd[0] -= fc.srcCoeff * acc[0] * J;
+    bd[1] -= fc.srcCoeff * acc[1] * J;
+  }
+  for(int m = 0; m < 2; ++m) {
+    const int32_t d = sA[2 * a + m][lane];
+    if(d < nInc) atomicAdd(rhs + d, bd[m]);  // one contribution per DOF and color
+  }
+}
+
+__global__ void k_split_pairs(int64_t n, const double *__restrict__ x, float2 *__restrict__ out)
+{
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    const float h = __double2float_rn(v);
+    out[i] = make_float2(h, __double2float_rn(v - (double)h));
+  }
+}
+
 // Local entry k = a*18 + j of the staged rows (2a+m) of a Taylor-Hood
 // element matrix -> index of the element-to-nonzero map (i = 2a+m; j < 12
 // velocity column j, 12 <= j < 15 pressure column j-12, 15 <= j < 18 the
@@ -801,6 +1008,21 @@ void launch_matrix_th_rows_f64(const RowAsm &ra, const FormCoeffs &fc, const Ref
   if(ra.nBlocks < 1) return;
   (k_matrix_th_rows<double><<<ra.nBlocks, 256, ra.capBytes, s>>>(ra, fc, dT, c0, values, accumulate),
    ::feng::count_launch());
+}
+
+void launch_assemble_residual_df(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
+                                 const float2 *uPair, const float2 *udotPair, double t, int64_t nInc,
+                                 double *rhs, int64_t begin, int64_t end, cudaStream_t s)
+{
+  if(end <= begin) return;
+  (k_residual_th_df<<<nblocks(begin, end), dim3(EPB, 7), 0, s>>>(dm, fc, dT, uPair, udotPair, t, nInc, rhs, begin,
+                                                                 end), ::feng::count_launch());
+}
+
+void launch_split_pairs(int64_t n, const double *x, float2 *out, cudaStream_t s)
+{
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 4096));
+  (k_split_pairs<<<g, 256, 0, s>>>(n, x, out), ::feng::count_launch());
 }
 
 void launch_assemble_residual(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,

@@ -49,6 +49,10 @@ struct RefTensors {
   // is itself exact to degree 5 (exact5), so both give the exact integrals.
   int exact5;
   double w5[7], phi5[7][6], dr5[7][6], ds5[7][6], psi5[7][3];
+  // The same 7-node rule as float pairs (hi + lo, lo = the double minus hi
+  // rounded to float) for the double-float residual.
+  float w5h[7], w5l[7], phi5h[7][6], phi5l[7][6], dr5h[7][6], dr5l[7][6], ds5h[7][6], ds5l[7][6];
+  float psi5h[7][3], psi5l[7][3];
 };
 
 // Constant coefficients of the fused forms (0 = form absent).
@@ -64,6 +68,9 @@ struct FormCoeffs {
   int srcKind;      // SourceKind of SOURCE / VECTOR_SOURCE
   double srcParam[4];
   double srcCoeff;  // multiplies the source (1 when present)
+  // conv, mass, sigma, mu, divu as float pairs (hi, lo) for the
+  // double-float residual
+  float pair[5][2];
 };
 
 struct DeviceMesh {
@@ -75,6 +82,7 @@ struct DeviceMesh {
   double *geo = nullptr;     // [5][nElm]     G00 G01 G10 G11 |J|   (G[r][k] = d r / d x_k)
   double *xy = nullptr;      // [6][nElm]     x0 y0 x1 y1 x2 y2
   int32_t *map = nullptr;    // [nloc*nloc][nElm] CSR position or -1
+  float2 *geoPair = nullptr; // [5][nElm] geo as float pairs (double-float residual)
 };
 
 // Row-owned Jacobian assembly of Taylor-Hood systems: one thread builds one
@@ -109,9 +117,19 @@ void launch_matrix_th_rows_f64(const RowAsm &ra, const FormCoeffs &fc, const Ref
 // order, accumulated into rhs with feNG's sign (rhs = sum of element Be).
 // exact5: the rule integrates degree 5 exactly (RefTensors::exact5), so the
 // Taylor-Hood residual may use the 7-node quadrature kernel.
+// dfloat: the Taylor-Hood 7-node kernel in double-float arithmetic (pairs of
+// floats, ~44-bit significands, on the FP32 pipes) instead of FP64.
 void launch_assemble_residual(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
                               const double *u, const double *udot, double t, int64_t nInc,
                               double *rhs, int64_t begin, int64_t end, cudaStream_t s, int exact5);
+// The Taylor-Hood 7-node residual in double-float arithmetic (pairs of
+// floats, ~44-bit significands, on the FP32 pipes) from u and u-dot split
+// into float pairs (launch_split_pairs) and dm.geoPair.
+void launch_assemble_residual_df(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
+                                 const float2 *uPair, const float2 *udotPair, double t, int64_t nInc,
+                                 double *rhs, int64_t begin, int64_t end, cudaStream_t s);
+// out[i] = (hi, lo) of x[i]: hi = x rounded to float, lo = the rest rounded.
+void launch_split_pairs(int64_t n, const double *x, float2 *out, cudaStream_t s);
 // Jacobian of the fused forms, in double or float.
 void launch_assemble_matrix_f64(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
                                 const double *u, double c0, double *values, int64_t begin,

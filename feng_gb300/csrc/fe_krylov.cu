@@ -947,6 +947,7 @@ struct Ws {
 Krylov::~Krylov()
 {
   cudaFree(V_); cudaFree(Z_); cudaFree(Z32_); cudaFree(V32_); cudaFree(v32_); cudaFree(w32_); cudaFree(zeroFlag_);
+  cudaFree(sellPtr_); cudaFree(sellCol_); cudaFree(sellSrc_); cudaFree(sellVal_);
   cudaFree(w_); cudaFree(r_); cudaFree(t_); cudaFree(p_); cudaFree(q_);
   cudaFree(diag_); cudaFree(diag32_); cudaFree(red_); cudaFree(dsum_);
   cudaFreeHost(hred_);
@@ -1016,6 +1017,7 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
       CK(cudaMalloc(&Z32_, sizeof(float) * ld32_ * m));
       CK(cudaMemset(V32_, 0, sizeof(float) * ld32_ * (m + 1)));
       CK(cudaMemset(Z32_, 0, sizeof(float) * ld32_ * m));
+      if(n_ >= 32 * 152) FE_TRY(build_sell());
     } else {
       CK(cudaMalloc(&V_, sizeof(double) * n_ * (m + 1)));
       CK(cudaMalloc(&Z_, sizeof(double) * n_ * m));
@@ -1113,11 +1115,88 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
   return FE_OK;
 }
 
+namespace {
+// y = A x on the sliced-ELL copy, FP32, thread = row (rows of a warp are one
+// slice, so every column and value load is one full line).
+__global__ void __launch_bounds__(256) k_spmv_sell(int64_t n, const int32_t *__restrict__ sp,
+                                                   const int32_t *__restrict__ sc, const float *__restrict__ sv,
+                                                   const float *__restrict__ x, float *__restrict__ y,
+                                                   const int *__restrict__ done)
+{
+  if(done && *done) return;
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if(row >= n) return;
+  const int64_t sl = row >> 5;
+  const int lane = (int)(row & 31);
+  const int32_t base = sp[sl], len = (sp[sl + 1] - base) >> 5;
+  float acc = 0.f;
+#pragma unroll 4
+  for(int32_t k = 0; k < len; ++k) {
+    const int32_t e = base + (k << 5) + lane;
+    acc = fmaf(__ldcs(sv + e), x[__ldcs(sc + e)], acc);
+  }
+  y[row] = acc;
+}
+
+// sliced-ELL values from the CSR values (padding: 0)
+__global__ void k_sell_gather(int64_t m, const int32_t *__restrict__ src, const float *__restrict__ a,
+                              float *__restrict__ out)
+{
+  for(int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t k = src[e];
+    out[e] = k >= 0 ? a[k] : 0.f;
+  }
+}
+}  // namespace
+
+int Krylov::build_sell()
+{
+  std::vector<int32_t> ia(n_ + 1), ja(A_.nnz);
+  CK(cudaMemcpy(ia.data(), A_.ia, sizeof(int32_t) * (n_ + 1), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(ja.data(), A_.ja, sizeof(int32_t) * A_.nnz, cudaMemcpyDeviceToHost));
+  const int64_t ns = (n_ + 31) / 32;
+  std::vector<int32_t> ptr(ns + 1, 0);
+  for(int64_t sl = 0; sl < ns; ++sl) {
+    int64_t len = 0;
+    for(int64_t r = sl * 32; r < std::min<int64_t>(n_, sl * 32 + 32); ++r) len = std::max<int64_t>(len, ia[r + 1] - ia[r]);
+    if(ptr[sl] + 32 * len >= (int64_t)INT32_MAX) return FE_OK;  // CSR only
+    ptr[sl + 1] = (int32_t)(ptr[sl] + 32 * len);
+  }
+  sellN_ = ptr[ns];
+  std::vector<int32_t> col(std::max<int64_t>(sellN_, 1)), src(col.size(), -1);
+  for(int64_t sl = 0; sl < ns; ++sl) {
+    const int32_t len = (ptr[sl + 1] - ptr[sl]) / 32;
+    for(int lane = 0; lane < 32; ++lane) {
+      const int64_t r = sl * 32 + lane;
+      for(int32_t k = 0; k < len; ++k) {
+        const int64_t e = ptr[sl] + (int64_t)k * 32 + lane;
+        if(r < n_ && ia[r] + k < ia[r + 1]) {
+          col[e] = ja[ia[r] + k];
+          src[e] = ia[r] + k;
+        } else {
+          col[e] = (int32_t)std::min<int64_t>(r, n_ - 1);  // padding: value 0 on an existing column
+        }
+      }
+    }
+  }
+  CK(cudaMalloc(&sellPtr_, sizeof(int32_t) * ptr.size()));
+  CK(cudaMalloc(&sellCol_, sizeof(int32_t) * col.size()));
+  CK(cudaMalloc(&sellSrc_, sizeof(int32_t) * src.size()));
+  CK(cudaMalloc(&sellVal_, sizeof(float) * col.size()));
+  CK(cudaMemcpy(sellPtr_, ptr.data(), sizeof(int32_t) * ptr.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(sellCol_, col.data(), sizeof(int32_t) * col.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(sellSrc_, src.data(), sizeof(int32_t) * src.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemset(sellVal_, 0, sizeof(float) * col.size()));
+  return FE_OK;
+}
+
 int Krylov::factor(const double *values64, const float *values32)
 {
   factoredOk_ = false;
   cur64_ = values64;
   cur32_ = values32;
+  if(opt.mixed && sellVal_ && values32)
+    (k_sell_gather<<<grid_for(sellN_, 256, 4096), 256, 0, s_>>>(sellN_, sellSrc_, values32, sellVal_), ::feng::count_launch());
   if(opt.precond == 0) { factoredOk_ = true; return FE_OK; }
   if(opt.precond == 3 || opt.precond == 4) {
     FE_TRY(factor_mg(values64, values32));
@@ -1182,6 +1261,7 @@ void Krylov::precond32(const float *r, float *z, const int *done)
   }
 }
 
+
 template <typename VA, typename VX, typename VY, typename ACC, bool RESID>
 static void spmv_launch(int lanes, int64_t n, const DeviceCSR &A, const VA *a, const VX *x,
                         const double *b, VY *y, const int *done, cudaStream_t s)
@@ -1207,6 +1287,17 @@ void Krylov::spmv32(const float *values, const double *x, double *y)
   const int gv = grid_for(n_, 256, 2048);
   (k_to_f32<<<gv, 256, 0, s_>>>(n_, x, v32_, nullptr), ::feng::count_launch());
   spmv_launch<float, float, double, float, false>(lanes_, n_, A_, values, v32_, nullptr, y, nullptr, s_);
+}
+
+int Krylov::spmvHot()
+{
+  if(!opt.mixed || !Z32_) {
+    set_error("no mixed-precision FGMRES");
+    return FE_INVALID_ARG;
+  }
+  if(sellVal_) (k_spmv_sell<<<grid_for(n_, 256, 1 << 20), 256, 0, s_>>>(n_, sellPtr_, sellCol_, sellVal_, Z32_, w32_, nullptr), ::feng::count_launch());
+  else if(cur32_) spmv_launch<float, float, float, float, false>(lanes_, n_, A_, cur32_, Z32_, nullptr, w32_, nullptr, s_);
+  return FE_OK;
 }
 
 int Krylov::applyPrecond(const double *r, double *z)
@@ -1371,7 +1462,11 @@ void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, i
     const float *vj = V32_ + (int64_t)j * ld32_;
     float *zj = Z32_ + (int64_t)j * ld32_;
     precond32(vj, zj, &w.gs->done);
-    spmv_launch<float, float, float, float, false>(lanes_, n_, A_, vals, zj, nullptr, w32_, &w.gs->done, s_);
+    if(sellVal_)
+      (k_spmv_sell<<<grid_for(n_, 256, 1 << 20), 256, 0, s_>>>(n_, sellPtr_, sellCol_, sellVal_, zj, w32_, &w.gs->done),
+       ::feng::count_launch());
+    else
+      spmv_launch<float, float, float, float, false>(lanes_, n_, A_, vals, zj, nullptr, w32_, &w.gs->done, s_);
     double *Hcol = w.gs->H + (int64_t)j * (MAXM + 1);
     if(opt.gsPasses == 2) {
       // always twice: dots, fused update + dots, update + norm

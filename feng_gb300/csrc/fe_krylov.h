@@ -126,6 +126,14 @@ class Krylov {
   double *Z_ = nullptr;   // m x n      preconditioned directions (FP64 path)
   float *Z32_ = nullptr;  // m x n      preconditioned directions (mixed path)
   float *V32_ = nullptr;  // (m+1) x n  Krylov basis of the mixed path, FP32
+  // Sliced-ELL copy of the FP32 matrix for the Arnoldi SpMV of the mixed
+  // path (slices of 32 rows padded to the longest row, entries column-major
+  // in the slice; padding: the row's own column, value 0), refreshed from the
+  // CSR values at each factor().
+  int32_t *sellPtr_ = nullptr, *sellCol_ = nullptr, *sellSrc_ = nullptr;  // sellSrc_: CSR position or -1
+  float *sellVal_ = nullptr;
+  int64_t sellN_ = 0;  // entries with padding
+  int build_sell();
   int *zeroFlag_ = nullptr;  // a device 0 ("not done") for gsStep
   int gsParts_ = 0;       // blocks of the FP32 Gram-Schmidt update passes
   int nSM_ = 1;           // multiprocessors of the device
@@ -181,6 +189,9 @@ class Krylov {
   // ncols columns (benchmark phases): mode 0 the dot pass (k_gs_dots), mode
   // 4 the update + norm pass (k_gs_upd).  bytes: algorithmic bytes.
   int gsStep(int mode, int ncols, int64_t *bytes);
+  // The Arnoldi SpMV of the mixed path on the current FP32 matrix (sliced
+  // ELL when built, else CSR), FP32 vectors (benchmark phase).
+  int spmvHot();
   int factor_mg(const double *values64, const float *values32);
   template <typename V> void apply_mg(const V *vals, const V *r, V *z, const int *skip);
 };

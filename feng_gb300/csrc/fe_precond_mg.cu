@@ -63,6 +63,7 @@ struct Krylov::MG {
   void *ir = nullptr, *iz = nullptr, *ip = nullptr, *iq = nullptr;
   double *part = nullptr;  // [2][1024] partial sums
   double *scal = nullptr;  // rz, pq
+  unsigned *count = nullptr;  // blocks done of the fused pressure sum (k_psum)
   ~MG()
   {
     cudaFree(dofX); cudaFree(dofY); cudaFree(pRows); cudaFree(upIa); cudaFree(upPos); cudaFree(upCol);
@@ -70,7 +71,7 @@ struct Krylov::MG {
     cudaFree(zy); cudaFree(dsum); cudaFree(ir); cudaFree(iz); cudaFree(ip); cudaFree(iq);
     cudaFree(part); cudaFree(scal); cudaFree(dnIa); cudaFree(dnPos); cudaFree(dnCol); cudaFree(slotOf);
     cudaFree(pMassDev); cudaFree(tP); cudaFree(consts); cudaFree(bxy); cudaFree(zxy); cudaFree(gVals);
-    cudaFree(pr); cudaFree(pz);
+    cudaFree(pr); cudaFree(pz); cudaFree(count);
   }
   template <typename V> void solveK(const V *b, V *x, cudaStream_t st);
 };
@@ -255,6 +256,46 @@ __global__ void k_psum_part(int64_t nP, const int32_t *__restrict__ rows, const 
     __syncthreads();
   }
   if(threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// *out = sum of r over the pressure rows in one launch: the partial sums of
+// k_psum_part, then the last block to finish sums them as k_dot_fin does
+// (same order, same bits).
+template <typename V>
+__global__ void k_psum(int64_t nP, const int32_t *__restrict__ rows, const V *__restrict__ r, double *part,
+                       unsigned *count, double *out)
+{
+  __shared__ double sh[256];
+  __shared__ bool last;
+  double s = 0.;
+  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nP; k += (int64_t)gridDim.x * blockDim.x)
+    s += (double)r[rows[k]];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for(int o = 128; o > 0; o >>= 1) {
+    if(threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if(threadIdx.x == 0) {
+    part[blockIdx.x] = sh[0];
+    __threadfence();
+    last = atomicAdd(count, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if(!last) return;
+  __threadfence();
+  double t = 0.;
+  for(int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) t += __ldcg(part + i);
+  sh[threadIdx.x] = t;
+  __syncthreads();
+  for(int o = 128; o > 0; o >>= 1) {
+    if(threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if(threadIdx.x == 0) {
+    *out = sh[0];
+    *count = 0;
+  }
 }
 
 // partial sums of a double array
@@ -455,6 +496,8 @@ int Krylov::setup_mg(const PrecondInfo &pi)
   CKM(cudaMalloc(&M.scal, sizeof(double) * 4));
   CKM(cudaMalloc(&M.consts, sizeof(double) * 4));
   CKM(cudaMemset(M.scal, 0, sizeof(double) * 4));
+  CKM(cudaMalloc(&M.count, sizeof(unsigned)));
+  CKM(cudaMemset(M.count, 0, sizeof(unsigned)));
   // Host pattern for the diagonal positions and the G block.
   std::vector<int32_t> hia(n_ + 1), hja(A_.nnz);
   CKM(cudaMemcpy(hia.data(), A_.ia, sizeof(int32_t) * (n_ + 1), cudaMemcpyDeviceToHost));
@@ -653,8 +696,7 @@ void Krylov::apply_mg(const V *vals, const V *r, V *z, const int *skip)
                                                   vals, r, z, (V *)M.bx, (V *)M.by, skip), ::feng::count_launch());
   } else {
     const int gp = (int)std::min<int64_t>(NPART, std::max<int64_t>(1, (M.nP + 255) / 256));
-    (k_psum_part<V><<<gp, 256, 0, s_>>>(M.nP, M.pRows, r, M.part), ::feng::count_launch());
-    (k_dot_fin<<<1, 256, 0, s_>>>(gp, M.part, M.scal + 3), ::feng::count_launch());
+    (k_psum<V><<<gp, 256, 0, s_>>>(M.nP, M.pRows, r, M.part, M.count, M.scal + 3), ::feng::count_launch());
     const double *cr = M.scal + 3;
     if constexpr(sizeof(V) == 8)
       (k_pressure<V, double><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.pRows, M.pScale64, M.pMassDev, cr, M.consts,
@@ -678,10 +720,19 @@ void Krylov::apply_mg(const V *vals, const V *r, V *z, const int *skip)
       (k_vel_rhs_pair<V><<<grid(2 * M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, M.upIa, nullptr, M.upCol,
                                                                (const V *)M.gVals, r, z, (V *)M.bxy, skip),
        ::feng::count_launch());
-      if constexpr(sizeof(V) == 8) M.amg->vcycle2_64((const double *)M.bxy, (double *)M.zxy);
-      else M.amg->vcycle2_32((const float *)M.bxy, (float *)M.zxy);
-      (k_vel_out_pair<V><<<grid(2 * M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, (const V *)M.zxy, M.consts,
-                                                              z, skip), ::feng::count_launch());
+      // the finest post-smoothing pass writes z_u (times 1/s) itself when
+      // it can; otherwise the interleaved result is scattered here
+      AMGDevice::OutMap om;
+      om.dofX = M.dofX;
+      om.dofY = M.dofY;
+      om.scale = M.consts;
+      om.z = z;
+      bool written;
+      if constexpr(sizeof(V) == 8) written = M.amg->vcycle2_64((const double *)M.bxy, (double *)M.zxy, &om);
+      else written = M.amg->vcycle2_32((const float *)M.bxy, (float *)M.zxy, &om);
+      if(!written)
+        (k_vel_out_pair<V><<<grid(2 * M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, (const V *)M.zxy, M.consts,
+                                                                z, skip), ::feng::count_launch());
       return;
     }
     (k_vel_rhs<V><<<grid(M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, M.upIa, M.upPos, M.upCol,

@@ -209,6 +209,19 @@ void build_ref_tensors(const QuadRule &q, RefTensors &T)
     T.psi5[k][1] = q5.r[k];
     T.psi5[k][2] = q5.s[k];
   }
+  auto split = [](double x, float &h, float &l) {
+    h = (float)x;
+    l = (float)(x - (double)h);
+  };
+  for(int k = 0; k < 7; ++k) {
+    split(T.w5[k], T.w5h[k], T.w5l[k]);
+    for(int a = 0; a < 6; ++a) {
+      split(T.phi5[k][a], T.phi5h[k][a], T.phi5l[k][a]);
+      split(T.dr5[k][a], T.dr5h[k][a], T.dr5l[k][a]);
+      split(T.ds5[k][a], T.ds5h[k][a], T.ds5l[k][a]);
+    }
+    for(int j = 0; j < 3; ++j) split(T.psi5[k][j], T.psi5h[k][j], T.psi5l[k][j]);
+  }
 }
 
 SystemCUDA::~SystemCUDA()
@@ -219,6 +232,7 @@ SystemCUDA::~SystemCUDA()
   cudaFree(udot_); cudaFree(hist_[1]); cudaFree(hist_[2]); cudaFree(scratch_);
   cudaFree(conRows_); cudaFree(conColPos_); cudaFree(perMaster_); cudaFree(perSlave_);
   cudaFree(ra_.blockRows); cudaFree(ra_.rowPtr); cudaFree(ra_.rowEnt); cudaFree(ra_.offs); cudaFree(ra_.pack);
+  cudaFree(dm_.geoPair); cudaFree(uPair_); cudaFree(udotPair_);
   if(ev0_) cudaEventDestroy(ev0_);
   if(ev1_) cudaEventDestroy(ev1_);
   if(s_) cudaStreamDestroy(s_);
@@ -287,6 +301,13 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
     }
   }
   if(fc_.srcKind < 0 || fc_.srcKind > SRC_SIN_BODY) { set_error("unknown source kind"); return FE_INVALID_ARG; }
+  {
+    const double cf[5] = {fc_.conv, fc_.mass, fc_.sigma, fc_.mu, fc_.divu};
+    for(int k = 0; k < 5; ++k) {
+      fc_.pair[k][0] = (float)cf[k];
+      fc_.pair[k][1] = (float)(cf[k] - (double)fc_.pair[k][0]);
+    }
+  }
 
   // Host tables: coloring, pattern, scatter map.
   Mesh2D tmpMesh;  // only the triangle connectivity is needed for coloring
@@ -363,6 +384,16 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
   CK(cudaMemcpy(dm_.geo, geo.data(), sizeof(double) * geo.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(dm_.xy, xy.data(), sizeof(double) * xy.size(), cudaMemcpyHostToDevice));
   if(t.elemType == ELEM_TAYLOR_HOOD) FE_TRY(build_row_assembly(adrP, map));
+  if(t.elemType == ELEM_TAYLOR_HOOD && opt.precision == 1) {
+    // geometry as float pairs for the double-float residual
+    std::vector<float2> gp(geo.size());
+    for(size_t i = 0; i < geo.size(); ++i) {
+      const float h = (float)geo[i];
+      gp[i] = make_float2(h, (float)(geo[i] - (double)h));
+    }
+    CK(cudaMalloc(&dm_.geoPair, sizeof(float2) * gp.size()));
+    CK(cudaMemcpy(dm_.geoPair, gp.data(), sizeof(float2) * gp.size(), cudaMemcpyHostToDevice));
+  }
   if(!useRows_) {
     // the colored scatter's element-to-nonzero map
     CK(cudaMalloc(&dm_.map, sizeof(int32_t) * map.size()));
@@ -396,6 +427,10 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
   CK(cudaMalloc(&du_, sizeof(double) * nInc_));
   CK(cudaMalloc(&u_, sizeof(double) * nDofs_));
   CK(cudaMalloc(&udot_, sizeof(double) * nDofs_));
+  if(dm_.geoPair) {
+    CK(cudaMalloc(&uPair_, sizeof(float2) * nDofs_));
+    CK(cudaMalloc(&udotPair_, sizeof(float2) * nDofs_));
+  }
   CK(cudaMemsetAsync(u_, 0, sizeof(double) * nDofs_, s_));
   CK(cudaMemsetAsync(udot_, 0, sizeof(double) * nDofs_, s_));
   CK(cudaMemsetAsync(du_, 0, sizeof(double) * nInc_, s_));
@@ -753,12 +788,25 @@ int SystemCUDA::setResidualToZero()
   return FE_OK;
 }
 
+void SystemCUDA::launch_residual(double *out)
+{
+  if(dfResidual()) {
+    launch_split_pairs(nDofs_, u_, uPair_, s_);
+    if(fc_.hasMass) launch_split_pairs(nDofs_, udot_, udotPair_, s_);
+    for(int c = 0; c < dm_.nColors; ++c)
+      launch_assemble_residual_df(dm_, fc_, dT_, uPair_, udotPair_, t_, nInc_, out, dm_.colorOff[c],
+                                  dm_.colorOff[c + 1], s_);
+    return;
+  }
+  for(int c = 0; c < dm_.nColors; ++c)
+    launch_assemble_residual(dm_, fc_, dT_, u_, udot_, t_, nInc_, out, dm_.colorOff[c], dm_.colorOff[c + 1], s_,
+                             exact5_);
+}
+
 int SystemCUDA::assembleResiduals()
 {
   begin_phase();
-  for(int c = 0; c < dm_.nColors; ++c)
-    launch_assemble_residual(dm_, fc_, dT_, u_, udot_, t_, nInc_, rhs_, dm_.colorOff[c],
-                             dm_.colorOff[c + 1], s_, exact5_);
+  launch_residual(rhs_);
   CK(cudaGetLastError());
   times.residual_ms += end_phase();
   times.residual_calls++;
@@ -1065,7 +1113,7 @@ int SystemCUDA::benchPhase(int which, int reps, size_t flushBytes, double *avgMs
   CK(cudaMemsetAsync(x, 0, sizeof(double) * nInc_, s_));
   CK(cudaMemcpyAsync(x, rhs_, sizeof(double) * nInc_, cudaMemcpyDeviceToDevice, s_));
   if(which != 1) FE_TRY(ensureMatrixZeroed());
-  if(which == 3 || which == 4) FE_TRY(factorIfPending());
+  if(which >= 2 && which <= 4) FE_TRY(factorIfPending());
   const int savedTiming = timing;
   timing = 0;
   double total = 0.;
@@ -1079,9 +1127,7 @@ int SystemCUDA::benchPhase(int which, int reps, size_t flushBytes, double *avgMs
     CK(cudaEventRecord(ev0_, s_));
     switch(which) {
       case 0:
-        for(int c = 0; c < dm_.nColors; ++c)
-          launch_assemble_residual(dm_, fc_, dT_, u_, udot_, t_, nInc_, y, dm_.colorOff[c],
-                                   dm_.colorOff[c + 1], s_, exact5_);
+        launch_residual(y);
         break;
       case 1:
         // as in a Newton step: zeroed matrix, then the Jacobian (the
@@ -1090,8 +1136,10 @@ int SystemCUDA::benchPhase(int which, int reps, size_t flushBytes, double *avgMs
         status = launch_matrix();
         break;
       case 2:
+        // the Krylov loop's SpMV: FP64 (plain), or the mixed Arnoldi SpMV
+        // on FP32 vectors
         if(vals64_) kry_.spmv64(vals64_, x, y);
-        else kry_.spmv32(vals32_, x, y);
+        else status = kry_.spmvHot();
         break;
       case 3:
         status = kry_.applyPrecond(x, y);
@@ -1181,9 +1229,18 @@ int newton_solve(SystemCUDA &sys, const NewtonOptions &o, NewtonStats &st)
     FE_TRY(sys.constrainEssentialComponents());
     FE_TRY(sys.applyPeriodicity());
     if(o.linearRtolMin > 0 && scale > 0) {
-      // Inexact Newton: solve only as far as the nonlinear residual warrants.
+      // Inexact Newton: solve only as far as the nonlinear residual warrants
+      // (a tenth of its relative size), and never further than the stop
+      // needs: R(u + du) = R + J du to second order, and ||.||inf <= ||.||2,
+      // so a linear residual of 0.3 relResidual ||R0||inf in the 2-norm
+      // brings the next residual under the stop.
       const double ratio = normResidual / scale;
-      sys.krylov().opt.rtol = std::max(o.linearRtolMin, std::min(1e-2, 0.1 * ratio));
+      double rtol = std::max(o.linearRtolMin, std::min(1e-2, 0.1 * ratio));
+      if(o.relResidual > 0) {
+        const double r2 = sys.krylov().norm2(sys.dRhs());
+        if(r2 > 0) rtol = std::max(rtol, std::min(1e-2, 0.3 * o.relResidual * scale / r2));
+      }
+      sys.krylov().opt.rtol = rtol;
     }
     int nIt = 0;
     int s = sys.solve(&normCorrection, nullptr, &normAxb, &nIt);

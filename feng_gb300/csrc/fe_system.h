@@ -168,6 +168,11 @@ class SystemCUDA {
   // them first.
   mutable bool zeroPending_ = false;
   int ensureMatrixZeroed() const;
+  // The mixed path assembles the Taylor-Hood residual in double-float on
+  // the FP32 pipes (FP64-class accuracy, the 7-node rule); otherwise FP64.
+  int dfResidual() const { return dm_.geoPair && exact5_ ? 1 : 0; }
+  void launch_residual(double *out);  // the residual launches of assembleResiduals
+  float2 *uPair_ = nullptr, *udotPair_ = nullptr;
   int launch_matrix();  // the Jacobian launches of assembleMatrices
   int build_row_assembly(const std::vector<int32_t> &adrP, const std::vector<int32_t> &map);
   DeviceCSR csr_;

@@ -2,7 +2,8 @@
 from tests/golden/make_golden.py), through the C ABI.
 
 Tolerances: assembled FP64 matrix and residual 1e-12 relative to their max
-norm; FP32 matrix 1e-5 relative; converged solutions 1e-8 relative."""
+norm (the mixed path's double-float residual too); FP32 matrix 1e-5
+relative; converged solutions 1e-8 relative."""
 import numpy as np
 import pytest
 
@@ -46,7 +47,30 @@ def test_assembly_fp32_matrix(name):
     sys = fe.createLinearSystem(fe.CUDA, forms, num, fe.LinearSolverOptions(precond="ilu0", precision="mixed"))
     vals, rhs = _assemble(sys, g["u0"])
     assert rel_err(vals, g["values0"]) <= TOL_FP32
-    assert rel_err(rhs, g["rhs0"]) <= TOL_FP64  # the residual stays FP64
+    assert rel_err(rhs, g["rhs0"]) <= TOL_FP64  # the residual: double-float, FP64-class
+
+
+def test_double_float_residual_with_mass_matches_fp64():
+    """The mixed path's residual (double-float, k_residual_th_df) against the
+    FP64 kernel on the lid-driven cavity forms (transient mass with a
+    nonzero u-dot, convection, stress, divergence) at a random state."""
+    from helpers import cavity_spaces
+    mesh = fe.Mesh2DP1.generate_square(8, jitter=0.1, seed=3)
+    num, forms = cavity_spaces(mesh, 100.0)
+    rng = np.random.default_rng(5)
+    u = ud = None
+    res = {}
+    for prec in ("fp64", "mixed"):
+        sys = fe.createLinearSystem(fe.CUDA, forms, num, fe.LinearSolverOptions(precond="ilu0", precision=prec))
+        if u is None:
+            u = rng.uniform(-1, 1, sys.nDofs)
+            ud = rng.uniform(-1, 1, sys.nDofs)
+        sys.setSolution(u, ud)
+        sys.setToZero()
+        sys.assembleResiduals()
+        sys.synchronize()
+        res[prec] = sys.getRHS()
+    assert rel_err(res["mixed"], res["fp64"]) <= TOL_FP64
 
 
 @pytest.mark.parametrize("name", golden_names())
