@@ -434,6 +434,7 @@ template <typename V>
 int upload_sell(const HostCSR &A, int32_t **sellPtr, int32_t **sellCol, void **sellVal)
 {
   const int64_t n = A.n, ns = (n + 31) / 32;
+  const int64_t mcols = A.m > 0 ? A.m : n;
   std::vector<int32_t> ptr(ns + 1, 0);
   for(int64_t sl = 0; sl < ns; ++sl) {
     int64_t len = 0;
@@ -454,7 +455,7 @@ int upload_sell(const HostCSR &A, int32_t **sellPtr, int32_t **sellCol, void **s
           col[e] = (int32_t)A.ja[src];
           val[e] = (V)A.a[src];
         } else {
-          col[e] = (int32_t)std::min<int64_t>(r, n - 1);  // padding: value 0 on an existing column
+          col[e] = (int32_t)std::min<int64_t>(r, mcols - 1);  // padding: value 0 on an existing column
           val[e] = (V)0;
         }
       }
