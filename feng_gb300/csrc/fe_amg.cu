@@ -369,6 +369,34 @@ __global__ void __launch_bounds__(256) k_cheb_post_sell(int64_t n, const int32_t
   }
 }
 
+// y = b + P xc on the sliced-ELL copy of P (thread = fine row).
+template <typename V, int NV>
+__global__ void __launch_bounds__(256) k_prolong_sell(int64_t n, const int32_t *__restrict__ sp,
+                                                      const int32_t *__restrict__ sc, const V *__restrict__ sv,
+                                                      const V *__restrict__ xc, const V *__restrict__ b,
+                                                      V *__restrict__ y, const int *__restrict__ skip)
+{
+  if(skip && *skip) return;
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if(row >= n) return;
+  const int64_t sl = row >> 5;
+  const int lane = (int)(row & 31);
+  const int32_t base = sp[sl], len = (sp[sl + 1] - base) >> 5;
+  V acc[NV];
+#pragma unroll
+  for(int c = 0; c < NV; ++c) acc[c] = 0;
+#pragma unroll 4
+  for(int32_t k = 0; k < len; ++k) {
+    const int32_t e = base + (k << 5) + lane;
+    const V a = __ldcs(sv + e);
+    const Vals<V, NV> xv = ldv<V, NV>(xc, __ldcs(sc + e));
+#pragma unroll
+    for(int c = 0; c < NV; ++c) acc[c] += a * xv.v[c];
+  }
+#pragma unroll
+  for(int c = 0; c < NV; ++c) y[row * NV + c] = b[row * NV + c] + acc[c];
+}
+
 // Last step of a smoothing whose residual is not needed afterwards: x += d
 // only (the step's product with A would be discarded).
 template <typename V>
@@ -487,6 +515,7 @@ AMGDevice::~AMGDevice()
     cudaFree(L.Aa); cudaFree(L.Pa); cudaFree(L.Ra); cudaFree(L.dinv); cudaFree(L.diag);
     cudaFree(L.x); cudaFree(L.b); cudaFree(L.r); cudaFree(L.d0); cudaFree(L.d1);
     cudaFree(L.sellPtr); cudaFree(L.sellCol); cudaFree(L.sellVal);
+    cudaFree(L.sellPPtr); cudaFree(L.sellPCol); cudaFree(L.sellPVal);
   }
   cudaFree(coarseInv_);
 }
@@ -526,6 +555,9 @@ int AMGDevice::upload(const AMGHierarchy &H, const AMGParams &p, int fp32, cudaS
       FE_TRY(upload_idx(&L.Pia, h.P.ia));
       FE_TRY(upload_idx(&L.Pja, h.P.ja));
       FE_TRY(fp32 ? upload_vec<float>(&L.Pa, h.P.a) : upload_vec<double>(&L.Pa, h.P.a));
+      if(l == 0 && h.P.n >= 32 * 152)
+        FE_TRY(fp32 ? upload_sell<float>(h.P, &L.sellPPtr, &L.sellPCol, &L.sellPVal)
+                    : upload_sell<double>(h.P, &L.sellPPtr, &L.sellPCol, &L.sellPVal));
       FE_TRY(upload_idx(&L.Ria, h.R.ia));
       FE_TRY(upload_idx(&L.Rja, h.R.ja));
       FE_TRY(fp32 ? upload_vec<float>(&L.Ra, h.R.a) : upload_vec<double>(&L.Ra, h.R.a));
@@ -609,7 +641,11 @@ void AMGDevice::vcycle_t(int l, const V *b, V *x)
     // y = x + P xc into this level's free scratch, then one pass
     // x = y + D^-1 (b - A y) / theta (the restart and the step in one)
     V *y = (V *)L.d1;
-    csr<V, 4, NV>(L.lanesP, L.n, L.Pia, L.Pja, (const V *)L.Pa, (const V *)C.x, x, y, s_, skip_);
+    if(L.sellPPtr)
+      (k_prolong_sell<V, NV><<<grid(L.n), 256, 0, s_>>>(L.n, L.sellPPtr, L.sellPCol, (const V *)L.sellPVal,
+                                                        (const V *)C.x, x, y, skip_), ::feng::count_launch());
+    else
+      csr<V, 4, NV>(L.lanesP, L.n, L.Pia, L.Pja, (const V *)L.Pa, (const V *)C.x, x, y, s_, skip_);
     const double lo = p_.chebyLow * L.lmax, hi = p_.chebyHigh * L.lmax, theta = 0.5 * (hi + lo);
     const V it = (V)(1.0 / theta);
     const int g = grid(L.n * L.lanesA);

@@ -95,12 +95,14 @@ class AMGDevice {
     double lmax = 0;
     int lanesA = 4, lanesP = 4, lanesR = 4;
     // Sliced-ELL copy of A (slices of 32 rows, each padded to its longest
-    // row with the row's own column and value 0, entries column-major in
-    // the slice): one thread per row, every load a full line.  Built for
-    // the finest level only.
+    // row with a valid column and value 0, entries column-major in the
+    // slice): one thread per row, every load a full line.  Built for the
+    // finest level only, for A and for the prolongation P.
     int32_t *sellPtr = nullptr;  // [nSlices + 1] first entry of each slice
     int32_t *sellCol = nullptr;
     void *sellVal = nullptr;
+    int32_t *sellPPtr = nullptr, *sellPCol = nullptr;  // the same for P
+    void *sellPVal = nullptr;
   };
   template <typename V, int NV> void vcycle_t(int l, const V *b, V *x);
   OutMap out_;

@@ -490,9 +490,9 @@ __global__ void __launch_bounds__(RB, 3) k_gs32(int64_t n4, int64_t ld, const fl
 }
 
 // h_c = V_c . w for c < ncols and ||w||^2.  Grid: x = blocks of rows (each
-// thread takes groups of 4 rows, grid-stride), y = groups of eight columns,
-// so every thread keeps eight FP32 accumulators and issues its eight basis
-// loads together; the ||w||^2 column belongs to y = 0.  Per warp a butterfly
+// thread takes groups of 4 rows, two groups per step, grid-stride), y =
+// groups of eight columns, so every thread keeps eight FP32 accumulators and
+// issues its sixteen basis loads together; the ||w||^2 column belongs to y = 0.  Per warp a butterfly
 // sums the eight accumulators over the lanes (the last three steps as a
 // reduce-scatter: lane l ends with column l % 8), the warps are summed in
 // FP64, one partial per row block and column; the last block sums the
@@ -524,16 +524,28 @@ __global__ void __launch_bounds__(RB) k_gs_dots(int64_t n4, int64_t ld, const fl
   const float4 *w4 = reinterpret_cast<const float4 *>(w);
   const float4 *V4 = reinterpret_cast<const float4 *>(V);
   const int64_t ld4 = ld / 4;
-  for(int64_t g = (int64_t)blockIdx.x * RB + threadIdx.x; g < n4; g += (int64_t)gridDim.x * RB) {
+  const int64_t stride = (int64_t)gridDim.x * RB;
+  for(int64_t g = (int64_t)blockIdx.x * RB + threadIdx.x; g < n4; g += 2 * stride) {
+    const int64_t g2 = g + stride;
+    const bool two = g2 < n4;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 x = w4[g];
-    if(wcol) wq = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, wq))));
-    float4 v[8];
+    const float4 x2 = two ? w4[g2] : z4;
+    if(wcol) {
+      wq = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, wq))));
+      wq = fmaf(x2.x, x2.x, fmaf(x2.y, x2.y, fmaf(x2.z, x2.z, fmaf(x2.w, x2.w, wq))));
+    }
+    float4 v[8], v2[8];
 #pragma unroll
-    for(int u = 0; u < 8; ++u)
-      v[u] = c0 + u < ncols ? __ldcs(V4 + (int64_t)(c0 + u) * ld4 + g) : make_float4(0.f, 0.f, 0.f, 0.f);
+    for(int u = 0; u < 8; ++u) {
+      v[u] = c0 + u < ncols ? __ldcs(V4 + (int64_t)(c0 + u) * ld4 + g) : z4;
+      v2[u] = (two && c0 + u < ncols) ? __ldcs(V4 + (int64_t)(c0 + u) * ld4 + g2) : z4;
+    }
 #pragma unroll
-    for(int u = 0; u < 8; ++u)
+    for(int u = 0; u < 8; ++u) {
       acc[u] = fmaf(v[u].x, x.x, fmaf(v[u].y, x.y, fmaf(v[u].z, x.z, fmaf(v[u].w, x.w, acc[u]))));
+      acc[u] = fmaf(v2[u].x, x2.x, fmaf(v2[u].y, x2.y, fmaf(v2[u].z, x2.z, fmaf(v2[u].w, x2.w, acc[u]))));
+    }
   }
   // lanes l, l^8, l^16, l^24 first, then a reduce-scatter over the low bits
 #pragma unroll
