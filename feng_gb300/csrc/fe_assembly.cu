@@ -857,11 +857,104 @@ __global__ void k_pack_th(DeviceMesh dm, int hasConv, const double *__restrict__
   }
 }
 
-// Thread = CSR row.  Entry (p, li): li < 12 is velocity row (a = li / 2,
-// component m = li % 2) of element p, whose 12 velocity and 3 pressure
-// columns are the element-matrix row of k_matrix_th; li >= 12 is pressure
-// row j = li - 12, whose 12 velocity columns are divu * int psi_j d_m phi_a.
-// The arithmetic is k_matrix_th's, restricted to one row.
+// Both component rows (a, 0) and (a, 1) of velocity function a of an
+// element, from its packed data e (u, G, J): A[m][12] velocity columns and
+// the pressure-column factors Bp[m][3] -- k_matrix_th's arithmetic for one
+// (element, a).
+template <typename V>
+__device__ __forceinline__ void th_rows_pair(const SharedTensors<V> &sT, const FormCoeffs &fc, double c0,
+                                             const V *e, int a, V (&A)[2][12], V (&Bp)[2][3])
+{
+  const V G[2][2] = {{e[12], e[13]}, {e[14], e[15]}};
+  const V J = e[16];
+#pragma unroll
+  for(int m = 0; m < 2; ++m)
+#pragma unroll
+    for(int j = 0; j < 12; ++j) A[m][j] = 0;
+  if(fc.hasConv) {
+    V U[12];
+#pragma unroll
+    for(int i = 0; i < 12; ++i) U[i] = e[i];
+    V V0[2][6];
+#pragma unroll
+    for(int c = 0; c < 6; ++c)
+#pragma unroll
+      for(int q = 0; q < 2; ++q) V0[q][c] = U[2 * c] * G[q][0] + U[2 * c + 1] * G[q][1];
+    const V cc = (V)fc.conv * J;
+#pragma unroll
+    for(int b = 0; b < 6; ++b) {
+      V W = 0, Z[2][2] = {{0, 0}, {0, 0}};
+#pragma unroll
+      for(int c = 0; c < 6; ++c) {
+        W += V0[0][c] * sT.T[0][a][c][b] + V0[1][c] * sT.T[1][a][c][b];
+        const V t0 = sT.T[0][a][b][c], t1 = sT.T[1][a][b][c];
+        const V uc0 = U[2 * c], uc1 = U[2 * c + 1];
+        Z[0][0] += uc0 * t0; Z[0][1] += uc1 * t0;
+        Z[1][0] += uc0 * t1; Z[1][1] += uc1 * t1;
+      }
+#pragma unroll
+      for(int m = 0; m < 2; ++m)
+#pragma unroll
+        for(int n = 0; n < 2; ++n) {
+          V v = G[0][n] * Z[0][m] + G[1][n] * Z[1][m];
+          if(m == n) v += W;
+          A[m][2 * b + n] += cc * v;
+        }
+    }
+  }
+  if(fc.hasSigma) {
+    const V cs = -(V)fc.sigma * (V)fc.mu * J;
+    V GG[2][2][2][2];
+#pragma unroll
+    for(int k = 0; k < 2; ++k)
+#pragma unroll
+      for(int l = 0; l < 2; ++l)
+#pragma unroll
+        for(int q = 0; q < 2; ++q)
+#pragma unroll
+          for(int s2 = 0; s2 < 2; ++s2) GG[k][l][q][s2] = G[q][k] * G[s2][l];
+#pragma unroll
+    for(int b = 0; b < 6; ++b) {
+      V S[2][2];
+#pragma unroll
+      for(int k = 0; k < 2; ++k)
+#pragma unroll
+        for(int l = 0; l < 2; ++l) {
+          V v = 0;
+#pragma unroll
+          for(int q = 0; q < 2; ++q)
+#pragma unroll
+            for(int s2 = 0; s2 < 2; ++s2) v += GG[k][l][q][s2] * sT.K[q][s2][a][b];
+          S[k][l] = v;
+        }
+      const V tr = S[0][0] + S[1][1];
+#pragma unroll
+      for(int m = 0; m < 2; ++m)
+#pragma unroll
+        for(int n = 0; n < 2; ++n) A[m][2 * b + n] += cs * ((m == n ? tr : (V)0) + S[n][m]);
+    }
+  }
+  if(fc.hasMass) {
+    const V cm = (V)fc.mass * (V)c0 * J;
+#pragma unroll
+    for(int b = 0; b < 6; ++b) {
+      A[0][2 * b] += cm * sT.M[a][b];
+      A[1][2 * b + 1] += cm * sT.M[a][b];
+    }
+  }
+#pragma unroll
+  for(int m = 0; m < 2; ++m)
+#pragma unroll
+    for(int j = 0; j < 3; ++j) Bp[m][j] = (G[0][m] * sT.D[0][j][a] + G[1][m] * sT.D[1][j][a]) * J;
+}
+
+// Thread = unit (RowAsm): a pair of component rows of one velocity node, or
+// one row.  Entry (p, li): li < 12 is velocity row (a = li / 2, component
+// m = li % 2) of element p, whose 12 velocity and 3 pressure columns are the
+// element-matrix row of k_matrix_th; li >= 12 is pressure row j = li - 12,
+// whose 12 velocity columns are divu * int psi_j d_m phi_a.  A pair takes
+// the entries of its component-0 row and builds both rows (same columns,
+// same offsets); the arithmetic is k_matrix_th's.
 template <typename V>
 __global__ void __launch_bounds__(256) k_matrix_th_rows(RowAsm ra, FormCoeffs fc, const RefTensors *__restrict__ gT,
                                                         double c0, V *__restrict__ values, int accumulate)
@@ -870,12 +963,38 @@ __global__ void __launch_bounds__(256) k_matrix_th_rows(RowAsm ra, FormCoeffs fc
   V *sv = reinterpret_cast<V *>(rowsmem);
   __shared__ SharedTensors<V> sT;
   load_tensors(sT, gT);
-  const int32_t r0 = ra.blockRows[blockIdx.x], r1 = ra.blockRows[blockIdx.x + 1];
-  const int32_t base = ra.ia[r0], L = ra.ia[r1] - base;
+  const int32_t uA = ra.blockUnits[blockIdx.x], uB = ra.blockUnits[blockIdx.x + 1];
+  const int32_t base = ra.ia[ra.unitRow[uA]], L = ra.ia[ra.unitRow[uB]] - base;
   for(int i = threadIdx.x; i < L; i += blockDim.x) sv[i] = accumulate ? values[base + i] : (V)0;
   __syncthreads();
-  const int32_t r = r0 + (int32_t)threadIdx.x;
-  if(r < r1) {
+  const int32_t u = uA + (int32_t)threadIdx.x;
+  if(u < uB && ra.unitTwo[u]) {
+    const int32_t r = ra.unitRow[u];
+    V *row0 = sv + (ra.ia[r] - base), *row1 = sv + (ra.ia[r + 1] - base);
+    const V *pk = reinterpret_cast<const V *>(ra.pack);
+    for(int32_t k = ra.rowPtr[r]; k < ra.rowPtr[r + 1]; ++k) {
+      const int32_t ent = ra.rowEnt[k];
+      const int64_t p = ent >> 4;
+      const int a = (ent & 15) >> 1;
+      uint8_t off[16];
+      *reinterpret_cast<uint4 *>(off) = reinterpret_cast<const uint4 *>(ra.offs)[k];
+      V A[2][12], Bp[2][3];
+      th_rows_pair<V>(sT, fc, c0, pk + p * ROWASM_PACK, a, A, Bp);
+#pragma unroll
+      for(int j = 0; j < 12; ++j)
+        if(off[j] != 255) {
+          row0[off[j]] += A[0][j];
+          row1[off[j]] += A[1][j];
+        }
+#pragma unroll
+      for(int j = 0; j < 3; ++j)
+        if(off[12 + j] != 255) {
+          row0[off[12 + j]] += fc.hasSigma ? (V)fc.sigma * Bp[0][j] : (V)0;
+          row1[off[12 + j]] += fc.hasSigma ? (V)fc.sigma * Bp[1][j] : (V)0;
+        }
+    }
+  } else if(u < uB) {
+    const int32_t r = ra.unitRow[u];
     V *row = sv + (ra.ia[r] - base);
     const V *pk = reinterpret_cast<const V *>(ra.pack);
     for(int32_t k = ra.rowPtr[r]; k < ra.rowPtr[r + 1]; ++k) {

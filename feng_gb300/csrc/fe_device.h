@@ -91,10 +91,15 @@ struct DeviceMesh {
 // contiguous range of CSR values, which the block then writes once.  No
 // atomics, no element-to-nonzero map; each value is the same sum, in the
 // same order, as the colored scatter.
+// Units: a velocity node's two component rows together when they hold the
+// same columns (one thread builds both, sharing the element terms), else one
+// row.
 struct RowAsm {
   int nBlocks = 0;
   int capBytes = 0;               // dynamic shared memory of a block
-  int32_t *blockRows = nullptr;   // [nBlocks + 1] first row of each block
+  int32_t *blockUnits = nullptr;  // [nBlocks + 1] first unit of each block
+  int32_t *unitRow = nullptr;     // [nUnits + 1] first row of each unit (the last entry: nInc)
+  int8_t *unitTwo = nullptr;      // [nUnits] 1: rows r (component 0) and r + 1 (component 1)
   int32_t *rowPtr = nullptr;      // [nInc + 1] entries of each row
   int32_t *rowEnt = nullptr;      // [nEnt] p * 16 + local row (p: color-order element)
   uint8_t *offs = nullptr;        // [nEnt][16] column offset in the row of each local column (255: none)

@@ -231,7 +231,8 @@ SystemCUDA::~SystemCUDA()
   cudaFree(vals64_); cudaFree(vals32_); cudaFree(rhs_); cudaFree(du_); cudaFree(u_);
   cudaFree(udot_); cudaFree(hist_[1]); cudaFree(hist_[2]); cudaFree(scratch_);
   cudaFree(conRows_); cudaFree(conColPos_); cudaFree(perMaster_); cudaFree(perSlave_);
-  cudaFree(ra_.blockRows); cudaFree(ra_.rowPtr); cudaFree(ra_.rowEnt); cudaFree(ra_.offs); cudaFree(ra_.pack);
+  cudaFree(ra_.blockUnits); cudaFree(ra_.unitRow); cudaFree(ra_.unitTwo); cudaFree(ra_.rowPtr); cudaFree(ra_.rowEnt);
+  cudaFree(ra_.offs); cudaFree(ra_.pack);
   cudaFree(dm_.geoPair); cudaFree(uPair_); cudaFree(udotPair_);
   if(ev0_) cudaEventDestroy(ev0_);
   if(ev1_) cudaEventDestroy(ev1_);
@@ -758,23 +759,47 @@ int SystemCUDA::build_row_assembly(const std::vector<int32_t> &adrP, const std::
         if(pos >= 0) offs[(size_t)16 * k + j] = (uint8_t)(pos - pat_.ia[d]);
       }
     }
+  // Units: rows r, r + 1 together when r holds only component-0 entries,
+  // r + 1 the component-1 entries of the same elements in the same order,
+  // and both rows the same columns (then the offsets are the same).
+  std::vector<int32_t> unitRow;
+  std::vector<int8_t> unitTwo;
+  for(int64_t r = 0; r < nInc_;) {
+    bool two = r + 1 < nInc_ && rowPtr[r + 1] - rowPtr[r] == rowPtr[r + 2] - rowPtr[r + 1] &&
+               pat_.ia[r + 1] - pat_.ia[r] == pat_.ia[r + 2] - pat_.ia[r + 1] && rowPtr[r + 1] > rowPtr[r];
+    for(int32_t k = rowPtr[r]; two && k < rowPtr[r + 1]; ++k) {
+      const int32_t e0 = rowEnt[k], e1 = rowEnt[k + (rowPtr[r + 1] - rowPtr[r])];
+      two = (e0 & 15) < 12 && (e0 & 1) == 0 && e1 == e0 + 1;
+    }
+    for(int64_t j = 0; two && j < pat_.ia[r + 1] - pat_.ia[r]; ++j)
+      two = pat_.ja[pat_.ia[r] + j] == pat_.ja[pat_.ia[r + 1] + j];
+    unitRow.push_back((int32_t)r);
+    unitTwo.push_back(two ? 1 : 0);
+    r += two ? 2 : 1;
+  }
+  const int64_t nUnits = (int64_t)unitRow.size();
+  unitRow.push_back((int32_t)nInc_);
   const int vs = opt.precision == 0 ? 8 : 4;
   const int cap = 40 * 1024 / vs;  // values per block in shared memory
-  std::vector<int32_t> blockRows{0};
-  int64_t r0 = 0;
-  while(r0 < nInc_) {
-    int64_t r1 = r0 + 1;
-    while(r1 < nInc_ && r1 - r0 < 256 && pat_.ia[r1 + 1] - pat_.ia[r0] <= cap) ++r1;
-    blockRows.push_back((int32_t)r1);
-    r0 = r1;
+  std::vector<int32_t> blockUnits{0};
+  int64_t u0 = 0;
+  while(u0 < nUnits) {
+    int64_t u1 = u0 + 1;
+    while(u1 < nUnits && u1 - u0 < 256 && pat_.ia[unitRow[u1 + 1]] - pat_.ia[unitRow[u0]] <= cap) ++u1;
+    blockUnits.push_back((int32_t)u1);
+    u0 = u1;
   }
-  ra_.nBlocks = (int)blockRows.size() - 1;
+  ra_.nBlocks = (int)blockUnits.size() - 1;
   ra_.capBytes = cap * vs;
-  CK(cudaMalloc(&ra_.blockRows, sizeof(int32_t) * blockRows.size()));
+  CK(cudaMalloc(&ra_.blockUnits, sizeof(int32_t) * blockUnits.size()));
+  CK(cudaMalloc(&ra_.unitRow, sizeof(int32_t) * unitRow.size()));
+  CK(cudaMalloc(&ra_.unitTwo, std::max<size_t>(1, unitTwo.size())));
   CK(cudaMalloc(&ra_.rowPtr, sizeof(int32_t) * rowPtr.size()));
   CK(cudaMalloc(&ra_.rowEnt, sizeof(int32_t) * rowEnt.size()));
   CK(cudaMalloc(&ra_.offs, offs.size()));
-  CK(cudaMemcpy(ra_.blockRows, blockRows.data(), sizeof(int32_t) * blockRows.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ra_.blockUnits, blockUnits.data(), sizeof(int32_t) * blockUnits.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ra_.unitRow, unitRow.data(), sizeof(int32_t) * unitRow.size(), cudaMemcpyHostToDevice));
+  if(!unitTwo.empty()) CK(cudaMemcpy(ra_.unitTwo, unitTwo.data(), unitTwo.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ra_.rowPtr, rowPtr.data(), sizeof(int32_t) * rowPtr.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ra_.rowEnt, rowEnt.data(), sizeof(int32_t) * rowEnt.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ra_.offs, offs.data(), offs.size(), cudaMemcpyHostToDevice));
