@@ -718,7 +718,8 @@ __global__ void __launch_bounds__(RB, 4) k_gs_upd(int64_t n4, int64_t ld, const 
   }
 }
 
-// v = w * (1 / ||w||) in FP32, 4 rows per thread; the scale comes from k_gs32<., 2>.
+// v = w * (1 / ||w||) in FP32, 4 rows per thread; the scale comes from the
+// last update + norm pass (k_gs_upd<., true> or k_gs32<., 2>).
 // gated: only after a second Gram-Schmidt pass (otherwise k_gs_upd wrote v).
 __global__ void k_scale32(int64_t n4, const float *__restrict__ w, float *__restrict__ v, const RedState *st,
                           const int *__restrict__ done, int gated)
