@@ -10,38 +10,60 @@ namespace feng {
 
 namespace {
 
-// C = A * B (Gustavson's row-by-row product with a dense marker).
+// C = A * B (Gustavson's row-by-row product with a dense marker), rows in
+// parallel: a symbolic pass for the row sizes, then the numeric pass; each
+// row is formed exactly as a serial product would form it.
 HostCSR spgemm(const HostCSR &A, const HostCSR &B)
 {
   HostCSR C;
   C.n = A.n;
   C.m = B.m;
   C.ia.assign(A.n + 1, 0);
-  std::vector<int64_t> marker(B.m, -1);
-  std::vector<double> acc(B.m, 0.);
-  std::vector<int32_t> cols;
-  for(int64_t i = 0; i < A.n; ++i) {
-    cols.clear();
-    for(int64_t k = A.ia[i]; k < A.ia[i + 1]; ++k) {
-      const int32_t j = A.ja[k];
-      const double av = A.a[k];
-      for(int64_t l = B.ia[j]; l < B.ia[j + 1]; ++l) {
-        const int32_t c = B.ja[l];
-        if(marker[c] != i) {
-          marker[c] = i;
-          acc[c] = 0.;
-          cols.push_back(c);
+  parallel_for(A.n, [&](int64_t r0, int64_t r1) {
+    std::vector<int64_t> marker(B.m, -1);
+    for(int64_t i = r0; i < r1; ++i) {
+      int64_t c = 0;
+      for(int64_t k = A.ia[i]; k < A.ia[i + 1]; ++k) {
+        const int32_t j = A.ja[k];
+        for(int64_t l = B.ia[j]; l < B.ia[j + 1]; ++l)
+          if(marker[B.ja[l]] != i) {
+            marker[B.ja[l]] = i;
+            ++c;
+          }
+      }
+      C.ia[i + 1] = c;
+    }
+  }, 1024);
+  for(int64_t i = 0; i < A.n; ++i) C.ia[i + 1] += C.ia[i];
+  C.ja.resize(C.ia[A.n]);
+  C.a.resize(C.ia[A.n]);
+  parallel_for(A.n, [&](int64_t r0, int64_t r1) {
+    std::vector<int64_t> marker(B.m, -1);
+    std::vector<double> acc(B.m, 0.);
+    std::vector<int32_t> cols;
+    for(int64_t i = r0; i < r1; ++i) {
+      cols.clear();
+      for(int64_t k = A.ia[i]; k < A.ia[i + 1]; ++k) {
+        const int32_t j = A.ja[k];
+        const double av = A.a[k];
+        for(int64_t l = B.ia[j]; l < B.ia[j + 1]; ++l) {
+          const int32_t c = B.ja[l];
+          if(marker[c] != i) {
+            marker[c] = i;
+            acc[c] = 0.;
+            cols.push_back(c);
+          }
+          acc[c] += av * B.a[l];
         }
-        acc[c] += av * B.a[l];
+      }
+      std::sort(cols.begin(), cols.end());
+      int64_t o = C.ia[i];
+      for(int32_t c : cols) {
+        C.ja[o] = c;
+        C.a[o++] = acc[c];
       }
     }
-    std::sort(cols.begin(), cols.end());
-    for(int32_t c : cols) {
-      C.ja.push_back(c);
-      C.a.push_back(acc[c]);
-    }
-    C.ia[i + 1] = (int64_t)C.ja.size();
-  }
+  }, 1024);
   return C;
 }
 

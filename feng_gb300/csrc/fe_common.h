@@ -3,10 +3,12 @@
 // 0 is success, negative values are errors.
 #pragma once
 
+#include <algorithm>
 #include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace feng {
@@ -34,6 +36,26 @@ extern thread_local int g_capturing;
 inline void count_launch()
 {
   if(!g_capturing) g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
+// Host loops of the set-up over [0, n) split into contiguous ranges run by
+// up to 32 threads (f(begin, end)); small n runs inline.
+template <typename F>
+void parallel_for(int64_t n, F &&f, int64_t grain = 1 << 14)
+{
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int64_t T = std::min<int64_t>({(int64_t)hw, 32, (n + grain - 1) / grain});
+  if(T <= 1) {
+    if(n > 0) f((int64_t)0, n);
+    return;
+  }
+  const int64_t chunk = (n + T - 1) / T;
+  std::vector<std::thread> th;
+  for(int64_t t = 0; t < T; ++t) {
+    const int64_t b = t * chunk, e = std::min(n, b + chunk);
+    if(b < e) th.emplace_back([&f, b, e] { f(b, e); });
+  }
+  for(auto &x : th) x.join();
 }
 
 #define FE_TRY(expr)                   \

@@ -267,50 +267,62 @@ int validate_coloring(const Mesh2D &m, const Coloring &col)
 // Sparsity pattern, restating feEZCompressedRowStorage
 // (feCompressedRowStorage.cpp:15-135): the diagonal of every unknown row, plus
 // every (adrI, adrJ) pair of every matrix form with both DOFs unknown, sorted
-// and made unique row by row.  Rows are gathered here by counting sort instead
-// of per-row push_back, which yields the same sets.
+// and made unique row by row.  Rows are gathered here through the DOF-to-element
+// adjacency, row by row in parallel, which yields the same sets.
 int build_csr_pattern(const ElementTables &et, int64_t nInc, CSRPattern &pat)
 {
   const int nl = et.nloc;
   const int64_t nt = et.nElm;
-  std::vector<int64_t> cnt(nInc + 1, 0);
-  for(int64_t r = 0; r < nInc; ++r) cnt[r + 1] = 1;
-  for(int64_t t = 0; t < nt; ++t) {
-    const int64_t *a = &et.adr[t * nl];
-    for(int i = 0; i < nl; ++i) {
-      if(a[i] >= nInc) continue;
-      int c = 0;
-      for(int j = 0; j < nl; ++j) c += (et.mask[i * nl + j] && a[j] < nInc);
-      cnt[a[i] + 1] += c;
-    }
+  // Unknown DOF -> (element, local index) adjacency, elements in order.
+  std::vector<int64_t> dptr(nInc + 1, 0);
+  for(int64_t t = 0; t < nt; ++t)
+    for(int i = 0; i < nl; ++i)
+      if(et.adr[t * nl + i] < nInc) ++dptr[et.adr[t * nl + i] + 1];
+  for(int64_t r = 0; r < nInc; ++r) dptr[r + 1] += dptr[r];
+  std::vector<int64_t> adj(dptr[nInc]);
+  {
+    std::vector<int64_t> fill(dptr.begin(), dptr.end() - 1);
+    for(int64_t t = 0; t < nt; ++t)
+      for(int i = 0; i < nl; ++i) {
+        const int64_t d = et.adr[t * nl + i];
+        if(d < nInc) adj[fill[d]++] = t * nl + i;
+      }
   }
-  for(int64_t r = 0; r < nInc; ++r) cnt[r + 1] += cnt[r];
-  std::vector<int32_t> buf(cnt[nInc]);
-  std::vector<int64_t> pos(cnt.begin(), cnt.end() - 1);
-  for(int64_t r = 0; r < nInc; ++r) buf[pos[r]++] = (int32_t)r;
-  for(int64_t t = 0; t < nt; ++t) {
-    const int64_t *a = &et.adr[t * nl];
-    for(int i = 0; i < nl; ++i) {
-      if(a[i] >= nInc) continue;
-      for(int j = 0; j < nl; ++j)
-        if(et.mask[i * nl + j] && a[j] < nInc) buf[pos[a[i]]++] = (int32_t)a[j];
-    }
-  }
+  // Row r: its diagonal and the coupled unknown DOFs of the elements that
+  // hold it, sorted and unique, written once into a slot of 1 + nl deg(r)
+  // entries (slot r starts at r + nl dptr[r]), then compacted.
+  std::vector<int32_t> buf((size_t)(nInc + (int64_t)nl * dptr[nInc]));
   pat = CSRPattern();
   pat.n = nInc;
   pat.ia.assign(nInc + 1, 0);
-  pat.ja.reserve(cnt[nInc] / 2);
-  for(int64_t r = 0; r < nInc; ++r) {
-    auto b = buf.begin() + cnt[r], e = buf.begin() + cnt[r + 1];
-    std::sort(b, e);
-    e = std::unique(b, e);
-    pat.ja.insert(pat.ja.end(), b, e);
-    pat.ia[r + 1] = (int64_t)pat.ja.size();
-  }
-  if(pat.nnz() >= (int64_t)INT32_MAX) {
+  parallel_for(nInc, [&](int64_t r0, int64_t r1) {
+    for(int64_t r = r0; r < r1; ++r) {
+      int32_t *v = buf.data() + r + (int64_t)nl * dptr[r];
+      int32_t *e = v;
+      *e++ = (int32_t)r;
+      for(int64_t k = dptr[r]; k < dptr[r + 1]; ++k) {
+        const int64_t t = adj[k] / nl;
+        const int i = (int)(adj[k] - t * nl);
+        const int64_t *a = &et.adr[t * nl];
+        for(int j = 0; j < nl; ++j)
+          if(et.mask[i * nl + j] && a[j] < nInc) *e++ = (int32_t)a[j];
+      }
+      std::sort(v, e);
+      pat.ia[r + 1] = std::unique(v, e) - v;
+    }
+  });
+  for(int64_t r = 0; r < nInc; ++r) pat.ia[r + 1] += pat.ia[r];
+  if(pat.ia[nInc] >= (int64_t)INT32_MAX) {
     set_error("more than 2^31 nonzeros: 32-bit scatter map does not fit");
     return FE_INVALID_ARG;
   }
+  pat.ja.resize(pat.ia[nInc]);
+  parallel_for(nInc, [&](int64_t r0, int64_t r1) {
+    for(int64_t r = r0; r < r1; ++r) {
+      const int32_t *v = buf.data() + r + (int64_t)nl * dptr[r];
+      std::copy(v, v + (pat.ia[r + 1] - pat.ia[r]), pat.ja.begin() + pat.ia[r]);
+    }
+  });
   return FE_OK;
 }
 
@@ -320,23 +332,34 @@ int build_scatter_map(const ElementTables &et, const Coloring &col, const CSRPat
   const int nl = et.nloc;
   const int64_t nt = et.nElm;
   map.assign((size_t)nl * nl * nt, -1);
-  for(int64_t p = 0; p < nt; ++p) {
-    const int32_t t = col.elements[p];
-    const int64_t *a = &et.adr[(int64_t)t * nl];
-    for(int i = 0; i < nl; ++i) {
-      if(a[i] >= nInc) continue;
-      const int32_t *rb = pat.ja.data() + pat.ia[a[i]];
-      const int32_t *re = pat.ja.data() + pat.ia[a[i] + 1];
-      for(int j = 0; j < nl; ++j) {
-        if(!et.mask[i * nl + j] || a[j] >= nInc) continue;
-        const int32_t *f = std::lower_bound(rb, re, (int32_t)a[j]);
-        if(f == re || *f != a[j]) {
-          set_error("pattern misses (%lld,%lld)", (long long)a[i], (long long)a[j]);
-          return FE_ERROR;
+  std::atomic<int> missing{0};
+  int64_t missI = 0, missJ = 0;
+  parallel_for(nt, [&](int64_t p0, int64_t p1) {
+    for(int64_t p = p0; p < p1; ++p) {
+      const int32_t t = col.elements[p];
+      const int64_t *a = &et.adr[(int64_t)t * nl];
+      for(int i = 0; i < nl; ++i) {
+        if(a[i] >= nInc) continue;
+        const int32_t *rb = pat.ja.data() + pat.ia[a[i]];
+        const int32_t *re = pat.ja.data() + pat.ia[a[i] + 1];
+        for(int j = 0; j < nl; ++j) {
+          if(!et.mask[i * nl + j] || a[j] >= nInc) continue;
+          const int32_t *f = std::lower_bound(rb, re, (int32_t)a[j]);
+          if(f == re || *f != a[j]) {
+            if(missing.exchange(1) == 0) {
+              missI = a[i];
+              missJ = a[j];
+            }
+            continue;
+          }
+          map[(size_t)(i * nl + j) * nt + p] = (int32_t)(f - pat.ja.data());
         }
-        map[(size_t)(i * nl + j) * nt + p] = (int32_t)(f - pat.ja.data());
       }
     }
+  });
+  if(missing.load()) {
+    set_error("pattern misses (%lld,%lld)", (long long)missI, (long long)missJ);
+    return FE_ERROR;
   }
   return FE_OK;
 }

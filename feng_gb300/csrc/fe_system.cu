@@ -748,17 +748,25 @@ int SystemCUDA::build_row_assembly(const std::vector<int32_t> &adrP, const std::
   const int64_t nEnt = rowPtr[nInc_];
   std::vector<int32_t> rowEnt(std::max<int64_t>(nEnt, 1)), fill(rowPtr.begin(), rowPtr.end() - 1);
   std::vector<uint8_t> offs((size_t)16 * std::max<int64_t>(nEnt, 1), 255);
+  std::vector<int32_t> rowOf(std::max<int64_t>(nEnt, 1));
   for(int64_t p = 0; p < nE; ++p)
     for(int li = 0; li < nl; ++li) {
       const int32_t d = adrP[(size_t)li * nE + p];
       if(d >= nInc_) continue;
       const int32_t k = fill[d]++;
       rowEnt[k] = (int32_t)(p * 16 + li);
+      rowOf[k] = d;
+    }
+  parallel_for(nEnt, [&](int64_t k0, int64_t k1) {
+    for(int64_t k = k0; k < k1; ++k) {
+      const int64_t p = rowEnt[k] >> 4;
+      const int li = rowEnt[k] & 15;
       for(int j = 0; j < nl; ++j) {
         const int32_t pos = map[(size_t)(li * nl + j) * nE + p];
-        if(pos >= 0) offs[(size_t)16 * k + j] = (uint8_t)(pos - pat_.ia[d]);
+        if(pos >= 0) offs[(size_t)16 * k + j] = (uint8_t)(pos - pat_.ia[rowOf[k]]);
       }
     }
+  });
   // Units: rows r, r + 1 together when r holds only component-0 entries,
   // r + 1 the component-1 entries of the same elements in the same order,
   // and both rows the same columns (then the offsets are the same).
