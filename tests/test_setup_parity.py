@@ -76,3 +76,25 @@ def test_true_problem_sizes():
     m = fe.Mesh2DP1.generate_square(32, -0.5, 1.5, -0.5, 1.5, jitter=0.1, seed=1)
     num, _ = problem_spaces("ns_kovasznay", m)
     assert num.nDofs == 2 * 65 * 65 + 33 * 33
+
+
+def test_threaded_setup_is_deterministic():
+    """The set-up runs over host threads (pattern row by row, coloring,
+    numbering): two builds of the same 96 x 96 Taylor-Hood problem give the
+    same arrays, bit for bit, and the pattern rows are sorted, unique and hold
+    their diagonal."""
+    import feng_gb300 as fe
+    out = []
+    for _ in range(2):
+        mesh = fe.Mesh2DP1.generate_square(96, -0.5, 1.5, -0.5, 1.5, jitter=0.1, seed=11)
+        num, _ = problem_spaces("ns_kovasznay", mesh)
+        st = num.setup(256)
+        ia, ja = st.pattern()
+        off, el = st.coloring()
+        out.append((ia, ja, off, el, st.elementDofs()))
+    for a, b in zip(out[0], out[1]):
+        np.testing.assert_array_equal(a, b)
+    ia, ja = out[0][0], out[0][1]
+    for r in range(0, len(ia) - 1, 997):
+        row = ja[ia[r]:ia[r + 1]]
+        assert np.all(np.diff(row) > 0) and r in row
