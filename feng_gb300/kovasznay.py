@@ -82,12 +82,15 @@ def main(argv=None):
                          "numbers: 0 residual, 1 Jacobian, 2 SpMV, 3 preconditioner, 4 finest smoother pass, "
                          "5 Gram-Schmidt dots, 6 Gram-Schmidt update)")
     ap.add_argument("--phase-reps", type=int, default=20)
+    ap.add_argument("--errors", action="store_true",
+                    help="after the solves, L2 errors of velocity and pressure against the exact Kovasznay flow "
+                         "(feNorm VECTOR_L2_ERROR / L2_ERROR on the device)")
     args = ap.parse_args(argv)
 
     from . import api as fe
     from ._lib import check
     ts0 = time.perf_counter()
-    _, num, forms = build(args.n, args.re)
+    mesh, num, forms = build(args.n, args.re)
     ts1 = time.perf_counter()
     check(fe._lib.load().fe_cuda_set_device(0))  # CUDA context creation, timed apart
     ts2 = time.perf_counter()
@@ -110,6 +113,15 @@ def main(argv=None):
             runs.append({"seconds": time.perf_counter() - t0, "newton_iterations": st["iterations"],
                          "krylov_iterations": st["krylov_iterations"],
                          "rel_residual": st["residual"] / st["residual0"] if st["residual0"] else 0.0})
+    errors = {}
+    if args.errors and runs:
+        from . import exact
+        sol = fe.feSolution(sys_)
+        sol.pull()
+        uS = next(sp for f in forms for sp in f.spaces if sp.element == fe.VECTOR_LAGRANGE)
+        pS = next(sp for f in forms for sp in f.spaces if sp.element == fe.LAGRANGE)
+        errors = {"u_l2": fe.createNorm(fe.VECTOR_L2_ERROR, [uS], sol, None, exact.kovasznay_velocity(args.re)).compute(),
+                  "p_l2": fe.createNorm(fe.L2_ERROR, [pS], sol, exact.kovasznay_pressure(args.re)).compute()}
     phases = {}
     for w in [int(v) for v in args.phases.split(",") if v.strip()]:
         # device time per run with the L2 flushed before each run; bytes:
@@ -128,7 +140,7 @@ def main(argv=None):
                       "unknowns": sys_.nInc, "nnz": sys_.nnz,
                       "setup_s": {"mesh_numbering_pattern": ts1 - ts0, "cuda_context": ts2 - ts1,
                                   "system_create": ts3 - ts2},
-                      "solves": runs, "phases": phases}))
+                      "solves": runs, "errors": errors, "phases": phases}))
 
 
 if __name__ == "__main__":
