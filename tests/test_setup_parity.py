@@ -98,3 +98,25 @@ def test_threaded_setup_is_deterministic():
     for r in range(0, len(ia) - 1, 997):
         row = ja[ia[r]:ia[r + 1]]
         assert np.all(np.diff(row) > 0) and r in row
+
+
+def test_mesh_from_arrays_round_trip_and_errors():
+    """fe_mesh_from_arrays rebuilds the same mesh (vertices, triangles,
+    boundary lines, pressure point, edge numbering) from the arrays of
+    another, and refuses out-of-range vertex indices and empty meshes."""
+    import feng_gb300 as fe
+    from feng_gb300._lib import FeError
+    m = fe.Mesh2DP1.generate_square(12, 0.0, 1.0, 0.0, 1.0, jitter=0.1, seed=5)
+    a = m.arrays()
+    b = fe.Mesh2DP1.from_arrays(a["x"], a["y"], a["tri"], a["bnd"], a["point"]).arrays()
+    for k in ("x", "y", "tri", "tri_edges", "bnd"):
+        np.testing.assert_array_equal(a[k], b[k])
+    assert a["point"] == b["point"] and a["n_edges"] == b["n_edges"]
+    bad = a["tri"].copy()
+    bad[3, 1] = len(a["x"])
+    with pytest.raises(FeError):
+        fe.Mesh2DP1.from_arrays(a["x"], a["y"], bad, a["bnd"], a["point"])
+    with pytest.raises(FeError):
+        fe.Mesh2DP1.from_arrays(a["x"], a["y"], a["tri"], a["bnd"], len(a["x"]))
+    with pytest.raises(FeError):
+        fe.Mesh2DP1.from_arrays(a["x"][:0], a["y"][:0], a["tri"][:0], a["bnd"][:0], -1)
