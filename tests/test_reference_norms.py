@@ -64,3 +64,32 @@ def test_fixture_meshes_read_back_from_the_reference_files():
             np.testing.assert_array_equal(a["x"], g[f"{key}{i}_x"])
             np.testing.assert_array_equal(a["tri"], g[f"{key}{i}_tri"])
             np.testing.assert_array_equal(a["bnd"], g[f"{key}{i}_bnd"])
+
+
+def test_oracle_l2_error_closed_forms():
+    """The oracle's norm on known answers: a P2 field interpolating a
+    quadratic is exact (error at rounding level), and with u_h = 0 the error
+    of a constant c over the domain is |c| sqrt(area) (both components for
+    the vector norm)."""
+    import feng_gb300 as fe
+    mesh = fe.Mesh2DP1.generate_square(10, -0.5, 1.5, -0.5, 1.5, jitter=0.1, seed=3)
+    from helpers import problem_spaces
+    num, _ = problem_spaces("ns_kovasznay", mesh)
+    st = num.setup(256)
+    x, y, fld, comp, _ = st.dofInfo()
+    adr, xy = st.elementDofs(), element_xy(mesh)
+    quad = quadrature_rule(8)
+    def quad_u(xx, yy):
+        return (xx * xx - 0.5 * xx * yy + 0.25, -yy * yy + xx)
+    u = np.zeros(st.nDofs)
+    qu = quad_u(x, y)
+    for c in range(2):
+        sel = (fld == 0) & (comp == c)
+        u[sel] = qu[c][sel]
+    assert l2_error(num.elem_type, adr, xy, u, quad, quad_u, 0) < 1e-13
+    area = 4.0
+    zero = np.zeros(st.nDofs)
+    e = l2_error(num.elem_type, adr, xy, zero, quad, lambda xx, yy: (np.full_like(xx, 3.0), np.full_like(xx, 4.0)), 0)
+    assert e == pytest.approx(5.0 * np.sqrt(area), rel=1e-13)
+    ep = l2_error(num.elem_type, adr, xy, zero, quad, lambda xx, yy: (np.full_like(xx, -2.0),), 1)
+    assert ep == pytest.approx(2.0 * np.sqrt(area), rel=1e-13)
