@@ -57,10 +57,19 @@ class Mesh2DP1:
         return cls(h)
 
     @classmethod
-    def from_msh(cls, path: str):
+    def from_msh(cls, path: str, domain: str = "Domaine", boundary: Sequence[str] = ("Bord",),
+                 point: str | None = "PointPression"):
+        """Reads an ASCII msh 4.1 file.  `domain`, `boundary` and `point` name
+        the file's physical groups taken as "Domaine" (triangles), "Bord"
+        (the lines of all listed groups) and "PointPression" (None: none)."""
         lib = _lib.load()
         h = C.c_void_p()
-        check(lib.fe_mesh_read_msh(str(path).encode(), C.byref(h)))
+        if domain == "Domaine" and tuple(boundary) == ("Bord",) and point == "PointPression":
+            check(lib.fe_mesh_read_msh(str(path).encode(), C.byref(h)))
+        else:
+            names = (C.c_char_p * max(len(boundary), 1))(*[b.encode() for b in boundary])
+            check(lib.fe_mesh_read_msh_groups(str(path).encode(), domain.encode(), names, len(boundary),
+                                              None if point is None else point.encode(), C.byref(h)))
         return cls(h)
 
     @classmethod

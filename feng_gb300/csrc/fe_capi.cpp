@@ -161,6 +161,30 @@ int fe_mesh_read_msh(const char *path, fe_mesh **out)
   GUARD_END
 }
 
+int fe_mesh_read_msh_groups(const char *path, const char *domain, const char *const *boundary,
+                            int n_boundary, const char *point, fe_mesh **out)
+{
+  GUARD_BEGIN
+  if(!out || !path || !domain || n_boundary < 0 || (n_boundary > 0 && !boundary)) {
+    set_error("null argument");
+    return FE_INVALID_ARG;
+  }
+  MeshGroups g;
+  g.domain = domain;
+  g.boundary.clear();
+  for(int i = 0; i < n_boundary; ++i) {
+    if(!boundary[i]) { set_error("null boundary group name"); return FE_INVALID_ARG; }
+    g.boundary.push_back(boundary[i]);
+  }
+  g.point = point ? point : "";
+  auto *m = new fe_mesh();
+  int s = mesh_read_msh41(m->m, path, g);
+  if(s) { delete m; return s; }
+  *out = m;
+  return FE_OK;
+  GUARD_END
+}
+
 int fe_mesh_from_arrays(int64_t nv, const double *x, const double *y, int64_t nt, const int32_t *tri,
                         int64_t nb, const int32_t *bnd, int32_t point, fe_mesh **out)
 {

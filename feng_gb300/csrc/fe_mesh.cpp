@@ -172,7 +172,7 @@ int mesh_write_msh41(const Mesh2D &m, const std::string &path)
   return rc;
 }
 
-int mesh_read_msh41(Mesh2D &m, const std::string &path)
+int mesh_read_msh41(Mesh2D &m, const std::string &path, const MeshGroups &groups)
 {
   std::ifstream in(path);
   if(!in.good()) {
@@ -267,11 +267,17 @@ int mesh_read_msh41(Mesh2D &m, const std::string &path)
     int d = kv.first.first;
     auto ph = entityPhys.find(kv.first);
     std::string name = ph == entityPhys.end() ? "" : physNames[{d, ph->second}];
-    if(d == 2 && name == "Domaine") m.tri.insert(m.tri.end(), kv.second.begin(), kv.second.end());
-    else if(d == 1 && name == "Bord") m.bnd.insert(m.bnd.end(), kv.second.begin(), kv.second.end());
-    else if(d == 0 && name == "PointPression" && !kv.second.empty()) m.point = kv.second[0];
+    const bool isBoundary =
+        std::find(groups.boundary.begin(), groups.boundary.end(), name) != groups.boundary.end();
+    if(d == 2 && name == groups.domain) m.tri.insert(m.tri.end(), kv.second.begin(), kv.second.end());
+    else if(d == 1 && isBoundary) m.bnd.insert(m.bnd.end(), kv.second.begin(), kv.second.end());
+    else if(d == 0 && !groups.point.empty() && name == groups.point && !kv.second.empty())
+      m.point = kv.second[0];
   }
-  if(m.tri.empty()) { set_error("no \"Domaine\" triangles in %s", path.c_str()); return FE_READ_ERROR; }
+  if(m.tri.empty()) {
+    set_error("no \"%s\" triangles in %s", groups.domain.c_str(), path.c_str());
+    return FE_READ_ERROR;
+  }
   return m.build_topology();
 }
 

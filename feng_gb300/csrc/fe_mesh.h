@@ -57,8 +57,19 @@ int mesh_generate_square(Mesh2D &m, int n, double x0, double x1, double y0, doub
 // Writes the mesh as an ASCII Gmsh 4.1 file readable by feMesh2DP1.
 int mesh_write_msh41(const Mesh2D &m, const std::string &path);
 
-// Reads an ASCII Gmsh 4.1 file with one "Domaine" (triangles), one "Bord"
-// (lines) and optionally one "PointPression" (point) physical group.
-int mesh_read_msh41(Mesh2D &m, const std::string &path);
+// Physical groups of a msh file that play the three roles of Mesh2D: the
+// triangles of `domain`, the lines of every group in `boundary` (merged, in
+// the file's entity order) and the vertex of `point` (empty: none).  feNG
+// addresses groups by name (createFiniteElementSpace(..., cncGeoID, ...),
+// src/feSpace.cpp:11-60); the defaults are the names its test meshes use.
+struct MeshGroups {
+  std::string domain = "Domaine";
+  std::vector<std::string> boundary = {"Bord"};
+  std::string point = "PointPression";
+};
+
+// Reads an ASCII Gmsh 4.1 file: the triangles of groups.domain (required),
+// the lines of groups.boundary and the vertex of groups.point (optional).
+int mesh_read_msh41(Mesh2D &m, const std::string &path, const MeshGroups &groups = MeshGroups());
 
 }  // namespace feng

@@ -10,6 +10,10 @@ solutions of the benchmark problems:
 * ``kovasznay``    Kovasznay (1948) laminar wake behind a grid, exact steady
                    Navier-Stokes solution for Reynolds number Re.
 * ``cavity_lid``   lid-driven cavity: u = (1, 0) on y = y_top, 0 elsewhere.
+* ``poiseuille``   plane Poiseuille flow in the channel [0, L] x [0, H]:
+                   u = (-dpdx/2 y (H - y), 0), p = -dpdx (L - x)
+                   (tests/withLinearSolver/navier_stokes.cpp:177-193,
+                   stokes.cpp:166-181).
 """
 from __future__ import annotations
 
@@ -67,3 +71,17 @@ def zero_vector(x, y):
 
 def zero_scalar(x, y):
     return (np.zeros_like(x),)
+
+
+def poiseuille_velocity(height: float = 1.0, dpdx: float = -1.0):
+    def f(x, y):
+        return (-dpdx / 2.0 * y * (height - y), np.zeros_like(np.asarray(y, np.float64)))
+
+    return f
+
+
+def poiseuille_pressure(length: float = 5.0, dpdx: float = -1.0):
+    def f(x, y):
+        return (-dpdx * (length - x),)
+
+    return f

@@ -154,6 +154,14 @@ int fe_cuda_device_count(int *count);
 int fe_mesh_generate_square(int n, double x0, double x1, double y0, double y1, double jitter,
                             uint64_t seed, fe_mesh **out);
 int fe_mesh_read_msh(const char *path, fe_mesh **out);
+/* As fe_mesh_read_msh with the physical groups named by the caller: the
+ * triangles of `domain` become "Domaine", the lines of the n_boundary groups
+ * in `boundary` (merged in the file's entity order) "Bord", the vertex of
+ * `point` (NULL or "": none) "PointPression".  feNG selects a space's
+ * connectivity by physical name (createFiniteElementSpace cncGeoID,
+ * src/feSpace.cpp:11-60); this maps a file's names onto the three roles. */
+int fe_mesh_read_msh_groups(const char *path, const char *domain, const char *const *boundary,
+                            int n_boundary, const char *point, fe_mesh **out);
 int fe_mesh_write_msh(const fe_mesh *m, const char *path);
 /* A mesh from caller arrays (0-based): vertices x, y; counter-clockwise
  * triangles of "Domaine"; boundary lines of "Bord" (oriented like the

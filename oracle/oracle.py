@@ -255,20 +255,28 @@ def l2_error(elem_type, adr, elem_xy, u, quad, fct, field):
     return np.sqrt(res)
 
 
-def newton_direct(op, u, tol_residual=1e-10, tol_correction=1e-10, max_iter=20):
+def newton_direct(op, u, tol_residual=1e-10, tol_correction=1e-10, max_iter=20, rows=()):
     """Newton iterations on the oracle's residual and Jacobian with a direct
     sparse solve (scipy SuperLU), in feNG's convention: A du = rhs (rhs = sum
     of element Be), u[:nInc] += du; stops on the absolute max-norms of the
-    residual or the correction (src/feNonLinearSolver.cpp:38-181)."""
+    residual or the correction (src/feNonLinearSolver.cpp:38-181).  `rows`
+    are the unknowns of essential components (setEssentialComponent): their
+    rows of A and rhs are constrained before the solve and the stop test
+    (src/feNonLinearSolver.cpp:94, constrainEssentialComponents), so they
+    keep their initial values."""
     import scipy.sparse as sp
     import scipy.sparse.linalg as spl
     k = op.keep
     u = np.array(u, np.float64)
     for it in range(max_iter):
         rhs = op.residual(u)
+        vals = None
+        if len(rows):
+            vals, rhs = constrain(k["ia"], k["ja"], op.matrix(u), rhs, rows=rows)
         if np.max(np.abs(rhs)) <= tol_residual:
             return u, it
-        a = sp.csr_matrix((op.matrix(u), k["ja"], k["ia"]), shape=(op.n_inc, op.n_inc))
+        a = sp.csr_matrix((op.matrix(u) if vals is None else vals, k["ja"], k["ia"]),
+                          shape=(op.n_inc, op.n_inc))
         du = spl.spsolve(a.tocsc(), rhs)
         u[:op.n_inc] += du
         if np.max(np.abs(du)) <= tol_correction:

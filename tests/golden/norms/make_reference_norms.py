@@ -5,6 +5,10 @@
   pressure point):
     - data/mmsMeshes/square1-4.msh (tests/withLinearSolver/scalarFE.cpp:772)
     - data/square1-4.msh            (tests/withLinearSolver/navier_stokes.cpp:149)
+* the channel mesh of the Poiseuille tests, data/poiseuille0.msh
+  (tests/withLinearSolver/navier_stokes.cpp:297, stokes.cpp:286): the
+  triangles of "Domain", the lines of "NoSlip" and "Inlet" (the essential
+  boundary) and the lines of "Outlet";
 * the L2 errors those tests print in their golden output files:
     - tests/withLinearSolver/scalarFE_diffusion.output, block "P2 field 0"
       (P2 diffusion, u = sin(pi x) sin(pi y), quadrature degree 8)
@@ -47,6 +51,10 @@ def main(ref=Path("/root/reference")):
             out[f"{key}{i}_x"], out[f"{key}{i}_y"] = a["x"], a["y"]
             out[f"{key}{i}_tri"], out[f"{key}{i}_bnd"] = a["tri"], a["bnd"]
             out[f"{key}{i}_point"] = np.int32(a["point"])
+    pm = ref / "data/poiseuille0.msh"
+    a = fe.Mesh2DP1.from_msh(pm, domain="Domain", boundary=("NoSlip", "Inlet"), point=None).arrays()
+    out["pois_x"], out["pois_y"], out["pois_tri"], out["pois_bnd"] = a["x"], a["y"], a["tri"], a["bnd"]
+    out["pois_outlet"] = fe.Mesh2DP1.from_msh(pm, domain="Domain", boundary=("Outlet",), point=None).arrays()["bnd"]
     t = (ref / "tests/withLinearSolver/scalarFE_diffusion.output").read_text()
     out["diff_nelm"], out["diff_err_u"] = parse_block(t, "Diffusion - Error on u - Lagrange elements P2 field 0")
     t = (ref / "tests/withLinearSolver/navier_stokes_MMS.output").read_text()

@@ -97,6 +97,52 @@ def convergence_case(g, key, i):
     return mesh, num, forms, [u, p], [exact.ns_mms_velocity, exact.ns_mms_pressure]
 
 
+def poiseuille_case(g, stokes):
+    """The Poiseuille tests of the reference on data/poiseuille0.msh,
+    divergence formulation, P2-P1, quadrature degree 8
+    (tests/withLinearSolver/navier_stokes.cpp:194-290, stokes.cpp:183-279):
+    velocity essential on "NoSlip" and "Inlet" (one space here: the exact
+    profile vanishes on the walls), the vertical velocity constrained on
+    "Outlet" (setEssentialComponent(1)), pressure free.  Navier-Stokes:
+    convective acceleration +1, divergence +1, Newtonian stress -1 with
+    viscosity 1; Stokes: divergence +1, stress +1.  Returns (mesh, numbering,
+    forms, outlet rows, exact functions)."""
+    uex, pex = exact.poiseuille_velocity(), exact.poiseuille_pressure()
+    mesh = fe.Mesh2DP1.from_arrays(g["pois_x"], g["pois_y"], g["pois_tri"], g["pois_bnd"], -1)
+    u = fe.createFiniteElementSpace(mesh, fe.VECTOR_LAGRANGE, 2, "U", "Domaine", 8, exact.zero_vector)
+    uB = fe.createFiniteElementSpace(mesh, fe.VECTOR_LAGRANGE, 2, "U", "Bord", 8, uex)
+    p = fe.createFiniteElementSpace(mesh, fe.LAGRANGE, 1, "P", "Domaine", 8, exact.zero_scalar)
+    num = fe.feMetaNumber(mesh, [uB, u, p], [uB])
+    forms = [fe.createBilinearForm([p, u], fe.feSysElm_MixedDivergence(1.0))]
+    if stokes:
+        forms.append(fe.createBilinearForm([u, p], fe.feSysElm_DivergenceNewtonianStress(1.0, 1.0)))
+    else:
+        forms.insert(0, fe.createBilinearForm([u], fe.feSysElm_VectorConvectiveAcceleration(1.0)))
+        forms.append(fe.createBilinearForm([u, p], fe.feSysElm_DivergenceNewtonianStress(-1.0, 1.0)))
+    return mesh, num, forms, outlet_rows(mesh, num, g["pois_outlet"], 1), [uex, pex]
+
+
+def outlet_rows(mesh, num, lines, comp):
+    """Unknowns of velocity component `comp` on the given boundary lines (the
+    rows constrainEssentialComponents collects from the addressing vectors of
+    a space on those lines, src/feLinearSystemMklPardiso.cpp:994-1030): the
+    P2 vertex and edge DOFs of each line, taken from the triangle that holds
+    it (local node k of a Taylor-Hood element, component c, at 2k+c; edge
+    nodes 3-5 join local vertices (0,1), (1,2), (2,0))."""
+    st = num.setup(256)
+    tri, adr = mesh.arrays()["tri"], st.elementDofs()
+    rows = set()
+    for a, b in np.asarray(lines).reshape(-1, 2):
+        t = int(np.flatnonzero((tri == a).any(1) & (tri == b).any(1))[0])
+        la, lb = int(np.flatnonzero(tri[t] == a)[0]), int(np.flatnonzero(tri[t] == b)[0])
+        le = 3 + next(k for k in range(3) if {k, (k + 1) % 3} == {la, lb})
+        for node in (la, lb, le):
+            d = int(adr[t, 2 * node + comp])
+            if d < st.nInc:
+                rows.add(d)
+    return np.array(sorted(rows), np.int64)
+
+
 def essential_state(num, fcts_by_field):
     """Zero unknowns and the exact values on the essential DOFs (nodewise,
     as feSolution::initializeEssentialBC)."""

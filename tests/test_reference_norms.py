@@ -11,7 +11,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from helpers import convergence_case, element_xy, essential_state, reference_l2
+from helpers import convergence_case, element_xy, essential_state, poiseuille_case, reference_l2
 
 from feng_gb300.api import quadrature_rule
 from oracle.oracle import OracleProblem, l2_error, newton_direct
@@ -64,6 +64,50 @@ def test_fixture_meshes_read_back_from_the_reference_files():
             np.testing.assert_array_equal(a["x"], g[f"{key}{i}_x"])
             np.testing.assert_array_equal(a["tri"], g[f"{key}{i}_tri"])
             np.testing.assert_array_equal(a["bnd"], g[f"{key}{i}_bnd"])
+    pm = ref / "poiseuille0.msh"
+    a = fe.Mesh2DP1.from_msh(pm, domain="Domain", boundary=("NoSlip", "Inlet"), point=None).arrays()
+    for k in ("x", "y", "tri", "bnd"):
+        np.testing.assert_array_equal(a[k], g[f"pois_{k}"])
+    assert a["point"] == -1
+    o = fe.Mesh2DP1.from_msh(pm, domain="Domain", boundary=("Outlet",), point=None).arrays()
+    np.testing.assert_array_equal(o["bnd"], g["pois_outlet"])
+
+
+def _poiseuille(stokes, constrain_outlet=True):
+    g = reference_l2()
+    mesh, num, forms, rows, (uex, pex) = poiseuille_case(g, stokes)
+    st = num.setup(256)
+    ia, ja = st.pattern()
+    off, el = st.coloring()
+    adr, xy = st.elementDofs(), element_xy(mesh)
+    quad = quadrature_rule(8)
+    op = OracleProblem(num.elem_type, adr, xy, st.nInc, st.nDofs, off, el, ia, ja, quad,
+                       [f.sysElm for f in forms])
+    u0 = essential_state(num, [uex, lambda xx, yy: (np.zeros_like(xx),)])
+    # feNLSolverOptions{1e-10, 1e-10, 1e4, 10, ...}: at most 11 iterations.
+    u, its = newton_direct(op, u0, max_iter=11, rows=rows if constrain_outlet else ())
+    assert its < 11
+    return rows, [l2_error(num.elem_type, adr, xy, u, quad, f, field) for field, f in enumerate((uex, pex))]
+
+
+@pytest.mark.parametrize("stokes", [False, True], ids=["navier_stokes", "stokes"])
+def test_oracle_poiseuille_is_exact(stokes):
+    """The reference's Poiseuille tests (tests/withLinearSolver/
+    navier_stokes.cpp:368-380, stokes.cpp:358-375, P2-P1): the parabolic
+    velocity and linear pressure lie in the discrete spaces, so the solution
+    reproduces them; the reference asserts both L2 errors below 1e-13."""
+    rows, (eu, ep) = _poiseuille(stokes)
+    # Outlet x = 5: 4 vertices + 3 edge midpoints, the two wall corners essential.
+    assert len(rows) == 5
+    assert eu < 1e-13 and ep < 1e-13
+
+
+def test_oracle_poiseuille_needs_the_outlet_constraint():
+    """Without the vertical velocity constrained on the outlet the outlet is
+    traction-free, which the Poiseuille flow is not (shear stress u_y != 0
+    there): the errors are far from rounding level."""
+    _, (eu, ep) = _poiseuille(False, constrain_outlet=False)
+    assert eu > 1e-6 and ep > 1e-6
 
 
 def test_oracle_l2_error_closed_forms():

@@ -120,3 +120,25 @@ def test_mesh_from_arrays_round_trip_and_errors():
         fe.Mesh2DP1.from_arrays(a["x"], a["y"], a["tri"], a["bnd"], len(a["x"]))
     with pytest.raises(FeError):
         fe.Mesh2DP1.from_arrays(a["x"][:0], a["y"][:0], a["tri"][:0], a["bnd"][:0], -1)
+
+
+def test_msh_reader_named_groups(tmp_path):
+    """The reader maps a file's physical groups onto the three roles by name:
+    the default names read as before, explicit names give the same mesh, an
+    empty boundary list reads no lines, a missing domain group is an error
+    that names it."""
+    import feng_gb300 as fe
+    from feng_gb300._lib import FeError
+    m = fe.Mesh2DP1.generate_square(6, 0.0, 5.0, 0.0, 1.0, jitter=0.1, seed=2)
+    path = tmp_path / "channel.msh"
+    m.write_msh(path)
+    a = fe.Mesh2DP1.from_msh(path).arrays()
+    b = fe.Mesh2DP1.from_msh(path, domain="Domaine", boundary=["Bord"], point="PointPression").arrays()
+    for k in ("x", "y", "tri", "tri_edges", "bnd"):
+        np.testing.assert_array_equal(a[k], b[k])
+    assert a["point"] == b["point"] == 0
+    c = fe.Mesh2DP1.from_msh(path, domain="Domaine", boundary=(), point=None).arrays()
+    assert c["bnd"].shape == (0, 2) and c["point"] == -1
+    np.testing.assert_array_equal(a["tri"], c["tri"])
+    with pytest.raises(FeError, match="Domain"):
+        fe.Mesh2DP1.from_msh(path, domain="Domain", boundary=("Bord",), point=None)
