@@ -87,6 +87,8 @@ SIGNATURES = {
     "fe_mesh_generate_square": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                           C.c_double, C.c_uint64, C.POINTER(P)]),
     "fe_mesh_read_msh": (C.c_int, [C.c_char_p, C.POINTER(P)]),
+    "fe_export_vtk": (C.c_int, [P, P, P, C.POINTER(C.c_char_p), C.c_int, C.POINTER(C.c_char_p), C.c_int,
+                                C.c_int, C.c_char_p]),
     "fe_mesh_read_msh_groups": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_char_p), C.c_int,
                                           C.c_char_p, C.POINTER(P)]),
     "fe_mesh_write_msh": (C.c_int, [P, C.c_char_p]),

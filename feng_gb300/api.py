@@ -531,6 +531,48 @@ class feSolution:
         return self.u
 
 
+# ---- visualisation export (src/feExporter.h, src/feExporter.cpp) -----------------
+
+VTK = "VTK"
+
+
+class feExporterVTK:
+    """feExporterVTK (src/feExporter.h:68-98): writes the solution as the
+    reference's legacy ASCII VTK file (fe_export_vtk), on the host.  `sol` is
+    a feSolution (its device copy is read) or an array of every DOF."""
+
+    def __init__(self, numbering: feMetaNumber, sol, mesh: Mesh2DP1, spaces: Sequence[feSpace]):
+        self.numbering, self.sol, self.mesh = numbering, sol, mesh
+        self.spaces = list(spaces)
+
+    def writeStep(self, fileName, requiredFields: Sequence[str] = (), precision: int = 6):
+        """writeStep (src/feExporter.cpp:854-990): the fields of the domain
+        spaces (those named in requiredFields, if any); `precision`
+        significant digits (the reference writes 6)."""
+        num = self.numbering
+        u = self.sol.pull() if isinstance(self.sol, feSolution) else self.sol
+        u = np.ascontiguousarray(u, np.float64)
+        if u.shape != (num.nDofs,):
+            raise ValueError(f"the solution must hold {num.nDofs} DOFs")
+        wanted = [s.fieldID for s in self.spaces if s.cncGeoID == "Domaine"]
+        if requiredFields:
+            wanted = [f for f in wanted if f in requiredFields]
+        if not wanted:
+            raise ValueError("no field of a domain space to export")
+        names = (C.c_char_p * len(num.fieldIDs))(*[f.encode() for f in num.fieldIDs])
+        req = (C.c_char_p * len(wanted))(*[f.encode() for f in wanted])
+        st = num.setup()
+        check(_lib.load().fe_export_vtk(self.mesh._h, st._h, ptr(u), names, len(num.fieldIDs), req, len(wanted),
+                                        int(precision), str(fileName).encode()))
+
+
+def createVisualizationExporter(fmt, numbering, solution, mesh, spaces):
+    """createVisualizationExporter (src/feExporter.cpp:65-77) for VTK."""
+    if fmt != VTK:
+        raise ValueError(f"unsupported visualization format {fmt!r}")
+    return feExporterVTK(numbering, solution, mesh, spaces)
+
+
 # ---- error norms (src/feNorm.h, src/feNorm.cpp) ---------------------------------
 
 L2_ERROR, VECTOR_L2_ERROR = "L2_ERROR", "VECTOR_L2_ERROR"

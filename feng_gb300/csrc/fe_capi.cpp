@@ -10,6 +10,7 @@
 
 #include "../../include/feng_cuda.h"
 #include "fe_common.h"
+#include "fe_export.h"
 #include "fe_mesh.h"
 #include "fe_setup.h"
 #include "fe_system.h"
@@ -52,6 +53,8 @@ struct fe_cuda_system {
 };
 
 struct fe_setup {
+  std::vector<SpaceDesc> spaces;
+  int64_t nVertices = 0, nEdges = 0;  // of the mesh the setup was built on
   Numbering num;
   ElementTables et;
   Coloring col;
@@ -270,6 +273,9 @@ int fe_setup_create(const fe_mesh *m, const fe_space_desc *spaces, int nspaces, 
   std::unique_ptr<fe_setup> S(new fe_setup());
   const Mesh2D &M = m->m;
   FE_TRY(build_numbering(M, sp, S->num));
+  S->spaces = sp;
+  S->nVertices = M.n_vertices();
+  S->nEdges = M.n_edges;
   // The element's fields: the P2 space on the domain, and for Taylor-Hood the
   // P1 space on the domain.
   int fieldU = -1, fieldP = -1;
@@ -931,5 +937,49 @@ extern "C" int fe_cuda_apply_periodicity(fe_cuda_system *s)
   GUARD_BEGIN
   if(!s) { set_error("null argument"); return FE_INVALID_ARG; }
   return s->sys.applyPeriodicity();
+  GUARD_END
+}
+
+int fe_export_vtk(const fe_mesh *m, const fe_setup *s, const double *solution,
+                  const char *const *field_names, int n_field_names, const char *const *required,
+                  int n_required, int precision, const char *path)
+{
+  GUARD_BEGIN
+  if(!m || !s || !solution || !field_names || !path || n_required < 0 || (n_required > 0 && !required)) {
+    set_error("null argument");
+    return FE_INVALID_ARG;
+  }
+  if(m->m.n_vertices() != s->nVertices || m->m.n_edges != s->nEdges) {
+    set_error("the setup was not built on this mesh");
+    return FE_INVALID_ARG;
+  }
+  if(n_field_names != s->num.nFields) {
+    set_error("%d field names for %d fields", n_field_names, s->num.nFields);
+    return FE_INVALID_ARG;
+  }
+  for(int f = 0; f < n_field_names; ++f)
+    if(!field_names[f]) { set_error("null field name"); return FE_INVALID_ARG; }
+  for(int i = 0; i < n_required; ++i) {
+    if(!required[i]) { set_error("null field name"); return FE_INVALID_ARG; }
+    bool known = false;
+    for(int f = 0; f < n_field_names; ++f) known |= std::string(required[i]) == field_names[f];
+    if(!known) { set_error("no field named \"%s\"", required[i]); return FE_INVALID_ARG; }
+  }
+  // Fields with a space on the domain, in the order of their first domain
+  // space, filtered by `required`.
+  std::vector<ExportField> fields;
+  for(const SpaceDesc &d : s->spaces) {
+    if(d.cnc != CNC_DOMAIN) continue;
+    bool seen = false;
+    for(const ExportField &e : fields) seen |= e.field == d.field;
+    if(seen) continue;
+    bool wanted = n_required == 0;
+    for(int i = 0; i < n_required; ++i) wanted |= std::string(required[i]) == field_names[d.field];
+    if(wanted) fields.push_back({d.field, field_names[d.field], d.degree});
+  }
+  // The reference fills an unordered_map in space order and writes in its
+  // iteration order, which for the two fields of this path is the reverse.
+  std::reverse(fields.begin(), fields.end());
+  return export_vtk(m->m, s->num, solution, fields, precision == 0 ? 6 : precision, path);
   GUARD_END
 }

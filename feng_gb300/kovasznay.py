@@ -85,6 +85,8 @@ def main(argv=None):
     ap.add_argument("--errors", action="store_true",
                     help="after the solves, L2 errors of velocity and pressure against the exact Kovasznay flow "
                          "(feNorm VECTOR_L2_ERROR / L2_ERROR on the device)")
+    ap.add_argument("--vtk", default="",
+                    help="after the solves, write the solution to this legacy VTK file (feExporterVTK layout)")
     args = ap.parse_args(argv)
 
     from . import api as fe
@@ -122,6 +124,8 @@ def main(argv=None):
         pS = next(sp for f in forms for sp in f.spaces if sp.element == fe.LAGRANGE)
         errors = {"u_l2": fe.createNorm(fe.VECTOR_L2_ERROR, [uS], sol, None, exact.kovasznay_velocity(args.re)).compute(),
                   "p_l2": fe.createNorm(fe.L2_ERROR, [pS], sol, exact.kovasznay_pressure(args.re)).compute()}
+    if args.vtk and runs:
+        fe.createVisualizationExporter(fe.VTK, num, sys_.getSolution(), mesh, num.spaces).writeStep(args.vtk)
     phases = {}
     for w in [int(v) for v in args.phases.split(",") if v.strip()]:
         # device time per run with the L2 flushed before each run; bytes:

@@ -205,6 +205,25 @@ int fe_setup_get_blocks(const fe_setup *s, int32_t *block_of_row);
 /* Quadrature rule: n points (<= 16), r, s, w [n]. */
 int fe_quadrature_rule(int degree, int *n, double *r, double *s, double *w);
 
+/* ---- VTK export (feExporterVTK::writeStep, src/feExporter.h:36-116,
+ * src/feExporter.cpp:854-990), on the host, no device needed.
+ * Writes the legacy ASCII VTK file the reference writes for continuous
+ * fields on a P1 triangle mesh: the vertices, then one node per edge midpoint
+ * (edges in ascending (min vertex, max vertex) order) when a field is P2;
+ * 6-node quadratic triangles (VTK type 22), or 3-node triangles (5) when every
+ * field is P1; one FIELD array per field (2-vectors with a zero third
+ * component).  solution [n_dofs] holds every DOF (unknowns, then essential
+ * DOFs).  field_names [n_field_names = number of fields] name the fields in
+ * the order of fe_space_desc.field; required [n_required] selects fields by
+ * name (0: every field with a space on "Domaine").  Fields are written in the
+ * reverse order of their first space on "Domaine", as the reference writes
+ * "U" then "P" (P first).  precision: significant digits, 0 = 6 (the
+ * reference's stream default), up to 17 for a lossless file.  m must be the
+ * mesh s was created on. */
+int fe_export_vtk(const fe_mesh *m, const fe_setup *s, const double *solution,
+                  const char *const *field_names, int n_field_names, const char *const *required,
+                  int n_required, int precision, const char *path);
+
 /* ---- system creation */
 /* Standalone route: device system from a host set-up. */
 int fe_cuda_system_create(const fe_setup *setup, const fe_form_desc *forms, int nforms,

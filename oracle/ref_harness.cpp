@@ -261,6 +261,27 @@ void mms_src(const feFunctionArguments &a, const std::vector<double> &, std::vec
 
 }  // namespace
 
+// The solution as the reference's legacy VTK exporter writes it
+// (feExporterVTK::writeStep, src/feExporter.cpp:854-990).
+// With a pressure field, also the pressure alone (requiredFields {"P"}):
+// a P1 field only, so 3-node triangles without mid-edge nodes.
+feStatus write_vtk(const std::string &dir, feMetaNumber &numbering, feSolution &sol, feMesh2DP1 &mesh,
+                   const std::vector<feSpace *> &spaces)
+{
+  feExporter *exporter = nullptr;
+  feCheck(createVisualizationExporter(exporter, VTK, &numbering, &sol, &mesh, spaces));
+  feCheck(exporter->writeStep(dir + "/solution.vtk"));
+  delete exporter;
+  bool hasP = false;
+  for(feSpace *s : spaces) hasP |= s->getFieldID() == "P";
+  if(hasP) {
+    feCheck(createVisualizationExporter(exporter, VTK, &numbering, &sol, &mesh, spaces));
+    feCheck(exporter->writeStep(dir + "/solution_p.vtk", {"P"}));
+    delete exporter;
+  }
+  return FE_STATUS_OK;
+}
+
 int main(int argc, char **argv)
 {
   if(argc < 4) {
@@ -378,6 +399,7 @@ int main(int argc, char **argv)
                                  0.0, nSteps * g_dt, nSteps));
     feCheck(ti->makeSteps(nSteps));
     std::vector<double> traj = sol.getSolution();
+    feCheck(write_vtk(out, numbering, sol, mesh, spaces));
     write_raw(out + "/ia.i64", ia);
     write_raw(out + "/ja.i64", ja);
     write_raw(out + "/adr.i64", adr);
@@ -425,6 +447,7 @@ int main(int argc, char **argv)
   sys->assembleResiduals(&sol);
   double rfinal = 0;
   sys->getRHSMaxNorm(&rfinal);
+  feCheck(write_vtk(out, numbering, sol, mesh, spaces));
 
   write_raw(out + "/ia.i64", ia);
   write_raw(out + "/ja.i64", ja);

@@ -7,7 +7,9 @@ mesh with this package's generator (the same file the backend reads), runs
 the reference's spaces, numbering, coloring, CSR pattern, element kernels
 and a Newton solve (or a BDF2 run of the lid-driven cavity with the
 reference's BDF2Integrator) on it, and stores the arrays as compressed .npz
-files next to this script.
+files next to this script, with the legacy VTK file the reference's exporter
+(feExporterVTK::writeStep) writes for the final solution (key "vtk", the
+file's bytes; "vtk_p": the pressure alone, requiredFields {"P"}).
 
     python tests/golden/make_golden.py [--ref /root/reference]
 """
@@ -40,6 +42,11 @@ TRANSIENT = [
 ]
 
 
+def vtk_p(td):
+    p = td / "solution_p.vtk"
+    return dict(vtk_p=np.fromfile(p, np.uint8)) if p.exists() else {}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -69,6 +76,8 @@ def main():
                 u0=np.fromfile(td / "u0.f64"), values0=np.fromfile(td / "values0.f64"),
                 rhs0=np.fromfile(td / "rhs0.f64"), usol=np.fromfile(td / "usol.f64"),
                 quad=np.fromfile(td / "quad.f64").reshape(-1, 3),
+                vtk=np.fromfile(td / "solution.vtk", np.uint8),
+                **vtk_p(td),
             )
             np.savez_compressed(HERE / f"{name}.npz", **out)
             print(name, meta["nInc"], meta["nDofs"], len(out["ja"]))
@@ -92,6 +101,8 @@ def main():
                 color_offsets=np.fromfile(td / "color_offsets.i64", np.int64),
                 color_elements=np.fromfile(td / "color_elements.i32", np.int32),
                 usol=np.fromfile(td / "traj.f64"), quad=np.fromfile(td / "quad.f64").reshape(-1, 3),
+                vtk=np.fromfile(td / "solution.vtk", np.uint8),
+                **vtk_p(td),
             )
             np.savez_compressed(HERE / f"{name}.npz", **out)
             print(name, meta["nInc"], meta["nDofs"], len(out["ja"]))
