@@ -38,3 +38,8 @@ def test_invalid_arguments_return_status_without_gpu():
     assert lib.fe_mesh_generate_square(0, 0, 1, 0, 1, 0.1, 1, ctypes.byref(h)) == -3
     assert b"invalid" in lib.fe_cuda_last_error()
     assert lib.fe_mesh_read_msh(b"/nonexistent.msh", ctypes.byref(h)) == -2
+    names = (ctypes.c_char_p * 1)(b"Bord")
+    assert lib.fe_mesh_read_msh_groups(None, b"Domaine", names, 1, None, ctypes.byref(h)) == -3
+    assert lib.fe_mesh_read_msh_groups(b"/nonexistent.msh", b"Domaine", None, 1, None, ctypes.byref(h)) == -3
+    assert lib.fe_mesh_read_msh_groups(b"/nonexistent.msh", b"Domaine", names, 1, None, ctypes.byref(h)) == -2
+    assert lib.fe_export_vtk(None, None, None, None, 0, None, 0, 0, b"x.vtk") == -3
