@@ -89,6 +89,11 @@ SIGNATURES = {
     "fe_mesh_read_msh": (C.c_int, [C.c_char_p, C.POINTER(P)]),
     "fe_export_vtk": (C.c_int, [P, P, P, C.POINTER(C.c_char_p), C.c_int, C.POINTER(C.c_char_p), C.c_int,
                                 C.c_int, C.c_char_p]),
+    "fe_mesh3d_generate_cube": (C.c_int, [C.c_int, P, C.c_double, C.c_uint64, C.POINTER(P)]),
+    "fe_mesh3d_write_msh": (C.c_int, [P, C.c_char_p]),
+    "fe_mesh3d_sizes": (C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "fe_mesh3d_arrays": (C.c_int, [P, P, P, P, P, P]),
+    "fe_mesh3d_destroy": (None, [P]),
     "fe_mesh_read_msh_groups": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_char_p), C.c_int,
                                           C.c_char_p, C.POINTER(P)]),
     "fe_mesh_write_msh": (C.c_int, [P, C.c_char_p]),

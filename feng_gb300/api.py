@@ -110,6 +110,48 @@ class Mesh2DP1:
             self._lib.fe_mesh_destroy(h)
 
 
+class Mesh3DP1:
+    """Tetrahedral mesh with physical groups "Domaine" (tetrahedra) and
+    "Bord" (boundary triangles), read by the reference as feMesh2DP1."""
+
+    def __init__(self, handle):
+        self._h = handle
+        self._lib = _lib.load()
+
+    @classmethod
+    def generate_cube(cls, n: int, x0=0.0, x1=1.0, y0=0.0, y1=1.0, z0=0.0, z1=1.0, jitter=0.05, seed=1):
+        """n^3 cells, 6 Kuhn tetrahedra each, interior vertices jittered by
+        U(-jitter h, jitter h) per axis (SplitMix64 seeded with `seed`)."""
+        lib = _lib.load()
+        box = np.array([x0, x1, y0, y1, z0, z1], np.float64)
+        h = C.c_void_p()
+        check(lib.fe_mesh3d_generate_cube(n, ptr(box), jitter, seed, C.byref(h)))
+        return cls(h)
+
+    def write_msh(self, path: str):
+        check(self._lib.fe_mesh3d_write_msh(self._h, str(path).encode()))
+
+    def sizes(self):
+        nv, nt, nb = C.c_int64(), C.c_int64(), C.c_int64()
+        check(self._lib.fe_mesh3d_sizes(self._h, C.byref(nv), C.byref(nt), C.byref(nb)))
+        return nv.value, nt.value, nb.value
+
+    def arrays(self):
+        nv, nt, nb = self.sizes()
+        x, y, z = np.empty(nv), np.empty(nv), np.empty(nv)
+        tet, bnd = np.empty(4 * nt, np.int32), np.empty(3 * nb, np.int32)
+        check(self._lib.fe_mesh3d_arrays(self._h, ptr(x), ptr(y), ptr(z), ptr(tet), ptr(bnd)))
+        return dict(x=x, y=y, z=z, tet=tet.reshape(-1, 4), bnd=bnd.reshape(-1, 3))
+
+    def getNumElements(self):
+        return self.sizes()[1]
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h:
+            self._lib.fe_mesh3d_destroy(h)
+
+
 @dataclass
 class feSpace:
     mesh: Mesh2DP1

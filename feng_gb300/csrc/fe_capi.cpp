@@ -12,6 +12,7 @@
 #include "fe_common.h"
 #include "fe_export.h"
 #include "fe_mesh.h"
+#include "fe_mesh3d.h"
 #include "fe_setup.h"
 #include "fe_system.h"
 #include "fe_transient.h"
@@ -38,6 +39,10 @@ using namespace feng;
 
 struct fe_mesh {
   Mesh2D m;
+};
+
+struct fe_mesh3d {
+  Mesh3D m;
 };
 
 struct fe_cuda_system {
@@ -247,6 +252,48 @@ int fe_mesh_arrays(const fe_mesh *m, double *x, double *y, int32_t *tri, int32_t
 }
 
 void fe_mesh_destroy(fe_mesh *m) { delete m; }
+
+int fe_mesh3d_generate_cube(int n, const double *box, double jitter, uint64_t seed, fe_mesh3d **out)
+{
+  GUARD_BEGIN
+  if(!out || !box) { set_error("null argument"); return FE_INVALID_ARG; }
+  std::unique_ptr<fe_mesh3d> m(new fe_mesh3d());
+  FE_TRY(mesh3d_generate_cube(m->m, n, box, jitter, seed));
+  *out = m.release();
+  return FE_OK;
+  GUARD_END
+}
+
+int fe_mesh3d_write_msh(const fe_mesh3d *m, const char *path)
+{
+  GUARD_BEGIN
+  if(!m || !path) { set_error("null argument"); return FE_INVALID_ARG; }
+  return mesh3d_write_msh41(m->m, path);
+  GUARD_END
+}
+
+int fe_mesh3d_sizes(const fe_mesh3d *m, int64_t *nv, int64_t *nt, int64_t *nb)
+{
+  if(!m) { set_error("null mesh"); return FE_INVALID_ARG; }
+  if(nv) *nv = m->m.n_vertices();
+  if(nt) *nt = m->m.n_tets();
+  if(nb) *nb = m->m.n_boundary();
+  return FE_OK;
+}
+
+int fe_mesh3d_arrays(const fe_mesh3d *m, double *x, double *y, double *z, int32_t *tet, int32_t *bnd)
+{
+  if(!m) { set_error("null mesh"); return FE_INVALID_ARG; }
+  const Mesh3D &M = m->m;
+  if(x) std::copy(M.x.begin(), M.x.end(), x);
+  if(y) std::copy(M.y.begin(), M.y.end(), y);
+  if(z) std::copy(M.z.begin(), M.z.end(), z);
+  if(tet) std::copy(M.tet.begin(), M.tet.end(), tet);
+  if(bnd) std::copy(M.bnd.begin(), M.bnd.end(), bnd);
+  return FE_OK;
+}
+
+void fe_mesh3d_destroy(fe_mesh3d *m) { delete m; }
 
 static int to_spaces(const fe_space_desc *spaces, int n, std::vector<SpaceDesc> &out)
 {

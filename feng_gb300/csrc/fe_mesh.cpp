@@ -12,26 +12,6 @@
 
 namespace feng {
 
-namespace {
-
-// SplitMix64 (Steele, Lea, Flood 2014): the generator named in the mesh
-// header comment, so the jitter can be regenerated from the seed alone.
-struct SplitMix64 {
-  uint64_t s;
-  explicit SplitMix64(uint64_t seed) : s(seed) {}
-  uint64_t next()
-  {
-    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-  }
-  // Uniform double in [-1, 1) with 53 random bits.
-  double uniform_pm1() { return (double)(next() >> 11) * (2.0 / 9007199254740992.0) - 1.0; }
-};
-
-}  // namespace
-
 int Mesh2D::build_topology()
 {
   const int64_t nt = n_triangles();

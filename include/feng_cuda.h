@@ -65,6 +65,7 @@ extern "C" {
 #define FE_CNC_POINT 2     /* "PointPression" */
 
 typedef struct fe_mesh fe_mesh;
+typedef struct fe_mesh3d fe_mesh3d;
 typedef struct fe_cuda_system fe_cuda_system;
 
 /* One bilinear/linear form: createBilinearForm(spaces, new feSysElm_*(coeffs)),
@@ -176,6 +177,19 @@ int fe_mesh_sizes(const fe_mesh *m, int64_t *n_vertices, int64_t *n_triangles, i
 int fe_mesh_arrays(const fe_mesh *m, double *x, double *y, int32_t *tri, int32_t *tri_edges,
                    int32_t *bnd, int32_t *point);
 void fe_mesh_destroy(fe_mesh *m);
+
+/* ---- 3D tetrahedral meshes ("Domaine" tetrahedra, "Bord" boundary
+ * triangles; read by the reference as feMesh2DP1, src/feMeshRead.cpp:1481-1538).
+ * fe_mesh3d_generate_cube: n^3 cells of box {x0,x1,y0,y1,z0,z1}, 6 Kuhn
+ * tetrahedra per cell (positive volumes, conforming), interior vertices
+ * jittered by U(-jitter h, jitter h) per axis from SplitMix64(seed); boundary
+ * triangles oriented outwards. */
+int fe_mesh3d_generate_cube(int n, const double *box, double jitter, uint64_t seed, fe_mesh3d **out);
+int fe_mesh3d_write_msh(const fe_mesh3d *m, const char *path);
+int fe_mesh3d_sizes(const fe_mesh3d *m, int64_t *n_vertices, int64_t *n_tets, int64_t *n_boundary);
+/* Any output may be NULL.  x,y,z [nv]; tet [4 nt]; bnd [3 nb]. */
+int fe_mesh3d_arrays(const fe_mesh3d *m, double *x, double *y, double *z, int32_t *tet, int32_t *bnd);
+void fe_mesh3d_destroy(fe_mesh3d *m);
 
 /* ---- host set-up of the standalone route (no device needed):
  * DOF numbering (feMetaNumber, src/feNumber.cpp:677-835), element-to-DOF

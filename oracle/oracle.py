@@ -282,3 +282,75 @@ def newton_direct(op, u, tol_residual=1e-10, tol_correction=1e-10, max_iter=20, 
         if np.max(np.abs(du)) <= tol_correction:
             return u, it + 1
     return u, max_iter
+
+
+# ---- P2 tetrahedra: diffusion + source (numpy restatement) ---------------------
+
+# Local edges of a tetrahedron, in the order of its edge DOFs
+# (_edgesOrder, src/feTetrahedron.h:31; getTetLagrangeBarycentricCoord,
+# src/feTetrahedron.cpp:170-194).
+TET_EDGES = ((0, 2), (2, 1), (1, 0), (1, 3), (3, 0), (3, 2))
+
+
+def tet_p2_basis(r, s, t):
+    """feSpaceTetPn with n = 2 (src/feSpace_3D.cpp:104-235): barycentric
+    l = (1 - r - s - t, r, s, t); vertex functions l_i (2 l_i - 1), then edge
+    functions 4 l_a l_b over TET_EDGES.  Returns phi (nq, 10) and the
+    reference gradients d phi / d(r, s, t) (nq, 10, 3)."""
+    r, s, t = (np.asarray(v, np.float64) for v in (r, s, t))
+    lam = np.stack([1 - r - s - t, r, s, t], -1)
+    dlam = np.array([[-1, -1, -1], [1, 0, 0], [0, 1, 0], [0, 0, 1]], np.float64)
+    phi = [lam[..., i] * (2 * lam[..., i] - 1) for i in range(4)]
+    phi += [4 * lam[..., a] * lam[..., b] for a, b in TET_EDGES]
+    dphi = [np.multiply.outer(4 * lam[..., i] - 1, dlam[i]) for i in range(4)]
+    dphi += [4 * (np.multiply.outer(lam[..., b], dlam[a]) + np.multiply.outer(lam[..., a], dlam[b]))
+             for a, b in TET_EDGES]
+    return np.stack(phi, -1), np.stack(dphi, -2)
+
+
+def tet_p2_diffusion(adr, tet_xyz, quad, u, n_inc, ia, ja, coeff=1.0, source=None):
+    """CSR values and residual of feSysElm_Diffusion<3> (+ feSysElm_Source)
+    on P2 tetrahedra, scattered as the MKL backend does (rows and columns of
+    essential DOFs dropped; feLinearSystemMklPardiso.cpp:501-749):
+
+      Ae_ij = sum_q k grad phi_i . grad phi_j J w       (src/feSysElm.cpp:531-556)
+      Be_i  = - sum_q k grad phi_i . grad u_h J w       (src/feSysElm.cpp:558-583)
+              - sum_q phi_i f(x_q) J w                  (src/feSysElm.cpp:16-27)
+
+    with the affine map of the P1 tetrahedron (J = det [x1-x0, x2-x0, x3-x0],
+    grad phi = J^-T d phi/d(r,s,t)) and x_q interpolated from the vertices.
+    adr (nElm, 10); tet_xyz (nElm, 4, 3); quad (nq, 4) rows r, s, t, w;
+    source(x, y, z) -> f or None."""
+    adr = np.asarray(adr, np.int64).reshape(-1, 10)
+    X = np.asarray(tet_xyz, np.float64).reshape(-1, 4, 3)
+    q = np.asarray(quad, np.float64).reshape(-1, 4)
+    ia, ja = np.asarray(ia, np.int64), np.asarray(ja, np.int64)
+    jm = np.stack([X[:, 1] - X[:, 0], X[:, 2] - X[:, 0], X[:, 3] - X[:, 0]], -1)
+    det, inv = np.linalg.det(jm), np.linalg.inv(jm)
+    phi, dphi = tet_p2_basis(q[:, 0], q[:, 1], q[:, 2])
+    w = q[:, 3]
+    grad = np.einsum("qfk,ekx->eqfx", dphi, inv)
+    ae = coeff * np.einsum("eqix,eqjx,q,e->eij", grad, grad, w, det)
+    gu = np.einsum("eqfx,ef->eqx", grad, np.asarray(u, np.float64)[adr])
+    be = -coeff * np.einsum("eqix,eqx,q,e->ei", grad, gu, w, det)
+    if source is not None:
+        psi = np.stack([1 - q[:, 0] - q[:, 1] - q[:, 2], q[:, 0], q[:, 1], q[:, 2]], -1)
+        xq = np.einsum("qv,evx->eqx", psi, X)
+        f = source(xq[..., 0], xq[..., 1], xq[..., 2])
+        be -= np.einsum("qi,eq,q,e->ei", phi, f, w, det)
+    rhs = np.zeros(n_inc)
+    keep = adr < n_inc
+    np.add.at(rhs, adr[keep], be[keep])
+    rows = np.broadcast_to(adr[:, :, None], ae.shape)
+    cols = np.broadcast_to(adr[:, None, :], ae.shape)
+    m = (rows < n_inc) & (cols < n_inc)
+    # Position of (r, c) in the pattern: rows in order, columns ascending
+    # within a row, so row * (n + 1) + column ascends over the whole array.
+    lin = np.repeat(np.arange(n_inc), np.diff(ia)) * (n_inc + 1) + ja
+    want = rows[m] * (n_inc + 1) + cols[m]
+    pos = np.minimum(np.searchsorted(lin, want), len(lin) - 1)
+    if not np.array_equal(lin[pos], want):
+        raise ValueError("an element coupling lies outside the CSR pattern")
+    values = np.zeros(len(ja))
+    np.add.at(values, pos, ae[m])
+    return values, rhs

@@ -12,7 +12,7 @@
 // the CSR row) and solves with the vendored Eigen SparseLU.
 //
 // usage: ref_harness <mesh.msh> <problem> <outdir> [Re] [seed]
-//   problem: diffusion | ns_kovasznay | ns_mms | ns_cavity_bdf2 (then [dt] [steps])
+//   problem: diffusion | diffusion3d | ns_kovasznay | ns_mms | ns_cavity_bdf2 (then [dt] [steps])
 // writes raw little-endian arrays (see write_* calls) and meta.txt.
 #include <Eigen/Sparse>
 #include <Eigen/SparseLU>
@@ -222,6 +222,14 @@ double sinsin_src(const feFunctionArguments &a, const std::vector<double> &)
 {
   return -2. * M_PI * M_PI * sin(M_PI * a.pos[0]) * sin(M_PI * a.pos[1]);
 }
+double sinsinsin(const feFunctionArguments &a, const std::vector<double> &)
+{
+  return sin(M_PI * a.pos[0]) * sin(M_PI * a.pos[1]) * sin(M_PI * a.pos[2]);
+}
+double sinsinsin_src(const feFunctionArguments &a, const std::vector<double> &)
+{
+  return -3. * M_PI * M_PI * sin(M_PI * a.pos[0]) * sin(M_PI * a.pos[1]) * sin(M_PI * a.pos[2]);
+}
 double kov_lambda() { return g_re / 2. - sqrt(g_re * g_re / 4. + 4. * M_PI * M_PI); }
 void kov_u(const feFunctionArguments &a, const std::vector<double> &, std::vector<double> &r)
 {
@@ -285,7 +293,7 @@ feStatus write_vtk(const std::string &dir, feMetaNumber &numbering, feSolution &
 int main(int argc, char **argv)
 {
   if(argc < 4) {
-    fprintf(stderr, "usage: %s mesh.msh diffusion|ns_kovasznay|ns_mms|ns_cavity_bdf2 outdir [Re] [seed] [dt] [steps]\n", argv[0]);
+    fprintf(stderr, "usage: %s mesh.msh diffusion|diffusion3d|ns_kovasznay|ns_mms|ns_cavity_bdf2 outdir [Re] [seed] [dt] [steps]\n", argv[0]);
     return 2;
   }
   const std::string meshFile = argv[1], problem = argv[2], out = argv[3];
@@ -297,6 +305,8 @@ int main(int argc, char **argv)
 
   feMesh2DP1 mesh(meshFile);
   feFunction fSinSin(sinsin), fSrc(sinsin_src), fKovP(kov_p), fMmsP(mms_p);
+  feFunction fSin3(sinsinsin), fSrc3(sinsinsin_src);
+  const bool dim3 = problem == "diffusion3d";
   feVectorFunction fKovU(kov_u), fMmsU(mms_u), fMmsSrc(mms_src);
   feConstantFunction fMu(1.0 / g_re);
   feVectorFunction fLid(cavity_lid);
@@ -305,9 +315,9 @@ int main(int argc, char **argv)
   std::vector<feSpace *> spaces, essential, domainSpaces;
   std::vector<feBilinearForm *> forms;
   int degQ = 4;
-  if(problem == "diffusion") {
+  if(problem == "diffusion" || dim3) {
     feSpace *u = nullptr, *uB = nullptr;
-    feCheck(createFiniteElementSpace(uB, &mesh, elementType::LAGRANGE, 2, "U", "Bord", degQ, &fSinSin));
+    feCheck(createFiniteElementSpace(uB, &mesh, elementType::LAGRANGE, 2, "U", "Bord", degQ, dim3 ? &fSin3 : &fSinSin));
     feCheck(createFiniteElementSpace(u, &mesh, elementType::LAGRANGE, 2, "U", "Domaine", degQ, &scalarConstant::zero));
     spaces = {uB, u};
     essential = {uB};
@@ -329,10 +339,13 @@ int main(int argc, char **argv)
   feMetaNumber numbering(&mesh, spaces, essential);
   feSolution sol(numbering.getNbDOFs(), spaces, essential);
 
-  if(problem == "diffusion") {
+  if(problem == "diffusion" || dim3) {
     feBilinearForm *diff = nullptr, *src = nullptr;
-    feCheck(createBilinearForm(diff, {domainSpaces[0]}, new feSysElm_Diffusion<2>(&scalarConstant::one)));
-    feCheck(createBilinearForm(src, {domainSpaces[0]}, new feSysElm_Source(&fSrc)));
+    if(dim3)
+      feCheck(createBilinearForm(diff, {domainSpaces[0]}, new feSysElm_Diffusion<3>(&scalarConstant::one)));
+    else
+      feCheck(createBilinearForm(diff, {domainSpaces[0]}, new feSysElm_Diffusion<2>(&scalarConstant::one)));
+    feCheck(createBilinearForm(src, {domainSpaces[0]}, new feSysElm_Source(dim3 ? &fSrc3 : &fSrc)));
     forms = {diff, src};
   } else {
     feSpace *u = domainSpaces[0], *p = domainSpaces[1];
@@ -385,7 +398,13 @@ int main(int argc, char **argv)
     const auto &w = s->getQuadratureWeights();
     const auto &r = s->getRQuadraturePoints();
     const auto &q = s->getSQuadraturePoints();
-    for(size_t k = 0; k < w.size(); ++k) { quad.push_back(r[k]); quad.push_back(q[k]); quad.push_back(w[k]); }
+    const auto &z = s->getTQuadraturePoints();
+    for(size_t k = 0; k < w.size(); ++k) {
+      quad.push_back(r[k]);
+      quad.push_back(q[k]);
+      if(dim3) quad.push_back(z[k]);  // 3D rules: r, s, t, w
+      quad.push_back(w[k]);
+    }
   }
 
   if(cavity) {
@@ -447,7 +466,7 @@ int main(int argc, char **argv)
   sys->assembleResiduals(&sol);
   double rfinal = 0;
   sys->getRHSMaxNorm(&rfinal);
-  feCheck(write_vtk(out, numbering, sol, mesh, spaces));
+  if(!dim3) feCheck(write_vtk(out, numbering, sol, mesh, spaces));
 
   write_raw(out + "/ia.i64", ia);
   write_raw(out + "/ja.i64", ja);

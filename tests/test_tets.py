@@ -1,0 +1,97 @@
+"""Tetrahedral meshes and the P2 diffusion oracle on them, against the
+reference run on the same mesh (tests/golden/diffusion3d_p2_4.npz, made by
+tests/golden/make_golden.py: the reference reads the generated msh file and
+assembles feSysElm_Diffusion<3> + feSysElm_Source on feSpaceTetPn(2), then
+solves).  Runs on the CPU."""
+from collections import Counter
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import feng_gb300 as fe
+from feng_gb300._lib import FeError
+from oracle.oracle import tet_p2_diffusion
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def _golden():
+    return np.load(GOLDEN / "diffusion3d_p2_4.npz")
+
+
+def _sinsinsin_src(x, y, z):
+    return -3 * np.pi ** 2 * np.sin(np.pi * x) * np.sin(np.pi * y) * np.sin(np.pi * z)
+
+
+def test_cube_mesh_reproduces_fixture():
+    g = _golden()
+    a = fe.Mesh3DP1.generate_cube(int(g["n"]), jitter=float(g["jitter"]), seed=int(g["seed"])).arrays()
+    for k in ("x", "y", "z", "tet", "bnd"):
+        np.testing.assert_array_equal(a[k], g[k])
+
+
+def test_cube_mesh_is_conforming_and_oriented():
+    n = 5
+    m = fe.Mesh3DP1.generate_cube(n, 0.0, 2.0, -1.0, 0.5, 0.0, 1.0, jitter=0.05, seed=7)
+    a = m.arrays()
+    assert m.sizes() == ((n + 1) ** 3, 6 * n ** 3, 12 * n * n)
+    x = np.stack([a["x"], a["y"], a["z"]], 1)
+    t = a["tet"]
+    vol = np.einsum("ij,ij->i", x[t[:, 1]] - x[t[:, 0]],
+                    np.cross(x[t[:, 2]] - x[t[:, 0]], x[t[:, 3]] - x[t[:, 0]])) / 6
+    assert vol.min() > 0
+    assert vol.sum() == pytest.approx(2.0 * 1.5 * 1.0, rel=1e-13)
+    faces = Counter(tuple(sorted(tt[f])) for tt in t for f in ([0, 1, 2], [0, 1, 3], [0, 2, 3], [1, 2, 3]))
+    assert set(faces.values()) <= {1, 2}
+    assert {k for k, c in faces.items() if c == 1} == {tuple(sorted(b)) for b in a["bnd"]}
+    b = a["bnd"]
+    normal = np.cross(x[b[:, 1]] - x[b[:, 0]], x[b[:, 2]] - x[b[:, 0]])
+    assert np.all(np.einsum("ij,ij->i", normal, x[b].mean(1) - np.array([1.0, -0.25, 0.5])) > 0)
+    # the seed alone fixes the jitter
+    np.testing.assert_array_equal(fe.Mesh3DP1.generate_cube(n, 0.0, 2.0, -1.0, 0.5, 0.0, 1.0, jitter=0.05,
+                                                            seed=7).arrays()["x"], a["x"])
+
+
+def test_cube_mesh_arguments():
+    for kw in (dict(n=0), dict(n=2, jitter=0.3), dict(n=2, x1=-1.0)):
+        with pytest.raises(FeError):
+            fe.Mesh3DP1.generate_cube(**kw)
+
+
+def test_reference_reads_cube_mesh_as_generated():
+    """The reference's reader takes the file: 6 n^3 tetrahedra, and P2 DOFs
+    on the (2n+1)^3 lattice of vertices and edge midpoints, the interior
+    ones unknown."""
+    g = _golden()
+    n = int(g["n"])
+    assert len(g["adr"]) == 10 * 6 * n ** 3
+    assert int(g["nDofs"]) == (2 * n + 1) ** 3 and int(g["nInc"]) == (2 * n - 1) ** 3
+
+
+def test_oracle_tet_diffusion_matches_reference():
+    g = _golden()
+    xyz = np.stack([g["x"], g["y"], g["z"]], 1)[g["tet"]]
+    vals, rhs = tet_p2_diffusion(g["adr"], xyz, g["quad"], g["u0"], int(g["nInc"]), g["ia"], g["ja"],
+                                 source=_sinsinsin_src)
+    assert np.max(np.abs(vals - g["values0"])) <= 1e-12 * np.max(np.abs(g["values0"]))
+    assert np.max(np.abs(rhs - g["rhs0"])) <= 1e-12 * np.max(np.abs(g["rhs0"]))
+
+
+def test_oracle_tet_diffusion_solution_matches_reference():
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    g = _golden()
+    n_inc = int(g["nInc"])
+    xyz = np.stack([g["x"], g["y"], g["z"]], 1)[g["tet"]]
+    u = g["usol"].copy()
+    u[:n_inc] = 0.0
+    vals, rhs = tet_p2_diffusion(g["adr"], xyz, g["quad"], u, n_inc, g["ia"], g["ja"], source=_sinsinsin_src)
+    du = spl.spsolve(sp.csr_matrix((vals, g["ja"], g["ia"]), shape=(n_inc, n_inc)).tocsc(), rhs)
+    u[:n_inc] += du
+    assert np.max(np.abs(u - g["usol"])) <= 1e-8 * np.max(np.abs(g["usol"]))
+    # The vertex values approximate u = sin(pi x) sin(pi y) sin(pi z).
+    adr = g["adr"].reshape(-1, 10)
+    v, d = g["tet"].reshape(-1), adr[:, :4].reshape(-1)
+    exact = np.sin(np.pi * g["x"][v]) * np.sin(np.pi * g["y"][v]) * np.sin(np.pi * g["z"][v])
+    assert np.max(np.abs(u[d] - exact)) < 0.02
