@@ -29,11 +29,14 @@ def load_golden(name):
 
 
 def golden_names(transient=False):
-    """Fixture names: the steady cases (assembly state + Newton solution), or
-    the BDF2 runs with transient=True."""
+    """Fixture names of the triangle cases: the steady cases (assembly state
+    + Newton solution), or the BDF2 runs with transient=True.  Tetrahedral
+    fixtures (key "tet") have their own tests."""
     out = []
     for p in sorted(GOLDEN.glob("*.npz")):
         with np.load(p) as z:
+            if "tet" in z.files:
+                continue
             if ("steps" in z.files) == transient:
                 out.append(p.stem)
     return out
