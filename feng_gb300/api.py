@@ -39,7 +39,7 @@ SOURCE, DIFFUSION, VECTOR_SOURCE, TRANSIENT_VECTOR_MASS = 1, 2, 3, 4
 MIXED_DIVERGENCE, VECTOR_CONVECTIVE_ACCELERATION, DIV_NEWTONIAN_STRESS = 5, 6, 7
 # Device source registry (FE_SRC_*)
 SRC_NONE, SRC_SIN_SIN, SRC_NS_MMS_POLY, SRC_CONST_VEC, SRC_SIN_BODY = 0, 1, 2, 3, 4
-ELEM_P2, ELEM_TAYLOR_HOOD = 1, 2
+ELEM_P2, ELEM_TAYLOR_HOOD, ELEM_TET_P2, ELEM_TET_TAYLOR_HOOD = 1, 2, 3, 4
 
 
 class Mesh2DP1:
@@ -164,7 +164,9 @@ class feSpace:
 
     @property
     def ncomp(self):
-        return 2 if self.element == VECTOR_LAGRANGE else 1
+        if self.element != VECTOR_LAGRANGE:
+            return 1
+        return 3 if isinstance(self.mesh, Mesh3DP1) else 2
 
 
 def createFiniteElementSpace(mesh, element, degree, fieldID, cncGeoID, degreeQuadrature, fct=None):
@@ -199,8 +201,11 @@ class feMetaNumber:
                                     int(any(s is e for e in self.essentialSpaces)))
         self._desc = arr
         dom = [s for s in self.spaces if s.cncGeoID == "Domaine"]
-        self.elem_type = ELEM_TAYLOR_HOOD if any(
-            s.element == VECTOR_LAGRANGE and s.degree == 2 for s in dom) else ELEM_P2
+        vector = any(s.element == VECTOR_LAGRANGE and s.degree == 2 for s in dom)
+        if isinstance(mesh, Mesh3DP1):
+            self.elem_type = ELEM_TET_TAYLOR_HOOD if vector else ELEM_TET_P2
+        else:
+            self.elem_type = ELEM_TAYLOR_HOOD if vector else ELEM_P2
         qdeg = {s.degreeQuadrature for s in dom}
         if len(qdeg) != 1:
             raise ValueError("the domain spaces must share one quadrature degree")
@@ -230,9 +235,14 @@ class feSetup:
         self.lib = _lib.load()
         self.numbering = numbering
         h = C.c_void_p()
-        check(self.lib.fe_setup_create(numbering.mesh._h, C.cast(numbering._desc, C.c_void_p),
-                                       len(numbering.spaces), numbering.elem_type,
-                                       numbering.quad_degree, pc_block_rows, C.byref(h)))
+        if isinstance(numbering.mesh, Mesh3DP1):
+            check(self.lib.fe_setup3d_create(numbering.mesh._h, C.cast(numbering._desc, C.c_void_p),
+                                             len(numbering.spaces), numbering.elem_type, pc_block_rows,
+                                             C.byref(h)))
+        else:
+            check(self.lib.fe_setup_create(numbering.mesh._h, C.cast(numbering._desc, C.c_void_p),
+                                           len(numbering.spaces), numbering.elem_type,
+                                           numbering.quad_degree, pc_block_rows, C.byref(h)))
         self._h = h
         n = [C.c_int64() for _ in range(4)]
         nc, nl = C.c_int(), C.c_int()
@@ -268,6 +278,12 @@ class feSetup:
         v = np.empty(self.nDofs, np.int32)
         check(self.lib.fe_setup_get_dof_info(self._h, ptr(x), ptr(y), ptr(f), ptr(c), ptr(v)))
         return x, y, f, c, v
+
+    def dofZ(self):
+        """z coordinate of every DOF (tetrahedral meshes)."""
+        z = np.empty(self.nDofs)
+        check(self.lib.fe_setup_get_dof_z(self._h, ptr(z)))
+        return z
 
     def blocks(self):
         b = np.empty(self.nInc, np.int32)

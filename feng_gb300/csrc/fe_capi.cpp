@@ -58,6 +58,7 @@ struct fe_cuda_system {
 };
 
 struct fe_setup {
+  bool tets = false;                  // built on a tetrahedral mesh
   std::vector<SpaceDesc> spaces;
   int64_t nVertices = 0, nEdges = 0;  // of the mesh the setup was built on
   Numbering num;
@@ -309,6 +310,52 @@ static int to_spaces(const fe_space_desc *spaces, int n, std::vector<SpaceDesc> 
   return FE_OK;
 }
 
+// Block-Jacobi partition: unknowns grouped by the smallest mesh vertex
+// they touch, in contiguous vertex ranges, so a block holds the velocity and
+// pressure unknowns of one patch (velocity rows first, as numbered).
+// Saddle-point rows (the pressure field, whose diagonal no form fills) get a
+// nonzero ILU(0) pivot only through eliminated velocity unknowns of the same
+// block: a pressure row with no velocity unknown in its block (next to
+// essential velocities at a block border) joins the block of its first
+// coupled velocity unknown.
+static void block_partition(const Numbering &num, const CSRPattern &pat, const int32_t *edge_v, int64_t nEdges,
+                            int64_t nv, int pc_block_rows, bool saddle, int fieldU, int fieldP,
+                            std::vector<int32_t> &blockOfRow)
+{
+  const int64_t nInc = num.nInc;
+  const int64_t nb = pc_block_rows > 0 ? std::max<int64_t>(1, nInc / pc_block_rows) : 1;
+  std::vector<int64_t> key(num.nDofs, 0);
+  for(int f = 0; f < num.nFields; ++f) {
+    const int C = num.fieldComp[f];
+    for(int64_t v = 0; v < nv; ++v)
+      for(int c = 0; c < C; ++c) {
+        int64_t d = num.vdof[f][v * C + c];
+        if(d >= 0) key[d] = v;
+      }
+    for(int64_t e = 0; e < nEdges; ++e)
+      for(int c = 0; c < C; ++c) {
+        int64_t d = num.edof[f][e * C + c];
+        if(d >= 0) key[d] = std::min(edge_v[2 * e], edge_v[2 * e + 1]);
+      }
+  }
+  blockOfRow.resize(nInc);
+  for(int64_t i = 0; i < nInc; ++i) blockOfRow[i] = (int32_t)((key[i] * nb) / nv);
+  if(saddle && nb > 1) {
+    for(int64_t i = 0; i < nInc; ++i) {
+      if(num.dof_field[i] != fieldP) continue;
+      int64_t firstU = -1;
+      bool inBlock = false;
+      for(int64_t k = pat.ia[i]; k < pat.ia[i + 1]; ++k) {
+        const int32_t j = pat.ja[k];
+        if(num.dof_field[j] != fieldU) continue;
+        if(firstU < 0) firstU = j;
+        if(blockOfRow[j] == blockOfRow[i]) { inBlock = true; break; }
+      }
+      if(!inBlock && firstU >= 0) blockOfRow[i] = blockOfRow[firstU];
+    }
+  }
+}
+
 int fe_setup_create(const fe_mesh *m, const fe_space_desc *spaces, int nspaces, int elem_type,
                     int quad_degree, int pc_block_rows, fe_setup **out)
 {
@@ -336,47 +383,8 @@ int fe_setup_create(const fe_mesh *m, const fe_space_desc *spaces, int nspaces, 
   FE_TRY(color_elements(M, S->col));
   FE_TRY(build_csr_pattern(S->et, S->num.nInc, S->pat));
   FE_TRY(triangle_rule(quad_degree, S->quad));
-  // Block-Jacobi partition: unknowns grouped by the smallest mesh vertex
-  // they touch, in contiguous vertex ranges, so a block holds the velocity
-  // and pressure unknowns of one patch (velocity rows first, as numbered).
-  const int64_t nInc = S->num.nInc;
-  const int64_t nb = pc_block_rows > 0 ? std::max<int64_t>(1, nInc / pc_block_rows) : 1;
-  const int64_t nv = M.n_vertices();
-  std::vector<int64_t> key(S->num.nDofs, 0);
-  for(int f = 0; f < S->num.nFields; ++f) {
-    const int C = S->num.fieldComp[f];
-    for(int64_t v = 0; v < nv; ++v)
-      for(int c = 0; c < C; ++c) {
-        int64_t d = S->num.vdof[f][v * C + c];
-        if(d >= 0) key[d] = v;
-      }
-    for(int64_t e = 0; e < M.n_edges; ++e)
-      for(int c = 0; c < C; ++c) {
-        int64_t d = S->num.edof[f][e * C + c];
-        if(d >= 0) key[d] = std::min(M.edge_v[2 * e], M.edge_v[2 * e + 1]);
-      }
-  }
-  S->blockOfRow.resize(nInc);
-  for(int64_t i = 0; i < nInc; ++i) S->blockOfRow[i] = (int32_t)((key[i] * nb) / nv);
-  // Saddle-point rows (the pressure field, whose diagonal no form fills)
-  // get a nonzero ILU(0) pivot only through eliminated velocity unknowns of
-  // the same block.  A pressure row with no velocity unknown in its block
-  // (next to essential velocities at a block border) joins the block of its
-  // first coupled velocity unknown.
-  if(elem_type == ELEM_TAYLOR_HOOD && nb > 1) {
-    for(int64_t i = 0; i < nInc; ++i) {
-      if(S->num.dof_field[i] != fieldP) continue;
-      int64_t firstU = -1;
-      bool inBlock = false;
-      for(int64_t k = S->pat.ia[i]; k < S->pat.ia[i + 1]; ++k) {
-        const int32_t j = S->pat.ja[k];
-        if(S->num.dof_field[j] != fieldU) continue;
-        if(firstU < 0) firstU = j;
-        if(S->blockOfRow[j] == S->blockOfRow[i]) { inBlock = true; break; }
-      }
-      if(!inBlock && firstU >= 0) S->blockOfRow[i] = S->blockOfRow[firstU];
-    }
-  }
+  block_partition(S->num, S->pat, M.edge_v.data(), M.n_edges, M.n_vertices(), pc_block_rows,
+                  elem_type == ELEM_TAYLOR_HOOD, fieldU, fieldP, S->blockOfRow);
   S->elemXY.resize(M.n_triangles() * 6);
   for(int64_t t = 0; t < M.n_triangles(); ++t)
     for(int k = 0; k < 3; ++k) {
@@ -386,6 +394,50 @@ int fe_setup_create(const fe_mesh *m, const fe_space_desc *spaces, int nspaces, 
   *out = S.release();
   return FE_OK;
   GUARD_END
+}
+
+int fe_setup3d_create(const fe_mesh3d *m, const fe_space_desc *spaces, int nspaces, int elem_type,
+                      int pc_block_rows, fe_setup **out)
+{
+  GUARD_BEGIN
+  if(!m || !out) { set_error("null argument"); return FE_INVALID_ARG; }
+  if(pc_block_rows < 0) { set_error("negative block size"); return FE_INVALID_ARG; }
+  if(elem_type != ELEM_TET_P2 && elem_type != ELEM_TET_TAYLOR_HOOD) {
+    set_error("element type %d is not a tetrahedral type", elem_type);
+    return FE_INVALID_ARG;
+  }
+  std::vector<SpaceDesc> sp;
+  FE_TRY(to_spaces(spaces, nspaces, sp));
+  std::unique_ptr<fe_setup> S(new fe_setup());
+  const Mesh3D &M = m->m;
+  S->tets = true;
+  FE_TRY(build_numbering3d(M, sp, S->num));
+  S->spaces = sp;
+  S->nVertices = M.n_vertices();
+  S->nEdges = M.n_edges;
+  int fieldU = -1, fieldP = -1;
+  for(const SpaceDesc &d : sp) {
+    if(d.cnc != CNC_DOMAIN) continue;
+    if(d.degree == 2 && fieldU < 0) fieldU = d.field;
+    if(d.degree == 1 && fieldP < 0) fieldP = d.field;
+  }
+  FE_TRY(build_element_tables3d(M, S->num, elem_type, fieldU, elem_type == ELEM_TET_TAYLOR_HOOD ? fieldP : -1,
+                                S->et));
+  FE_TRY(color_elements3d(M, S->col));
+  FE_TRY(build_csr_pattern(S->et, S->num.nInc, S->pat));
+  block_partition(S->num, S->pat, M.edge_v.data(), M.n_edges, M.n_vertices(), pc_block_rows,
+                  elem_type == ELEM_TET_TAYLOR_HOOD, fieldU, fieldP, S->blockOfRow);
+  *out = S.release();
+  return FE_OK;
+  GUARD_END
+}
+
+int fe_setup_get_dof_z(const fe_setup *s, double *z)
+{
+  if(!s) { set_error("null setup"); return FE_INVALID_ARG; }
+  if(!s->tets) { set_error("a triangle set-up has no z coordinates"); return FE_INVALID_ARG; }
+  if(z) std::copy(s->num.dof_z.begin(), s->num.dof_z.end(), z);
+  return FE_OK;
 }
 
 void fe_setup_destroy(fe_setup *s) { delete s; }
@@ -467,6 +519,10 @@ int fe_cuda_system_create(const fe_setup *setup, const fe_form_desc *forms, int 
 {
   GUARD_BEGIN
   if(!setup || !out || (!forms && nforms > 0)) { set_error("null argument"); return FE_INVALID_ARG; }
+  if(setup->tets) {
+    set_error("device systems on tetrahedral set-ups are not built yet");
+    return FE_INVALID_ARG;
+  }
   FE_TRY(check_options(opt));
   if(opt->quad_degree != setup->quad.degree) {
     set_error("options ask for quadrature degree %d, the set-up was built with %d",
@@ -996,7 +1052,7 @@ int fe_export_vtk(const fe_mesh *m, const fe_setup *s, const double *solution,
     set_error("null argument");
     return FE_INVALID_ARG;
   }
-  if(m->m.n_vertices() != s->nVertices || m->m.n_edges != s->nEdges) {
+  if(s->tets || m->m.n_vertices() != s->nVertices || m->m.n_edges != s->nEdges) {
     set_error("the setup was not built on this mesh");
     return FE_INVALID_ARG;
   }

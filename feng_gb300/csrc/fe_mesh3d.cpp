@@ -3,10 +3,58 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <unordered_map>
 
 #include "fe_common.h"
 
 namespace feng {
+
+const int TET_FACES[4][3] = {{0, 2, 1}, {0, 1, 3}, {0, 3, 2}, {3, 1, 2}};
+const int TET_EDGES[6][2] = {{0, 2}, {2, 1}, {1, 0}, {1, 3}, {3, 0}, {3, 2}};
+
+int Mesh3D::build_topology()
+{
+  const int64_t nv = n_vertices(), nt = n_tets(), nb = n_boundary();
+  for(int32_t v : tet)
+    if(v < 0 || v >= nv) { set_error("tetrahedron vertex out of range"); return FE_INVALID_ARG; }
+  for(int32_t v : bnd)
+    if(v < 0 || v >= nv) { set_error("boundary triangle vertex out of range"); return FE_INVALID_ARG; }
+  std::unordered_map<uint64_t, int32_t> id;
+  id.reserve((size_t)(nv * 8 + 16));
+  edge_v.clear();
+  auto key = [](int32_t a, int32_t b) {
+    return ((uint64_t)(uint32_t)std::min(a, b) << 32) | (uint32_t)std::max(a, b);
+  };
+  auto add = [&](int32_t a, int32_t b) {
+    auto r = id.emplace(key(a, b), (int32_t)(edge_v.size() / 2));
+    if(r.second) {
+      edge_v.push_back(a);
+      edge_v.push_back(b);
+    }
+    return r.first->second;
+  };
+  bnd_edges.assign(nb * 3, -1);
+  for(int64_t i = 0; i < nb; ++i)
+    for(int k = 0; k < 3; ++k) bnd_edges[3 * i + k] = add(bnd[3 * i + k], bnd[3 * i + (k + 1) % 3]);
+  const int64_t nBndEdges = (int64_t)edge_v.size() / 2;
+  for(int64_t t = 0; t < nt; ++t)
+    for(int f = 0; f < 4; ++f) {
+      const int32_t v[3] = {tet[4 * t + TET_FACES[f][0]], tet[4 * t + TET_FACES[f][1]], tet[4 * t + TET_FACES[f][2]]};
+      for(int k = 0; k < 3; ++k) add(v[k], v[(k + 1) % 3]);
+    }
+  n_edges = (int64_t)edge_v.size() / 2;
+  tet_edges.assign(nt * 6, -1);
+  for(int64_t t = 0; t < nt; ++t)
+    for(int k = 0; k < 6; ++k)
+      tet_edges[6 * t + k] = id.at(key(tet[4 * t + TET_EDGES[k][0]], tet[4 * t + TET_EDGES[k][1]]));
+  // Every boundary edge must belong to a tetrahedron: edges only the
+  // boundary created and no tetrahedron met mean a stray boundary triangle.
+  std::vector<uint8_t> used((size_t)n_edges, 0);
+  for(int32_t e : tet_edges) used[e] = 1;
+  for(int64_t e = 0; e < nBndEdges; ++e)
+    if(!used[e]) { set_error("boundary triangle edge %lld is not an edge of the tetrahedra", (long long)e); return FE_INVALID_ARG; }
+  return FE_OK;
+}
 
 namespace {
 
@@ -106,7 +154,7 @@ int mesh3d_generate_cube(Mesh3D &m, int n, const double box[6], double jitter, u
           m.bnd.insert(m.bnd.end(), t2, t2 + 3);
         }
     }
-  return FE_OK;
+  return m.build_topology();
 }
 
 int mesh3d_write_msh41(const Mesh3D &m, const std::string &path)

@@ -18,7 +18,28 @@ struct Mesh3D {
   int64_t n_vertices() const { return (int64_t)x.size(); }
   int64_t n_tets() const { return (int64_t)tet.size() / 4; }
   int64_t n_boundary() const { return (int64_t)bnd.size() / 3; }
+
+  // Derived by build_topology():
+  int64_t n_edges = 0;
+  std::vector<int32_t> edge_v;     // [nEdges*2] vertices of each edge (first-seen orientation)
+  std::vector<int32_t> tet_edges;  // [nTet*6] edge of local edge k, in TET_EDGES order
+  std::vector<int32_t> bnd_edges;  // [nBnd*3] edge joining local vertices k and (k+1)%3
+
+  // Numbers the edges in the order the reference's reader creates them for a
+  // file holding the "Bord" triangles before the tetrahedra
+  // (src/feMeshRead.cpp:1320-1345, 1481-1538): the edges (k, k+1) of each
+  // boundary triangle, then, for each tetrahedron, the edges (0,1), (1,2),
+  // (2,0) of its facets taken in TET_FACES order (Tetrahedron::createBoundary,
+  // src/feTetrahedron.cpp:6-32).  Checks that every edge of a boundary
+  // triangle is an edge of the tetrahedra.
+  int build_topology();
 };
+
+// Facets and edges of a tetrahedron in the reference's local order
+// (_facesOrder, _edgesOrder, src/feTetrahedron.h:30-31); edge k of a P2
+// tetrahedron carries its local DOF 4 + k.
+extern const int TET_FACES[4][3];
+extern const int TET_EDGES[6][2];
 
 // Structured n x n x n grid on the box, each cell split into the 6
 // tetrahedra of the Kuhn (Freudenthal) triangulation: for each ordering

@@ -188,35 +188,34 @@ int build_element_tables(const Mesh2D &m, const Numbering &num, int type, int fi
 // algorithm 1 (feCncGeo.cpp:752-790): each round walks the uncolored elements
 // in index order, takes an element whose uncolored vertex-neighbours were not
 // taken earlier in the round, and blocks those neighbours.
-int color_elements(const Mesh2D &m, Coloring &col)
+int color_by_vertices(const int32_t *ev, int nvpe, int64_t ne, int64_t nv, int maxColors, Coloring &col)
 {
-  const int64_t nt = m.n_triangles(), nv = m.n_vertices();
   std::vector<int64_t> vstart(nv + 1, 0);
-  for(int64_t i = 0; i < nt * 3; ++i) vstart[m.tri[i] + 1]++;
+  for(int64_t i = 0; i < ne * nvpe; ++i) vstart[ev[i] + 1]++;
   for(int64_t v = 0; v < nv; ++v) vstart[v + 1] += vstart[v];
-  std::vector<int32_t> velm(nt * 3);
+  std::vector<int32_t> velm(ne * nvpe);
   std::vector<int64_t> fill(vstart.begin(), vstart.end() - 1);
-  for(int64_t t = 0; t < nt; ++t)
-    for(int k = 0; k < 3; ++k) velm[fill[m.tri[3 * t + k]]++] = (int32_t)t;
+  for(int64_t t = 0; t < ne; ++t)
+    for(int k = 0; k < nvpe; ++k) velm[fill[ev[nvpe * t + k]]++] = (int32_t)t;
 
   col = Coloring();
-  col.elm_color.assign(nt, -1);
-  std::vector<int8_t> blocked(nt, 0);
+  col.elm_color.assign(ne, -1);
+  std::vector<int8_t> blocked(ne, 0);
   int64_t done = 0;
   col.offsets.push_back(0);
-  while(done < nt) {
+  while(done < ne) {
     const int c = col.nColors;
-    for(int64_t k = 0; k < nt; ++k) {
+    for(int64_t k = 0; k < ne; ++k) {
       if(col.elm_color[k] != -1 || blocked[k]) continue;
-      for(int j = 0; j < 3; ++j) {
-        int32_t v = m.tri[3 * k + j];
+      for(int j = 0; j < nvpe; ++j) {
+        int32_t v = ev[nvpe * k + j];
         for(int64_t p = vstart[v]; p < vstart[v + 1]; ++p) {
           int32_t o = velm[p];
           if(o != k && col.elm_color[o] == -1) blocked[o] = 1;
         }
       }
     }
-    for(int64_t k = 0; k < nt; ++k) {
+    for(int64_t k = 0; k < ne; ++k) {
       if(col.elm_color[k] != -1) continue;
       if(blocked[k]) { blocked[k] = 0; continue; }
       col.elm_color[k] = c;
@@ -225,12 +224,17 @@ int color_elements(const Mesh2D &m, Coloring &col)
     }
     col.nColors++;
     col.offsets.push_back((int64_t)col.elements.size());
-    if(col.nColors > 64) {
+    if(col.nColors > maxColors) {
       set_error("coloring did not terminate");
       return FE_ERROR;
     }
   }
   return FE_OK;
+}
+
+int color_elements(const Mesh2D &m, Coloring &col)
+{
+  return color_by_vertices(m.tri.data(), 3, m.n_triangles(), m.n_vertices(), 64, col);
 }
 
 int validate_coloring(const Mesh2D &m, const Coloring &col)
@@ -289,40 +293,55 @@ int build_csr_pattern(const ElementTables &et, int64_t nInc, CSRPattern &pat)
       }
   }
   // Row r: its diagonal and the coupled unknown DOFs of the elements that
-  // hold it, sorted and unique, written once into a slot of 1 + nl deg(r)
-  // entries (slot r starts at r + nl dptr[r]), then compacted.
-  std::vector<int32_t> buf((size_t)(nInc + (int64_t)nl * dptr[nInc]));
+  // hold it, sorted and unique.  Consecutive rows are built in chunks on the
+  // host threads, each chunk into its own array, then copied into place, so
+  // the scratch memory is the size of the pattern.
+  constexpr int64_t kRows = 1 << 12;
+  const int64_t nChunks = (nInc + kRows - 1) / kRows;
+  std::vector<std::vector<int32_t>> part((size_t)nChunks);
   pat = CSRPattern();
   pat.n = nInc;
   pat.ia.assign(nInc + 1, 0);
-  parallel_for(nInc, [&](int64_t r0, int64_t r1) {
-    for(int64_t r = r0; r < r1; ++r) {
-      int32_t *v = buf.data() + r + (int64_t)nl * dptr[r];
-      int32_t *e = v;
-      *e++ = (int32_t)r;
-      for(int64_t k = dptr[r]; k < dptr[r + 1]; ++k) {
-        const int64_t t = adj[k] / nl;
-        const int i = (int)(adj[k] - t * nl);
-        const int64_t *a = &et.adr[t * nl];
-        for(int j = 0; j < nl; ++j)
-          if(et.mask[i * nl + j] && a[j] < nInc) *e++ = (int32_t)a[j];
-      }
-      std::sort(v, e);
-      pat.ia[r + 1] = std::unique(v, e) - v;
-    }
-  });
+  parallel_for(
+      nChunks,
+      [&](int64_t c0, int64_t c1) {
+        std::vector<int32_t> row;
+        for(int64_t c = c0; c < c1; ++c) {
+          std::vector<int32_t> &out = part[(size_t)c];
+          const int64_t rEnd = std::min(nInc, (c + 1) * kRows);
+          for(int64_t r = c * kRows; r < rEnd; ++r) {
+            row.clear();
+            row.push_back((int32_t)r);
+            for(int64_t k = dptr[r]; k < dptr[r + 1]; ++k) {
+              const int64_t t = adj[k] / nl;
+              const int i = (int)(adj[k] - t * nl);
+              const int64_t *a = &et.adr[t * nl];
+              for(int j = 0; j < nl; ++j)
+                if(et.mask[i * nl + j] && a[j] < nInc) row.push_back((int32_t)a[j]);
+            }
+            std::sort(row.begin(), row.end());
+            const auto e = std::unique(row.begin(), row.end());
+            pat.ia[r + 1] = e - row.begin();
+            out.insert(out.end(), row.begin(), e);
+          }
+        }
+      },
+      1);
   for(int64_t r = 0; r < nInc; ++r) pat.ia[r + 1] += pat.ia[r];
   if(pat.ia[nInc] >= (int64_t)INT32_MAX) {
     set_error("more than 2^31 nonzeros: 32-bit scatter map does not fit");
     return FE_INVALID_ARG;
   }
   pat.ja.resize(pat.ia[nInc]);
-  parallel_for(nInc, [&](int64_t r0, int64_t r1) {
-    for(int64_t r = r0; r < r1; ++r) {
-      const int32_t *v = buf.data() + r + (int64_t)nl * dptr[r];
-      std::copy(v, v + (pat.ia[r + 1] - pat.ia[r]), pat.ja.begin() + pat.ia[r]);
-    }
-  });
+  parallel_for(
+      nChunks,
+      [&](int64_t c0, int64_t c1) {
+        for(int64_t c = c0; c < c1; ++c) {
+          std::copy(part[(size_t)c].begin(), part[(size_t)c].end(), pat.ja.begin() + pat.ia[c * kRows]);
+          std::vector<int32_t>().swap(part[(size_t)c]);
+        }
+      },
+      1);
   return FE_OK;
 }
 

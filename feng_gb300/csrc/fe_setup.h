@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "fe_mesh.h"
+#include "fe_mesh3d.h"
 
 namespace feng {
 
@@ -43,6 +44,8 @@ struct SpaceDesc {
 enum ElemType : int {
   ELEM_P2 = 1,            // scalar P2 triangle, 6 local DOFs
   ELEM_TAYLOR_HOOD = 2,   // vector P2 (interleaved) + scalar P1, 12 + 3 local DOFs
+  ELEM_TET_P2 = 3,        // scalar P2 tetrahedron, 4 vertex + 6 edge DOFs
+  ELEM_TET_TAYLOR_HOOD = 4,  // 3-vector P2 (interleaved) + scalar P1, 30 + 4 local DOFs
 };
 
 struct Numbering {
@@ -52,7 +55,7 @@ struct Numbering {
   std::vector<std::vector<int64_t>> vdof;      // [field][vertex*comp + c]  (-1: none)
   std::vector<std::vector<int64_t>> edof;      // [field][edge*comp + c]
   // Physical location and field/component of every DOF.
-  std::vector<double> dof_x, dof_y;
+  std::vector<double> dof_x, dof_y, dof_z;  // dof_z: tetrahedral meshes only
   std::vector<int32_t> dof_field, dof_comp;
   std::vector<uint8_t> dof_is_vertex;
 };
@@ -79,9 +82,26 @@ struct Coloring {
   std::vector<int32_t> elements;     // elements listed color by color, ascending within a color
 };
 
+// feCncGeo::colorElements(1) (src/feCncGeo.cpp:735) on elements given by
+// nvpe vertices each (ev [ne*nvpe]): triangles or tetrahedra.
+int color_by_vertices(const int32_t *ev, int nvpe, int64_t ne, int64_t nv, int maxColors, Coloring &col);
 int color_elements(const Mesh2D &m, Coloring &col);
 // Checks that no two elements of one color share a vertex.
 int validate_coloring(const Mesh2D &m, const Coloring &col);
+
+// Tetrahedral meshes.  The numbering restates feMetaNumber for spaces on
+// "Domaine" (tetrahedra, feSpaceTetPn) and "Bord" (triangles): per pass
+// (unknown DOFs, then essential DOFs) and per field, the vertices in index
+// order, then the edges in Mesh3D::build_topology order, components
+// interleaved (src/feNumber.cpp:677-835, the same rule as on triangles).
+int build_numbering3d(const Mesh3D &m, const std::vector<SpaceDesc> &spaces, Numbering &num);
+// ELEM_TET_P2: 4 vertex DOFs then the 6 edge DOFs in TET_EDGES order
+// (feSpaceTetPn::initializeAddressingVector, src/feSpace_3D.cpp:293-320).
+// ELEM_TET_TAYLOR_HOOD: velocity node k (vertices, then edges) component c at
+// 3k + c, pressure vertex j at 30 + j.
+int build_element_tables3d(const Mesh3D &m, const Numbering &num, int type, int fieldU, int fieldP,
+                           ElementTables &et);
+int color_elements3d(const Mesh3D &m, Coloring &col);
 
 struct CSRPattern {
   int64_t n = 0;

@@ -58,6 +58,8 @@ extern "C" {
 /* ---- element types of the fused kernels */
 #define FE_ELEM_P2 1            /* scalar Lagrange P2 triangle, 6 local DOFs          */
 #define FE_ELEM_TAYLOR_HOOD 2   /* vector P2 (interleaved x,y) + P1, 12 + 3 local DOFs */
+#define FE_ELEM_TET_P2 3        /* scalar P2 tetrahedron, 10 local DOFs */
+#define FE_ELEM_TET_TAYLOR_HOOD 4  /* vector P2 (interleaved x,y,z) + P1 on tetrahedra, 30 + 4 */
 
 /* ---- connectivities a space lives on (feMesh physical names) */
 #define FE_CNC_DOMAIN 0    /* "Domaine"       */
@@ -203,6 +205,18 @@ typedef struct fe_setup fe_setup;
 int fe_setup_create(const fe_mesh *m, const fe_space_desc *spaces, int nspaces, int elem_type,
                     int quad_degree, int pc_block_rows, fe_setup **out);
 void fe_setup_destroy(fe_setup *s);
+/* The same host set-up on a tetrahedral mesh, elem_type FE_ELEM_TET_P2 (scalar
+ * P2, 10 local DOFs: 4 vertices, then the edges (0,2) (2,1) (1,0) (1,3) (3,0)
+ * (3,2), feSpaceTetPn(2)) or FE_ELEM_TET_TAYLOR_HOOD (3-vector P2
+ * interleaved + P1, 34 local DOFs; no reference counterpart).  Spaces on
+ * FE_CNC_DOMAIN (tetrahedra) and FE_CNC_BOUNDARY (triangles).  Numbering,
+ * element tables, coloring and CSR pattern as the reference builds them on
+ * the same msh file; no quadrature rule (get_* of the triangle set-up work,
+ * fe_cuda_system_create refuses it). */
+int fe_setup3d_create(const fe_mesh3d *m, const fe_space_desc *spaces, int nspaces, int elem_type,
+                      int pc_block_rows, fe_setup **out);
+/* z coordinate of every DOF (tetrahedral set-ups only). */
+int fe_setup_get_dof_z(const fe_setup *s, double *z);
 int fe_setup_sizes(const fe_setup *s, int64_t *n_inc, int64_t *n_dofs, int64_t *nnz,
                    int64_t *n_elm, int *n_colors, int *nloc);
 /* Outputs may be NULL.  ia [n_inc+1], ja [nnz]. */

@@ -95,3 +95,43 @@ def test_oracle_tet_diffusion_solution_matches_reference():
     v, d = g["tet"].reshape(-1), adr[:, :4].reshape(-1)
     exact = np.sin(np.pi * g["x"][v]) * np.sin(np.pi * g["y"][v]) * np.sin(np.pi * g["z"][v])
     assert np.max(np.abs(u[d] - exact)) < 0.02
+
+
+def _tet_numbering(mesh):
+    uB = fe.createFiniteElementSpace(mesh, fe.LAGRANGE, 2, "U", "Bord", 4)
+    u = fe.createFiniteElementSpace(mesh, fe.LAGRANGE, 2, "U", "Domaine", 4)
+    return fe.feMetaNumber(mesh, [uB, u], [uB])
+
+
+def test_tet_setup_bit_exact():
+    """Numbering, element DOF tables, coloring and CSR pattern built here on
+    the generated mesh equal the reference's on the same msh file."""
+    g = _golden()
+    mesh = fe.Mesh3DP1.generate_cube(int(g["n"]), jitter=float(g["jitter"]), seed=int(g["seed"]))
+    num = _tet_numbering(mesh)
+    assert num.elem_type == fe.api.ELEM_TET_P2
+    st = num.setup()
+    assert (st.nInc, st.nDofs, st.nloc) == (int(g["nInc"]), int(g["nDofs"]), 10)
+    np.testing.assert_array_equal(st.elementDofs().reshape(-1), g["adr"])
+    ia, ja = st.pattern()
+    np.testing.assert_array_equal(ia, g["ia"])
+    np.testing.assert_array_equal(ja, g["ja"])
+    off, el = st.coloring()
+    np.testing.assert_array_equal(off, g["color_offsets"])
+    np.testing.assert_array_equal(el, g["color_elements"])
+    # DOF locations: vertices and edge midpoints
+    x, y, f, c, isv = st.dofInfo()
+    z = st.dofZ()
+    adr = g["adr"].reshape(-1, 10)
+    xyz = np.stack([g["x"], g["y"], g["z"]], 1)
+    np.testing.assert_array_equal(np.stack([x, y, z], 1)[adr[:, :4]], xyz[g["tet"]])
+    assert np.all(isv[adr[:, :4]] == 1) and np.all(isv[adr[:, 4:]] == 0)
+
+
+def test_tet_setup_is_deterministic():
+    """The set-up of a larger mesh (threaded pattern build) is the same twice."""
+    m = fe.Mesh3DP1.generate_cube(10, jitter=0.05, seed=3)
+    a = _tet_numbering(m).setup()
+    b = _tet_numbering(m).setup()
+    np.testing.assert_array_equal(a.pattern()[1], b.pattern()[1])
+    np.testing.assert_array_equal(a.elementDofs(), b.elementDofs())
