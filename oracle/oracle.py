@@ -324,7 +324,6 @@ def tet_p2_diffusion(adr, tet_xyz, quad, u, n_inc, ia, ja, coeff=1.0, source=Non
     adr = np.asarray(adr, np.int64).reshape(-1, 10)
     X = np.asarray(tet_xyz, np.float64).reshape(-1, 4, 3)
     q = np.asarray(quad, np.float64).reshape(-1, 4)
-    ia, ja = np.asarray(ia, np.int64), np.asarray(ja, np.int64)
     jm = np.stack([X[:, 1] - X[:, 0], X[:, 2] - X[:, 0], X[:, 3] - X[:, 0]], -1)
     det, inv = np.linalg.det(jm), np.linalg.inv(jm)
     phi, dphi = tet_p2_basis(q[:, 0], q[:, 1], q[:, 2])
@@ -338,12 +337,22 @@ def tet_p2_diffusion(adr, tet_xyz, quad, u, n_inc, ia, ja, coeff=1.0, source=Non
         xq = np.einsum("qv,evx->eqx", psi, X)
         f = source(xq[..., 0], xq[..., 1], xq[..., 2])
         be -= np.einsum("qi,eq,q,e->ei", phi, f, w, det)
+    return _scatter(adr, ae, be, n_inc, ia, ja)
+
+
+def _scatter(adr, ae, be, n_inc, ia, ja, mask=None):
+    """MKL-style scatter of element matrices ae (nElm, nloc, nloc) and
+    vectors be (nElm, nloc): entries with an essential row or column are
+    dropped; mask (nloc, nloc) selects the coupled local pairs."""
+    ia, ja = np.asarray(ia, np.int64), np.asarray(ja, np.int64)
     rhs = np.zeros(n_inc)
     keep = adr < n_inc
     np.add.at(rhs, adr[keep], be[keep])
     rows = np.broadcast_to(adr[:, :, None], ae.shape)
     cols = np.broadcast_to(adr[:, None, :], ae.shape)
     m = (rows < n_inc) & (cols < n_inc)
+    if mask is not None:
+        m &= np.asarray(mask, bool)[None]
     # Position of (r, c) in the pattern: rows in order, columns ascending
     # within a row, so row * (n + 1) + column ascends over the whole array.
     lin = np.repeat(np.arange(n_inc), np.diff(ia)) * (n_inc + 1) + ja
@@ -354,3 +363,123 @@ def tet_p2_diffusion(adr, tet_xyz, quad, u, n_inc, ia, ja, coeff=1.0, source=Non
     values = np.zeros(len(ja))
     np.add.at(values, pos, ae[m])
     return values, rhs
+
+
+# ---- Taylor-Hood forms on triangles and tetrahedra (numpy restatement) ---------
+
+TRI_EDGES = ((0, 1), (1, 2), (2, 0))
+
+
+def p2_basis(ref, edges):
+    """P2 Lagrange basis on a simplex of dimension d = ref.shape[-1] at the
+    reference points ref (nq, d): barycentric l = (1 - sum, ref...), vertex
+    functions l_i (2 l_i - 1), then 4 l_a l_b over `edges`.  Returns phi
+    (nq, n) and d phi / d ref (nq, n, d)."""
+    ref = np.asarray(ref, np.float64)
+    d = ref.shape[-1]
+    lam = np.concatenate([1 - ref.sum(-1, keepdims=True), ref], -1)
+    dlam = np.vstack([-np.ones(d), np.eye(d)])
+    phi = [lam[:, i] * (2 * lam[:, i] - 1) for i in range(d + 1)]
+    phi += [4 * lam[:, a] * lam[:, b] for a, b in edges]
+    dphi = [np.multiply.outer(4 * lam[:, i] - 1, dlam[i]) for i in range(d + 1)]
+    dphi += [4 * (np.multiply.outer(lam[:, b], dlam[a]) + np.multiply.outer(lam[:, a], dlam[b])) for a, b in edges]
+    return np.stack(phi, -1), np.stack(dphi, -2)
+
+
+def taylor_hood(adr, vert_xyz, quad, u, n_inc, ia, ja, conv=0.0, sigma=0.0, mu=1.0, divu=0.0, mass=0.0,
+                udot=None, c0=0.0, source=None):
+    """CSR values and residual of the Taylor-Hood forms on triangles (d = 2,
+    the reference's forms) or tetrahedra (d = 3, the same weak forms, which
+    the reference does not instantiate), scattered as the MKL backend does.
+    Local layout: velocity node k (vertices, then edges) component c at
+    d k + c, pressure vertex j after the velocity.  Gradient convention
+    (grad u)_mn = d_m u_n.  With W = J w at each quadrature node:
+
+    VectorConvectiveAcceleration (src/feVectorSysElm.cpp:1171-1240)
+      Be_kc -= conv W phi_k (u . grad u)_c
+      A_kc,la += conv W phi_k (phi_l d_a u_c + delta_ca u . grad phi_l)
+    DivergenceNewtonianStress (src/feVectorSysElm.cpp:1454-1530)
+      Be_kc -= sigma W (p d_c phi_k - mu sum_m (d_m u_c + d_c u_m) d_m phi_k)
+      A_kc,la += -sigma mu W (delta_ca grad phi_k . grad phi_l + d_a phi_k d_c phi_l)
+      A_kc,pj += sigma W psi_j d_c phi_k
+    MixedDivergence (src/feVectorSysElm.cpp:685-747)
+      Be_pj -= divu W (div u) psi_j;  A_pj,la += divu W psi_j d_a phi_l
+    TransientVectorMass (src/feVectorSysElm.cpp:390-427)
+      Be_kc -= mass W udot_c phi_k;  A_kc,lc += mass c0 W phi_k phi_l
+    VectorSource (src/feVectorSysElm.cpp:112-130)
+      Be_kc -= W f_c(x_q) phi_k, source(*coords) -> tuple of d arrays.
+
+    vert_xyz (nElm, d+1, d); quad (nq, d+1) rows (reference point, w)."""
+    q = np.asarray(quad, np.float64)
+    d = q.shape[1] - 1
+    nv, edges = d + 1, (TRI_EDGES if d == 2 else TET_EDGES)
+    n2 = nv + len(edges)
+    nloc = d * n2 + nv
+    adr = np.asarray(adr, np.int64).reshape(-1, nloc)
+    X = np.asarray(vert_xyz, np.float64).reshape(-1, nv, d)
+    ref, w = q[:, :d], q[:, d]
+    jm = np.stack([X[:, i + 1] - X[:, 0] for i in range(d)], -1)
+    det, inv = np.linalg.det(jm), np.linalg.inv(jm)
+    phi, dphi = p2_basis(ref, edges)
+    psi = np.concatenate([1 - ref.sum(-1, keepdims=True), ref], -1)
+    G = np.einsum("qkr,erx->eqkx", dphi, inv)                 # grad phi_k
+    W = det[:, None] * w[None, :]                             # (ne, nq)
+    ue = np.asarray(u, np.float64)[adr]
+    U, P = ue[:, :d * n2].reshape(-1, n2, d), ue[:, d * n2:]
+    uq = np.einsum("qk,ekn->eqn", phi, U)
+    gu = np.einsum("eqkm,ekn->eqmn", G, U)
+    pq = np.einsum("qj,ej->eq", psi, P)
+    ne_ = len(adr)
+    bu = np.zeros((ne_, n2, d))
+    bp = np.zeros((ne_, nv))
+    A = np.zeros((ne_, n2, d, n2, d))
+    Aup = np.zeros((ne_, n2, d, nv))
+    Apu = np.zeros((ne_, nv, n2, d))
+    eye = np.eye(d)
+    if conv:
+        ugu = np.einsum("eqm,eqmn->eqn", uq, gu)
+        bu -= conv * np.einsum("eq,qk,eqc->ekc", W, phi, ugu)
+        A += conv * np.einsum("zq,qk,ql,zqac->zkcla", W, phi, phi, gu)
+        A += conv * np.einsum("zq,qk,zqm,zqlm,ca->zkcla", W, phi, uq, G, eye)
+    if sigma:
+        sym = gu + np.swapaxes(gu, -1, -2)                    # d_m u_c + d_c u_m at [m, c]
+        bu -= sigma * (np.einsum("eq,eq,eqkc->ekc", W, pq, G) -
+                       mu * np.einsum("eq,eqmc,eqkm->ekc", W, sym, G))
+        A += -sigma * mu * (np.einsum("zq,zqkm,zqlm,ca->zkcla", W, G, G, eye) +
+                            np.einsum("zq,zqka,zqlc->zkcla", W, G, G))
+        Aup += sigma * np.einsum("eq,qj,eqkc->ekcj", W, psi, G)
+    if divu:
+        div = np.einsum("eqmm->eq", gu)
+        bp -= divu * np.einsum("eq,eq,qj->ej", W, div, psi)
+        Apu += divu * np.einsum("zq,qj,zqla->zjla", W, psi, G)
+    if mass:
+        ud = np.einsum("qk,ekn->eqn", phi, np.asarray(udot, np.float64)[adr][:, :d * n2].reshape(-1, n2, d))
+        bu -= mass * np.einsum("eq,eqc,qk->ekc", W, ud, phi)
+        A += mass * c0 * np.einsum("zq,qk,ql,ca->zkcla", W, phi, phi, eye)
+    if source is not None:
+        xq = np.einsum("qv,evx->eqx", psi, X)
+        f = np.stack(np.broadcast_arrays(*source(*(xq[..., i] for i in range(d)))), -1)
+        bu -= np.einsum("eq,eqc,qk->ekc", W, f, phi)
+    nu = d * n2
+    ae = np.zeros((ne_, nloc, nloc))
+    ae[:, :nu, :nu] = A.reshape(ne_, nu, nu)
+    ae[:, :nu, nu:] = Aup.reshape(ne_, nu, nv)
+    ae[:, nu:, :nu] = Apu.reshape(ne_, nv, nu)
+    be = np.concatenate([bu.reshape(ne_, nu), bp], 1)
+    mask = np.ones((nloc, nloc), bool)
+    mask[nu:, nu:] = False                                    # no pressure-pressure form
+    return _scatter(adr, ae, be, n_inc, ia, ja, mask)
+
+
+def ns_mms_source(x, y):
+    """Source of the reference's Navier-Stokes manufactured solution
+    u = (x^4 y^4, -4/5 x^3 y^5), p = x^2 y^2 with its sign convention
+    (tests/withLinearSolver/navier_stokes.cpp:33-51): f = (u.grad)u + grad p
+    - lap u, negated."""
+    x, y = np.asarray(x, np.float64), np.asarray(y, np.float64)
+    u0, u1 = x ** 4 * y ** 4, -0.8 * x ** 3 * y ** 5
+    conv0 = u0 * 4 * x ** 3 * y ** 4 + u1 * 4 * x ** 4 * y ** 3
+    conv1 = u0 * (-2.4) * x ** 2 * y ** 5 + u1 * (-4) * x ** 3 * y ** 4
+    lap0 = 12 * (x ** 2 * y ** 4 + x ** 4 * y ** 2)
+    lap1 = -0.8 * (6 * x * y ** 5 + 20 * x ** 3 * y ** 3)
+    return (-(-conv0 - 2 * x * y ** 2 + lap0), -(-conv1 - 2 * x ** 2 * y + lap1))
