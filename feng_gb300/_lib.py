@@ -93,6 +93,8 @@ SIGNATURES = {
     "fe_setup_get_dof_z": (C.c_int, [P, P]),
     "fe_mesh3d_generate_cube": (C.c_int, [C.c_int, P, C.c_double, C.c_uint64, C.POINTER(P)]),
     "fe_mesh3d_write_msh": (C.c_int, [P, C.c_char_p]),
+    "fe_mesh3d_read_msh": (C.c_int, [C.c_char_p, C.POINTER(P)]),
+    "fe_mesh3d_from_arrays": (C.c_int, [C.c_int64, P, P, P, C.c_int64, P, C.c_int64, P, C.POINTER(P)]),
     "fe_mesh3d_sizes": (C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "fe_mesh3d_arrays": (C.c_int, [P, P, P, P, P, P]),
     "fe_mesh3d_destroy": (None, [P]),

@@ -128,6 +128,25 @@ class Mesh3DP1:
         check(lib.fe_mesh3d_generate_cube(n, ptr(box), jitter, seed, C.byref(h)))
         return cls(h)
 
+    @classmethod
+    def from_msh(cls, path: str):
+        """Reads the "Domaine" tetrahedra and "Bord" triangles of a msh 4.1 file."""
+        lib = _lib.load()
+        h = C.c_void_p()
+        check(lib.fe_mesh3d_read_msh(str(path).encode(), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_arrays(cls, x, y, z, tet, bnd):
+        lib = _lib.load()
+        x, y, z = (np.ascontiguousarray(v, np.float64) for v in (x, y, z))
+        tet = np.ascontiguousarray(tet, np.int32).reshape(-1)
+        bnd = np.ascontiguousarray(bnd, np.int32).reshape(-1)
+        h = C.c_void_p()
+        check(lib.fe_mesh3d_from_arrays(len(x), ptr(x), ptr(y), ptr(z), len(tet) // 4, ptr(tet), len(bnd) // 3,
+                                        ptr(bnd), C.byref(h)))
+        return cls(h)
+
     def write_msh(self, path: str):
         check(self._lib.fe_mesh3d_write_msh(self._h, str(path).encode()))
 

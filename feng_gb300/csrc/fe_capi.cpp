@@ -265,6 +265,37 @@ int fe_mesh3d_generate_cube(int n, const double *box, double jitter, uint64_t se
   GUARD_END
 }
 
+int fe_mesh3d_read_msh(const char *path, fe_mesh3d **out)
+{
+  GUARD_BEGIN
+  if(!out || !path) { set_error("null argument"); return FE_INVALID_ARG; }
+  std::unique_ptr<fe_mesh3d> m(new fe_mesh3d());
+  FE_TRY(mesh3d_read_msh41(m->m, path));
+  *out = m.release();
+  return FE_OK;
+  GUARD_END
+}
+
+int fe_mesh3d_from_arrays(int64_t nv, const double *x, const double *y, const double *z, int64_t nt,
+                          const int32_t *tet, int64_t nb, const int32_t *bnd, fe_mesh3d **out)
+{
+  GUARD_BEGIN
+  if(!out || nv <= 0 || nt <= 0 || nb < 0 || !x || !y || !z || !tet || (nb > 0 && !bnd)) {
+    set_error("invalid arguments");
+    return FE_INVALID_ARG;
+  }
+  std::unique_ptr<fe_mesh3d> m(new fe_mesh3d());
+  m->m.x.assign(x, x + nv);
+  m->m.y.assign(y, y + nv);
+  m->m.z.assign(z, z + nv);
+  m->m.tet.assign(tet, tet + 4 * nt);
+  if(nb > 0) m->m.bnd.assign(bnd, bnd + 3 * nb);
+  FE_TRY(m->m.build_topology());
+  *out = m.release();
+  return FE_OK;
+  GUARD_END
+}
+
 int fe_mesh3d_write_msh(const fe_mesh3d *m, const char *path)
 {
   GUARD_BEGIN

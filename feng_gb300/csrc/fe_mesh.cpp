@@ -9,6 +9,7 @@
 #include <unordered_map>
 
 #include "fe_common.h"
+#include "fe_msh.h"
 
 namespace feng {
 
@@ -154,104 +155,28 @@ int mesh_write_msh41(const Mesh2D &m, const std::string &path)
 
 int mesh_read_msh41(Mesh2D &m, const std::string &path, const MeshGroups &groups)
 {
-  std::ifstream in(path);
-  if(!in.good()) {
-    set_error("mesh file \"%s\" does not exist", path.c_str());
-    return FE_READ_ERROR;
-  }
+  MshData d;
+  FE_TRY(read_msh41(path, d));
   m = Mesh2D();
-  std::string tok;
-  std::map<std::pair<int, int>, std::string> physNames;           // (dim, physTag) -> name
-  std::map<std::pair<int, int>, int> entityPhys;                  // (dim, entityTag) -> physTag
-  std::unordered_map<long long, int32_t> nodeIndex;               // gmsh node tag -> index
-  // Element blocks keyed like the reference's entity map (dim, entity tag).
+  m.x = std::move(d.x);
+  m.y = std::move(d.y);
+  // Element blocks keyed like the reference's entity map (dim, entity tag);
+  // blocks of one entity appended in file order.
   std::map<std::pair<int, int>, std::vector<int32_t>> blocks;
-  std::map<std::pair<int, int>, int> blockType;
-  // Triangles in file order (for edge tags) and their key order.
-  while(in >> tok) {
-    if(tok == "$MeshFormat") {
-      double ver; int ftype, dsize;
-      in >> ver >> ftype >> dsize;
-      if(ver < 4.0 || ftype != 0) {
-        set_error("only ASCII msh 4.1 is supported (got %g, type %d)", ver, ftype);
-        return FE_READ_ERROR;
-      }
-    } else if(tok == "$PhysicalNames") {
-      int np; in >> np;
-      for(int i = 0; i < np; ++i) {
-        int d, t; std::string name;
-        in >> d >> t;
-        std::getline(in, name);
-        size_t a = name.find('"'), b = name.rfind('"');
-        if(a == std::string::npos || b <= a) { set_error("bad physical name"); return FE_READ_ERROR; }
-        physNames[{d, t}] = name.substr(a + 1, b - a - 1);
-      }
-    } else if(tok == "$Entities") {
-      int np, nc, ns, nvol; in >> np >> nc >> ns >> nvol;
-      for(int i = 0; i < np; ++i) {
-        int tag, nphys; double a, b, c; in >> tag >> a >> b >> c >> nphys;
-        for(int j = 0; j < nphys; ++j) { int p; in >> p; if(j == 0) entityPhys[{0, tag}] = p; }
-      }
-      for(int d = 1; d <= 3; ++d) {
-        int cnt = d == 1 ? nc : d == 2 ? ns : nvol;
-        for(int i = 0; i < cnt; ++i) {
-          int tag, nphys, nbnd; double bb[6];
-          in >> tag;
-          for(double &v : bb) in >> v;
-          in >> nphys;
-          for(int j = 0; j < nphys; ++j) { int p; in >> p; if(j == 0) entityPhys[{d, tag}] = p; }
-          in >> nbnd;
-          for(int j = 0; j < nbnd; ++j) { int q; in >> q; }
-        }
-      }
-    } else if(tok == "$Nodes") {
-      long long nblocks, nnodes, mn, mx; in >> nblocks >> nnodes >> mn >> mx;
-      m.x.resize(nnodes); m.y.resize(nnodes);
-      int32_t cnt = 0;
-      for(long long b = 0; b < nblocks; ++b) {
-        int d, t, par; long long nn; in >> d >> t >> par >> nn;
-        std::vector<long long> tags(nn);
-        for(auto &tg : tags) in >> tg;
-        for(long long i = 0; i < nn; ++i) {
-          double x, y, z; in >> x >> y >> z;
-          nodeIndex[tags[i]] = cnt;
-          m.x[cnt] = x; m.y[cnt] = y; ++cnt;
-        }
-      }
-      if(cnt != nnodes || (long long)nodeIndex.size() != nnodes) {
-        set_error("vertex indices are not unique"); return FE_READ_ERROR;
-      }
-    } else if(tok == "$Elements") {
-      long long nblocks, nel, mn, mx; in >> nblocks >> nel >> mn >> mx;
-      for(long long b = 0; b < nblocks; ++b) {
-        int d, t, type; long long ne; in >> d >> t >> type >> ne;
-        int npe = type == 15 ? 1 : type == 1 ? 2 : type == 2 ? 3 : -1;
-        if(npe < 0) { set_error("unsupported gmsh element type %d", type); return FE_READ_ERROR; }
-        auto &blk = blocks[{d, t}];
-        blockType[{d, t}] = type;
-        for(long long e = 0; e < ne; ++e) {
-          long long etag; in >> etag;
-          for(int k = 0; k < npe; ++k) {
-            long long nt; in >> nt;
-            auto it = nodeIndex.find(nt);
-            if(it == nodeIndex.end()) { set_error("element node %lld does not exist", nt); return FE_READ_ERROR; }
-            blk.push_back(it->second);
-          }
-        }
-      }
-    }
+  for(const MshBlock &b : d.blocks) {
+    auto &blk = blocks[{b.dim, b.tag}];
+    blk.insert(blk.end(), b.nodes.begin(), b.nodes.end());
   }
   // Edge tags follow triangle file order; connectivity follows entity-key
   // order.  For files with a single surface entity both coincide.
   for(auto &kv : blocks) {
-    int d = kv.first.first;
-    auto ph = entityPhys.find(kv.first);
-    std::string name = ph == entityPhys.end() ? "" : physNames[{d, ph->second}];
+    const int dim = kv.first.first;
+    const std::string name = d.name_of(dim, kv.first.second);
     const bool isBoundary =
         std::find(groups.boundary.begin(), groups.boundary.end(), name) != groups.boundary.end();
-    if(d == 2 && name == groups.domain) m.tri.insert(m.tri.end(), kv.second.begin(), kv.second.end());
-    else if(d == 1 && isBoundary) m.bnd.insert(m.bnd.end(), kv.second.begin(), kv.second.end());
-    else if(d == 0 && !groups.point.empty() && name == groups.point && !kv.second.empty())
+    if(dim == 2 && name == groups.domain) m.tri.insert(m.tri.end(), kv.second.begin(), kv.second.end());
+    else if(dim == 1 && isBoundary) m.bnd.insert(m.bnd.end(), kv.second.begin(), kv.second.end());
+    else if(dim == 0 && !groups.point.empty() && name == groups.point && !kv.second.empty())
       m.point = kv.second[0];
   }
   if(m.tri.empty()) {

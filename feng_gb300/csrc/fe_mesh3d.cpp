@@ -6,6 +6,7 @@
 #include <unordered_map>
 
 #include "fe_common.h"
+#include "fe_msh.h"
 
 namespace feng {
 
@@ -194,6 +195,37 @@ int mesh3d_write_msh41(const Mesh3D &m, const std::string &path)
   fclose(f);
   if(rc) set_error("write error on %s", path.c_str());
   return rc;
+}
+
+int mesh3d_read_msh41(Mesh3D &m, const std::string &path, const std::string &domain,
+                      const std::vector<std::string> &boundary)
+{
+  MshData d;
+  FE_TRY(read_msh41(path, d));
+  m = Mesh3D();
+  m.x = std::move(d.x);
+  m.y = std::move(d.y);
+  m.z = std::move(d.z);
+  bool seenTets = false;
+  for(const MshBlock &b : d.blocks) {
+    const std::string name = d.name_of(b.dim, b.tag);
+    if(b.dim == 3 && b.type == 4 && name == domain) {
+      m.tet.insert(m.tet.end(), b.nodes.begin(), b.nodes.end());
+      seenTets = true;
+    } else if(b.dim == 2 && b.type == 2 &&
+              std::find(boundary.begin(), boundary.end(), name) != boundary.end()) {
+      if(seenTets) {
+        set_error("boundary triangles follow tetrahedra in %s; they must precede them", path.c_str());
+        return FE_READ_ERROR;
+      }
+      m.bnd.insert(m.bnd.end(), b.nodes.begin(), b.nodes.end());
+    }
+  }
+  if(m.tet.empty()) {
+    set_error("no \"%s\" tetrahedra in %s", domain.c_str(), path.c_str());
+    return FE_READ_ERROR;
+  }
+  return m.build_topology();
 }
 
 }  // namespace feng

@@ -60,4 +60,11 @@ int mesh3d_generate_cube(Mesh3D &m, int n, const double box[6], double jitter, u
 // tetrahedra), all nodes in the volume's block.
 int mesh3d_write_msh41(const Mesh3D &m, const std::string &path);
 
+// Reads an ASCII Gmsh 4.1 file: the tetrahedra of the `domain` volumes and
+// the triangles of the `boundary` surfaces, each in file order; nodes in
+// file order.  Boundary triangles must precede the tetrahedra in the file
+// (as Gmsh writes them), the order in which the edges are numbered.
+int mesh3d_read_msh41(Mesh3D &m, const std::string &path, const std::string &domain = "Domaine",
+                      const std::vector<std::string> &boundary = {"Bord"});
+
 }  // namespace feng

@@ -1,0 +1,110 @@
+#include "fe_msh.h"
+
+#include <fstream>
+#include <unordered_map>
+
+#include "fe_common.h"
+
+namespace feng {
+
+std::string MshData::name_of(int dim, int tag) const
+{
+  auto ph = entityPhys.find({dim, tag});
+  if(ph == entityPhys.end()) return "";
+  auto nm = physNames.find({dim, ph->second});
+  return nm == physNames.end() ? "" : nm->second;
+}
+
+int read_msh41(const std::string &path, MshData &out)
+{
+  std::ifstream in(path);
+  if(!in.good()) {
+    set_error("mesh file \"%s\" does not exist", path.c_str());
+    return FE_READ_ERROR;
+  }
+  out = MshData();
+  std::unordered_map<long long, int32_t> nodeIndex;  // gmsh node tag -> index
+  std::string tok;
+  while(in >> tok) {
+    if(tok == "$MeshFormat") {
+      double ver; int ftype, dsize;
+      in >> ver >> ftype >> dsize;
+      if(ver < 4.0 || ftype != 0) {
+        set_error("only ASCII msh 4.1 is supported (got %g, type %d)", ver, ftype);
+        return FE_READ_ERROR;
+      }
+    } else if(tok == "$PhysicalNames") {
+      int np; in >> np;
+      for(int i = 0; i < np; ++i) {
+        int d, t; std::string name;
+        in >> d >> t;
+        std::getline(in, name);
+        size_t a = name.find('"'), b = name.rfind('"');
+        if(a == std::string::npos || b <= a) { set_error("bad physical name"); return FE_READ_ERROR; }
+        out.physNames[{d, t}] = name.substr(a + 1, b - a - 1);
+      }
+    } else if(tok == "$Entities") {
+      int np, nc, ns, nvol; in >> np >> nc >> ns >> nvol;
+      for(int i = 0; i < np; ++i) {
+        int tag, nphys; double a, b, c; in >> tag >> a >> b >> c >> nphys;
+        for(int j = 0; j < nphys; ++j) { int p; in >> p; if(j == 0) out.entityPhys[{0, tag}] = p; }
+      }
+      for(int d = 1; d <= 3; ++d) {
+        int cnt = d == 1 ? nc : d == 2 ? ns : nvol;
+        for(int i = 0; i < cnt; ++i) {
+          int tag, nphys, nbnd; double bb[6];
+          in >> tag;
+          for(double &v : bb) in >> v;
+          in >> nphys;
+          for(int j = 0; j < nphys; ++j) { int p; in >> p; if(j == 0) out.entityPhys[{d, tag}] = p; }
+          in >> nbnd;
+          for(int j = 0; j < nbnd; ++j) { int q; in >> q; }
+        }
+      }
+    } else if(tok == "$Nodes") {
+      long long nblocks, nnodes, mn, mx; in >> nblocks >> nnodes >> mn >> mx;
+      if(nnodes < 0 || nnodes > (1ll << 31) - 1) { set_error("bad node count"); return FE_READ_ERROR; }
+      out.x.resize(nnodes); out.y.resize(nnodes); out.z.resize(nnodes);
+      int32_t cnt = 0;
+      for(long long b = 0; b < nblocks; ++b) {
+        int d, t, par; long long nn; in >> d >> t >> par >> nn;
+        if(nn < 0 || cnt + nn > nnodes) { set_error("bad node block"); return FE_READ_ERROR; }
+        std::vector<long long> tags(nn);
+        for(auto &tg : tags) in >> tg;
+        for(long long i = 0; i < nn; ++i) {
+          double x, y, z; in >> x >> y >> z;
+          nodeIndex[tags[i]] = cnt;
+          out.x[cnt] = x; out.y[cnt] = y; out.z[cnt] = z; ++cnt;
+        }
+      }
+      if(cnt != nnodes || (long long)nodeIndex.size() != nnodes) {
+        set_error("vertex indices are not unique"); return FE_READ_ERROR;
+      }
+    } else if(tok == "$Elements") {
+      long long nblocks, nel, mn, mx; in >> nblocks >> nel >> mn >> mx;
+      for(long long b = 0; b < nblocks; ++b) {
+        MshBlock blk;
+        long long ne;
+        in >> blk.dim >> blk.tag >> blk.type >> ne;
+        const int npe = blk.type == 15 ? 1 : blk.type == 1 ? 2 : blk.type == 2 ? 3 : blk.type == 4 ? 4 : -1;
+        if(npe < 0) { set_error("unsupported gmsh element type %d", blk.type); return FE_READ_ERROR; }
+        if(ne < 0) { set_error("bad element block"); return FE_READ_ERROR; }
+        blk.nodes.reserve((size_t)ne * npe);
+        for(long long e = 0; e < ne; ++e) {
+          long long etag; in >> etag;
+          for(int k = 0; k < npe; ++k) {
+            long long nt; in >> nt;
+            auto it = nodeIndex.find(nt);
+            if(it == nodeIndex.end()) { set_error("element node %lld does not exist", nt); return FE_READ_ERROR; }
+            blk.nodes.push_back(it->second);
+          }
+        }
+        out.blocks.push_back(std::move(blk));
+      }
+    }
+  }
+  if(in.bad()) { set_error("read error on %s", path.c_str()); return FE_READ_ERROR; }
+  return FE_OK;
+}
+
+}  // namespace feng

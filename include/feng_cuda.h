@@ -188,6 +188,15 @@ void fe_mesh_destroy(fe_mesh *m);
  * triangles oriented outwards. */
 int fe_mesh3d_generate_cube(int n, const double *box, double jitter, uint64_t seed, fe_mesh3d **out);
 int fe_mesh3d_write_msh(const fe_mesh3d *m, const char *path);
+/* Reads "Domaine" tetrahedra and "Bord" triangles (the triangles must precede
+ * the tetrahedra in the file, as Gmsh writes them). */
+int fe_mesh3d_read_msh(const char *path, fe_mesh3d **out);
+/* A mesh from caller arrays (0-based): vertices; tetrahedra of "Domaine";
+ * boundary triangles of "Bord".  Same result as reading a msh file holding
+ * these entities in this order. */
+int fe_mesh3d_from_arrays(int64_t n_vertices, const double *x, const double *y, const double *z,
+                          int64_t n_tets, const int32_t *tet, int64_t n_boundary, const int32_t *bnd,
+                          fe_mesh3d **out);
 int fe_mesh3d_sizes(const fe_mesh3d *m, int64_t *n_vertices, int64_t *n_tets, int64_t *n_boundary);
 /* Any output may be NULL.  x,y,z [nv]; tet [4 nt]; bnd [3 nb]. */
 int fe_mesh3d_arrays(const fe_mesh3d *m, double *x, double *y, double *z, int32_t *tet, int32_t *bnd);

@@ -483,3 +483,20 @@ def ns_mms_source(x, y):
     lap0 = 12 * (x ** 2 * y ** 4 + x ** 4 * y ** 2)
     lap1 = -0.8 * (6 * x * y ** 5 + 20 * x ** 3 * y ** 3)
     return (-(-conv0 - 2 * x * y ** 2 + lap0), -(-conv1 - 2 * x ** 2 * y + lap1))
+
+
+def l2_error_tet(adr, tet_xyz, u, quad, fct):
+    """feNorm L2_ERROR of a scalar P2 field on tetrahedra (src/feNorm.cpp:323-391):
+    over the elements in mesh order and the rule's nodes, sum |f - u_h|^2 J w,
+    u_h from the element's 10 DOFs (feSpaceTetPn(2) basis), positions from the
+    P1 geometry; returns the square root."""
+    q = np.asarray(quad, np.float64).reshape(-1, 4)
+    X = np.asarray(tet_xyz, np.float64).reshape(-1, 4, 3)
+    adr = np.asarray(adr, np.int64).reshape(-1, 10)
+    phi, _ = tet_p2_basis(q[:, 0], q[:, 1], q[:, 2])
+    psi = np.stack([1 - q[:, 0] - q[:, 1] - q[:, 2], q[:, 0], q[:, 1], q[:, 2]], -1)
+    det = np.linalg.det(np.stack([X[:, 1] - X[:, 0], X[:, 2] - X[:, 0], X[:, 3] - X[:, 0]], -1))
+    xq = np.einsum("qv,evx->eqx", psi, X)
+    uh = np.asarray(u, np.float64)[adr] @ phi.T
+    e2 = (fct(xq[..., 0], xq[..., 1], xq[..., 2]) - uh) ** 2
+    return float(np.sqrt(((e2 * q[None, :, 3]).sum(1) * det).sum()))

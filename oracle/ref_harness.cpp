@@ -315,6 +315,8 @@ int main(int argc, char **argv)
   std::vector<feSpace *> spaces, essential, domainSpaces;
   std::vector<feBilinearForm *> forms;
   int degQ = 4;
+  // Tetrahedral runs may ask for another rule (its values are written out).
+  if(dim3 && getenv("FE_HARNESS_QDEG")) degQ = atoi(getenv("FE_HARNESS_QDEG"));
   if(problem == "diffusion" || dim3) {
     feSpace *u = nullptr, *uB = nullptr;
     feCheck(createFiniteElementSpace(uB, &mesh, elementType::LAGRANGE, 2, "U", "Bord", degQ, dim3 ? &fSin3 : &fSinSin));

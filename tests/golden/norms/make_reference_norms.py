@@ -9,16 +9,27 @@
   (tests/withLinearSolver/navier_stokes.cpp:297, stokes.cpp:286): the
   triangles of "Domain", the lines of "NoSlip" and "Inlet" (the essential
   boundary) and the lines of "Outlet";
+* the tetrahedral meshes data/cube1-3.msh of the interpolation test
+  (tests/withoutLinearSolver/interpolation.cpp:50), read with this package's
+  reader, with the reference's own element DOF tables, CSR pattern and
+  coloring for P2 spaces on them (the reference harness, oracle/ref_harness.cpp,
+  diffusion3d) and its degree-12 tetrahedral rule;
 * the L2 errors those tests print in their golden output files:
     - tests/withLinearSolver/scalarFE_diffusion.output, block "P2 field 0"
       (P2 diffusion, u = sin(pi x) sin(pi y), quadrature degree 8)
     - tests/withLinearSolver/navier_stokes_MMS.output, "Divergence
-      formulation" blocks (Taylor-Hood P2-P1 MMS, velocity and pressure).
+      formulation" blocks (Taylor-Hood P2-P1 MMS, velocity and pressure)
+    - tests/withoutLinearSolver/interpolationScalar.output, block
+      "Dimension 3 - Lagrange elements P2" (nodal P2 interpolation of
+      x^6 + y^6 on the cubes, quadrature degree 12).
 
 Run where the reference exists:  python tests/golden/norms/make_reference_norms.py [REF_ROOT]
 """
+import os
 import re
+import subprocess
 import sys
+import tempfile
 from pathlib import Path
 
 import numpy as np
@@ -55,6 +66,26 @@ def main(ref=Path("/root/reference")):
     a = fe.Mesh2DP1.from_msh(pm, domain="Domain", boundary=("NoSlip", "Inlet"), point=None).arrays()
     out["pois_x"], out["pois_y"], out["pois_tri"], out["pois_bnd"] = a["x"], a["y"], a["tri"], a["bnd"]
     out["pois_outlet"] = fe.Mesh2DP1.from_msh(pm, domain="Domain", boundary=("Outlet",), point=None).arrays()["bnd"]
+    root = HERE.parents[2]
+    subprocess.run(["make", "-C", str(root / "oracle"), "ref", f"REF={ref}", "-j8"], check=True,
+                   capture_output=True)
+    for i in range(1, 4):
+        cm = ref / f"data/cube{i}.msh"
+        a = fe.Mesh3DP1.from_msh(cm).arrays()
+        for k in ("x", "y", "z", "tet", "bnd"):
+            out[f"cube{i}_{k}"] = a[k]
+        with tempfile.TemporaryDirectory() as td:
+            subprocess.run([str(root / "oracle/_ref/ref_harness"), str(cm), "diffusion3d", td, "1", "1"], check=True,
+                           env={**os.environ, "FE_HARNESS_QDEG": "12"})
+            td = Path(td)
+            out[f"cube{i}_adr"] = np.fromfile(td / "adr.i64", np.int64)
+            out[f"cube{i}_ia"] = np.fromfile(td / "ia.i64", np.int64)
+            out[f"cube{i}_ja"] = np.fromfile(td / "ja.i64", np.int64)
+            out[f"cube{i}_color_offsets"] = np.fromfile(td / "color_offsets.i64", np.int64)
+            out[f"cube{i}_color_elements"] = np.fromfile(td / "color_elements.i32", np.int32)
+            out["tet_quad12"] = np.fromfile(td / "quad.f64").reshape(-1, 4)
+    t = (ref / "tests/withoutLinearSolver/interpolationScalar.output").read_text()
+    out["interp3d_p2_nelm"], out["interp3d_p2_err"] = parse_block(t, "Dimension 3 - Lagrange elements P2")
     t = (ref / "tests/withLinearSolver/scalarFE_diffusion.output").read_text()
     out["diff_nelm"], out["diff_err_u"] = parse_block(t, "Diffusion - Error on u - Lagrange elements P2 field 0")
     t = (ref / "tests/withLinearSolver/navier_stokes_MMS.output").read_text()

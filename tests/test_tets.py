@@ -135,3 +135,57 @@ def test_tet_setup_is_deterministic():
     b = _tet_numbering(m).setup()
     np.testing.assert_array_equal(a.pattern()[1], b.pattern()[1])
     np.testing.assert_array_equal(a.elementDofs(), b.elementDofs())
+
+
+def _cube(g, i):
+    return fe.Mesh3DP1.from_arrays(*(g[f"cube{i}_{k}"] for k in ("x", "y", "z", "tet", "bnd")))
+
+
+@pytest.mark.parametrize("i", [1, 2, 3])
+def test_tet_setup_on_reference_meshes_bit_exact(i):
+    """The reference's own Gmsh meshes data/cube1-3.msh (read by this
+    package's reader, tests/golden/norms/make_reference_norms.py): element
+    DOF tables, CSR pattern and coloring equal the reference's."""
+    from helpers import reference_l2
+    g = reference_l2()
+    st = _tet_numbering(_cube(g, i)).setup()
+    np.testing.assert_array_equal(st.elementDofs().reshape(-1), g[f"cube{i}_adr"])
+    ia, ja = st.pattern()
+    np.testing.assert_array_equal(ia, g[f"cube{i}_ia"])
+    np.testing.assert_array_equal(ja, g[f"cube{i}_ja"])
+    off, el = st.coloring()
+    np.testing.assert_array_equal(off, g[f"cube{i}_color_offsets"])
+    np.testing.assert_array_equal(el, g[f"cube{i}_color_elements"])
+
+
+def test_tet_interpolation_errors_match_reference_output():
+    """tests/withoutLinearSolver/interpolationScalar.output, "Dimension 3 -
+    Lagrange elements P2": x^6 + y^6 interpolated at the P2 nodes of
+    data/cube1-3.msh, L2 error with the degree-12 rule, printed with 7
+    significant digits (interpolation.cpp:12-100)."""
+    from helpers import reference_l2
+    from oracle.oracle import l2_error_tet
+    g = reference_l2()
+    for i in range(1, 4):
+        mesh = _cube(g, i)
+        st = _tet_numbering(mesh).setup()
+        x, y, *_ = st.dofInfo()
+        u = x ** 6 + y ** 6
+        xyz = np.stack([g[f"cube{i}_x"], g[f"cube{i}_y"], g[f"cube{i}_z"]], 1)[g[f"cube{i}_tet"]]
+        e = l2_error_tet(st.elementDofs(), xyz, u, g["tet_quad12"], lambda a, b, c: a ** 6 + b ** 6)
+        assert len(g[f"cube{i}_tet"]) == g["interp3d_p2_nelm"][i - 1]
+        assert f"{e:.6e}" == f"{float(g['interp3d_p2_err'][i - 1]):.6e}"
+
+
+def test_tet_reader_reads_reference_files():
+    """Where the reference checkout exists: the fixture arrays are what the
+    reader makes of data/cube1-3.msh."""
+    from helpers import reference_l2
+    ref = Path("/root/reference/data")
+    if not ref.exists():
+        pytest.skip("reference checkout absent")
+    g = reference_l2()
+    for i in range(1, 4):
+        a = fe.Mesh3DP1.from_msh(ref / f"cube{i}.msh").arrays()
+        for k in ("x", "y", "z", "tet", "bnd"):
+            np.testing.assert_array_equal(a[k], g[f"cube{i}_{k}"])
