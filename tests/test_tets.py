@@ -189,3 +189,20 @@ def test_tet_reader_reads_reference_files():
         a = fe.Mesh3DP1.from_msh(ref / f"cube{i}.msh").arrays()
         for k in ("x", "y", "z", "tet", "bnd"):
             np.testing.assert_array_equal(a[k], g[f"cube{i}_{k}"])
+
+
+def test_msh_readers_refuse_truncated_files(tmp_path):
+    """A file cut anywhere in its node or element sections is an error, not
+    a mesh read from uninitialised counts."""
+    m3 = fe.Mesh3DP1.generate_cube(2, seed=1)
+    m3.write_msh(tmp_path / "c.msh")
+    m2 = fe.Mesh2DP1.generate_square(4)
+    m2.write_msh(tmp_path / "s.msh")
+    for name, reader in (("c.msh", fe.Mesh3DP1.from_msh), ("s.msh", fe.Mesh2DP1.from_msh)):
+        text = (tmp_path / name).read_text()
+        start = text.index("$Nodes")
+        for frac in (0.1, 0.3, 0.5, 0.7, 0.9):
+            cut = start + int((len(text) - start) * frac)
+            (tmp_path / "t.msh").write_text(text[:cut])
+            with pytest.raises(FeError):
+                reader(tmp_path / "t.msh")
