@@ -6,6 +6,7 @@ direct sparse solve, errors by the oracle's restatement of feNorm.
 
 The golden files print 7 significant digits (%e); as the reference's test
 (compareOutputFiles), the errors must print the same."""
+import os
 from pathlib import Path
 
 import numpy as np
@@ -54,7 +55,7 @@ def test_fixture_meshes_read_back_from_the_reference_files():
     """Where the reference checkout exists: the fixture arrays are what this
     package's msh reader makes of the reference's mesh files."""
     import feng_gb300 as fe
-    ref = Path("/root/reference/data")
+    ref = Path(os.environ.get("FENG_REFERENCE", "/root/reference")) / "data"
     if not ref.exists():
         pytest.skip("reference checkout absent")
     g = reference_l2()

@@ -4,6 +4,7 @@ tests/golden/make_golden.py: the reference reads the generated msh file and
 assembles feSysElm_Diffusion<3> + feSysElm_Source on feSpaceTetPn(2), then
 solves).  Runs on the CPU."""
 from collections import Counter
+import os
 from pathlib import Path
 
 import numpy as np
@@ -181,7 +182,7 @@ def test_tet_reader_reads_reference_files():
     """Where the reference checkout exists: the fixture arrays are what the
     reader makes of data/cube1-3.msh."""
     from helpers import reference_l2
-    ref = Path("/root/reference/data")
+    ref = Path(os.environ.get("FENG_REFERENCE", "/root/reference")) / "data"
     if not ref.exists():
         pytest.skip("reference checkout absent")
     g = reference_l2()
