@@ -89,6 +89,7 @@ SIGNATURES = {
     "fe_mesh_read_msh": (C.c_int, [C.c_char_p, C.POINTER(P)]),
     "fe_export_vtk": (C.c_int, [P, P, P, C.POINTER(C.c_char_p), C.c_int, C.POINTER(C.c_char_p), C.c_int,
                                 C.c_int, C.c_char_p]),
+    "fe_tet_quadrature_rule": (C.c_int, [C.c_int, C.POINTER(C.c_int), P, P, P, P]),
     "fe_setup3d_create": (C.c_int, [P, P, C.c_int, C.c_int, C.c_int, C.POINTER(P)]),
     "fe_setup_get_dof_z": (C.c_int, [P, P]),
     "fe_mesh3d_generate_cube": (C.c_int, [C.c_int, P, C.c_double, C.c_uint64, C.POINTER(P)]),

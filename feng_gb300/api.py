@@ -320,6 +320,16 @@ def quadrature_rule(degree: int):
     return r[:k].copy(), s[:k].copy(), w[:k].copy()
 
 
+def tet_quadrature_rule(degree: int):
+    """Symmetric tetrahedral rule of the given degree (1..8): r, s, t, w."""
+    lib = _lib.load()
+    n = C.c_int()
+    check(lib.fe_tet_quadrature_rule(degree, C.byref(n), None, None, None, None))
+    r, s, t, w = (np.empty(n.value) for _ in range(4))
+    check(lib.fe_tet_quadrature_rule(degree, C.byref(n), ptr(r), ptr(s), ptr(t), ptr(w)))
+    return r, s, t, w
+
+
 @dataclass
 class feSysElm:
     kind: int

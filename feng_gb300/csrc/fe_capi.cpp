@@ -530,6 +530,21 @@ int fe_setup_get_blocks(const fe_setup *s, int32_t *block_of_row)
   return FE_OK;
 }
 
+int fe_tet_quadrature_rule(int degree, int *n, double *r, double *s, double *t, double *w)
+{
+  GUARD_BEGIN
+  if(!n) { set_error("null argument"); return FE_INVALID_ARG; }
+  QuadRule q;
+  FE_TRY(tet_rule(degree, q));
+  *n = q.n();
+  if(r) std::copy(q.r.begin(), q.r.end(), r);
+  if(s) std::copy(q.s.begin(), q.s.end(), s);
+  if(t) std::copy(q.t.begin(), q.t.end(), t);
+  if(w) std::copy(q.w.begin(), q.w.end(), w);
+  return FE_OK;
+  GUARD_END
+}
+
 int fe_quadrature_rule(int degree, int *n, double *r, double *s, double *w)
 {
   GUARD_BEGIN

@@ -25,9 +25,15 @@ namespace feng {
 struct QuadRule {
   int degree = 0;
   std::vector<double> r, s, w;
+  std::vector<double> t;  // third reference coordinate (tetrahedral rules only)
   int n() const { return (int)w.size(); }
 };
 int triangle_rule(int degree, QuadRule &q);
+// Fully symmetric rules on the reference tetrahedron (0,0,0)-(1,0,0)-(0,1,0)-
+// (0,0,1), weights summing to 1/6, degrees 1 to 8 with the orbit structure of
+// the reference's rules (getGQTetPts, src/feQuadratureTet.cpp:3342): number
+// of points 1, 4, 5, 11, 14, 24, 31, 43.
+int tet_rule(int degree, QuadRule &q);
 
 // Geometric connectivities a space can live on.
 enum Cnc : int { CNC_DOMAIN = 0, CNC_BOUNDARY = 1, CNC_POINT = 2 };

@@ -241,6 +241,10 @@ int fe_setup_get_dof_info(const fe_setup *s, double *x, double *y, int32_t *fiel
 int fe_setup_get_blocks(const fe_setup *s, int32_t *block_of_row);
 /* Quadrature rule: n points (<= 16), r, s, w [n]. */
 int fe_quadrature_rule(int degree, int *n, double *r, double *s, double *w);
+/* Tetrahedral rule of degree 1..8 (1, 4, 5, 11, 14, 24, 31, 43 points; the
+ * orbit structures of getGQTetPts, src/feQuadratureTet.cpp:3342), weights
+ * summing to 1/6; outputs may be NULL to query n. */
+int fe_tet_quadrature_rule(int degree, int *n, double *r, double *s, double *t, double *w);
 
 /* ---- VTK export (feExporterVTK::writeStep, src/feExporter.h:36-116,
  * src/feExporter.cpp:854-990), on the host, no device needed.

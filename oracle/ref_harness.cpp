@@ -408,6 +408,7 @@ int main(int argc, char **argv)
       quad.push_back(w[k]);
     }
   }
+  write_raw(out + "/quad.f64", quad);  // also when a later step fails
 
   if(cavity) {
     // BDF2 from rest (BDF1 starter of 0.1 dt, the reference's default) with

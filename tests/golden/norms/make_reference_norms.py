@@ -13,7 +13,7 @@
   (tests/withoutLinearSolver/interpolation.cpp:50), read with this package's
   reader, with the reference's own element DOF tables, CSR pattern and
   coloring for P2 spaces on them (the reference harness, oracle/ref_harness.cpp,
-  diffusion3d) and its degree-12 tetrahedral rule;
+  diffusion3d) and its tetrahedral rules of degrees 1-8 and 12;
 * the L2 errors those tests print in their golden output files:
     - tests/withLinearSolver/scalarFE_diffusion.output, block "P2 field 0"
       (P2 diffusion, u = sin(pi x) sin(pi y), quadrature degree 8)
@@ -84,6 +84,13 @@ def main(ref=Path("/root/reference")):
             out[f"cube{i}_color_offsets"] = np.fromfile(td / "color_offsets.i64", np.int64)
             out[f"cube{i}_color_elements"] = np.fromfile(td / "color_elements.i32", np.int32)
             out["tet_quad12"] = np.fromfile(td / "quad.f64").reshape(-1, 4)
+    # The reference's tetrahedral rules of degrees 1-8 (low degrees make the
+    # harness's P2 solve singular after the rule is written: not checked).
+    for deg in range(1, 9):
+        with tempfile.TemporaryDirectory() as td:
+            subprocess.run([str(root / "oracle/_ref/ref_harness"), str(ref / "data/cube1.msh"), "diffusion3d", td,
+                            "1", "1"], env={**os.environ, "FE_HARNESS_QDEG": str(deg)}, capture_output=True)
+            out[f"tet_quad{deg}"] = np.fromfile(Path(td) / "quad.f64").reshape(-1, 4)
     t = (ref / "tests/withoutLinearSolver/interpolationScalar.output").read_text()
     out["interp3d_p2_nelm"], out["interp3d_p2_err"] = parse_block(t, "Dimension 3 - Lagrange elements P2")
     t = (ref / "tests/withLinearSolver/scalarFE_diffusion.output").read_text()
