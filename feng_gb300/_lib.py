@@ -99,6 +99,8 @@ SIGNATURES = {
     "fe_mesh3d_sizes": (C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "fe_mesh3d_arrays": (C.c_int, [P, P, P, P, P, P]),
     "fe_mesh3d_destroy": (None, [P]),
+    "fe_export_vtk3d": (C.c_int, [P, P, P, C.POINTER(C.c_char_p), C.c_int, C.POINTER(C.c_char_p), C.c_int,
+                                  C.c_int, C.c_char_p]),
     "fe_mesh_read_msh_groups": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_char_p), C.c_int,
                                           C.c_char_p, C.POINTER(P)]),
     "fe_mesh_write_msh": (C.c_int, [P, C.c_char_p]),

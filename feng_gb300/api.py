@@ -649,8 +649,10 @@ class feExporterVTK:
         names = (C.c_char_p * len(num.fieldIDs))(*[f.encode() for f in num.fieldIDs])
         req = (C.c_char_p * len(wanted))(*[f.encode() for f in wanted])
         st = num.setup()
-        check(_lib.load().fe_export_vtk(self.mesh._h, st._h, ptr(u), names, len(num.fieldIDs), req, len(wanted),
-                                        int(precision), str(fileName).encode()))
+        lib = _lib.load()
+        fn = lib.fe_export_vtk3d if isinstance(self.mesh, Mesh3DP1) else lib.fe_export_vtk
+        check(fn(self.mesh._h, st._h, ptr(u), names, len(num.fieldIDs), req, len(wanted), int(precision),
+                 str(fileName).encode()))
 
 
 def createVisualizationExporter(fmt, numbering, solution, mesh, spaces):

@@ -1089,17 +1089,15 @@ extern "C" int fe_cuda_apply_periodicity(fe_cuda_system *s)
   GUARD_END
 }
 
-int fe_export_vtk(const fe_mesh *m, const fe_setup *s, const double *solution,
-                  const char *const *field_names, int n_field_names, const char *const *required,
-                  int n_required, int precision, const char *path)
+// Fields to export: those with a space on the domain, in the order of their
+// first domain space, filtered by `required`, then reversed: the reference
+// fills an unordered_map in space order and writes in its iteration order,
+// which for the two fields of this path is the reverse.
+static int export_fields(const fe_setup *s, const char *const *field_names, int n_field_names,
+                         const char *const *required, int n_required, std::vector<ExportField> &fields)
 {
-  GUARD_BEGIN
-  if(!m || !s || !solution || !field_names || !path || n_required < 0 || (n_required > 0 && !required)) {
+  if(!field_names || n_required < 0 || (n_required > 0 && !required)) {
     set_error("null argument");
-    return FE_INVALID_ARG;
-  }
-  if(s->tets || m->m.n_vertices() != s->nVertices || m->m.n_edges != s->nEdges) {
-    set_error("the setup was not built on this mesh");
     return FE_INVALID_ARG;
   }
   if(n_field_names != s->num.nFields) {
@@ -1114,9 +1112,7 @@ int fe_export_vtk(const fe_mesh *m, const fe_setup *s, const double *solution,
     for(int f = 0; f < n_field_names; ++f) known |= std::string(required[i]) == field_names[f];
     if(!known) { set_error("no field named \"%s\"", required[i]); return FE_INVALID_ARG; }
   }
-  // Fields with a space on the domain, in the order of their first domain
-  // space, filtered by `required`.
-  std::vector<ExportField> fields;
+  fields.clear();
   for(const SpaceDesc &d : s->spaces) {
     if(d.cnc != CNC_DOMAIN) continue;
     bool seen = false;
@@ -1126,9 +1122,38 @@ int fe_export_vtk(const fe_mesh *m, const fe_setup *s, const double *solution,
     for(int i = 0; i < n_required; ++i) wanted |= std::string(required[i]) == field_names[d.field];
     if(wanted) fields.push_back({d.field, field_names[d.field], d.degree});
   }
-  // The reference fills an unordered_map in space order and writes in its
-  // iteration order, which for the two fields of this path is the reverse.
   std::reverse(fields.begin(), fields.end());
+  return FE_OK;
+}
+
+int fe_export_vtk(const fe_mesh *m, const fe_setup *s, const double *solution,
+                  const char *const *field_names, int n_field_names, const char *const *required,
+                  int n_required, int precision, const char *path)
+{
+  GUARD_BEGIN
+  if(!m || !s || !solution || !path) { set_error("null argument"); return FE_INVALID_ARG; }
+  if(s->tets || m->m.n_vertices() != s->nVertices || m->m.n_edges != s->nEdges) {
+    set_error("the setup was not built on this mesh");
+    return FE_INVALID_ARG;
+  }
+  std::vector<ExportField> fields;
+  FE_TRY(export_fields(s, field_names, n_field_names, required, n_required, fields));
   return export_vtk(m->m, s->num, solution, fields, precision == 0 ? 6 : precision, path);
+  GUARD_END
+}
+
+int fe_export_vtk3d(const fe_mesh3d *m, const fe_setup *s, const double *solution,
+                    const char *const *field_names, int n_field_names, const char *const *required,
+                    int n_required, int precision, const char *path)
+{
+  GUARD_BEGIN
+  if(!m || !s || !solution || !path) { set_error("null argument"); return FE_INVALID_ARG; }
+  if(!s->tets || m->m.n_vertices() != s->nVertices || m->m.n_edges != s->nEdges) {
+    set_error("the setup was not built on this mesh");
+    return FE_INVALID_ARG;
+  }
+  std::vector<ExportField> fields;
+  FE_TRY(export_fields(s, field_names, n_field_names, required, n_required, fields));
+  return export_vtk3d(m->m, s->num, solution, fields, precision == 0 ? 6 : precision, path);
   GUARD_END
 }

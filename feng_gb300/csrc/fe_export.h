@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "fe_mesh.h"
+#include "fe_mesh3d.h"
 #include "fe_setup.h"
 
 namespace feng {
@@ -42,5 +43,15 @@ struct ExportField {
 // (1..17; the reference writes 6).
 int export_vtk(const Mesh2D &m, const Numbering &num, const double *solution,
                const std::vector<ExportField> &fields, int precision, const std::string &path);
+
+// The same file for a tetrahedral mesh, with the same rules for nodes and
+// values (vertices, then edge midpoints in ascending vertex-pair order;
+// 3-vectors written as they are).  Cells are VTK_QUADRATIC_TETRA (24, VTK's
+// node order: vertices, then edges (0,1) (1,2) (0,2) (0,3) (1,3) (2,3)) or
+// VTK_TETRA (10) when every field is P1.  The reference's exporter has no
+// tetrahedral P2 layout (it writes 6-node triangle cells for any
+// P2 field), so this one follows VTK's.
+int export_vtk3d(const Mesh3D &m, const Numbering &num, const double *solution,
+                 const std::vector<ExportField> &fields, int precision, const std::string &path);
 
 }  // namespace feng

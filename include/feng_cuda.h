@@ -264,6 +264,13 @@ int fe_tet_quadrature_rule(int degree, int *n, double *r, double *s, double *t, 
 int fe_export_vtk(const fe_mesh *m, const fe_setup *s, const double *solution,
                   const char *const *field_names, int n_field_names, const char *const *required,
                   int n_required, int precision, const char *path);
+/* The same for a tetrahedral set-up: VTK_QUADRATIC_TETRA cells (24, VTK's node
+ * order: vertices, then edges (0,1) (1,2) (0,2) (0,3) (1,3) (2,3)), or
+ * VTK_TETRA (10) when every field is P1; 3-vectors written as they are.  The
+ * reference has no tetrahedral P2 layout to follow. */
+int fe_export_vtk3d(const fe_mesh3d *m, const fe_setup *s, const double *solution,
+                    const char *const *field_names, int n_field_names, const char *const *required,
+                    int n_required, int precision, const char *path);
 
 /* ---- system creation */
 /* Standalone route: device system from a host set-up. */

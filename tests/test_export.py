@@ -137,3 +137,49 @@ def test_vtk_arguments(tmp_path):
         fe.createVisualizationExporter(fe.VTK, num, g["usol"], other, num.spaces).writeStep(tmp_path / "x.vtk")
     with pytest.raises(ValueError):
         fe.createVisualizationExporter("GMSH", num, g["usol"], mesh, num.spaces)
+
+
+def test_vtk_tetrahedra(tmp_path):
+    """Tetrahedral export: vertices then edge midpoints, VTK_QUADRATIC_TETRA
+    cells whose edge nodes sit at the midpoints of VTK's edges (0,1) (1,2)
+    (0,2) (0,3) (1,3) (2,3), the DOF values at their nodes, and VTK_TETRA
+    cells without mid-edge nodes when only the P1 field is written."""
+    mesh = fe.Mesh3DP1.generate_cube(2, jitter=0.05, seed=4)
+    spaces = [fe.createFiniteElementSpace(mesh, fe.VECTOR_LAGRANGE, 2, "U", "Domaine", 4),
+              fe.createFiniteElementSpace(mesh, fe.VECTOR_LAGRANGE, 2, "U", "Bord", 4),
+              fe.createFiniteElementSpace(mesh, fe.LAGRANGE, 1, "P", "Domaine", 4)]
+    num = fe.feMetaNumber(mesh, spaces, [spaces[1]])
+    st = num.setup()
+    u = np.random.default_rng(1).uniform(-1, 1, st.nDofs)
+    ex = fe.createVisualizationExporter(fe.VTK, num, u, mesh, num.spaces)
+    ex.writeStep(tmp_path / "t.vtk", precision=17)
+    lines = (tmp_path / "t.vtk").read_text().splitlines()
+    a = mesh.arrays()
+    nv, nt = len(a["x"]), len(a["tet"])
+    n_nodes = int(lines[4].split()[1])
+    pts = np.array([[float(v) for v in ln.split()] for ln in lines[5:5 + n_nodes]])
+    np.testing.assert_array_equal(pts[:nv], np.stack([a["x"], a["y"], a["z"]], 1))
+    c0 = 5 + n_nodes
+    assert lines[c0] == f"CELLS {nt} {nt * 11}"
+    cells = np.array([[int(v) for v in ln.split()] for ln in lines[c0 + 1:c0 + 1 + nt]])
+    assert np.all(cells[:, 0] == 10)
+    np.testing.assert_array_equal(cells[:, 1:5], a["tet"])
+    for k, (i, j) in enumerate([(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)]):
+        mid = (pts[cells[:, 1 + i]] + pts[cells[:, 1 + j]]) / 2
+        np.testing.assert_allclose(pts[cells[:, 5 + k]], mid, rtol=0, atol=1e-15)
+    t0 = c0 + 1 + nt
+    assert lines[t0] == f"CELL_TYPES {nt}" and set(lines[t0 + 1:t0 + 1 + nt]) == {"24"}
+    f = _fields(lines)
+    assert list(f) == ["P", "U"]
+    s_, w, n = f["U"]
+    vel = np.array([float(v) for v in lines[s_:s_ + w * n]]).reshape(n, 3)
+    x, y, fld, comp, _ = st.dofInfo()
+    z = st.dofZ()
+    key = {tuple(p): i for i, p in enumerate(pts)}
+    for d in np.flatnonzero(fld == 0):
+        v = u[d] if abs(u[d]) >= 1e-20 else 0.0
+        assert vel[key[(x[d], y[d], z[d])], comp[d]] == v
+    ex.writeStep(tmp_path / "p.vtk", requiredFields=["P"])
+    text = (tmp_path / "p.vtk").read_text()
+    assert f"POINTS {nv} double" in text and f"CELLS {nt} {nt * 5}" in text
+    assert "\n10\n" in text and "\n24\n" not in text
