@@ -295,7 +295,9 @@ int build_csr_pattern(const ElementTables &et, int64_t nInc, CSRPattern &pat)
   // Row r: its diagonal and the coupled unknown DOFs of the elements that
   // hold it, sorted and unique.  Consecutive rows are built in chunks on the
   // host threads, each chunk into its own array, then copied into place, so
-  // the scratch memory is the size of the pattern.
+  // the scratch memory is the size of the pattern.  A per-thread stamp
+  // (last row that took each column) drops repeated columns while gathering,
+  // so only the unique columns are sorted.
   constexpr int64_t kRows = 1 << 12;
   const int64_t nChunks = (nInc + kRows - 1) / kRows;
   std::vector<std::vector<int32_t>> part((size_t)nChunks);
@@ -306,23 +308,29 @@ int build_csr_pattern(const ElementTables &et, int64_t nInc, CSRPattern &pat)
       nChunks,
       [&](int64_t c0, int64_t c1) {
         std::vector<int32_t> row;
+        std::vector<int32_t> stamp((size_t)nInc, -1);
         for(int64_t c = c0; c < c1; ++c) {
           std::vector<int32_t> &out = part[(size_t)c];
           const int64_t rEnd = std::min(nInc, (c + 1) * kRows);
           for(int64_t r = c * kRows; r < rEnd; ++r) {
             row.clear();
             row.push_back((int32_t)r);
+            stamp[(size_t)r] = (int32_t)r;
             for(int64_t k = dptr[r]; k < dptr[r + 1]; ++k) {
               const int64_t t = adj[k] / nl;
               const int i = (int)(adj[k] - t * nl);
               const int64_t *a = &et.adr[t * nl];
-              for(int j = 0; j < nl; ++j)
-                if(et.mask[i * nl + j] && a[j] < nInc) row.push_back((int32_t)a[j]);
+              for(int j = 0; j < nl; ++j) {
+                const int64_t col = a[j];
+                if(et.mask[i * nl + j] && col < nInc && stamp[(size_t)col] != (int32_t)r) {
+                  stamp[(size_t)col] = (int32_t)r;
+                  row.push_back((int32_t)col);
+                }
+              }
             }
             std::sort(row.begin(), row.end());
-            const auto e = std::unique(row.begin(), row.end());
-            pat.ia[r + 1] = e - row.begin();
-            out.insert(out.end(), row.begin(), e);
+            pat.ia[r + 1] = (int64_t)row.size();
+            out.insert(out.end(), row.begin(), row.end());
           }
         }
       },
