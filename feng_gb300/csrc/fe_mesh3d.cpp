@@ -3,7 +3,6 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
-#include <unordered_map>
 
 #include "fe_common.h"
 #include "fe_msh.h"
@@ -20,19 +19,24 @@ int Mesh3D::build_topology()
     if(v < 0 || v >= nv) { set_error("tetrahedron vertex out of range"); return FE_INVALID_ARG; }
   for(int32_t v : bnd)
     if(v < 0 || v >= nv) { set_error("boundary triangle vertex out of range"); return FE_INVALID_ARG; }
-  std::unordered_map<uint64_t, int32_t> id;
-  id.reserve((size_t)(nv * 8 + 16));
+  // Edges of each vertex to higher-numbered neighbours: (neighbour, edge id).
+  std::vector<std::vector<std::pair<int32_t, int32_t>>> adj((size_t)nv);
   edge_v.clear();
-  auto key = [](int32_t a, int32_t b) {
-    return ((uint64_t)(uint32_t)std::min(a, b) << 32) | (uint32_t)std::max(a, b);
+  auto find = [&](int32_t a, int32_t b) {
+    const int32_t lo = std::min(a, b), hi = std::max(a, b);
+    for(const auto &p : adj[(size_t)lo])
+      if(p.first == hi) return p.second;
+    return (int32_t)-1;
   };
   auto add = [&](int32_t a, int32_t b) {
-    auto r = id.emplace(key(a, b), (int32_t)(edge_v.size() / 2));
-    if(r.second) {
+    int32_t e = find(a, b);
+    if(e < 0) {
+      e = (int32_t)(edge_v.size() / 2);
+      adj[(size_t)std::min(a, b)].push_back({std::max(a, b), e});
       edge_v.push_back(a);
       edge_v.push_back(b);
     }
-    return r.first->second;
+    return e;
   };
   bnd_edges.assign(nb * 3, -1);
   for(int64_t i = 0; i < nb; ++i)
@@ -47,7 +51,7 @@ int Mesh3D::build_topology()
   tet_edges.assign(nt * 6, -1);
   for(int64_t t = 0; t < nt; ++t)
     for(int k = 0; k < 6; ++k)
-      tet_edges[6 * t + k] = id.at(key(tet[4 * t + TET_EDGES[k][0]], tet[4 * t + TET_EDGES[k][1]]));
+      tet_edges[6 * t + k] = find(tet[4 * t + TET_EDGES[k][0]], tet[4 * t + TET_EDGES[k][1]]);
   // Every boundary edge must belong to a tetrahedron: edges only the
   // boundary created and no tetrahedron met mean a stray boundary triangle.
   std::vector<uint8_t> used((size_t)n_edges, 0);
