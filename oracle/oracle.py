@@ -1,7 +1,10 @@
-"""ctypes binding of the CPU oracle (oracle/fe_oracle.c).
+"""The CPU oracle: a ctypes binding of its C restatement (oracle/fe_oracle.c,
+oracle/mlp_oracle.c) and numpy restatements of the error norms, the direct
+Newton solve and the tetrahedral forms (P2 diffusion; Taylor-Hood forms on
+triangles and tetrahedra).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
-bench.py's CPU-baseline leg, never by the product.  Built by
+bench.py's CPU-baseline leg, never by the product.  The C part is built by
 ``make -C oracle port`` into oracle/_ref/libfeoracle.so.
 """
 from __future__ import annotations
