@@ -30,7 +30,7 @@ struct Mesh3D {
   // (src/feMeshRead.cpp:1320-1345, 1481-1538): the edges (k, k+1) of each
   // boundary triangle, then, for each tetrahedron, the edges (0,1), (1,2),
   // (2,0) of its facets taken in TET_FACES order (Tetrahedron::createBoundary,
-  // src/feTetrahedron.cpp:6-32).  Checks that every edge of a boundary
+  // src/feTetrahedron.cpp:6-72).  Checks that every edge of a boundary
   // triangle is an edge of the tetrahedra.
   int build_topology();
 };
