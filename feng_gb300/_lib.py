@@ -172,6 +172,8 @@ SIGNATURES = {
     "fe_cuda_transient_create": (C.c_int, [P, C.POINTER(TransientOptions), C.POINTER(NewtonOptions),
                                            C.POINTER(P)]),
     "fe_cuda_transient_steps": (C.c_int, [P, C.c_int, P]),
+    "fe_cuda_transient_get_network": (C.c_int, [P, P]),
+    "fe_cuda_transient_set_network": (C.c_int, [P, P]),
     "fe_cuda_transient_destroy": (None, [P]),
     "fe_mlp_sizes": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                C.POINTER(C.c_int), C.POINTER(C.c_int64)]),

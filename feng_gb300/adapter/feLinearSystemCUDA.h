@@ -148,8 +148,14 @@ public:
     assembleMatrices(sol, onlyTransient);
     assembleResiduals(sol);
   }
-  void assembleMatrices(const feSolution *sol, const bool /*onlyTransient*/) override
+  void assembleMatrices(const feSolution *sol, const bool onlyTransient) override
   {
+    // The reference's backends then assemble only the forms with
+    // isTransientMatrix() (solves for the time derivative); the fused device
+    // kernels assemble every form together, so that mode is refused rather
+    // than silently solved with the full Jacobian.
+    if(onlyTransient)
+      throw std::runtime_error("feLinearSystemCUDA: transient-only matrix assembly is not offloaded");
     upload(sol);
     check(fe_cuda_assemble_matrices(_sys), "fe_cuda_assemble_matrices");
   }

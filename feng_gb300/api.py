@@ -791,13 +791,32 @@ class BDF2Integrator:
         check(system.lib.fe_cuda_transient_create(system._h, C.byref(o), C.byref(n), C.byref(h)))
         self._h = h
 
-    def makeSteps(self, nSteps: int):
-        """Advances nSteps steps; returns one statistics dict per step."""
+    def makeSteps(self, nSteps: int, raise_on_failure: bool = True):
+        """Advances nSteps steps; returns one statistics dict per step.  A step
+        whose Newton solve fails stops the run: FeError is raised, or with
+        raise_on_failure=False the steps done so far are returned, the last
+        one carrying the failure in "status"."""
         st = (_lib.StepStats * max(nSteps, 1))()
-        check(self.system.lib.fe_cuda_transient_steps(self._h, nSteps, C.cast(st, C.c_void_p)))
+        s = self.system.lib.fe_cuda_transient_steps(self._h, nSteps, C.cast(st, C.c_void_p))
+        if raise_on_failure:
+            check(s)
         if self.sol is not None:
             self.sol.pull()
-        return [{k: getattr(s, k) for k, _ in _lib.StepStats._fields_} for s in st[:nSteps]]
+        return [{k: getattr(x, k) for k, _ in _lib.StepStats._fields_} for x in st[:nSteps] if x.step > 0]
+
+    def getNetwork(self) -> np.ndarray:
+        """The learned guess's network parameters (float32, fe_mlp packing)."""
+        n = C.c_int64()
+        d = [C.c_int() for _ in range(4)]
+        check(self.system.lib.fe_mlp_sizes(*[C.byref(v) for v in d], C.byref(n)))
+        out = np.empty(n.value, np.float32)
+        check(self.system.lib.fe_cuda_transient_get_network(self._h, ptr(out)))
+        return out
+
+    def setNetwork(self, params):
+        """Warm-starts the learned guess from saved parameters."""
+        p = np.ascontiguousarray(params, np.float32)
+        check(self.system.lib.fe_cuda_transient_set_network(self._h, ptr(p)))
 
     def __del__(self):
         h, self._h = getattr(self, "_h", None), None

@@ -57,11 +57,13 @@ def run(n: int, re: float, dt: float, steps: int, guess: str, precision: str = "
 
 
 def summarize(stats, first: int):
-    """Means over steps >= first (1-based)."""
-    late = [s for s in stats if s["step"] >= first]
+    """Means over the converged steps >= first (1-based); steps whose status
+    is not 0 are counted in failed_steps and left out of the means."""
+    failed = sum(1 for s in stats if s["step"] >= first and s["status"] != 0)
+    late = [s for s in stats if s["step"] >= first and s["status"] == 0]
     if not late:
-        return {}
-    return {"steps": len(late),
+        return {"steps": 0, "failed_steps": failed}
+    return {"steps": len(late), "failed_steps": failed,
             "step_ms": statistics.mean(s["step_ms"] for s in late),
             "newton_iterations": statistics.mean(s["newton_iterations"] for s in late),
             "krylov_iterations": statistics.mean(s["krylov_iterations"] for s in late),

@@ -1052,6 +1052,22 @@ extern "C" int fe_cuda_transient_steps(fe_transient *t, int nsteps, fe_step_stat
   GUARD_END
 }
 
+extern "C" int fe_cuda_transient_get_network(const fe_transient *t, float *params)
+{
+  GUARD_BEGIN
+  if(!t || !params) { set_error("null argument"); return FE_INVALID_ARG; }
+  return t->tr.getNetwork(params);
+  GUARD_END
+}
+
+extern "C" int fe_cuda_transient_set_network(fe_transient *t, const float *params)
+{
+  GUARD_BEGIN
+  if(!t || !params) { set_error("null argument"); return FE_INVALID_ARG; }
+  return t->tr.setNetwork(params);
+  GUARD_END
+}
+
 extern "C" void fe_cuda_transient_destroy(fe_transient *t) { delete t; }
 
 // ---- partially essential components and periodicity (feLinearSystem::

@@ -38,6 +38,13 @@ inline void count_launch()
   if(!g_capturing) g_launches.fetch_add(1, std::memory_order_relaxed);
 }
 
+// Maximum that propagates NaN (CUDA's fmax returns the non-NaN operand, which
+// would let a NaN residual vanish from a max-norm and read as convergence).
+#ifdef __CUDACC__
+__host__ __device__ __forceinline__ double nan_max(double a, double b) { return (a > b || a != a) ? a : b; }
+__host__ __device__ __forceinline__ float nan_maxf(float a, float b) { return (a > b || a != a) ? a : b; }
+#endif
+
 // Host loops of the set-up over [0, n) split into contiguous ranges run by
 // up to 32 threads (f(begin, end)); small n runs inline.
 template <typename F>

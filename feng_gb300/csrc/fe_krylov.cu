@@ -96,14 +96,14 @@ __device__ double block_sum(double v, double *sh)
 
 __device__ double block_max(double v, double *sh)
 {
-  for(int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  for(int o = 16; o > 0; o >>= 1) v = nan_max(v, __shfl_down_sync(0xffffffffu, v, o));
   const int w = threadIdx.x / 32, l = threadIdx.x % 32;
   if(l == 0) sh[w] = v;
   __syncthreads();
   v = 0;
   if(threadIdx.x < blockDim.x / 32) v = sh[threadIdx.x];
   if(w == 0)
-    for(int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    for(int o = 16; o > 0; o >>= 1) v = nan_max(v, __shfl_down_sync(0xffffffffu, v, o));
   __syncthreads();
   return v;
 }
@@ -135,7 +135,7 @@ __device__ void finish_reduction(const double (&v)[K], double *partials, RedStat
     double s = 0.;
     for(int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
       const double p = __ldcg(partials + k * MAXRED + i);
-      s = MAX ? fmax(s, p) : s + p;
+      s = MAX ? nan_max(s, p) : s + p;
     }
     s = MAX ? block_max(s, sh) : block_sum(s, sh);
     if(threadIdx.x == 0) {
@@ -162,7 +162,7 @@ __global__ void k_absmax(int64_t n, const double *__restrict__ x, double *partia
   double v[1] = {0.};
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
       i += (int64_t)gridDim.x * blockDim.x)
-    v[0] = fmax(v[0], fabs(x[i]));
+    v[0] = nan_max(v[0], fabs(x[i]));
   finish_reduction<1, true>(v, partials, st, out);
 }
 

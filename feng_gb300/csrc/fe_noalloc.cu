@@ -10,9 +10,12 @@
 // The array's name is only a host-side stand-in in host code: the device
 // address is obtained once per device with cudaGetSymbolAddress (with that
 // device current) and passed to the kernel.  The first call on a device does
-// this set-up, so it should come before any stream capture.  Every call
-// shares the one array, so calls that overlap on the GPU (two streams, two
-// threads) race; the counter is cleared by each call before its kernel.
+// this set-up, so it should come before any stream capture.  The cached
+// address belongs to the device's primary context: after cudaDeviceReset on
+// a device, this entry point must not be called on it again in the same
+// process.  Every call shares the one array, so calls that overlap on the GPU
+// (two streams, two threads) race; the counter is cleared by each call before
+// its kernel.  A NaN anywhere in the input makes the result NaN.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -53,12 +56,12 @@ __global__ void __launch_bounds__(NA_THREADS) k_max_norm_noalloc(const double *_
   double m = 0.;
   for(int k = 0; k < NA_PER_THREAD; ++k) {
     const int64_t i = base + (int64_t)k * NA_THREADS + threadIdx.x;
-    if(i < n) m = fmax(m, fabs(x[i]));
+    if(i < n) m = nan_max(m, fabs(x[i]));
   }
   sh[threadIdx.x] = m;
   __syncthreads();
   for(int o = NA_THREADS / 2; o > 0; o >>= 1) {
-    if(threadIdx.x < o) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + o]);
+    if(threadIdx.x < o) sh[threadIdx.x] = nan_max(sh[threadIdx.x], sh[threadIdx.x + o]);
     __syncthreads();
   }
   if(threadIdx.x == 0) {
@@ -70,11 +73,11 @@ __global__ void __launch_bounds__(NA_THREADS) k_max_norm_noalloc(const double *_
   if(!last) return;
   __threadfence();
   double r = 0.;
-  for(int b = threadIdx.x; b < (int)gridDim.x; b += NA_THREADS) r = fmax(r, ((volatile double *)sc->partial)[b]);
+  for(int b = threadIdx.x; b < (int)gridDim.x; b += NA_THREADS) r = nan_max(r, ((volatile double *)sc->partial)[b]);
   sh[threadIdx.x] = r;
   __syncthreads();
   for(int o = NA_THREADS / 2; o > 0; o >>= 1) {
-    if(threadIdx.x < o) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + o]);
+    if(threadIdx.x < o) sh[threadIdx.x] = nan_max(sh[threadIdx.x], sh[threadIdx.x + o]);
     __syncthreads();
   }
   if(threadIdx.x == 0) {

@@ -255,6 +255,14 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
     set_error("quadrature rule with %d nodes is not supported (1..16)", t.quad.n());
     return FE_INVALID_ARG;
   }
+  // Every DOF id indexes host and device arrays below: range-check them
+  // before any table is built from them.
+  for(int64_t k = 0; k < nE * (int64_t)nloc_; ++k)
+    if(t.adr[k] < 0 || t.adr[k] >= nDofs_) {
+      set_error("element %lld: DOF id %lld out of range [0, %lld)", (long long)(k / nloc_), (long long)t.adr[k],
+                (long long)nDofs_);
+      return FE_INVALID_ARG;
+    }
   if((t.elemType == ELEM_P2 && nloc_ != 6) || (t.elemType == ELEM_TAYLOR_HOOD && nloc_ != 15) ||
      (t.elemType != ELEM_P2 && t.elemType != ELEM_TAYLOR_HOOD)) {
     set_error("element type %d with %d local DOFs is not supported", t.elemType, nloc_);
@@ -657,10 +665,16 @@ int SystemCUDA::l2Error(int field, const double *hostExact, double *err)
 int SystemCUDA::validateColoring() const
 {
   const int64_t nE = (int64_t)adrHost_.size() / std::max(nloc_, 1);
-  if((int64_t)col_.elements.size() != nE || (int64_t)col_.offsets.size() != col_.nColors + 1) {
+  if((int64_t)col_.elements.size() != nE || (int64_t)col_.offsets.size() != col_.nColors + 1 ||
+     col_.offsets.front() != 0 || col_.offsets.back() != nE) {
     set_error("coloring does not list every element");
     return FE_BAD_COLORING;
   }
+  for(int c = 0; c < col_.nColors; ++c)
+    if(col_.offsets[c + 1] < col_.offsets[c]) {
+      set_error("color offsets decrease at color %d", c);
+      return FE_BAD_COLORING;
+    }
   std::vector<int32_t> stamp(nDofs_, -1);
   std::vector<uint8_t> seen(nE, 0);
   for(int c = 0; c < col_.nColors; ++c)
@@ -1242,12 +1256,18 @@ int newton_solve(SystemCUDA &sys, const NewtonOptions &o, NewtonStats &st)
   double normResidual = 0, normCorrection = 0, normAxb = 0, previous = 1e22;
   const double baseRtol = sys.krylov().opt.rtol;
   while(true) {
-    if(!o.stationary) FE_TRY(sys.computeSolDot());
-    // As feLinearSystemMklPardiso::setToZero (:967-971): a reused Jacobian
-    // (and its preconditioner) is kept.
-    if(recompute) FE_TRY(sys.setToZero());
-    else FE_TRY(sys.setResidualToZero());
-    FE_TRY(sys.assembleResiduals());
+    if(iter == 0 && o.residualReady) {
+      // The caller assembled u-dot and R(u) for this u (a time step's guess
+      // judged by its residual): only the Jacobian is cleared.
+      if(recompute) FE_TRY(sys.setMatrixToZero());
+    } else {
+      if(!o.stationary) FE_TRY(sys.computeSolDot());
+      // As feLinearSystemMklPardiso::setToZero (:967-971): a reused Jacobian
+      // (and its preconditioner) is kept.
+      if(recompute) FE_TRY(sys.setToZero());
+      else FE_TRY(sys.setResidualToZero());
+      FE_TRY(sys.assembleResiduals());
+    }
     FE_TRY(sys.getRHSMaxNorm(&normResidual));
     if(iter == 0) st.residual0 = normResidual;
     st.residual = normResidual;
@@ -1281,6 +1301,11 @@ int newton_solve(SystemCUDA &sys, const NewtonOptions &o, NewtonStats &st)
     st.krylovIterations += nIt;
     if(s != FE_OK && s != FE_NOT_CONVERGED) { st.status = s; return s; }
     if(s == FE_NOT_CONVERGED && o.linearRtolMin <= 0) { st.status = s; return s; }
+    if(!std::isfinite(normCorrection)) {
+      set_error("non-finite Newton correction");
+      st.status = FE_NONFINITE;
+      return FE_NONFINITE;
+    }
     if(normResidual > o.tolDivergence) {
       set_error("residual norm %g above divergence tolerance %g", normResidual, o.tolDivergence);
       st.status = FE_NOT_CONVERGED;

@@ -213,6 +213,7 @@ struct NewtonOptions {
   double relResidual = 0.0;       // extra stop: ||R||inf <= relResidual * ||R0||inf (0: off)
   double linearRtolMin = 0.0;     // >0: adaptive linear tolerance max(min, 0.1*||R||/||R0||)
   double residualScale = 0.0;     // >0: replaces ||R0||inf in the two relative tests above
+  int residualReady = 0;          // 1: u-dot and the residual of the current u are already assembled
 };
 
 struct NewtonStats {

@@ -47,13 +47,13 @@ __global__ void k_sigma(int64_t nNodes, int64_t nInc, const int32_t *__restrict_
   float su = 0.f, sp = 0.f;
   for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nNodes; k += (int64_t)gridDim.x * blockDim.x) {
     const int32_t u = nd[4 * k], v = nd[4 * k + 1], p = nd[4 * k + 2];
-    if(u < nInc) su = fmaxf(su, (float)fabs(h1[u] - h2[u]));
-    if(v < nInc) su = fmaxf(su, (float)fabs(h1[v] - h2[v]));
-    if(p == nd[4 * k + 3] && p < nInc) sp = fmaxf(sp, (float)fabs(h1[p] - h2[p]));
+    if(u < nInc) su = nan_maxf(su, (float)fabs(h1[u] - h2[u]));
+    if(v < nInc) su = nan_maxf(su, (float)fabs(h1[v] - h2[v]));
+    if(p == nd[4 * k + 3] && p < nInc) sp = nan_maxf(sp, (float)fabs(h1[p] - h2[p]));
   }
   for(int o = 16; o > 0; o >>= 1) {
-    su = fmaxf(su, __shfl_xor_sync(0xffffffffu, su, o));
-    sp = fmaxf(sp, __shfl_xor_sync(0xffffffffu, sp, o));
+    su = nan_maxf(su, __shfl_xor_sync(0xffffffffu, su, o));
+    sp = nan_maxf(sp, __shfl_xor_sync(0xffffffffu, sp, o));
   }
   if((threadIdx.x & 31) == 0) {
     atomic_max_pos(sig, su);
@@ -292,13 +292,14 @@ int Transient::residualNorm(double *norm)
   return sys_->getRHSMaxNorm(norm);
 }
 
-int Transient::newton(double scale, NewtonStats &ns)
+int Transient::newton(double scale, NewtonStats &ns, bool residualReady)
 {
   NewtonOptions n = no_;
   n.residualScale = scale;
-  const int s = newton_solve(*sys_, n, ns);
-  if(s != FE_OK && s != FE_NOT_CONVERGED) return s;
-  return FE_OK;
+  n.residualReady = residualReady ? 1 : 0;
+  // A step whose Newton solve did not converge is reported to the caller
+  // (the reference exits there, src/feNonLinearSolver.cpp:174-180).
+  return newton_solve(*sys_, n, ns);
 }
 
 // Rotation of the history and the step's time-level set-up (rotate,
@@ -396,53 +397,49 @@ int Transient::step(StepStats &st)
        ::feng::count_launch());
       CKT(cudaGetLastError());
     }
+    bool residualReady = false;
     if(learn && trained_ > 0 && st.step >= o_.useFrom) {
-      // The learned correction is tried at full, half and quarter length
-      // (each candidate judged by the FP64 residual); the extrapolation is
-      // kept when no candidate beats it.
+      // One learned candidate (the extrapolation plus the network's
+      // correction), judged against the extrapolation by the FP64 residual;
+      // the extrapolation is kept when the candidate does not beat it.  The
+      // candidate's residual is evaluated last, so when it wins that
+      // residual is Newton's first one.  A non-finite candidate residual
+      // never wins (the comparison is false for NaN).
       FE_TRY(mlp_.forward(X_, nNodes_, Y_));
-      double re = 0., best = 0.;
+      double re = 0., rm = 0.;
       CKT(cudaMemcpyAsync(sys_->dU(), ue_, bytes, cudaMemcpyDeviceToDevice, s));
       FE_TRY(residualNorm(&re));
       st.residualExtrap = re;
-      best = re;
-      float bestScale = 0.f;
-      for(float scale : {1.f, 0.5f, 0.25f}) {
-        CKT(cudaMemcpyAsync(um_, ue_, bytes, cudaMemcpyDeviceToDevice, s));
-        (k_apply<<<grid_of(nNodes_), 256, 0, s>>>(nNodes_, nInc, nodeDof_, Y_, sig_, scale, ue_, um_),
-         ::feng::count_launch());
-        CKT(cudaGetLastError());
-        double rm = 0.;
-        CKT(cudaMemcpyAsync(sys_->dU(), um_, bytes, cudaMemcpyDeviceToDevice, s));
-        FE_TRY(residualNorm(&rm));
-        if(rm < best) {
-          best = rm;
-          bestScale = scale;
-        }
-      }
       CKT(cudaMemcpyAsync(um_, ue_, bytes, cudaMemcpyDeviceToDevice, s));
-      if(bestScale > 0.f) {
-        (k_apply<<<grid_of(nNodes_), 256, 0, s>>>(nNodes_, nInc, nodeDof_, Y_, sig_, bestScale, ue_, um_),
-         ::feng::count_launch());
-        CKT(cudaGetLastError());
-        used = GUESS_LEARNED;
-      }
+      (k_apply<<<grid_of(nNodes_), 256, 0, s>>>(nNodes_, nInc, nodeDof_, Y_, sig_, 1.f, ue_, um_),
+       ::feng::count_launch());
+      CKT(cudaGetLastError());
       CKT(cudaMemcpyAsync(sys_->dU(), um_, bytes, cudaMemcpyDeviceToDevice, s));
+      const int r = residualNorm(&rm);
+      if(r != FE_OK && r != FE_NONFINITE) return r;
+      if(r == FE_OK && rm < re) {
+        used = GUESS_LEARNED;
+        residualReady = true;
+      } else {
+        CKT(cudaMemcpyAsync(sys_->dU(), ue_, bytes, cudaMemcpyDeviceToDevice, s));
+      }
     } else if(canExtrap) {
       CKT(cudaMemcpyAsync(sys_->dU(), ue_, bytes, cudaMemcpyDeviceToDevice, s));
     }
     st.guessUsed = used;
     CKT(cudaEventRecord(e1_, s));
     NewtonStats ns;
-    FE_TRY(newton(rref, ns));
+    const int ns_status = newton(rref, ns, residualReady);
+    if(ns_status != FE_OK && ns_status != FE_NOT_CONVERGED) return ns_status;
     st.newtonIterations = ns.iterations;
     st.krylovIterations = ns.krylovIterations;
     st.residualGuess = ns.residual0;
     if(used == GUESS_EXTRAPOLATE && st.residualExtrap == 0.) st.residualExtrap = ns.residual0;
     st.residual = ns.residual;
     st.status = ns.status;
-    // Online training on the correction this step revealed.
-    if(learn && st.step >= o_.trainFrom && o_.trainIters > 0) {
+    // Online training on the correction this step revealed (a step that
+    // did not converge reveals none).
+    if(learn && ns_status == FE_OK && st.step >= o_.trainFrom && o_.trainIters > 0) {
       CKT(cudaEventRecord(e2_, s));
       (k_targets<<<grid_of(nNodes_), 256, 0, s>>>(nNodes_, nInc, nodeDof_, sys_->dU(), ue_, sig_, T_, M_),
        ::feng::count_launch());
@@ -472,7 +469,9 @@ int Transient::step(StepStats &st)
   st.stepMs = ms;
   st.guessMs = gm;
   ++steps_;
-  return FE_OK;
+  // A step whose Newton solve did not converge is reported (the reference
+  // exits there, src/feNonLinearSolver.cpp:174-180); its statistics are kept.
+  return st.status;
 }
 
 }  // namespace feng

@@ -23,6 +23,7 @@
 
 #include <cstdint>
 
+#include "fe_common.h"
 #include "fe_mlp.h"
 #include "fe_system.h"
 
@@ -62,6 +63,21 @@ class Transient {
   int step(StepStats &st);
   int64_t nodes() const { return nNodes_; }
   int stepsDone() const { return steps_; }
+  // The learned guess's network parameters (MLPDims::P floats, host): a
+  // network saved from an earlier run warm-starts this one (it counts as
+  // trained, so it may be used from use_from on).
+  int getNetwork(float *params) const
+  {
+    if(o_.guess != GUESS_LEARNED) { set_error("the integrator has no network (guess is not learned)"); return FE_INVALID_ARG; }
+    return mlp_.getParams(params);
+  }
+  int setNetwork(const float *params)
+  {
+    if(o_.guess != GUESS_LEARNED) { set_error("the integrator has no network (guess is not learned)"); return FE_INVALID_ARG; }
+    const int s = mlp_.setParams(params);
+    if(s == 0 && trained_ == 0) trained_ = 1;
+    return s;
+  }
 
  private:
   SystemCUDA *sys_ = nullptr;
@@ -84,7 +100,7 @@ class Transient {
   // step start, end of the guess, start and end of training
   cudaEvent_t e0_ = nullptr, e1_ = nullptr, e2_ = nullptr, e3_ = nullptr;
   int residualNorm(double *norm);
-  int newton(double scale, NewtonStats &ns);
+  int newton(double scale, NewtonStats &ns, bool residualReady = false);
   int bdf1Start(StepStats &st);
 };
 

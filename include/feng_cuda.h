@@ -440,6 +440,12 @@ int fe_cuda_transient_create(fe_cuda_system *s, const fe_transient_options *o,
                              const fe_newton_options *newton, fe_transient **out);
 /* Advances nsteps steps; stats [nsteps] may be NULL. */
 int fe_cuda_transient_steps(fe_transient *t, int nsteps, fe_step_stats *stats);
+/* The learned guess's network (fe_mlp_sizes' nparams floats, the packing of
+ * fe_mlp_set_params): saved after a run, restored to warm-start another (a
+ * restored network may be used from use_from on; no counterpart in the
+ * reference). */
+int fe_cuda_transient_get_network(const fe_transient *t, float *params);
+int fe_cuda_transient_set_network(fe_transient *t, const float *params);
 void fe_cuda_transient_destroy(fe_transient *t);
 
 /* ---- the learned-guess MLP alone, through host buffers (tests and tools; same
@@ -468,8 +474,10 @@ int fe_mlp_train_step(fe_mlp *m, const float *x, const float *t, const float *ma
  * FE_NOALLOC_MAX_N; larger n is rejected with FE_CUDA_INVALID_ARG.  `stream`
  * is a cudaStream_t (NULL: the legacy default stream); the call waits for it
  * and writes the result to host memory.  The first call on each device looks
- * up the scratch's device address (make it before any stream capture).  All
- * calls share the one scratch array: calls that overlap on the GPU race. */
+ * up the scratch's device address (make it before any stream capture); that
+ * address is kept for the life of the process, so the call must not be used
+ * on a device after cudaDeviceReset.  All calls share the one scratch array:
+ * calls that overlap on the GPU race.  A NaN in x gives a NaN result. */
 #define FE_NOALLOC_MAX_N 4194304
 int fe_cuda_max_norm_noalloc(const double *x, int64_t n, void *stream, double *result);
 

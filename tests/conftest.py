@@ -23,6 +23,21 @@ def built_library():
     return build.LIB
 
 
+def reference_root():
+    """The reference checkout (CPU tests that read it skip without it):
+    FENG_REFERENCE, else the location the build recorded when it compiled
+    the reference library into oracle/_ref; None when neither exists."""
+    import os
+    env = os.environ.get("FENG_REFERENCE")
+    if env:
+        return Path(env) if Path(env).exists() else None
+    rec = ROOT / "oracle" / "_ref" / "REFERENCE"
+    if rec.exists():
+        p = Path(rec.read_text().strip())
+        return p if p.exists() else None
+    return None
+
+
 def load_golden(name):
     with np.load(GOLDEN / f"{name}.npz") as z:
         return {k: z[k] for k in z.files}

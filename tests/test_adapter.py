@@ -7,9 +7,9 @@ from pathlib import Path
 
 import pytest
 
-from conftest import ROOT
+from conftest import ROOT, reference_root
 
-REF = Path(os.environ.get("FENG_REFERENCE", "/root/reference"))
+REF = reference_root() or Path("/nonexistent")
 LIBREF = ROOT / "oracle" / "_ref" / "libfeNG.a"
 
 

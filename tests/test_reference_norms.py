@@ -55,9 +55,11 @@ def test_fixture_meshes_read_back_from_the_reference_files():
     """Where the reference checkout exists: the fixture arrays are what this
     package's msh reader makes of the reference's mesh files."""
     import feng_gb300 as fe
-    ref = Path(os.environ.get("FENG_REFERENCE", "/root/reference")) / "data"
-    if not ref.exists():
+    from conftest import reference_root
+    root = reference_root()
+    if root is None:
         pytest.skip("reference checkout absent")
+    ref = root / "data"
     g = reference_l2()
     for key, sub in (("diff", "mmsMeshes/square"), ("ns", "square")):
         for i in range(1, 5):

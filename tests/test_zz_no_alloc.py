@@ -41,11 +41,17 @@ def test_noalloc_max_norm_matches_regular_entry_point():
     # The caller owns the input: a device copy of the residual made by torch.
     x = torch.from_numpy(rhs).to("cuda:0")
     torch.cuda.synchronize()
+    # A first call loads the kernel's module (and with it the static scratch)
+    # if nothing had; after it, the device's free memory must not move.
+    out = C.c_double(-1.0)
+    assert lib.fe_cuda_max_norm_noalloc(C.c_void_p(x.data_ptr()), x.numel(), None, C.byref(out)) == 0
+    free_before = torch.cuda.mem_get_info(0)[0]
     for _ in range(2):                        # two calls in a row share the static scratch
         out = C.c_double(-1.0)
         s = lib.fe_cuda_max_norm_noalloc(C.c_void_p(x.data_ptr()), x.numel(), None, C.byref(out))
         assert s == 0, lib.fe_cuda_last_error()
         assert abs(out.value - expected) <= TOL * expected
+    assert torch.cuda.mem_get_info(0)[0] == free_before, "the entry point allocated device memory"
 
     # Sizes beyond the static scratch are rejected before any work.
     out = C.c_double(-1.0)
