@@ -304,7 +304,16 @@ struct fo_precond {
   double *pscale;    /* viscosity / lumped mass for pressure rows */
   double *tmp;
   const double *A;   /* current matrix values (for the G z_p product) */
+  fo_spmg *spmg;     /* kinds 4, 5 */
 };
+
+fo_precond *fo_precond_from_spmg(fo_spmg *S)
+{
+  fo_precond *pc = calloc(1, sizeof(fo_precond));
+  pc->kind = 4;
+  pc->spmg = S;
+  return pc;
+}
 
 fo_precond *fo_precond_create(int kind, int64_t n, const int64_t *ia, const int32_t *ja,
                               const int32_t *block_of_row, const int32_t *is_pressure,
@@ -374,6 +383,7 @@ fo_precond *fo_precond_create(int kind, int64_t n, const int64_t *ia, const int3
 int fo_precond_factor(fo_precond *pc, const double *a)
 {
   pc->A = a;
+  if(pc->kind == 4) return fo_spmg_factor(pc->spmg, a);
   if(pc->kind == 2) {
     for(int64_t i = 0; i < pc->n; ++i) {
       double d = 0.;
@@ -436,7 +446,9 @@ static void ilu_apply(fo_precond *pc, const double *r, double *z)
 void fo_precond_apply(fo_precond *pc, const double *r, double *z)
 {
   const int64_t n = pc->n;
-  if(pc->kind == 0) {
+  if(pc->kind == 4) {
+    fo_spmg_apply(pc->spmg, r, z);
+  } else if(pc->kind == 0) {
     memcpy(z, r, sizeof(double) * n);
   } else if(pc->kind == 2) {
     for(int64_t i = 0; i < n; ++i) z[i] = r[i] * pc->dinv[i];
@@ -459,7 +471,7 @@ void fo_precond_apply(fo_precond *pc, const double *r, double *z)
 
 void fo_precond_destroy(fo_precond *pc)
 {
-  if(!pc) return;
+  if(!pc) return;  /* a kind-4 object does not own its multigrid (fo_spmg_destroy) */
   free(pc->bstart); free(pc->perm); free(pc->lia); free(pc->lja); free(pc->src);
   free(pc->ldiag); free(pc->f); free(pc->dinv); free(pc->pscale); free(pc->tmp);
   free(pc);
@@ -468,6 +480,8 @@ void fo_precond_destroy(fo_precond *pc)
 /* ---------------------------------------------------------------------------
  * Krylov
  * ------------------------------------------------------------------------- */
+#define FO_MAX_RESTART 200
+
 static double dot(int64_t n, const double *x, const double *y, int nt)
 {
   double s = 0.;
@@ -497,12 +511,14 @@ int fo_krylov_solve(int method, int m, int max_iter, double rtol, double atol, i
     while(it < max_iter && sqrt(rr) > tol) {
       fo_spmv(n, ia, ja, a, p, q, nt);
       const double alpha = rz / dot(n, p, q, nt);
+#pragma omp parallel for num_threads(nt) schedule(static)
       for(int64_t i = 0; i < n; ++i) { x[i] += alpha * p[i]; r[i] -= alpha * q[i]; }
       rr = dot(n, r, r, nt);
       fo_precond_apply(pc, r, z);
       const double rzn = dot(n, r, z, nt);
       const double beta = rzn / rz;
       rz = rzn;
+#pragma omp parallel for num_threads(nt) schedule(static)
       for(int64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
       ++it;
     }
@@ -513,6 +529,7 @@ int fo_krylov_solve(int method, int m, int max_iter, double rtol, double atol, i
     return st->converged ? 0 : -5;
   }
   /* FGMRES(m), right preconditioning, CGS2 Arnoldi */
+  if(m < 1 || m > FO_MAX_RESTART) return -3;
   double *V = malloc(sizeof(double) * n * (m + 1)), *Z = malloc(sizeof(double) * n * m);
   double *w = malloc(sizeof(double) * n);
   double *H = calloc((size_t)(m + 1) * m, sizeof(double));
@@ -523,10 +540,12 @@ int fo_krylov_solve(int method, int m, int max_iter, double rtol, double atol, i
   double est = bn;
   while(total < max_iter) {
     fo_spmv(n, ia, ja, a, x, w, nt);
+#pragma omp parallel for num_threads(nt) schedule(static)
     for(int64_t i = 0; i < n; ++i) w[i] = b[i] - w[i];
     const double beta = sqrt(dot(n, w, w, nt));
     est = beta;
     if(beta <= tol) break;
+#pragma omp parallel for num_threads(nt) schedule(static)
     for(int64_t i = 0; i < n; ++i) V[i] = w[i] / beta;
     for(int i = 0; i <= m; ++i) g[i] = 0.;
     g[0] = beta;
@@ -536,15 +555,29 @@ int fo_krylov_solve(int method, int m, int max_iter, double rtol, double atol, i
       fo_spmv(n, ia, ja, a, Z + (int64_t)j * n, w, nt);
       for(int c = 0; c <= j; ++c) H[c * m + j] = 0.;
       for(int pass = 0; pass < 2; ++pass) {
-        for(int c = 0; c <= j; ++c) h[c] = dot(n, V + (int64_t)c * n, w, nt);
-        for(int c = 0; c <= j; ++c) {
-          H[c * m + j] += h[c];
-          const double *vc = V + (int64_t)c * n;
-          for(int64_t i = 0; i < n; ++i) w[i] -= h[c] * vc[i];
+        /* classical Gram-Schmidt: all products, then one update pass */
+        for(int c = 0; c <= j; ++c) h[c] = 0.;
+#pragma omp parallel num_threads(nt)
+        {
+          double hl[FO_MAX_RESTART + 1];
+          for(int c = 0; c <= j; ++c) hl[c] = 0.;
+#pragma omp for schedule(static)
+          for(int64_t i = 0; i < n; ++i)
+            for(int c = 0; c <= j; ++c) hl[c] += V[(int64_t)c * n + i] * w[i];
+#pragma omp critical
+          for(int c = 0; c <= j; ++c) h[c] += hl[c];
+        }
+        for(int c = 0; c <= j; ++c) H[c * m + j] += h[c];
+#pragma omp parallel for num_threads(nt) schedule(static)
+        for(int64_t i = 0; i < n; ++i) {
+          double t = w[i];
+          for(int c = 0; c <= j; ++c) t -= h[c] * V[(int64_t)c * n + i];
+          w[i] = t;
         }
       }
       const double hn = sqrt(dot(n, w, w, nt));
       H[(j + 1) * m + j] = hn;
+#pragma omp parallel for num_threads(nt) schedule(static)
       for(int64_t i = 0; i < n; ++i) V[(int64_t)(j + 1) * n + i] = hn > 0 ? w[i] / hn : 0.;
       for(int c = 0; c < j; ++c) {
         const double t = cs[c] * H[c * m + j] + sn[c] * H[(c + 1) * m + j];
@@ -568,13 +601,16 @@ int fo_krylov_solve(int method, int m, int max_iter, double rtol, double atol, i
       for(int c = i + 1; c < k; ++c) s -= H[i * m + c] * y[c];
       y[i] = s / H[i * m + i];
     }
-    for(int c = 0; c < k; ++c) {
-      const double *zc = Z + (int64_t)c * n;
-      for(int64_t i = 0; i < n; ++i) x[i] += y[c] * zc[i];
+#pragma omp parallel for num_threads(nt) schedule(static)
+    for(int64_t i = 0; i < n; ++i) {
+      double t = x[i];
+      for(int c = 0; c < k; ++c) t += y[c] * Z[(int64_t)c * n + i];
+      x[i] = t;
     }
     if(est <= tol) break;
   }
   fo_spmv(n, ia, ja, a, x, w, nt);
+#pragma omp parallel for num_threads(nt) schedule(static)
   for(int64_t i = 0; i < n; ++i) w[i] = b[i] - w[i];
   st->rnorm = sqrt(dot(n, w, w, nt));
   st->iterations = total;
@@ -615,4 +651,55 @@ void fo_periodicity(int64_t n, const int64_t *ia, const int32_t *ja, double *val
     for(int64_t k = ia[s]; k < ia[s + 1]; ++k) values[k] = ja[k] == s ? 1. : (ja[k] == m ? -1. : 0.);
     rhs[s] = 0.;
   }
+}
+
+/* ---- element coloring: feCncGeo::colorElements algorithm 1
+ * (src/feCncGeo.cpp:752-790).  Rounds over the uncolored elements in index
+ * order: every uncolored element that is not yet blocked blocks its
+ * uncolored vertex-neighbours; the elements left unblocked take the round's
+ * color, the blocked ones are released for the next round. */
+int fo_color_elements(const int32_t *ev, int nvpe, int64_t ne, int64_t nv, int32_t *color)
+{
+  int64_t *vs = calloc(nv + 1, sizeof(int64_t));
+  for(int64_t i = 0; i < ne * nvpe; ++i) {
+    if(ev[i] < 0 || ev[i] >= nv) { free(vs); return -3; }
+    vs[ev[i] + 1]++;
+  }
+  for(int64_t v = 0; v < nv; ++v) vs[v + 1] += vs[v];
+  int32_t *ve = malloc(sizeof(int32_t) * (ne * nvpe > 0 ? ne * nvpe : 1));
+  int64_t *pos = malloc(sizeof(int64_t) * (nv > 0 ? nv : 1));
+  memcpy(pos, vs, sizeof(int64_t) * nv);
+  for(int64_t t = 0; t < ne; ++t)
+    for(int k = 0; k < nvpe; ++k) ve[pos[ev[nvpe * t + k]]++] = (int32_t)t;
+  free(pos);
+  unsigned char *blk = calloc(ne > 0 ? ne : 1, 1);
+  for(int64_t t = 0; t < ne; ++t) color[t] = -1;
+  int64_t left = ne;
+  int nc = 0;
+  while(left > 0) {
+    if(nc >= 64) { nc = -1; break; }
+    for(int64_t t = 0; t < ne; ++t) {
+      if(color[t] >= 0 || blk[t]) continue;
+      for(int k = 0; k < nvpe; ++k) {
+        const int32_t v = ev[nvpe * t + k];
+        for(int64_t p = vs[v]; p < vs[v + 1]; ++p)
+          if(ve[p] != t && color[ve[p]] < 0) blk[ve[p]] = 1;
+      }
+    }
+    for(int64_t t = 0; t < ne; ++t) {
+      if(color[t] >= 0) continue;
+      if(blk[t]) blk[t] = 0;
+      else { color[t] = nc; --left; }
+    }
+    ++nc;
+  }
+  free(vs); free(ve); free(blk);
+  return nc;
+}
+
+/* Thread count of the OpenMP regions that take none explicitly (the
+ * multigrid of fe_oracle_mg.c). */
+void fo_set_threads(int n)
+{
+  if(n > 0) omp_set_num_threads(n);
 }

@@ -73,6 +73,39 @@ int fo_precond_factor(fo_precond *pc, const double *values);
 void fo_precond_apply(fo_precond *pc, const double *r, double *z);
 void fo_precond_destroy(fo_precond *pc);
 
+/* Smoothed-aggregation multigrid and the block-triangular saddle-point
+ * preconditioner (fe_oracle_mg.c).  kind 4: Taylor-Hood (nn velocity nodes
+ * with rows dofx/dofy, np pressure rows prows with lumped masses pmass; K the
+ * scalar P2 stiffness on the nodes; sigma, divu the stress and divergence
+ * coefficients); kind 5: scalar (nodes = unknown rows dofx, K on them).
+ * The index arrays of the system (ia, ja) must outlive the object. */
+typedef struct fo_mg fo_mg;
+fo_mg *fo_mg_create(int64_t n, const int64_t *ia, const int32_t *ja, const double *a, double theta,
+                    int64_t coarse_size);
+void fo_mg_vcycle(fo_mg *M, const double *b, double *x, int nv);
+int fo_mg_levels(const fo_mg *M);
+double fo_mg_diag_sum(const fo_mg *M);
+void fo_mg_destroy(fo_mg *M);
+typedef struct fo_spmg fo_spmg;
+fo_spmg *fo_spmg_create(int kind, int64_t n, const int64_t *ia, const int32_t *ja, int64_t nn,
+                        const int64_t *kia, const int32_t *kja, const double *ka, const int32_t *dofx,
+                        const int32_t *dofy, int64_t np, const int32_t *prows, const double *pmass,
+                        double sigma, double divu);
+int fo_spmg_factor(fo_spmg *S, const double *values);
+void fo_spmg_apply(fo_spmg *S, const double *r, double *z);
+void fo_spmg_destroy(fo_spmg *S);
+/* A preconditioner object that applies S (kinds 4 and 5; S stays owned by
+ * the caller). */
+fo_precond *fo_precond_from_spmg(fo_spmg *S);
+
+/* Greedy vertex-sharing coloring of elements given by nvpe vertices each
+ * (feCncGeo::colorElements algorithm 1, src/feCncGeo.cpp:752-790): writes
+ * the color of each element; returns the number of colors (< 0 on error). */
+int fo_color_elements(const int32_t *ev, int nvpe, int64_t ne, int64_t nv, int32_t *color);
+
+/* Threads of the OpenMP regions without an explicit count. */
+void fo_set_threads(int n);
+
 typedef struct fo_krylov_stats {
   int iterations;
   int converged;

@@ -40,7 +40,12 @@ class feLinearSystemRef : public feLinearSystem {
   std::vector<double> values, rhs, du;
   double lastAxb = 0;
   Eigen::SparseMatrix<double> A;
+  // Fill-reducing ordering of the direct solve: COLAMD (Eigen's default) or,
+  // with FE_HARNESS_ORDERING=amd, minimum degree on A + A^T (much less fill
+  // on large 2D meshes).  Both give the solution to rounding.
   Eigen::SparseLU<Eigen::SparseMatrix<double>> lu;
+  Eigen::SparseLU<Eigen::SparseMatrix<double>, Eigen::AMDOrdering<int>> luAmd;
+  bool useAmd = getenv("FE_HARNESS_ORDERING") && std::string(getenv("FE_HARNESS_ORDERING")) == "amd";
   bool factored = false;
 
   feLinearSystemRef(std::vector<feBilinearForm *> forms, const feMetaNumber *numbering)
@@ -157,12 +162,17 @@ class feLinearSystemRef : public feLinearSystem {
       A = Eigen::SparseMatrix<double>(nInc, nInc);
       A.setFromTriplets(trip.begin(), trip.end());
       A.makeCompressed();
-      lu.compute(A);
-      if(lu.info() != Eigen::Success) return false;
+      if(useAmd) {
+        luAmd.compute(A);
+        if(luAmd.info() != Eigen::Success) return false;
+      } else {
+        lu.compute(A);
+        if(lu.info() != Eigen::Success) return false;
+      }
       factored = true;
     }
     Eigen::Map<Eigen::VectorXd> b(rhs.data(), nInc);
-    Eigen::VectorXd x = lu.solve(b);
+    Eigen::VectorXd x = useAmd ? Eigen::VectorXd(luAmd.solve(b)) : Eigen::VectorXd(lu.solve(b));
     for(feInt i = 0; i < nInc; ++i) du[i] = x[i];
     double mdu = 0, mr = 0, axb = 0;
     Eigen::VectorXd res = A * x - b;
@@ -421,6 +431,30 @@ int main(int argc, char **argv)
                                  0.0, nSteps * g_dt, nSteps));
     feCheck(ti->makeSteps(nSteps));
     std::vector<double> traj = sol.getSolution();
+    {
+      // Transient assembly state: the last step's BDF coefficient c0 and
+      // time derivative, unknowns replaced by U(-1,1) (std::mt19937_64 with
+      // the seed): the residual and the Jacobian, TransientVectorMass
+      // included, at that state.
+      std::vector<double> ut = traj;
+      std::mt19937_64 rng(seed);
+      std::uniform_real_distribution<double> U(-1.0, 1.0);
+      for(feInt i = 0; i < nInc; ++i) ut[i] = U(rng);
+      sol.getSolution() = ut;
+      solAtTimeN = ut;
+      const std::vector<double> udt = sol.getSolutionDot();
+      sys->setMatrixToZero();
+      sys->setResidualToZero();
+      sys->assembleResiduals(&sol);
+      sys->assembleMatrices(&sol, false);
+      write_raw(out + "/u0.f64", ut);
+      write_raw(out + "/udot0.f64", udt);
+      write_raw(out + "/values0.f64", sys->values);
+      write_raw(out + "/rhs0.f64", sys->rhs);
+      std::vector<double> c0t = {sol.getC0(), sol.getCurrentTime()};
+      write_raw(out + "/c0t.f64", c0t);
+      sol.getSolution() = traj;
+    }
     feCheck(write_vtk(out, numbering, sol, mesh, spaces));
     write_raw(out + "/ia.i64", ia);
     write_raw(out + "/ja.i64", ja);
@@ -448,9 +482,20 @@ int main(int argc, char **argv)
   feNLSolverOptions NL{1e-10, 1e-12, 1e4, 30, 3, 1e-1};
   feCheck(createTimeIntegrator(ti, timeIntegratorScheme::STATIONARY, NL, sys, &sol, &mesh, norms, {nullptr, 1, ""}));
   std::vector<double> u0 = sol.getSolution();  // essential DOFs initialised by the integrator
-  std::mt19937_64 rng(seed);
-  std::uniform_real_distribution<double> U(-1.0, 1.0);
-  for(feInt i = 0; i < nInc; ++i) u0[i] = U(rng);
+  if(getenv("FE_HARNESS_U0")) {
+    // Unknowns of the assembly state from a raw file of nInc doubles (large
+    // cases: the fixture script draws them from a seed the tests can redraw).
+    FILE *fu = fopen(getenv("FE_HARNESS_U0"), "rb");
+    if(!fu || fread(u0.data(), sizeof(double), nInc, fu) != (size_t)nInc) {
+      fprintf(stderr, "cannot read %ld doubles from %s\n", (long)nInc, getenv("FE_HARNESS_U0"));
+      return 1;
+    }
+    fclose(fu);
+  } else {
+    std::mt19937_64 rng(seed);
+    std::uniform_real_distribution<double> U(-1.0, 1.0);
+    for(feInt i = 0; i < nInc; ++i) u0[i] = U(rng);
+  }
   std::vector<double> ubc = sol.getSolution();
   sol.getSolution() = u0;
   solAtTimeN = sol.getSolution();
@@ -459,6 +504,23 @@ int main(int argc, char **argv)
   sys->assembleMatrices(&sol, false);
   std::vector<double> values0 = sys->values, rhs0 = sys->rhs;
 
+  if(getenv("FE_HARNESS_NOSOLVE")) {
+    // Assembly state only (large meshes whose direct solve takes long).
+    write_raw(out + "/ia.i64", ia);
+    write_raw(out + "/ja.i64", ja);
+    write_raw(out + "/adr.i64", adr);
+    write_raw(out + "/color_offsets.i64", colOff);
+    write_raw(out + "/color_elements.i32", colEl);
+    write_raw(out + "/u0.f64", u0);
+    write_raw(out + "/values0.f64", values0);
+    write_raw(out + "/rhs0.f64", rhs0);
+    FILE *f = fopen((out + "/meta.txt").c_str(), "w");
+    fprintf(f, "problem %s\nnInc %ld\nnDofs %ld\nnnz %zu\nnElm %d\nnColors %d\nnloc %zu\nquad_degree %d\nre %.17g\nseed %lu\n",
+            problem.c_str(), (long)nInc, (long)nDofs, ja.size(), nElm, cnc->getNbColor(),
+            adr.size() / nElm, degQ, g_re, seed);
+    fclose(f);
+    return 0;
+  }
   // Converged solution from the BC-initialised zero state.
   for(feInt i = 0; i < nInc; ++i) ubc[i] = 0.;
   sol.getSolution() = ubc;
