@@ -546,6 +546,8 @@ def main():
             "newton_step_s": t_forc / args.steps,
             "newton_iterations": round(statistics.mean(s["iterations"] for s in st_forc), 2),
             "krylov_iterations": round(statistics.mean(s["krylov_iterations"] for s in st_forc), 1),
+            "converged": all(s["return"] == 0 for s in st_forc),
+            "final_rel_residual": max(s["residual"] / s["residual0"] for s in st_forc),
             "note": "FP64 everywhere, linear tolerance max(1e-6, min(1e-2, 0.1 ||R||/||R0||)) as the mixed arm"},
         "speedup_mixed_vs_fp64": plain_s / value,
         "speedup_split": {"inexact_newton_forcing": plain_s / (t_forc / args.steps),

@@ -39,6 +39,7 @@ SOURCE, DIFFUSION, VECTOR_SOURCE, TRANSIENT_VECTOR_MASS = 1, 2, 3, 4
 MIXED_DIVERGENCE, VECTOR_CONVECTIVE_ACCELERATION, DIV_NEWTONIAN_STRESS = 5, 6, 7
 # Device source registry (FE_SRC_*)
 SRC_NONE, SRC_SIN_SIN, SRC_NS_MMS_POLY, SRC_CONST_VEC, SRC_SIN_BODY = 0, 1, 2, 3, 4
+SRC_SIN3, SRC_SIN3_BODY = 5, 6   # tetrahedra
 ELEM_P2, ELEM_TAYLOR_HOOD, ELEM_TET_P2, ELEM_TET_TAYLOR_HOOD = 1, 2, 3, 4
 
 
@@ -407,7 +408,10 @@ class feLinearSystemCUDA:
     (src/feLinearSystem.h:43-169)."""
 
     def __init__(self, forms: Sequence[feBilinearForm], numbering: feMetaNumber,
-                 options: LinearSolverOptions | None = None):
+                 options: LinearSolverOptions | None = None, rule=None):
+        """rule: optional quadrature rule rows (r, s, [t,] w) replacing the one
+        of the spaces' degree (e.g. the reference's tabulated values); it is
+        kept by the numbering's set-up for later systems too."""
         self.lib = _lib.load()
         self.forms = list(forms)
         self.numbering = numbering
@@ -419,6 +423,9 @@ class feLinearSystemCUDA:
         self.quad_degree = numbering.quad_degree
         rows = 0 if self.options.precond == "ilu0" else self.options.pc_block_rows
         self.setup = numbering.setup(rows)
+        if rule is not None:
+            r = np.ascontiguousarray(rule, np.float64)
+            check(self.lib.fe_setup_set_quadrature(self.setup._h, len(r), ptr(r)))
         fa = (_lib.FormDesc * len(self.forms))()
         for i, f in enumerate(self.forms):
             se = f.sysElm
@@ -571,10 +578,10 @@ class feLinearSystemCUDA:
         check(self.lib.fe_cuda_synchronize(self._h))
 
 
-def createLinearSystem(kind, forms, numbering, options: LinearSolverOptions | None = None):
+def createLinearSystem(kind, forms, numbering, options: LinearSolverOptions | None = None, rule=None):
     if kind != CUDA:
         raise ValueError("only the CUDA backend is provided")
-    return feLinearSystemCUDA(forms, numbering, options)
+    return feLinearSystemCUDA(forms, numbering, options, rule)
 
 
 class feSolution:
@@ -587,6 +594,7 @@ class feSolution:
         self.t = 0.0
         self.c0 = 0.0
         self.dof_x, self.dof_y, self.dof_field, self.dof_comp = system.dofInfo()
+        self.dof_z = system.setup.dofZ() if isinstance(system.numbering.mesh, Mesh3DP1) else None
 
     def initializeEssentialBC(self, t: float = 0.0):
         """Nodewise essential values (feSolution::initializeEssentialBC,
@@ -600,7 +608,8 @@ class feSolution:
                 continue
             sel = ess[self.dof_field[ess] == fi]
             for s in spaces:
-                vals = s.fct(self.dof_x[sel], self.dof_y[sel])
+                xyz = (self.dof_x[sel], self.dof_y[sel]) + (() if self.dof_z is None else (self.dof_z[sel],))
+                vals = s.fct(*xyz)
                 comp = self.dof_comp[sel]
                 out = np.empty(len(sel))
                 for c in range(len(vals)):

@@ -1,0 +1,461 @@
+// Element assembly on tetrahedra: scalar P2 (DIFFUSION + SOURCE, the
+// reference's feSysElm_Diffusion<3> and feSysElm_Source on feSpaceTetPn(2),
+// src/feSysElm.cpp:16-27, 520-589) and Taylor-Hood P2-P1 (the vector forms
+// of src/feVectorSysElm.cpp in three dimensions, which the reference
+// instantiates only in two).
+//
+// Colored kernels: one launch per element color; a block holds 32 elements
+// (lane = element) x 10 warps (warp = P2 function a).  Thread (e, a) forms
+// the element-matrix rows of the DOFs of function a (one scalar row, or the
+// three velocity component rows), and threads a < 4 the pressure row of P1
+// function a.  Entries go to the CSR values through the element-to-nonzero
+// map as L2 reductions (one contribution per entry and color: the sums of a
+// colored read-modify-write, in color order).
+//
+// Arithmetic: affine (P1) geometry, so grad phi = G^T dphi/d(r,s,t) with
+// G[r][k] = d r_r / d x_k constant per element and every quadrature sum of
+// the weak forms is a reference tensor (RefTensorsTet, built from the same
+// rule's nodes and weights) contracted with G, J and the element's DOF values:
+//   int dphi_a/dx_k dphi_b/dx_l = J sum_rs G[r][k] G[s][l] K[r][s][a][b]
+//   int phi_a phi_c dphi_b/dx_k = J sum_r  G[r][k] T[r][a][c][b]
+//   int psi_j dphi_a/dx_k       = J sum_r  G[r][k] D[r][j][a]
+//   int phi_a phi_b             = J M[a][b]
+// Source terms are summed over the rule's nodes (non-polynomial integrands).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "fe_common.h"
+#include "fe_device.h"
+#include "fe_mesh3d.h"
+#include "fe_setup.h"
+
+namespace feng {
+
+namespace {
+
+constexpr int EPB = 32;
+constexpr int TPB = 10;  // warps per block: one per P2 function
+constexpr double PI = 3.14159265358979323846;
+constexpr int NTEN = 900 + 3000 + 120 + 100;  // K, T, D, M
+
+// x-component (or scalar value) of the tetrahedral sources at a point.
+__device__ __forceinline__ double source_x(int kind, const double *p, double x, double y, double z)
+{
+  if(kind == SRC_SIN3 || kind == SRC_SIN3_BODY) return p[0] * sin(PI * x) * sin(PI * y) * sin(PI * z);
+  return 0.;
+}
+
+template <typename V>
+struct TetTensors {
+  const V *K, *T, *D, *M;
+  __device__ V k(int r, int s, int a, int b) const { return K[((r * 3 + s) * 10 + a) * 10 + b]; }
+  __device__ V t(int r, int a, int c, int b) const { return T[((r * 10 + a) * 10 + c) * 10 + b]; }
+  __device__ V d(int r, int j, int a) const { return D[(r * 4 + j) * 10 + a]; }
+  __device__ V m(int a, int b) const { return M[a * 10 + b]; }
+};
+
+template <typename V>
+__device__ TetTensors<V> load_tet_tensors(V *sh, const RefTensorsTet *g)
+{
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+  const double *src[4] = {&g->K[0][0][0][0], &g->T[0][0][0][0], &g->D[0][0][0], &g->M[0][0]};
+  const int len[4] = {900, 3000, 120, 100};
+  int off = 0;
+  for(int k = 0; k < 4; ++k) {
+    for(int i = tid; i < len[k]; i += nt) sh[off + i] = (V)src[k][i];
+    off += len[k];
+  }
+  return TetTensors<V>{sh, sh + 900, sh + 3900, sh + 4020};
+}
+
+// ---------------------------------------------------------------------------
+// Residual, FP64: scalar P2 and Taylor-Hood.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(EPB *TPB) k_residual_tet(DeviceMesh dm, FormCoeffs fc, const RefTensorsTet *__restrict__ gT,
+                                                           const double *__restrict__ u, const double *__restrict__ udot,
+                                                           int64_t nInc, double *__restrict__ rhs, int64_t begin,
+                                                           int64_t end)
+{
+  extern __shared__ __align__(16) double smem[];
+  const bool th = fc.elemType == 4;
+  const int nq = gT->nq;
+  double *sTen = smem;
+  double *sU = sTen + NTEN;           // [30][EPB] (scalar: [10][EPB])
+  double *sUd = sU + 30 * EPB;        // [30][EPB]
+  double *sG = sUd + 30 * EPB;        // [10][EPB]
+  double *sP = sG + 10 * EPB;         // [4][EPB]
+  double *sF = sP + 4 * EPB;          // [nq][EPB]
+  const int lane = threadIdx.x, a = threadIdx.y;
+  const int64_t p = begin + (int64_t)blockIdx.x * EPB + lane;
+  const bool live = p < end;
+  const int64_t nE = dm.nElm;
+  const TetTensors<double> Tt = load_tet_tensors(sTen, gT);
+  if(live) {
+    if(th) {
+      for(int m = 0; m < 3; ++m) {
+        const int32_t d = dm.adr[(int64_t)(3 * a + m) * nE + p];
+        sU[(3 * a + m) * EPB + lane] = u[d];
+        sUd[(3 * a + m) * EPB + lane] = (fc.hasMass && udot) ? udot[d] : 0.;
+      }
+      if(a < 4) sP[a * EPB + lane] = u[dm.adr[(int64_t)(30 + a) * nE + p]];
+    } else {
+      sU[a * EPB + lane] = u[dm.adr[(int64_t)a * nE + p]];
+    }
+    sG[a * EPB + lane] = dm.geo[(int64_t)a * nE + p];
+    if(fc.srcKind == SRC_SIN3 || fc.srcKind == SRC_SIN3_BODY) {
+      double X[4][3];
+      for(int v = 0; v < 4; ++v)
+        for(int k = 0; k < 3; ++k) X[v][k] = dm.xy[(int64_t)(3 * v + k) * nE + p];
+      for(int q = a; q < nq; q += TPB) {
+        const double r = gT->qr[q], s = gT->qs[q], t = gT->qt[q], l0 = 1. - r - s - t;
+        double x[3];
+        for(int k = 0; k < 3; ++k) x[k] = l0 * X[0][k] + r * X[1][k] + s * X[2][k] + t * X[3][k];
+        sF[q * EPB + lane] = source_x(fc.srcKind, fc.srcParam, x[0], x[1], x[2]);
+      }
+    }
+  }
+  __syncthreads();
+  if(!live) return;
+  double G[3][3];
+  for(int r = 0; r < 3; ++r)
+    for(int k = 0; k < 3; ++k) G[r][k] = sG[(3 * r + k) * EPB + lane];
+  const double J = sG[9 * EPB + lane];
+  // source integral of phi_a: sum_q w phi_a(q) f(q)
+  double srcA = 0.;
+  if(fc.srcKind == SRC_SIN3 || fc.srcKind == SRC_SIN3_BODY)
+    for(int q = 0; q < nq; ++q) srcA += gT->phi[q][a] * sF[q * EPB + lane] * gT->qw[q];
+  if(!th) {
+    // Be_a -= k grad phi_a . grad u   (feSysElm.cpp:558-583),  Be_a -= phi_a f   (feSysElm.cpp:16-27)
+    double GG[3][3];
+    for(int r = 0; r < 3; ++r)
+      for(int s = 0; s < 3; ++s) GG[r][s] = G[r][0] * G[s][0] + G[r][1] * G[s][1] + G[r][2] * G[s][2];
+    double acc = 0.;
+    for(int b = 0; b < 10; ++b) {
+      double L = 0.;
+      for(int r = 0; r < 3; ++r)
+        for(int s = 0; s < 3; ++s) L += GG[r][s] * Tt.k(r, s, a, b);
+      acc += L * sU[b * EPB + lane];
+    }
+    double be = fc.hasDiff ? -fc.diff * acc * J : 0.;
+    if(fc.srcKind == SRC_SIN3) be -= fc.srcCoeff * srcA * J;
+    const int32_t d = dm.adr[(int64_t)a * nE + p];
+    if(d < nInc) atomicAdd(rhs + d, be);
+    return;
+  }
+  double be[3] = {0., 0., 0.};
+  if(fc.hasConv) {
+    // Be_(a,m) -= c int phi_a (u . grad u)_m = c J sum_b W_b u_(b,m),
+    // W_b = sum_c sum_r (sum_k G[r][k] u_(c,k)) T[r][a][c][b]
+    double V0[3][10];
+    for(int c = 0; c < 10; ++c)
+      for(int r = 0; r < 3; ++r)
+        V0[r][c] = G[r][0] * sU[(3 * c) * EPB + lane] + G[r][1] * sU[(3 * c + 1) * EPB + lane] +
+                   G[r][2] * sU[(3 * c + 2) * EPB + lane];
+    for(int b = 0; b < 10; ++b) {
+      double W = 0.;
+      for(int c = 0; c < 10; ++c)
+        for(int r = 0; r < 3; ++r) W += V0[r][c] * Tt.t(r, a, c, b);
+      for(int m = 0; m < 3; ++m) be[m] -= fc.conv * J * W * sU[(3 * b + m) * EPB + lane];
+    }
+  }
+  if(fc.hasSigma) {
+    // Be_(a,m) -= sigma (p d_m phi_a - mu sum_n (d_n u_m + d_m u_n) d_n phi_a)
+    //   = -sigma sum_j p_j Bp[m][j] + sigma mu J sum_b (tr S_ab u_(b,m) + sum_n S_ab[n][m] u_(b,n))
+    for(int b = 0; b < 10; ++b) {
+      double P[3][3], S[3][3];
+      for(int r = 0; r < 3; ++r)
+        for(int l = 0; l < 3; ++l) P[r][l] = Tt.k(r, 0, a, b) * G[0][l] + Tt.k(r, 1, a, b) * G[1][l] + Tt.k(r, 2, a, b) * G[2][l];
+      for(int k = 0; k < 3; ++k)
+        for(int l = 0; l < 3; ++l) S[k][l] = G[0][k] * P[0][l] + G[1][k] * P[1][l] + G[2][k] * P[2][l];
+      const double tr = S[0][0] + S[1][1] + S[2][2];
+      const double ub[3] = {sU[(3 * b) * EPB + lane], sU[(3 * b + 1) * EPB + lane], sU[(3 * b + 2) * EPB + lane]};
+      for(int m = 0; m < 3; ++m)
+        be[m] += fc.sigma * fc.mu * J * (tr * ub[m] + S[0][m] * ub[0] + S[1][m] * ub[1] + S[2][m] * ub[2]);
+    }
+    for(int m = 0; m < 3; ++m) {
+      double acc = 0.;
+      for(int j = 0; j < 4; ++j) {
+        const double bp = (G[0][m] * Tt.d(0, j, a) + G[1][m] * Tt.d(1, j, a) + G[2][m] * Tt.d(2, j, a)) * J;
+        acc += sP[j * EPB + lane] * bp;
+      }
+      be[m] -= fc.sigma * acc;
+    }
+  }
+  if(fc.hasMass) {
+    // Be_(a,m) -= c int udot_m phi_a   (feVectorSysElm.cpp:409-427)
+    for(int m = 0; m < 3; ++m) {
+      double acc = 0.;
+      for(int b = 0; b < 10; ++b) acc += Tt.m(a, b) * sUd[(3 * b + m) * EPB + lane];
+      be[m] -= fc.mass * J * acc;
+    }
+  }
+  if(fc.srcKind == SRC_SIN3_BODY) be[0] -= fc.srcCoeff * srcA * J;
+  else if(fc.srcKind == SRC_CONST_VEC) {
+    double ia = 0.;
+    for(int q = 0; q < nq; ++q) ia += gT->phi[q][a] * gT->qw[q];
+    for(int m = 0; m < 3; ++m) be[m] -= fc.srcCoeff * fc.srcParam[m] * ia * J;
+  }
+  for(int m = 0; m < 3; ++m) {
+    const int32_t d = dm.adr[(int64_t)(3 * a + m) * nE + p];
+    if(d < nInc) atomicAdd(rhs + d, be[m]);
+  }
+  if(fc.hasDivu && a < 4) {
+    // Be_pj -= c int (div u) psi_j = c J sum_b sum_n u_(b,n) sum_r G[r][n] D[r][j][b]
+    const int j = a;
+    double acc = 0.;
+    for(int b = 0; b < 10; ++b)
+      for(int n = 0; n < 3; ++n)
+        acc += sU[(3 * b + n) * EPB + lane] * (G[0][n] * Tt.d(0, j, b) + G[1][n] * Tt.d(1, j, b) + G[2][n] * Tt.d(2, j, b));
+    const int32_t d = dm.adr[(int64_t)(30 + j) * nE + p];
+    if(d < nInc) atomicAdd(rhs + d, -fc.divu * J * acc);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Jacobian, scalar P2 and Taylor-Hood, in V = double or float.
+// ---------------------------------------------------------------------------
+template <typename V>
+__global__ void __launch_bounds__(EPB *TPB) k_matrix_tet(DeviceMesh dm, FormCoeffs fc, const RefTensorsTet *__restrict__ gT,
+                                                         const double *__restrict__ u, double c0, V *__restrict__ values,
+                                                         int64_t begin, int64_t end)
+{
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  V *smem = (V *)smemRaw;
+  const bool th = fc.elemType == 4;
+  V *sTen = smem;
+  V *sU = sTen + NTEN;       // [30][EPB]
+  V *sG = sU + 30 * EPB;     // [10][EPB]
+  V *sV0 = sG + 10 * EPB;    // [3][10][EPB]  V0[r][c] = sum_k G[r][k] u_(c,k)
+  const int lane = threadIdx.x, a = threadIdx.y;
+  const int64_t p0 = begin + (int64_t)blockIdx.x * EPB;
+  const int64_t p = p0 + lane;
+  const bool live = p < end;
+  const int64_t nE = dm.nElm;
+  const int nloc = th ? 34 : 10;
+  const TetTensors<V> Tt = load_tet_tensors(sTen, gT);
+  if(live) {
+    sG[a * EPB + lane] = (V)dm.geo[(int64_t)a * nE + p];
+    if(th && fc.hasConv)
+      for(int m = 0; m < 3; ++m) sU[(3 * a + m) * EPB + lane] = (V)u[dm.adr[(int64_t)(3 * a + m) * nE + p]];
+  } else {
+    sG[a * EPB + lane] = 0;
+    for(int m = 0; m < 3; ++m) sU[(3 * a + m) * EPB + lane] = 0;
+  }
+  __syncthreads();
+  V G[3][3];
+  for(int r = 0; r < 3; ++r)
+    for(int k = 0; k < 3; ++k) G[r][k] = sG[(3 * r + k) * EPB + lane];
+  const V J = sG[9 * EPB + lane];
+  if(!th) {
+    // A_ab += k J sum_rs (G G^T)[r][s] K[r][s][a][b]   (feSysElm.cpp:531-556)
+    V GG[3][3];
+    for(int r = 0; r < 3; ++r)
+      for(int s = 0; s < 3; ++s) GG[r][s] = G[r][0] * G[s][0] + G[r][1] * G[s][1] + G[r][2] * G[s][2];
+    const V cd = (V)fc.diff * J;
+    for(int b = 0; b < 10; ++b) {
+      V L = 0;
+      for(int r = 0; r < 3; ++r)
+        for(int s = 0; s < 3; ++s) L += GG[r][s] * Tt.k(r, s, a, b);
+      const int32_t pos = live ? __ldg(dm.map + (int64_t)(a * 10 + b) * nE + p) : -1;
+      if(pos >= 0) atomicAdd(values + pos, cd * L);
+    }
+    return;
+  }
+  if(fc.hasConv) {
+    for(int r = 0; r < 3; ++r)
+      sV0[(r * 10 + a) * EPB + lane] =
+          G[r][0] * sU[(3 * a) * EPB + lane] + G[r][1] * sU[(3 * a + 1) * EPB + lane] + G[r][2] * sU[(3 * a + 2) * EPB + lane];
+  }
+  __syncthreads();
+  // W_b = sum_c sum_r V0[r][c] T[r][a][c][b] (the u . grad phi_b term), all m
+  V W[10];
+  for(int b = 0; b < 10; ++b) {
+    V w = 0;
+    if(fc.hasConv)
+      for(int c = 0; c < 10; ++c)
+        for(int r = 0; r < 3; ++r) w += sV0[(r * 10 + c) * EPB + lane] * Tt.t(r, a, c, b);
+    W[b] = w;
+  }
+  const V cc = (V)fc.conv * J, cs = -(V)fc.sigma * (V)fc.mu * J, cm = (V)fc.mass * (V)c0 * J;
+  for(int m = 0; m < 3; ++m) {
+    V A[30];
+    for(int j = 0; j < 30; ++j) A[j] = 0;
+    for(int b = 0; b < 10; ++b) {
+      if(fc.hasConv) {
+        // A_(a,m),(b,n) += c [delta_mn phi_a (u . grad phi_b) + phi_a phi_b d_n u_m]
+        // (feVectorSysElm.cpp:1171-1240)
+        V Z[3];
+        for(int r = 0; r < 3; ++r) {
+          V z = 0;
+          for(int c = 0; c < 10; ++c) z += sU[(3 * c + m) * EPB + lane] * Tt.t(r, a, b, c);
+          Z[r] = z;
+        }
+        for(int n = 0; n < 3; ++n) {
+          V v = G[0][n] * Z[0] + G[1][n] * Z[1] + G[2][n] * Z[2];
+          if(n == m) v += W[b];
+          A[3 * b + n] += cc * v;
+        }
+      }
+      if(fc.hasSigma) {
+        // A_(a,m),(b,n) += -c mu [delta_mn grad phi_a . grad phi_b + d_n phi_a d_m phi_b]
+        // (feVectorSysElm.cpp:1454-1492); S[k][l] = int d_k phi_a d_l phi_b / J
+        V P[3][3];
+        for(int r = 0; r < 3; ++r)
+          for(int l = 0; l < 3; ++l) P[r][l] = Tt.k(r, 0, a, b) * G[0][l] + Tt.k(r, 1, a, b) * G[1][l] + Tt.k(r, 2, a, b) * G[2][l];
+        V tr = 0;
+        for(int k = 0; k < 3; ++k) tr += G[0][k] * P[0][k] + G[1][k] * P[1][k] + G[2][k] * P[2][k];
+        for(int n = 0; n < 3; ++n) {
+          const V snm = G[0][n] * P[0][m] + G[1][n] * P[1][m] + G[2][n] * P[2][m];
+          A[3 * b + n] += cs * ((n == m ? tr : (V)0) + snm);
+        }
+      }
+      if(fc.hasMass) A[3 * b + m] += cm * Tt.m(a, b);   // (feVectorSysElm.cpp:390-408)
+    }
+    if(!live) continue;
+    const int row = 3 * a + m;
+    for(int j = 0; j < 30; ++j) {
+      const int32_t pos = __ldg(dm.map + (int64_t)(row * nloc + j) * nE + p);
+      if(pos >= 0) atomicAdd(values + pos, A[j]);
+    }
+    // pressure columns of row (a,m) (sigma int psi_j d_m phi_a) and the
+    // column (a,m) of the pressure rows (divu int psi_j d_m phi_a)
+    for(int j = 0; j < 4; ++j) {
+      const V bp = (G[0][m] * Tt.d(0, j, a) + G[1][m] * Tt.d(1, j, a) + G[2][m] * Tt.d(2, j, a)) * J;
+      if(fc.hasSigma) {
+        const int32_t pos = __ldg(dm.map + (int64_t)(row * nloc + 30 + j) * nE + p);
+        if(pos >= 0) atomicAdd(values + pos, (V)fc.sigma * bp);
+      }
+      if(fc.hasDivu) {
+        const int32_t pos = __ldg(dm.map + (int64_t)((30 + j) * nloc + row) * nE + p);
+        if(pos >= 0) atomicAdd(values + pos, (V)fc.divu * bp);
+      }
+    }
+  }
+}
+
+__global__ void k_build_map(const int32_t *__restrict__ adr, int64_t nE, int nloc, const uint8_t *__restrict__ mask,
+                            const int32_t *__restrict__ ia, const int32_t *__restrict__ ja, int64_t nInc,
+                            int32_t *__restrict__ map, unsigned long long *missing)
+{
+  const int64_t total = (int64_t)nloc * nloc * nE;
+  for(int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = t % nE, ij = t / nE;
+    const int i = (int)(ij / nloc), j = (int)(ij % nloc);
+    int32_t pos = -1;
+    if(mask[ij]) {
+      const int32_t row = adr[(int64_t)i * nE + p], col = adr[(int64_t)j * nE + p];
+      if(row < nInc && col < nInc) {
+        int32_t lo = ia[row], hi = ia[row + 1] - 1;
+        while(lo <= hi) {
+          const int32_t mid = (lo + hi) >> 1, c = ja[mid];
+          if(c == col) { pos = mid; break; }
+          if(c < col) lo = mid + 1;
+          else hi = mid - 1;
+        }
+        if(pos < 0) atomicAdd(missing, 1ull);
+      }
+    }
+    map[t] = pos;
+  }
+}
+
+size_t residual_smem(int nq) { return sizeof(double) * (NTEN + (30 + 30 + 10 + 4 + nq) * EPB); }
+template <typename V>
+size_t matrix_smem() { return sizeof(V) * (NTEN + (30 + 10 + 30) * EPB); }
+
+int64_t nblk(int64_t begin, int64_t end) { return (end - begin + EPB - 1) / EPB; }
+
+}  // namespace
+
+void build_ref_tensors_tet(const QuadRule &q, RefTensorsTet &T)
+{
+  T = RefTensorsTet();
+  T.nq = std::min(q.n(), TET_MAXQ);
+  for(int k = 0; k < T.nq; ++k) {
+    const double r = q.r[k], s = q.s[k], t = q.t[k], w = q.w[k];
+    const double l[4] = {1. - r - s - t, r, s, t};
+    const double dl[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    double phi[10], dphi[10][3];
+    for(int v = 0; v < 4; ++v) {
+      phi[v] = l[v] * (2. * l[v] - 1.);
+      for(int d = 0; d < 3; ++d) dphi[v][d] = (4. * l[v] - 1.) * dl[v][d];
+    }
+    for(int e = 0; e < 6; ++e) {
+      const int va = TET_EDGES[e][0], vb = TET_EDGES[e][1];
+      phi[4 + e] = 4. * l[va] * l[vb];
+      for(int d = 0; d < 3; ++d) dphi[4 + e][d] = 4. * (l[vb] * dl[va][d] + l[va] * dl[vb][d]);
+    }
+    T.qw[k] = w; T.qr[k] = r; T.qs[k] = s; T.qt[k] = t;
+    for(int a = 0; a < 10; ++a) T.phi[k][a] = phi[a];
+    for(int rr = 0; rr < 3; ++rr)
+      for(int ss = 0; ss < 3; ++ss)
+        for(int a = 0; a < 10; ++a)
+          for(int b = 0; b < 10; ++b) T.K[rr][ss][a][b] += w * dphi[a][rr] * dphi[b][ss];
+    for(int rr = 0; rr < 3; ++rr)
+      for(int a = 0; a < 10; ++a)
+        for(int c = 0; c < 10; ++c)
+          for(int b = 0; b < 10; ++b) T.T[rr][a][c][b] += w * phi[a] * phi[c] * dphi[b][rr];
+    for(int rr = 0; rr < 3; ++rr)
+      for(int j = 0; j < 4; ++j)
+        for(int a = 0; a < 10; ++a) T.D[rr][j][a] += w * l[j] * dphi[a][rr];
+    for(int a = 0; a < 10; ++a)
+      for(int b = 0; b < 10; ++b) T.M[a][b] += w * phi[a] * phi[b];
+  }
+}
+
+void launch_assemble_residual_tet(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensorsTet *dT,
+                                  const double *u, const double *udot, int64_t nInc, double *rhs, int64_t begin,
+                                  int64_t end, cudaStream_t s)
+{
+  if(end <= begin) return;
+  const size_t sm = residual_smem(TET_MAXQ);
+  static bool set = false;
+  if(!set) {
+    cudaFuncSetAttribute(k_residual_tet, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    set = true;
+  }
+  (k_residual_tet<<<(unsigned)nblk(begin, end), dim3(EPB, TPB), sm, s>>>(dm, fc, dT, u, udot, nInc, rhs, begin, end),
+   ::feng::count_launch());
+}
+
+template <typename V>
+static void launch_matrix_tet(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensorsTet *dT, const double *u,
+                              double c0, V *values, int64_t begin, int64_t end, cudaStream_t s)
+{
+  if(end <= begin) return;
+  const size_t sm = matrix_smem<V>();
+  static bool set = false;
+  if(!set) {
+    cudaFuncSetAttribute(k_matrix_tet<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    set = true;
+  }
+  (k_matrix_tet<V><<<(unsigned)nblk(begin, end), dim3(EPB, TPB), sm, s>>>(dm, fc, dT, u, c0, values, begin, end),
+   ::feng::count_launch());
+}
+
+void launch_assemble_matrix_tet_f64(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensorsTet *dT,
+                                    const double *u, double c0, double *values, int64_t begin, int64_t end,
+                                    cudaStream_t s)
+{
+  launch_matrix_tet<double>(dm, fc, dT, u, c0, values, begin, end, s);
+}
+
+void launch_assemble_matrix_tet_f32(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensorsTet *dT,
+                                    const double *u, double c0, float *values, int64_t begin, int64_t end,
+                                    cudaStream_t s)
+{
+  launch_matrix_tet<float>(dm, fc, dT, u, c0, values, begin, end, s);
+}
+
+void launch_build_map(const int32_t *adr, int64_t nElm, int nloc, const uint8_t *mask, const int32_t *ia,
+                      const int32_t *ja, int64_t nInc, int32_t *map, unsigned long long *missing, cudaStream_t s)
+{
+  const int64_t total = (int64_t)nloc * nloc * nElm;
+  const int64_t blocks = std::min<int64_t>((total + 255) / 256, 152 * 32);
+  (k_build_map<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, s>>>(adr, nElm, nloc, mask, ia, ja, nInc, map, missing),
+   ::feng::count_launch());
+}
+
+}  // namespace feng

@@ -458,7 +458,34 @@ int fe_setup3d_create(const fe_mesh3d *m, const fe_space_desc *spaces, int nspac
   FE_TRY(build_csr_pattern(S->et, S->num.nInc, S->pat));
   block_partition(S->num, S->pat, M.edge_v.data(), M.n_edges, M.n_vertices(), pc_block_rows,
                   elem_type == ELEM_TET_TAYLOR_HOOD, fieldU, fieldP, S->blockOfRow);
+  // vertex coordinates per tetrahedron: x0 y0 z0 ... x3 y3 z3
+  S->elemXY.resize(M.n_tets() * 12);
+  for(int64_t t = 0; t < M.n_tets(); ++t)
+    for(int k = 0; k < 4; ++k) {
+      const int32_t v = M.tet[4 * t + k];
+      S->elemXY[12 * t + 3 * k] = M.x[v];
+      S->elemXY[12 * t + 3 * k + 1] = M.y[v];
+      S->elemXY[12 * t + 3 * k + 2] = M.z[v];
+    }
   *out = S.release();
+  return FE_OK;
+  GUARD_END
+}
+
+int fe_setup_set_quadrature(fe_setup *s, int nq, const double *rule)
+{
+  GUARD_BEGIN
+  if(!s || nq < 1 || !rule) { set_error("null argument or empty rule"); return FE_INVALID_ARG; }
+  const int d = s->tets ? 3 : 2;
+  QuadRule q;
+  q.degree = s->quad.degree;
+  for(int k = 0; k < nq; ++k) {
+    q.r.push_back(rule[(d + 1) * k]);
+    q.s.push_back(rule[(d + 1) * k + 1]);
+    if(s->tets) q.t.push_back(rule[(d + 1) * k + 2]);
+    q.w.push_back(rule[(d + 1) * k + d]);
+  }
+  s->quad = q;
   return FE_OK;
   GUARD_END
 }
@@ -565,12 +592,11 @@ int fe_cuda_system_create(const fe_setup *setup, const fe_form_desc *forms, int 
 {
   GUARD_BEGIN
   if(!setup || !out || (!forms && nforms > 0)) { set_error("null argument"); return FE_INVALID_ARG; }
-  if(setup->tets) {
-    set_error("device systems on tetrahedral set-ups are not built yet");
-    return FE_INVALID_ARG;
-  }
   FE_TRY(check_options(opt));
-  if(opt->quad_degree != setup->quad.degree) {
+  if(setup->tets) {
+    // tetrahedra: the set-up's own rule when one was given
+    // (fe_setup_set_quadrature), else the rule of the options' degree
+  } else if(opt->quad_degree != setup->quad.degree) {
     set_error("options ask for quadrature degree %d, the set-up was built with %d",
               opt->quad_degree, setup->quad.degree);
     return FE_INVALID_ARG;
@@ -590,6 +616,7 @@ int fe_cuda_system_create(const fe_setup *setup, const fe_form_desc *forms, int 
   // the options re-partitions by contiguous index ranges.
   T.blockOfRow = &setup->blockOfRow;
   T.quad = setup->quad;
+  if(setup->tets && setup->quad.n() == 0) FE_TRY(tet_rule(opt->quad_degree, T.quad));
   std::vector<FormDesc> fd;
   to_forms(forms, nforms, fd);
   FE_TRY(S->sys.init(T, fd.data(), nforms, to_sys_options(opt)));
@@ -606,11 +633,30 @@ int fe_cuda_system_create_from_tables(int elem_type, int64_t n_elm, const int64_
                                       const fe_form_desc *forms, int nforms,
                                       const fe_cuda_options *opt, fe_cuda_system **out)
 {
+  return fe_cuda_system_create_from_tables_rule(elem_type, n_elm, adr, elem_xy, n_inc, n_dofs, n_colors,
+                                                color_offsets, color_elements, ia, ja, block_of_row, forms, nforms,
+                                                opt, 0, nullptr, out);
+}
+
+int fe_cuda_system_create_from_tables_rule(int elem_type, int64_t n_elm, const int64_t *adr,
+                                           const double *elem_xy, int64_t n_inc, int64_t n_dofs,
+                                           int n_colors, const int64_t *color_offsets,
+                                           const int32_t *color_elements, const int64_t *ia,
+                                           const int32_t *ja, const int32_t *block_of_row,
+                                           const fe_form_desc *forms, int nforms,
+                                           const fe_cuda_options *opt, int nq, const double *rule,
+                                           fe_cuda_system **out)
+{
   GUARD_BEGIN
-  if(!out || !adr || !elem_xy || (!forms && nforms > 0)) { set_error("null argument"); return FE_INVALID_ARG; }
+  if(!out || !adr || !elem_xy || (!forms && nforms > 0) || (nq > 0 && !rule) || nq < 0) {
+    set_error("null argument or negative rule size");
+    return FE_INVALID_ARG;
+  }
   FE_TRY(check_options(opt));
   std::unique_ptr<fe_cuda_system> S(new fe_cuda_system());
-  const int nloc = elem_type == ELEM_P2 ? 6 : elem_type == ELEM_TAYLOR_HOOD ? 15 : 0;
+  const bool tet = elem_type == ELEM_TET_P2 || elem_type == ELEM_TET_TAYLOR_HOOD;
+  const int nloc = elem_type == ELEM_P2 ? 6 : elem_type == ELEM_TAYLOR_HOOD ? 15 : elem_type == ELEM_TET_P2 ? 10
+                 : elem_type == ELEM_TET_TAYLOR_HOOD ? 34 : 0;
   if(!nloc) { set_error("unknown element type %d", elem_type); return FE_INVALID_ARG; }
   SystemTables T;
   T.elemType = elem_type;
@@ -622,7 +668,7 @@ int fe_cuda_system_create_from_tables(int elem_type, int64_t n_elm, const int64_
   T.elemXY = elem_xy;
   Coloring col;
   if(color_offsets && color_elements && n_colors > 0) {
-    if(n_colors > 64) { set_error("at most 64 colors"); return FE_BAD_COLORING; }
+    if(n_colors > MAX_COLORS) { set_error("at most %d colors", MAX_COLORS); return FE_BAD_COLORING; }
     col.nColors = n_colors;
     col.offsets.assign(color_offsets, color_offsets + n_colors + 1);
     col.elements.assign(color_elements, color_elements + n_elm);
@@ -652,11 +698,27 @@ int fe_cuda_system_create_from_tables(int elem_type, int64_t n_elm, const int64_
       if(b < 0) { set_error("negative block id"); return FE_INVALID_ARG; }
     T.blockOfRow = &blocks;
   }
-  FE_TRY(triangle_rule(opt->quad_degree, T.quad));
+  if(nq > 0) {
+    // the caller's rule, rows (r, s, [t,] w): the reference's own values
+    // (feSpace::getRQuadraturePoints etc.) reproduce its sums exactly
+    const int d = tet ? 3 : 2;
+    T.quad = QuadRule();
+    T.quad.degree = opt->quad_degree;
+    for(int k = 0; k < nq; ++k) {
+      T.quad.r.push_back(rule[(d + 1) * k]);
+      T.quad.s.push_back(rule[(d + 1) * k + 1]);
+      if(tet) T.quad.t.push_back(rule[(d + 1) * k + 2]);
+      T.quad.w.push_back(rule[(d + 1) * k + d]);
+    }
+  } else if(tet) {
+    FE_TRY(tet_rule(opt->quad_degree, T.quad));
+  } else {
+    FE_TRY(triangle_rule(opt->quad_degree, T.quad));
+  }
   std::vector<FormDesc> fd;
   to_forms(forms, nforms, fd);
+  // init range-checks the DOF ids and validates the coloring before use
   FE_TRY(S->sys.init(T, fd.data(), nforms, to_sys_options(opt)));
-  if(T.coloring) FE_TRY(S->sys.validateColoring());
   *out = S.release();
   return FE_OK;
   GUARD_END

@@ -7,6 +7,8 @@
 
 namespace feng {
 
+struct QuadRule;
+
 // Weak forms the fused element kernels know, named after feNG's
 // elementSystemType (feSysElm.h:13-77).
 enum FormKind : int {
@@ -27,6 +29,27 @@ enum SourceKind : int {
   SRC_NS_MMS_POLY = 2,    // vector  manufactured NS source of u=(x^4y^4, -4/5 x^3y^5), p=x^2y^2
   SRC_CONST_VEC = 3,      // vector  f = (p0, p1)
   SRC_SIN_BODY = 4,       // vector  f = (p0 sin(pi x) sin(pi y), 0)
+  SRC_SIN3 = 5,           // scalar  f = p0 sin(pi x) sin(pi y) sin(pi z)          (tetrahedra)
+  SRC_SIN3_BODY = 6,      // vector  f = (p0 sin(pi x) sin(pi y) sin(pi z), 0, 0)  (tetrahedra)
+};
+
+// Reference-element tensors of a tetrahedral rule (sums over its nodes,
+// weights included; r, s, t the reference directions, a, b, c P2 functions
+// in the local order of feSpaceTetPn(2): vertices, then TET_EDGES; j P1):
+//   K[r][s][a][b] = sum_q w dphi_a/dr dphi_b/ds
+//   T[r][a][c][b] = sum_q w phi_a phi_c dphi_b/dr
+//   D[r][j][a]    = sum_q w psi_j dphi_a/dr
+//   M[a][b]       = sum_q w phi_a phi_b
+// plus the rule itself and the P2 values at its nodes for the sources.
+constexpr int TET_MAXQ = 64;
+struct RefTensorsTet {
+  double K[3][3][10][10];
+  double T[3][10][10][10];
+  double D[3][4][10];
+  double M[10][10];
+  int nq;
+  double qw[TET_MAXQ], qr[TET_MAXQ], qs[TET_MAXQ], qt[TET_MAXQ];
+  double phi[TET_MAXQ][10];
 };
 
 // Reference-element tensors of one quadrature rule (all sums over the rule's
@@ -73,14 +96,18 @@ struct FormCoeffs {
   float pair[5][2];
 };
 
+// Colors of an element coloring (tetrahedral meshes need more than triangles).
+constexpr int MAX_COLORS = 256;
+
 struct DeviceMesh {
   int64_t nElm = 0;
   int nloc = 0;
   int nColors = 0;
-  int64_t colorOff[65];
+  int64_t colorOff[MAX_COLORS + 1];
   int32_t *adr = nullptr;    // [nloc][nElm]  global DOF per local DOF, color order
   double *geo = nullptr;     // [5][nElm]     G00 G01 G10 G11 |J|   (G[r][k] = d r / d x_k)
-  double *xy = nullptr;      // [6][nElm]     x0 y0 x1 y1 x2 y2
+                             // tetrahedra: [10][nElm] G[3][3] row-major, J
+  double *xy = nullptr;      // [6][nElm]     x0 y0 x1 y1 x2 y2 (tetrahedra: [12][nElm] x0 y0 z0 ... z3)
   int32_t *map = nullptr;    // [nloc*nloc][nElm] CSR position or -1
   float2 *geoPair = nullptr; // [5][nElm] geo as float pairs (double-float residual)
 };
@@ -142,5 +169,27 @@ void launch_assemble_matrix_f64(const DeviceMesh &dm, const FormCoeffs &fc, cons
 void launch_assemble_matrix_f32(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensors *dT,
                                 const double *u, double c0, float *values, int64_t begin,
                                 int64_t end, cudaStream_t s);
+
+// Tetrahedra (fe_assembly_tet.cu): residual (FP64) and Jacobian (FP64 or
+// FP32) of the fused forms on elements [begin, end) of the color order, the
+// Jacobian scattered through the element-to-nonzero map (dm.map); scalar P2
+// (DIFFUSION + SOURCE) or Taylor-Hood P2-P1 (the vector forms).
+void build_ref_tensors_tet(const QuadRule &q, RefTensorsTet &T);
+void launch_assemble_residual_tet(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensorsTet *dT,
+                                  const double *u, const double *udot, int64_t nInc, double *rhs,
+                                  int64_t begin, int64_t end, cudaStream_t s);
+void launch_assemble_matrix_tet_f64(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensorsTet *dT,
+                                    const double *u, double c0, double *values, int64_t begin, int64_t end,
+                                    cudaStream_t s);
+void launch_assemble_matrix_tet_f32(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensorsTet *dT,
+                                    const double *u, double c0, float *values, int64_t begin, int64_t end,
+                                    cudaStream_t s);
+// Element-to-nonzero map on the device: map[(i nloc + j) nElm + p] = CSR
+// position of (adr[i][p], adr[j][p]) (binary search in the row), -1 where
+// either DOF is essential or the pair is outside mask [nloc*nloc]; *missing
+// counts coupled pairs absent from the pattern (must stay 0).
+void launch_build_map(const int32_t *adr, int64_t nElm, int nloc, const uint8_t *mask, const int32_t *ia,
+                      const int32_t *ja, int64_t nInc, int32_t *map, unsigned long long *missing,
+                      cudaStream_t s);
 
 }  // namespace feng

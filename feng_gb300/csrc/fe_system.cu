@@ -227,7 +227,7 @@ void build_ref_tensors(const QuadRule &q, RefTensors &T)
 SystemCUDA::~SystemCUDA()
 {
   cudaFree(dm_.adr); cudaFree(dm_.geo); cudaFree(dm_.xy); cudaFree(dm_.map);
-  cudaFree(dT_); cudaFree(csr_.ia); cudaFree(csr_.ja); cudaFree(csr_.diag);
+  cudaFree(dT_); cudaFree(dTt_); cudaFree(csr_.ia); cudaFree(csr_.ja); cudaFree(csr_.diag);
   cudaFree(vals64_); cudaFree(vals32_); cudaFree(rhs_); cudaFree(du_); cudaFree(u_);
   cudaFree(udot_); cudaFree(hist_[1]); cudaFree(hist_[2]); cudaFree(scratch_);
   cudaFree(conRows_); cudaFree(conColPos_); cudaFree(perMaster_); cudaFree(perSlave_);
@@ -251,8 +251,10 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
     set_error("invalid system tables");
     return FE_INVALID_ARG;
   }
-  if(t.quad.n() < 1 || t.quad.n() > 16) {
-    set_error("quadrature rule with %d nodes is not supported (1..16)", t.quad.n());
+  const bool tet = t.elemType == ELEM_TET_P2 || t.elemType == ELEM_TET_TAYLOR_HOOD;
+  const int qmax = tet ? TET_MAXQ : 16;
+  if(t.quad.n() < 1 || t.quad.n() > qmax || (tet && (int)t.quad.t.size() != t.quad.n())) {
+    set_error("quadrature rule with %d nodes is not supported (1..%d)", t.quad.n(), qmax);
     return FE_INVALID_ARG;
   }
   // Every DOF id indexes host and device arrays below: range-check them
@@ -264,7 +266,8 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
       return FE_INVALID_ARG;
     }
   if((t.elemType == ELEM_P2 && nloc_ != 6) || (t.elemType == ELEM_TAYLOR_HOOD && nloc_ != 15) ||
-     (t.elemType != ELEM_P2 && t.elemType != ELEM_TAYLOR_HOOD)) {
+     (t.elemType == ELEM_TET_P2 && nloc_ != 10) || (t.elemType == ELEM_TET_TAYLOR_HOOD && nloc_ != 34) ||
+     (t.elemType != ELEM_P2 && t.elemType != ELEM_TAYLOR_HOOD && !tet)) {
     set_error("element type %d with %d local DOFs is not supported", t.elemType, nloc_);
     return FE_INVALID_ARG;
   }
@@ -279,7 +282,7 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
   fc_.elemType = t.elemType;
   for(int i = 0; i < nforms; ++i) {
     const FormDesc &f = forms[i];
-    const bool vec = t.elemType == ELEM_TAYLOR_HOOD;
+    const bool vec = t.elemType == ELEM_TAYLOR_HOOD || t.elemType == ELEM_TET_TAYLOR_HOOD;
     switch(f.kind) {
       case FORM_DIFFUSION:
         if(vec) { set_error("DIFFUSION needs a scalar P2 element"); return FE_INVALID_ARG; }
@@ -309,7 +312,14 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
         return FE_INVALID_ARG;
     }
   }
-  if(fc_.srcKind < 0 || fc_.srcKind > SRC_SIN_BODY) { set_error("unknown source kind"); return FE_INVALID_ARG; }
+  if(fc_.srcKind < 0 || fc_.srcKind > SRC_SIN3_BODY) { set_error("unknown source kind"); return FE_INVALID_ARG; }
+  {
+    // sources the kernels of each element family evaluate
+    const int k = fc_.srcKind;
+    const bool ok = tet ? (k == SRC_NONE || k == SRC_SIN3 || k == SRC_SIN3_BODY || k == SRC_CONST_VEC)
+                        : (k <= SRC_SIN_BODY);
+    if(!ok) { set_error("source kind %d is not available on this element", k); return FE_INVALID_ARG; }
+  }
   {
     const double cf[5] = {fc_.conv, fc_.mass, fc_.sigma, fc_.mu, fc_.divu};
     for(int k = 0; k < 5; ++k) {
@@ -319,47 +329,80 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
   }
 
   // Host tables: coloring, pattern, scatter map.
-  Mesh2D tmpMesh;  // only the triangle connectivity is needed for coloring
   ElementTables et;
   et.type = t.elemType; et.nloc = nloc_; et.nElm = nE;
   et.adr.assign(t.adr, t.adr + nE * nloc_);
-  if(t.elemType == ELEM_P2) et.mask.assign(36, 1);
+  if(t.elemType == ELEM_P2 || t.elemType == ELEM_TET_P2) et.mask.assign(nloc_ * nloc_, 1);
   else {
-    et.mask.assign(225, 0);
-    for(int i = 0; i < 15; ++i)
-      for(int j = 0; j < 15; ++j) et.mask[i * 15 + j] = (i < 12 || j < 12) ? 1 : 0;
+    // velocity rows couple to every column, pressure rows to velocity columns
+    const int nu = nloc_ == 15 ? 12 : 30;
+    et.mask.assign(nloc_ * nloc_, 0);
+    for(int i = 0; i < nloc_; ++i)
+      for(int j = 0; j < nloc_; ++j) et.mask[i * nloc_ + j] = (i < nu || j < nu) ? 1 : 0;
   }
   if(t.coloring && !t.coloring->elements.empty()) {
     col_ = *t.coloring;
   } else {
-    // Color on the vertex DOFs of the element (first three local functions
-    // of the scalar field / first component of the vector field).
-    tmpMesh.x.assign(nDofs_, 0.); tmpMesh.y.assign(nDofs_, 0.);
-    tmpMesh.tri.resize(nE * 3);
-    const int stride = t.elemType == ELEM_P2 ? 1 : 2;
+    // Color on the vertex DOFs of the element (first local functions of the
+    // scalar field / first component of the vector field), which number the
+    // vertices one to one.
+    const int nvpe = tet ? 4 : 3;
+    const int stride = (t.elemType == ELEM_P2 || t.elemType == ELEM_TET_P2) ? 1 : tet ? 3 : 2;
+    std::vector<int32_t> ev(nE * nvpe);
     for(int64_t e = 0; e < nE; ++e)
-      for(int k = 0; k < 3; ++k) tmpMesh.tri[3 * e + k] = (int32_t)t.adr[e * nloc_ + k * stride];
-    FE_TRY(color_elements(tmpMesh, col_));
+      for(int k = 0; k < nvpe; ++k) ev[nvpe * e + k] = (int32_t)t.adr[e * nloc_ + k * stride];
+    FE_TRY(color_by_vertices(ev.data(), nvpe, nE, nDofs_, MAX_COLORS, col_));
   }
-  if(col_.nColors > 64 || (int64_t)col_.elements.size() != nE) {
+  if(col_.nColors > MAX_COLORS || (int64_t)col_.elements.size() != nE) {
     set_error("invalid coloring");
     return FE_BAD_COLORING;
   }
+  const int nxy = tet ? 12 : 6;  // vertex coordinates per element
   adrHost_.assign(t.adr, t.adr + nE * nloc_);
-  elemXYHost_.assign(t.elemXY, t.elemXY + nE * 6);
+  elemXYHost_.assign(t.elemXY, t.elemXY + nE * nxy);
   elemType_ = t.elemType;
   FE_TRY(validateColoring());
   if(t.pattern && t.pattern->n == nInc_) pat_ = *t.pattern;
   else FE_TRY(build_csr_pattern(et, nInc_, pat_));
   std::vector<int32_t> map;
-  FE_TRY(build_scatter_map(et, col_, pat_, nInc_, map));
+  // Tetrahedra: the element-to-nonzero map is built on the device below.
+  if(!tet) FE_TRY(build_scatter_map(et, col_, pat_, nInc_, map));
 
   // Color-ordered SoA element data.
   std::vector<int32_t> adrP((size_t)nloc_ * nE);
-  std::vector<double> geo(5 * nE), xy(6 * nE);
+  std::vector<double> geo((tet ? 10 : 5) * nE), xy(nxy * nE);
   for(int64_t p = 0; p < nE; ++p) {
     const int64_t e = col_.elements[p];
     for(int i = 0; i < nloc_; ++i) adrP[(size_t)i * nE + p] = (int32_t)t.adr[e * nloc_ + i];
+    if(tet) {
+      // P1 tetrahedron: columns of dx/d(r,s,t) = x1-x0, x2-x0, x3-x0;
+      // G = its inverse (G[r][k] = d r_r / d x_k), J its determinant
+      // (feCncGeo::computeElementTransformation in 3D).
+      const double *c = t.elemXY + 12 * e;
+      double Jm[3][3];
+      for(int k = 0; k < 3; ++k)
+        for(int r = 0; r < 3; ++r) Jm[k][r] = c[3 * (r + 1) + k] - c[k];
+      const double det = Jm[0][0] * (Jm[1][1] * Jm[2][2] - Jm[1][2] * Jm[2][1]) -
+                         Jm[0][1] * (Jm[1][0] * Jm[2][2] - Jm[1][2] * Jm[2][0]) +
+                         Jm[0][2] * (Jm[1][0] * Jm[2][1] - Jm[1][1] * Jm[2][0]);
+      if(!(std::fabs(det) > 0)) {
+        set_error("element %lld has a zero Jacobian", (long long)e);
+        return FE_INVALID_ARG;
+      }
+      // inverse: G[r][k] = cofactor(k, r) / det
+      const double G[3][3] = {
+          {(Jm[1][1] * Jm[2][2] - Jm[1][2] * Jm[2][1]) / det, (Jm[0][2] * Jm[2][1] - Jm[0][1] * Jm[2][2]) / det,
+           (Jm[0][1] * Jm[1][2] - Jm[0][2] * Jm[1][1]) / det},
+          {(Jm[1][2] * Jm[2][0] - Jm[1][0] * Jm[2][2]) / det, (Jm[0][0] * Jm[2][2] - Jm[0][2] * Jm[2][0]) / det,
+           (Jm[0][2] * Jm[1][0] - Jm[0][0] * Jm[1][2]) / det},
+          {(Jm[1][0] * Jm[2][1] - Jm[1][1] * Jm[2][0]) / det, (Jm[0][1] * Jm[2][0] - Jm[0][0] * Jm[2][1]) / det,
+           (Jm[0][0] * Jm[1][1] - Jm[0][1] * Jm[1][0]) / det}};
+      for(int r = 0; r < 3; ++r)
+        for(int k = 0; k < 3; ++k) geo[(size_t)(3 * r + k) * nE + p] = G[r][k];
+      geo[(size_t)9 * nE + p] = det;
+      for(int k = 0; k < 12; ++k) xy[(size_t)k * nE + p] = c[k];
+      continue;
+    }
     const double *c = t.elemXY + 6 * e;
     // P1 geometry: dx/dr = x1-x0, dx/ds = x2-x0 (feCncGeo::computeElementTransformation,
     // feCncGeo.cpp:651-670)
@@ -403,16 +446,26 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
     CK(cudaMalloc(&dm_.geoPair, sizeof(float2) * gp.size()));
     CK(cudaMemcpy(dm_.geoPair, gp.data(), sizeof(float2) * gp.size(), cudaMemcpyHostToDevice));
   }
-  if(!useRows_) {
+  if(!useRows_ && !tet) {
     // the colored scatter's element-to-nonzero map
     CK(cudaMalloc(&dm_.map, sizeof(int32_t) * map.size()));
     CK(cudaMemcpy(dm_.map, map.data(), sizeof(int32_t) * map.size(), cudaMemcpyHostToDevice));
   }
 
   RefTensors hT;
-  build_ref_tensors(t.quad, hT);
-  exact5_ = hT.exact5;
-  nq_ = hT.nq;
+  std::unique_ptr<RefTensorsTet> hTt;
+  if(tet) {
+    hTt = std::make_unique<RefTensorsTet>();
+    build_ref_tensors_tet(t.quad, *hTt);
+    exact5_ = 0;
+    nq_ = hTt->nq;
+    CK(cudaMalloc(&dTt_, sizeof(RefTensorsTet)));
+    CK(cudaMemcpy(dTt_, hTt.get(), sizeof(RefTensorsTet), cudaMemcpyHostToDevice));
+  } else {
+    build_ref_tensors(t.quad, hT);
+    exact5_ = hT.exact5;
+    nq_ = hT.nq;
+  }
   CK(cudaMalloc(&dT_, sizeof(RefTensors)));
   CK(cudaMemcpy(dT_, &hT, sizeof(RefTensors), cudaMemcpyHostToDevice));
 
@@ -427,6 +480,29 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
   CK(cudaMemcpy(csr_.ia, ia32.data(), sizeof(int32_t) * (nInc_ + 1), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(csr_.ja, pat_.ja.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice));
   (k_diagpos<<<gridFor(nInc_), 256, 0, s_>>>(nInc_, csr_.ia, csr_.ja, csr_.diag), ::feng::count_launch());
+  if(tet) {
+    // Element-to-nonzero map built on the device (nloc^2 entries per
+    // element): a binary search of every coupled pair in its CSR row.
+    const size_t mapLen = (size_t)nloc_ * nloc_ * nE;
+    std::vector<uint8_t> mask(et.mask.begin(), et.mask.end());
+    uint8_t *dMask = nullptr;
+    unsigned long long *dMissing = nullptr, missing = 0;
+    CK(cudaMalloc(&dm_.map, sizeof(int32_t) * mapLen));
+    CK(cudaMalloc(&dMask, mask.size()));
+    CK(cudaMalloc(&dMissing, sizeof(unsigned long long)));
+    CK(cudaMemcpy(dMask, mask.data(), mask.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemset(dMissing, 0, sizeof(unsigned long long)));
+    launch_build_map(dm_.adr, nE, nloc_, dMask, csr_.ia, csr_.ja, nInc_, dm_.map, dMissing, s_);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&missing, dMissing, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s_));
+    CK(cudaStreamSynchronize(s_));
+    cudaFree(dMask);
+    cudaFree(dMissing);
+    if(missing) {
+      set_error("%llu coupled DOF pairs are missing from the CSR pattern", missing);
+      return FE_INVALID_ARG;
+    }
+  }
   if(opt.precision == 0) CK(cudaMalloc(&vals64_, sizeof(double) * nnz));
   else CK(cudaMalloc(&vals32_, sizeof(float) * nnz));
   zeroPending_ = true;
@@ -457,12 +533,86 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
   PrecondInfo pinfo;
   HostCSR lap;
   if(ko.precond == 3 || ko.precond == 4) {
-    ko.precond = t.elemType == ELEM_P2 ? 3 : 4;
-    FE_TRY(build_precond_info(t, hT, lap, pinfo));
+    if(t.elemType == ELEM_TET_TAYLOR_HOOD) {
+      set_error("the multigrid preconditioner is built for triangles and scalar P2 tetrahedra");
+      return FE_INVALID_ARG;
+    }
+    ko.precond = (t.elemType == ELEM_P2 || t.elemType == ELEM_TET_P2) ? 3 : 4;
+    if(tet) FE_TRY(build_precond_info_tet(t, *hTt, lap, pinfo));
+    else FE_TRY(build_precond_info(t, hT, lap, pinfo));
     pinfo.innerIterations = opt.mgInner;
     pinfo.chebyDegree = std::max(1, std::min(6, opt.mgSmooth));
   }
   FE_TRY(kry_.setup(csr_, blocks, nbHint, ko, s_, &pinfo));
+  return FE_OK;
+}
+
+// Scalar P2 tetrahedra: the P2 stiffness on the unknown DOFs (the
+// multigrid's operator; the system's own Laplacian up to the coefficient).
+int SystemCUDA::build_precond_info_tet(const SystemTables &t, const RefTensorsTet &T, HostCSR &lap, PrecondInfo &pi)
+{
+  const int64_t nE = t.nElm;
+  std::vector<int32_t> nodeOf(nDofs_, -1);
+  int64_t nN = 0;
+  for(int64_t e = 0; e < nE; ++e)
+    for(int a = 0; a < 10; ++a) {
+      const int64_t d = t.adr[e * 10 + a];
+      if(d < nInc_ && nodeOf[d] < 0) {
+        nodeOf[d] = (int32_t)nN++;
+        pi.nodeDofX.push_back((int32_t)d);
+      }
+    }
+  std::vector<std::pair<int64_t, double>> coo;
+  coo.reserve(nE * 100);
+  for(int64_t e = 0; e < nE; ++e) {
+    const double *c = t.elemXY + 12 * e;
+    double Jm[3][3];
+    for(int k = 0; k < 3; ++k)
+      for(int r = 0; r < 3; ++r) Jm[k][r] = c[3 * (r + 1) + k] - c[k];
+    const double det = Jm[0][0] * (Jm[1][1] * Jm[2][2] - Jm[1][2] * Jm[2][1]) -
+                       Jm[0][1] * (Jm[1][0] * Jm[2][2] - Jm[1][2] * Jm[2][0]) +
+                       Jm[0][2] * (Jm[1][0] * Jm[2][1] - Jm[1][1] * Jm[2][0]);
+    const double G[3][3] = {
+        {(Jm[1][1] * Jm[2][2] - Jm[1][2] * Jm[2][1]) / det, (Jm[0][2] * Jm[2][1] - Jm[0][1] * Jm[2][2]) / det,
+         (Jm[0][1] * Jm[1][2] - Jm[0][2] * Jm[1][1]) / det},
+        {(Jm[1][2] * Jm[2][0] - Jm[1][0] * Jm[2][2]) / det, (Jm[0][0] * Jm[2][2] - Jm[0][2] * Jm[2][0]) / det,
+         (Jm[0][2] * Jm[1][0] - Jm[0][0] * Jm[1][2]) / det},
+        {(Jm[1][0] * Jm[2][1] - Jm[1][1] * Jm[2][0]) / det, (Jm[0][1] * Jm[2][0] - Jm[0][0] * Jm[2][1]) / det,
+         (Jm[0][0] * Jm[1][1] - Jm[0][1] * Jm[1][0]) / det}};
+    double GG[3][3];
+    for(int r = 0; r < 3; ++r)
+      for(int s2 = 0; s2 < 3; ++s2) GG[r][s2] = G[r][0] * G[s2][0] + G[r][1] * G[s2][1] + G[r][2] * G[s2][2];
+    int32_t nd[10];
+    for(int a = 0; a < 10; ++a) {
+      const int64_t d = t.adr[e * 10 + a];
+      nd[a] = d < nInc_ ? nodeOf[d] : -1;
+    }
+    for(int a = 0; a < 10; ++a) {
+      if(nd[a] < 0) continue;
+      for(int b = 0; b < 10; ++b) {
+        if(nd[b] < 0) continue;
+        double v = 0.;
+        for(int r = 0; r < 3; ++r)
+          for(int s2 = 0; s2 < 3; ++s2) v += GG[r][s2] * T.K[r][s2][a][b];
+        coo.push_back({(int64_t)nd[a] * nN + nd[b], std::fabs(det) * v});
+      }
+    }
+  }
+  std::sort(coo.begin(), coo.end(),
+            [](const std::pair<int64_t, double> &x, const std::pair<int64_t, double> &y) { return x.first < y.first; });
+  lap = HostCSR();
+  lap.n = lap.m = nN;
+  lap.ia.assign(nN + 1, 0);
+  for(size_t k = 0; k < coo.size();) {
+    const int64_t key = coo[k].first;
+    double v = 0.;
+    while(k < coo.size() && coo[k].first == key) v += coo[k++].second;
+    lap.ja.push_back((int32_t)(key % nN));
+    lap.a.push_back(v);
+    lap.ia[key / nN + 1] = (int64_t)lap.ja.size();
+  }
+  for(int64_t i = 0; i < nN; ++i) lap.ia[i + 1] = std::max(lap.ia[i + 1], lap.ia[i]);
+  pi.lap = &lap;
   return FE_OK;
 }
 
@@ -604,6 +754,10 @@ int SystemCUDA::build_precond_info(const SystemTables &t, const RefTensors &T, H
 
 int SystemCUDA::normPoints(int *nq, double *hostX, double *hostY)
 {
+  if(tet()) {
+    set_error("error norms on the device are built for triangles");
+    return FE_INVALID_ARG;
+  }
   if(!nq) {
     set_error("null argument");
     return FE_INVALID_ARG;
@@ -625,6 +779,10 @@ int SystemCUDA::normPoints(int *nq, double *hostX, double *hostY)
 
 int SystemCUDA::l2Error(int field, const double *hostExact, double *err)
 {
+  if(tet()) {
+    set_error("error norms on the device are built for triangles");
+    return FE_INVALID_ARG;
+  }
   if(!hostExact || !err) {
     set_error("null argument");
     return FE_INVALID_ARG;
@@ -837,6 +995,11 @@ int SystemCUDA::setResidualToZero()
 
 void SystemCUDA::launch_residual(double *out)
 {
+  if(tet()) {
+    for(int c = 0; c < dm_.nColors; ++c)
+      launch_assemble_residual_tet(dm_, fc_, dTt_, u_, udot_, nInc_, out, dm_.colorOff[c], dm_.colorOff[c + 1], s_);
+    return;
+  }
   if(dfResidual()) {
     launch_split_pairs(nDofs_, u_, uPair_, s_);
     if(fc_.hasMass) launch_split_pairs(nDofs_, udot_, udotPair_, s_);
@@ -875,6 +1038,15 @@ int SystemCUDA::launch_matrix()
     return FE_OK;
   }
   FE_TRY(ensureMatrixZeroed());
+  if(tet()) {
+    for(int c = 0; c < dm_.nColors; ++c) {
+      if(vals64_)
+        launch_assemble_matrix_tet_f64(dm_, fc_, dTt_, u_, c0_, vals64_, dm_.colorOff[c], dm_.colorOff[c + 1], s_);
+      else
+        launch_assemble_matrix_tet_f32(dm_, fc_, dTt_, u_, c0_, vals32_, dm_.colorOff[c], dm_.colorOff[c + 1], s_);
+    }
+    return FE_OK;
+  }
   for(int c = 0; c < dm_.nColors; ++c) {
     if(vals64_)
       launch_assemble_matrix_f64(dm_, fc_, dT_, u_, c0_, vals64_, dm_.colorOff[c],

@@ -41,7 +41,7 @@ struct SystemTables {
   int nloc = 0;
   int64_t nInc = 0, nDofs = 0;
   const int64_t *adr = nullptr;       // [nElm*nloc]
-  const double *elemXY = nullptr;     // [nElm*6] x0 y0 x1 y1 x2 y2
+  const double *elemXY = nullptr;     // [nElm*6] x0 y0 x1 y1 x2 y2 (tetrahedra: [nElm*12] x0 y0 z0 ... z3)
   // optional (computed when null/empty):
   const Coloring *coloring = nullptr;
   const CSRPattern *pattern = nullptr;
@@ -197,6 +197,9 @@ class SystemCUDA {
   int begin_phase();
   float end_phase();
   int build_precond_info(const SystemTables &t, const RefTensors &T, HostCSR &lap, PrecondInfo &pi);
+  int build_precond_info_tet(const SystemTables &t, const RefTensorsTet &T, HostCSR &lap, PrecondInfo &pi);
+  RefTensorsTet *dTt_ = nullptr;  // tetrahedral reference tensors (device)
+  bool tet() const { return elemType_ == ELEM_TET_P2 || elemType_ == ELEM_TET_TAYLOR_HOOD; }
 };
 
 // Reference-element tensors of a quadrature rule (host, FP64).

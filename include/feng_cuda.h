@@ -54,6 +54,8 @@ extern "C" {
 #define FE_SRC_NS_MMS_POLY 2  /* NS manufactured source, tests/withLinearSolver/navier_stokes.cpp:33-51 */
 #define FE_SRC_CONST_VEC 3    /* (p0, p1)                                        */
 #define FE_SRC_SIN_BODY 4     /* (p0 sin(pi x) sin(pi y), 0)                     */
+#define FE_SRC_SIN3 5         /* p0 sin(pi x) sin(pi y) sin(pi z)      (tetrahedra) */
+#define FE_SRC_SIN3_BODY 6    /* (p0 sin(pi x) sin(pi y) sin(pi z), 0, 0) (tetrahedra) */
 
 /* ---- element types of the fused kernels */
 #define FE_ELEM_P2 1            /* scalar Lagrange P2 triangle, 6 local DOFs          */
@@ -225,6 +227,10 @@ void fe_setup_destroy(fe_setup *s);
 int fe_setup3d_create(const fe_mesh3d *m, const fe_space_desc *spaces, int nspaces, int elem_type,
                       int pc_block_rows, fe_setup **out);
 /* z coordinate of every DOF (tetrahedral set-ups only). */
+/* Replaces the set-up's quadrature rule (nq rows (r, s, w) or, on
+ * tetrahedra, (r, s, t, w)), e.g. with the reference's tabulated values;
+ * without it a tetrahedral set-up takes the rule of the options' degree. */
+int fe_setup_set_quadrature(fe_setup *s, int nq, const double *rule);
 int fe_setup_get_dof_z(const fe_setup *s, double *z);
 int fe_setup_sizes(const fe_setup *s, int64_t *n_inc, int64_t *n_dofs, int64_t *nnz,
                    int64_t *n_elm, int *n_colors, int *nloc);
@@ -288,6 +294,21 @@ int fe_cuda_system_create_from_tables(int elem_type, int64_t n_elm, const int64_
                                       const int32_t *ja, const int32_t *block_of_row,
                                       const fe_form_desc *forms, int nforms,
                                       const fe_cuda_options *opt, fe_cuda_system **out);
+/* As fe_cuda_system_create_from_tables, with the quadrature rule given as nq
+ * rows (r, s, w) on triangles or (r, s, t, w) on tetrahedra (the reference's
+ * own tabulated values, feSpace::getRQuadraturePoints / getSQuadraturePoints /
+ * getTQuadraturePoints / getQuadratureWeights); nq = 0: the rule of
+ * opt->quad_degree.  Element types: FE_ELEM_P2, FE_ELEM_TAYLOR_HOOD (elem_xy
+ * [n_elm*6]) and FE_ELEM_TET_P2, FE_ELEM_TET_TAYLOR_HOOD (elem_xy [n_elm*12],
+ * x y z of the four vertices). */
+int fe_cuda_system_create_from_tables_rule(int elem_type, int64_t n_elm, const int64_t *adr,
+                                           const double *elem_xy, int64_t n_inc, int64_t n_dofs,
+                                           int n_colors, const int64_t *color_offsets,
+                                           const int32_t *color_elements, const int64_t *ia,
+                                           const int32_t *ja, const int32_t *block_of_row,
+                                           const fe_form_desc *forms, int nforms,
+                                           const fe_cuda_options *opt, int nq, const double *rule,
+                                           fe_cuda_system **out);
 void fe_cuda_system_destroy(fe_cuda_system *s);
 
 int fe_cuda_system_sizes(const fe_cuda_system *s, int64_t *n_inc, int64_t *n_dofs, int64_t *nnz,
