@@ -172,6 +172,7 @@ SIGNATURES = {
     "fe_cuda_transient_create": (C.c_int, [P, C.POINTER(TransientOptions), C.POINTER(NewtonOptions),
                                            C.POINTER(P)]),
     "fe_cuda_transient_steps": (C.c_int, [P, C.c_int, P]),
+    "fe_cuda_apply_preconditioner": (C.c_int, [P, P, P]),
     "fe_setup_set_quadrature": (C.c_int, [P, C.c_int, P]),
     "fe_cuda_system_create_from_tables_rule": (C.c_int, [C.c_int, C.c_int64, P, P, C.c_int64, C.c_int64, C.c_int, P, P,
                                                           P, P, P, P, C.c_int, P, C.c_int, P, P]),

@@ -509,6 +509,13 @@ class feLinearSystemCUDA:
         return dict(status=s, normDx=dx.value, normRHS=rhs.value, normAxb=axb.value,
                     nIter=it.value)
 
+    def applyPreconditioner(self, r):
+        """z = M^-1 r with the current preconditioner (PETSc's PCApply)."""
+        r = np.ascontiguousarray(r, np.float64)
+        z = np.empty(self.nInc)
+        check(self.lib.fe_cuda_apply_preconditioner(self._h, ptr(r), ptr(z)))
+        return z
+
     def correctSolution(self):
         check(self.lib.fe_cuda_correct_solution(self._h))
 

@@ -851,6 +851,14 @@ int fe_cuda_get_rhs(const fe_cuda_system *s, double *rhs)
   return s->sys.getRHS(rhs);
 }
 
+int fe_cuda_apply_preconditioner(fe_cuda_system *s, const double *r, double *z)
+{
+  GUARD_BEGIN
+  if(!s || !r || !z) { set_error("null argument"); return FE_INVALID_ARG; }
+  return s->sys.applyPreconditioner(r, z);
+  GUARD_END
+}
+
 int fe_cuda_get_du(const fe_cuda_system *s, double *du)
 {
   if(!s || !du) { set_error("null argument"); return FE_INVALID_ARG; }

@@ -762,70 +762,131 @@ __global__ void k_gmres_init(GmresState *gs, const RedState *st)
 }
 
 // ---------------------------------------------------------------------------
-// Block-Jacobi ILU(0): one thread per block, rows in ascending order.
-// Factorisation: IKJ variant restricted to the pattern (Saad Alg. 10.4).
+// Block-Jacobi ILU(0) (Saad Alg. 10.4, IKJ variant restricted to the pattern),
+// level-scheduled: one warp per row, the rows of a level in parallel.  The
+// factorisation applies each row's updates in the serial order (ascending
+// pivots k, each entry once per k), so the factors equal the serial ones bit
+// for bit; the triangular solves sum each row in a warp-tree order.
 // ---------------------------------------------------------------------------
+constexpr int ILU_NARROW_THREADS = 1024;  // one block of 32 warps runs a run of narrow levels
+
 template <typename VF>
-__global__ void k_ilu_factor(int64_t nBlocks, const int32_t *__restrict__ bstart,
-                             const int32_t *__restrict__ perm, const int32_t *__restrict__ lia,
-                             const int32_t *__restrict__ lja, const int32_t *__restrict__ ldiag,
-                             const int32_t *__restrict__ srcPos, const double *__restrict__ v64,
-                             const float *__restrict__ v32, VF *__restrict__ f,
-                             int *__restrict__ status)
+__global__ void k_ilu_copy(int64_t lnnz, const int32_t *__restrict__ srcPos, const double *__restrict__ v64,
+                           const float *__restrict__ v32, VF *__restrict__ f)
 {
-  const int64_t blk = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if(blk >= nBlocks) return;
-  for(int32_t q = bstart[blk]; q < bstart[blk + 1]; ++q) {
-    const int32_t i = perm[q];
-    const int32_t rb = lia[i], re = lia[i + 1], rd = ldiag[i];
-    for(int32_t k = rb; k < re; ++k) f[k] = v64 ? (VF)v64[srcPos[k]] : (VF)v32[srcPos[k]];
-    // eliminate with previous rows k < i (entries before the diagonal)
-    for(int32_t kk = rb; kk < rd; ++kk) {
-      const int32_t kr = lja[kk];
-      const VF piv = f[ldiag[kr]];
-      if(piv == (VF)0) { atomicExch(status, 1); return; }
-      const VF lik = f[kk] / piv;
-      f[kk] = lik;
-      // row i entries j > kr: subtract lik * U(kr, j) where (kr,j) exists
-      int32_t p = ldiag[kr] + 1;
-      const int32_t pe = lia[kr + 1];
-      for(int32_t jj = kk + 1; jj < re && p < pe; ++jj) {
-        const int32_t col = lja[jj];
-        while(p < pe && lja[p] < col) ++p;
-        if(p < pe && lja[p] == col) f[jj] -= lik * f[p];
+  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < lnnz; k += (int64_t)gridDim.x * blockDim.x)
+    f[k] = v64 ? (VF)v64[srcPos[k]] : (VF)v32[srcPos[k]];
+}
+
+// Row i (one warp): for each pivot k of its L part in ascending order,
+// l_ik = a_ik / u_kk, then a_ij -= l_ik u_kj for the entries j > k of row i
+// that row k holds (binary search in row k's U part, lanes over j).
+template <typename VF>
+__device__ __forceinline__ void ilu_factor_row(int32_t i, const int32_t *__restrict__ lia,
+                                               const int32_t *__restrict__ lja, const int32_t *__restrict__ ldiag,
+                                               VF *__restrict__ f, int *__restrict__ status)
+{
+  const int lane = threadIdx.x & 31;
+  const int32_t rb = lia[i], re = lia[i + 1], rd = ldiag[i];
+  for(int32_t kk = rb; kk < rd; ++kk) {
+    const int32_t kr = lja[kk];
+    const VF piv = f[ldiag[kr]];
+    if(piv == (VF)0) {
+      if(lane == 0) atomicExch(status, 1);
+      return;
+    }
+    const VF lik = f[kk] / piv;
+    __syncwarp();
+    if(lane == 0) f[kk] = lik;
+    const int32_t ub = ldiag[kr] + 1, ue = lia[kr + 1];
+    for(int32_t jj = kk + 1 + lane; jj < re; jj += 32) {
+      const int32_t col = lja[jj];
+      int32_t lo = ub, hi = ue - 1;
+      while(lo <= hi) {
+        const int32_t mid = (lo + hi) >> 1, c = lja[mid];
+        if(c == col) {
+          f[jj] -= lik * f[mid];
+          break;
+        }
+        if(c < col) lo = mid + 1;
+        else hi = mid - 1;
       }
     }
+    __syncwarp();
+  }
+  if(lane == 0) {
     const VF d = f[rd];
-    if(d == (VF)0) { atomicExch(status, 1); return; }
-    if(!isfinite((double)d)) { atomicExch(status, 2); return; }
+    if(d == (VF)0) atomicExch(status, 1);
+    else if(!isfinite((double)d)) atomicExch(status, 2);
   }
 }
 
-// z = (LU)^{-1} r on each block.
-template <typename VF, typename VV>
-__global__ void k_ilu_solve(int64_t nBlocks, const int32_t *__restrict__ bstart,
-                            const int32_t *__restrict__ perm, const int32_t *__restrict__ lia,
-                            const int32_t *__restrict__ lja, const int32_t *__restrict__ ldiag,
-                            const VF *__restrict__ f, const VV *__restrict__ r,
-                            VV *__restrict__ z, const int *__restrict__ done)
+// z_i = r_i - sum_{k < i} l_ik z_k (lower) or z_i = (z_i - sum_{k > i} u_ik z_k) / u_ii (upper).
+template <typename VF, typename VV, bool LOWER>
+__device__ __forceinline__ void ilu_solve_row(int32_t i, const int32_t *__restrict__ lia,
+                                              const int32_t *__restrict__ lja, const int32_t *__restrict__ ldiag,
+                                              const VF *__restrict__ f, const VV *__restrict__ r, VV *__restrict__ z)
+{
+  const int lane = threadIdx.x & 31;
+  const int32_t d = ldiag[i];
+  const int32_t b = LOWER ? lia[i] : d + 1, e = LOWER ? d : lia[i + 1];
+  VF s = 0;
+  for(int32_t k = b + lane; k < e; k += 32) s += f[k] * (VF)z[lja[k]];
+  for(int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if(lane == 0) {
+    if(LOWER) z[i] = (VV)((VF)r[i] - s);
+    else z[i] = (VV)(((VF)z[i] - s) / f[d]);
+  }
+}
+
+// A run of narrow levels: one block, levels in order, a barrier between them.
+template <typename VF>
+__global__ void __launch_bounds__(ILU_NARROW_THREADS) k_ilu_factor_run(
+    int32_t lv0, int32_t lv1, const int32_t *__restrict__ lvl, const int32_t *__restrict__ rows,
+    const int32_t *__restrict__ lia, const int32_t *__restrict__ lja, const int32_t *__restrict__ ldiag,
+    VF *__restrict__ f, int *__restrict__ status)
+{
+  const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for(int32_t lv = lv0; lv < lv1; ++lv) {
+    for(int32_t q = lvl[lv] + warp; q < lvl[lv + 1]; q += nw) ilu_factor_row<VF>(rows[q], lia, lja, ldiag, f, status);
+    __syncthreads();
+  }
+}
+
+// One wide level over many blocks (warp per row).
+template <typename VF>
+__global__ void k_ilu_factor_level(int32_t q0, int32_t q1, const int32_t *__restrict__ rows,
+                                   const int32_t *__restrict__ lia, const int32_t *__restrict__ lja,
+                                   const int32_t *__restrict__ ldiag, VF *__restrict__ f, int *__restrict__ status)
+{
+  const int64_t q = q0 + ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  if(q < q1) ilu_factor_row<VF>(rows[q], lia, lja, ldiag, f, status);
+}
+
+template <typename VF, typename VV, bool LOWER>
+__global__ void __launch_bounds__(ILU_NARROW_THREADS) k_ilu_solve_run(
+    int32_t lv0, int32_t lv1, const int32_t *__restrict__ lvl, const int32_t *__restrict__ rows,
+    const int32_t *__restrict__ lia, const int32_t *__restrict__ lja, const int32_t *__restrict__ ldiag,
+    const VF *__restrict__ f, const VV *__restrict__ r, VV *__restrict__ z, const int *__restrict__ done)
 {
   if(done && *done) return;
-  const int64_t blk = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if(blk >= nBlocks) return;
-  const int32_t qb = bstart[blk], qe = bstart[blk + 1];
-  for(int32_t q = qb; q < qe; ++q) {
-    const int32_t i = perm[q];
-    VF s = (VF)r[i];
-    for(int32_t k = lia[i]; k < ldiag[i]; ++k) s -= f[k] * (VF)z[lja[k]];
-    z[i] = (VV)s;
+  const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for(int32_t lv = lv0; lv < lv1; ++lv) {
+    for(int32_t q = lvl[lv] + warp; q < lvl[lv + 1]; q += nw)
+      ilu_solve_row<VF, VV, LOWER>(rows[q], lia, lja, ldiag, f, r, z);
+    __syncthreads();
   }
-  for(int32_t q = qe - 1; q >= qb; --q) {
-    const int32_t i = perm[q];
-    VF s = (VF)z[i];
-    const int32_t d = ldiag[i];
-    for(int32_t k = d + 1; k < lia[i + 1]; ++k) s -= f[k] * (VF)z[lja[k]];
-    z[i] = (VV)(s / f[d]);
-  }
+}
+
+template <typename VF, typename VV, bool LOWER>
+__global__ void k_ilu_solve_level(int32_t q0, int32_t q1, const int32_t *__restrict__ rows,
+                                  const int32_t *__restrict__ lia, const int32_t *__restrict__ lja,
+                                  const int32_t *__restrict__ ldiag, const VF *__restrict__ f,
+                                  const VV *__restrict__ r, VV *__restrict__ z, const int *__restrict__ done)
+{
+  if(done && *done) return;
+  const int64_t q = q0 + ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  if(q < q1) ilu_solve_row<VF, VV, LOWER>(rows[q], lia, lja, ldiag, f, r, z);
 }
 
 template <typename VV, typename VD>
@@ -966,6 +1027,7 @@ Krylov::~Krylov()
   cudaFreeHost(hred_);
   cudaFree(ilu_.blockStart); cudaFree(ilu_.perm); cudaFree(ilu_.lia); cudaFree(ilu_.lja);
   cudaFree(ilu_.ldiag); cudaFree(ilu_.srcPos); cudaFree(ilu_.vals); cudaFree(ilu_.status);
+  cudaFree(ilu_.rowsL); cudaFree(ilu_.rowsU); cudaFree(ilu_.lvlL); cudaFree(ilu_.lvlU);
   cudaFree(red_state_); cudaFree(gmres_); cudaFree(cg_);
   cudaFreeHost(h_gmres_); cudaFreeHost(h_cg_); cudaFreeHost(hflag_); cudaFreeHost(htol_);
   for(auto &g : graphs_) cudaGraphExecDestroy(g.second);
@@ -1124,8 +1186,120 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
     CK(cudaMemcpy(ilu_.lja, lja.data(), sizeof(int32_t) * ilu_.lnnz, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ilu_.ldiag, ldiag.data(), sizeof(int32_t) * n_, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ilu_.srcPos, src.data(), sizeof(int32_t) * ilu_.lnnz, cudaMemcpyHostToDevice));
+    FE_TRY(build_ilu_levels(lia, lja, ldiag));
   }
   return FE_OK;
+}
+
+// Level schedules of the factor's L and U parts and their segments (see
+// DeviceBlockILU).  A level is wide when its rows would keep one block of
+// 32 warps busy for several rounds.
+int Krylov::build_ilu_levels(const std::vector<int32_t> &lia, const std::vector<int32_t> &lja,
+                             const std::vector<int32_t> &ldiag)
+{
+  const int64_t n = n_;
+  constexpr int32_t WIDE = 256;  // rows
+  auto schedule = [&](bool lower, std::vector<int32_t> &rows, std::vector<int32_t> &lvl,
+                      std::vector<DeviceBlockILU::Segment> &seg) {
+    std::vector<int32_t> level(n, 0);
+    int32_t nl = 0;
+    if(lower) {
+      for(int64_t i = 0; i < n; ++i) {
+        int32_t m = 0;
+        for(int32_t k = lia[i]; k < ldiag[i]; ++k) m = std::max(m, level[lja[k]] + 1);
+        level[i] = m;
+        nl = std::max(nl, m + 1);
+      }
+    } else {
+      for(int64_t i = n - 1; i >= 0; --i) {
+        int32_t m = 0;
+        for(int32_t k = ldiag[i] + 1; k < lia[i + 1]; ++k) m = std::max(m, level[lja[k]] + 1);
+        level[i] = m;
+        nl = std::max(nl, m + 1);
+      }
+    }
+    lvl.assign(nl + 1, 0);
+    for(int64_t i = 0; i < n; ++i) lvl[level[i] + 1]++;
+    for(int32_t l = 0; l < nl; ++l) lvl[l + 1] += lvl[l];
+    rows.resize(n);
+    std::vector<int32_t> fill(lvl.begin(), lvl.end() - 1);
+    for(int64_t i = 0; i < n; ++i) rows[fill[level[i]]++] = (int32_t)i;  // ascending within a level
+    seg.clear();
+    for(int32_t l = 0; l < nl;) {
+      const int32_t cnt = lvl[l + 1] - lvl[l];
+      if(cnt > WIDE) {
+        seg.push_back({1, l, l + 1, cnt, lvl[l], lvl[l + 1]});
+        ++l;
+        continue;
+      }
+      int32_t e = l, r = 0;
+      while(e < nl && lvl[e + 1] - lvl[e] <= WIDE) {
+        r += lvl[e + 1] - lvl[e];
+        ++e;
+      }
+      seg.push_back({0, l, e, r, lvl[l], lvl[e]});
+      l = e;
+    }
+    return nl;
+  };
+  std::vector<int32_t> rl, ll, ru, lu;
+  ilu_.nLevL = schedule(true, rl, ll, ilu_.segL);
+  ilu_.nLevU = schedule(false, ru, lu, ilu_.segU);
+  CK(cudaMalloc(&ilu_.rowsL, sizeof(int32_t) * n));
+  CK(cudaMalloc(&ilu_.rowsU, sizeof(int32_t) * n));
+  CK(cudaMalloc(&ilu_.lvlL, sizeof(int32_t) * ll.size()));
+  CK(cudaMalloc(&ilu_.lvlU, sizeof(int32_t) * lu.size()));
+  CK(cudaMemcpy(ilu_.rowsL, rl.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ilu_.rowsU, ru.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ilu_.lvlL, ll.data(), sizeof(int32_t) * ll.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ilu_.lvlU, lu.data(), sizeof(int32_t) * lu.size(), cudaMemcpyHostToDevice));
+  return FE_OK;
+}
+
+template <typename VF>
+void Krylov::ilu_factor_levels(const double *values64, const float *values32)
+{
+  VF *f = (VF *)ilu_.vals;
+  (k_ilu_copy<VF><<<grid_for(ilu_.lnnz, 256, 4096), 256, 0, s_>>>(ilu_.lnnz, ilu_.srcPos, values64, values32, f),
+   ::feng::count_launch());
+  for(const auto &sg : ilu_.segL) {
+    if(sg.wide)
+      (k_ilu_factor_level<VF><<<(unsigned)(((int64_t)sg.rows * 32 + 255) / 256), 256, 0, s_>>>(
+           sg.q0, sg.q1, ilu_.rowsL, ilu_.lia, ilu_.lja, ilu_.ldiag, f, ilu_.status),
+       ::feng::count_launch());
+    else
+      (k_ilu_factor_run<VF><<<1, ILU_NARROW_THREADS, 0, s_>>>(sg.lv0, sg.lv1, ilu_.lvlL, ilu_.rowsL, ilu_.lia,
+                                                                ilu_.lja, ilu_.ldiag, f, ilu_.status),
+       ::feng::count_launch());
+  }
+}
+
+template <typename VF, typename VV>
+void Krylov::ilu_solve_levels(const VV *r, VV *z, const int *done)
+{
+  const VF *f = (const VF *)ilu_.vals;
+  for(const auto &sg : ilu_.segL) {
+    if(sg.wide)
+      (k_ilu_solve_level<VF, VV, true><<<(unsigned)(((int64_t)sg.rows * 32 + 255) / 256), 256, 0, s_>>>(
+           sg.q0, sg.q1, ilu_.rowsL, ilu_.lia, ilu_.lja, ilu_.ldiag, f, r, z, done),
+       ::feng::count_launch());
+    else
+      (k_ilu_solve_run<VF, VV, true><<<1, ILU_NARROW_THREADS, 0, s_>>>(sg.lv0, sg.lv1, ilu_.lvlL, ilu_.rowsL,
+                                                                         ilu_.lia, ilu_.lja, ilu_.ldiag, f, r, z,
+                                                                         done),
+       ::feng::count_launch());
+  }
+  for(const auto &sg : ilu_.segU) {
+    if(sg.wide)
+      (k_ilu_solve_level<VF, VV, false><<<(unsigned)(((int64_t)sg.rows * 32 + 255) / 256), 256, 0, s_>>>(
+           sg.q0, sg.q1, ilu_.rowsU, ilu_.lia, ilu_.lja, ilu_.ldiag, f, r, z, done),
+       ::feng::count_launch());
+    else
+      (k_ilu_solve_run<VF, VV, false><<<1, ILU_NARROW_THREADS, 0, s_>>>(sg.lv0, sg.lv1, ilu_.lvlU, ilu_.rowsU,
+                                                                          ilu_.lia, ilu_.lja, ilu_.ldiag, f, r, z,
+                                                                          done),
+       ::feng::count_launch());
+  }
 }
 
 namespace {
@@ -1222,15 +1396,8 @@ int Krylov::factor(const double *values64, const float *values32)
     if(opt.mixed) (k_inv_diag<float, float><<<g, 256, 0, s_>>>(n_, A_.diag, values32, diag32_, ilu_.status), ::feng::count_launch());
     else (k_inv_diag<double, double><<<g, 256, 0, s_>>>(n_, A_.diag, values64, diag_, ilu_.status), ::feng::count_launch());
   } else {
-    const int g = grid_for(ilu_.nBlocks, 64, 1 << 20);
-    if(opt.mixed)
-      (k_ilu_factor<float><<<g, 64, 0, s_>>>(ilu_.nBlocks, ilu_.blockStart, ilu_.perm, ilu_.lia,
-                                            ilu_.lja, ilu_.ldiag, ilu_.srcPos, nullptr, values32,
-                                            (float *)ilu_.vals, ilu_.status), ::feng::count_launch());
-    else
-      (k_ilu_factor<double><<<g, 64, 0, s_>>>(ilu_.nBlocks, ilu_.blockStart, ilu_.perm, ilu_.lia,
-                                             ilu_.lja, ilu_.ldiag, ilu_.srcPos, values64, nullptr,
-                                             (double *)ilu_.vals, ilu_.status), ::feng::count_launch());
+    if(opt.mixed) ilu_factor_levels<float>(nullptr, values32);
+    else ilu_factor_levels<double>(values64, nullptr);
   }
   CK(cudaGetLastError());
   int hs = 0;
@@ -1253,9 +1420,7 @@ void Krylov::precond64(const double *r, double *z, const int *done)
   } else if(opt.precond == 2) {
     (k_jacobi<double, double><<<grid_for(n_, 256, 4096), 256, 0, s_>>>(n_, diag_, r, z, done), ::feng::count_launch());
   } else {
-    (k_ilu_solve<double, double><<<grid_for(ilu_.nBlocks, 64, 1 << 20), 64, 0, s_>>>(
-      ilu_.nBlocks, ilu_.blockStart, ilu_.perm, ilu_.lia, ilu_.lja, ilu_.ldiag,
-      (const double *)ilu_.vals, r, z, done), ::feng::count_launch());
+    ilu_solve_levels<double, double>(r, z, done);
   }
 }
 
@@ -1268,9 +1433,7 @@ void Krylov::precond32(const float *r, float *z, const int *done)
   } else if(opt.precond == 2) {
     (k_jacobi<float, float><<<grid_for(n_, 256, 4096), 256, 0, s_>>>(n_, diag32_, r, z, done), ::feng::count_launch());
   } else {
-    (k_ilu_solve<float, float><<<grid_for(ilu_.nBlocks, 64, 1 << 20), 64, 0, s_>>>(
-      ilu_.nBlocks, ilu_.blockStart, ilu_.perm, ilu_.lia, ilu_.lja, ilu_.ldiag,
-      (const float *)ilu_.vals, r, z, done), ::feng::count_launch());
+    ilu_solve_levels<float, float>(r, z, done);
   }
 }
 

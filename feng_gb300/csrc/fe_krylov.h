@@ -39,6 +39,21 @@ struct DeviceBlockILU {
   int64_t lnnz = 0;
   void *vals = nullptr;           // [lnnz] factor values (double or float)
   int *status = nullptr;          // device flag: 0 ok, 1 zero pivot, 2 non-finite
+  // Level schedules: a row's lower (upper) level is one more than the
+  // highest level of the rows its L (U) part references, so the rows of one
+  // level are independent.  rowsL/rowsU: rows by level, ascending within a
+  // level; lvlL/lvlU: [nLevels+1] offsets.  Segments: runs of narrow levels
+  // processed by one block (a block barrier between levels) or one wide
+  // level launched over many blocks.
+  int32_t *rowsL = nullptr, *lvlL = nullptr, *rowsU = nullptr, *lvlU = nullptr;
+  struct Segment {
+    int wide;          // 1: one level over many blocks; 0: levels [lv0, lv1) in one block
+    int32_t lv0, lv1;
+    int32_t rows;      // rows of the segment
+    int32_t q0, q1;    // their range in rowsL / rowsU
+  };
+  std::vector<Segment> segL, segU;
+  int32_t nLevL = 0, nLevU = 0;
 };
 
 // Host description of the multigrid-based preconditioners:
@@ -112,6 +127,12 @@ class Krylov {
                          int maxIt, KrylovStats &st);
   int solve_cg64(const double *vals, const double *b, double *x, double tolAbs, int maxIt,
                  KrylovStats &st);
+  int build_ilu_levels(const std::vector<int32_t> &lia, const std::vector<int32_t> &lja,
+                       const std::vector<int32_t> &ldiag);
+  template <typename VF>
+  void ilu_factor_levels(const double *values64, const float *values32);
+  template <typename VF, typename VV>
+  void ilu_solve_levels(const VV *r, VV *z, const int *done);
   void precond64(const double *r, double *z, const int *skip);
   void precond32(const float *r, float *z, const int *skip);
   double dot(const double *x, const double *y);

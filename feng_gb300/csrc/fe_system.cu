@@ -1409,6 +1409,31 @@ int SystemCUDA::getRHS(double *hostRhs) const
   return FE_OK;
 }
 
+// One application z = M^-1 r of the current preconditioner (built from the
+// current matrix if that changed), host vectors of nInc entries.
+int SystemCUDA::applyPreconditioner(const double *hostR, double *hostZ)
+{
+  FE_TRY(ensureMatrixZeroed());
+  FE_TRY(factorIfPending());
+  double *r = nullptr, *z = nullptr;
+  CK(cudaMalloc(&r, sizeof(double) * nInc_));
+  if(cudaMalloc(&z, sizeof(double) * nInc_) != cudaSuccess) {
+    cudaFree(r);
+    set_error("device allocation failed");
+    return FE_CUDA_FAIL;
+  }
+  int st = FE_OK;
+  if(cudaMemcpyAsync(r, hostR, sizeof(double) * nInc_, cudaMemcpyHostToDevice, s_) != cudaSuccess) st = FE_CUDA_FAIL;
+  if(st == FE_OK) st = kry_.applyPrecond(r, z);
+  if(st == FE_OK && cudaMemcpyAsync(hostZ, z, sizeof(double) * nInc_, cudaMemcpyDeviceToHost, s_) != cudaSuccess)
+    st = FE_CUDA_FAIL;
+  if(cudaStreamSynchronize(s_) != cudaSuccess) st = FE_CUDA_FAIL;
+  cudaFree(r);
+  cudaFree(z);
+  if(st == FE_CUDA_FAIL) set_error("preconditioner application failed on the device");
+  return st;
+}
+
 int SystemCUDA::getDu(double *hostDu) const
 {
   CK(cudaMemcpyAsync(hostDu, du_, sizeof(double) * nInc_, cudaMemcpyDeviceToHost, s_));

@@ -110,6 +110,7 @@ class SystemCUDA {
   int getMatrix(double *hostValues) const;  // FP64 copy of the current values
   int getRHS(double *hostRhs) const;
   int getDu(double *hostDu) const;
+  int applyPreconditioner(const double *hostR, double *hostZ);
   int validateColoring() const;
   // Error norms of feNorm (src/feNorm.cpp:323-391, 1399-1443) on the
   // system's quadrature rule: normPoints gives the rule's nodes on every

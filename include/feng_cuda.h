@@ -357,6 +357,9 @@ int fe_cuda_correct_solution(fe_cuda_system *s);
 int fe_cuda_get_matrix(const fe_cuda_system *s, double *values);
 int fe_cuda_get_rhs(const fe_cuda_system *s, double *rhs);
 int fe_cuda_get_du(const fe_cuda_system *s, double *du);
+/* One application z = M^-1 r of the preconditioner (PETSc's PCApply),
+ * built from the current matrix first if needed; r, z host arrays [n_inc]. */
+int fe_cuda_apply_preconditioner(fe_cuda_system *s, const double *r, double *z);
 
 /* ---- Newton driver (solveNewtonRaphson, src/feNonLinearSolver.cpp:38-181) */
 int fe_cuda_newton(fe_cuda_system *s, const fe_newton_options *o, fe_newton_stats *st);

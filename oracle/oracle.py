@@ -163,6 +163,22 @@ class OracleProblem:
             self.lib.fo_precond_destroy(pc)
 
 
+    def apply_ilu(self, values, r, block_of_row=None):
+        """z = (LU)^-1 r with the serial (block-Jacobi) ILU(0) of values."""
+        k = self.keep
+        blk = None if block_of_row is None else np.ascontiguousarray(block_of_row, np.int32)
+        pc = self.lib.fo_precond_create(1, self.n_inc, _p(k["ia"]), _p(k["ja"]), _p(blk), None, None, 1.0)
+        try:
+            vals = np.ascontiguousarray(values, np.float64)
+            if self.lib.fo_precond_factor(pc, _p(vals)) != 0:
+                raise RuntimeError("oracle ILU(0): zero pivot")
+            z = np.zeros(self.n_inc)
+            self.lib.fo_precond_apply(pc, _p(np.ascontiguousarray(r, np.float64)), _p(z))
+            return z
+        finally:
+            self.lib.fo_precond_destroy(pc)
+
+
 # ---- learned-guess MLP (oracle/mlp_oracle.c) ----------------------------------
 
 def _f64(a):
