@@ -58,7 +58,8 @@ def parse():
     ap.add_argument("--transient-steps", type=int, default=400,
                     help="BDF2 steps of the lid-driven cavity leg (configuration C4; 0: skip)")
     ap.add_argument("--legs", type=int, default=1,
-                    help="1: also time the diffusion 64x64 (C1) and Kovasznay 512x512 (C3) configurations")
+                    help="1: also time the diffusion 64x64 (C1), Kovasznay 512x512 (C3) and 64^3 tetrahedra (C5) "
+                         "configurations")
     return ap.parse_args()
 
 
@@ -422,6 +423,61 @@ def c3_leg(n=512, reps=2):
     return out
 
 
+def c5_leg(n=64, reps=5):
+    """Config C5's system on the device: the unit cube, n^3 cells of 6 Kuhn
+    tetrahedra jittered by +-0.05 h (seed 1), P2-P1 Taylor-Hood with the
+    unsteady Navier-Stokes forms (transient mass, convection at Re 100,
+    stress, divergence, body force sin(pi x) sin(pi y) sin(pi z) in x),
+    degree-5 rule (exact for the forms' polynomial integrands).  Times the
+    host set-up, the system creation (device element-to-nonzero map), and
+    residual and Jacobian assembly (FP64 and mixed: FP32 Jacobian) with the
+    L2 flushed before each run.  Assembly bytes per launch:
+    nnz s_A + nElm 34 4 + nVert 3 8 + nDofs 8 k_in + nInc 8."""
+    import feng_gb300 as fe
+    from feng_gb300._lib import check
+    out = {"workload": f"cube_{n}^3_kuhn_tets_p2p1_navier_stokes_re100"}
+    t0 = time.perf_counter()
+    mesh = fe.Mesh3DP1.generate_cube(n, jitter=0.05, seed=1)
+    u = fe.createFiniteElementSpace(mesh, fe.VECTOR_LAGRANGE, 2, "U", "Domaine", 5)
+    uB = fe.createFiniteElementSpace(mesh, fe.VECTOR_LAGRANGE, 2, "U", "Bord", 5)
+    p = fe.createFiniteElementSpace(mesh, fe.LAGRANGE, 1, "P", "Domaine", 5)
+    num = fe.feMetaNumber(mesh, [u, uB, p], [uB])
+    forms = [fe.createBilinearForm([u], fe.feSysElm_TransientVectorMass(1.0)),
+             fe.createBilinearForm([u], fe.feSysElm_VectorConvectiveAcceleration(1.0)),
+             fe.createBilinearForm([p, u], fe.feSysElm_MixedDivergence(1.0)),
+             fe.createBilinearForm([u, p], fe.feSysElm_DivergenceNewtonianStress(-1.0, 1.0 / 100.0)),
+             fe.createBilinearForm([u], fe.feSysElm_VectorSource(fe.api.SRC_SIN3_BODY, (1.0,)))]
+    out["host_setup_s"] = time.perf_counter() - t0
+    nvert = mesh.sizes()[0]
+    peak, peak_kind = measured_peaks()
+    for prec in ("fp64", "mixed"):
+        t0 = time.perf_counter()
+        sys_ = fe.createLinearSystem(fe.CUDA, forms, num, fe.LinearSolverOptions(precond="jacobi", precision=prec))
+        sys_.synchronize()
+        create_s = time.perf_counter() - t0
+        rng = np.random.default_rng(1)
+        sys_.setSolution(rng.uniform(-1, 1, sys_.nDofs), rng.uniform(-1, 1, sys_.nDofs))
+        sys_.setTime(0.0, 300.0)
+        ph = {}
+        for which, name in ((0, "residual"), (1, "jacobian")):
+            ms = C.c_double()
+            check(sys_.lib.fe_cuda_bench_phase(sys_._h, which, reps, 256 << 20, C.byref(ms)))
+            ph[name] = ms.value
+        sA = 8 if prec == "fp64" else 4
+        base = sys_.nElm * 34 * 4 + nvert * 3 * 8 + sys_.nDofs * 8 * 2
+        by = {"residual": base + sys_.nInc * 8, "jacobian": sys_.nnz * sA + base}
+        out[prec] = {"system_create_s": create_s,
+                     **{f"{k}_ms": v for k, v in ph.items()},
+                     "assembly_melem_s": sys_.nElm / ((ph["residual"] + ph["jacobian"]) / 1e3) / 1e6,
+                     "roofline_jacobian": {"bound": "hbm", "bytes_per_launch": by["jacobian"],
+                                           "achieved": by["jacobian"] / (ph["jacobian"] / 1e3) / 1e9,
+                                           "peak": peak, "unit": "GB/s", "peak_source": peak_kind,
+                                           "frac": by["jacobian"] / (ph["jacobian"] / 1e3) / 1e9 / peak}}
+        out.update(elements=sys_.nElm, unknowns=sys_.nInc, dofs=sys_.nDofs, nnz=sys_.nnz, colors=sys_.nColors)
+        del sys_
+    return out
+
+
 def transient_leg(steps, n=384, re=1000.0, dt=0.005):
     """Config C4: lid-driven cavity from rest, BDF2 dt 0.005, `steps` steps.
     Arms: the plain FP64 solver with the reference's guess (previous
@@ -567,6 +623,7 @@ def main():
     if args.legs:
         line["c1"] = c1_leg()
         line["c3"] = c3_leg()
+        line["c5"] = c5_leg()
     if args.transient_steps > 0:
         line["transient"] = transient_leg(args.transient_steps)
     if rank == 0:

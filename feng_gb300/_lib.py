@@ -63,7 +63,8 @@ class StepStats(C.Structure):
                 ("status", C.c_int32), ("guess_used", C.c_int32), ("t", C.c_double),
                 ("residual_ref", C.c_double), ("residual_guess", C.c_double),
                 ("residual_extrap", C.c_double), ("residual", C.c_double), ("step_ms", C.c_double),
-                ("guess_ms", C.c_double), ("train_ms", C.c_double), ("train_loss", C.c_double)]
+                ("guess_ms", C.c_double), ("train_ms", C.c_double), ("train_loss", C.c_double),
+                ("guess_scale", C.c_double)]
 
 
 class NewtonStats(C.Structure):

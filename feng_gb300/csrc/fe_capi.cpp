@@ -1115,6 +1115,7 @@ extern "C" int fe_cuda_transient_steps(fe_transient *t, int nsteps, fe_step_stat
       o.guess_ms = st.guessMs;
       o.train_ms = st.trainMs;
       o.train_loss = st.trainLoss;
+      o.guess_scale = st.guessScale;
     }
     if(r != FE_OK) return r;
   }

@@ -1476,6 +1476,12 @@ int Krylov::spmvHot()
   return FE_OK;
 }
 
+__global__ void k_f32_to_f64(int64_t n, const float *__restrict__ x, double *__restrict__ y)
+{
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (double)x[i];
+}
+
 int Krylov::applyPrecond(const double *r, double *z)
 {
   if(!factoredOk_) {
@@ -1484,8 +1490,10 @@ int Krylov::applyPrecond(const double *r, double *z)
   }
   if(opt.mixed) {
     const int gv = grid_for(n_, 256, 2048);
+    float *zf = Z32_ ? Z32_ : w32_;
     (k_to_f32<<<gv, 256, 0, s_>>>(n_, r, v32_, nullptr), ::feng::count_launch());
-    precond32(v32_, Z32_ ? Z32_ : w32_, nullptr);
+    precond32(v32_, zf, nullptr);
+    if(z) (k_f32_to_f64<<<gv, 256, 0, s_>>>(n_, zf, z), ::feng::count_launch());
   } else {
     precond64(r, z, nullptr);
   }

@@ -116,6 +116,7 @@ class Krylov {
   void spmv32(const float *values, const double *x, double *y);
   // One preconditioner application z = M^-1 r (the FP32 path rounds r).
   int applyPrecond(const double *r, double *z);
+  double dot(const double *x, const double *y);
   double norm2(const double *x);
   double norminf(const double *x);
   KrylovOptions opt;
@@ -135,7 +136,6 @@ class Krylov {
   void ilu_solve_levels(const VV *r, VV *z, const int *done);
   void precond64(const double *r, double *z, const int *skip);
   void precond32(const float *r, float *z, const int *skip);
-  double dot(const double *x, const double *y);
 
   DeviceCSR A_;
   DeviceBlockILU ilu_;

@@ -1352,6 +1352,12 @@ int SystemCUDA::benchPhase(int which, int reps, size_t flushBytes, double *avgMs
         // as in a Newton step: zeroed matrix, then the Jacobian (the
         // row-owned assembly writes the values, the colored scatter adds)
         if(useRows_) zeroPending_ = true;
+        else {
+          // the colored scatter adds: its zeroing pass is part of the phase
+          zeroPending_ = true;
+          status = ensureMatrixZeroed();
+          if(status != FE_OK) break;
+        }
         status = launch_matrix();
         break;
       case 2:
@@ -1432,6 +1438,18 @@ int SystemCUDA::applyPreconditioner(const double *hostR, double *hostZ)
   cudaFree(z);
   if(st == FE_CUDA_FAIL) set_error("preconditioner application failed on the device");
   return st;
+}
+
+int SystemCUDA::jacobianTimes(const double *x, double *y)
+{
+  if(!matrixValid_ || zeroPending_) {
+    set_error("no assembled Jacobian");
+    return FE_INVALID_ARG;
+  }
+  if(vals64_) kry_.spmv64(vals64_, x, y);
+  else kry_.spmv32(vals32_, x, y);
+  CK(cudaGetLastError());
+  return FE_OK;
 }
 
 int SystemCUDA::getDu(double *hostDu) const

@@ -111,6 +111,9 @@ class SystemCUDA {
   int getRHS(double *hostRhs) const;
   int getDu(double *hostDu) const;
   int applyPreconditioner(const double *hostR, double *hostZ);
+  // y = J x with the Jacobian last assembled (device vectors of nInc
+  // entries); FE_INVALID_ARG when no assembled Jacobian is held.
+  int jacobianTimes(const double *x, double *y);
   int validateColoring() const;
   // Error norms of feNorm (src/feNorm.cpp:323-391, 1399-1443) on the
   // system's quadrature rule: normPoints gives the rule's nodes on every

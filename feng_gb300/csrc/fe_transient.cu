@@ -108,6 +108,21 @@ __global__ void k_apply(int64_t nNodes, int64_t nInc, const int32_t *__restrict_
   }
 }
 
+// d = um - ue on the unknowns.
+__global__ void k_diff(int64_t n, const double *__restrict__ a, const double *__restrict__ b, double *__restrict__ d)
+{
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    d[i] = a[i] - b[i];
+}
+
+// um = ue + alpha d on the unknowns (the essential entries of um are ue's).
+__global__ void k_add_scaled(int64_t n, const double *__restrict__ ue, double alpha, const double *__restrict__ d,
+                             double *__restrict__ um)
+{
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    um[i] = ue[i] + alpha * d[i];
+}
+
 // Training targets (u^{n+1} - ue) / s with their mask.
 __global__ void k_targets(int64_t nNodes, int64_t nInc, const int32_t *__restrict__ nd, const double *__restrict__ u,
                           const double *__restrict__ ue, const float *__restrict__ sig, float *__restrict__ T,
@@ -151,6 +166,8 @@ Transient::~Transient()
   cudaFree(h3_);
   cudaFree(ue_);
   cudaFree(um_);
+  cudaFree(dv_);
+  cudaFree(jd_);
   cudaFree(X_);
   cudaFree(Y_);
   cudaFree(T_);
@@ -180,6 +197,8 @@ int Transient::init(SystemCUDA *sys, const TransientOptions &o, const NewtonOpti
   CKT(cudaMalloc(&h3_, sizeof(double) * nDofs));
   CKT(cudaMalloc(&ue_, sizeof(double) * nDofs));
   CKT(cudaMalloc(&um_, sizeof(double) * nDofs));
+  CKT(cudaMalloc(&dv_, sizeof(double) * std::max<int64_t>(1, sys->nInc())));
+  CKT(cudaMalloc(&jd_, sizeof(double) * std::max<int64_t>(1, sys->nInc())));
   CKT(cudaEventCreate(&e0_));
   CKT(cudaEventCreate(&e1_));
   CKT(cudaEventCreate(&e2_));
@@ -399,12 +418,15 @@ int Transient::step(StepStats &st)
     }
     bool residualReady = false;
     if(learn && trained_ > 0 && st.step >= o_.useFrom) {
-      // One learned candidate (the extrapolation plus the network's
-      // correction), judged against the extrapolation by the FP64 residual;
-      // the extrapolation is kept when the candidate does not beat it.  The
-      // candidate's residual is evaluated last, so when it wins that
-      // residual is Newton's first one.  A non-finite candidate residual
-      // never wins (the comparison is false for NaN).
+      // One learned candidate ue + alpha d (d: the network's correction),
+      // judged against the extrapolation by the FP64 residual; the
+      // extrapolation is kept when the candidate does not beat it.  alpha
+      // minimises the linearised residual ||R(ue) - alpha J d||_2 with the
+      // Jacobian still held from the previous step: alpha = <R, J d> /
+      // <J d, J d>, kept in [0, 2] (1 without a Jacobian).  The candidate's
+      // residual is evaluated last, so when it wins that residual is
+      // Newton's first one.  A non-finite candidate residual never wins
+      // (the comparison is false for NaN).
       FE_TRY(mlp_.forward(X_, nNodes_, Y_));
       double re = 0., rm = 0.;
       CKT(cudaMemcpyAsync(sys_->dU(), ue_, bytes, cudaMemcpyDeviceToDevice, s));
@@ -414,6 +436,15 @@ int Transient::step(StepStats &st)
       (k_apply<<<grid_of(nNodes_), 256, 0, s>>>(nNodes_, nInc, nodeDof_, Y_, sig_, 1.f, ue_, um_),
        ::feng::count_launch());
       CKT(cudaGetLastError());
+      double alpha = 1.;
+      (k_diff<<<grid_of(nInc), 256, 0, s>>>(nInc, um_, ue_, dv_), ::feng::count_launch());
+      if(sys_->jacobianTimes(dv_, jd_) == FE_OK) {
+        const double jj = sys_->krylov().dot(jd_, jd_), rj = sys_->krylov().dot(sys_->dRhs(), jd_);
+        if(jj > 0 && std::isfinite(jj) && std::isfinite(rj)) alpha = std::min(2., std::max(0., rj / jj));
+        (k_add_scaled<<<grid_of(nInc), 256, 0, s>>>(nInc, ue_, alpha, dv_, um_), ::feng::count_launch());
+        CKT(cudaGetLastError());
+      }
+      st.guessScale = alpha;
       CKT(cudaMemcpyAsync(sys_->dU(), um_, bytes, cudaMemcpyDeviceToDevice, s));
       const int r = residualNorm(&rm);
       if(r != FE_OK && r != FE_NONFINITE) return r;

@@ -54,6 +54,7 @@ struct StepStats {
   double residual = 0;          // final ||R||inf
   double stepMs = 0, guessMs = 0, trainMs = 0;
   double trainLoss = -1;        // loss of the last Adam step of this time step (-1: none)
+  double guessScale = 0;        // step length alpha of the learned correction (0: none formed)
 };
 
 class Transient {
@@ -88,6 +89,7 @@ class Transient {
   float *geo_ = nullptr;        // [nNodes x 6] geometry features
   double *h3_ = nullptr;        // u^{n-2}
   double *ue_ = nullptr, *um_ = nullptr;  // extrapolated and learned guesses
+  double *dv_ = nullptr, *jd_ = nullptr;  // learned correction d (unknowns) and J d
   float *X_ = nullptr, *Y_ = nullptr, *T_ = nullptr, *M_ = nullptr;
   float *sig_ = nullptr;        // [2] scales of the last solution differences (velocity, pressure)
   float *loss_ = nullptr;       // [1] last Adam loss

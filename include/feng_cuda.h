@@ -426,9 +426,12 @@ int fe_cuda_apply_periodicity(fe_cuda_system *s);
  *                         three solutions and 6 geometry features) trained online
  *                         with device forward/backward/Adam kernels on the
  *                         corrections of converged steps from step train_from;
- *                         from step use_from the extrapolation and the learned
- *                         guess are both evaluated with the FP64 residual and the
- *                         smaller one is used (no counterpart in the reference). */
+ *                         from step use_from the correction d is scaled by the
+ *                         step length alpha minimising the linearised residual
+ *                         with the Jacobian held from the previous step, the
+ *                         extrapolation and ue + alpha d are both evaluated with
+ *                         the FP64 residual and the smaller one is used (no
+ *                         counterpart in the reference). */
 #define FE_GUESS_PREVIOUS 0
 #define FE_GUESS_EXTRAPOLATE 1
 #define FE_GUESS_LEARNED 2
@@ -459,6 +462,7 @@ typedef struct fe_step_stats {
   double guess_ms;         /* ... up to the end of the guess */
   double train_ms;         /* ... of the training after the step */
   double train_loss;       /* loss of the last Adam step (-1: no training) */
+  double guess_scale;      /* step length alpha of the learned correction (0: none formed) */
 } fe_step_stats;
 int fe_cuda_transient_create(fe_cuda_system *s, const fe_transient_options *o,
                              const fe_newton_options *newton, fe_transient **out);
