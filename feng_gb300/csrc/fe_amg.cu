@@ -547,7 +547,8 @@ int AMGDevice::upload(const AMGHierarchy &H, const AMGParams &p, int fp32, cudaS
     for(size_t i = 0; i < dg.size(); ++i) dg[i] = 1.0 / h.dinv[i];
     FE_TRY(fp32 ? upload_vec<float>(&L.diag, dg) : upload_vec<double>(&L.diag, dg));
     // room for two interleaved components (vcycle2)
-    for(void **v : {&L.x, &L.b, &L.r, &L.d0, &L.d1}) CKA(cudaMalloc(v, 2 * vs * std::max<int64_t>(1, L.n)));
+    // room for up to three interleaved components per row
+    for(void **v : {&L.x, &L.b, &L.r, &L.d0, &L.d1}) CKA(cudaMalloc(v, 3 * vs * std::max<int64_t>(1, L.n)));
     if(l + 1 < H.levels.size()) {
       L.nc = h.P.m;
       L.lanesP = lanes_for(h.P);
@@ -702,6 +703,18 @@ bool AMGDevice::vcycle2_32(const float *b, float *x, const OutMap *om)
   vcycle_t<float, 2>(0, b, x);
   out_ = OutMap();
   return outWritten_;
+}
+
+void AMGDevice::vcycle3_64(const double *b, double *x)
+{
+  out_ = OutMap();
+  vcycle_t<double, 3>(0, b, x);
+}
+
+void AMGDevice::vcycle3_32(const float *b, float *x)
+{
+  out_ = OutMap();
+  vcycle_t<float, 3>(0, b, x);
 }
 
 void AMGDevice::fineStep2()

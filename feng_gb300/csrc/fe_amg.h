@@ -72,6 +72,10 @@ class AMGDevice {
   // returns true; x does not hold the result), otherwise x holds it.
   bool vcycle2_64(const double *b, double *x, const OutMap *om = nullptr);
   bool vcycle2_32(const float *b, float *x, const OutMap *om = nullptr);
+  // Three interleaved components (b[3 i + c]): the velocity of tetrahedral
+  // Taylor-Hood systems, one pass over each level operator; x holds the result.
+  void vcycle3_64(const double *b, double *x);
+  void vcycle3_32(const float *b, float *x);
   // y = A x with the finest operator.
   void spmv64(const double *x, double *y);
   void spmv32(const float *x, float *y);

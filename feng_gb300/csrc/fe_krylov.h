@@ -70,6 +70,7 @@ struct PrecondInfo {
   const HostCSR *massV = nullptr;        // scalar P2 mass on the nodes (same pattern as lap)
   const HostCSR *lapP = nullptr;         // P1 stiffness on the pressure unknowns (kind 4)
   std::vector<int32_t> nodeDofX, nodeDofY;  // unknown DOF of each node (per component)
+  std::vector<int32_t> nodeDofZ;         // third velocity component (tetrahedra; empty in 2D)
   std::vector<int32_t> pRows;            // pressure unknowns (kind 4)
   std::vector<double> pMass;             // lumped pressure mass of pRows
   double sigma = 1, divu = 1;            // DIV_NEWTONIAN_STRESS / MIXED_DIVERGENCE coefficients

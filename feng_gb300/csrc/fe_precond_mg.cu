@@ -39,6 +39,12 @@ struct Krylov::MG {
   int kind = 0;
   int64_t nNodes = 0, nP = 0;
   int32_t *dofX = nullptr, *dofY = nullptr, *pRows = nullptr;
+  // Tetrahedral Taylor-Hood: three components, slot q = 3 k + c of node k
+  // is row dofC[q]; vectors bxy / zxy then hold the three components
+  // interleaved.  nc = 2 on triangles (the paired kernels above).
+  int nc = 2;
+  int32_t *dofC = nullptr;
+  double vfac = 1.5;  // diag(A_xx) / (mu diag(K)) of the symmetric-gradient operator: 1 + 1/dim
   int32_t *upIa = nullptr, *upPos = nullptr, *upCol = nullptr;  // G block, rows = velocity slot 2k+c
   void *gVals = nullptr;  // the G block's values, gathered contiguous at each factor()
   int64_t nG = 0;
@@ -71,7 +77,7 @@ struct Krylov::MG {
     cudaFree(zy); cudaFree(dsum); cudaFree(ir); cudaFree(iz); cudaFree(ip); cudaFree(iq);
     cudaFree(part); cudaFree(scal); cudaFree(dnIa); cudaFree(dnPos); cudaFree(dnCol); cudaFree(slotOf);
     cudaFree(pMassDev); cudaFree(tP); cudaFree(consts); cudaFree(bxy); cudaFree(zxy); cudaFree(gVals);
-    cudaFree(pr); cudaFree(pz); cudaFree(count);
+    cudaFree(pr); cudaFree(pz); cudaFree(count); cudaFree(dofC);
   }
   template <typename V> void solveK(const V *b, V *x, cudaStream_t st);
 };
@@ -444,6 +450,56 @@ __global__ void k_vel_out(int64_t nN, const int32_t *__restrict__ dofX, const in
   }
 }
 
+// Three-component variants (tetrahedra): slot q = nc k + c.
+// b[q] = r_u - G z_p on slot q.
+template <typename V>
+__global__ void k_vel_rhs_nc(int64_t nq, const int32_t *__restrict__ dofC, const int32_t *__restrict__ upIa,
+                             const int32_t *__restrict__ upCol, const V *__restrict__ g, const V *__restrict__ r,
+                             const V *__restrict__ z, V *__restrict__ b, const int *__restrict__ skip)
+{
+  if(skip && *skip) return;
+  for(int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (int64_t)gridDim.x * blockDim.x) {
+    V t = r[dofC[q]];
+    for(int32_t e = upIa[q]; e < upIa[q + 1]; ++e) t -= g[e] * z[upCol[e]];
+    b[q] = t;
+  }
+}
+
+template <typename V>
+__global__ void k_vel_out_nc(int64_t nq, const int32_t *__restrict__ dofC, const V *__restrict__ zc,
+                             const double *__restrict__ consts, V *__restrict__ z, const int *__restrict__ skip)
+{
+  if(skip && *skip) return;
+  const V f = (V)consts[0];
+  for(int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (int64_t)gridDim.x * blockDim.x)
+    z[dofC[q]] = zc[q] * f;
+}
+
+// g = G c per slot (row sums of the G block).
+template <typename V>
+__global__ void k_gsum_nc(int64_t nq, const int32_t *__restrict__ upIa, const int32_t *__restrict__ upPos,
+                          const V *__restrict__ a, V *__restrict__ b)
+{
+  for(int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.;
+    for(int32_t e = upIa[q]; e < upIa[q + 1]; ++e) s += (double)a[upPos[e]];
+    b[q] = (V)s;
+  }
+}
+
+// t_p = (D w)_p with w given per slot.
+template <typename V>
+__global__ void k_dw_nc(int64_t nP, const int32_t *__restrict__ dnIa, const int32_t *__restrict__ dnPos,
+                        const int32_t *__restrict__ dnCol, const int32_t *__restrict__ slotOf,
+                        const V *__restrict__ a, const V *__restrict__ w, double *__restrict__ t)
+{
+  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nP; k += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.;
+    for(int32_t e = dnIa[k]; e < dnIa[k + 1]; ++e) s += (double)a[dnPos[e]] * (double)w[slotOf[dnCol[e]]];
+    t[k] = s;
+  }
+}
+
 template <typename T>
 int up(T **dst, const std::vector<T> &v)
 {
@@ -476,6 +532,12 @@ int Krylov::setup_mg(const PrecondInfo &pi)
   ap.chebyDegree = pi.chebyDegree;
   M.params = ap;
   M.inner = pi.innerIterations;
+  M.nc = pi.nodeDofZ.empty() ? 2 : 3;
+  M.vfac = M.nc == 3 ? 4.0 / 3.0 : 1.5;
+  if(M.nc == 3 && (M.kind != 4 || M.inner > 0 || (int64_t)pi.nodeDofZ.size() != M.nNodes)) {
+    set_error("three-component multigrid: Taylor-Hood, one V-cycle per application, a DOF per node");
+    return FE_INVALID_ARG;
+  }
   if(M.kind == 4) {
     M.lapH = *pi.lap;
     if(pi.massV) M.massH = *pi.massV;
@@ -490,7 +552,7 @@ int Krylov::setup_mg(const PrecondInfo &pi)
   const size_t vs = M.fp32 ? sizeof(float) : sizeof(double);
   for(void **v : {&M.bx, &M.by, &M.zx, &M.zy, &M.ir, &M.iz, &M.ip, &M.iq})
     CKM(cudaMalloc(v, vs * M.nNodes));
-  for(void **v : {&M.bxy, &M.zxy}) CKM(cudaMalloc(v, 2 * vs * M.nNodes));
+  for(void **v : {&M.bxy, &M.zxy}) CKM(cudaMalloc(v, 3 * vs * M.nNodes));
   CKM(cudaMalloc(&M.dsum, sizeof(double)));
   CKM(cudaMalloc(&M.part, sizeof(double) * NPART));
   CKM(cudaMalloc(&M.scal, sizeof(double) * 4));
@@ -519,15 +581,21 @@ int Krylov::setup_mg(const PrecondInfo &pi)
       if(p < 0 || p >= n_) { set_error("pressure row out of range"); return FE_INVALID_ARG; }
       isP[p] = 1;
     }
-    std::vector<int32_t> ia2(2 * M.nNodes + 1, 0), pos, col;
+    const int nc = M.nc;
+    auto dofOf = [&](int64_t k, int c) {
+      return c == 0 ? pi.nodeDofX[k] : c == 1 ? pi.nodeDofY[k] : pi.nodeDofZ[k];
+    };
+    std::vector<int32_t> ia2(nc * M.nNodes + 1, 0), pos, col, dofC(nc * M.nNodes);
     for(int64_t k = 0; k < M.nNodes; ++k)
-      for(int c = 0; c < 2; ++c) {
-        const int32_t d = c == 0 ? pi.nodeDofX[k] : pi.nodeDofY[k];
+      for(int c = 0; c < nc; ++c) {
+        const int32_t d = dofOf(k, c);
         if(d < 0 || d >= n_) { set_error("node DOF out of range"); return FE_INVALID_ARG; }
+        dofC[nc * k + c] = d;
         for(int32_t e = hia[d]; e < hia[d + 1]; ++e)
           if(isP[hja[e]]) { pos.push_back(e); col.push_back(hja[e]); }
-        ia2[2 * k + c + 1] = (int32_t)pos.size();
+        ia2[nc * k + c + 1] = (int32_t)pos.size();
       }
+    if(nc == 3) FE_TRY(up(&M.dofC, dofC));
     FE_TRY(up(&M.upIa, ia2));
     FE_TRY(up(&M.upPos, pos));
     M.nG = (int64_t)pos.size();
@@ -536,10 +604,8 @@ int Krylov::setup_mg(const PrecondInfo &pi)
     FE_TRY(up(&M.pRows, pi.pRows));
     // D block (pressure rows -> velocity columns) and the slot of each velocity DOF.
     std::vector<int32_t> slot(n_, -1);
-    for(int64_t k = 0; k < M.nNodes; ++k) {
-      slot[pi.nodeDofX[k]] = (int32_t)(2 * k);
-      slot[pi.nodeDofY[k]] = (int32_t)(2 * k + 1);
-    }
+    for(int64_t k = 0; k < M.nNodes; ++k)
+      for(int c = 0; c < nc; ++c) slot[dofOf(k, c)] = (int32_t)(nc * k + c);
     std::vector<int32_t> dia(M.nP + 1, 0), dpos, dcol;
     for(int64_t k = 0; k < M.nP; ++k) {
       const int32_t p = pi.pRows[k];
@@ -587,7 +653,7 @@ int Krylov::factor_mg(const double *values64, const float *values32)
     std::vector<double> sc(M.nP);
     std::vector<float> sc32(M.nP);
     for(int64_t k = 0; k < M.nP; ++k) {
-      sc[k] = -M.s / (1.5 * M.sigma * M.divu * M.pMass[k]);
+      sc[k] = -M.s / (M.vfac * M.sigma * M.divu * M.pMass[k]);
       sc32[k] = (float)sc[k];
     }
     CKM(cudaMemcpyAsync(M.pScale64, sc.data(), sizeof(double) * M.nP, cudaMemcpyHostToDevice, s_));
@@ -598,7 +664,20 @@ int Krylov::factor_mg(const double *values64, const float *values32)
     // Jacobian with the velocity solve A^-1 ~ (s K)^-1.
     const int g = grid(M.nNodes);
     double sum2 = 0.;
-    if(values64) {
+    if(M.nc == 3) {
+      const int64_t nq = 3 * M.nNodes;
+      if(values64) {
+        (k_gsum_nc<double><<<grid(nq), 256, 0, s_>>>(nq, M.upIa, M.upPos, values64, (double *)M.bxy), ::feng::count_launch());
+        M.amg->vcycle3_64((const double *)M.bxy, (double *)M.zxy);
+        (k_dw_nc<double><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values64,
+                                                   (const double *)M.zxy, M.tP), ::feng::count_launch());
+      } else {
+        (k_gsum_nc<float><<<grid(nq), 256, 0, s_>>>(nq, M.upIa, M.upPos, values32, (float *)M.bxy), ::feng::count_launch());
+        M.amg->vcycle3_32((const float *)M.bxy, (float *)M.zxy);
+        (k_dw_nc<float><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values32,
+                                                  (const float *)M.zxy, M.tP), ::feng::count_launch());
+      }
+    } else if(values64) {
       (k_gsum<double><<<g, 256, 0, s_>>>(M.nNodes, M.upIa, M.upPos, values64, (double *)M.bx, (double *)M.by), ::feng::count_launch());
       M.solveK<double>((const double *)M.bx, (double *)M.zx, s_);
       M.solveK<double>((const double *)M.by, (double *)M.zy, s_);
@@ -617,7 +696,12 @@ int Krylov::factor_mg(const double *values64, const float *values32)
     CKM(cudaMemcpyAsync(&sum2, M.dsum, sizeof(double), cudaMemcpyDeviceToHost, s_));
     CKM(cudaStreamSynchronize(s_));
     M.cSc = -sum2 / M.s;
-    if(!std::isfinite(M.cSc) || M.cSc == 0.) M.cSc = 0.;  // no deflation
+    // Against the lumped-mass estimate c^T S c ~ -vfac sigma c_div c^T M c / s:
+    // a negligible value means the pressure is determined only up to a
+    // constant (no pressure DOF fixed); then the constant mode is only
+    // projected out of z_p (no lift).
+    const double massEst = std::fabs(M.vfac * M.sigma * M.divu * M.cMc / M.s);
+    if(!std::isfinite(M.cSc) || std::fabs(M.cSc) <= 1e-8 * massEst) M.cSc = 0.;  // no deflation
   }
   // Scalars read by the (graph-replayed) apply kernels.
   M.hconst[0] = 1.0 / M.s;
@@ -713,6 +797,19 @@ void Krylov::apply_mg(const V *vals, const V *r, V *z, const int *skip)
       else M.amgP->vcycle32((const float *)M.pr, (float *)M.pz);
       (k_p_add<V><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.pRows, (const V *)M.pz, M.consts, z, skip),
        ::feng::count_launch());
+    }
+    if(M.nc == 3) {
+      // The three velocity components through one V-cycle on interleaved
+      // right-hand sides, then z_u = (1/s) x.
+      const int64_t nq = 3 * M.nNodes;
+      (k_vel_rhs_nc<V><<<grid(nq), 256, 0, s_>>>(nq, M.dofC, M.upIa, M.upCol, (const V *)M.gVals, r, z, (V *)M.bxy,
+                                                 skip),
+       ::feng::count_launch());
+      if constexpr(sizeof(V) == 8) M.amg->vcycle3_64((const double *)M.bxy, (double *)M.zxy);
+      else M.amg->vcycle3_32((const float *)M.bxy, (float *)M.zxy);
+      (k_vel_out_nc<V><<<grid(nq), 256, 0, s_>>>(nq, M.dofC, (const V *)M.zxy, M.consts, z, skip),
+       ::feng::count_launch());
+      return;
     }
     if(M.inner <= 0) {
       // Both velocity components through one paired V-cycle (one pass over

@@ -533,12 +533,9 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
   PrecondInfo pinfo;
   HostCSR lap;
   if(ko.precond == 3 || ko.precond == 4) {
-    if(t.elemType == ELEM_TET_TAYLOR_HOOD) {
-      set_error("the multigrid preconditioner is built for triangles and scalar P2 tetrahedra");
-      return FE_INVALID_ARG;
-    }
     ko.precond = (t.elemType == ELEM_P2 || t.elemType == ELEM_TET_P2) ? 3 : 4;
-    if(tet) FE_TRY(build_precond_info_tet(t, *hTt, lap, pinfo));
+    if(t.elemType == ELEM_TET_TAYLOR_HOOD) FE_TRY(build_precond_info_tet_th(t, *hTt, lap, pinfo));
+    else if(tet) FE_TRY(build_precond_info_tet(t, *hTt, lap, pinfo));
     else FE_TRY(build_precond_info(t, hT, lap, pinfo));
     pinfo.innerIterations = opt.mgInner;
     pinfo.chebyDegree = std::max(1, std::min(6, opt.mgSmooth));
@@ -613,6 +610,184 @@ int SystemCUDA::build_precond_info_tet(const SystemTables &t, const RefTensorsTe
   }
   for(int64_t i = 0; i < nN; ++i) lap.ia[i + 1] = std::max(lap.ia[i + 1], lap.ia[i]);
   pi.lap = &lap;
+  return FE_OK;
+}
+
+// Geometry of a P1 tetrahedron: G[r][k] = d r_r / d x_k and det J.
+static double tet_geometry(const double *c, double G[3][3])
+{
+  double Jm[3][3];
+  for(int k = 0; k < 3; ++k)
+    for(int r = 0; r < 3; ++r) Jm[k][r] = c[3 * (r + 1) + k] - c[k];
+  const double det = Jm[0][0] * (Jm[1][1] * Jm[2][2] - Jm[1][2] * Jm[2][1]) -
+                     Jm[0][1] * (Jm[1][0] * Jm[2][2] - Jm[1][2] * Jm[2][0]) +
+                     Jm[0][2] * (Jm[1][0] * Jm[2][1] - Jm[1][1] * Jm[2][0]);
+  G[0][0] = (Jm[1][1] * Jm[2][2] - Jm[1][2] * Jm[2][1]) / det;
+  G[0][1] = (Jm[0][2] * Jm[2][1] - Jm[0][1] * Jm[2][2]) / det;
+  G[0][2] = (Jm[0][1] * Jm[1][2] - Jm[0][2] * Jm[1][1]) / det;
+  G[1][0] = (Jm[1][2] * Jm[2][0] - Jm[1][0] * Jm[2][2]) / det;
+  G[1][1] = (Jm[0][0] * Jm[2][2] - Jm[0][2] * Jm[2][0]) / det;
+  G[1][2] = (Jm[0][2] * Jm[1][0] - Jm[0][0] * Jm[1][2]) / det;
+  G[2][0] = (Jm[1][0] * Jm[2][1] - Jm[1][1] * Jm[2][0]) / det;
+  G[2][1] = (Jm[0][1] * Jm[2][0] - Jm[0][0] * Jm[2][1]) / det;
+  G[2][2] = (Jm[0][0] * Jm[1][1] - Jm[0][1] * Jm[1][0]) / det;
+  return det;
+}
+
+// Tetrahedral Taylor-Hood: the operators of the saddle-point multigrid
+// (the three-component version of build_precond_info).  Velocity nodes are
+// the unknown first-component DOFs in DOF order (their three components are
+// consecutive DOFs); the scalar P2 stiffness K and mass M on them take the
+// pattern of the system's x-velocity block and are summed element by
+// element, colors in sequence and the elements of one color in parallel
+// (they share no DOF); pressure unknowns with their lumped P1 masses |J|/24
+// per vertex and the P1 Laplacian on them (Cahouet-Chabard term).
+int SystemCUDA::build_precond_info_tet_th(const SystemTables &t, const RefTensorsTet &T, HostCSR &lap,
+                                          PrecondInfo &pi)
+{
+  const int64_t nE = t.nElm;
+  std::vector<int32_t> nodeOf(nDofs_, -1);
+  std::vector<uint8_t> isX(nDofs_, 0);
+  for(int64_t e = 0; e < nE; ++e)
+    for(int a = 0; a < 10; ++a) {
+      const int64_t dx = t.adr[e * 34 + 3 * a];
+      if(dx < nInc_) {
+        if(t.adr[e * 34 + 3 * a + 1] >= nInc_ || t.adr[e * 34 + 3 * a + 2] >= nInc_) {
+          set_error("a velocity node with an essential component is not supported by the multigrid preconditioner");
+          return FE_INVALID_ARG;
+        }
+        isX[dx] = 1;
+      }
+    }
+  int64_t nN = 0;
+  for(int64_t d = 0; d < nInc_; ++d)
+    if(isX[d]) {
+      nodeOf[d] = (int32_t)nN++;
+      pi.nodeDofX.push_back((int32_t)d);
+      pi.nodeDofY.push_back((int32_t)(d + 1));
+      pi.nodeDofZ.push_back((int32_t)(d + 2));
+    }
+  for(int64_t k = 0; k < nN; ++k)
+    if(pi.nodeDofY[k] >= nInc_ || pi.nodeDofZ[k] >= nInc_ || isX[pi.nodeDofY[k]] || isX[pi.nodeDofZ[k]]) {
+      set_error("velocity components of a node are not consecutive DOFs");
+      return FE_INVALID_ARG;
+    }
+  // K and M pattern: row k = the x-velocity columns of row nodeDofX[k]
+  lap = HostCSR();
+  lap.n = lap.m = nN;
+  lap.ia.assign(nN + 1, 0);
+  for(int64_t k = 0; k < nN; ++k) {
+    const int64_t d = pi.nodeDofX[k];
+    int64_t c = 0;
+    for(int64_t q = pat_.ia[d]; q < pat_.ia[d + 1]; ++q) c += nodeOf[pat_.ja[q]] >= 0;
+    lap.ia[k + 1] = lap.ia[k] + c;
+  }
+  lap.ja.resize(lap.ia[nN]);
+  lap.a.assign(lap.ia[nN], 0.);
+  parallel_for(nN, [&](int64_t k0, int64_t k1) {
+    for(int64_t k = k0; k < k1; ++k) {
+      int64_t o = lap.ia[k];
+      const int64_t d = pi.nodeDofX[k];
+      for(int64_t q = pat_.ia[d]; q < pat_.ia[d + 1]; ++q)
+        if(nodeOf[pat_.ja[q]] >= 0) lap.ja[o++] = nodeOf[pat_.ja[q]];
+    }
+  });
+  massV_ = HostCSR();
+  massV_.n = massV_.m = nN;
+  massV_.ia = lap.ia;
+  massV_.ja = lap.ja;
+  massV_.a.assign(lap.ia[nN], 0.);
+  std::vector<double> pm(nDofs_, 0.);
+  for(int c = 0; c < col_.nColors; ++c) {
+    const int64_t b0 = col_.offsets[c], b1 = col_.offsets[c + 1];
+    parallel_for(b1 - b0, [&](int64_t q0, int64_t q1) {
+      for(int64_t q = b0 + q0; q < b0 + q1; ++q) {
+        const int64_t e = col_.elements[q];
+        double G[3][3];
+        const double det = tet_geometry(t.elemXY + 12 * e, G);
+        double GG[3][3];
+        for(int r = 0; r < 3; ++r)
+          for(int s2 = 0; s2 < 3; ++s2) GG[r][s2] = G[r][0] * G[s2][0] + G[r][1] * G[s2][1] + G[r][2] * G[s2][2];
+        int32_t nd[10];
+        for(int a = 0; a < 10; ++a) {
+          const int64_t d = t.adr[e * 34 + 3 * a];
+          nd[a] = d < nInc_ ? nodeOf[d] : -1;
+        }
+        for(int a = 0; a < 10; ++a) {
+          if(nd[a] < 0) continue;
+          const int32_t *rb = lap.ja.data() + lap.ia[nd[a]], *re = lap.ja.data() + lap.ia[nd[a] + 1];
+          for(int b = 0; b < 10; ++b) {
+            if(nd[b] < 0) continue;
+            const int64_t pos = std::lower_bound(rb, re, nd[b]) - lap.ja.data();
+            double v = 0.;
+            for(int r = 0; r < 3; ++r)
+              for(int s2 = 0; s2 < 3; ++s2) v += GG[r][s2] * T.K[r][s2][a][b];
+            lap.a[pos] += std::fabs(det) * v;
+            massV_.a[pos] += std::fabs(det) * T.M[a][b];
+          }
+        }
+        for(int j = 0; j < 4; ++j) pm[t.adr[e * 34 + 30 + j]] += std::fabs(det) / 24.0;
+      }
+    });
+  }
+  pi.lap = &lap;
+  pi.massV = &massV_;
+  // pressure unknowns (in DOF order), their lumped masses and the P1 Laplacian
+  std::vector<int32_t> pIdx(nDofs_, -1);
+  for(int64_t e = 0; e < nE; ++e)
+    for(int j = 0; j < 4; ++j) {
+      const int64_t d = t.adr[e * 34 + 30 + j];
+      if(d < nInc_) pIdx[d] = 0;
+    }
+  nPLap_ = 0;
+  for(int64_t d = 0; d < nInc_; ++d)
+    if(pIdx[d] == 0) {
+      pIdx[d] = nPLap_++;
+      pi.pRows.push_back((int32_t)d);
+      pi.pMass.push_back(pm[d]);
+    }
+  std::vector<std::pair<int64_t, double>> cooP;
+  cooP.reserve(nE * 16);
+  for(int64_t e = 0; e < nE; ++e) {
+    double G[3][3];
+    const double det = tet_geometry(t.elemXY + 12 * e, G);
+    // grad psi_j = G^T grad_ref psi_j, grad_ref psi = (-1,-1,-1), e_1, e_2, e_3
+    double g[4][3];
+    for(int k = 0; k < 3; ++k) {
+      g[0][k] = -(G[0][k] + G[1][k] + G[2][k]);
+      for(int j = 1; j < 4; ++j) g[j][k] = G[j - 1][k];
+    }
+    int32_t pk[4];
+    for(int j = 0; j < 4; ++j) {
+      const int64_t d = t.adr[e * 34 + 30 + j];
+      pk[j] = d < nInc_ ? pIdx[d] : -1;
+    }
+    for(int i = 0; i < 4; ++i) {
+      if(pk[i] < 0) continue;
+      for(int j = 0; j < 4; ++j) {
+        if(pk[j] < 0) continue;
+        cooP.push_back({(int64_t)pk[i] << 32 | (uint32_t)pk[j],
+                        std::fabs(det) / 6.0 * (g[i][0] * g[j][0] + g[i][1] * g[j][1] + g[i][2] * g[j][2])});
+      }
+    }
+  }
+  std::sort(cooP.begin(), cooP.end(),
+            [](const std::pair<int64_t, double> &x, const std::pair<int64_t, double> &y) { return x.first < y.first; });
+  lapP_ = HostCSR();
+  lapP_.n = lapP_.m = nPLap_;
+  lapP_.ia.assign(nPLap_ + 1, 0);
+  for(size_t k = 0; k < cooP.size();) {
+    const int64_t key = cooP[k].first;
+    double v = 0.;
+    while(k < cooP.size() && cooP[k].first == key) v += cooP[k++].second;
+    lapP_.ja.push_back((int32_t)(key & 0xffffffff));
+    lapP_.a.push_back(v);
+    lapP_.ia[(key >> 32) + 1] = (int64_t)lapP_.ja.size();
+  }
+  for(int64_t i = 0; i < nPLap_; ++i) lapP_.ia[i + 1] = std::max(lapP_.ia[i + 1], lapP_.ia[i]);
+  pi.lapP = &lapP_;
+  pi.sigma = fc_.hasSigma ? fc_.sigma : 1.0;
+  pi.divu = fc_.hasDivu ? fc_.divu : 1.0;
   return FE_OK;
 }
 

@@ -202,6 +202,7 @@ class SystemCUDA {
   float end_phase();
   int build_precond_info(const SystemTables &t, const RefTensors &T, HostCSR &lap, PrecondInfo &pi);
   int build_precond_info_tet(const SystemTables &t, const RefTensorsTet &T, HostCSR &lap, PrecondInfo &pi);
+  int build_precond_info_tet_th(const SystemTables &t, const RefTensorsTet &T, HostCSR &lap, PrecondInfo &pi);
   RefTensorsTet *dTt_ = nullptr;  // tetrahedral reference tensors (device)
   bool tet() const { return elemType_ == ELEM_TET_P2 || elemType_ == ELEM_TET_TAYLOR_HOOD; }
 };

@@ -124,3 +124,28 @@ def test_tet_taylor_hood_matches_oracle(precision):
                                                     0.0 * x, 0.0 * x))
     assert rel_err(sys_.getRHS(), rhs) <= TOL_FP64
     assert rel_err(sys_.getMatrix(), vals) <= (TOL_FP64 if precision == "fp64" else TOL_FP32)
+
+
+@pytest.mark.parametrize("n", [4, 6])
+def test_tet_bdf2_three_component_multigrid(n):
+    """Unsteady Navier-Stokes in the cube on tetrahedra (config C5's case at a
+    small size): BDF2 steps from rest with the saddle-point multigrid on the
+    three velocity components, plain FP64 and mixed precision.  Both reach
+    the relative residual stop at every step in a bounded number of Krylov
+    iterations and give the same flow (the pressure up to its constant)."""
+    from feng_gb300 import cube
+    out = {}
+    for prec, guess in (("fp64", "previous"), ("mixed", "extrapolate")):
+        sys_, stats = cube.run(n, 100.0, 0.01, 3, guess, prec, rel=1e-10)
+        assert all(s["status"] == 0 for s in stats), stats
+        assert all(s["krylov_iterations"] <= 150 * max(1, s["newton_iterations"]) for s in stats), stats
+        out[prec] = (sys_, sys_.getSolution())
+    sys_, uf = out["fp64"]
+    _, um = out["mixed"]
+    x, y, fld, comp = sys_.dofInfo()
+    vel = np.arange(sys_.nDofs)[fld == 0]
+    prs = np.arange(sys_.nDofs)[fld == 1]
+    assert np.max(np.abs(uf[vel])) > 1e-6          # the body force moved the fluid
+    assert np.max(np.abs(um[vel] - uf[vel])) <= 1e-6 * np.max(np.abs(uf[vel]))
+    pf, pm = uf[prs] - uf[prs].mean(), um[prs] - um[prs].mean()
+    assert np.max(np.abs(pm - pf)) <= 1e-5 * np.max(np.abs(pf))
