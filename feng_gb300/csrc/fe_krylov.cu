@@ -574,8 +574,9 @@ __global__ void __launch_bounds__(RB) k_gs_dots(int64_t n4, int64_t ld, const fl
       for(int k = 0; k < RB / 32; ++k) sum += (double)red[k][t];
       partials[(int64_t)col * MAXRED + blockIdx.x] = sum;
     }
+    // only the threads that wrote partials order them before the counter
+    __threadfence();
   }
-  __threadfence();
   __syncthreads();
   if(threadIdx.x == 0) last = atomicAdd(&st->counter, 1u) == gridDim.x * gridDim.y - 1;
   __syncthreads();

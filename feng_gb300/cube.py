@@ -52,8 +52,13 @@ def make_system(num, forms, precision: str, precond: str = "amg", **solver):
 def run(n: int, re: float, dt: float, steps: int, guess: str, precision: str = "mixed", rel: float = 1e-8,
         solver=None):
     """BDF2 steps from rest; returns (system, per-step statistics)."""
-    from . import api as fe
     _, num, forms = build(n, re)
+    return run_on(num, forms, dt, steps, guess, precision, rel, solver)
+
+
+def run_on(num, forms, dt: float, steps: int, guess: str, precision: str = "mixed", rel: float = 1e-8, solver=None):
+    """BDF2 steps from rest on a numbering and forms of build()."""
+    from . import api as fe
     sys_, sol = make_system(num, forms, precision, **(solver or {}))
     nl = fe.feNLSolverOptions(tolResidual=0.0, tolCorrection=0.0, tolDivergence=1e12, maxIter=30,
                               relResidual=rel, linearRtolMin=1e-6 if precision == "mixed" else 0.0)
