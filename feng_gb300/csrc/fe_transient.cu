@@ -300,6 +300,8 @@ int Transient::init(SystemCUDA *sys, const TransientOptions &o, const NewtonOpti
   nHist_ = 0;
   steps_ = 0;
   trained_ = 0;
+  lostStreak_ = 0;
+  skipUntil_ = 0;
   return FE_OK;
 }
 
@@ -399,7 +401,12 @@ int Transient::step(StepStats &st)
     const int64_t nDofs = sys_->nDofs(), nInc = sys_->nInc();
     const size_t bytes = sizeof(double) * nDofs;
     const bool canExtrap = o_.guess != GUESS_PREVIOUS && nHist_ >= 2;
-    const bool learn = o_.guess == GUESS_LEARNED && nHist_ >= 3;
+    // Back-off: after LOSE_LIMIT consecutive steps where the learned
+    // candidate did not beat the extrapolation, the network is neither
+    // evaluated nor trained for BACKOFF_STEPS steps, then tried again.
+    constexpr int LOSE_LIMIT = 8, BACKOFF_STEPS = 32;
+    const bool backoff = st.step < skipUntil_;
+    const bool learn = o_.guess == GUESS_LEARNED && nHist_ >= 3 && !backoff;
     int used = GUESS_PREVIOUS;
     if(canExtrap) {
       (k_extrapolate<<<grid_of(nDofs), 256, 0, s>>>(nDofs, nInc, sys_->dHist(1), sys_->dHist(2), d0 / d1, ue_),
@@ -451,8 +458,13 @@ int Transient::step(StepStats &st)
       if(r == FE_OK && rm < re) {
         used = GUESS_LEARNED;
         residualReady = true;
+        lostStreak_ = 0;
       } else {
         CKT(cudaMemcpyAsync(sys_->dU(), ue_, bytes, cudaMemcpyDeviceToDevice, s));
+        if(++lostStreak_ >= LOSE_LIMIT) {
+          skipUntil_ = st.step + 1 + BACKOFF_STEPS;
+          lostStreak_ = 0;
+        }
       }
     } else if(canExtrap) {
       CKT(cudaMemcpyAsync(sys_->dU(), ue_, bytes, cudaMemcpyDeviceToDevice, s));

@@ -99,6 +99,8 @@ class Transient {
   int nHist_ = 0;               // valid history levels
   int steps_ = 0;
   int trained_ = 0;             // time steps that trained the network
+  int lostStreak_ = 0;          // consecutive steps the learned candidate lost
+  int skipUntil_ = 0;           // back-off: no network evaluation or training before this step
   // step start, end of the guess, start and end of training
   cudaEvent_t e0_ = nullptr, e1_ = nullptr, e2_ = nullptr, e3_ = nullptr;
   int residualNorm(double *norm);

@@ -430,8 +430,9 @@ int fe_cuda_apply_periodicity(fe_cuda_system *s);
  *                         step length alpha minimising the linearised residual
  *                         with the Jacobian held from the previous step, the
  *                         extrapolation and ue + alpha d are both evaluated with
- *                         the FP64 residual and the smaller one is used (no
- *                         counterpart in the reference). */
+ *                         the FP64 residual and the smaller one is used; after 8
+ *                         losses in a row the network is neither evaluated nor
+ *                         trained for 32 steps (no counterpart in the reference). */
 #define FE_GUESS_PREVIOUS 0
 #define FE_GUESS_EXTRAPOLATE 1
 #define FE_GUESS_LEARNED 2
