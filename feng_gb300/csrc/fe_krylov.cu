@@ -1540,6 +1540,57 @@ int Krylov::gsStep(int mode, int ncols, int64_t *bytes)
   return FE_OK;
 }
 
+int Krylov::gsStepStream(int mode, int ncols, int reps, double *avgMs)
+{
+  if(!V32_ || (mode != 0 && mode != 4) || ncols < 1 || ncols > opt.restart || reps < 1 || !avgMs) {
+    set_error("no mixed FP32 basis, or an invalid Gram-Schmidt request");
+    return FE_INVALID_ARG;
+  }
+  if(!zeroFlag_) {
+    CK(cudaMalloc(&zeroFlag_, sizeof(int)));
+    CK(cudaMemsetAsync(zeroFlag_, 0, sizeof(int), s_));
+  }
+  int dev = 0, l2 = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
+  // one copy: ncols + 1 basis columns (the pass reads ncols, the update
+  // writes none of them) and w
+  const size_t colBytes = sizeof(float) * (size_t)ld32_;
+  const size_t per = (size_t)(ncols + 2) * colBytes;
+  const int copies = (int)std::max<size_t>(2, (3 * (size_t)l2) / per + 1);
+  char *buf = nullptr;
+  CK(cudaMalloc(&buf, per * copies));
+  for(int c = 0; c < copies; ++c) {
+    CK(cudaMemcpyAsync(buf + per * c, V32_, (size_t)(ncols + 1) * colBytes, cudaMemcpyDeviceToDevice, s_));
+    CK(cudaMemcpyAsync(buf + per * c + (size_t)(ncols + 1) * colBytes, w32_, colBytes, cudaMemcpyDeviceToDevice, s_));
+  }
+  float *V0 = V32_, *w0 = w32_;
+  Ws w = Ws_INIT(this);
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  auto pass = [&](int c) {
+    V32_ = (float *)(buf + per * c);
+    w32_ = (float *)(buf + per * c + (size_t)(ncols + 1) * colBytes);
+    if(mode == 0) gs32(0, ncols, nullptr, w.gs->hcur, w.gs->H, zeroFlag_, 0);
+    else gs32(4, ncols, w.gs->hcur, nullptr, w.gs->H + ncols, zeroFlag_, 0);
+  };
+  for(int c = 0; c < copies; ++c) pass(c);  // warm-up round
+  CK(cudaEventRecord(a, s_));
+  for(int r = 0; r < reps; ++r) pass(r % copies);
+  CK(cudaEventRecord(b, s_));
+  V32_ = V0;
+  w32_ = w0;
+  CK(cudaEventSynchronize(b));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(buf);
+  *avgMs = ms / reps;
+  return FE_OK;
+}
+
 // One FP32 Gram-Schmidt pass over the first ncols basis vectors: mode 0 the
 // dot pass (k_gs_dots), 5 the dot pass with the Pythagoras norm, 1 update +
 // dots, 2 update + norm (k_gs32), 3 the update that writes the next basis

@@ -211,6 +211,11 @@ class Krylov {
   // ncols columns (benchmark phases): mode 0 the dot pass (k_gs_dots), mode
   // 4 the update + norm pass (k_gs_upd).  bytes: algorithmic bytes.
   int gsStep(int mode, int ncols, int64_t *bytes);
+  // The same pass launched reps times back to back, cycling through copies
+  // of the basis and w that together exceed three times the L2 (each launch
+  // reads data evicted by the others), timed as a batch with CUDA events:
+  // the average time of a pass as it runs inside the Arnoldi loop.
+  int gsStepStream(int mode, int ncols, int reps, double *avgMs);
   // The Arnoldi SpMV of the mixed path on the current FP32 matrix (sliced
   // ELL when built, else CSR), FP32 vectors (benchmark phase).
   int spmvHot();

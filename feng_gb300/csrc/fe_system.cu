@@ -1495,6 +1495,12 @@ int SystemCUDA::computeSolDot()
 
 int SystemCUDA::benchPhase(int which, int reps, size_t flushBytes, double *avgMs)
 {
+  if(which == 7 || which == 8) {
+    // the Gram-Schmidt passes of phases 5 and 6 back to back over a working
+    // set larger than the L2 (see Krylov::gsStepStream)
+    FE_TRY(ensureMatrixZeroed());
+    return kry_.gsStepStream(which == 7 ? 0 : 4, std::max(1, kry_.opt.restart / 2), std::max(reps, 1) * 10, avgMs);
+  }
   if(which < 0 || which > 6 || reps < 1) {
     set_error("invalid benchmark request");
     return FE_INVALID_ARG;

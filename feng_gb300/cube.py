@@ -35,7 +35,7 @@ def build(n: int, re: float, jitter: float = 0.05, seed: int = 1):
              fe.createBilinearForm([u], fe.feSysElm_VectorConvectiveAcceleration(1.0)),
              fe.createBilinearForm([p, u], fe.feSysElm_MixedDivergence(1.0)),
              fe.createBilinearForm([u, p], fe.feSysElm_DivergenceNewtonianStress(-1.0, 1.0 / re)),
-             fe.createBilinearForm([u], fe.feSysElm_VectorSource(fe.api.SRC_SIN3_BODY, (-1.0,)))]
+             fe.createBilinearForm([u], fe.feSysElm_VectorSource(fe.SRC_SIN3_BODY, (-1.0,)))]
     return m, num, forms
 
 

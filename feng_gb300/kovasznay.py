@@ -80,7 +80,7 @@ def main(argv=None):
     ap.add_argument("--phases", default="",
                     help="after the solves, time these benchmark phases (comma list of fe_cuda_bench_phase "
                          "numbers: 0 residual, 1 Jacobian, 2 SpMV, 3 preconditioner, 4 finest smoother pass, "
-                         "5 Gram-Schmidt dots, 6 Gram-Schmidt update)")
+                         "5 Gram-Schmidt dots, 6 Gram-Schmidt update, 7 and 8 the same two streamed back to back)")
     ap.add_argument("--phase-reps", type=int, default=20)
     ap.add_argument("--errors", action="store_true",
                     help="after the solves, L2 errors of velocity and pressure against the exact Kovasznay flow "
@@ -129,7 +129,7 @@ def main(argv=None):
     phases = {}
     for w in [int(v) for v in args.phases.split(",") if v.strip()]:
         # device time per run with the L2 flushed before each run; bytes:
-        # algorithmic bytes where the library defines them (phases 4-6)
+        # algorithmic bytes where the library defines them (phases 4-8)
         ms = C.c_double()
         check(lib.fe_cuda_bench_phase(sys_._h, w, args.phase_reps, 256 << 20, C.byref(ms)))
         ph = {"us": ms.value * 1e3}

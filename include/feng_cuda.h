@@ -374,15 +374,19 @@ int fe_cuda_reset_times(fe_cuda_system *s);
  * application, 4 one finest-level multigrid pre-smoothing pass (zero start
  * fused with the first Chebyshev step, both velocity components), 5 one
  * Gram-Schmidt dot pass of the mixed FGMRES over restart/2 basis vectors,
- * 6 one Gram-Schmidt update + norm pass over restart/2 basis vectors.
- * Phases 5 and 6 need a mixed-precision system that has solved once.  Uses
+ * 6 one Gram-Schmidt update + norm pass over restart/2 basis vectors;
+ * 7 and 8 the passes of 5 and 6 launched 10 * reps times back to back, with
+ * no flush between them, cycling through copies of the basis that together
+ * exceed three times the L2 (the mean time of a pass inside the Arnoldi
+ * loop, where the launches follow one another; flush_bytes unused).
+ * Phases 5 to 8 need a mixed-precision system that has solved once.  Uses
  * the current solution state. */
 int fe_cuda_bench_phase(fe_cuda_system *s, int which, int reps, int64_t flush_bytes, double *avg_ms);
 /* Algorithmic bytes of one run of phase 4 (finest multigrid operator read
  * once, each vector entry read or written once). */
 int fe_cuda_smoother_bytes(fe_cuda_system *s, int64_t *bytes);
-/* Algorithmic bytes of one run of phase 4, 5 or 6 (every operand read or
- * written once). */
+/* Algorithmic bytes of one run of phase 4, 5, 6, 7 or 8 (every operand read
+ * or written once). */
 int fe_cuda_phase_bytes(fe_cuda_system *s, int which, int64_t *bytes);
 /* Kernel launches of the library since load (graph replays count their
  * kernel nodes). */
