@@ -132,11 +132,8 @@ public:
   }
   void getResidualMaxNorm(double *norm) const override
   {
-    std::vector<double> du(_nInc);
-    check(fe_cuda_get_du(_sys, du.data()), "fe_cuda_get_du");
-    double m = 0.;
-    for(double v : du) m = std::max(m, std::fabs(v));
-    *norm = m;
+    // reduced on the device: du stays there
+    check(fe_cuda_get_du_max_norm(_sys, norm), "fe_cuda_get_du_max_norm");
   }
 
   void setToZero() override { check(fe_cuda_set_to_zero(_sys), "fe_cuda_set_to_zero"); }

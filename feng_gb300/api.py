@@ -555,6 +555,13 @@ class feLinearSystemCUDA:
         check(self.lib.fe_cuda_get_du(self._h, ptr(v)))
         return v
 
+    def getResidualMaxNorm(self):
+        """max |du| of the last correction, reduced on the device
+        (feLinearSystem::getResidualMaxNorm)."""
+        n = C.c_double()
+        check(self.lib.fe_cuda_get_du_max_norm(self._h, C.byref(n)))
+        return n.value
+
     def pattern(self):
         ia = np.empty(self.nInc + 1, np.int64)
         ja = np.empty(self.nnz, np.int32)

@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstring>
 #include <memory>
@@ -863,6 +864,19 @@ int fe_cuda_get_du(const fe_cuda_system *s, double *du)
 {
   if(!s || !du) { set_error("null argument"); return FE_INVALID_ARG; }
   return s->sys.getDu(du);
+}
+
+int fe_cuda_get_du_max_norm(fe_cuda_system *s, double *norm)
+{
+  GUARD_BEGIN
+  if(!s || !norm) { set_error("null argument"); return FE_INVALID_ARG; }
+  *norm = s->sys.krylov().norminf(s->sys.dDu());
+  if(!std::isfinite(*norm)) {
+    set_error("non-finite Newton correction");
+    return FE_NONFINITE;
+  }
+  return FE_OK;
+  GUARD_END
 }
 
 int fe_cuda_newton(fe_cuda_system *s, const fe_newton_options *o, fe_newton_stats *st)

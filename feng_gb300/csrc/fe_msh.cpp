@@ -30,7 +30,8 @@ int read_msh41(const std::string &path, MshData &out)
     if(tok == "$MeshFormat") {
       double ver = 0; int ftype = -1, dsize;
       in >> ver >> ftype >> dsize;
-      if(!in || ver < 4.0 || ftype != 0) {
+      // the 4.1 layout only (4.0 lists node tags and coordinates differently)
+      if(!in || ver < 4.1 - 1e-9 || ver >= 5.0 || ftype != 0) {
         set_error("only ASCII msh 4.1 is supported (got %g, type %d)", ver, ftype);
         return FE_READ_ERROR;
       }

@@ -357,6 +357,10 @@ int fe_cuda_correct_solution(fe_cuda_system *s);
 int fe_cuda_get_matrix(const fe_cuda_system *s, double *values);
 int fe_cuda_get_rhs(const fe_cuda_system *s, double *rhs);
 int fe_cuda_get_du(const fe_cuda_system *s, double *du);
+/* max |du| of the last correction on the device (getResidualMaxNorm,
+ * src/feLinearSystemMklPardiso.cpp:352-355), without copying du to the host;
+ * FE_CUDA_NONFINITE if it holds a NaN or an infinity. */
+int fe_cuda_get_du_max_norm(fe_cuda_system *s, double *norm);
 /* One application z = M^-1 r of the preconditioner (PETSc's PCApply),
  * built from the current matrix first if needed; r, z host arrays [n_inc]. */
 int fe_cuda_apply_preconditioner(fe_cuda_system *s, const double *r, double *z);

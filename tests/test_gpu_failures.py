@@ -190,3 +190,19 @@ def test_dof_id_out_of_range_is_refused():
     with pytest.raises(FeError) as e:
         TablesSystem(bad, forms, fe.LinearSolverOptions(precond="ilu0"))
     assert e.value.status == INVALID_ARG
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_correction_max_norm_on_device(precision):
+    """getResidualMaxNorm reduces du on the device (the same NaN-propagating
+    max as the residual norm): equal to max |du| of the downloaded
+    correction."""
+    g, sys = _kovasznay(precision)
+    sys.setSolution(g["u0"].copy())
+    sys.setToZero()
+    sys.assembleResiduals()
+    sys.assembleMatrices()
+    sys.solve()
+    du = sys.getDu()
+    assert np.all(np.isfinite(du)) and np.abs(du).max() > 0
+    assert sys.getResidualMaxNorm() == np.abs(du).max()
