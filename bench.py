@@ -465,7 +465,11 @@ def c5_leg(n=64, reps=5, steps=50, steps_fp64=10):
         sA = 8 if prec == "fp64" else 4
         base = sys_.nElm * 34 * 4 + nvert * 3 * 8 + sys_.nDofs * 8 * 2
         by = {"residual": base + sys_.nInc * 8, "jacobian": sys_.nnz * sA + base}
-        out[prec] = {"system_create_s": create_s,
+        route = sys_.jacobianRoute
+        out[prec] = {"system_create_s": create_s, "jacobian_route": "row-owned" if route else "colored scatter",
+                     "jacobian_kernel": ("k_pack_tet + k_matrix_tet_rows (FP32, warp per velocity node / pressure row)"
+                                         if route else f"k_matrix_tet<{'double' if prec == 'fp64' else 'float'}> "
+                                         "(colored, L2 reductions through the element-to-nonzero map)"),
                      **{f"{k}_ms": v for k, v in ph.items()},
                      "assembly_melem_s": sys_.nElm / ((ph["residual"] + ph["jacobian"]) / 1e3) / 1e6,
                      "roofline_jacobian": {"bound": "hbm", "bytes_per_launch": by["jacobian"],

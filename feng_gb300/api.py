@@ -555,6 +555,13 @@ class feLinearSystemCUDA:
         check(self.lib.fe_cuda_get_du(self._h, ptr(v)))
         return v
 
+    @property
+    def jacobianRoute(self):
+        """1: row-owned Jacobian assembly, 0: colored scatter."""
+        r = C.c_int()
+        check(self.lib.fe_cuda_jacobian_route(self._h, C.byref(r)))
+        return r.value
+
     def getResidualMaxNorm(self):
         """max |du| of the last correction, reduced on the device
         (feLinearSystem::getResidualMaxNorm)."""

@@ -361,6 +361,194 @@ __global__ void k_build_map(const int32_t *__restrict__ adr, int64_t nE, int nlo
   }
 }
 
+// ---------------------------------------------------------------------------
+// Row-owned FP32 Taylor-Hood Jacobian (RowAsmTet).
+// ---------------------------------------------------------------------------
+constexpr int RT_WARPS = 8;
+
+// pack[p][0..29] = u at the velocity DOFs (local order 3 a + m), [30..38] =
+// G, [39] = J: 32 elements per block, read per local DOF (coalesced over
+// elements), written per element (coalesced) through shared memory.
+__global__ void __launch_bounds__(256) k_pack_tet(DeviceMesh dm, int hasConv, const double *__restrict__ u,
+                                                  float *__restrict__ pack)
+{
+  __shared__ float sh[32][ROWTET_PACK + 1];
+  const int64_t nE = dm.nElm;
+  for(int64_t p0 = (int64_t)blockIdx.x * 32; p0 < nE; p0 += (int64_t)gridDim.x * 32) {
+    const int cnt = (int)(nE - p0 < 32 ? nE - p0 : 32);
+    for(int idx = threadIdx.x; idx < 32 * ROWTET_PACK; idx += blockDim.x) {
+      const int i = idx >> 5, l = idx & 31;
+      if(l >= cnt) continue;
+      const int64_t p = p0 + l;
+      float v;
+      if(i < 30) v = hasConv ? (float)u[dm.adr[(int64_t)i * nE + p]] : 0.f;
+      else v = (float)dm.geo[(int64_t)(i - 30) * nE + p];
+      sh[l][i] = v;
+    }
+    __syncthreads();
+    for(int idx = threadIdx.x; idx < cnt * ROWTET_PACK; idx += blockDim.x)
+      pack[p0 * ROWTET_PACK + idx] = sh[idx / ROWTET_PACK][idx % ROWTET_PACK];
+    __syncthreads();
+  }
+}
+
+__global__ void k_rowtet_offsets(int64_t nEnt, const int32_t *__restrict__ ent, const int32_t *__restrict__ entRow,
+                                 const int32_t *__restrict__ map, int64_t nE, const int32_t *__restrict__ ia,
+                                 uint8_t *__restrict__ offs)
+{
+  const int64_t total = nEnt * ROWTET_OFFS;
+  for(int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = t / ROWTET_OFFS;
+    const int j = (int)(t % ROWTET_OFFS);
+    uint8_t o = 255;
+    if(j < 34) {
+      const int32_t e = ent[k];
+      const int64_t p = e >> 6;
+      const int li = e & 63;
+      const int32_t pos = map[(int64_t)(li * 34 + j) * nE + p];
+      if(pos >= 0) o = (uint8_t)(pos - ia[entRow[k]]);
+    }
+    offs[t] = o;
+  }
+}
+
+// A persistent grid walks the row blocks; per block the CSR values of its
+// units live in shared memory.  Warp w takes units uA + w, uA + w + 8, ...
+// and, for each of a unit's entries in order, the element's terms:
+//   velocity unit, lane (m, b) = (lane / 10, lane % 10), lane < 30: the
+//   columns (b, n) of row (a, m) -- k_matrix_tet's convection, stress and
+//   mass terms; lanes (m, j) = (lane / 4, lane % 4), lane < 12: the pressure
+//   columns sigma J sum_r G[r][m] D[r][j][a];
+//   pressure unit (row of P1 function j), lane (a, m) = (lane / 3, lane % 3),
+//   lane < 30: divu J sum_r G[r][m] D[r][j][a].
+// Every value gets one contribution per element, in the entries' (color)
+// order: the colored scatter's sum.
+__global__ void __launch_bounds__(RT_WARPS * 32) k_matrix_tet_rows(RowAsmTet ra, FormCoeffs fc,
+                                                                   const RefTensorsTet *__restrict__ gT, double c0,
+                                                                   float *__restrict__ values, int accumulate)
+{
+  extern __shared__ __align__(16) unsigned char rtsm[];
+  float *sTen = reinterpret_cast<float *>(rtsm);
+  float *sv = sTen + NTEN;
+  __shared__ float sE[RT_WARPS][ROWTET_PACK];
+  __shared__ float sV0[RT_WARPS][30];
+  __shared__ __align__(16) uint8_t sOff[RT_WARPS][ROWTET_OFFS];
+  const TetTensors<float> Tt = load_tet_tensors(sTen, gT);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const float fconv = (float)fc.conv, fcs = -(float)fc.sigma * (float)fc.mu, fcm = (float)fc.mass * (float)c0;
+  const float fsig = (float)fc.sigma, fdiv = (float)fc.divu;
+  for(int blk = blockIdx.x; blk < ra.nBlocks; blk += gridDim.x) {
+    const int32_t uA = ra.blockUnits[blk], uB = ra.blockUnits[blk + 1];
+    const int32_t base = ra.ia[ra.unitRow[uA]], L = ra.ia[ra.unitRow[uB]] - base;
+    __syncthreads();  // the previous block's values are written out (and the tensors loaded)
+    for(int i = tid; i < L; i += blockDim.x) sv[i] = accumulate ? values[base + i] : 0.f;
+    __syncthreads();
+    for(int32_t un = uA + warp; un < uB; un += RT_WARPS) {
+      const int32_t r = ra.unitRow[un];
+      const bool vel = ra.unitKind[un] == 3;
+      float *row0 = sv + (ra.ia[r] - base);
+      const int32_t rl = ra.ia[r + 1] - ra.ia[r];
+      for(int32_t k = ra.unitPtr[un]; k < ra.unitPtr[un + 1]; ++k) {
+        const int32_t e = ra.ent[k];
+        const int64_t p = e >> 6;
+        const int li = e & 63;
+        const float *pk = ra.pack + p * ROWTET_PACK;
+        sE[warp][lane] = pk[lane];
+        if(lane < ROWTET_PACK - 32) sE[warp][32 + lane] = pk[32 + lane];
+        if(lane < ROWTET_OFFS / 4)
+          reinterpret_cast<uint32_t *>(sOff[warp])[lane] =
+              reinterpret_cast<const uint32_t *>(ra.offs + (int64_t)k * ROWTET_OFFS)[lane];
+        __syncwarp();
+        const float *E = sE[warp];
+        const float J = E[39];
+        float G[3][3];
+#pragma unroll
+        for(int q = 0; q < 3; ++q)
+#pragma unroll
+          for(int l = 0; l < 3; ++l) G[q][l] = E[30 + 3 * q + l];
+        if(vel) {
+          const int a = li / 3;
+          if(fc.hasConv && lane < 30) {
+            const int q = lane / 10, c = lane % 10;
+            sV0[warp][lane] = G[q][0] * E[3 * c] + G[q][1] * E[3 * c + 1] + G[q][2] * E[3 * c + 2];
+          }
+          __syncwarp();
+          if(lane < 30) {
+            const int m = lane / 10, b = lane % 10;
+            float A[3] = {0.f, 0.f, 0.f};
+            if(fc.hasConv) {
+              // W = sum_c sum_r V0[r][c] T[r][a][c][b], Z_r = sum_c u_(c,m) T[r][a][b][c]
+              float W = 0.f, Z[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+              for(int c = 0; c < 10; ++c) {
+#pragma unroll
+                for(int q = 0; q < 3; ++q) W += sV0[warp][q * 10 + c] * Tt.t(q, a, c, b);
+                const float um = E[3 * c + m];
+#pragma unroll
+                for(int q = 0; q < 3; ++q) Z[q] += um * Tt.t(q, a, b, c);
+              }
+              const float cc = fconv * J;
+#pragma unroll
+              for(int n = 0; n < 3; ++n) {
+                float v = G[0][n] * Z[0] + G[1][n] * Z[1] + G[2][n] * Z[2];
+                if(n == m) v += W;
+                A[n] += cc * v;
+              }
+            }
+            if(fc.hasSigma) {
+              float P[3][3];
+#pragma unroll
+              for(int q = 0; q < 3; ++q)
+#pragma unroll
+                for(int l = 0; l < 3; ++l)
+                  P[q][l] = Tt.k(q, 0, a, b) * G[0][l] + Tt.k(q, 1, a, b) * G[1][l] + Tt.k(q, 2, a, b) * G[2][l];
+              float tr = 0.f;
+#pragma unroll
+              for(int kk = 0; kk < 3; ++kk) tr += G[0][kk] * P[0][kk] + G[1][kk] * P[1][kk] + G[2][kk] * P[2][kk];
+              const float cs = fcs * J;
+#pragma unroll
+              for(int n = 0; n < 3; ++n) {
+                const float snm = G[0][n] * P[0][m] + G[1][n] * P[1][m] + G[2][n] * P[2][m];
+                A[n] += cs * ((n == m ? tr : 0.f) + snm);
+              }
+            }
+            if(fc.hasMass) {
+              const float mv = fcm * J * Tt.m(a, b);
+#pragma unroll
+              for(int n = 0; n < 3; ++n)
+                if(n == m) A[n] += mv;
+            }
+            float *row = row0 + m * rl;
+#pragma unroll
+            for(int n = 0; n < 3; ++n) {
+              const uint8_t o = sOff[warp][3 * b + n];
+              if(o != 255) row[o] += A[n];
+            }
+          }
+          if(fc.hasSigma && lane < 12) {
+            const int m = lane >> 2, j = lane & 3;
+            const uint8_t o = sOff[warp][30 + j];
+            if(o != 255) {
+              const float bp = (G[0][m] * Tt.d(0, j, a) + G[1][m] * Tt.d(1, j, a) + G[2][m] * Tt.d(2, j, a)) * J;
+              row0[m * rl + o] += fsig * bp;
+            }
+          }
+        } else if(fc.hasDivu && lane < 30) {
+          const int j = li - 30, a = lane / 3, m = lane % 3;
+          const uint8_t o = sOff[warp][lane];
+          if(o != 255) {
+            const float bp = (G[0][m] * Tt.d(0, j, a) + G[1][m] * Tt.d(1, j, a) + G[2][m] * Tt.d(2, j, a)) * J;
+            row0[o] += fdiv * bp;
+          }
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    for(int i = tid; i < L; i += blockDim.x) values[base + i] = sv[i];
+  }
+}
+
 size_t residual_smem(int nq) { return sizeof(double) * (NTEN + (30 + 30 + 10 + 4 + nq) * EPB); }
 template <typename V>
 size_t matrix_smem() { return sizeof(V) * (NTEN + (30 + 10 + 30) * EPB); }
@@ -447,6 +635,38 @@ void launch_assemble_matrix_tet_f32(const DeviceMesh &dm, const FormCoeffs &fc, 
                                     cudaStream_t s)
 {
   launch_matrix_tet<float>(dm, fc, dT, u, c0, values, begin, end, s);
+}
+
+void launch_pack_tet_f32(const DeviceMesh &dm, const FormCoeffs &fc, const double *u, float *pack, cudaStream_t s)
+{
+  const int64_t blocks = std::min<int64_t>((dm.nElm + 31) / 32, 152 * 16);
+  (k_pack_tet<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, s>>>(dm, fc.hasConv, u, pack), ::feng::count_launch());
+}
+
+void launch_rowtet_offsets(int64_t nEnt, const int32_t *ent, const int32_t *entRow, const int32_t *map,
+                           int64_t nElm, const int32_t *ia, uint8_t *offs, cudaStream_t s)
+{
+  const int64_t blocks = std::min<int64_t>((nEnt * ROWTET_OFFS + 255) / 256, 152 * 32);
+  (k_rowtet_offsets<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, s>>>(nEnt, ent, entRow, map, nElm, ia, offs),
+   ::feng::count_launch());
+}
+
+void launch_matrix_tet_rows_f32(const RowAsmTet &ra, const FormCoeffs &fc, const RefTensorsTet *dT, double c0,
+                                float *values, int accumulate, cudaStream_t s)
+{
+  if(ra.nBlocks <= 0) return;
+  const size_t sm = sizeof(float) * NTEN + (size_t)ra.capBytes;
+  static size_t set = 0;
+  if(set != sm) {
+    cudaFuncSetAttribute(k_matrix_tet_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    set = sm;
+  }
+  int dev = 0, nsm = 152, perSM = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_matrix_tet_rows, RT_WARPS * 32, sm);
+  const int grid = (int)std::min<int64_t>(ra.nBlocks, (int64_t)nsm * std::max(perSM, 1));
+  (k_matrix_tet_rows<<<grid, RT_WARPS * 32, sm, s>>>(ra, fc, dT, c0, values, accumulate), ::feng::count_launch());
 }
 
 void launch_build_map(const int32_t *adr, int64_t nElm, int nloc, const uint8_t *mask, const int32_t *ia,

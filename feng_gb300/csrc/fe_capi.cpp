@@ -866,6 +866,13 @@ int fe_cuda_get_du(const fe_cuda_system *s, double *du)
   return s->sys.getDu(du);
 }
 
+int fe_cuda_jacobian_route(const fe_cuda_system *s, int *route)
+{
+  if(!s || !route) { set_error("null argument"); return FE_INVALID_ARG; }
+  *route = s->sys.jacobianRoute();
+  return FE_OK;
+}
+
 int fe_cuda_get_du_max_norm(fe_cuda_system *s, double *norm)
 {
   GUARD_BEGIN

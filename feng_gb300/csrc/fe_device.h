@@ -135,6 +135,38 @@ struct RowAsm {
 };
 constexpr int ROWASM_PACK = 20;
 
+// Row-owned FP32 Jacobian of tetrahedral Taylor-Hood systems: one warp per
+// unit -- the three component rows of a velocity node (rows r, r + 1, r + 2,
+// which hold the same columns and the same elements), or one pressure row --
+// sums the element-matrix rows of the elements holding its DOF, in color
+// order, inside a shared-memory copy of its block's contiguous range of CSR
+// values, which the block then writes once.  Lane (m, b) of a velocity unit
+// forms the three columns (b, n) of row m; the element's packed data (u at
+// the 30 velocity DOFs, G, J) and the entry's column offsets are staged per
+// warp.  No atomics and no element-to-nonzero map at assembly time.
+struct RowAsmTet {
+  int nBlocks = 0;
+  int capBytes = 0;               // row values of a block in shared memory
+  int32_t *blockUnits = nullptr;  // [nBlocks + 1] first unit of each block
+  int32_t *unitRow = nullptr;     // [nUnits + 1] first row of each unit (the last entry: nInc)
+  int8_t *unitKind = nullptr;     // [nUnits] 3: velocity node (three rows), 1: pressure row
+  int32_t *unitPtr = nullptr;     // [nUnits + 1] entries of each unit
+  int32_t *ent = nullptr;         // [nEnt] p * 64 + local DOF of the unit's first row (3 a, or 30 + j)
+  uint8_t *offs = nullptr;        // [nEnt][ROWTET_OFFS] offset of local column j in the row (255: none)
+  float *pack = nullptr;          // [nElm][ROWTET_PACK] u at the 30 velocity DOFs, G[3][3], J
+  const int32_t *ia = nullptr;    // CSR row pointers
+};
+constexpr int ROWTET_PACK = 40;
+constexpr int ROWTET_OFFS = 40;
+
+void launch_pack_tet_f32(const DeviceMesh &dm, const FormCoeffs &fc, const double *u, float *pack, cudaStream_t s);
+// Column offsets of every entry from the element-to-nonzero map: entry k
+// (ent[k], first row entRow[k]) gets map[(li * 34 + j) * nElm + p] - ia[row].
+void launch_rowtet_offsets(int64_t nEnt, const int32_t *ent, const int32_t *entRow, const int32_t *map,
+                           int64_t nElm, const int32_t *ia, uint8_t *offs, cudaStream_t s);
+void launch_matrix_tet_rows_f32(const RowAsmTet &ra, const FormCoeffs &fc, const RefTensorsTet *dT, double c0,
+                                float *values, int accumulate, cudaStream_t s);
+
 // Per-element data of the row-owned assembly (RowAsm::pack), from u.
 void launch_pack_th_f32(const DeviceMesh &dm, const FormCoeffs &fc, const double *u, float *pack, cudaStream_t s);
 void launch_pack_th_f64(const DeviceMesh &dm, const FormCoeffs &fc, const double *u, double *pack, cudaStream_t s);

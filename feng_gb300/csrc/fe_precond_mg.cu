@@ -737,8 +737,29 @@ int Krylov::setTransientShift(double c0, double mu)
   M.lapDiagSum = M.amg->finestDiagSum();
   // Pressure Laplacian multigrid (built once) and the Cahouet-Chabard weight.
   if(c0 > 0. && !M.amgP) {
+    // With no pressure DOF fixed (velocity prescribed on the whole boundary,
+    // the pressure determined up to a constant) the P1 Laplacian is the pure
+    // Neumann one: constants span its null space and the coarsest direct
+    // solve would divide by a rounding-level pivot.  A diagonal shift of
+    // 1e-6 keeps it regular; k_p_gather projects the input to zero sum, so
+    // the shift only bounds the constant part of the output (a null vector
+    // of the saddle-point operator).
+    HostCSR Lp = M.lapPH;
+    double dmax = 0., rmax = 0.;
+    for(int64_t i = 0; i < Lp.n; ++i) {
+      double rs = 0.;
+      for(int64_t k = Lp.ia[i]; k < Lp.ia[i + 1]; ++k) {
+        rs += Lp.a[k];
+        if(Lp.ja[k] == i) dmax = std::max(dmax, std::fabs(Lp.a[k]));
+      }
+      rmax = std::max(rmax, std::fabs(rs));
+    }
+    if(rmax <= 1e-10 * dmax)
+      for(int64_t i = 0; i < Lp.n; ++i)
+        for(int64_t k = Lp.ia[i]; k < Lp.ia[i + 1]; ++k)
+          if(Lp.ja[k] == i) Lp.a[k] *= 1. + 1e-6;
     AMGHierarchy HP;
-    FE_TRY(amg_build(M.lapPH, M.params, HP));
+    FE_TRY(amg_build(Lp, M.params, HP));
     auto ap = std::make_unique<AMGDevice>();
     FE_TRY(ap->upload(HP, M.params, M.fp32, s_));
     M.amgP = std::move(ap);

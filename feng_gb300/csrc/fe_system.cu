@@ -233,6 +233,8 @@ SystemCUDA::~SystemCUDA()
   cudaFree(conRows_); cudaFree(conColPos_); cudaFree(perMaster_); cudaFree(perSlave_);
   cudaFree(ra_.blockUnits); cudaFree(ra_.unitRow); cudaFree(ra_.unitTwo); cudaFree(ra_.rowPtr); cudaFree(ra_.rowEnt);
   cudaFree(ra_.offs); cudaFree(ra_.pack);
+  cudaFree(rat_.blockUnits); cudaFree(rat_.unitRow); cudaFree(rat_.unitKind); cudaFree(rat_.unitPtr);
+  cudaFree(rat_.ent); cudaFree(rat_.offs); cudaFree(rat_.pack);
   cudaFree(dm_.geoPair); cudaFree(uPair_); cudaFree(udotPair_);
   if(ev0_) cudaEventDestroy(ev0_);
   if(ev1_) cudaEventDestroy(ev1_);
@@ -502,11 +504,21 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
       set_error("%llu coupled DOF pairs are missing from the CSR pattern", missing);
       return FE_INVALID_ARG;
     }
+    if(t.elemType == ELEM_TET_TAYLOR_HOOD) {
+      FE_TRY(build_row_assembly_tet(adrP, mask));
+      if(useRowsTet_) {
+        // the row-owned FP32 Jacobian is the only user of the map
+        CK(cudaFree(dm_.map));
+        dm_.map = nullptr;
+      }
+    }
   }
   if(opt.precision == 0) CK(cudaMalloc(&vals64_, sizeof(double) * nnz));
   else CK(cudaMalloc(&vals32_, sizeof(float) * nnz));
   zeroPending_ = true;
   ra_.ia = csr_.ia;
+  rat_.ia = csr_.ia;
+  if(useRowsTet_) CK(cudaMalloc(&rat_.pack, sizeof(float) * ROWTET_PACK * nE));
   if(useRows_) CK(cudaMalloc(&ra_.pack, (opt.precision == 0 ? sizeof(double) : sizeof(float)) * ROWASM_PACK * nE));
   CK(cudaMalloc(&rhs_, sizeof(double) * nInc_));
   CK(cudaMalloc(&du_, sizeof(double) * nInc_));
@@ -1162,6 +1174,104 @@ int SystemCUDA::build_row_assembly(const std::vector<int32_t> &adrP, const std::
   return FE_OK;
 }
 
+// Tables of the row-owned tetrahedral Taylor-Hood FP32 Jacobian (RowAsmTet):
+// units -- a velocity node's three component rows r, r + 1, r + 2 when they
+// hold the entries (element, 3 a + m) of the same elements in the same order
+// and the same columns, or a pressure row -- with the entries of their first
+// row in increasing color-order element (the colored scatter's summation
+// order); the column offsets come from the device element-to-nonzero map.
+// Declines (the colored scatter stays) for FP64 systems, rows of 255 or more
+// entries, or velocity rows that do not form such triples.
+int SystemCUDA::build_row_assembly_tet(const std::vector<int32_t> &adrP, const std::vector<uint8_t> &mask)
+{
+  const int64_t nE = dm_.nElm;
+  const int nl = nloc_;
+  if(opt.precision != 1 || nl != 34 || nE >= (int64_t(1) << 25)) return FE_OK;
+  for(int64_t r = 0; r < nInc_; ++r)
+    if(pat_.ia[r + 1] - pat_.ia[r] >= 255) return FE_OK;
+  for(int a = 0; a < 10; ++a)
+    for(int m = 1; m < 3; ++m)
+      for(int j = 0; j < nl; ++j)
+        if(mask[(3 * a + m) * nl + j] != mask[(3 * a) * nl + j]) return FE_OK;
+  std::vector<int32_t> rowPtr(nInc_ + 1, 0);
+  for(int li = 0; li < nl; ++li)
+    for(int64_t p = 0; p < nE; ++p) {
+      const int32_t d = adrP[(size_t)li * nE + p];
+      if(d < nInc_) ++rowPtr[d + 1];
+    }
+  for(int64_t r = 0; r < nInc_; ++r) rowPtr[r + 1] += rowPtr[r];
+  std::vector<int32_t> rowEnt(std::max<int32_t>(rowPtr[nInc_], 1)), fill(rowPtr.begin(), rowPtr.end() - 1);
+  for(int64_t p = 0; p < nE; ++p)
+    for(int li = 0; li < nl; ++li) {
+      const int32_t d = adrP[(size_t)li * nE + p];
+      if(d < nInc_) rowEnt[fill[d]++] = (int32_t)(p * 64 + li);
+    }
+  std::vector<int32_t> unitRow, unitPtr{0}, ent, entRow;
+  std::vector<int8_t> unitKind;
+  for(int64_t r = 0; r < nInc_;) {
+    const int32_t k0 = rowPtr[r], n0 = rowPtr[r + 1] - k0;
+    const bool vel = n0 > 0 && (rowEnt[k0] & 63) < 30;
+    if(vel) {
+      bool ok = r + 2 < nInc_ && rowPtr[r + 2] - rowPtr[r + 1] == n0 && rowPtr[r + 3] - rowPtr[r + 2] == n0;
+      const int64_t rl = pat_.ia[r + 1] - pat_.ia[r];
+      ok = ok && pat_.ia[r + 2] - pat_.ia[r + 1] == rl && pat_.ia[r + 3] - pat_.ia[r + 2] == rl;
+      for(int32_t k = 0; ok && k < n0; ++k) {
+        const int32_t e = rowEnt[k0 + k];
+        ok = (e & 63) % 3 == 0 && rowEnt[rowPtr[r + 1] + k] == e + 1 && rowEnt[rowPtr[r + 2] + k] == e + 2;
+      }
+      for(int64_t j = 0; ok && j < rl; ++j)
+        ok = pat_.ja[pat_.ia[r] + j] == pat_.ja[pat_.ia[r + 1] + j] && pat_.ja[pat_.ia[r] + j] == pat_.ja[pat_.ia[r + 2] + j];
+      if(!ok) return FE_OK;
+    } else {
+      for(int32_t k = 0; k < n0; ++k)
+        if((rowEnt[k0 + k] & 63) < 30) return FE_OK;
+    }
+    unitRow.push_back((int32_t)r);
+    unitKind.push_back(vel ? 3 : 1);
+    for(int32_t k = 0; k < n0; ++k) {
+      ent.push_back(rowEnt[k0 + k]);
+      entRow.push_back((int32_t)r);
+    }
+    unitPtr.push_back((int32_t)ent.size());
+    r += vel ? 3 : 1;
+  }
+  const int64_t nUnits = (int64_t)unitRow.size();
+  unitRow.push_back((int32_t)nInc_);
+  const int cap = 32 * 1024 / (int)sizeof(float);  // row values per block in shared memory
+  std::vector<int32_t> blockUnits{0};
+  for(int64_t u0 = 0; u0 < nUnits;) {
+    int64_t u1 = u0 + 1;
+    while(u1 < nUnits && u1 - u0 < 128 && pat_.ia[unitRow[u1 + 1]] - pat_.ia[unitRow[u0]] <= cap) ++u1;
+    blockUnits.push_back((int32_t)u1);
+    u0 = u1;
+  }
+  const int64_t nEnt = (int64_t)ent.size();
+  rat_.nBlocks = (int)blockUnits.size() - 1;
+  rat_.capBytes = cap * (int)sizeof(float);
+  int32_t *dEntRow = nullptr;
+  CK(cudaMalloc(&rat_.blockUnits, sizeof(int32_t) * blockUnits.size()));
+  CK(cudaMalloc(&rat_.unitRow, sizeof(int32_t) * unitRow.size()));
+  CK(cudaMalloc(&rat_.unitKind, std::max<size_t>(1, unitKind.size())));
+  CK(cudaMalloc(&rat_.unitPtr, sizeof(int32_t) * unitPtr.size()));
+  CK(cudaMalloc(&rat_.ent, sizeof(int32_t) * std::max<int64_t>(nEnt, 1)));
+  CK(cudaMalloc(&dEntRow, sizeof(int32_t) * std::max<int64_t>(nEnt, 1)));
+  CK(cudaMalloc(&rat_.offs, (size_t)ROWTET_OFFS * std::max<int64_t>(nEnt, 1)));
+  CK(cudaMemcpy(rat_.blockUnits, blockUnits.data(), sizeof(int32_t) * blockUnits.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(rat_.unitRow, unitRow.data(), sizeof(int32_t) * unitRow.size(), cudaMemcpyHostToDevice));
+  if(!unitKind.empty()) CK(cudaMemcpy(rat_.unitKind, unitKind.data(), unitKind.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(rat_.unitPtr, unitPtr.data(), sizeof(int32_t) * unitPtr.size(), cudaMemcpyHostToDevice));
+  if(nEnt) {
+    CK(cudaMemcpy(rat_.ent, ent.data(), sizeof(int32_t) * nEnt, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dEntRow, entRow.data(), sizeof(int32_t) * nEnt, cudaMemcpyHostToDevice));
+    launch_rowtet_offsets(nEnt, rat_.ent, dEntRow, dm_.map, nE, csr_.ia, rat_.offs, s_);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s_));
+  }
+  cudaFree(dEntRow);
+  useRowsTet_ = true;
+  return FE_OK;
+}
+
 int SystemCUDA::setResidualToZero()
 {
   CK(cudaMemsetAsync(rhs_, 0, sizeof(double) * nInc_, s_));
@@ -1210,6 +1320,13 @@ int SystemCUDA::launch_matrix()
       launch_pack_th_f32(dm_, fc_, u_, (float *)ra_.pack, s_);
       launch_matrix_th_rows_f32(ra_, fc_, dT_, c0_, vals32_, acc, s_);
     }
+    return FE_OK;
+  }
+  if(useRowsTet_) {
+    const int acc = zeroPending_ ? 0 : 1;
+    zeroPending_ = false;
+    launch_pack_tet_f32(dm_, fc_, u_, rat_.pack, s_);
+    launch_matrix_tet_rows_f32(rat_, fc_, dTt_, c0_, vals32_, acc, s_);
     return FE_OK;
   }
   FE_TRY(ensureMatrixZeroed());
@@ -1532,7 +1649,7 @@ int SystemCUDA::benchPhase(int which, int reps, size_t flushBytes, double *avgMs
       case 1:
         // as in a Newton step: zeroed matrix, then the Jacobian (the
         // row-owned assembly writes the values, the colored scatter adds)
-        if(useRows_) zeroPending_ = true;
+        if(useRows_ || useRowsTet_) zeroPending_ = true;
         else {
           // the colored scatter adds: its zeroing pass is part of the phase
           zeroPending_ = true;

@@ -131,6 +131,8 @@ class SystemCUDA {
   // preconditioner application, 4 one finest-level multigrid smoother step
   // (two components).  Returns the mean milliseconds per run.
   int benchPhase(int which, int reps, size_t flushBytes, double *avgMs);
+  // 1 when the Jacobian is assembled row-owned (no scatter), 0 colored.
+  int jacobianRoute() const { return useRows_ || useRowsTet_ ? 1 : 0; }
 
   // Host copies of the set-up tables (original element order).
   const std::vector<int64_t> &elementTable() const { return adrHost_; }
@@ -167,6 +169,10 @@ class SystemCUDA {
   // than 255).
   RowAsm ra_;
   bool useRows_ = false;
+  // Row-owned FP32 Jacobian of tetrahedral Taylor-Hood systems.
+  RowAsmTet rat_;
+  bool useRowsTet_ = false;
+  int build_row_assembly_tet(const std::vector<int32_t> &adrP, const std::vector<uint8_t> &mask);
   // setMatrixToZero is deferred: the next row-owned assembly overwrites the
   // values instead of adding to them; any other use of the values zeroes
   // them first.

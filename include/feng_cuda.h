@@ -313,6 +313,11 @@ void fe_cuda_system_destroy(fe_cuda_system *s);
 
 int fe_cuda_system_sizes(const fe_cuda_system *s, int64_t *n_inc, int64_t *n_dofs, int64_t *nnz,
                          int64_t *n_elm, int *n_colors);
+/* How the Jacobian is assembled: 1 row-owned (each CSR row summed by its
+ * owner in color order; the FP32 Taylor-Hood Jacobians whose rows hold fewer
+ * than 255 entries), 0 the colored scatter.  Both give the same sums in
+ * the same order. */
+int fe_cuda_jacobian_route(const fe_cuda_system *s, int *route);
 int fe_cuda_get_pattern(const fe_cuda_system *s, int64_t *ia, int32_t *ja);
 int fe_cuda_get_coloring(const fe_cuda_system *s, int64_t *offsets, int32_t *elements);
 /* Rejects a coloring in which two elements of one color share a vertex DOF. */

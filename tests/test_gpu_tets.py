@@ -124,6 +124,14 @@ def test_tet_taylor_hood_matches_oracle(precision):
                                                     0.0 * x, 0.0 * x))
     assert rel_err(sys_.getRHS(), rhs) <= TOL_FP64
     assert rel_err(sys_.getMatrix(), vals) <= (TOL_FP64 if precision == "fp64" else TOL_FP32)
+    # the FP32 Jacobian is assembled row-owned (warp per velocity node or
+    # pressure row), the FP64 one by the colored scatter; a second assembly
+    # after setToZero overwrites the values, it does not add to them
+    assert sys_.jacobianRoute == (1 if precision == "mixed" else 0)
+    sys_.setToZero()
+    sys_.assembleMatrices()
+    sys_.synchronize()
+    assert rel_err(sys_.getMatrix(), vals) <= (TOL_FP64 if precision == "fp64" else TOL_FP32)
 
 
 @pytest.mark.parametrize("n", [4, 6])
