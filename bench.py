@@ -447,6 +447,7 @@ def c5_leg(n=64, reps=5, steps=50, steps_fp64=10):
     t0 = time.perf_counter()
     mesh, num, forms = cube.build(n, 100.0)
     out["host_setup_s"] = time.perf_counter() - t0
+    out["pattern_on_device"] = num.setup().patternOnDevice
     nvert = mesh.sizes()[0]
     peak, peak_kind = measured_peaks()
     for prec in ("fp64", "mixed"):

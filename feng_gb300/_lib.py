@@ -153,6 +153,8 @@ SIGNATURES = {
     "fe_cuda_get_du": (C.c_int, [P, P]),
     "fe_cuda_get_du_max_norm": (C.c_int, [P, C.POINTER(C.c_double)]),
     "fe_cuda_jacobian_route": (C.c_int, [P, C.POINTER(C.c_int)]),
+    "fe_setup_set_pattern_mode": (C.c_int, [C.c_int]),
+    "fe_setup_pattern_on_device": (C.c_int, [P, C.POINTER(C.c_int)]),
     "fe_cuda_newton": (C.c_int, [P, C.POINTER(NewtonOptions), C.POINTER(NewtonStats)]),
     "fe_cuda_get_times": (C.c_int, [P, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                     C.POINTER(C.c_double), C.POINTER(C.c_double)]),

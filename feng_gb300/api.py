@@ -247,9 +247,16 @@ class feMetaNumber:
         return self.nDofs
 
 
+def setPatternMode(mode: int):
+    """Where set-ups build the CSR pattern: -1 the CUDA device when one is
+    present (default), 0 the host threads, 1 the device."""
+    check(_lib.load().fe_setup_set_pattern_mode(int(mode)))
+
+
 class feSetup:
-    """Host set-up of the standalone route (fe_setup_* in include/feng_cuda.h);
-    needs no GPU."""
+    """Set-up of the standalone route (fe_setup_* in include/feng_cuda.h):
+    host threads, the CSR pattern on the device when one is present; needs
+    no GPU."""
 
     def __init__(self, numbering: feMetaNumber, pc_block_rows: int = 256):
         self.lib = _lib.load()
@@ -280,6 +287,12 @@ class feSetup:
         ja = np.empty(self.nnz, np.int32)
         check(self.lib.fe_setup_get_pattern(self._h, ptr(ia), ptr(ja)))
         return ia, ja
+
+    @property
+    def patternOnDevice(self) -> bool:
+        v = C.c_int()
+        check(self.lib.fe_setup_pattern_on_device(self._h, C.byref(v)))
+        return bool(v.value)
 
     def coloring(self):
         off = np.empty(self.nColors + 1, np.int64)

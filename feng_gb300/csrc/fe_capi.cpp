@@ -66,6 +66,7 @@ struct fe_setup {
   ElementTables et;
   Coloring col;
   CSRPattern pat;
+  int patternOnDevice = 0;            // the pattern was built on the device
   std::vector<int32_t> blockOfRow;
   std::vector<double> elemXY;
   QuadRule quad;
@@ -413,7 +414,7 @@ int fe_setup_create(const fe_mesh *m, const fe_space_desc *spaces, int nspaces, 
   FE_TRY(build_element_tables(M, S->num, elem_type, fieldU,
                               elem_type == ELEM_TAYLOR_HOOD ? fieldP : -1, S->et));
   FE_TRY(color_elements(M, S->col));
-  FE_TRY(build_csr_pattern(S->et, S->num.nInc, S->pat));
+  FE_TRY(build_csr_pattern_auto(S->et, S->num.nInc, S->pat, &S->patternOnDevice));
   FE_TRY(triangle_rule(quad_degree, S->quad));
   block_partition(S->num, S->pat, M.edge_v.data(), M.n_edges, M.n_vertices(), pc_block_rows,
                   elem_type == ELEM_TAYLOR_HOOD, fieldU, fieldP, S->blockOfRow);
@@ -456,7 +457,7 @@ int fe_setup3d_create(const fe_mesh3d *m, const fe_space_desc *spaces, int nspac
   FE_TRY(build_element_tables3d(M, S->num, elem_type, fieldU, elem_type == ELEM_TET_TAYLOR_HOOD ? fieldP : -1,
                                 S->et));
   FE_TRY(color_elements3d(M, S->col));
-  FE_TRY(build_csr_pattern(S->et, S->num.nInc, S->pat));
+  FE_TRY(build_csr_pattern_auto(S->et, S->num.nInc, S->pat, &S->patternOnDevice));
   block_partition(S->num, S->pat, M.edge_v.data(), M.n_edges, M.n_vertices(), pc_block_rows,
                   elem_type == ELEM_TET_TAYLOR_HOOD, fieldU, fieldP, S->blockOfRow);
   // vertex coordinates per tetrahedron: x0 y0 z0 ... x3 y3 z3
@@ -864,6 +865,18 @@ int fe_cuda_get_du(const fe_cuda_system *s, double *du)
 {
   if(!s || !du) { set_error("null argument"); return FE_INVALID_ARG; }
   return s->sys.getDu(du);
+}
+
+int fe_setup_set_pattern_mode(int mode)
+{
+  return set_pattern_mode(mode);
+}
+
+int fe_setup_pattern_on_device(const fe_setup *s, int *on_device)
+{
+  if(!s || !on_device) { set_error("null argument"); return FE_INVALID_ARG; }
+  *on_device = s->patternOnDevice;
+  return FE_OK;
 }
 
 int fe_cuda_jacobian_route(const fe_cuda_system *s, int *route)

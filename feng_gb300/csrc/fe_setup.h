@@ -117,6 +117,15 @@ struct CSRPattern {
 };
 
 int build_csr_pattern(const ElementTables &et, int64_t nInc, CSRPattern &pat);
+// The same pattern built on the current CUDA device (fe_pattern.cu).
+int build_csr_pattern_device(const ElementTables &et, int64_t nInc, CSRPattern &pat);
+// Where set-ups build their pattern: -1 on the device when one is present
+// (the default; the host when a row exceeds the device path's capacity),
+// 0 on the host, 1 on the device.
+int set_pattern_mode(int mode);
+int pattern_mode();
+// The pattern by the current mode; *onDevice (may be NULL) tells which ran.
+int build_csr_pattern_auto(const ElementTables &et, int64_t nInc, CSRPattern &pat, int *onDevice);
 
 // For each element (in coloring order) and each coupled local pair (i,j), the
 // position of (adr_i, adr_j) in the CSR arrays, or -1 when either DOF is

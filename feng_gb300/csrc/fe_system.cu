@@ -365,7 +365,7 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
   elemType_ = t.elemType;
   FE_TRY(validateColoring());
   if(t.pattern && t.pattern->n == nInc_) pat_ = *t.pattern;
-  else FE_TRY(build_csr_pattern(et, nInc_, pat_));
+  else FE_TRY(build_csr_pattern_auto(et, nInc_, pat_, nullptr));
   std::vector<int32_t> map;
   // Tetrahedra: the element-to-nonzero map is built on the device below.
   if(!tet) FE_TRY(build_scatter_map(et, col_, pat_, nInc_, map));

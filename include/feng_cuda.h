@@ -204,14 +204,16 @@ int fe_mesh3d_sizes(const fe_mesh3d *m, int64_t *n_vertices, int64_t *n_tets, in
 int fe_mesh3d_arrays(const fe_mesh3d *m, double *x, double *y, double *z, int32_t *tet, int32_t *bnd);
 void fe_mesh3d_destroy(fe_mesh3d *m);
 
-/* ---- host set-up of the standalone route (no device needed):
- * DOF numbering (feMetaNumber, src/feNumber.cpp:677-835), element-to-DOF
- * tables of elem_type (the P2 space on "Domaine" is the scalar / velocity
- * field, the P1 space on "Domaine" the pressure), element coloring
- * (feCncGeo::colorElements(1), src/feCncGeo.cpp:735), CSR pattern
- * (feEZCompressedRowStorage, src/feCompressedRowStorage.cpp:15-135),
- * quadrature rule (getGQTPts, src/feQuadratureTri.cpp:874) and a
- * block-Jacobi partition with about pc_block_rows unknowns per block. */
+/* ---- set-up of the standalone route: DOF numbering (feMetaNumber,
+ * src/feNumber.cpp:677-835), element-to-DOF tables of elem_type (the P2
+ * space on "Domaine" is the scalar / velocity field, the P1 space on
+ * "Domaine" the pressure), element coloring (feCncGeo::colorElements(1),
+ * src/feCncGeo.cpp:735), CSR pattern (feEZCompressedRowStorage,
+ * src/feCompressedRowStorage.cpp:15-135), quadrature rule (getGQTPts,
+ * src/feQuadratureTri.cpp:874) and a block-Jacobi partition with about
+ * pc_block_rows unknowns per block.  All on the host threads except the CSR
+ * pattern, which is built on the current CUDA device when one is present
+ * (the same pattern, bit for bit; fe_setup_set_pattern_mode). */
 typedef struct fe_setup fe_setup;
 int fe_setup_create(const fe_mesh *m, const fe_space_desc *spaces, int nspaces, int elem_type,
                     int quad_degree, int pc_block_rows, fe_setup **out);
@@ -226,12 +228,20 @@ void fe_setup_destroy(fe_setup *s);
  * fe_cuda_system_create refuses it). */
 int fe_setup3d_create(const fe_mesh3d *m, const fe_space_desc *spaces, int nspaces, int elem_type,
                       int pc_block_rows, fe_setup **out);
-/* z coordinate of every DOF (tetrahedral set-ups only). */
 /* Replaces the set-up's quadrature rule (nq rows (r, s, w) or, on
  * tetrahedra, (r, s, t, w)), e.g. with the reference's tabulated values;
  * without it a tetrahedral set-up takes the rule of the options' degree. */
 int fe_setup_set_quadrature(fe_setup *s, int nq, const double *rule);
+/* z coordinate of every DOF (tetrahedral set-ups only). */
 int fe_setup_get_dof_z(const fe_setup *s, double *z);
+/* Where the set-ups created afterwards (and the systems created from tables
+ * without a pattern) build the CSR pattern: -1 on the current CUDA device
+ * when one is present, else on the host (the default; also the host when a
+ * row has more than 1023 candidate columns), 0 on the host threads, 1 on the
+ * device (an error without one).  Process-wide. */
+int fe_setup_set_pattern_mode(int mode);
+/* 1 when the set-up's pattern was built on the device. */
+int fe_setup_pattern_on_device(const fe_setup *s, int *on_device);
 int fe_setup_sizes(const fe_setup *s, int64_t *n_inc, int64_t *n_dofs, int64_t *nnz,
                    int64_t *n_elm, int *n_colors, int *nloc);
 /* Outputs may be NULL.  ia [n_inc+1], ja [nnz]. */
