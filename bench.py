@@ -229,7 +229,7 @@ def algorithmic_bytes(sys_, nvert, precision):
     from feng_gb300._lib import check
     out = {"residual_assembly": res, "matrix_assembly": mat, "spmv": spmv}
     for which, name in ((4, "smoother_step"), (5, "gs_dots"), (6, "gs_update"), (7, "gs_dots_stream"),
-                        (8, "gs_update_stream")):
+                        (8, "gs_update_stream"), (9, "gs_dots_bulk"), (10, "gs_dots_bulk_stream")):
         if which > 4 and precision != "mixed":
             continue
         b = C.c_int64()
@@ -261,7 +261,8 @@ def phase_bench(sys_, mixed, reps=20):
     out = {}
     phases = [(0, "residual_assembly"), (1, "matrix_assembly"), (2, "spmv"), (3, "preconditioner"),
               (4, "smoother_step")] + ([(5, "gs_dots"), (6, "gs_update"), (7, "gs_dots_stream"),
-                                        (8, "gs_update_stream")] if mixed else [])
+                                        (8, "gs_update_stream"), (9, "gs_dots_bulk"),
+                                        (10, "gs_dots_bulk_stream")] if mixed else [])
     for which, name in phases:
         ms = C.c_double()
         check(sys_.lib.fe_cuda_bench_phase(sys_._h, which, reps, 256 << 20, C.byref(ms)))
@@ -586,8 +587,9 @@ def main():
     shares = {"assembly": ph["residual_ms"] + ph["matrix_ms"], "krylov_solve": ph["solve_ms"],
               "preconditioner_build": ph["factor_ms"]}
     # The dominant kernel of the Newton step (the Krylov solve is ~97% of it,
-    # and its largest kernel by time is the Gram-Schmidt dot pass): k_gs_dots
-    # at the mean column count of a restart cycle.
+    # and its largest kernel by time is the Gram-Schmidt dot pass): the
+    # first-pass dot kernel, k_gs_dots_bulk, at the mean column count of a
+    # restart cycle.
     def roofline(key, kernel, traffic_key):
         # the streamed timing (launches back to back over cold data) where the
         # phase has one, with the single flushed launch beside it
@@ -601,7 +603,10 @@ def main():
         if ks:
             out["single_launch"] = {"ms": k["ms"], "achieved": k["gbs"], "frac": k["gbs"] / peak}
         return out
-    roof = roofline("gs_dots", "k_gs_dots (FP32 Gram-Schmidt dot pass, 25 basis vectors)", "k_gs_dots@25")
+    roof = roofline("gs_dots_bulk", "k_gs_dots_bulk (FP32 Gram-Schmidt dot pass, cp.async.bulk stages, "
+                    "25 basis vectors)", "k_gs_dots_bulk@25")
+    roof_gsd = roofline("gs_dots", "k_gs_dots (register-streaming dot pass with its reduction tail, second "
+                        "Gram-Schmidt pass and small systems, 25 basis vectors)", "k_gs_dots@25")
     roof_gsu = roofline("gs_update", "k_gs_upd<32,true> (FP32 Gram-Schmidt update + norm, 25 basis vectors)",
                         "k_gs_upd<32,true>@25")
     roof_sm = roofline("smoother_step", "k_cheb_first_sell<float,2> (finest AMG level, both velocity components)",
@@ -642,7 +647,8 @@ def main():
                           "mixed_precision_at_same_forcing": (t_forc / args.steps) / value},
         "phase_share_ms": shares,
         "kernels": kern,
-        "roofline": roof, "roofline_gs_update": roof_gsu, "roofline_smoother": roof_sm,
+        "roofline": roof, "roofline_gs_dots_register": roof_gsd, "roofline_gs_update": roof_gsu,
+        "roofline_smoother": roof_sm,
         "roofline_assembly": roof_asm, "roofline_spmv": roof_spmv,
         "e2e": {"value": e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": l_mixed,

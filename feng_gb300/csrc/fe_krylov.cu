@@ -623,6 +623,156 @@ __global__ void __launch_bounds__(RB) k_gs_dots(int64_t n4, int64_t ld, const fl
   }
 }
 
+// ---- bulk-copy (TMA) streaming: mbarrier and cp.async.bulk in inline PTX
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned bytes)
+{
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                   smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// global -> shared, completion counted in bytes on the mbarrier (16-byte
+// aligned addresses, a multiple of 16 bytes)
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes, uint64_t *bar)
+{
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+// Waits for the phase of the given parity; false when 2^22 polls ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity)
+{
+  for(int it = 0; it < (1 << 22); ++it) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_addr(bar)), "r"(parity)
+                 : "memory");
+    if(ok) return true;
+  }
+  return false;
+}
+
+constexpr int BULK_MAXST = 8;  // stages of the bulk dot pass
+constexpr int BULK_ACC = 32;   // column accumulators per thread
+
+// The first Gram-Schmidt dot pass with bulk copies (mode 6): one block per
+// SM walks chunks of `rows` rows (a power of two, 256..1024); per stage the
+// chunk of w and of each of the ncols columns lands in shared memory (one
+// cp.async.bulk per column, issued by the lanes of warp 0; completion on the
+// stage's mbarrier, waited for with a bound), `nst` stages in flight.
+// Thread (g, q), q < rows / 4, g < G = 1024 / rows, takes float4 row q of the
+// chunk and the columns c = g (mod G).  Per block, the FP64 partial of every
+// column and of ||w||^2 (column ncols) goes to partials[c][blockIdx.x]; no
+// reduction tail: the update pass that follows (k_gs_upd, FROMPART) sums
+// them.  A wait that runs out writes NaN partials (the Arnoldi step then
+// fails as non-finite) after a bounded wait for the copies in flight.
+__global__ void __launch_bounds__(RB, 1) k_gs_dots_bulk(int64_t ld, const float *__restrict__ V, int ncols,
+                                                        const float *__restrict__ w, double *partials,
+                                                        const int *__restrict__ done, int rows, int nst)
+{
+  if(*done) return;
+  extern __shared__ __align__(128) unsigned char gsmem[];
+  float *buf = reinterpret_cast<float *>(gsmem);  // [nst][ncols + 1][rows]
+  __shared__ uint64_t full[BULK_MAXST];
+  __shared__ double red[RB / 32][BULK_ACC + 1];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int F = rows / 4, G = RB / F, g = tid / F, q = tid % F;
+  const int nsl = ncols + 1;
+  const int64_t nChunks = (ld + rows - 1) / rows;
+  if(tid == 0) {
+    for(int i = 0; i < nst; ++i) mbar_init(&full[i], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // warp 0: stage st <- chunk ch (lane 0 arms the barrier first)
+  auto issue = [&](int st, int64_t ch) {
+    const int64_t r0 = ch * rows;
+    const unsigned bytes = (unsigned)((ld - r0 < rows ? ld - r0 : rows) * 4);
+    if(lane == 0) mbar_arrive_expect_tx(&full[st], bytes * nsl);
+    __syncwarp();
+    float *dst = buf + (int64_t)st * nsl * rows;
+    for(int c = lane; c < nsl; c += 32)
+      bulk_copy_g2s(dst + (int64_t)c * rows, c == 0 ? w + r0 : V + (int64_t)(c - 1) * ld + r0, bytes, &full[st]);
+  };
+  if(warp == 0)
+    for(int i = 0; i < nst; ++i)
+      if(blockIdx.x + (int64_t)i * gridDim.x < nChunks) issue(i, blockIdx.x + (int64_t)i * gridDim.x);
+  float acc[BULK_ACC];
+#pragma unroll
+  for(int i = 0; i < BULK_ACC; ++i) acc[i] = 0.f;
+  float wq = 0.f;
+  const int slots = (ncols + G - 1) / G;
+  bool ok = true;
+  int k = 0;
+  for(int64_t ch = blockIdx.x; ch < nChunks; ch += gridDim.x, ++k) {
+    const int st = k % nst;
+    if(!__syncthreads_and(mbar_wait_bounded(&full[st], (unsigned)((k / nst) & 1)))) {
+      ok = false;
+      break;
+    }
+    const int64_t r0 = ch * rows;
+    if((int64_t)4 * q < ld - r0) {
+      const float4 *src = reinterpret_cast<const float4 *>(buf + (int64_t)st * nsl * rows);
+      const float4 x = src[q];
+      if(g == 0) wq = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, wq))));
+#pragma unroll
+      for(int i = 0; i < BULK_ACC; ++i) {
+        const int c = g + i * G;
+        if(i < slots && c < ncols) {
+          const float4 v = src[(int64_t)(c + 1) * F + q];
+          acc[i] = fmaf(v.x, x.x, fmaf(v.y, x.y, fmaf(v.z, x.z, fmaf(v.w, x.w, acc[i]))));
+        }
+      }
+    }
+    __syncthreads();
+    const int64_t nx = ch + (int64_t)nst * gridDim.x;
+    if(warp == 0 && nx < nChunks) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(st, nx);
+    }
+  }
+  if(!ok) {
+    // let the copies in flight land before the block exits
+    for(int i = 0; i < nst; ++i) {
+      mbar_wait_bounded(&full[i], 0);
+      mbar_wait_bounded(&full[i], 1);
+    }
+    for(int c = tid; c <= ncols; c += RB) partials[(int64_t)c * MAXRED + blockIdx.x] = __longlong_as_double(0x7ff8000000000000ll);
+    return;
+  }
+#pragma unroll
+  for(int i = 0; i < BULK_ACC; ++i) {
+    if(i < slots) {
+      float a = acc[i];
+      for(int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+      if(lane == 0) red[warp][i] = (double)a;
+    }
+  }
+  for(int o = 16; o > 0; o >>= 1) wq += __shfl_xor_sync(0xffffffffu, wq, o);
+  if(lane == 0) red[warp][BULK_ACC] = (double)wq;
+  __syncthreads();
+  if(tid <= ncols) {
+    // column c: slot c / G of the warps of group c % G (warp order)
+    const int c = tid;
+    const int gg = c < ncols ? c % G : 0, slot = c < ncols ? c / G : BULK_ACC;
+    const int wpg = F / 32;  // warps per group
+    double sum = 0.;
+    for(int k2 = 0; k2 < wpg; ++k2) sum += red[gg * wpg + k2][slot];
+    partials[(int64_t)c * MAXRED + blockIdx.x] = sum;
+  }
+}
+
 // The update pass w - V h over c < ncols.
 // NORM: the result goes back to w and its squared norm is reduced (one FP64
 // partial per block, the last block sums them in block order): H[j+1][j] =
@@ -633,17 +783,60 @@ __global__ void __launch_bounds__(RB) k_gs_dots(int64_t n4, int64_t ld, const fl
 // !NORM (after a dot pass that took the norm by Pythagoras): unless a second
 // pass was asked for, the result times st->finv is the next basis vector
 // (vnext); otherwise it goes back to w.
-template <int CMAX, bool NORM>
+// FROMPART (NORM, first pass, after k_gs_dots_bulk): every block first sums
+// the dot pass's per-block partials (nparts per column, the same order in
+// every block) into h and ||w||^2; block 0 stores h as hcur and as the
+// Hessenberg column (Hcol[c], c < ncols) and ||w||^2 in st->result[2]; the
+// norm partials of this pass go to the column after the last dot column.
+template <int CMAX, bool NORM, bool FROMPART = false>
 __global__ void __launch_bounds__(RB, 4) k_gs_upd(int64_t n4, int64_t ld, const float *__restrict__ V, int ncols,
                                                   const double *__restrict__ hprev, float *__restrict__ w,
                                                   float *__restrict__ vnext, RedState *st, double *partials,
-                                                  double *Hnext, const int *__restrict__ done, int second)
+                                                  double *Hnext, const int *__restrict__ done, int second,
+                                                  int nparts = 0, double *hcur = nullptr, double *Hcol = nullptr)
 {
   if(*done || (NORM && second && !st->reorth)) return;
   __shared__ float hs[CMAX];
   __shared__ double wred[RB / 32];
+  __shared__ double hsd[CMAX + 1];
   __shared__ bool last;
-  for(int c = threadIdx.x; c < CMAX; c += RB) hs[c] = c < ncols ? (float)hprev[c] : 0.f;
+  if constexpr(FROMPART) {
+    // columns c = warp + 8 u, all loads of a round in flight at once
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for(int c0 = warp; c0 <= ncols; c0 += 4 * (RB / 32)) {
+      double sm[4] = {0., 0., 0., 0.};
+#pragma unroll
+      for(int u = 0; u < 4; ++u) {
+        const int c = c0 + u * (RB / 32);
+#pragma unroll
+        for(int b8 = 0; b8 < 8; ++b8) {
+          const int b = lane + 32 * b8;
+          if(c <= ncols && b < nparts) sm[u] += __ldcg(partials + (int64_t)c * MAXRED + b);
+        }
+      }
+#pragma unroll
+      for(int u = 0; u < 4; ++u) {
+        double v = sm[u];
+        for(int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        const int c = c0 + u * (RB / 32);
+        if(lane == 0 && c <= ncols) hsd[c] = v;
+      }
+    }
+    __syncthreads();
+    for(int c = threadIdx.x; c < CMAX; c += RB) hs[c] = c < ncols ? (float)hsd[c] : 0.f;
+    if(blockIdx.x == 0)
+      for(int c = threadIdx.x; c <= ncols; c += RB) {
+        if(c < ncols) {
+          hcur[c] = hsd[c];
+          Hcol[c] = hsd[c];
+        } else {
+          st->result[2] = hsd[c];
+        }
+      }
+    partials += (int64_t)(ncols + 1) * MAXRED;
+  } else {
+    for(int c = threadIdx.x; c < CMAX; c += RB) hs[c] = c < ncols ? (float)hprev[c] : 0.f;
+  }
   __syncthreads();
   const bool again = NORM || st->reorth != 0;
   const float inv = NORM ? 1.f : st->finv;
@@ -713,7 +906,7 @@ __global__ void __launch_bounds__(RB, 4) k_gs_upd(int64_t n4, int64_t ld, const 
       st->result[0] = sum;
       *Hnext = nrm;
       st->finv = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
-      if(!second) st->reorth = sum < 1e-2 * st->result[2] ? 1 : 0;
+      if(!second) st->reorth = sum < 1e-2 * (FROMPART ? hsd[ncols] : st->result[2]) ? 1 : 0;
       st->counter = 0;
     }
   }
@@ -1108,6 +1301,12 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
   }
   // whole waves of the update passes (three blocks per SM)
   gsParts_ = grid_for((n_ + 3) / 4, RB, std::min(MAXRED, 3 * nSM_));
+  // bulk-copy dot pass: one block per SM (the update pass sums up to 256
+  // partials per column), basis columns long enough to fill the stages
+  if(opt.method == 1 && opt.mixed && nSM_ <= 256 && ld32_ >= (int64_t)1024 * nSM_) {
+    CK(cudaFuncSetAttribute(k_gs_dots_bulk, cudaFuncAttributeMaxDynamicSharedMemorySize, 220000));
+    bulkGs_ = true;
+  }
   CK(cudaMalloc(&v32_, sizeof(float) * n_));
   CK(cudaMalloc(&w32_, sizeof(float) * ((n_ + 63) / 64 * 64)));
   CK(cudaMemset(w32_, 0, sizeof(float) * ((n_ + 63) / 64 * 64)));
@@ -1523,7 +1722,7 @@ double Krylov::norminf(const double *x)
 
 int Krylov::gsStep(int mode, int ncols, int64_t *bytes)
 {
-  if(!V32_ || (mode != 0 && mode != 4) || ncols < 1 || ncols > opt.restart) {
+  if(!V32_ || (mode != 0 && mode != 4 && !(mode == 6 && bulkGs_)) || ncols < 1 || ncols > opt.restart) {
     set_error("no mixed FP32 basis, or an invalid Gram-Schmidt request");
     return FE_INVALID_ARG;
   }
@@ -1533,16 +1732,18 @@ int Krylov::gsStep(int mode, int ncols, int64_t *bytes)
   }
   Ws w = Ws_INIT(this);
   if(mode == 0) gs32(0, ncols, nullptr, w.gs->hcur, w.gs->H, zeroFlag_, 0);
+  else if(mode == 6) gs32(6, ncols, nullptr, nullptr, nullptr, zeroFlag_, 0);
   else gs32(4, ncols, w.gs->hcur, nullptr, w.gs->H + ncols, zeroFlag_, 0);
   // dots: ncols columns and w read; update: ncols columns and w read, w
   // written
-  if(bytes) *bytes = (int64_t)(ncols + (mode == 0 ? 1 : 2)) * ld32_ * (int64_t)sizeof(float);
+  if(bytes) *bytes = (int64_t)(ncols + (mode == 4 ? 2 : 1)) * ld32_ * (int64_t)sizeof(float);
   return FE_OK;
 }
 
 int Krylov::gsStepStream(int mode, int ncols, int reps, double *avgMs)
 {
-  if(!V32_ || (mode != 0 && mode != 4) || ncols < 1 || ncols > opt.restart || reps < 1 || !avgMs) {
+  if(!V32_ || (mode != 0 && mode != 4 && !(mode == 6 && bulkGs_)) || ncols < 1 || ncols > opt.restart || reps < 1 ||
+     !avgMs) {
     set_error("no mixed FP32 basis, or an invalid Gram-Schmidt request");
     return FE_INVALID_ARG;
   }
@@ -1573,6 +1774,7 @@ int Krylov::gsStepStream(int mode, int ncols, int reps, double *avgMs)
     V32_ = (float *)(buf + per * c);
     w32_ = (float *)(buf + per * c + (size_t)(ncols + 1) * colBytes);
     if(mode == 0) gs32(0, ncols, nullptr, w.gs->hcur, w.gs->H, zeroFlag_, 0);
+    else if(mode == 6) gs32(6, ncols, nullptr, nullptr, nullptr, zeroFlag_, 0);
     else gs32(4, ncols, w.gs->hcur, nullptr, w.gs->H + ncols, zeroFlag_, 0);
   };
   for(int c = 0; c < copies; ++c) pass(c);  // warm-up round
@@ -1591,10 +1793,28 @@ int Krylov::gsStepStream(int mode, int ncols, int reps, double *avgMs)
   return FE_OK;
 }
 
+// Rows per chunk and stages of the bulk dot pass for ncols columns and w:
+// two or more stages within 220,000 bytes of shared memory, at most
+// BULK_ACC column accumulators per thread; rows = 0 when none fits.
+void Krylov::bulkCfg(int ncols, int &rows, int &nst) const
+{
+  const int64_t budget = 220000;
+  for(rows = 1024; rows >= 256; rows >>= 1) {
+    const int G = 1024 / rows;
+    if((ncols + G - 1) / G > BULK_ACC) continue;
+    const int64_t per = (int64_t)(ncols + 1) * rows * (int64_t)sizeof(float);
+    nst = (int)std::min<int64_t>(BULK_MAXST, budget / per);
+    if(nst >= 2) return;
+  }
+  rows = 0;
+  nst = 0;
+}
+
 // One FP32 Gram-Schmidt pass over the first ncols basis vectors: mode 0 the
 // dot pass (k_gs_dots), 5 the dot pass with the Pythagoras norm, 1 update +
 // dots, 2 update + norm (k_gs32), 3 the update that writes the next basis
-// vector, 4 update + norm (k_gs_upd).
+// vector, 4 update + norm (k_gs_upd), 6 the bulk-copy dot pass (partials
+// only, k_gs_dots_bulk), 7 update + norm summing those partials first.
 void Krylov::gs32(int mode, int ncols, const double *hprev, double *hcur, double *Hcol, const int *done, int pass)
 {
   RedState *st = (RedState *)red_state_;
@@ -1614,6 +1834,26 @@ void Krylov::gs32(int mode, int ncols, const double *hprev, double *hcur, double
     else                                                                                                        \
       (k_gs_upd<C, true><<<gu, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, nullptr, st, red_, Hcol, done, pass), ::feng::count_launch()); \
   } while(0)
+  if(mode == 6) {
+    int rows = 0, nst = 0;
+    bulkCfg(ncols, rows, nst);
+    const size_t sm = (size_t)nst * (ncols + 1) * rows * sizeof(float);
+    (k_gs_dots_bulk<<<nSM_, RB, sm, s_>>>(ld32_, V32_, ncols, w32_, red_, done, rows, nst), ::feng::count_launch());
+    return;
+  }
+  if(mode == 7) {
+    // hcur, Hcol: outputs (h, and the Hessenberg column with its norm entry)
+#define FE_GS_BULK_UPD(C)                                                                                         \
+  (k_gs_upd<C, true, true><<<gu, RB, 0, s_>>>(n4, ld32_, V32_, ncols, nullptr, w32_, nullptr, st, red_,           \
+                                              Hcol + ncols, done, 0, nSM_, hcur, Hcol),                           \
+   ::feng::count_launch())
+    if(ncols <= 8) FE_GS_BULK_UPD(8);
+    else if(ncols <= 16) FE_GS_BULK_UPD(16);
+    else if(ncols <= 32) FE_GS_BULK_UPD(32);
+    else FE_GS_BULK_UPD(64);
+#undef FE_GS_BULK_UPD
+    return;
+  }
   if(mode == 0 || mode == 5) {
     // mode 5: the dot pass that also takes the norm of the update by Pythagoras
     // about four blocks per SM in all: each block loops over several row
@@ -1722,9 +1962,16 @@ void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, i
     } else {
       // once (dot pass, update + norm pass), and a second time only when
       // the update kept less than a tenth of ||w|| (decided on the device,
-      // so the replayed graph is fixed)
-      gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 0);
-      gs32(4, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done, 0);
+      // so the replayed graph is fixed); the first dot pass streams the
+      // basis through bulk copies and leaves its per-block sums to the
+      // update pass
+      if(bulkGs_) {
+        gs32(6, j + 1, nullptr, nullptr, nullptr, &w.gs->done, 0);
+        gs32(7, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 0);
+      } else {
+        gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 0);
+        gs32(4, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done, 0);
+      }
       gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 1);
       gs32(4, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done, 1);
     }

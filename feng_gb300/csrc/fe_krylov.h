@@ -159,6 +159,8 @@ class Krylov {
   int *zeroFlag_ = nullptr;  // a device 0 ("not done") for gsStep
   int gsParts_ = 0;       // blocks of the FP32 Gram-Schmidt update passes
   int nSM_ = 1;           // multiprocessors of the device
+  bool bulkGs_ = false;   // first dot pass by bulk copies (k_gs_dots_bulk)
+  void bulkCfg(int ncols, int &rows, int &nst) const;
   int64_t ld32_ = 0;      // leading dimension of V32_ / Z32_ (multiple of 64)
   // pass: 0 first pass (the update + norm decides on reorthogonalisation),
   // 1 the conditional second pass, 2 the last pass of an unconditional CGS2

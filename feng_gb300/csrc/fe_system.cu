@@ -1612,13 +1612,14 @@ int SystemCUDA::computeSolDot()
 
 int SystemCUDA::benchPhase(int which, int reps, size_t flushBytes, double *avgMs)
 {
-  if(which == 7 || which == 8) {
-    // the Gram-Schmidt passes of phases 5 and 6 back to back over a working
-    // set larger than the L2 (see Krylov::gsStepStream)
+  if(which == 7 || which == 8 || which == 10) {
+    // the Gram-Schmidt passes of phases 5, 6 and 9 back to back over a
+    // working set larger than the L2 (see Krylov::gsStepStream)
     FE_TRY(ensureMatrixZeroed());
-    return kry_.gsStepStream(which == 7 ? 0 : 4, std::max(1, kry_.opt.restart / 2), std::max(reps, 1) * 10, avgMs);
+    return kry_.gsStepStream(which == 7 ? 0 : which == 8 ? 4 : 6, std::max(1, kry_.opt.restart / 2),
+                             std::max(reps, 1) * 10, avgMs);
   }
-  if(which < 0 || which > 6 || reps < 1) {
+  if(which < 0 || which > 9 || which == 7 || which == 8 || reps < 1) {
     set_error("invalid benchmark request");
     return FE_INVALID_ARG;
   }
@@ -1672,7 +1673,8 @@ int SystemCUDA::benchPhase(int which, int reps, size_t flushBytes, double *avgMs
         break;
       case 5:
       case 6:
-        status = kry_.gsStep(which == 5 ? 0 : 4, std::max(1, kry_.opt.restart / 2), nullptr);
+      case 9:
+        status = kry_.gsStep(which == 5 ? 0 : which == 6 ? 4 : 6, std::max(1, kry_.opt.restart / 2), nullptr);
         break;
     }
     CK(cudaEventRecord(ev1_, s_));

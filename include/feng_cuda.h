@@ -397,15 +397,18 @@ int fe_cuda_reset_times(fe_cuda_system *s);
  * 7 and 8 the passes of 5 and 6 launched 10 * reps times back to back, with
  * no flush between them, cycling through copies of the basis that together
  * exceed three times the L2 (the mean time of a pass inside the Arnoldi
- * loop, where the launches follow one another; flush_bytes unused).
- * Phases 5 to 8 need a mixed-precision system that has solved once.  Uses
- * the current solution state. */
+ * loop, where the launches follow one another; flush_bytes unused);
+ * 9 the bulk-copy dot pass (the first Gram-Schmidt pass of the mixed FGMRES
+ * on large systems: k_gs_dots_bulk, per-block partials that the update pass
+ * sums) over restart/2 basis vectors, 10 the same streamed as 7.
+ * Phases 5 to 10 need a mixed-precision system that has solved once (9 and
+ * 10 one large enough for the bulk pass).  Uses the current solution state. */
 int fe_cuda_bench_phase(fe_cuda_system *s, int which, int reps, int64_t flush_bytes, double *avg_ms);
 /* Algorithmic bytes of one run of phase 4 (finest multigrid operator read
  * once, each vector entry read or written once). */
 int fe_cuda_smoother_bytes(fe_cuda_system *s, int64_t *bytes);
-/* Algorithmic bytes of one run of phase 4, 5, 6, 7 or 8 (every operand read
- * or written once). */
+/* Algorithmic bytes of one run of phase 4 to 10 (every operand read or
+ * written once). */
 int fe_cuda_phase_bytes(fe_cuda_system *s, int which, int64_t *bytes);
 /* Kernel launches of the library since load (graph replays count their
  * kernel nodes). */
