@@ -412,6 +412,27 @@ __global__ void k_rowtet_offsets(int64_t nEnt, const int32_t *__restrict__ ent, 
   }
 }
 
+// One lane's share of entry k: pack words lane and 32 + lane, offset word
+// lane, and the entry's local DOF.
+struct RowTetFetch {
+  float pa, pb;
+  uint32_t po;
+  int li;
+};
+
+__device__ __forceinline__ RowTetFetch rowtet_fetch(const int32_t *__restrict__ ent, const float *__restrict__ pack,
+                                                    const uint8_t *__restrict__ offs, int32_t k, int lane)
+{
+  RowTetFetch f{0.f, 0.f, 0u, 0};
+  const int32_t e = ent[k];
+  const float *pk = pack + (int64_t)(e >> 6) * ROWTET_PACK;
+  f.pa = pk[lane];
+  if(lane < ROWTET_PACK - 32) f.pb = pk[32 + lane];
+  if(lane < ROWTET_OFFS / 4) f.po = reinterpret_cast<const uint32_t *>(offs + (int64_t)k * ROWTET_OFFS)[lane];
+  f.li = e & 63;
+  return f;
+}
+
 // A persistent grid walks the row blocks; per block the CSR values of its
 // units live in shared memory.  Warp w takes units uA + w, uA + w + 8, ...
 // and, for each of a unit's entries in order, the element's terms:
@@ -448,17 +469,17 @@ __global__ void __launch_bounds__(RT_WARPS * 32) k_matrix_tet_rows(RowAsmTet ra,
       const bool vel = ra.unitKind[un] == 3;
       float *row0 = sv + (ra.ia[r] - base);
       const int32_t rl = ra.ia[r + 1] - ra.ia[r];
-      for(int32_t k = ra.unitPtr[un]; k < ra.unitPtr[un + 1]; ++k) {
-        const int32_t e = ra.ent[k];
-        const int64_t p = e >> 6;
-        const int li = e & 63;
-        const float *pk = ra.pack + p * ROWTET_PACK;
-        sE[warp][lane] = pk[lane];
-        if(lane < ROWTET_PACK - 32) sE[warp][32 + lane] = pk[32 + lane];
-        if(lane < ROWTET_OFFS / 4)
-          reinterpret_cast<uint32_t *>(sOff[warp])[lane] =
-              reinterpret_cast<const uint32_t *>(ra.offs + (int64_t)k * ROWTET_OFFS)[lane];
+      const int32_t kb = ra.unitPtr[un], ke = ra.unitPtr[un + 1];
+      // the next entry's packed element data and column offsets are loaded
+      // into registers while the current one is computed
+      RowTetFetch nx = kb < ke ? rowtet_fetch(ra.ent, ra.pack, ra.offs, kb, lane) : RowTetFetch{0.f, 0.f, 0u, 0};
+      for(int32_t k = kb; k < ke; ++k) {
+        const int li = nx.li;
+        sE[warp][lane] = nx.pa;
+        if(lane < ROWTET_PACK - 32) sE[warp][32 + lane] = nx.pb;
+        if(lane < ROWTET_OFFS / 4) reinterpret_cast<uint32_t *>(sOff[warp])[lane] = nx.po;
         __syncwarp();
+        if(k + 1 < ke) nx = rowtet_fetch(ra.ent, ra.pack, ra.offs, k + 1, lane);
         const float *E = sE[warp];
         const float J = E[39];
         float G[3][3];
@@ -469,8 +490,9 @@ __global__ void __launch_bounds__(RT_WARPS * 32) k_matrix_tet_rows(RowAsmTet ra,
         if(vel) {
           const int a = li / 3;
           if(fc.hasConv && lane < 30) {
+            // (runtime row index: G read from shared memory, not indexed in registers)
             const int q = lane / 10, c = lane % 10;
-            sV0[warp][lane] = G[q][0] * E[3 * c] + G[q][1] * E[3 * c + 1] + G[q][2] * E[3 * c + 2];
+            sV0[warp][lane] = E[30 + 3 * q] * E[3 * c] + E[31 + 3 * q] * E[3 * c + 1] + E[32 + 3 * q] * E[3 * c + 2];
           }
           __syncwarp();
           if(lane < 30) {
@@ -506,9 +528,13 @@ __global__ void __launch_bounds__(RT_WARPS * 32) k_matrix_tet_rows(RowAsmTet ra,
 #pragma unroll
               for(int kk = 0; kk < 3; ++kk) tr += G[0][kk] * P[0][kk] + G[1][kk] * P[1][kk] + G[2][kk] * P[2][kk];
               const float cs = fcs * J;
+              // column m of P by selects (m is a runtime lane index)
+              float Pm[3];
+#pragma unroll
+              for(int qq = 0; qq < 3; ++qq) Pm[qq] = m == 0 ? P[qq][0] : (m == 1 ? P[qq][1] : P[qq][2]);
 #pragma unroll
               for(int n = 0; n < 3; ++n) {
-                const float snm = G[0][n] * P[0][m] + G[1][n] * P[1][m] + G[2][n] * P[2][m];
+                const float snm = G[0][n] * Pm[0] + G[1][n] * Pm[1] + G[2][n] * Pm[2];
                 A[n] += cs * ((n == m ? tr : 0.f) + snm);
               }
             }
@@ -529,7 +555,7 @@ __global__ void __launch_bounds__(RT_WARPS * 32) k_matrix_tet_rows(RowAsmTet ra,
             const int m = lane >> 2, j = lane & 3;
             const uint8_t o = sOff[warp][30 + j];
             if(o != 255) {
-              const float bp = (G[0][m] * Tt.d(0, j, a) + G[1][m] * Tt.d(1, j, a) + G[2][m] * Tt.d(2, j, a)) * J;
+              const float bp = (E[30 + m] * Tt.d(0, j, a) + E[33 + m] * Tt.d(1, j, a) + E[36 + m] * Tt.d(2, j, a)) * J;
               row0[m * rl + o] += fsig * bp;
             }
           }
@@ -537,7 +563,7 @@ __global__ void __launch_bounds__(RT_WARPS * 32) k_matrix_tet_rows(RowAsmTet ra,
           const int j = li - 30, a = lane / 3, m = lane % 3;
           const uint8_t o = sOff[warp][lane];
           if(o != 255) {
-            const float bp = (G[0][m] * Tt.d(0, j, a) + G[1][m] * Tt.d(1, j, a) + G[2][m] * Tt.d(2, j, a)) * J;
+            const float bp = (E[30 + m] * Tt.d(0, j, a) + E[33 + m] * Tt.d(1, j, a) + E[36 + m] * Tt.d(2, j, a)) * J;
             row0[o] += fdiv * bp;
           }
         }

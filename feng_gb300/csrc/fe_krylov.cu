@@ -1303,7 +1303,11 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
   gsParts_ = grid_for((n_ + 3) / 4, RB, std::min(MAXRED, 3 * nSM_));
   // bulk-copy dot pass: one block per SM (the update pass sums up to 256
   // partials per column), basis columns long enough to fill the stages
-  if(opt.method == 1 && opt.mixed && nSM_ <= 256 && ld32_ >= (int64_t)1024 * nSM_) {
+  // FENG_GS_BULK=0 keeps the register-streaming dot pass with its own
+  // reduction (the same sums; for comparisons)
+  bool bulkOk = true;
+  if(const char *e = std::getenv("FENG_GS_BULK")) bulkOk = std::strcmp(e, "0") != 0;
+  if(bulkOk && opt.method == 1 && opt.mixed && nSM_ <= 256 && ld32_ >= (int64_t)1024 * nSM_) {
     CK(cudaFuncSetAttribute(k_gs_dots_bulk, cudaFuncAttributeMaxDynamicSharedMemorySize, 220000));
     bulkGs_ = true;
   }
