@@ -229,7 +229,7 @@ def algorithmic_bytes(sys_, nvert, precision):
     from feng_gb300._lib import check
     out = {"residual_assembly": res, "matrix_assembly": mat, "spmv": spmv}
     for which, name in ((4, "smoother_step"), (5, "gs_dots"), (6, "gs_update"), (7, "gs_dots_stream"),
-                        (8, "gs_update_stream"), (9, "gs_dots_bulk"), (10, "gs_dots_bulk_stream")):
+                        (8, "gs_update_stream"), (9, "gs_dots_groups")):
         if which > 4 and precision != "mixed":
             continue
         b = C.c_int64()
@@ -256,13 +256,16 @@ def phase_bench(sys_, mixed, reps=20):
     one launch between two events: the launch latency and the tail are in
     it) and once streamed (10 x reps launches back to back between two
     events over basis copies larger than three L2s: the mean time of a pass
-    as it runs inside the Arnoldi loop)."""
+    as it runs inside the Arnoldi loop); the dot pass also by the
+    column-group kernel.  In-graph timings: the preconditioner application
+    replayed back to back from a CUDA graph, and one Arnoldi step of a full
+    FGMRES(50) restart cycle replayed from its graph (all 50 steps run)."""
     from feng_gb300._lib import check
     out = {}
     phases = [(0, "residual_assembly"), (1, "matrix_assembly"), (2, "spmv"), (3, "preconditioner"),
-              (4, "smoother_step")] + ([(5, "gs_dots"), (6, "gs_update"), (7, "gs_dots_stream"),
-                                        (8, "gs_update_stream"), (9, "gs_dots_bulk"),
-                                        (10, "gs_dots_bulk_stream")] if mixed else [])
+              (4, "smoother_step"), (11, "preconditioner_in_graph"), (12, "arnoldi_step_in_graph")] + (
+                  [(5, "gs_dots"), (6, "gs_update"), (7, "gs_dots_stream"), (8, "gs_update_stream"),
+                   (9, "gs_dots_groups")] if mixed else [])
     for which, name in phases:
         ms = C.c_double()
         check(sys_.lib.fe_cuda_bench_phase(sys_._h, which, reps, 256 << 20, C.byref(ms)))
@@ -586,10 +589,10 @@ def main():
     ph = ph_mixed
     shares = {"assembly": ph["residual_ms"] + ph["matrix_ms"], "krylov_solve": ph["solve_ms"],
               "preconditioner_build": ph["factor_ms"]}
-    # The dominant kernel of the Newton step (the Krylov solve is ~97% of it,
-    # and its largest kernel by time is the Gram-Schmidt dot pass): the
-    # first-pass dot kernel, k_gs_dots_bulk, at the mean column count of a
-    # restart cycle.
+    # The dominant kernel of the Newton step: the Krylov solve is ~97% of
+    # it, and its largest kernel by device time is the Arnoldi SpMV
+    # (k_spmv_sell, one launch per FGMRES iteration; profiles/ holds the
+    # launch list with the shares).
     def roofline(key, kernel, traffic_key):
         # the streamed timing (launches back to back over cold data) where the
         # phase has one, with the single flushed launch beside it
@@ -603,10 +606,9 @@ def main():
         if ks:
             out["single_launch"] = {"ms": k["ms"], "achieved": k["gbs"], "frac": k["gbs"] / peak}
         return out
-    roof = roofline("gs_dots_bulk", "k_gs_dots_bulk (FP32 Gram-Schmidt dot pass, cp.async.bulk stages, "
-                    "25 basis vectors)", "k_gs_dots_bulk@25")
-    roof_gsd = roofline("gs_dots", "k_gs_dots (register-streaming dot pass with its reduction tail, second "
-                        "Gram-Schmidt pass and small systems, 25 basis vectors)", "k_gs_dots@25")
+    roof = roofline("spmv", "k_spmv_sell (FGMRES inner SpMV, sliced ELL, FP32)", "k_spmv_sell")
+    roof_gsd = roofline("gs_dots", "k_gs_dots_all<16> (FP32 Gram-Schmidt dot pass, one pass over w and every "
+                        "column, 25 basis vectors)", "k_gs_dots_all@25")
     roof_gsu = roofline("gs_update", "k_gs_upd<32,true> (FP32 Gram-Schmidt update + norm, 25 basis vectors)",
                         "k_gs_upd<32,true>@25")
     roof_sm = roofline("smoother_step", "k_cheb_first_sell<float,2> (finest AMG level, both velocity components)",
@@ -615,10 +617,6 @@ def main():
     roof_asm = {"kernel": "k_pack_th + k_matrix_th_rows<float> (row-owned Jacobian assembly)", "bound": "hbm",
                 "achieved": asm["gbs"], "peak": peak, "unit": "GB/s", "frac": asm["gbs"] / peak,
                 "peak_source": peak_kind, "traffic": ncu_traffic("k_matrix_th_rows<float>")}
-    sp = kern["mixed"]["spmv"]
-    roof_spmv = {"kernel": "k_spmv_sell (FGMRES inner SpMV, sliced ELL, FP32)", "bound": "hbm", "achieved": sp["gbs"],
-                 "peak": peak, "unit": "GB/s", "frac": sp["gbs"] / peak, "peak_source": peak_kind,
-                 "traffic": ncu_traffic("k_spmv_sell")}
 
     nits_p = round(statistics.mean(s["iterations"] for s in st_plain), 2)
     kits_p = round(statistics.mean(s["krylov_iterations"] for s in st_plain), 1)
@@ -653,9 +651,8 @@ def main():
                                   "but not used here: it does not reach the stop"},
         "phase_share_ms": shares,
         "kernels": kern,
-        "roofline": roof, "roofline_gs_dots_register": roof_gsd, "roofline_gs_update": roof_gsu,
-        "roofline_smoother": roof_sm,
-        "roofline_assembly": roof_asm, "roofline_spmv": roof_spmv,
+        "roofline": roof, "roofline_gs_dots": roof_gsd, "roofline_gs_update": roof_gsu,
+        "roofline_smoother": roof_sm, "roofline_assembly": roof_asm,
         "e2e": {"value": e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": l_mixed,
         "gpu_launches_plain_fp64": l_plain,

@@ -9,6 +9,7 @@
 
 #include "fe_amg.h"
 #include "fe_common.h"
+#include "fe_launch.h"
 
 namespace feng {
 
@@ -95,6 +96,7 @@ __global__ void __launch_bounds__(256) k_csr(int64_t n, const int32_t *__restric
                                              const V *__restrict__ x, const V *__restrict__ b,
                                              V *__restrict__ y, const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
   const int sub = threadIdx.x % LANES;
@@ -135,9 +137,9 @@ void csr(int lanes, int64_t n, const int32_t *ia, const int32_t *ja, const V *a,
          V *y, cudaStream_t s, const int *skip)
 {
   const int g = grid(n * lanes);
-  if(lanes == 8) (k_csr<V, 8, MODE, NV><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y, skip), ::feng::count_launch());
-  else if(lanes == 16) (k_csr<V, 16, MODE, NV><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y, skip), ::feng::count_launch());
-  else (k_csr<V, 4, MODE, NV><<<g, 256, 0, s>>>(n, ia, ja, a, x, b, y, skip), ::feng::count_launch());
+  if(lanes == 8) ::feng::launch_k(k_csr<V, 8, MODE, NV>, g, 256, 0, s, n, ia, ja, a, x, b, y, skip);
+  else if(lanes == 16) ::feng::launch_k(k_csr<V, 16, MODE, NV>, g, 256, 0, s, n, ia, ja, a, x, b, y, skip);
+  else ::feng::launch_k(k_csr<V, 4, MODE, NV>, g, 256, 0, s, n, ia, ja, a, x, b, y, skip);
 }
 
 // Chebyshev start (x = 0): r = D^-1 b, d = r / theta, x = 0.
@@ -145,6 +147,7 @@ template <typename V, int NV>
 __global__ void k_cheb_start(int64_t n, const V *__restrict__ dinv, const V *__restrict__ b, V *__restrict__ r,
                              V *__restrict__ d, V *__restrict__ x, V inv_theta, const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * NV; i += (int64_t)gridDim.x * blockDim.x) {
     const V ri = dinv[i / NV] * b[i];
@@ -162,6 +165,7 @@ __global__ void __launch_bounds__(256) k_cheb_restart(int64_t n, const int32_t *
                                                       const V *__restrict__ x, V *__restrict__ r,
                                                       V *__restrict__ d, V inv_theta, const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
   const int sub = threadIdx.x % LANES;
@@ -189,6 +193,7 @@ __global__ void __launch_bounds__(256) k_cheb_step(int64_t n, const int32_t *__r
                                                    V *__restrict__ dn, V *__restrict__ r,
                                                    V *__restrict__ x, V c1, V c2, const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
   const int sub = threadIdx.x % LANES;
@@ -222,6 +227,7 @@ __global__ void __launch_bounds__(256) k_cheb_first(int64_t n, const int32_t *__
                                                     V *__restrict__ dn, V *__restrict__ r, V *__restrict__ x,
                                                     V inv_theta, V c1, V c2, const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
   const int sub = threadIdx.x % LANES;
@@ -271,6 +277,7 @@ __global__ void __launch_bounds__(256) k_cheb_post(int64_t n, const int32_t *__r
                                                    const int32_t *__restrict__ dofY, const double *__restrict__ scale,
                                                    V *__restrict__ out)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
   const int sub = threadIdx.x % LANES;
@@ -299,6 +306,7 @@ __global__ void __launch_bounds__(256) k_cheb_first_sell(int64_t n, const int32_
                                                          V *__restrict__ dn, V *__restrict__ r, V *__restrict__ x,
                                                          V inv_theta, V c1, V c2, const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if(row >= n) return;
@@ -340,6 +348,7 @@ __global__ void __launch_bounds__(256) k_cheb_post_sell(int64_t n, const int32_t
                                                         const int32_t *__restrict__ dofY,
                                                         const double *__restrict__ scale, V *__restrict__ out)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if(row >= n) return;
@@ -376,6 +385,7 @@ __global__ void __launch_bounds__(256) k_prolong_sell(int64_t n, const int32_t *
                                                       const V *__restrict__ xc, const V *__restrict__ b,
                                                       V *__restrict__ y, const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if(row >= n) return;
@@ -402,6 +412,7 @@ __global__ void __launch_bounds__(256) k_prolong_sell(int64_t n, const int32_t *
 template <typename V>
 __global__ void k_cheb_last(int64_t m, const V *__restrict__ d, V *__restrict__ x, const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
     x[i] += d[i];
@@ -412,6 +423,7 @@ template <typename V, int NV>
 __global__ void k_dense(int64_t n, const V *__restrict__ M, const V *__restrict__ b, V *__restrict__ x,
                         const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
   const int lane = threadIdx.x % 32;
@@ -591,31 +603,30 @@ static void chebyshev(int lanes, int64_t n, const int32_t *ia, const int32_t *ja
     const double rhoN = 1.0 / (2.0 * sigma - rho);
     const V c1 = (V)(rhoN * rho), c2 = (V)(2.0 * rhoN / delta);
     const V it = (V)(1.0 / theta);
-    if(sp) (k_cheb_first_sell<V, NV><<<grid(n), 256, 0, s>>>(n, sp, sc, sv, dinv, b, dn, r, x, it, c1, c2, skip), ::feng::count_launch());
-    else if(lanes == 16) (k_cheb_first<V, 16, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, dn, r, x, it, c1, c2, skip), ::feng::count_launch());
-    else if(lanes == 8) (k_cheb_first<V, 8, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, dn, r, x, it, c1, c2, skip), ::feng::count_launch());
-    else (k_cheb_first<V, 4, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, dn, r, x, it, c1, c2, skip), ::feng::count_launch());
+    if(sp) ::feng::launch_k(k_cheb_first_sell<V, NV>, grid(n), 256, 0, s, n, sp, sc, sv, dinv, b, dn, r, x, it, c1, c2, skip);
+    else if(lanes == 16) ::feng::launch_k(k_cheb_first<V, 16, NV>, g, 256, 0, s, n, ia, ja, a, dinv, b, dn, r, x, it, c1, c2, skip);
+    else if(lanes == 8) ::feng::launch_k(k_cheb_first<V, 8, NV>, g, 256, 0, s, n, ia, ja, a, dinv, b, dn, r, x, it, c1, c2, skip);
+    else ::feng::launch_k(k_cheb_first<V, 4, NV>, g, 256, 0, s, n, ia, ja, a, dinv, b, dn, r, x, it, c1, c2, skip);
     rho = rhoN;
     std::swap(d, dn);
     k0 = 1;
   } else if(zeroStart) {
-    (k_cheb_start<V, NV><<<grid(n * NV), 256, 0, s>>>(n, dinv, b, r, d0, x, (V)(1.0 / theta), skip),
-     ::feng::count_launch());
+    ::feng::launch_k(k_cheb_start<V, NV>, grid(n * NV), 256, 0, s, n, dinv, b, r, d0, x, (V)(1.0 / theta), skip);
   } else {
-    if(lanes == 16) (k_cheb_restart<V, 16, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip), ::feng::count_launch());
-    else if(lanes == 8) (k_cheb_restart<V, 8, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip), ::feng::count_launch());
-    else (k_cheb_restart<V, 4, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip), ::feng::count_launch());
+    if(lanes == 16) ::feng::launch_k(k_cheb_restart<V, 16, NV>, g, 256, 0, s, n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip);
+    else if(lanes == 8) ::feng::launch_k(k_cheb_restart<V, 8, NV>, g, 256, 0, s, n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip);
+    else ::feng::launch_k(k_cheb_restart<V, 4, NV>, g, 256, 0, s, n, ia, ja, a, dinv, b, x, r, d0, (V)(1.0 / theta), skip);
   }
   for(int k = k0; k < p.chebyDegree; ++k) {
     if(!needResidual && k == p.chebyDegree - 1) {
-      (k_cheb_last<V><<<grid(n * NV), 256, 0, s>>>(n * NV, d, x, skip), ::feng::count_launch());
+      ::feng::launch_k(k_cheb_last<V>, grid(n * NV), 256, 0, s, n * NV, d, x, skip);
       break;
     }
     const double rhoN = 1.0 / (2.0 * sigma - rho);
     const V c1 = (V)(rhoN * rho), c2 = (V)(2.0 * rhoN / delta);
-    if(lanes == 16) (k_cheb_step<V, 16, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2, skip), ::feng::count_launch());
-    else if(lanes == 8) (k_cheb_step<V, 8, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2, skip), ::feng::count_launch());
-    else (k_cheb_step<V, 4, NV><<<g, 256, 0, s>>>(n, ia, ja, a, dinv, d, dn, r, x, c1, c2, skip), ::feng::count_launch());
+    if(lanes == 16) ::feng::launch_k(k_cheb_step<V, 16, NV>, g, 256, 0, s, n, ia, ja, a, dinv, d, dn, r, x, c1, c2, skip);
+    else if(lanes == 8) ::feng::launch_k(k_cheb_step<V, 8, NV>, g, 256, 0, s, n, ia, ja, a, dinv, d, dn, r, x, c1, c2, skip);
+    else ::feng::launch_k(k_cheb_step<V, 4, NV>, g, 256, 0, s, n, ia, ja, a, dinv, d, dn, r, x, c1, c2, skip);
     rho = rhoN;
     std::swap(d, dn);
   }
@@ -626,7 +637,7 @@ void AMGDevice::vcycle_t(int l, const V *b, V *x)
 {
   Lev &L = lv_[l];
   if(l == (int)lv_.size() - 1) {
-    (k_dense<V, NV><<<grid(L.n * 32), 256, 0, s_>>>(L.n, (const V *)coarseInv_, b, x, skip_), ::feng::count_launch());
+    ::feng::launch_k(k_dense<V, NV>, grid(L.n * 32), 256, 0, s_, L.n, (const V *)coarseInv_, b, x, skip_);
     return;
   }
   Lev &C = lv_[l + 1];
@@ -643,8 +654,8 @@ void AMGDevice::vcycle_t(int l, const V *b, V *x)
     // x = y + D^-1 (b - A y) / theta (the restart and the step in one)
     V *y = (V *)L.d1;
     if(L.sellPPtr)
-      (k_prolong_sell<V, NV><<<grid(L.n), 256, 0, s_>>>(L.n, L.sellPPtr, L.sellPCol, (const V *)L.sellPVal,
-                                                        (const V *)C.x, x, y, skip_), ::feng::count_launch());
+      ::feng::launch_k(k_prolong_sell<V, NV>, grid(L.n), 256, 0, s_, L.n, L.sellPPtr, L.sellPCol, (const V *)L.sellPVal,
+                                                        (const V *)C.x, x, y, skip_);
     else
       csr<V, 4, NV>(L.lanesP, L.n, L.Pia, L.Pja, (const V *)L.Pa, (const V *)C.x, x, y, s_, skip_);
     const double lo = p_.chebyLow * L.lmax, hi = p_.chebyHigh * L.lmax, theta = 0.5 * (hi + lo);
@@ -654,14 +665,12 @@ void AMGDevice::vcycle_t(int l, const V *b, V *x)
     if(L.sellPtr) {
       const V *sv = (const V *)L.sellVal;
       if(l == 0 && NV == 2 && out_.z) {
-        (k_cheb_post_sell<V, NV, true><<<grid(L.n), 256, 0, s_>>>(L.n, L.sellPtr, L.sellCol, sv, dinv, b, y, x, it, skip_,
-                                                                 out_.dofX, out_.dofY, out_.scale, (V *)out_.z),
-         ::feng::count_launch());
+        ::feng::launch_k(k_cheb_post_sell<V, NV, true>, grid(L.n), 256, 0, s_, L.n, L.sellPtr, L.sellCol, sv, dinv, b, y, x, it, skip_,
+                                                                 out_.dofX, out_.dofY, out_.scale, (V *)out_.z);
         outWritten_ = true;
       } else {
-        (k_cheb_post_sell<V, NV, false><<<grid(L.n), 256, 0, s_>>>(L.n, L.sellPtr, L.sellCol, sv, dinv, b, y, x, it,
-                                                                  skip_, nullptr, nullptr, nullptr, nullptr),
-         ::feng::count_launch());
+        ::feng::launch_k(k_cheb_post_sell<V, NV, false>, grid(L.n), 256, 0, s_, L.n, L.sellPtr, L.sellCol, sv, dinv, b, y, x, it,
+                                                                  skip_, nullptr, nullptr, nullptr, nullptr);
       }
       return;
     }
@@ -669,15 +678,15 @@ void AMGDevice::vcycle_t(int l, const V *b, V *x)
       const int32_t *dx = out_.dofX, *dy = out_.dofY;
       const double *sc = out_.scale;
       V *z = (V *)out_.z;
-      if(L.lanesA == 16) (k_cheb_post<V, 16, NV, true><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, dx, dy, sc, z), ::feng::count_launch());
-      else if(L.lanesA == 8) (k_cheb_post<V, 8, NV, true><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, dx, dy, sc, z), ::feng::count_launch());
-      else (k_cheb_post<V, 4, NV, true><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, dx, dy, sc, z), ::feng::count_launch());
+      if(L.lanesA == 16) ::feng::launch_k(k_cheb_post<V, 16, NV, true>, g, 256, 0, s_, L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, dx, dy, sc, z);
+      else if(L.lanesA == 8) ::feng::launch_k(k_cheb_post<V, 8, NV, true>, g, 256, 0, s_, L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, dx, dy, sc, z);
+      else ::feng::launch_k(k_cheb_post<V, 4, NV, true>, g, 256, 0, s_, L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, dx, dy, sc, z);
       outWritten_ = true;
       return;
     }
-    if(L.lanesA == 16) (k_cheb_post<V, 16, NV, false><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, nullptr, nullptr, nullptr, nullptr), ::feng::count_launch());
-    else if(L.lanesA == 8) (k_cheb_post<V, 8, NV, false><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, nullptr, nullptr, nullptr, nullptr), ::feng::count_launch());
-    else (k_cheb_post<V, 4, NV, false><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, nullptr, nullptr, nullptr, nullptr), ::feng::count_launch());
+    if(L.lanesA == 16) ::feng::launch_k(k_cheb_post<V, 16, NV, false>, g, 256, 0, s_, L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, nullptr, nullptr, nullptr, nullptr);
+    else if(L.lanesA == 8) ::feng::launch_k(k_cheb_post<V, 8, NV, false>, g, 256, 0, s_, L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, nullptr, nullptr, nullptr, nullptr);
+    else ::feng::launch_k(k_cheb_post<V, 4, NV, false>, g, 256, 0, s_, L.n, L.Aia, L.Aja, A, dinv, b, y, x, it, skip_, nullptr, nullptr, nullptr, nullptr);
     return;
   }
   csr<V, 2, NV>(L.lanesP, L.n, L.Pia, L.Pja, (const V *)L.Pa, (const V *)C.x, nullptr, x, s_, skip_);
@@ -730,11 +739,11 @@ void AMGDevice::fineStep2()
     V *dn = (V *)L.d1, *r = (V *)L.r, *x = (V *)L.x;
     const V it = (V)0.5, c1 = (V)0.5, c2 = (V)0.5;
     if(L.sellPtr)
-      (k_cheb_first_sell<V, 2><<<grid(L.n), 256, 0, s_>>>(L.n, L.sellPtr, L.sellCol, (const V *)L.sellVal, dinv, b, dn,
-                                                          r, x, it, c1, c2, skip_), ::feng::count_launch());
-    else if(L.lanesA == 16) (k_cheb_first<V, 16, 2><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, a, dinv, b, dn, r, x, it, c1, c2, skip_), ::feng::count_launch());
-    else if(L.lanesA == 8) (k_cheb_first<V, 8, 2><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, a, dinv, b, dn, r, x, it, c1, c2, skip_), ::feng::count_launch());
-    else (k_cheb_first<V, 4, 2><<<g, 256, 0, s_>>>(L.n, L.Aia, L.Aja, a, dinv, b, dn, r, x, it, c1, c2, skip_), ::feng::count_launch());
+      ::feng::launch_k(k_cheb_first_sell<V, 2>, grid(L.n), 256, 0, s_, L.n, L.sellPtr, L.sellCol, (const V *)L.sellVal, dinv, b, dn,
+                                                          r, x, it, c1, c2, skip_);
+    else if(L.lanesA == 16) ::feng::launch_k(k_cheb_first<V, 16, 2>, g, 256, 0, s_, L.n, L.Aia, L.Aja, a, dinv, b, dn, r, x, it, c1, c2, skip_);
+    else if(L.lanesA == 8) ::feng::launch_k(k_cheb_first<V, 8, 2>, g, 256, 0, s_, L.n, L.Aia, L.Aja, a, dinv, b, dn, r, x, it, c1, c2, skip_);
+    else ::feng::launch_k(k_cheb_first<V, 4, 2>, g, 256, 0, s_, L.n, L.Aia, L.Aja, a, dinv, b, dn, r, x, it, c1, c2, skip_);
   };
   if(fp32_) go(float());
   else go(double());

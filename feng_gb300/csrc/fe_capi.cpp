@@ -972,7 +972,7 @@ int fe_cuda_phase_bytes(fe_cuda_system *s, int which, int64_t *bytes)
   GUARD_BEGIN
   if(!s || !bytes) { set_error("null argument"); return FE_INVALID_ARG; }
   if(which == 4) return fe_cuda_smoother_bytes(s, bytes);
-  if(which < 5 || which > 10) { set_error("no byte count for phase %d", which); return FE_INVALID_ARG; }
+  if(which < 5 || which > 9) { set_error("no byte count for phase %d", which); return FE_INVALID_ARG; }
   Krylov &k = s->sys.krylov();
   const int mode = which == 5 || which == 7 ? 0 : which == 6 || which == 8 ? 4 : 6;
   const int r = k.gsStep(mode, std::max(1, k.opt.restart / 2), bytes);

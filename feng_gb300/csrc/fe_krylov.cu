@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "fe_common.h"
+#include "fe_launch.h"
 #include "fe_krylov.h"
 
 namespace feng {
@@ -36,6 +37,7 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int32_t *__restri
                                               const double *__restrict__ b, VY *__restrict__ y,
                                               const int *__restrict__ done)
 {
+  FE_PDL_ENTRY();
   if(done && *done) return;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
   const int sub = threadIdx.x % LANES;
@@ -149,6 +151,7 @@ __device__ void finish_reduction(const double (&v)[K], double *partials, RedStat
 __global__ void k_dot(int64_t n, const double *__restrict__ x, const double *__restrict__ y,
                       double *partials, RedState *st, double *out)
 {
+  FE_PDL_ENTRY();
   double v[1] = {0.};
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
       i += (int64_t)gridDim.x * blockDim.x)
@@ -159,6 +162,7 @@ __global__ void k_dot(int64_t n, const double *__restrict__ x, const double *__r
 __global__ void k_absmax(int64_t n, const double *__restrict__ x, double *partials, RedState *st,
                          double *out)
 {
+  FE_PDL_ENTRY();
   double v[1] = {0.};
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
       i += (int64_t)gridDim.x * blockDim.x)
@@ -171,6 +175,7 @@ __global__ void k_mdot_partial(int64_t n, const double *__restrict__ V, int ncol
                                const double *__restrict__ w, double *partials,
                                const int *__restrict__ done)
 {
+  FE_PDL_ENTRY();
   if(*done) return;
   __shared__ double sh[RB / 32];
   const int c = blockIdx.y;
@@ -187,6 +192,7 @@ __global__ void k_mdot_partial(int64_t n, const double *__restrict__ V, int ncol
 __global__ void k_mdot_final(int nparts, double *partials, double *hcur, double *Hcol, int accum,
                              const int *__restrict__ done)
 {
+  FE_PDL_ENTRY();
   if(*done) return;
   __shared__ double sh[RB / 32];
   const int c = blockIdx.x;
@@ -204,6 +210,7 @@ __global__ void k_mupdate(int64_t n, const double *__restrict__ V, int ncols,
                           const double *__restrict__ h, double *__restrict__ w,
                           const int *__restrict__ done)
 {
+  FE_PDL_ENTRY();
   if(*done) return;
   __shared__ double sh[MAXM + 1];
   for(int c = threadIdx.x; c < ncols; c += blockDim.x) sh[c] = h[c];
@@ -220,6 +227,7 @@ __global__ void k_mupdate(int64_t n, const double *__restrict__ V, int ncols,
 __global__ void k_norm_to(int64_t n, const double *__restrict__ w, double *partials, RedState *st,
                           const int *__restrict__ done)
 {
+  FE_PDL_ENTRY();
   if(*done) return;
   double v[1] = {0.};
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -232,6 +240,7 @@ __global__ void k_norm_to(int64_t n, const double *__restrict__ w, double *parti
 __global__ void k_scale_from(int64_t n, const double *__restrict__ w, double *__restrict__ v,
                              const RedState *st, double *Hsub, const int *__restrict__ done)
 {
+  FE_PDL_ENTRY();
   if(*done) return;
   const double nrm = sqrt(st->result[0]);
   if(blockIdx.x == 0 && threadIdx.x == 0) *Hsub = nrm;
@@ -245,6 +254,7 @@ template <typename VO>
 __global__ void k_scale_vec(int64_t n, const double *__restrict__ w, VO *__restrict__ v,
                             const double *__restrict__ s, int invert)
 {
+  FE_PDL_ENTRY();
   const double f = invert ? (*s > 0 ? 1.0 / *s : 0.0) : *s;
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
       i += (int64_t)gridDim.x * blockDim.x)
@@ -254,6 +264,7 @@ __global__ void k_scale_vec(int64_t n, const double *__restrict__ w, VO *__restr
 __global__ void k_to_f32(int64_t n, const double *__restrict__ x, float *__restrict__ y,
                          const int *__restrict__ done)
 {
+  FE_PDL_ENTRY();
   if(done && *done) return;
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
       i += (int64_t)gridDim.x * blockDim.x)
@@ -278,18 +289,19 @@ struct GmresState : GmresHead {
 // One warp: the column and the previous rotations are staged in shared
 // memory, the (inherently sequential) rotation chain runs on lane 0 out of
 // registers and shared memory, and the column is written back by the warp.
-__global__ void k_givens(GmresState *gs, int j)
+// Applies the previous rotations to Hessenberg column j, forms rotation j,
+// updates g and the residual estimate, sets done (one warp; sh, scs, ssn:
+// shared arrays of MAXM + 1, MAXM, MAXM doubles).
+__device__ void givens_warp(GmresState *gs, int j, int lane, double *sh, double *scs, double *ssn)
 {
-  if(gs->done) return;
-  __shared__ double sh[MAXM + 1], scs[MAXM], ssn[MAXM];
   double *h = gs->H + (int64_t)j * (MAXM + 1);
-  for(int i = threadIdx.x; i <= j + 1; i += blockDim.x) sh[i] = h[i];
-  for(int i = threadIdx.x; i < j; i += blockDim.x) {
+  for(int i = lane; i <= j + 1; i += 32) sh[i] = h[i];
+  for(int i = lane; i < j; i += 32) {
     scs[i] = gs->cs[i];
     ssn[i] = gs->sn[i];
   }
   __syncwarp();
-  if(threadIdx.x == 0) {
+  if(lane == 0) {
     double hi = sh[0];
     for(int i = 0; i < j; ++i) {
       const double c = scs[i], s = ssn[i], hn = sh[i + 1];
@@ -299,8 +311,8 @@ __global__ void k_givens(GmresState *gs, int j)
     sh[j] = hi;
   }
   __syncwarp();
-  for(int i = threadIdx.x; i < j; i += blockDim.x) h[i] = sh[i];
-  if(threadIdx.x != 0) return;
+  for(int i = lane; i < j; i += 32) h[i] = sh[i];
+  if(lane != 0) return;
   const double a = sh[j], b = sh[j + 1];
   const double r = hypot(a, b);
   double c = 1., s = 0.;
@@ -316,10 +328,19 @@ __global__ void k_givens(GmresState *gs, int j)
   if(!(gs->est > gs->tol) || b == 0.0 || !isfinite(gs->est)) gs->done = 1;
 }
 
+__global__ void k_givens(GmresState *gs, int j)
+{
+  FE_PDL_ENTRY();
+  if(gs->done) return;
+  __shared__ double sh[MAXM + 1], scs[MAXM], ssn[MAXM];
+  givens_warp(gs, j, threadIdx.x, sh, scs, ssn);
+}
+
 // y = R^-1 g with R the upper triangle of H (k x k): one block, R staged in
 // shared memory; row i's dot with the solved tail is a block reduction.
 __global__ void k_backsolve(GmresState *gs)
 {
+  FE_PDL_ENTRY();
   // dynamic: the column-major upper triangle of the restart length m
   // (m (m + 1) / 2 doubles), sized at launch
   extern __shared__ double sR[];
@@ -351,6 +372,7 @@ template <typename VZ>
 __global__ void k_xupdate(int64_t n, int64_t ld, const VZ *__restrict__ Z, const GmresState *gs,
                           double *__restrict__ x)
 {
+  FE_PDL_ENTRY();
   __shared__ double sy[MAXM];
   const int k = gs->k;
   for(int c = threadIdx.x; c < k; c += blockDim.x) sy[c] = gs->y[c];
@@ -390,6 +412,7 @@ __global__ void __launch_bounds__(RB, 3) k_gs32(int64_t n4, int64_t ld, const fl
                                              double *partials, RedState *st, double *hcur, double *Hcol,
                                              const int *__restrict__ done, int pass)
 {
+  FE_PDL_ENTRY();
   // Rows are taken four at a time (16-byte loads); the basis columns have a
   // leading dimension ld that is a multiple of 4 and rows n..ld-1 hold zeros.
   // MODE 2, pass 0: decides whether a second pass is needed (the update kept
@@ -465,9 +488,11 @@ __global__ void __launch_bounds__(RB, 3) k_gs32(int64_t n4, int64_t ld, const fl
     double s8[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
     const int nb = (int)gridDim.x;
     for(int b0 = lane; b0 < nb; b0 += 256) {
+      double v[8];
 #pragma unroll
-      for(int q = 0; q < 8; ++q)
-        if(b0 + 32 * q < nb) s8[q] += __ldcg(pc + b0 + 32 * q);
+      for(int q = 0; q < 8; ++q) v[q] = __ldcg(pc + (b0 + 32 * q < nb ? b0 + 32 * q : 0));
+#pragma unroll
+      for(int q = 0; q < 8; ++q) s8[q] += b0 + 32 * q < nb ? v[q] : 0.;
     }
     double sum = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
     for(int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
@@ -510,6 +535,7 @@ __global__ void __launch_bounds__(RB) k_gs_dots(int64_t n4, int64_t ld, const fl
                                                 double *hcur, double *Hcol, const int *__restrict__ done,
                                                 int second, int pyth)
 {
+  FE_PDL_ENTRY();
   if(*done || (second && !st->reorth)) return;
   __shared__ float red[RB / 32][9];
   __shared__ double hsum[MAXM + 1];
@@ -587,9 +613,11 @@ __global__ void __launch_bounds__(RB) k_gs_dots(int64_t n4, int64_t ld, const fl
     double s8[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
     const int nb = (int)gridDim.x;
     for(int b0 = lane; b0 < nb; b0 += 256) {
+      double v[8];
 #pragma unroll
-      for(int q = 0; q < 8; ++q)
-        if(b0 + 32 * q < nb) s8[q] += __ldcg(pc + b0 + 32 * q);
+      for(int q = 0; q < 8; ++q) v[q] = __ldcg(pc + (b0 + 32 * q < nb ? b0 + 32 * q : 0));
+#pragma unroll
+      for(int q = 0; q < 8; ++q) s8[q] += b0 + 32 * q < nb ? v[q] : 0.;
     }
     double sum = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
     for(int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
@@ -623,154 +651,117 @@ __global__ void __launch_bounds__(RB) k_gs_dots(int64_t n4, int64_t ld, const fl
   }
 }
 
-// ---- bulk-copy (TMA) streaming: mbarrier and cp.async.bulk in inline PTX
-__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
+// h_c = V_c . w for c < ncols and ||w||^2 in one pass over w and the
+// columns, shaped as the update pass: thread = one float4 row of w at a
+// time (grid-stride over one wave of blocks), the columns in batches of 8
+// loads, CMAX FP32 accumulators per thread (64 registers: four blocks per
+// SM): block (x, y) takes the columns CMAX y .. CMAX y + CMAX - 1 (more than
+// 16 columns: grid y > 1, each slice re-reading w).  Per block each accumulator is summed over the lanes
+// (butterfly) and the warps (FP64, warp order) into one partial per row
+// block x and column (||w||^2: column ncols, from y = 0); the last block to
+// finish sums the partials (RB / (ncols + 1) threads per column, each over a
+// fixed stride of row blocks in rounds of 32 loads, then in thread order)
+// into hcur / Hcol (second = 0: Hcol = h; 1: the reorthogonalisation pass,
+// run only when it was asked for, adds h to Hcol) and st->result[2].
+// gridDim.x <= MAXRED.
+template <int CMAX>
+__global__ void __launch_bounds__(RB, 4) k_gs_dots_all(int64_t n4, int64_t ld, const float *__restrict__ V,
+                                                      int ncols, const float *__restrict__ w, double *partials,
+                                                      RedState *st, double *hcur, double *Hcol,
+                                                      const int *__restrict__ done, int second)
 {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned bytes)
-{
-  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
-                   smem_addr(bar)),
-               "r"(bytes)
-               : "memory");
-}
-
-// global -> shared, completion counted in bytes on the mbarrier (16-byte
-// aligned addresses, a multiple of 16 bytes)
-__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes, uint64_t *bar)
-{
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_addr(dst)),
-               "l"(src), "r"(bytes), "r"(smem_addr(bar))
-               : "memory");
-}
-
-// Waits for the phase of the given parity; false when 2^22 polls ran out.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity)
-{
-  for(int it = 0; it < (1 << 22); ++it) {
-    uint32_t ok;
-    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-                 : "=r"(ok)
-                 : "r"(smem_addr(bar)), "r"(parity)
-                 : "memory");
-    if(ok) return true;
-  }
-  return false;
-}
-
-constexpr int BULK_MAXST = 8;  // stages of the bulk dot pass
-constexpr int BULK_ACC = 32;   // column accumulators per thread
-
-// The first Gram-Schmidt dot pass with bulk copies (mode 6): one block per
-// SM walks chunks of `rows` rows (a power of two, 256..1024); per stage the
-// chunk of w and of each of the ncols columns lands in shared memory (one
-// cp.async.bulk per column, issued by the lanes of warp 0; completion on the
-// stage's mbarrier, waited for with a bound), `nst` stages in flight.
-// Thread (g, q), q < rows / 4, g < G = 1024 / rows, takes float4 row q of the
-// chunk and the columns c = g (mod G).  Per block, the FP64 partial of every
-// column and of ||w||^2 (column ncols) goes to partials[c][blockIdx.x]; no
-// reduction tail: the update pass that follows (k_gs_upd, FROMPART) sums
-// them.  A wait that runs out writes NaN partials (the Arnoldi step then
-// fails as non-finite) after a bounded wait for the copies in flight.
-__global__ void __launch_bounds__(RB, 1) k_gs_dots_bulk(int64_t ld, const float *__restrict__ V, int ncols,
-                                                        const float *__restrict__ w, double *partials,
-                                                        const int *__restrict__ done, int rows, int nst)
-{
-  if(*done) return;
-  extern __shared__ __align__(128) unsigned char gsmem[];
-  float *buf = reinterpret_cast<float *>(gsmem);  // [nst][ncols + 1][rows]
-  __shared__ uint64_t full[BULK_MAXST];
-  __shared__ double red[RB / 32][BULK_ACC + 1];
+  FE_PDL_ENTRY();
+  if(*done || (second && !st->reorth)) return;
+  __shared__ double red[RB / 32][CMAX + 1];
+  __shared__ double flat[RB];
+  __shared__ bool last;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int F = rows / 4, G = RB / F, g = tid / F, q = tid % F;
-  const int nsl = ncols + 1;
-  const int64_t nChunks = (ld + rows - 1) / rows;
-  if(tid == 0) {
-    for(int i = 0; i < nst; ++i) mbar_init(&full[i], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  __syncthreads();
-  // warp 0: stage st <- chunk ch (lane 0 arms the barrier first)
-  auto issue = [&](int st, int64_t ch) {
-    const int64_t r0 = ch * rows;
-    const unsigned bytes = (unsigned)((ld - r0 < rows ? ld - r0 : rows) * 4);
-    if(lane == 0) mbar_arrive_expect_tx(&full[st], bytes * nsl);
-    __syncwarp();
-    float *dst = buf + (int64_t)st * nsl * rows;
-    for(int c = lane; c < nsl; c += 32)
-      bulk_copy_g2s(dst + (int64_t)c * rows, c == 0 ? w + r0 : V + (int64_t)(c - 1) * ld + r0, bytes, &full[st]);
-  };
-  if(warp == 0)
-    for(int i = 0; i < nst; ++i)
-      if(blockIdx.x + (int64_t)i * gridDim.x < nChunks) issue(i, blockIdx.x + (int64_t)i * gridDim.x);
-  float acc[BULK_ACC];
+  const int cb = CMAX * blockIdx.y, cn = min(CMAX, ncols - cb);
+  const bool wcol = blockIdx.y == 0;
+  const float4 *w4 = reinterpret_cast<const float4 *>(w);
+  const float4 *V4 = reinterpret_cast<const float4 *>(V) + (int64_t)cb * (ld / 4);
+  const int64_t ld4 = ld / 4;
+  float acc[CMAX];
 #pragma unroll
-  for(int i = 0; i < BULK_ACC; ++i) acc[i] = 0.f;
+  for(int c = 0; c < CMAX; ++c) acc[c] = 0.f;
   float wq = 0.f;
-  const int slots = (ncols + G - 1) / G;
-  bool ok = true;
-  int k = 0;
-  for(int64_t ch = blockIdx.x; ch < nChunks; ch += gridDim.x, ++k) {
-    const int st = k % nst;
-    if(!__syncthreads_and(mbar_wait_bounded(&full[st], (unsigned)((k / nst) & 1)))) {
-      ok = false;
-      break;
-    }
-    const int64_t r0 = ch * rows;
-    if((int64_t)4 * q < ld - r0) {
-      const float4 *src = reinterpret_cast<const float4 *>(buf + (int64_t)st * nsl * rows);
-      const float4 x = src[q];
-      if(g == 0) wq = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, wq))));
+  for(int64_t g = (int64_t)blockIdx.x * RB + tid; g < n4; g += (int64_t)gridDim.x * RB) {
+    const float4 x = w4[g];
+    if(wcol) wq = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, wq))));
 #pragma unroll
-      for(int i = 0; i < BULK_ACC; ++i) {
-        const int c = g + i * G;
-        if(i < slots && c < ncols) {
-          const float4 v = src[(int64_t)(c + 1) * F + q];
-          acc[i] = fmaf(v.x, x.x, fmaf(v.y, x.y, fmaf(v.z, x.z, fmaf(v.w, x.w, acc[i]))));
+    for(int c0 = 0; c0 < CMAX; c0 += 8) {
+      if(c0 < cn) {
+        // one batch of eight loads in flight (clamped columns, the extra
+        // products dropped by selects)
+        float4 v[8];
+#pragma unroll
+        for(int u = 0; u < 8; ++u) v[u] = __ldcs(V4 + (int64_t)(c0 + u < cn ? c0 + u : c0) * ld4 + g);
+#pragma unroll
+        for(int u = 0; u < 8; ++u) {
+          const float t = fmaf(v[u].x, x.x, fmaf(v[u].y, x.y, fmaf(v[u].z, x.z, v[u].w * x.w)));
+          acc[c0 + u] += c0 + u < cn ? t : 0.f;
         }
       }
     }
-    __syncthreads();
-    const int64_t nx = ch + (int64_t)nst * gridDim.x;
-    if(warp == 0 && nx < nChunks) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue(st, nx);
-    }
-  }
-  if(!ok) {
-    // let the copies in flight land before the block exits
-    for(int i = 0; i < nst; ++i) {
-      mbar_wait_bounded(&full[i], 0);
-      mbar_wait_bounded(&full[i], 1);
-    }
-    for(int c = tid; c <= ncols; c += RB) partials[(int64_t)c * MAXRED + blockIdx.x] = __longlong_as_double(0x7ff8000000000000ll);
-    return;
   }
 #pragma unroll
-  for(int i = 0; i < BULK_ACC; ++i) {
-    if(i < slots) {
-      float a = acc[i];
-      for(int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-      if(lane == 0) red[warp][i] = (double)a;
+  for(int c = 0; c < CMAX; ++c) {
+    if(c < cn) {
+      float t = acc[c];
+      for(int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if(lane == 0) red[warp][c] = (double)t;
     }
   }
   for(int o = 16; o > 0; o >>= 1) wq += __shfl_xor_sync(0xffffffffu, wq, o);
-  if(lane == 0) red[warp][BULK_ACC] = (double)wq;
+  if(lane == 0) red[warp][CMAX] = (double)wq;
   __syncthreads();
-  if(tid <= ncols) {
-    // column c: slot c / G of the warps of group c % G (warp order)
-    const int c = tid;
-    const int gg = c < ncols ? c % G : 0, slot = c < ncols ? c / G : BULK_ACC;
-    const int wpg = F / 32;  // warps per group
+  if(tid < cn || (wcol && tid == CMAX)) {
+    const int col = tid < cn ? cb + tid : ncols;
     double sum = 0.;
-    for(int k2 = 0; k2 < wpg; ++k2) sum += red[gg * wpg + k2][slot];
-    partials[(int64_t)c * MAXRED + blockIdx.x] = sum;
+    for(int k = 0; k < RB / 32; ++k) sum += red[k][tid];
+    partials[(int64_t)col * MAXRED + blockIdx.x] = sum;
+    // only the threads that wrote partials order them before the counter
+    __threadfence();
   }
+  __syncthreads();
+  if(tid == 0) last = atomicAdd(&st->counter, 1u) == gridDim.x * gridDim.y - 1;
+  __syncthreads();
+  if(!last) return;
+  __threadfence();
+  const int nc = ncols + 1, T = max(1, RB / nc), nb = (int)gridDim.x;
+  // nc > RB (restart lengths above 255) is not launched
+  const int c = tid / T, s = tid - c * T;
+  double part = 0.;
+  if(c < nc) {
+    const double *pc = partials + (int64_t)c * MAXRED;
+    double v4[4] = {0., 0., 0., 0.};
+    for(int k0 = 0; s + T * k0 < nb; k0 += 16) {
+      // straight-line loads (indices clamped into the array, the extra ones
+      // zeroed by selects), so that all 16 are in flight at once
+      double v[16];
+#pragma unroll
+      for(int k = 0; k < 16; ++k) {
+        const int b = s + T * (k0 + k);
+        v[k] = __ldcg(pc + (b < nb ? b : 0));
+      }
+#pragma unroll
+      for(int k = 0; k < 16; ++k) v4[k & 3] += s + T * (k0 + k) < nb ? v[k] : 0.;
+    }
+    part = (v4[0] + v4[1]) + (v4[2] + v4[3]);
+  }
+  flat[tid] = part;
+  __syncthreads();
+  if(tid < nc) {
+    double sum = 0.;
+    for(int k = 0; k < T; ++k) sum += flat[tid * T + k];
+    if(tid == ncols) {
+      st->result[2] = sum;
+    } else {
+      hcur[tid] = sum;
+      Hcol[tid] = second ? Hcol[tid] + sum : sum;
+    }
+  }
+  if(tid == 0) st->counter = 0;
 }
 
 // The update pass w - V h over c < ncols.
@@ -783,60 +774,18 @@ __global__ void __launch_bounds__(RB, 1) k_gs_dots_bulk(int64_t ld, const float 
 // !NORM (after a dot pass that took the norm by Pythagoras): unless a second
 // pass was asked for, the result times st->finv is the next basis vector
 // (vnext); otherwise it goes back to w.
-// FROMPART (NORM, first pass, after k_gs_dots_bulk): every block first sums
-// the dot pass's per-block partials (nparts per column, the same order in
-// every block) into h and ||w||^2; block 0 stores h as hcur and as the
-// Hessenberg column (Hcol[c], c < ncols) and ||w||^2 in st->result[2]; the
-// norm partials of this pass go to the column after the last dot column.
-template <int CMAX, bool NORM, bool FROMPART = false>
+template <int CMAX, bool NORM>
 __global__ void __launch_bounds__(RB, 4) k_gs_upd(int64_t n4, int64_t ld, const float *__restrict__ V, int ncols,
                                                   const double *__restrict__ hprev, float *__restrict__ w,
                                                   float *__restrict__ vnext, RedState *st, double *partials,
-                                                  double *Hnext, const int *__restrict__ done, int second,
-                                                  int nparts = 0, double *hcur = nullptr, double *Hcol = nullptr)
+                                                  double *Hnext, const int *__restrict__ done, int second)
 {
+  FE_PDL_ENTRY();
   if(*done || (NORM && second && !st->reorth)) return;
   __shared__ float hs[CMAX];
   __shared__ double wred[RB / 32];
-  __shared__ double hsd[CMAX + 1];
   __shared__ bool last;
-  if constexpr(FROMPART) {
-    // columns c = warp + 8 u, all loads of a round in flight at once
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for(int c0 = warp; c0 <= ncols; c0 += 4 * (RB / 32)) {
-      double sm[4] = {0., 0., 0., 0.};
-#pragma unroll
-      for(int u = 0; u < 4; ++u) {
-        const int c = c0 + u * (RB / 32);
-#pragma unroll
-        for(int b8 = 0; b8 < 8; ++b8) {
-          const int b = lane + 32 * b8;
-          if(c <= ncols && b < nparts) sm[u] += __ldcg(partials + (int64_t)c * MAXRED + b);
-        }
-      }
-#pragma unroll
-      for(int u = 0; u < 4; ++u) {
-        double v = sm[u];
-        for(int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        const int c = c0 + u * (RB / 32);
-        if(lane == 0 && c <= ncols) hsd[c] = v;
-      }
-    }
-    __syncthreads();
-    for(int c = threadIdx.x; c < CMAX; c += RB) hs[c] = c < ncols ? (float)hsd[c] : 0.f;
-    if(blockIdx.x == 0)
-      for(int c = threadIdx.x; c <= ncols; c += RB) {
-        if(c < ncols) {
-          hcur[c] = hsd[c];
-          Hcol[c] = hsd[c];
-        } else {
-          st->result[2] = hsd[c];
-        }
-      }
-    partials += (int64_t)(ncols + 1) * MAXRED;
-  } else {
-    for(int c = threadIdx.x; c < CMAX; c += RB) hs[c] = c < ncols ? (float)hprev[c] : 0.f;
-  }
+  for(int c = threadIdx.x; c < CMAX; c += RB) hs[c] = c < ncols ? (float)hprev[c] : 0.f;
   __syncthreads();
   const bool again = NORM || st->reorth != 0;
   const float inv = NORM ? 1.f : st->finv;
@@ -895,9 +844,11 @@ __global__ void __launch_bounds__(RB, 4) k_gs_upd(int64_t n4, int64_t ld, const 
     double s8[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
     const int nb = (int)gridDim.x;
     for(int b0 = lane; b0 < nb; b0 += 256) {
+      double v[8];
 #pragma unroll
-      for(int k = 0; k < 8; ++k)
-        if(b0 + 32 * k < nb) s8[k] += __ldcg(partials + b0 + 32 * k);
+      for(int k = 0; k < 8; ++k) v[k] = __ldcg(partials + (b0 + 32 * k < nb ? b0 + 32 * k : 0));
+#pragma unroll
+      for(int k = 0; k < 8; ++k) s8[k] += b0 + 32 * k < nb ? v[k] : 0.;
     }
     double sum = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
     for(int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
@@ -906,7 +857,7 @@ __global__ void __launch_bounds__(RB, 4) k_gs_upd(int64_t n4, int64_t ld, const 
       st->result[0] = sum;
       *Hnext = nrm;
       st->finv = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
-      if(!second) st->reorth = sum < 1e-2 * (FROMPART ? hsd[ncols] : st->result[2]) ? 1 : 0;
+      if(!second) st->reorth = sum < 1e-2 * st->result[2] ? 1 : 0;
       st->counter = 0;
     }
   }
@@ -915,9 +866,15 @@ __global__ void __launch_bounds__(RB, 4) k_gs_upd(int64_t n4, int64_t ld, const 
 // v = w * (1 / ||w||) in FP32, 4 rows per thread; the scale comes from the
 // last update + norm pass (k_gs_upd<., true> or k_gs32<., 2>).
 // gated: only after a second Gram-Schmidt pass (otherwise k_gs_upd wrote v).
+// gs (ungated only): after its share of the scaling, warp 0 of block 0
+// applies the Givens rotations of step j (k_givens folded in; a block that
+// starts after the step converged skips its share of v, which the cycle no
+// longer reads).
 __global__ void k_scale32(int64_t n4, const float *__restrict__ w, float *__restrict__ v, const RedState *st,
-                          const int *__restrict__ done, int gated)
+                          const int *__restrict__ done, int gated, GmresState *gs = nullptr, int j = 0)
 {
+  FE_PDL_ENTRY();
+  __shared__ double sh[MAXM + 1], scs[MAXM], ssn[MAXM];
   if(*done || (gated && !st->reorth)) return;
   const float inv = st->finv;
   const float4 *w4 = reinterpret_cast<const float4 *>(w);
@@ -930,12 +887,14 @@ __global__ void k_scale32(int64_t n4, const float *__restrict__ w, float *__rest
     t.w *= inv;
     v4[g] = t;
   }
+  if(gs && blockIdx.x == 0 && threadIdx.x < 32) givens_warp(gs, j, threadIdx.x, sh, scs, ssn);
 }
 
 // V_0 = r / ||r|| rounded to FP32 (start of a mixed cycle), beta = ||r||.
 __global__ void k_scale_r32(int64_t n, const double *__restrict__ r, float *__restrict__ v, const RedState *st,
                             double *beta, const int *__restrict__ done)
 {
+  FE_PDL_ENTRY();
   if(*done) return;
   const double nrm = sqrt(st->result[0]);
   if(blockIdx.x == 0 && threadIdx.x == 0) *beta = nrm;
@@ -946,6 +905,7 @@ __global__ void k_scale_r32(int64_t n, const double *__restrict__ r, float *__re
 
 __global__ void k_gmres_init(GmresState *gs, const RedState *st)
 {
+  FE_PDL_ENTRY();
   const double beta = sqrt(st->result[0]);
   const double tol = gs->tol;
   gs->g[0] = beta;
@@ -968,6 +928,7 @@ template <typename VF>
 __global__ void k_ilu_copy(int64_t lnnz, const int32_t *__restrict__ srcPos, const double *__restrict__ v64,
                            const float *__restrict__ v32, VF *__restrict__ f)
 {
+  FE_PDL_ENTRY();
   for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < lnnz; k += (int64_t)gridDim.x * blockDim.x)
     f[k] = v64 ? (VF)v64[srcPos[k]] : (VF)v32[srcPos[k]];
 }
@@ -1040,6 +1001,7 @@ __global__ void __launch_bounds__(ILU_NARROW_THREADS) k_ilu_factor_run(
     const int32_t *__restrict__ lia, const int32_t *__restrict__ lja, const int32_t *__restrict__ ldiag,
     VF *__restrict__ f, int *__restrict__ status)
 {
+  FE_PDL_ENTRY();
   const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for(int32_t lv = lv0; lv < lv1; ++lv) {
     for(int32_t q = lvl[lv] + warp; q < lvl[lv + 1]; q += nw) ilu_factor_row<VF>(rows[q], lia, lja, ldiag, f, status);
@@ -1053,6 +1015,7 @@ __global__ void k_ilu_factor_level(int32_t q0, int32_t q1, const int32_t *__rest
                                    const int32_t *__restrict__ lia, const int32_t *__restrict__ lja,
                                    const int32_t *__restrict__ ldiag, VF *__restrict__ f, int *__restrict__ status)
 {
+  FE_PDL_ENTRY();
   const int64_t q = q0 + ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
   if(q < q1) ilu_factor_row<VF>(rows[q], lia, lja, ldiag, f, status);
 }
@@ -1063,6 +1026,7 @@ __global__ void __launch_bounds__(ILU_NARROW_THREADS) k_ilu_solve_run(
     const int32_t *__restrict__ lia, const int32_t *__restrict__ lja, const int32_t *__restrict__ ldiag,
     const VF *__restrict__ f, const VV *__restrict__ r, VV *__restrict__ z, const int *__restrict__ done)
 {
+  FE_PDL_ENTRY();
   if(done && *done) return;
   const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for(int32_t lv = lv0; lv < lv1; ++lv) {
@@ -1078,6 +1042,7 @@ __global__ void k_ilu_solve_level(int32_t q0, int32_t q1, const int32_t *__restr
                                   const int32_t *__restrict__ ldiag, const VF *__restrict__ f,
                                   const VV *__restrict__ r, VV *__restrict__ z, const int *__restrict__ done)
 {
+  FE_PDL_ENTRY();
   if(done && *done) return;
   const int64_t q = q0 + ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
   if(q < q1) ilu_solve_row<VF, VV, LOWER>(rows[q], lia, lja, ldiag, f, r, z);
@@ -1087,6 +1052,7 @@ template <typename VV, typename VD>
 __global__ void k_jacobi(int64_t n, const VD *__restrict__ dinv, const VV *__restrict__ r,
                          VV *__restrict__ z, const int *__restrict__ done)
 {
+  FE_PDL_ENTRY();
   if(done && *done) return;
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
       i += (int64_t)gridDim.x * blockDim.x)
@@ -1097,6 +1063,7 @@ template <typename VA, typename VD>
 __global__ void k_inv_diag(int64_t n, const int32_t *__restrict__ diag, const VA *__restrict__ a,
                            VD *__restrict__ dinv, int *__restrict__ status)
 {
+  FE_PDL_ENTRY();
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
       i += (int64_t)gridDim.x * blockDim.x) {
     const VA d = a[diag[i]];
@@ -1118,6 +1085,7 @@ __global__ void k_cg_xr(int64_t n, CGState *cs, const double *__restrict__ p,
                         const double *__restrict__ q, double *__restrict__ x,
                         double *__restrict__ r, double *partials, RedState *st)
 {
+  FE_PDL_ENTRY();
   // alpha = rz / pq ; x += alpha p ; r -= alpha q ; accumulate rr
   double v[1] = {0.};
   if(!cs->done) {
@@ -1135,6 +1103,7 @@ __global__ void k_cg_xr(int64_t n, CGState *cs, const double *__restrict__ p,
 
 __global__ void k_cg_check(CGState *cs, const RedState *st)
 {
+  FE_PDL_ENTRY();
   if(cs->done) return;
   cs->rr = st->result[0];
   cs->it++;
@@ -1144,6 +1113,7 @@ __global__ void k_cg_check(CGState *cs, const RedState *st)
 __global__ void k_cg_p(int64_t n, CGState *cs, const RedState *st, const double *__restrict__ z,
                        double *__restrict__ p, int first)
 {
+  FE_PDL_ENTRY();
   if(cs->done) return;
   const double rzNew = st->result[0];
   const double beta = first ? 0. : rzNew / cs->rz;
@@ -1156,12 +1126,14 @@ __global__ void k_cg_p(int64_t n, CGState *cs, const RedState *st, const double 
 
 __global__ void k_cg_rz(CGState *cs, const RedState *st)
 {
+  FE_PDL_ENTRY();
   if(cs->done) return;
   cs->rz = st->result[0];
 }
 
 __global__ void k_cg_pq(CGState *cs, const RedState *st)
 {
+  FE_PDL_ENTRY();
   if(cs->done) return;
   cs->pq = st->result[0];
   if(cs->pq == 0.0 || !isfinite(cs->pq)) cs->done = 1;
@@ -1170,6 +1142,7 @@ __global__ void k_cg_pq(CGState *cs, const RedState *st)
 __global__ void k_dot_if(int64_t n, const double *__restrict__ x, const double *__restrict__ y,
                          double *partials, RedState *st, const CGState *cs)
 {
+  FE_PDL_ENTRY();
   double v[1] = {0.};
   if(!cs->done)
     for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -1180,6 +1153,7 @@ __global__ void k_dot_if(int64_t n, const double *__restrict__ x, const double *
 
 __global__ void k_zero(int64_t n, double *x)
 {
+  FE_PDL_ENTRY();
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
       i += (int64_t)gridDim.x * blockDim.x)
     x[i] = 0.;
@@ -1187,6 +1161,7 @@ __global__ void k_zero(int64_t n, double *x)
 
 __global__ void k_copy(int64_t n, const double *__restrict__ a, double *__restrict__ b)
 {
+  FE_PDL_ENTRY();
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
       i += (int64_t)gridDim.x * blockDim.x)
     b[i] = a[i];
@@ -1194,6 +1169,7 @@ __global__ void k_copy(int64_t n, const double *__restrict__ a, double *__restri
 
 __global__ void k_axpy(int64_t n, double alpha, const double *__restrict__ x, double *__restrict__ y)
 {
+  FE_PDL_ENTRY();
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
       i += (int64_t)gridDim.x * blockDim.x)
     y[i] += alpha * x[i];
@@ -1301,16 +1277,10 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
   }
   // whole waves of the update passes (three blocks per SM)
   gsParts_ = grid_for((n_ + 3) / 4, RB, std::min(MAXRED, 3 * nSM_));
-  // bulk-copy dot pass: one block per SM (the update pass sums up to 256
-  // partials per column), basis columns long enough to fill the stages
-  // FENG_GS_BULK=0 keeps the register-streaming dot pass with its own
-  // reduction (the same sums; for comparisons)
-  bool bulkOk = true;
-  if(const char *e = std::getenv("FENG_GS_BULK")) bulkOk = std::strcmp(e, "0") != 0;
-  if(bulkOk && opt.method == 1 && opt.mixed && nSM_ <= 256 && ld32_ >= (int64_t)1024 * nSM_) {
-    CK(cudaFuncSetAttribute(k_gs_dots_bulk, cudaFuncAttributeMaxDynamicSharedMemorySize, 220000));
-    bulkGs_ = true;
-  }
+  // dot pass: one pass over all columns (k_gs_dots_all); FENG_GS_DOTS=groups
+  // keeps the column-group grid of k_gs_dots (the same products, summed in
+  // another order; for comparisons)
+  if(const char *e = std::getenv("FENG_GS_DOTS")) allDots_ = std::strcmp(e, "groups") != 0;
   CK(cudaMalloc(&v32_, sizeof(float) * n_));
   CK(cudaMalloc(&w32_, sizeof(float) * ((n_ + 63) / 64 * 64)));
   CK(cudaMemset(w32_, 0, sizeof(float) * ((n_ + 63) / 64 * 64)));
@@ -1464,17 +1434,14 @@ template <typename VF>
 void Krylov::ilu_factor_levels(const double *values64, const float *values32)
 {
   VF *f = (VF *)ilu_.vals;
-  (k_ilu_copy<VF><<<grid_for(ilu_.lnnz, 256, 4096), 256, 0, s_>>>(ilu_.lnnz, ilu_.srcPos, values64, values32, f),
-   ::feng::count_launch());
+  ::feng::launch_k(k_ilu_copy<VF>, grid_for(ilu_.lnnz, 256, 4096), 256, 0, s_, ilu_.lnnz, ilu_.srcPos, values64, values32, f);
   for(const auto &sg : ilu_.segL) {
     if(sg.wide)
-      (k_ilu_factor_level<VF><<<(unsigned)(((int64_t)sg.rows * 32 + 255) / 256), 256, 0, s_>>>(
-           sg.q0, sg.q1, ilu_.rowsL, ilu_.lia, ilu_.lja, ilu_.ldiag, f, ilu_.status),
-       ::feng::count_launch());
+      ::feng::launch_k(k_ilu_factor_level<VF>, (unsigned)(((int64_t)sg.rows * 32 + 255) / 256), 256, 0, s_, 
+           sg.q0, sg.q1, ilu_.rowsL, ilu_.lia, ilu_.lja, ilu_.ldiag, f, ilu_.status);
     else
-      (k_ilu_factor_run<VF><<<1, ILU_NARROW_THREADS, 0, s_>>>(sg.lv0, sg.lv1, ilu_.lvlL, ilu_.rowsL, ilu_.lia,
-                                                                ilu_.lja, ilu_.ldiag, f, ilu_.status),
-       ::feng::count_launch());
+      ::feng::launch_k(k_ilu_factor_run<VF>, 1, ILU_NARROW_THREADS, 0, s_, sg.lv0, sg.lv1, ilu_.lvlL, ilu_.rowsL, ilu_.lia,
+                                                                ilu_.lja, ilu_.ldiag, f, ilu_.status);
   }
 }
 
@@ -1484,25 +1451,21 @@ void Krylov::ilu_solve_levels(const VV *r, VV *z, const int *done)
   const VF *f = (const VF *)ilu_.vals;
   for(const auto &sg : ilu_.segL) {
     if(sg.wide)
-      (k_ilu_solve_level<VF, VV, true><<<(unsigned)(((int64_t)sg.rows * 32 + 255) / 256), 256, 0, s_>>>(
-           sg.q0, sg.q1, ilu_.rowsL, ilu_.lia, ilu_.lja, ilu_.ldiag, f, r, z, done),
-       ::feng::count_launch());
+      ::feng::launch_k(k_ilu_solve_level<VF, VV, true>, (unsigned)(((int64_t)sg.rows * 32 + 255) / 256), 256, 0, s_, 
+           sg.q0, sg.q1, ilu_.rowsL, ilu_.lia, ilu_.lja, ilu_.ldiag, f, r, z, done);
     else
-      (k_ilu_solve_run<VF, VV, true><<<1, ILU_NARROW_THREADS, 0, s_>>>(sg.lv0, sg.lv1, ilu_.lvlL, ilu_.rowsL,
+      ::feng::launch_k(k_ilu_solve_run<VF, VV, true>, 1, ILU_NARROW_THREADS, 0, s_, sg.lv0, sg.lv1, ilu_.lvlL, ilu_.rowsL,
                                                                          ilu_.lia, ilu_.lja, ilu_.ldiag, f, r, z,
-                                                                         done),
-       ::feng::count_launch());
+                                                                         done);
   }
   for(const auto &sg : ilu_.segU) {
     if(sg.wide)
-      (k_ilu_solve_level<VF, VV, false><<<(unsigned)(((int64_t)sg.rows * 32 + 255) / 256), 256, 0, s_>>>(
-           sg.q0, sg.q1, ilu_.rowsU, ilu_.lia, ilu_.lja, ilu_.ldiag, f, r, z, done),
-       ::feng::count_launch());
+      ::feng::launch_k(k_ilu_solve_level<VF, VV, false>, (unsigned)(((int64_t)sg.rows * 32 + 255) / 256), 256, 0, s_, 
+           sg.q0, sg.q1, ilu_.rowsU, ilu_.lia, ilu_.lja, ilu_.ldiag, f, r, z, done);
     else
-      (k_ilu_solve_run<VF, VV, false><<<1, ILU_NARROW_THREADS, 0, s_>>>(sg.lv0, sg.lv1, ilu_.lvlU, ilu_.rowsU,
+      ::feng::launch_k(k_ilu_solve_run<VF, VV, false>, 1, ILU_NARROW_THREADS, 0, s_, sg.lv0, sg.lv1, ilu_.lvlU, ilu_.rowsU,
                                                                           ilu_.lia, ilu_.lja, ilu_.ldiag, f, r, z,
-                                                                          done),
-       ::feng::count_launch());
+                                                                          done);
   }
 }
 
@@ -1514,6 +1477,7 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int64_t n, const int32_t *__r
                                                    const float *__restrict__ x, float *__restrict__ y,
                                                    const int *__restrict__ done)
 {
+  FE_PDL_ENTRY();
   if(done && *done) return;
   const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if(row >= n) return;
@@ -1533,6 +1497,7 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int64_t n, const int32_t *__r
 __global__ void k_sell_gather(int64_t m, const int32_t *__restrict__ src, const float *__restrict__ a,
                               float *__restrict__ out)
 {
+  FE_PDL_ENTRY();
   for(int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
     const int32_t k = src[e];
     out[e] = k >= 0 ? a[k] : 0.f;
@@ -1587,7 +1552,7 @@ int Krylov::factor(const double *values64, const float *values32)
   cur64_ = values64;
   cur32_ = values32;
   if(opt.mixed && sellVal_ && values32)
-    (k_sell_gather<<<grid_for(sellN_, 256, 4096), 256, 0, s_>>>(sellN_, sellSrc_, values32, sellVal_), ::feng::count_launch());
+    ::feng::launch_k(k_sell_gather, grid_for(sellN_, 256, 4096), 256, 0, s_, sellN_, sellSrc_, values32, sellVal_);
   if(opt.precond == 0) { factoredOk_ = true; return FE_OK; }
   if(opt.precond == 3 || opt.precond == 4) {
     FE_TRY(factor_mg(values64, values32));
@@ -1597,8 +1562,8 @@ int Krylov::factor(const double *values64, const float *values32)
   CK(cudaMemsetAsync(ilu_.status, 0, sizeof(int), s_));
   if(opt.precond == 2) {
     const int g = grid_for(n_, 256, 4096);
-    if(opt.mixed) (k_inv_diag<float, float><<<g, 256, 0, s_>>>(n_, A_.diag, values32, diag32_, ilu_.status), ::feng::count_launch());
-    else (k_inv_diag<double, double><<<g, 256, 0, s_>>>(n_, A_.diag, values64, diag_, ilu_.status), ::feng::count_launch());
+    if(opt.mixed) ::feng::launch_k(k_inv_diag<float, float>, g, 256, 0, s_, n_, A_.diag, values32, diag32_, ilu_.status);
+    else ::feng::launch_k(k_inv_diag<double, double>, g, 256, 0, s_, n_, A_.diag, values64, diag_, ilu_.status);
   } else {
     if(opt.mixed) ilu_factor_levels<float>(nullptr, values32);
     else ilu_factor_levels<double>(values64, nullptr);
@@ -1622,7 +1587,7 @@ void Krylov::precond64(const double *r, double *z, const int *done)
   } else if(opt.precond >= 3) {
     apply_mg<double>(cur64_, r, z, done);
   } else if(opt.precond == 2) {
-    (k_jacobi<double, double><<<grid_for(n_, 256, 4096), 256, 0, s_>>>(n_, diag_, r, z, done), ::feng::count_launch());
+    ::feng::launch_k(k_jacobi<double, double>, grid_for(n_, 256, 4096), 256, 0, s_, n_, diag_, r, z, done);
   } else {
     ilu_solve_levels<double, double>(r, z, done);
   }
@@ -1635,7 +1600,7 @@ void Krylov::precond32(const float *r, float *z, const int *done)
   } else if(opt.precond >= 3) {
     apply_mg<float>(cur32_, r, z, done);
   } else if(opt.precond == 2) {
-    (k_jacobi<float, float><<<grid_for(n_, 256, 4096), 256, 0, s_>>>(n_, diag32_, r, z, done), ::feng::count_launch());
+    ::feng::launch_k(k_jacobi<float, float>, grid_for(n_, 256, 4096), 256, 0, s_, n_, diag32_, r, z, done);
   } else {
     ilu_solve_levels<float, float>(r, z, done);
   }
@@ -1649,11 +1614,11 @@ static void spmv_launch(int lanes, int64_t n, const DeviceCSR &A, const VA *a, c
   const int64_t threads = n * lanes;
   const int grid = (int)((threads + 255) / 256);
   if(lanes == 16)
-    (k_spmv<VA, VX, VY, ACC, 16, RESID><<<grid, 256, 0, s>>>(n, A.ia, A.ja, a, x, b, y, done), ::feng::count_launch());
+    ::feng::launch_k(k_spmv<VA, VX, VY, ACC, 16, RESID>, grid, 256, 0, s, n, A.ia, A.ja, a, x, b, y, done);
   else if(lanes == 8)
-    (k_spmv<VA, VX, VY, ACC, 8, RESID><<<grid, 256, 0, s>>>(n, A.ia, A.ja, a, x, b, y, done), ::feng::count_launch());
+    ::feng::launch_k(k_spmv<VA, VX, VY, ACC, 8, RESID>, grid, 256, 0, s, n, A.ia, A.ja, a, x, b, y, done);
   else
-    (k_spmv<VA, VX, VY, ACC, 4, RESID><<<grid, 256, 0, s>>>(n, A.ia, A.ja, a, x, b, y, done), ::feng::count_launch());
+    ::feng::launch_k(k_spmv<VA, VX, VY, ACC, 4, RESID>, grid, 256, 0, s, n, A.ia, A.ja, a, x, b, y, done);
 }
 
 void Krylov::spmv64(const double *values, const double *x, double *y)
@@ -1665,7 +1630,7 @@ void Krylov::spmv64(const double *values, const double *x, double *y)
 void Krylov::spmv32(const float *values, const double *x, double *y)
 {
   const int gv = grid_for(n_, 256, 2048);
-  (k_to_f32<<<gv, 256, 0, s_>>>(n_, x, v32_, nullptr), ::feng::count_launch());
+  ::feng::launch_k(k_to_f32, gv, 256, 0, s_, n_, x, v32_, nullptr);
   spmv_launch<float, float, double, float, false>(lanes_, n_, A_, values, v32_, nullptr, y, nullptr, s_);
 }
 
@@ -1675,13 +1640,82 @@ int Krylov::spmvHot()
     set_error("no mixed-precision FGMRES");
     return FE_INVALID_ARG;
   }
-  if(sellVal_) (k_spmv_sell<<<grid_for(n_, 256, 1 << 20), 256, 0, s_>>>(n_, sellPtr_, sellCol_, sellVal_, Z32_, w32_, nullptr), ::feng::count_launch());
+  if(sellVal_) ::feng::launch_k(k_spmv_sell, grid_for(n_, 256, 1 << 20), 256, 0, s_, n_, sellPtr_, sellCol_, sellVal_, Z32_, w32_, nullptr);
   else if(cur32_) spmv_launch<float, float, float, float, false>(lanes_, n_, A_, cur32_, Z32_, nullptr, w32_, nullptr, s_);
   return FE_OK;
 }
 
+int Krylov::precondGraph(int reps, double *avgMs)
+{
+  if(!factoredOk_ || reps < 1 || !avgMs) {
+    set_error("preconditioner not built, or an invalid benchmark request");
+    return FE_INVALID_ARG;
+  }
+  if(opt.mixed && (!V32_ || !Z32_)) {
+    set_error("no mixed FP32 basis");
+    return FE_INVALID_ARG;
+  }
+  cudaGraph_t graph;
+  cudaGraphExec_t exec;
+  CK(cudaStreamBeginCapture(s_, cudaStreamCaptureModeThreadLocal));
+  ++g_capturing;
+  for(int r = 0; r < reps; ++r) {
+    if(opt.mixed) precond32(V32_, Z32_, nullptr);
+    else precond64(V_, Z_, nullptr);
+  }
+  --g_capturing;
+  CK(cudaStreamEndCapture(s_, &graph));
+  CK(cudaGraphInstantiate(&exec, graph, 0));
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  CK(cudaGraphLaunch(exec, s_));  // warm replay
+  CK(cudaEventRecord(a, s_));
+  CK(cudaGraphLaunch(exec, s_));
+  CK(cudaEventRecord(b, s_));
+  CK(cudaEventSynchronize(b));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  CK(cudaGetLastError());
+  *avgMs = ms / reps;
+  return FE_OK;
+}
+
+int Krylov::cycleGraph(bool mixed, const void *vals, const double *b, double *x, int reps, double *msPerStep)
+{
+  if(reps < 1 || !msPerStep || !useGraphs_ || opt.method != 1) {
+    set_error("an invalid benchmark request (FGMRES with CUDA graphs)");
+    return FE_INVALID_ARG;
+  }
+  const double saved = *htol_;
+  *htol_ = 0.;  // never converged: every kernel of the m steps runs
+  const int m = opt.restart;
+  cudaEvent_t a, e;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&e));
+  int st = run_cycle(mixed, vals, b, x, m);  // capture + warm replay
+  float ms = 0.f;
+  if(st == FE_OK) {
+    CK(cudaEventRecord(a, s_));
+    for(int r = 0; r < reps && st == FE_OK; ++r) st = run_cycle(mixed, vals, b, x, m);
+    CK(cudaEventRecord(e, s_));
+    CK(cudaEventSynchronize(e));
+    CK(cudaEventElapsedTime(&ms, a, e));
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(e);
+  *htol_ = saved;
+  *msPerStep = ms / ((double)reps * m);
+  return st;
+}
+
 __global__ void k_f32_to_f64(int64_t n, const float *__restrict__ x, double *__restrict__ y)
 {
+  FE_PDL_ENTRY();
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     y[i] = (double)x[i];
 }
@@ -1695,9 +1729,9 @@ int Krylov::applyPrecond(const double *r, double *z)
   if(opt.mixed) {
     const int gv = grid_for(n_, 256, 2048);
     float *zf = Z32_ ? Z32_ : w32_;
-    (k_to_f32<<<gv, 256, 0, s_>>>(n_, r, v32_, nullptr), ::feng::count_launch());
+    ::feng::launch_k(k_to_f32, gv, 256, 0, s_, n_, r, v32_, nullptr);
     precond32(v32_, zf, nullptr);
-    if(z) (k_f32_to_f64<<<gv, 256, 0, s_>>>(n_, zf, z), ::feng::count_launch());
+    if(z) ::feng::launch_k(k_f32_to_f64, gv, 256, 0, s_, n_, zf, z);
   } else {
     precond64(r, z, nullptr);
   }
@@ -1707,7 +1741,7 @@ int Krylov::applyPrecond(const double *r, double *z)
 double Krylov::dot(const double *x, const double *y)
 {
   Ws w = Ws_INIT(this);
-  (k_dot<<<nParts_, RB, 0, s_>>>(n_, x, y, red_, w.st, dsum_), ::feng::count_launch());
+  ::feng::launch_k(k_dot, nParts_, RB, 0, s_, n_, x, y, red_, w.st, dsum_);
   cudaMemcpyAsync(hred_, dsum_, sizeof(double), cudaMemcpyDeviceToHost, s_);
   cudaStreamSynchronize(s_);
   return hred_[0];
@@ -1718,7 +1752,7 @@ double Krylov::norm2(const double *x) { return sqrt(dot(x, x)); }
 double Krylov::norminf(const double *x)
 {
   Ws w = Ws_INIT(this);
-  (k_absmax<<<nParts_, RB, 0, s_>>>(n_, x, red_, w.st, dsum_), ::feng::count_launch());
+  ::feng::launch_k(k_absmax, nParts_, RB, 0, s_, n_, x, red_, w.st, dsum_);
   cudaMemcpyAsync(hred_, dsum_, sizeof(double), cudaMemcpyDeviceToHost, s_);
   cudaStreamSynchronize(s_);
   return hred_[0];
@@ -1726,7 +1760,7 @@ double Krylov::norminf(const double *x)
 
 int Krylov::gsStep(int mode, int ncols, int64_t *bytes)
 {
-  if(!V32_ || (mode != 0 && mode != 4 && !(mode == 6 && bulkGs_)) || ncols < 1 || ncols > opt.restart) {
+  if(!V32_ || (mode != 0 && mode != 4 && mode != 6) || ncols < 1 || ncols > opt.restart) {
     set_error("no mixed FP32 basis, or an invalid Gram-Schmidt request");
     return FE_INVALID_ARG;
   }
@@ -1735,9 +1769,8 @@ int Krylov::gsStep(int mode, int ncols, int64_t *bytes)
     CK(cudaMemsetAsync(zeroFlag_, 0, sizeof(int), s_));
   }
   Ws w = Ws_INIT(this);
-  if(mode == 0) gs32(0, ncols, nullptr, w.gs->hcur, w.gs->H, zeroFlag_, 0);
-  else if(mode == 6) gs32(6, ncols, nullptr, nullptr, nullptr, zeroFlag_, 0);
-  else gs32(4, ncols, w.gs->hcur, nullptr, w.gs->H + ncols, zeroFlag_, 0);
+  if(mode == 4) gs32(4, ncols, w.gs->hcur, nullptr, w.gs->H + ncols, zeroFlag_, 0);
+  else gs32(mode, ncols, nullptr, w.gs->hcur, w.gs->H, zeroFlag_, 0);
   // dots: ncols columns and w read; update: ncols columns and w read, w
   // written
   if(bytes) *bytes = (int64_t)(ncols + (mode == 4 ? 2 : 1)) * ld32_ * (int64_t)sizeof(float);
@@ -1746,7 +1779,7 @@ int Krylov::gsStep(int mode, int ncols, int64_t *bytes)
 
 int Krylov::gsStepStream(int mode, int ncols, int reps, double *avgMs)
 {
-  if(!V32_ || (mode != 0 && mode != 4 && !(mode == 6 && bulkGs_)) || ncols < 1 || ncols > opt.restart || reps < 1 ||
+  if(!V32_ || (mode != 0 && mode != 4) || ncols < 1 || ncols > opt.restart || reps < 1 ||
      !avgMs) {
     set_error("no mixed FP32 basis, or an invalid Gram-Schmidt request");
     return FE_INVALID_ARG;
@@ -1778,7 +1811,6 @@ int Krylov::gsStepStream(int mode, int ncols, int reps, double *avgMs)
     V32_ = (float *)(buf + per * c);
     w32_ = (float *)(buf + per * c + (size_t)(ncols + 1) * colBytes);
     if(mode == 0) gs32(0, ncols, nullptr, w.gs->hcur, w.gs->H, zeroFlag_, 0);
-    else if(mode == 6) gs32(6, ncols, nullptr, nullptr, nullptr, zeroFlag_, 0);
     else gs32(4, ncols, w.gs->hcur, nullptr, w.gs->H + ncols, zeroFlag_, 0);
   };
   for(int c = 0; c < copies; ++c) pass(c);  // warm-up round
@@ -1797,28 +1829,11 @@ int Krylov::gsStepStream(int mode, int ncols, int reps, double *avgMs)
   return FE_OK;
 }
 
-// Rows per chunk and stages of the bulk dot pass for ncols columns and w:
-// two or more stages within 220,000 bytes of shared memory, at most
-// BULK_ACC column accumulators per thread; rows = 0 when none fits.
-void Krylov::bulkCfg(int ncols, int &rows, int &nst) const
-{
-  const int64_t budget = 220000;
-  for(rows = 1024; rows >= 256; rows >>= 1) {
-    const int G = 1024 / rows;
-    if((ncols + G - 1) / G > BULK_ACC) continue;
-    const int64_t per = (int64_t)(ncols + 1) * rows * (int64_t)sizeof(float);
-    nst = (int)std::min<int64_t>(BULK_MAXST, budget / per);
-    if(nst >= 2) return;
-  }
-  rows = 0;
-  nst = 0;
-}
-
 // One FP32 Gram-Schmidt pass over the first ncols basis vectors: mode 0 the
 // dot pass (k_gs_dots), 5 the dot pass with the Pythagoras norm, 1 update +
 // dots, 2 update + norm (k_gs32), 3 the update that writes the next basis
-// vector, 4 update + norm (k_gs_upd), 6 the bulk-copy dot pass (partials
-// only, k_gs_dots_bulk), 7 update + norm summing those partials first.
+// vector, 4 update + norm (k_gs_upd), 6 the dot pass by column groups
+// (k_gs_dots; mode 0 runs k_gs_dots_all unless FENG_GS_DOTS=groups).
 void Krylov::gs32(int mode, int ncols, const double *hprev, double *hcur, double *Hcol, const int *done, int pass)
 {
   RedState *st = (RedState *)red_state_;
@@ -1828,37 +1843,30 @@ void Krylov::gs32(int mode, int ncols, const double *hprev, double *hcur, double
 #define FE_GS_LAUNCH(C)                                                                                         \
   do {                                                                                                          \
     if(mode == 0)                                                                                               \
-      (k_gs32<C, 0><<<g, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done, pass), ::feng::count_launch()); \
+      ::feng::launch_k(k_gs32<C, 0>, g, RB, 0, s_, n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done, pass); \
     else if(mode == 1)                                                                                          \
-      (k_gs32<C, 1><<<g, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done, pass), ::feng::count_launch()); \
+      ::feng::launch_k(k_gs32<C, 1>, g, RB, 0, s_, n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done, pass); \
     else if(mode == 2)                                                                                          \
-      (k_gs32<C, 2><<<g, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done, pass), ::feng::count_launch()); \
+      ::feng::launch_k(k_gs32<C, 2>, g, RB, 0, s_, n4, ld32_, V32_, ncols, hprev, w32_, red_, st, hcur, Hcol, done, pass); \
     else if(mode == 3)                                                                                          \
-      (k_gs_upd<C, false><<<gu, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, V32_ + (int64_t)ncols * ld32_, st, red_, nullptr, done, 0), ::feng::count_launch()); \
+      ::feng::launch_k(k_gs_upd<C, false>, gu, RB, 0, s_, n4, ld32_, V32_, ncols, hprev, w32_, V32_ + (int64_t)ncols * ld32_, st, red_, nullptr, done, 0); \
     else                                                                                                        \
-      (k_gs_upd<C, true><<<gu, RB, 0, s_>>>(n4, ld32_, V32_, ncols, hprev, w32_, nullptr, st, red_, Hcol, done, pass), ::feng::count_launch()); \
+      ::feng::launch_k(k_gs_upd<C, true>, gu, RB, 0, s_, n4, ld32_, V32_, ncols, hprev, w32_, nullptr, st, red_, Hcol, done, pass); \
   } while(0)
-  if(mode == 6) {
-    int rows = 0, nst = 0;
-    bulkCfg(ncols, rows, nst);
-    const size_t sm = (size_t)nst * (ncols + 1) * rows * sizeof(float);
-    (k_gs_dots_bulk<<<nSM_, RB, sm, s_>>>(ld32_, V32_, ncols, w32_, red_, done, rows, nst), ::feng::count_launch());
+  if(mode == 0 && allDots_) {
+    // one pass over w and every column (k_gs_dots_all), one wave of four
+    // blocks per SM over the slices of 16 columns
+    const int gy = (ncols + 15) / 16;
+    const int gd = (int)std::max<int64_t>(
+        1, std::min<int64_t>({(n4 + RB - 1) / RB, (int64_t)(4 * nSM_ + gy - 1) / gy, (int64_t)MAXRED}));
+#define FE_GSA_LAUNCH(C)                                                                                    \
+  ::feng::launch_k(k_gs_dots_all<C>, dim3(gd, gy), RB, 0, s_, n4, ld32_, V32_, ncols, w32_, red_, st, hcur, Hcol, done, pass)
+    if(ncols <= 8) FE_GSA_LAUNCH(8);
+    else FE_GSA_LAUNCH(16);
+#undef FE_GSA_LAUNCH
     return;
   }
-  if(mode == 7) {
-    // hcur, Hcol: outputs (h, and the Hessenberg column with its norm entry)
-#define FE_GS_BULK_UPD(C)                                                                                         \
-  (k_gs_upd<C, true, true><<<gu, RB, 0, s_>>>(n4, ld32_, V32_, ncols, nullptr, w32_, nullptr, st, red_,           \
-                                              Hcol + ncols, done, 0, nSM_, hcur, Hcol),                           \
-   ::feng::count_launch())
-    if(ncols <= 8) FE_GS_BULK_UPD(8);
-    else if(ncols <= 16) FE_GS_BULK_UPD(16);
-    else if(ncols <= 32) FE_GS_BULK_UPD(32);
-    else FE_GS_BULK_UPD(64);
-#undef FE_GS_BULK_UPD
-    return;
-  }
-  if(mode == 0 || mode == 5) {
+  if(mode == 0 || mode == 5 || mode == 6) {
     // mode 5: the dot pass that also takes the norm of the update by Pythagoras
     // about four blocks per SM in all: each block loops over several row
     // groups (fewer partials, one counter increment per block)
@@ -1866,8 +1874,7 @@ void Krylov::gs32(int mode, int ncols, const double *hprev, double *hcur, double
     const int64_t gx = std::max<int64_t>(
         1, std::min<int64_t>({(n4 + RB - 1) / RB, (int64_t)MAXRED, (int64_t)(4 * nSM_ + gy - 1) / gy}));
     const dim3 gb((unsigned)gx, (unsigned)gy);
-    (k_gs_dots<<<gb, RB, 0, s_>>>(n4, ld32_, V32_, ncols, w32_, red_, st, hcur, Hcol, done, pass, mode == 5 ? 1 : 0),
-     ::feng::count_launch());
+    ::feng::launch_k(k_gs_dots, gb, RB, 0, s_, n4, ld32_, V32_, ncols, w32_, red_, st, hcur, Hcol, done, pass, mode == 5 ? 1 : 0);
     return;
   }
   if(ncols <= 8) FE_GS_LAUNCH(8);
@@ -1894,9 +1901,9 @@ void Krylov::launch_cycle(bool mixed, const void *vals, const double *b, double 
   spmv_launch<double, double, double, double, true>(lanes_, n_, A_, (const double *)vals, x, b, w_, nullptr, s_);
   cudaMemsetAsync(&w.gs->done, 0, sizeof(int), s_);
   cudaMemcpyAsync(&w.gs->tol, htol_, sizeof(double), cudaMemcpyHostToDevice, s_);
-  (k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done), ::feng::count_launch());
-  (k_gmres_init<<<1, 1, 0, s_>>>(w.gs, w.st), ::feng::count_launch());
-  (k_scale_from<<<gv, 256, 0, s_>>>(n_, w_, V_, w.st, &w.gs->beta, &w.gs->done), ::feng::count_launch());
+  ::feng::launch_k(k_norm_to, nParts_, RB, 0, s_, n_, w_, red_, w.st, &w.gs->done);
+  ::feng::launch_k(k_gmres_init, 1, 1, 0, s_, w.gs, w.st);
+  ::feng::launch_k(k_scale_from, gv, 256, 0, s_, n_, w_, V_, w.st, &w.gs->beta, &w.gs->done);
   for(int j = 0; j < jmax; ++j) {
     double *vj = V_ + (int64_t)j * n_;
     {
@@ -1907,17 +1914,17 @@ void Krylov::launch_cycle(bool mixed, const void *vals, const double *b, double 
     }
     double *Hcol = w.gs->H + (int64_t)j * (MAXM + 1);
     for(int pass = 0; pass < 2; ++pass) {
-      (k_mdot_partial<<<dim3(nParts_, j + 1), RB, 0, s_>>>(n_, V_, j + 1, w_, red_, &w.gs->done), ::feng::count_launch());
-      (k_mdot_final<<<j + 1, RB, 0, s_>>>(nParts_, red_, w.gs->hcur, Hcol, pass, &w.gs->done), ::feng::count_launch());
-      (k_mupdate<<<gv, 256, 0, s_>>>(n_, V_, j + 1, w.gs->hcur, w_, &w.gs->done), ::feng::count_launch());
+      ::feng::launch_k(k_mdot_partial, dim3(nParts_, j + 1), RB, 0, s_, n_, V_, j + 1, w_, red_, &w.gs->done);
+      ::feng::launch_k(k_mdot_final, j + 1, RB, 0, s_, nParts_, red_, w.gs->hcur, Hcol, pass, &w.gs->done);
+      ::feng::launch_k(k_mupdate, gv, 256, 0, s_, n_, V_, j + 1, w.gs->hcur, w_, &w.gs->done);
     }
-    (k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done), ::feng::count_launch());
-    (k_scale_from<<<gv, 256, 0, s_>>>(n_, w_, V_ + (int64_t)(j + 1) * n_, w.st, Hcol + j + 1, &w.gs->done), ::feng::count_launch());
-    (k_givens<<<1, 32, 0, s_>>>(w.gs, j), ::feng::count_launch());
+    ::feng::launch_k(k_norm_to, nParts_, RB, 0, s_, n_, w_, red_, w.st, &w.gs->done);
+    ::feng::launch_k(k_scale_from, gv, 256, 0, s_, n_, w_, V_ + (int64_t)(j + 1) * n_, w.st, Hcol + j + 1, &w.gs->done);
+    ::feng::launch_k(k_givens, 1, 32, 0, s_, w.gs, j);
     if(poll && poll_done(&w.gs->done, j)) break;
   }
-  (k_backsolve<<<1, 128, backsolveSmem(opt.restart), s_>>>(w.gs), ::feng::count_launch());
-  (k_xupdate<double><<<gv, 256, 0, s_>>>(n_, n_, Z_, w.gs, x), ::feng::count_launch());
+  ::feng::launch_k(k_backsolve, 1, 128, backsolveSmem(opt.restart), s_, w.gs);
+  ::feng::launch_k(k_xupdate<double>, gv, 256, 0, s_, n_, n_, Z_, w.gs, x);
   cudaMemcpyAsync(h_gmres_, w.gs, sizeof(GmresHead), cudaMemcpyDeviceToHost, s_);
 }
 
@@ -1934,20 +1941,19 @@ void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, i
   spmv_launch<float, double, double, double, true>(lanes_, n_, A_, vals, x, b, w_, nullptr, s_);
   cudaMemsetAsync(&w.gs->done, 0, sizeof(int), s_);
   cudaMemcpyAsync(&w.gs->tol, htol_, sizeof(double), cudaMemcpyHostToDevice, s_);
-  (k_norm_to<<<nParts_, RB, 0, s_>>>(n_, w_, red_, w.st, &w.gs->done), ::feng::count_launch());
-  (k_gmres_init<<<1, 1, 0, s_>>>(w.gs, w.st), ::feng::count_launch());
-  (k_scale_r32<<<gv, 256, 0, s_>>>(n_, w_, V32_, w.st, &w.gs->beta, &w.gs->done), ::feng::count_launch());
+  ::feng::launch_k(k_norm_to, nParts_, RB, 0, s_, n_, w_, red_, w.st, &w.gs->done);
+  ::feng::launch_k(k_gmres_init, 1, 1, 0, s_, w.gs, w.st);
+  ::feng::launch_k(k_scale_r32, gv, 256, 0, s_, n_, w_, V32_, w.st, &w.gs->beta, &w.gs->done);
   const int g4 = grid_for(ld32_ / 4, 256, 4 * 152);
   for(int j = 0; j < jmax; ++j) {
     const float *vj = V32_ + (int64_t)j * ld32_;
     float *zj = Z32_ + (int64_t)j * ld32_;
     precond32(vj, zj, &w.gs->done);
+    double *Hcol = w.gs->H + (int64_t)j * (MAXM + 1);
     if(sellVal_)
-      (k_spmv_sell<<<grid_for(n_, 256, 1 << 20), 256, 0, s_>>>(n_, sellPtr_, sellCol_, sellVal_, zj, w32_, &w.gs->done),
-       ::feng::count_launch());
+      ::feng::launch_k(k_spmv_sell, grid_for(n_, 256, 1 << 20), 256, 0, s_, n_, sellPtr_, sellCol_, sellVal_, zj, w32_, &w.gs->done);
     else
       spmv_launch<float, float, float, float, false>(lanes_, n_, A_, vals, zj, nullptr, w32_, &w.gs->done, s_);
-    double *Hcol = w.gs->H + (int64_t)j * (MAXM + 1);
     if(opt.gsPasses == 2) {
       // always twice: dots, fused update + dots, update + norm
       gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 0);
@@ -1966,27 +1972,25 @@ void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, i
     } else {
       // once (dot pass, update + norm pass), and a second time only when
       // the update kept less than a tenth of ||w|| (decided on the device,
-      // so the replayed graph is fixed); the first dot pass streams the
-      // basis through bulk copies and leaves its per-block sums to the
-      // update pass
-      if(bulkGs_) {
-        gs32(6, j + 1, nullptr, nullptr, nullptr, &w.gs->done, 0);
-        gs32(7, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 0);
-      } else {
-        gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 0);
-        gs32(4, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done, 0);
-      }
+      // so the replayed graph is fixed)
+      gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 0);
+      gs32(4, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done, 0);
       gs32(0, j + 1, nullptr, w.gs->hcur, Hcol, &w.gs->done, 1);
       gs32(4, j + 1, w.gs->hcur, nullptr, Hcol + j + 1, &w.gs->done, 1);
     }
-    (k_scale32<<<g4, 256, 0, s_>>>(ld32_ / 4, w32_, V32_ + (int64_t)(j + 1) * ld32_, w.st, &w.gs->done,
-                                   opt.gsPasses == 3 ? 1 : 0),
-     ::feng::count_launch());
-    (k_givens<<<1, 32, 0, s_>>>(w.gs, j), ::feng::count_launch());
+    if(opt.gsPasses == 3) {
+      // gated scale (only after a second pass), then the rotations
+      ::feng::launch_k(k_scale32, g4, 256, 0, s_, ld32_ / 4, w32_, V32_ + (int64_t)(j + 1) * ld32_, w.st, &w.gs->done, 1,
+                       (GmresState *)nullptr, 0);
+      ::feng::launch_k(k_givens, 1, 32, 0, s_, w.gs, j);
+    } else {
+      ::feng::launch_k(k_scale32, g4, 256, 0, s_, ld32_ / 4, w32_, V32_ + (int64_t)(j + 1) * ld32_, w.st, &w.gs->done, 0, w.gs,
+                                     j);
+    }
     if(poll && poll_done(&w.gs->done, j)) break;
   }
-  (k_backsolve<<<1, 128, backsolveSmem(opt.restart), s_>>>(w.gs), ::feng::count_launch());
-  (k_xupdate<float><<<gv, 256, 0, s_>>>(n_, ld32_, Z32_, w.gs, x), ::feng::count_launch());
+  ::feng::launch_k(k_backsolve, 1, 128, backsolveSmem(opt.restart), s_, w.gs);
+  ::feng::launch_k(k_xupdate<float>, gv, 256, 0, s_, n_, ld32_, Z32_, w.gs, x);
   cudaMemcpyAsync(h_gmres_, w.gs, sizeof(GmresHead), cudaMemcpyDeviceToHost, s_);
 }
 
@@ -2093,31 +2097,31 @@ int Krylov::solve_cg64(const double *vals, const double *b, double *x, double to
   Ws w = Ws_INIT(this);
   const int gv = grid_for(n_, 256, 2048);
   // x = 0, r = b
-  (k_zero<<<gv, 256, 0, s_>>>(n_, x), ::feng::count_launch());
-  (k_copy<<<gv, 256, 0, s_>>>(n_, b, r_), ::feng::count_launch());
+  ::feng::launch_k(k_zero, gv, 256, 0, s_, n_, x);
+  ::feng::launch_k(k_copy, gv, 256, 0, s_, n_, b, r_);
   CGState init{};
   init.tol = tolAbs;
   init.done = 0;
   cudaMemcpyAsync(w.cg, &init, sizeof(CGState), cudaMemcpyHostToDevice, s_);
   // z = M r ; rz = r.z ; p = z
   precond64(r_, t_, &w.cg->done);
-  (k_dot_if<<<nParts_, RB, 0, s_>>>(n_, r_, t_, red_, w.st, w.cg), ::feng::count_launch());
-  (k_cg_p<<<gv, 256, 0, s_>>>(n_, w.cg, w.st, t_, p_, 1), ::feng::count_launch());
-  (k_cg_rz<<<1, 1, 0, s_>>>(w.cg, w.st), ::feng::count_launch());
+  ::feng::launch_k(k_dot_if, nParts_, RB, 0, s_, n_, r_, t_, red_, w.st, w.cg);
+  ::feng::launch_k(k_cg_p, gv, 256, 0, s_, n_, w.cg, w.st, t_, p_, 1);
+  ::feng::launch_k(k_cg_rz, 1, 1, 0, s_, w.cg, w.st);
   int it = 0;
   while(it < maxIt) {
     const int batch = std::min(8, maxIt - it);
     for(int k = 0; k < batch; ++k) {
       spmv_launch<double, double, double, double, false>(lanes_, n_, A_, vals, p_, nullptr, q_,
                                                          &w.cg->done, s_);
-      (k_dot_if<<<nParts_, RB, 0, s_>>>(n_, p_, q_, red_, w.st, w.cg), ::feng::count_launch());
-      (k_cg_pq<<<1, 1, 0, s_>>>(w.cg, w.st), ::feng::count_launch());
-      (k_cg_xr<<<nParts_, RB, 0, s_>>>(n_, w.cg, p_, q_, x, r_, red_, w.st), ::feng::count_launch());
-      (k_cg_check<<<1, 1, 0, s_>>>(w.cg, w.st), ::feng::count_launch());
+      ::feng::launch_k(k_dot_if, nParts_, RB, 0, s_, n_, p_, q_, red_, w.st, w.cg);
+      ::feng::launch_k(k_cg_pq, 1, 1, 0, s_, w.cg, w.st);
+      ::feng::launch_k(k_cg_xr, nParts_, RB, 0, s_, n_, w.cg, p_, q_, x, r_, red_, w.st);
+      ::feng::launch_k(k_cg_check, 1, 1, 0, s_, w.cg, w.st);
       precond64(r_, t_, &w.cg->done);
-      (k_dot_if<<<nParts_, RB, 0, s_>>>(n_, r_, t_, red_, w.st, w.cg), ::feng::count_launch());
-      (k_cg_p<<<gv, 256, 0, s_>>>(n_, w.cg, w.st, t_, p_, 0), ::feng::count_launch());
-      (k_cg_rz<<<1, 1, 0, s_>>>(w.cg, w.st), ::feng::count_launch());
+      ::feng::launch_k(k_dot_if, nParts_, RB, 0, s_, n_, r_, t_, red_, w.st, w.cg);
+      ::feng::launch_k(k_cg_p, gv, 256, 0, s_, n_, w.cg, w.st, t_, p_, 0);
+      ::feng::launch_k(k_cg_rz, 1, 1, 0, s_, w.cg, w.st);
     }
     it += batch;
     cudaMemcpyAsync(w.hcg, w.cg, sizeof(CGState), cudaMemcpyDeviceToHost, s_);
@@ -2143,7 +2147,7 @@ int Krylov::solve(const double *values64, const float *values32, const double *b
   st.rnorm0 = bn;
   if(!std::isfinite(bn)) { set_error("non-finite right-hand side"); return FE_NONFINITE; }
   const int gv = grid_for(n_, 256, 2048);
-  (k_zero<<<gv, 256, 0, s_>>>(n_, x), ::feng::count_launch());
+  ::feng::launch_k(k_zero, gv, 256, 0, s_, n_, x);
   const double tolAbs = std::max(opt.rtol * bn, opt.atol);
   if(bn <= opt.atol) { st.rnorm = bn; return FE_OK; }
   if(opt.method == 0) {

@@ -156,11 +156,10 @@ class Krylov {
   float *sellVal_ = nullptr;
   int64_t sellN_ = 0;  // entries with padding
   int build_sell();
+  bool allDots_ = true;       // dot pass k_gs_dots_all (else k_gs_dots)
   int *zeroFlag_ = nullptr;  // a device 0 ("not done") for gsStep
   int gsParts_ = 0;       // blocks of the FP32 Gram-Schmidt update passes
   int nSM_ = 1;           // multiprocessors of the device
-  bool bulkGs_ = false;   // first dot pass by bulk copies (k_gs_dots_bulk)
-  void bulkCfg(int ncols, int &rows, int &nst) const;
   int64_t ld32_ = 0;      // leading dimension of V32_ / Z32_ (multiple of 64)
   // pass: 0 first pass (the update + norm decides on reorthogonalisation),
   // 1 the conditional second pass, 2 the last pass of an unconditional CGS2
@@ -221,6 +220,16 @@ class Krylov {
   // The Arnoldi SpMV of the mixed path on the current FP32 matrix (sliced
   // ELL when built, else CSR), FP32 vectors (benchmark phase).
   int spmvHot();
+  // The preconditioner application of an Arnoldi step (the mixed path: the
+  // FP32 basis column 0 into Z column 0; FP64 otherwise), reps of them
+  // captured in one CUDA graph and replayed (after a warm replay) without
+  // anything between: ms per application (benchmark phase).
+  int precondGraph(int reps, double *avgMs);
+  // One full FGMRES(m) restart cycle of the current system (vals, b) from
+  // x, replayed from its captured CUDA graph with the convergence test
+  // disabled, so that all m Arnoldi steps run: ms per Arnoldi step, the
+  // cycle's residual and update included (benchmark phase; x is scratch).
+  int cycleGraph(bool mixed, const void *vals, const double *b, double *x, int reps, double *msPerStep);
   int factor_mg(const double *values64, const float *values32);
   template <typename V> void apply_mg(const V *vals, const V *r, V *z, const int *skip);
 };

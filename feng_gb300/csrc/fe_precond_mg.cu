@@ -14,6 +14,7 @@
 
 #include "fe_amg.h"
 #include "fe_common.h"
+#include "fe_launch.h"
 #include "fe_krylov.h"
 
 namespace feng {
@@ -89,6 +90,7 @@ constexpr int NPART = 512;
 template <typename V>
 __global__ void k_dot_part(int64_t n, const V *__restrict__ a, const V *__restrict__ b, double *part)
 {
+  FE_PDL_ENTRY();
   __shared__ double sh[256];
   double s = 0.;
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -104,6 +106,7 @@ __global__ void k_dot_part(int64_t n, const V *__restrict__ a, const V *__restri
 
 __global__ void k_dot_fin(int nparts, const double *__restrict__ part, double *out)
 {
+  FE_PDL_ENTRY();
   __shared__ double sh[256];
   double s = 0.;
   for(int i = threadIdx.x; i < nparts; i += blockDim.x) s += part[i];
@@ -122,6 +125,7 @@ template <typename V>
 __global__ void k_pcg_xr(int64_t n, const double *__restrict__ scal, const V *__restrict__ p,
                          const V *__restrict__ q, V *__restrict__ x, V *__restrict__ r)
 {
+  FE_PDL_ENTRY();
   const double pq = scal[1];
   const double alpha = (pq != 0. && isfinite(pq)) ? scal[0] / pq : 0.;
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -135,22 +139,26 @@ template <typename V>
 __global__ void k_pcg_p(int64_t n, const double *__restrict__ scal, const V *__restrict__ z, V *__restrict__ p,
                         int first)
 {
+  FE_PDL_ENTRY();
   const double beta = (first || scal[0] == 0.) ? 0. : scal[2] / scal[0];
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     p[i] = z[i] + (V)beta * p[i];
 }
 
-__global__ void k_pcg_shift(double *scal) { scal[0] = scal[2]; }
+__global__ void k_pcg_shift(double *scal) {
+  FE_PDL_ENTRY(); scal[0] = scal[2]; }
 
 template <typename V>
 __global__ void k_copy_v(int64_t n, const V *__restrict__ a, V *__restrict__ b)
 {
+  FE_PDL_ENTRY();
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     b[i] = a[i];
 }
 
 __global__ void k_zero_d(int64_t n, double *x)
 {
+  FE_PDL_ENTRY();
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) x[i] = 0.;
 }
 
@@ -177,25 +185,25 @@ void Krylov::MG::solveK(const V *b, V *x, cudaStream_t st)
   const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 4096));
   const int gp = (int)std::min<int64_t>(NPART, std::max<int64_t>(1, (n + 255) / 256));
   V *r = (V *)ir, *z = (V *)iz, *p = (V *)ip, *q = (V *)iq;
-  (k_copy_v<V><<<g, 256, 0, st>>>(n, b, r), ::feng::count_launch());
+  ::feng::launch_k(k_copy_v<V>, g, 256, 0, st, n, b, r);
   // x = 0 (written through r's type)
-  if constexpr(sizeof(V) == 8) (k_zero_d<<<g, 256, 0, st>>>(n, (double *)x), ::feng::count_launch());
+  if constexpr(sizeof(V) == 8) ::feng::launch_k(k_zero_d, g, 256, 0, st, n, (double *)x);
   else cudaMemsetAsync(x, 0, sizeof(float) * n, st);
   vc(r, z);
-  (k_dot_part<V><<<gp, 256, 0, st>>>(n, r, z, part), ::feng::count_launch());
-  (k_dot_fin<<<1, 256, 0, st>>>(gp, part, scal + 0), ::feng::count_launch());
-  (k_pcg_p<V><<<g, 256, 0, st>>>(n, scal, z, p, 1), ::feng::count_launch());
+  ::feng::launch_k(k_dot_part<V>, gp, 256, 0, st, n, r, z, part);
+  ::feng::launch_k(k_dot_fin, 1, 256, 0, st, gp, part, scal + 0);
+  ::feng::launch_k(k_pcg_p<V>, g, 256, 0, st, n, scal, z, p, 1);
   for(int it = 0; it < inner; ++it) {
     spmv(p, q);
-    (k_dot_part<V><<<gp, 256, 0, st>>>(n, p, q, part), ::feng::count_launch());
-    (k_dot_fin<<<1, 256, 0, st>>>(gp, part, scal + 1), ::feng::count_launch());
-    (k_pcg_xr<V><<<g, 256, 0, st>>>(n, scal, p, q, x, r), ::feng::count_launch());
+    ::feng::launch_k(k_dot_part<V>, gp, 256, 0, st, n, p, q, part);
+    ::feng::launch_k(k_dot_fin, 1, 256, 0, st, gp, part, scal + 1);
+    ::feng::launch_k(k_pcg_xr<V>, g, 256, 0, st, n, scal, p, q, x, r);
     if(it + 1 == inner) break;
     vc(r, z);
-    (k_dot_part<V><<<gp, 256, 0, st>>>(n, r, z, part), ::feng::count_launch());
-    (k_dot_fin<<<1, 256, 0, st>>>(gp, part, scal + 2), ::feng::count_launch());
-    (k_pcg_p<V><<<g, 256, 0, st>>>(n, scal, z, p, 0), ::feng::count_launch());
-    (k_pcg_shift<<<1, 1, 0, st>>>(scal), ::feng::count_launch());
+    ::feng::launch_k(k_dot_part<V>, gp, 256, 0, st, n, r, z, part);
+    ::feng::launch_k(k_dot_fin, 1, 256, 0, st, gp, part, scal + 2);
+    ::feng::launch_k(k_pcg_p<V>, g, 256, 0, st, n, scal, z, p, 0);
+    ::feng::launch_k(k_pcg_shift, 1, 1, 0, st, scal);
   }
 }
 
@@ -207,6 +215,7 @@ template <typename VA>
 __global__ void k_diag_sum(int64_t n, const int32_t *__restrict__ pos, const VA *__restrict__ a,
                            double *out)
 {
+  FE_PDL_ENTRY();
   __shared__ double sh[256];
   double s = 0.;
   for(int64_t i = threadIdx.x; i < n; i += blockDim.x) s += (double)a[pos[i]];
@@ -223,6 +232,7 @@ template <typename V>
 __global__ void k_scale_copy(int64_t n, const V *__restrict__ r, V *__restrict__ z, V f,
                              const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     z[i] = r[i] * f;
@@ -237,6 +247,7 @@ __global__ void k_pressure(int64_t nP, const int32_t *__restrict__ rows, const S
                            const double *__restrict__ consts, const V *__restrict__ r, V *__restrict__ z,
                            const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   const double c = *cr, cSc = consts[1], cMc = consts[2];
   const double shift = cMc > 0 ? c / cMc : 0., lift = cSc != 0. ? c / cSc : 0.;
@@ -251,6 +262,7 @@ __global__ void k_pressure(int64_t nP, const int32_t *__restrict__ rows, const S
 template <typename V>
 __global__ void k_psum_part(int64_t nP, const int32_t *__restrict__ rows, const V *__restrict__ r, double *part)
 {
+  FE_PDL_ENTRY();
   __shared__ double sh[256];
   double s = 0.;
   for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nP; k += (int64_t)gridDim.x * blockDim.x)
@@ -271,6 +283,7 @@ template <typename V>
 __global__ void k_psum(int64_t nP, const int32_t *__restrict__ rows, const V *__restrict__ r, double *part,
                        unsigned *count, double *out)
 {
+  FE_PDL_ENTRY();
   __shared__ double sh[256];
   __shared__ bool last;
   double s = 0.;
@@ -307,6 +320,7 @@ __global__ void k_psum(int64_t nP, const int32_t *__restrict__ rows, const V *__
 // partial sums of a double array
 __global__ void k_tsum(int64_t n, const double *__restrict__ t, double *part)
 {
+  FE_PDL_ENTRY();
   __shared__ double sh[256];
   double s = 0.;
   for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
@@ -325,6 +339,7 @@ template <typename V>
 __global__ void k_gsum(int64_t nN, const int32_t *__restrict__ upIa, const int32_t *__restrict__ upPos,
                        const V *__restrict__ a, V *__restrict__ bx, V *__restrict__ by)
 {
+  FE_PDL_ENTRY();
   for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nN; k += (int64_t)gridDim.x * blockDim.x)
     for(int c = 0; c < 2; ++c) {
       double s = 0.;
@@ -341,6 +356,7 @@ __global__ void k_dw(int64_t nP, const int32_t *__restrict__ dnIa, const int32_t
                      const V *__restrict__ a, const V *__restrict__ wx, const V *__restrict__ wy,
                      double *__restrict__ t)
 {
+  FE_PDL_ENTRY();
   for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nP; k += (int64_t)gridDim.x * blockDim.x) {
     double s = 0.;
     for(int32_t e = dnIa[k]; e < dnIa[k + 1]; ++e) {
@@ -360,6 +376,7 @@ __global__ void k_vel_rhs(int64_t nN, const int32_t *__restrict__ dofX, const in
                           const V *__restrict__ r, const V *__restrict__ z, V *__restrict__ bx,
                           V *__restrict__ by, const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nN; k += (int64_t)gridDim.x * blockDim.x) {
     for(int c = 0; c < 2; ++c) {
@@ -377,6 +394,7 @@ __global__ void k_vel_rhs(int64_t nN, const int32_t *__restrict__ dofX, const in
 template <typename V>
 __global__ void k_gather_vals(int64_t n, const int32_t *__restrict__ pos, const V *__restrict__ a, V *__restrict__ out)
 {
+  FE_PDL_ENTRY();
   for(int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
     out[e] = a[pos[e]];
 }
@@ -389,6 +407,7 @@ __global__ void k_p_gather(int64_t nP, const int32_t *__restrict__ rows, const d
                            const double *__restrict__ cr, const double *__restrict__ consts, const V *__restrict__ r,
                            V *__restrict__ pr, const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   const double cMc = consts[2];
   const double shift = cMc > 0 ? *cr / cMc : 0.;
@@ -400,6 +419,7 @@ template <typename V>
 __global__ void k_p_add(int64_t nP, const int32_t *__restrict__ rows, const V *__restrict__ pz,
                         const double *__restrict__ consts, V *__restrict__ z, const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   const V cc = (V)consts[3];
   for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nP; k += (int64_t)gridDim.x * blockDim.x)
@@ -414,6 +434,7 @@ __global__ void k_vel_rhs_pair(int64_t nN, const int32_t *__restrict__ dofX, con
                                const V *__restrict__ r, const V *__restrict__ z, V *__restrict__ bxy,
                                const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   for(int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 2 * nN; q += (int64_t)gridDim.x * blockDim.x) {
     const int64_t k = q >> 1;
@@ -429,6 +450,7 @@ __global__ void k_vel_out_pair(int64_t nN, const int32_t *__restrict__ dofX, con
                                const V *__restrict__ zxy, const double *__restrict__ consts, V *__restrict__ z,
                                const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   const V f = (V)consts[0];
   for(int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 2 * nN; q += (int64_t)gridDim.x * blockDim.x) {
@@ -442,6 +464,7 @@ __global__ void k_vel_out(int64_t nN, const int32_t *__restrict__ dofX, const in
                           const V *__restrict__ zx, const V *__restrict__ zy, const double *__restrict__ consts,
                           V *__restrict__ z, const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   const V f = (V)consts[0];
   for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nN; k += (int64_t)gridDim.x * blockDim.x) {
@@ -457,6 +480,7 @@ __global__ void k_vel_rhs_nc(int64_t nq, const int32_t *__restrict__ dofC, const
                              const int32_t *__restrict__ upCol, const V *__restrict__ g, const V *__restrict__ r,
                              const V *__restrict__ z, V *__restrict__ b, const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   for(int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (int64_t)gridDim.x * blockDim.x) {
     V t = r[dofC[q]];
@@ -469,6 +493,7 @@ template <typename V>
 __global__ void k_vel_out_nc(int64_t nq, const int32_t *__restrict__ dofC, const V *__restrict__ zc,
                              const double *__restrict__ consts, V *__restrict__ z, const int *__restrict__ skip)
 {
+  FE_PDL_ENTRY();
   if(skip && *skip) return;
   const V f = (V)consts[0];
   for(int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (int64_t)gridDim.x * blockDim.x)
@@ -480,6 +505,7 @@ template <typename V>
 __global__ void k_gsum_nc(int64_t nq, const int32_t *__restrict__ upIa, const int32_t *__restrict__ upPos,
                           const V *__restrict__ a, V *__restrict__ b)
 {
+  FE_PDL_ENTRY();
   for(int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (int64_t)gridDim.x * blockDim.x) {
     double s = 0.;
     for(int32_t e = upIa[q]; e < upIa[q + 1]; ++e) s += (double)a[upPos[e]];
@@ -493,6 +519,7 @@ __global__ void k_dw_nc(int64_t nP, const int32_t *__restrict__ dnIa, const int3
                         const int32_t *__restrict__ dnCol, const int32_t *__restrict__ slotOf,
                         const V *__restrict__ a, const V *__restrict__ w, double *__restrict__ t)
 {
+  FE_PDL_ENTRY();
   for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nP; k += (int64_t)gridDim.x * blockDim.x) {
     double s = 0.;
     for(int32_t e = dnIa[k]; e < dnIa[k + 1]; ++e) s += (double)a[dnPos[e]] * (double)w[slotOf[dnCol[e]]];
@@ -631,8 +658,8 @@ int Krylov::factor_mg(const double *values64, const float *values32)
 {
   MG &M = *mg_;
   M.amg->setSkip(nullptr);
-  if(values64) (k_diag_sum<double><<<1, 256, 0, s_>>>(M.nNodes, M.diagX, values64, M.dsum), ::feng::count_launch());
-  else (k_diag_sum<float><<<1, 256, 0, s_>>>(M.nNodes, M.diagX, values32, M.dsum), ::feng::count_launch());
+  if(values64) ::feng::launch_k(k_diag_sum<double>, 1, 256, 0, s_, M.nNodes, M.diagX, values64, M.dsum);
+  else ::feng::launch_k(k_diag_sum<float>, 1, 256, 0, s_, M.nNodes, M.diagX, values32, M.dsum);
   double sum = 0.;
   CKM(cudaMemcpyAsync(&sum, M.dsum, sizeof(double), cudaMemcpyDeviceToHost, s_));
   CKM(cudaStreamSynchronize(s_));
@@ -647,9 +674,9 @@ int Krylov::factor_mg(const double *values64, const float *values32)
   if(M.kind == 4) {
     // Contiguous copy of the G block's values for the apply kernels.
     if(values64)
-      (k_gather_vals<double><<<grid(M.nG), 256, 0, s_>>>(M.nG, M.upPos, values64, (double *)M.gVals), ::feng::count_launch());
+      ::feng::launch_k(k_gather_vals<double>, grid(M.nG), 256, 0, s_, M.nG, M.upPos, values64, (double *)M.gVals);
     else
-      (k_gather_vals<float><<<grid(M.nG), 256, 0, s_>>>(M.nG, M.upPos, values32, (float *)M.gVals), ::feng::count_launch());
+      ::feng::launch_k(k_gather_vals<float>, grid(M.nG), 256, 0, s_, M.nG, M.upPos, values32, (float *)M.gVals);
     std::vector<double> sc(M.nP);
     std::vector<float> sc32(M.nP);
     for(int64_t k = 0; k < M.nP; ++k) {
@@ -667,32 +694,32 @@ int Krylov::factor_mg(const double *values64, const float *values32)
     if(M.nc == 3) {
       const int64_t nq = 3 * M.nNodes;
       if(values64) {
-        (k_gsum_nc<double><<<grid(nq), 256, 0, s_>>>(nq, M.upIa, M.upPos, values64, (double *)M.bxy), ::feng::count_launch());
+        ::feng::launch_k(k_gsum_nc<double>, grid(nq), 256, 0, s_, nq, M.upIa, M.upPos, values64, (double *)M.bxy);
         M.amg->vcycle3_64((const double *)M.bxy, (double *)M.zxy);
-        (k_dw_nc<double><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values64,
-                                                   (const double *)M.zxy, M.tP), ::feng::count_launch());
+        ::feng::launch_k(k_dw_nc<double>, grid(M.nP), 256, 0, s_, M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values64,
+                                                   (const double *)M.zxy, M.tP);
       } else {
-        (k_gsum_nc<float><<<grid(nq), 256, 0, s_>>>(nq, M.upIa, M.upPos, values32, (float *)M.bxy), ::feng::count_launch());
+        ::feng::launch_k(k_gsum_nc<float>, grid(nq), 256, 0, s_, nq, M.upIa, M.upPos, values32, (float *)M.bxy);
         M.amg->vcycle3_32((const float *)M.bxy, (float *)M.zxy);
-        (k_dw_nc<float><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values32,
-                                                  (const float *)M.zxy, M.tP), ::feng::count_launch());
+        ::feng::launch_k(k_dw_nc<float>, grid(M.nP), 256, 0, s_, M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values32,
+                                                  (const float *)M.zxy, M.tP);
       }
     } else if(values64) {
-      (k_gsum<double><<<g, 256, 0, s_>>>(M.nNodes, M.upIa, M.upPos, values64, (double *)M.bx, (double *)M.by), ::feng::count_launch());
+      ::feng::launch_k(k_gsum<double>, g, 256, 0, s_, M.nNodes, M.upIa, M.upPos, values64, (double *)M.bx, (double *)M.by);
       M.solveK<double>((const double *)M.bx, (double *)M.zx, s_);
       M.solveK<double>((const double *)M.by, (double *)M.zy, s_);
-      (k_dw<double><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values64,
-                                                (const double *)M.zx, (const double *)M.zy, M.tP), ::feng::count_launch());
+      ::feng::launch_k(k_dw<double>, grid(M.nP), 256, 0, s_, M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values64,
+                                                (const double *)M.zx, (const double *)M.zy, M.tP);
     } else {
-      (k_gsum<float><<<g, 256, 0, s_>>>(M.nNodes, M.upIa, M.upPos, values32, (float *)M.bx, (float *)M.by), ::feng::count_launch());
+      ::feng::launch_k(k_gsum<float>, g, 256, 0, s_, M.nNodes, M.upIa, M.upPos, values32, (float *)M.bx, (float *)M.by);
       M.solveK<float>((const float *)M.bx, (float *)M.zx, s_);
       M.solveK<float>((const float *)M.by, (float *)M.zy, s_);
-      (k_dw<float><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values32,
-                                               (const float *)M.zx, (const float *)M.zy, M.tP), ::feng::count_launch());
+      ::feng::launch_k(k_dw<float>, grid(M.nP), 256, 0, s_, M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values32,
+                                               (const float *)M.zx, (const float *)M.zy, M.tP);
     }
     const int gp = (int)std::min<int64_t>(NPART, std::max<int64_t>(1, (M.nP + 255) / 256));
-    (k_tsum<<<gp, 256, 0, s_>>>(M.nP, M.tP, M.part), ::feng::count_launch());
-    (k_dot_fin<<<1, 256, 0, s_>>>(gp, M.part, M.dsum), ::feng::count_launch());
+    ::feng::launch_k(k_tsum, gp, 256, 0, s_, M.nP, M.tP, M.part);
+    ::feng::launch_k(k_dot_fin, 1, 256, 0, s_, gp, M.part, M.dsum);
     CKM(cudaMemcpyAsync(&sum2, M.dsum, sizeof(double), cudaMemcpyDeviceToHost, s_));
     CKM(cudaStreamSynchronize(s_));
     M.cSc = -sum2 / M.s;
@@ -797,47 +824,42 @@ void Krylov::apply_mg(const V *vals, const V *r, V *z, const int *skip)
   M.amg->setSkip(skip);
   if(M.kind == 3) {
     // z = (s K)^-1 r on the unknown rows (the nodes are the unknowns)
-    (k_vel_rhs<V><<<grid(M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofX, nullptr, nullptr, nullptr,
-                                                  vals, r, z, (V *)M.bx, (V *)M.by, skip), ::feng::count_launch());
+    ::feng::launch_k(k_vel_rhs<V>, grid(M.nNodes), 256, 0, s_, M.nNodes, M.dofX, M.dofX, nullptr, nullptr, nullptr,
+                                                  vals, r, z, (V *)M.bx, (V *)M.by, skip);
   } else {
     const int gp = (int)std::min<int64_t>(NPART, std::max<int64_t>(1, (M.nP + 255) / 256));
-    (k_psum<V><<<gp, 256, 0, s_>>>(M.nP, M.pRows, r, M.part, M.count, M.scal + 3), ::feng::count_launch());
+    ::feng::launch_k(k_psum<V>, gp, 256, 0, s_, M.nP, M.pRows, r, M.part, M.count, M.scal + 3);
     const double *cr = M.scal + 3;
     if constexpr(sizeof(V) == 8)
-      (k_pressure<V, double><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.pRows, M.pScale64, M.pMassDev, cr, M.consts,
-                                                        r, z, skip), ::feng::count_launch());
+      ::feng::launch_k(k_pressure<V, double>, grid(M.nP), 256, 0, s_, M.nP, M.pRows, M.pScale64, M.pMassDev, cr, M.consts,
+                                                        r, z, skip);
     else
-      (k_pressure<V, float><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.pRows, M.pScale32, M.pMassDev, cr, M.consts,
-                                                       r, z, skip), ::feng::count_launch());
+      ::feng::launch_k(k_pressure<V, float>, grid(M.nP), 256, 0, s_, M.nP, M.pRows, M.pScale32, M.pMassDev, cr, M.consts,
+                                                       r, z, skip);
     if(M.amgP) {
       // + c0 L_p^-1 r_p (Cahouet-Chabard); its V-cycle skips with the cycle
       M.amgP->setSkip(skip);
-      (k_p_gather<V><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.pRows, M.pMassDev, cr, M.consts, r, (V *)M.pr, skip),
-       ::feng::count_launch());
+      ::feng::launch_k(k_p_gather<V>, grid(M.nP), 256, 0, s_, M.nP, M.pRows, M.pMassDev, cr, M.consts, r, (V *)M.pr, skip);
       if constexpr(sizeof(V) == 8) M.amgP->vcycle64((const double *)M.pr, (double *)M.pz);
       else M.amgP->vcycle32((const float *)M.pr, (float *)M.pz);
-      (k_p_add<V><<<grid(M.nP), 256, 0, s_>>>(M.nP, M.pRows, (const V *)M.pz, M.consts, z, skip),
-       ::feng::count_launch());
+      ::feng::launch_k(k_p_add<V>, grid(M.nP), 256, 0, s_, M.nP, M.pRows, (const V *)M.pz, M.consts, z, skip);
     }
     if(M.nc == 3) {
       // The three velocity components through one V-cycle on interleaved
       // right-hand sides, then z_u = (1/s) x.
       const int64_t nq = 3 * M.nNodes;
-      (k_vel_rhs_nc<V><<<grid(nq), 256, 0, s_>>>(nq, M.dofC, M.upIa, M.upCol, (const V *)M.gVals, r, z, (V *)M.bxy,
-                                                 skip),
-       ::feng::count_launch());
+      ::feng::launch_k(k_vel_rhs_nc<V>, grid(nq), 256, 0, s_, nq, M.dofC, M.upIa, M.upCol, (const V *)M.gVals, r, z, (V *)M.bxy,
+                                                 skip);
       if constexpr(sizeof(V) == 8) M.amg->vcycle3_64((const double *)M.bxy, (double *)M.zxy);
       else M.amg->vcycle3_32((const float *)M.bxy, (float *)M.zxy);
-      (k_vel_out_nc<V><<<grid(nq), 256, 0, s_>>>(nq, M.dofC, (const V *)M.zxy, M.consts, z, skip),
-       ::feng::count_launch());
+      ::feng::launch_k(k_vel_out_nc<V>, grid(nq), 256, 0, s_, nq, M.dofC, (const V *)M.zxy, M.consts, z, skip);
       return;
     }
     if(M.inner <= 0) {
       // Both velocity components through one paired V-cycle (one pass over
       // each level operator for the two right-hand sides).
-      (k_vel_rhs_pair<V><<<grid(2 * M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, M.upIa, nullptr, M.upCol,
-                                                               (const V *)M.gVals, r, z, (V *)M.bxy, skip),
-       ::feng::count_launch());
+      ::feng::launch_k(k_vel_rhs_pair<V>, grid(2 * M.nNodes), 256, 0, s_, M.nNodes, M.dofX, M.dofY, M.upIa, nullptr, M.upCol,
+                                                               (const V *)M.gVals, r, z, (V *)M.bxy, skip);
       // the finest post-smoothing pass writes z_u (times 1/s) itself when
       // it can; otherwise the interleaved result is scattered here
       AMGDevice::OutMap om;
@@ -849,19 +871,19 @@ void Krylov::apply_mg(const V *vals, const V *r, V *z, const int *skip)
       if constexpr(sizeof(V) == 8) written = M.amg->vcycle2_64((const double *)M.bxy, (double *)M.zxy, &om);
       else written = M.amg->vcycle2_32((const float *)M.bxy, (float *)M.zxy, &om);
       if(!written)
-        (k_vel_out_pair<V><<<grid(2 * M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, (const V *)M.zxy, M.consts,
-                                                                z, skip), ::feng::count_launch());
+        ::feng::launch_k(k_vel_out_pair<V>, grid(2 * M.nNodes), 256, 0, s_, M.nNodes, M.dofX, M.dofY, (const V *)M.zxy, M.consts,
+                                                                z, skip);
       return;
     }
-    (k_vel_rhs<V><<<grid(M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.dofY, M.upIa, M.upPos, M.upCol,
-                                                  vals, r, z, (V *)M.bx, (V *)M.by, skip), ::feng::count_launch());
+    ::feng::launch_k(k_vel_rhs<V>, grid(M.nNodes), 256, 0, s_, M.nNodes, M.dofX, M.dofY, M.upIa, M.upPos, M.upCol,
+                                                  vals, r, z, (V *)M.bx, (V *)M.by, skip);
   }
   // The component solves run unconditionally; when `skip` is set their
   // output is discarded by the skipped scatter below.
   M.solveK<V>((const V *)M.bx, (V *)M.zx, s_);
   if(M.kind == 4) M.solveK<V>((const V *)M.by, (V *)M.zy, s_);
-  (k_vel_out<V><<<grid(M.nNodes), 256, 0, s_>>>(M.nNodes, M.dofX, M.kind == 4 ? M.dofY : nullptr,
-                                                (const V *)M.zx, (const V *)M.zy, M.consts, z, skip), ::feng::count_launch());
+  ::feng::launch_k(k_vel_out<V>, grid(M.nNodes), 256, 0, s_, M.nNodes, M.dofX, M.kind == 4 ? M.dofY : nullptr,
+                                                (const V *)M.zx, (const V *)M.zy, M.consts, z, skip);
 }
 
 template void Krylov::apply_mg<double>(const double *, const double *, double *, const int *);

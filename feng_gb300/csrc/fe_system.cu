@@ -1612,12 +1612,30 @@ int SystemCUDA::computeSolDot()
 
 int SystemCUDA::benchPhase(int which, int reps, size_t flushBytes, double *avgMs)
 {
-  if(which == 7 || which == 8 || which == 10) {
-    // the Gram-Schmidt passes of phases 5, 6 and 9 back to back over a
-    // working set larger than the L2 (see Krylov::gsStepStream)
+  if(which == 7 || which == 8) {
+    // the Gram-Schmidt passes of phases 5 and 6 back to back over a working
+    // set larger than the L2 (see Krylov::gsStepStream)
     FE_TRY(ensureMatrixZeroed());
-    return kry_.gsStepStream(which == 7 ? 0 : which == 8 ? 4 : 6, std::max(1, kry_.opt.restart / 2),
-                             std::max(reps, 1) * 10, avgMs);
+    return kry_.gsStepStream(which == 7 ? 0 : 4, std::max(1, kry_.opt.restart / 2), std::max(reps, 1) * 10, avgMs);
+  }
+  if(which == 11 || which == 12) {
+    // in-graph timings: the preconditioner application (11) and one Arnoldi
+    // step of a full restart cycle (12), see Krylov::precondGraph / cycleGraph
+    if(reps < 1) {
+      set_error("invalid benchmark request");
+      return FE_INVALID_ARG;
+    }
+    FE_TRY(ensureMatrixZeroed());
+    FE_TRY(factorIfPending());
+    if(which == 11) return kry_.precondGraph(std::max(reps, 1) * 5, avgMs);
+    double *x = nullptr;
+    CK(cudaMalloc(&x, sizeof(double) * nInc_));
+    CK(cudaMemsetAsync(x, 0, sizeof(double) * nInc_, s_));
+    const bool mixed = kry_.opt.mixed != 0;
+    const int st = kry_.cycleGraph(mixed, mixed ? (const void *)vals32_ : (const void *)vals64_, rhs_, x,
+                                   std::max(1, reps / 5), avgMs);
+    cudaFree(x);
+    return st;
   }
   if(which < 0 || which > 9 || which == 7 || which == 8 || reps < 1) {
     set_error("invalid benchmark request");

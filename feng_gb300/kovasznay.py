@@ -80,7 +80,9 @@ def main(argv=None):
     ap.add_argument("--phases", default="",
                     help="after the solves, time these benchmark phases (comma list of fe_cuda_bench_phase "
                          "numbers: 0 residual, 1 Jacobian, 2 SpMV, 3 preconditioner, 4 finest smoother pass, "
-                         "5 Gram-Schmidt dots, 6 Gram-Schmidt update, 7 and 8 the same two streamed back to back)")
+                         "5 Gram-Schmidt dots, 6 Gram-Schmidt update, 7 and 8 the same two streamed back to back, "
+                         "9 the dot pass of 5 by column groups, 11 the preconditioner in a CUDA graph, "
+                         "12 one Arnoldi step of a restart cycle replayed from its graph)")
     ap.add_argument("--phase-reps", type=int, default=20)
     ap.add_argument("--errors", action="store_true",
                     help="after the solves, L2 errors of velocity and pressure against the exact Kovasznay flow "
@@ -133,7 +135,7 @@ def main(argv=None):
         ms = C.c_double()
         check(lib.fe_cuda_bench_phase(sys_._h, w, args.phase_reps, 256 << 20, C.byref(ms)))
         ph = {"us": ms.value * 1e3}
-        if w >= 4:
+        if 4 <= w <= 9:
             by = C.c_int64()
             check(lib.fe_cuda_phase_bytes(sys_._h, w, C.byref(by)))
             ph["bytes"] = by.value

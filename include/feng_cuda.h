@@ -398,11 +398,16 @@ int fe_cuda_reset_times(fe_cuda_system *s);
  * no flush between them, cycling through copies of the basis that together
  * exceed three times the L2 (the mean time of a pass inside the Arnoldi
  * loop, where the launches follow one another; flush_bytes unused);
- * 9 the bulk-copy dot pass (the first Gram-Schmidt pass of the mixed FGMRES
- * on large systems: k_gs_dots_bulk, per-block partials that the update pass
- * sums) over restart/2 basis vectors, 10 the same streamed as 7.
- * Phases 5 to 10 need a mixed-precision system that has solved once (9 and
- * 10 one large enough for the bulk pass).  Uses the current solution state. */
+ * 9 the dot pass of 5 by the column-group kernel (k_gs_dots; phase 5 runs
+ * k_gs_dots_all, one pass over w and every column);
+ * 11 the preconditioner application of an Arnoldi step, 5 * reps of them
+ * captured in one CUDA graph and replayed back to back (flush_bytes unused);
+ * 12 one Arnoldi step of a full FGMRES restart cycle replayed from its CUDA
+ * graph with the convergence test disabled (reps / 5 cycles, at least one;
+ * the cycle's restart residual and solution update included; flush_bytes
+ * unused).
+ * Phases 5 to 9 need a mixed-precision system that has solved once, 11 and 12 a system that has solved
+ * once (12: FGMRES).  Uses the current solution state. */
 int fe_cuda_bench_phase(fe_cuda_system *s, int which, int reps, int64_t flush_bytes, double *avg_ms);
 /* Algorithmic bytes of one run of phase 4 (finest multigrid operator read
  * once, each vector entry read or written once). */
