@@ -298,6 +298,45 @@ __global__ void __launch_bounds__(256) k_cheb_post(int64_t n, const int32_t *__r
   }
 }
 
+// Walks the len entries of row lane of a sliced-ELL slice (entry k at
+// base + 32 k + lane) in order, calling f(column, value) for each, in steps
+// of UNR entries, software-pipelined: the next step's columns and values are
+// loaded before this step's gathers, so a step waits for one memory latency
+// instead of two.
+template <int UNR, typename V, typename F>
+__device__ __forceinline__ void sell_walk(int32_t base, int32_t len, int lane, const int32_t *__restrict__ sc,
+                                          const V *__restrict__ sv, F &&f)
+{
+  int32_t c[UNR];
+  V a[UNR];
+#pragma unroll
+  for(int u = 0; u < UNR; ++u) {
+    const bool ok = u < len;
+    const int32_t e = base + (u << 5) + lane;
+    c[u] = ok ? __ldcs(sc + e) : -1;
+    a[u] = ok ? __ldcs(sv + e) : (V)0;
+  }
+  for(int32_t k = 0; k < len; k += UNR) {
+    int32_t cn[UNR];
+    V an[UNR];
+#pragma unroll
+    for(int u = 0; u < UNR; ++u) {
+      const bool ok = k + UNR + u < len;
+      const int32_t e = base + ((k + UNR + u) << 5) + lane;
+      cn[u] = ok ? __ldcs(sc + e) : -1;
+      an[u] = ok ? __ldcs(sv + e) : (V)0;
+    }
+#pragma unroll
+    for(int u = 0; u < UNR; ++u)
+      if(c[u] >= 0) f(c[u], a[u]);
+#pragma unroll
+    for(int u = 0; u < UNR; ++u) {
+      c[u] = cn[u];
+      a[u] = an[u];
+    }
+  }
+}
+
 // k_cheb_first on the sliced-ELL copy of A: thread = row, both components.
 template <typename V, int NV>
 __global__ void __launch_bounds__(256) k_cheb_first_sell(int64_t n, const int32_t *__restrict__ sp,
@@ -316,15 +355,12 @@ __global__ void __launch_bounds__(256) k_cheb_first_sell(int64_t n, const int32_
   V acc[NV];
 #pragma unroll
   for(int c = 0; c < NV; ++c) acc[c] = 0;
-#pragma unroll 4
-  for(int32_t k = 0; k < len; ++k) {
-    const int32_t e = base + (k << 5) + lane;
-    const int32_t j = __ldcs(sc + e);
-    const V ak = __ldcs(sv + e) * dinv[j];
+  sell_walk<8, V>(base, len, lane, sc, sv, [&](int32_t j, V a) {
+    const V ak = a * dinv[j];
     const Vals<V, NV> bv = ldv<V, NV>(b, j);
 #pragma unroll
     for(int c = 0; c < NV; ++c) acc[c] += ak * bv.v[c];
-  }
+  });
   const V dv = dinv[row];
 #pragma unroll
   for(int c = 0; c < NV; ++c) {
@@ -358,15 +394,11 @@ __global__ void __launch_bounds__(256) k_cheb_post_sell(int64_t n, const int32_t
   V acc[NV];
 #pragma unroll
   for(int c = 0; c < NV; ++c) acc[c] = 0;
-#pragma unroll 4
-  for(int32_t k = 0; k < len; ++k) {
-    const int32_t e = base + (k << 5) + lane;
-    const int32_t j = __ldcs(sc + e);
-    const V ak = __ldcs(sv + e);
+  sell_walk<8, V>(base, len, lane, sc, sv, [&](int32_t j, V ak) {
     const Vals<V, NV> yv = ldv<V, NV>(y, j);
 #pragma unroll
     for(int c = 0; c < NV; ++c) acc[c] += ak * yv.v[c];
-  }
+  });
   const V dv = dinv[row];
 #pragma unroll
   for(int c = 0; c < NV; ++c) {
@@ -395,14 +427,11 @@ __global__ void __launch_bounds__(256) k_prolong_sell(int64_t n, const int32_t *
   V acc[NV];
 #pragma unroll
   for(int c = 0; c < NV; ++c) acc[c] = 0;
-#pragma unroll 4
-  for(int32_t k = 0; k < len; ++k) {
-    const int32_t e = base + (k << 5) + lane;
-    const V a = __ldcs(sv + e);
-    const Vals<V, NV> xv = ldv<V, NV>(xc, __ldcs(sc + e));
+  sell_walk<8, V>(base, len, lane, sc, sv, [&](int32_t j, V a) {
+    const Vals<V, NV> xv = ldv<V, NV>(xc, j);
 #pragma unroll
     for(int c = 0; c < NV; ++c) acc[c] += a * xv.v[c];
-  }
+  });
 #pragma unroll
   for(int c = 0; c < NV; ++c) y[row * NV + c] = b[row * NV + c] + acc[c];
 }

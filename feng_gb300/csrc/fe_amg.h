@@ -41,7 +41,12 @@ struct AMGParams {
   int maxLevels = 12;
   int64_t coarseSize = 1200;
   int chebyDegree = 2;
-  double chebyLow = 0.15;  // smoothing interval [low, high] * lmax
+  // smoothing interval [low, high] * lmax; degree 1 is damped Jacobi with
+  // weight 1 / theta, theta = (low + high) / 2 * lmax = 0.7 lmax: measured on
+  // the 256 x 256 Kovasznay system (FGMRES iterations per solve for theta /
+  // lmax = 0.525 / 0.6 / 0.675 / 0.7 / 0.775: diverged / 574 / 553 / 555 /
+  // 555), the flat side of the optimum, away from the divergence
+  double chebyLow = 0.35;
   double chebyHigh = 1.05;
 };
 

@@ -147,7 +147,9 @@ class Krylov {
   double *V_ = nullptr;   // (m+1) x n  Krylov basis, FP64
   double *Z_ = nullptr;   // m x n      preconditioned directions (FP64 path)
   float *Z32_ = nullptr;  // m x n      preconditioned directions (mixed path)
-  float *V32_ = nullptr;  // (m+1) x n  Krylov basis of the mixed path, FP32
+  float *V32_ = nullptr;  // (m+1) x n  Krylov basis of the mixed path, FP32, in row blocks of 1024
+                          // rows (column c of row block k at (k (m+1) + c) 1024)
+  float *vc32_ = nullptr;  // the newest basis vector, contiguous (the preconditioner's input)
   // Sliced-ELL copy of the FP32 matrix for the Arnoldi SpMV of the mixed
   // path (slices of 32 rows padded to the longest row, entries column-major
   // in the slice; padding: the row's own column, value 0), refreshed from the
@@ -160,7 +162,7 @@ class Krylov {
   int *zeroFlag_ = nullptr;  // a device 0 ("not done") for gsStep
   int gsParts_ = 0;       // blocks of the FP32 Gram-Schmidt update passes
   int nSM_ = 1;           // multiprocessors of the device
-  int64_t ld32_ = 0;      // leading dimension of V32_ / Z32_ (multiple of 64)
+  int64_t ld32_ = 0;      // rows of V32_ / Z32_ / w32_ (n rounded up to whole row blocks of V32_)
   // pass: 0 first pass (the update + norm decides on reorthogonalisation),
   // 1 the conditional second pass, 2 the last pass of an unconditional CGS2
   void gs32(int mode, int ncols, const double *hprev, double *hcur, double *Hcol, const int *done, int pass);
@@ -220,6 +222,7 @@ class Krylov {
   // The Arnoldi SpMV of the mixed path on the current FP32 matrix (sliced
   // ELL when built, else CSR), FP32 vectors (benchmark phase).
   int spmvHot();
+  void spmv_sell(const float *x, float *y, const int *done);
   // The preconditioner application of an Arnoldi step (the mixed path: the
   // FP32 basis column 0 into Z column 0; FP64 otherwise), reps of them
   // captured in one CUDA graph and replayed (after a warm replay) without

@@ -14,7 +14,7 @@
  *     Jacobi smoothing step (omega = 4 / (3 rho(D^-1 A))), Galerkin coarse
  *     operators, dense inverse of the coarsest level;
  *   - V-cycles with one degree-1 Chebyshev (weighted Jacobi) sweep before and
- *     after the coarse correction, weight 1 / (0.6 rho);
+ *     after the coarse correction, weight 1 / (0.7 rho);
  *   - the block upper-triangular preconditioner of Elman, Silvester and
  *     Wathen (Finite Elements and Fast Iterative Solvers, 2nd ed., ch. 9):
  *     z_p = S^-1 r_p with S^-1 ~ -(s / (1.5 sigma c_div)) M_p^-1 (lumped
@@ -346,7 +346,7 @@ static void vcycle(fo_mg *M, int l, const double *b, double *x, int nv)
       }
     return;
   }
-  const double it = 1.0 / (0.6 * M->lmax[l]);
+  const double it = 1.0 / (0.7 * M->lmax[l]);
   const double *dinv = M->dinv[l];
   double *res = M->t[l];
   /* pre-smoothing from zero, then the residual b - A x */
