@@ -498,7 +498,9 @@ def c5_leg(n=64, reps=5, steps=50, steps_fp64=10):
             summ = cavity.summarize(stats, 3)
             summ.update(steps_run=nsteps, wall_s_with_setup=wall, step_ms_total=sum(x["step_ms"] for x in stats),
                         newton_iterations_total=sum(x["newton_iterations"] for x in stats),
-                        krylov_iterations_total=sum(x["krylov_iterations"] for x in stats))
+                        krylov_iterations_total=sum(x["krylov_iterations"] for x in stats),
+                        # device time of the phases over all steps (CUDA events around each call)
+                        phase_ms_total=sys_.times())
             out[f"bdf2_{prec}"] = summ
             del sys_
         except Exception as e:  # recorded, so that the rest of the benchmark line still prints

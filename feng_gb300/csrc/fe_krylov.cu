@@ -878,8 +878,8 @@ __global__ void __launch_bounds__(RB, 4) k_gs_upd(int64_t n4, int m1, float *__r
 // v = w * (1 / ||w||) in FP32, 4 rows per thread; the scale comes from the
 // last update + norm pass (k_gs_upd<., true> or k_gs32<., 2>).
 // gated: only after a second Gram-Schmidt pass (otherwise k_gs_upd wrote v).
-// gs (ungated only): after its share of the scaling, warp 0 of block 0
-// applies the Givens rotations of step j (k_givens folded in; a block that
+// gs (ungated only): the last block does not scale; its warp 0 applies the
+// Givens rotations of step j meanwhile (k_givens folded in; a block that
 // starts after the step converged skips its share of v, which the cycle no
 // longer reads).
 // The result goes to column col of the row-blocked basis V and to its
@@ -891,11 +891,16 @@ __global__ void k_scale32(int64_t n4, const float *__restrict__ w, float *__rest
   FE_PDL_ENTRY();
   __shared__ double sh[MAXM + 1], scs[MAXM], ssn[MAXM];
   if(*done || (gated && !st->reorth)) return;
+  if(gs && blockIdx.x == gridDim.x - 1) {
+    if(threadIdx.x < 32) givens_warp(gs, j, threadIdx.x, sh, scs, ssn);
+    return;
+  }
+  const int nb = gs ? (int)gridDim.x - 1 : (int)gridDim.x;
   const float inv = st->finv;
   const float4 *w4 = reinterpret_cast<const float4 *>(w);
   float4 *V4 = reinterpret_cast<float4 *>(V);
   float4 *c4 = reinterpret_cast<float4 *>(vcopy);
-  for(int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n4; g += (int64_t)gridDim.x * blockDim.x) {
+  for(int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n4; g += (int64_t)nb * blockDim.x) {
     float4 t = w4[g];
     t.x *= inv;
     t.y *= inv;
@@ -904,7 +909,6 @@ __global__ void k_scale32(int64_t n4, const float *__restrict__ w, float *__rest
     V4[vidx4(g, col, m1)] = t;
     c4[g] = t;
   }
-  if(gs && blockIdx.x == 0 && threadIdx.x < 32) givens_warp(gs, j, threadIdx.x, sh, scs, ssn);
 }
 
 // V_0 = r / ||r|| rounded to FP32 (start of a mixed cycle; column 0 of the
@@ -2050,7 +2054,7 @@ void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, i
                        (GmresState *)nullptr, 0);
       ::feng::launch_k(k_givens, 1, 32, 0, s_, w.gs, j);
     } else {
-      ::feng::launch_k(k_scale32, g4, 256, 0, s_, ld32_ / 4, w32_, V32_, m1, j + 1, vc32_, w.st, &w.gs->done, 0,
+      ::feng::launch_k(k_scale32, g4 + 1, 256, 0, s_, ld32_ / 4, w32_, V32_, m1, j + 1, vc32_, w.st, &w.gs->done, 0,
                        w.gs, j);
     }
     if(poll && poll_done(&w.gs->done, j)) break;

@@ -77,10 +77,10 @@ def main(argv=None):
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--summary-from", type=int, default=3)
     args = ap.parse_args(argv)
-    _, stats = run(args.n, args.re, args.dt, args.steps, args.guess, args.precision)
+    sys_, stats = run(args.n, args.re, args.dt, args.steps, args.guess, args.precision)
     print(json.dumps({"case": f"cube_re{args.re:g}_{args.n}^3_dt{args.dt:g}", "guess": args.guess,
                       "precision": args.precision, "summary": summarize(stats, args.summary_from),
-                      "steps": stats}))
+                      "phase_ms_total": sys_.times(), "steps": stats}))
 
 
 if __name__ == "__main__":
