@@ -48,6 +48,11 @@ struct AMGParams {
   // 555), the flat side of the optimum, away from the divergence
   double chebyLow = 0.35;
   double chebyHigh = 1.05;
+  // levels whose operator averages more entries per row take the tentative
+  // prolongator unsmoothed (smoothing it multiplies the stencil of the next
+  // Galerkin operator: 189 -> 2,427 entries per row on the 32^3 cube's
+  // shifted velocity operator; two-dimensional P2 hierarchies stay below 48)
+  double smoothMaxRow = 64.0;
 };
 
 int amg_build(const HostCSR &A, const AMGParams &p, AMGHierarchy &H);

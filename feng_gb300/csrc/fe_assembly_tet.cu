@@ -28,6 +28,7 @@
 
 #include "fe_common.h"
 #include "fe_device.h"
+#include "fe_df.h"
 #include "fe_mesh3d.h"
 #include "fe_setup.h"
 
@@ -210,6 +211,189 @@ __global__ void __launch_bounds__(EPB *TPB) k_residual_tet(DeviceMesh dm, FormCo
         acc += sU[(3 * b + n) * EPB + lane] * (G[0][n] * Tt.d(0, j, b) + G[1][n] * Tt.d(1, j, b) + G[2][n] * Tt.d(2, j, b));
     const int32_t d = dm.adr[(int64_t)(30 + j) * nE + p];
     if(d < nInc) atomicAdd(rhs + d, -fc.divu * J * acc);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Residual of the Taylor-Hood forms in double-float (the mixed path): the
+// FP64 kernel's integrals evaluated at the form's own quadrature nodes --
+// the same nodes and weights the reference tensors are built from, so the
+// same sums regrouped -- with every product and sum in float pairs on the
+// FP32 pipes (the FP64 pipe of this part is ~64x slower).  Block: 32
+// elements x 14 warps.  Nodes q = warp, warp + 14, ...: u, grad u, u-dot and
+// p at the node, then the node's integrand coefficients (of phi_a, of the
+// three reference derivatives of phi_a, of psi_j) in shared memory; then
+// warp a < 10 forms the three velocity rows of P2 function a, warps 10-13
+// the four pressure rows.  The source (non-polynomial) and the scatter are
+// FP64, as in the FP64 kernel.  Inputs are float pairs: u, u-dot, geometry.
+constexpr int DFW = 14;   // warps per block
+constexpr int DFQ = 13;   // coefficients per node: f_m (3), F'_(r,m) (9), div (1)
+
+size_t residual_df_smem(int nq)
+{
+  return sizeof(dfl) * (30 + 30 + 4 + 10 + (size_t)nq * DFQ) * EPB + sizeof(double) * (size_t)nq * EPB +
+         sizeof(int32_t) * 34 * EPB;
+}
+
+__global__ void __launch_bounds__(EPB *DFW) k_residual_tet_df(DeviceMesh dm, FormCoeffs fc,
+                                                              const RefTensorsTet *__restrict__ gT,
+                                                              const float2 *__restrict__ up,
+                                                              const float2 *__restrict__ udp, int64_t nInc,
+                                                              double *__restrict__ rhs, int64_t begin, int64_t end)
+{
+  extern __shared__ __align__(16) unsigned char dfsmem[];
+  const int nq = gT->nq;
+  dfl *sU = reinterpret_cast<dfl *>(dfsmem);  // [30][EPB]
+  dfl *sUd = sU + 30 * EPB;                    // [30][EPB]
+  dfl *sP = sUd + 30 * EPB;                    // [4][EPB]
+  dfl *sG = sP + 4 * EPB;                      // [10][EPB]
+  dfl *sQ = sG + 10 * EPB;                     // [nq][DFQ][EPB]
+  double *sF = reinterpret_cast<double *>(sQ + (size_t)nq * DFQ * EPB);  // [nq][EPB]
+  int32_t *sA = reinterpret_cast<int32_t *>(sF + (size_t)nq * EPB);      // [34][EPB]
+  const int lane = threadIdx.x, w = threadIdx.y;
+  const int64_t p = begin + (int64_t)blockIdx.x * EPB + lane;
+  const bool live = p < end;
+  const int64_t nE = dm.nElm;
+  const bool src = fc.srcKind == SRC_SIN3_BODY;
+  if(live) {
+    for(int i = w; i < 34; i += DFW) {
+      const int32_t d = dm.adr[(int64_t)i * nE + p];
+      sA[i * EPB + lane] = d;
+      const float2 v = up[d];
+      if(i < 30) {
+        sU[i * EPB + lane] = {v.x, v.y};
+        if(fc.hasMass) {
+          const float2 t = udp[d];
+          sUd[i * EPB + lane] = {t.x, t.y};
+        } else {
+          sUd[i * EPB + lane] = df_zero();
+        }
+      } else {
+        sP[(i - 30) * EPB + lane] = {v.x, v.y};
+      }
+    }
+    if(w < 10) {
+      const float2 g = dm.geoPair[(int64_t)w * nE + p];
+      sG[w * EPB + lane] = {g.x, g.y};
+    }
+    if(src) {
+      double X[4][3];
+      for(int v = 0; v < 4; ++v)
+        for(int k = 0; k < 3; ++k) X[v][k] = dm.xy[(int64_t)(3 * v + k) * nE + p];
+      for(int q = w; q < nq; q += DFW) {
+        const double r = gT->qr[q], s = gT->qs[q], t = gT->qt[q], l0 = 1. - r - s - t;
+        double x[3];
+        for(int k = 0; k < 3; ++k) x[k] = l0 * X[0][k] + r * X[1][k] + s * X[2][k] + t * X[3][k];
+        sF[q * EPB + lane] = source_x(fc.srcKind, fc.srcParam, x[0], x[1], x[2]);
+      }
+    }
+  }
+  __syncthreads();
+  if(live) {
+    dfl G[3][3];
+    for(int r = 0; r < 3; ++r)
+      for(int k = 0; k < 3; ++k) G[r][k] = sG[(3 * r + k) * EPB + lane];
+    const dfl J = sG[9 * EPB + lane];
+    const dfl conv = {fc.pair[0][0], fc.pair[0][1]}, mass = {fc.pair[1][0], fc.pair[1][1]},
+              sig = {fc.pair[2][0], fc.pair[2][1]}, mu = {fc.pair[3][0], fc.pair[3][1]},
+              divu = {fc.pair[4][0], fc.pair[4][1]};
+    for(int q = w; q < nq; q += DFW) {
+      dfl uq[3], ur[3][3], udq[3];  // ur[r][m] = d u_m / d r_r
+      for(int m = 0; m < 3; ++m) {
+        uq[m] = df_zero();
+        udq[m] = df_zero();
+        for(int r = 0; r < 3; ++r) ur[r][m] = df_zero();
+      }
+      for(int b = 0; b < 10; ++b) {
+        const dfl ph = {gT->phih[q][b], gT->phil[q][b]};
+        const dfl dr[3] = {{gT->dphih[q][0][b], gT->dphil[q][0][b]},
+                           {gT->dphih[q][1][b], gT->dphil[q][1][b]},
+                           {gT->dphih[q][2][b], gT->dphil[q][2][b]}};
+        for(int m = 0; m < 3; ++m) {
+          const dfl v = sU[(3 * b + m) * EPB + lane];
+          uq[m] = df_fma(ph, v, uq[m]);
+          for(int r = 0; r < 3; ++r) ur[r][m] = df_fma(dr[r], v, ur[r][m]);
+          if(fc.hasMass) udq[m] = df_fma(ph, sUd[(3 * b + m) * EPB + lane], udq[m]);
+        }
+      }
+      dfl gu[3][3];  // gu[k][m] = d_k u_m = sum_r G[r][k] d u_m / d r_r
+      for(int k = 0; k < 3; ++k)
+        for(int m = 0; m < 3; ++m)
+          gu[k][m] = df_add(df_add(df_mul(G[0][k], ur[0][m]), df_mul(G[1][k], ur[1][m])), df_mul(G[2][k], ur[2][m]));
+      dfl pq = df_zero();
+      for(int j = 0; j < 4; ++j) pq = df_fma({gT->psih[q][j], gT->psil[q][j]}, sP[j * EPB + lane], pq);
+      const dfl wJ = df_mul({gT->qwh[q], gT->qwl[q]}, J);
+      dfl *Q = sQ + (size_t)q * DFQ * EPB + lane;
+      for(int m = 0; m < 3; ++m) {
+        dfl f = df_zero();
+        if(fc.hasConv)
+          f = df_sub(f, df_mul(conv, df_add(df_add(df_mul(uq[0], gu[0][m]), df_mul(uq[1], gu[1][m])),
+                                            df_mul(uq[2], gu[2][m]))));
+        if(fc.hasMass) f = df_sub(f, df_mul(mass, udq[m]));
+        Q[m * EPB] = df_mul(wJ, f);
+      }
+      // coefficient of d_k phi_a in component m, then of the reference
+      // derivatives: F'[r][m] = sum_k G[r][k] Fg[k][m]
+      dfl Fg[3][3];
+      for(int k = 0; k < 3; ++k)
+        for(int m = 0; m < 3; ++m) Fg[k][m] = df_zero();
+      if(fc.hasSigma) {
+        const dfl sw = df_neg(df_mul(sig, wJ));
+        for(int k = 0; k < 3; ++k)
+          for(int m = 0; m < 3; ++m)
+            Fg[k][m] = df_mul(sw, df_sub(k == m ? pq : df_zero(), df_mul(mu, df_add(gu[k][m], gu[m][k]))));
+      }
+      for(int r = 0; r < 3; ++r)
+        for(int m = 0; m < 3; ++m)
+          Q[(3 + 3 * r + m) * EPB] =
+              df_add(df_add(df_mul(G[r][0], Fg[0][m]), df_mul(G[r][1], Fg[1][m])), df_mul(G[r][2], Fg[2][m]));
+      Q[12 * EPB] = fc.hasDivu ? df_neg(df_mul(df_mul(divu, wJ), df_add(df_add(gu[0][0], gu[1][1]), gu[2][2])))
+                               : df_zero();
+    }
+  }
+  __syncthreads();
+  if(!live) return;
+  if(w >= 10) {
+    // pressure row j = w - 10:  Be_pj -= c int (div u) psi_j
+    if(!fc.hasDivu) return;
+    const int j = w - 10;
+    dfl acc = df_zero();
+    for(int q = 0; q < nq; ++q)
+      acc = df_fma(sQ[((size_t)q * DFQ + 12) * EPB + lane], {gT->psih[q][j], gT->psil[q][j]}, acc);
+    const int32_t d = sA[(30 + j) * EPB + lane];
+    if(d < nInc) atomicAdd(rhs + d, df_to(acc));
+    return;
+  }
+  const int a = w;
+  dfl be[3] = {df_zero(), df_zero(), df_zero()};
+  for(int q = 0; q < nq; ++q) {
+    const dfl *Q = sQ + (size_t)q * DFQ * EPB + lane;
+    const dfl ph = {gT->phih[q][a], gT->phil[q][a]};
+    const dfl dr[3] = {{gT->dphih[q][0][a], gT->dphil[q][0][a]},
+                       {gT->dphih[q][1][a], gT->dphil[q][1][a]},
+                       {gT->dphih[q][2][a], gT->dphil[q][2][a]}};
+    for(int m = 0; m < 3; ++m) {
+      dfl t = df_mul(Q[m * EPB], ph);
+      for(int r = 0; r < 3; ++r) t = df_add(t, df_mul(Q[(3 + 3 * r + m) * EPB], dr[r]));
+      be[m] = df_add(be[m], t);
+    }
+  }
+  double bd[3] = {df_to(be[0]), df_to(be[1]), df_to(be[2])};
+  if(src) {
+    // Be_(a,0) -= f phi_a J w over the form's rule, in FP64
+    const double J = dm.geo[(int64_t)9 * nE + p];
+    double srcA = 0.;
+    for(int q = 0; q < nq; ++q) srcA += gT->phi[q][a] * sF[q * EPB + lane] * gT->qw[q];
+    bd[0] -= fc.srcCoeff * srcA * J;
+  } else if(fc.srcKind == SRC_CONST_VEC) {
+    const double J = dm.geo[(int64_t)9 * nE + p];
+    double ia = 0.;
+    for(int q = 0; q < nq; ++q) ia += gT->phi[q][a] * gT->qw[q];
+    for(int m = 0; m < 3; ++m) bd[m] -= fc.srcCoeff * fc.srcParam[m] * ia * J;
+  }
+  for(int m = 0; m < 3; ++m) {
+    const int32_t d = sA[(3 * a + m) * EPB + lane];
+    if(d < nInc) atomicAdd(rhs + d, bd[m]);
   }
 }
 
@@ -603,6 +787,16 @@ void build_ref_tensors_tet(const QuadRule &q, RefTensorsTet &T)
     }
     T.qw[k] = w; T.qr[k] = r; T.qs[k] = s; T.qt[k] = t;
     for(int a = 0; a < 10; ++a) T.phi[k][a] = phi[a];
+    auto pair = [](double x, float &h, float &lo) {
+      h = (float)x;
+      lo = (float)(x - (double)h);
+    };
+    pair(w, T.qwh[k], T.qwl[k]);
+    for(int a = 0; a < 10; ++a) {
+      pair(phi[a], T.phih[k][a], T.phil[k][a]);
+      for(int d = 0; d < 3; ++d) pair(dphi[a][d], T.dphih[k][d][a], T.dphil[k][d][a]);
+    }
+    for(int j = 0; j < 4; ++j) pair(l[j], T.psih[k][j], T.psil[k][j]);
     for(int rr = 0; rr < 3; ++rr)
       for(int ss = 0; ss < 3; ++ss)
         for(int a = 0; a < 10; ++a)
@@ -631,6 +825,23 @@ void launch_assemble_residual_tet(const DeviceMesh &dm, const FormCoeffs &fc, co
     set = true;
   }
   (k_residual_tet<<<(unsigned)nblk(begin, end), dim3(EPB, TPB), sm, s>>>(dm, fc, dT, u, udot, nInc, rhs, begin, end),
+   ::feng::count_launch());
+}
+
+void launch_assemble_residual_tet_df(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensorsTet *dT, int nq,
+                                     const float2 *up, const float2 *udp, int64_t nInc, double *rhs, int64_t begin,
+                                     int64_t end, cudaStream_t s)
+{
+  if(end <= begin) return;
+  const size_t sm = residual_df_smem(nq);
+  static bool set = false;
+  if(!set) {
+    cudaFuncSetAttribute(k_residual_tet_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)residual_df_smem(TET_DF_MAXQ));
+    set = true;
+  }
+  (k_residual_tet_df<<<(unsigned)nblk(begin, end), dim3(EPB, DFW), sm, s>>>(dm, fc, dT, up, udp, nInc, rhs, begin,
+                                                                            end),
    ::feng::count_launch());
 }
 

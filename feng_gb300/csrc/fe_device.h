@@ -50,7 +50,18 @@ struct RefTensorsTet {
   int nq;
   double qw[TET_MAXQ], qr[TET_MAXQ], qs[TET_MAXQ], qt[TET_MAXQ];
   double phi[TET_MAXQ][10];
+  // The rule as float pairs (hi + lo, lo = the double minus hi) for the
+  // double-float residual: weights, P2 values and reference gradients
+  // (dphi[q][r][a] = d phi_a / d r_r at node q), P1 values.
+  float qwh[TET_MAXQ], qwl[TET_MAXQ];
+  float phih[TET_MAXQ][10], phil[TET_MAXQ][10];
+  float dphih[TET_MAXQ][3][10], dphil[TET_MAXQ][3][10];
+  float psih[TET_MAXQ][4], psil[TET_MAXQ][4];
 };
+// The double-float tetrahedral residual keeps every node's terms in shared
+// memory: rules of up to this many nodes (degree 6; higher degrees use the
+// FP64 kernel).
+constexpr int TET_DF_MAXQ = 24;
 
 // Reference-element tensors of one quadrature rule (all sums over the rule's
 // nodes, weights included):
@@ -109,7 +120,7 @@ struct DeviceMesh {
                              // tetrahedra: [10][nElm] G[3][3] row-major, J
   double *xy = nullptr;      // [6][nElm]     x0 y0 x1 y1 x2 y2 (tetrahedra: [12][nElm] x0 y0 z0 ... z3)
   int32_t *map = nullptr;    // [nloc*nloc][nElm] CSR position or -1
-  float2 *geoPair = nullptr; // [5][nElm] geo as float pairs (double-float residual)
+  float2 *geoPair = nullptr; // [5][nElm] geo as float pairs (double-float residual; tetrahedra [10][nElm])
 };
 
 // Row-owned Jacobian assembly of Taylor-Hood systems: one thread builds one
@@ -210,6 +221,11 @@ void build_ref_tensors_tet(const QuadRule &q, RefTensorsTet &T);
 void launch_assemble_residual_tet(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensorsTet *dT,
                                   const double *u, const double *udot, int64_t nInc, double *rhs,
                                   int64_t begin, int64_t end, cudaStream_t s);
+// The Taylor-Hood residual in double-float from float pairs of u, u-dot and
+// the geometry (dm.geoPair), rules of at most TET_DF_MAXQ nodes (nq).
+void launch_assemble_residual_tet_df(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensorsTet *dT, int nq,
+                                     const float2 *up, const float2 *udp, int64_t nInc, double *rhs, int64_t begin,
+                                     int64_t end, cudaStream_t s);
 void launch_assemble_matrix_tet_f64(const DeviceMesh &dm, const FormCoeffs &fc, const RefTensorsTet *dT,
                                     const double *u, double c0, double *values, int64_t begin, int64_t end,
                                     cudaStream_t s);

@@ -438,7 +438,10 @@ int SystemCUDA::init(const SystemTables &t, const FormDesc *forms, int nforms,
   CK(cudaMemcpy(dm_.geo, geo.data(), sizeof(double) * geo.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(dm_.xy, xy.data(), sizeof(double) * xy.size(), cudaMemcpyHostToDevice));
   if(t.elemType == ELEM_TAYLOR_HOOD) FE_TRY(build_row_assembly(adrP, map));
-  if(t.elemType == ELEM_TAYLOR_HOOD && opt.precision == 1) {
+  // the double-float residual of the mixed path: triangles, and tetrahedra
+  // with rules of at most TET_DF_MAXQ nodes
+  const bool dfTet = t.elemType == ELEM_TET_TAYLOR_HOOD && opt.precision == 1 && t.quad.n() <= TET_DF_MAXQ;
+  if((t.elemType == ELEM_TAYLOR_HOOD && opt.precision == 1) || dfTet) {
     // geometry as float pairs for the double-float residual
     std::vector<float2> gp(geo.size());
     for(size_t i = 0; i < geo.size(); ++i) {
@@ -1281,6 +1284,14 @@ int SystemCUDA::setResidualToZero()
 void SystemCUDA::launch_residual(double *out)
 {
   if(tet()) {
+    if(dfResidual()) {
+      launch_split_pairs(nDofs_, u_, uPair_, s_);
+      if(fc_.hasMass) launch_split_pairs(nDofs_, udot_, udotPair_, s_);
+      for(int c = 0; c < dm_.nColors; ++c)
+        launch_assemble_residual_tet_df(dm_, fc_, dTt_, nq_, uPair_, udotPair_, nInc_, out, dm_.colorOff[c],
+                                        dm_.colorOff[c + 1], s_);
+      return;
+    }
     for(int c = 0; c < dm_.nColors; ++c)
       launch_assemble_residual_tet(dm_, fc_, dTt_, u_, udot_, nInc_, out, dm_.colorOff[c], dm_.colorOff[c + 1], s_);
     return;

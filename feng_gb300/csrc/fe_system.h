@@ -180,7 +180,9 @@ class SystemCUDA {
   int ensureMatrixZeroed() const;
   // The mixed path assembles the Taylor-Hood residual in double-float on
   // the FP32 pipes (FP64-class accuracy, the 7-node rule); otherwise FP64.
-  int dfResidual() const { return dm_.geoPair && exact5_ ? 1 : 0; }
+  // the mixed path's residual in double-float (triangles: rules exact to
+  // degree 5; tetrahedra: Taylor-Hood with rules of at most TET_DF_MAXQ nodes)
+  int dfResidual() const { return dm_.geoPair && (exact5_ || tet()) ? 1 : 0; }
   void launch_residual(double *out);  // the residual launches of assembleResiduals
   float2 *uPair_ = nullptr, *udotPair_ = nullptr;
   int launch_matrix();  // the Jacobian launches of assembleMatrices
