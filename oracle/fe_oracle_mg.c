@@ -10,9 +10,11 @@
  * restates, from the published methods, the one the device path uses:
  *   - smoothed aggregation (Vanek, Mandel, Brezina, Computing 56, 1996):
  *     strength |a_ij| >= theta sqrt(|a_ii a_jj|), greedy three-pass
- *     aggregation, tentative prolongator with unit-norm columns, one damped
- *     Jacobi smoothing step (omega = 4 / (3 rho(D^-1 A))), Galerkin coarse
- *     operators, dense inverse of the coarsest level;
+ *     aggregation (the threshold halved while fewer than half of the rows
+ *     aggregate), tentative prolongator with unit-norm columns, one damped
+ *     Jacobi smoothing step (omega = 4 / (3 rho(D^-1 A))) except on levels
+ *     denser than 64 entries per row (plain aggregation there), Galerkin
+ *     coarse operators, dense inverse of the coarsest level;
  *   - V-cycles with one degree-1 Chebyshev (weighted Jacobi) sweep before and
  *     after the coarse correction, weight 1 / (0.7 rho);
  *   - the block upper-triangular preconditioner of Elman, Silvester and
@@ -236,7 +238,13 @@ fo_mg *fo_mg_create(int64_t n, const int64_t *ia, const int32_t *ja, const doubl
     M->t[lev] = calloc(2 * A.n, sizeof(double));
     if(A.n <= coarse_size || lev == MG_MAX_LEVELS - 1) break;
     int32_t *agg = malloc(sizeof(int32_t) * A.n);
-    const int64_t na = aggregate(&A, theta, agg);
+    /* the threshold is halved while fewer than half of the rows aggregate */
+    double th = theta;
+    int64_t na = aggregate(&A, th, agg);
+    for(int k = 0; k < 8 && 2 * na > A.n; ++k) {
+      th *= 0.5;
+      na = aggregate(&A, th, agg);
+    }
     if(na >= A.n || na == 0) { free(agg); break; }
     int64_t *size = calloc(na, sizeof(int64_t));
     for(int64_t i = 0; i < A.n; ++i) size[agg[i]]++;
@@ -250,6 +258,15 @@ fo_mg *fo_mg_create(int64_t n, const int64_t *ia, const int32_t *ja, const doubl
     T.ia[A.n] = A.n;
     free(size);
     free(agg);
+    if(A.ia[A.n] > 64 * A.n) {
+      /* plain aggregation on levels denser than 64 entries per row: P = T */
+      M->P[lev] = T;
+      M->R[lev] = transpose(&T);
+      csr_t AP0 = spgemm(&A, &T);
+      A = spgemm(&M->R[lev], &AP0);
+      csr_free(&AP0);
+      continue;
+    }
     /* P = (I - omega D^-1 A) T */
     const double omega = 4.0 / (3.0 * M->lmax[lev]);
     csr_t AT = spgemm(&A, &T);
