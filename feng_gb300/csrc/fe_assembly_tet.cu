@@ -235,7 +235,7 @@ size_t residual_df_smem(int nq)
          sizeof(int32_t) * 34 * EPB;
 }
 
-__global__ void __launch_bounds__(EPB *DFW) k_residual_tet_df(DeviceMesh dm, FormCoeffs fc,
+__global__ void __launch_bounds__(EPB *DFW, 2) k_residual_tet_df(DeviceMesh dm, FormCoeffs fc,
                                                               const RefTensorsTet *__restrict__ gT,
                                                               const float2 *__restrict__ up,
                                                               const float2 *__restrict__ udp, int64_t nInc,

@@ -1553,6 +1553,53 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int64_t n, const int32_t *__r
   y[row] = acc;
 }
 
+// r = b - A x on the sliced-ELL copy of the FP32 matrix with FP64 x and
+// FP64 accumulation (the mixed FGMRES's restart residual: iterative
+// refinement), thread = row, the pipelined walk of k_spmv_sell.
+template <int UNR>
+__global__ void __launch_bounds__(256) k_resid_sell(int64_t n, const int32_t *__restrict__ sp,
+                                                    const int32_t *__restrict__ sc, const float *__restrict__ sv,
+                                                    const double *__restrict__ x, const double *__restrict__ b,
+                                                    double *__restrict__ y)
+{
+  FE_PDL_ENTRY();
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if(row >= n) return;
+  const int64_t sl = row >> 5;
+  const int lane = (int)(row & 31);
+  const int32_t base = sp[sl], len = (sp[sl + 1] - base) >> 5;
+  double acc = 0.;
+  int32_t c[UNR];
+  float a[UNR];
+#pragma unroll
+  for(int u = 0; u < UNR; ++u) {
+    const bool ok = u < len;
+    const int32_t e = base + (u << 5) + lane;
+    c[u] = ok ? __ldcs(sc + e) : -1;
+    a[u] = ok ? __ldcs(sv + e) : 0.f;
+  }
+  for(int32_t k = 0; k < len; k += UNR) {
+    int32_t cn[UNR];
+    float an[UNR];
+#pragma unroll
+    for(int u = 0; u < UNR; ++u) {
+      const bool ok = k + UNR + u < len;
+      const int32_t e = base + ((k + UNR + u) << 5) + lane;
+      cn[u] = ok ? __ldcs(sc + e) : -1;
+      an[u] = ok ? __ldcs(sv + e) : 0.f;
+    }
+#pragma unroll
+    for(int u = 0; u < UNR; ++u)
+      if(c[u] >= 0) acc = fma((double)a[u], x[c[u]], acc);
+#pragma unroll
+    for(int u = 0; u < UNR; ++u) {
+      c[u] = cn[u];
+      a[u] = an[u];
+    }
+  }
+  y[row] = b[row] - acc;
+}
+
 // sliced-ELL values from the CSR values (padding: 0)
 __global__ void k_sell_gather(int64_t m, const int32_t *__restrict__ src, const float *__restrict__ a,
                               float *__restrict__ out)
@@ -1771,6 +1818,17 @@ int Krylov::cycleGraph(bool mixed, const void *vals, const double *b, double *x,
   *htol_ = saved;
   *msPerStep = ms / ((double)reps * m);
   return st;
+}
+
+// r = b - A x for the FP32 matrix with FP64 x and accumulation: the sliced
+// copy when it is built (it holds the same values), else the CSR kernel.
+void Krylov::resid32(const float *vals, const double *x, const double *b, double *r)
+{
+  if(sellVal_)
+    ::feng::launch_k(k_resid_sell<8>, grid_for(n_, 256, 1 << 20), 256, 0, s_, n_, sellPtr_, sellCol_, sellVal_, x, b,
+                     r);
+  else
+    spmv_launch<float, double, double, double, true>(lanes_, n_, A_, vals, x, b, r, nullptr, s_);
 }
 
 void Krylov::spmv_sell(const float *x, float *y, const int *done)
@@ -2006,7 +2064,7 @@ void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, i
 {
   Ws w = Ws_INIT(this);
   const int gv = grid_for(n_, 256, 2048);
-  spmv_launch<float, double, double, double, true>(lanes_, n_, A_, vals, x, b, w_, nullptr, s_);
+  resid32(vals, x, b, w_);
   cudaMemsetAsync(&w.gs->done, 0, sizeof(int), s_);
   cudaMemcpyAsync(&w.gs->tol, htol_, sizeof(double), cudaMemcpyHostToDevice, s_);
   ::feng::launch_k(k_norm_to, nParts_, RB, 0, s_, n_, w_, red_, w.st, &w.gs->done);
@@ -2150,7 +2208,7 @@ int Krylov::solve_fgmres_mixed(const float *vals32, const double *b, double *x, 
     st.iterations = total;
     if(!std::isfinite(hd->est)) { set_error("non-finite residual in mixed FGMRES"); return FE_NONFINITE; }
     // Refinement check on the true residual.
-    spmv_launch<float, double, double, double, true>(lanes_, n_, A_, vals32, x, b, w_, nullptr, s_);
+    resid32(vals32, x, b, w_);
     st.rnorm = norm2(w_);
     if(st.rnorm <= tolAbs) break;
     if(total >= maxIt || hd->k == 0) break;

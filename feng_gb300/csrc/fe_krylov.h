@@ -223,6 +223,7 @@ class Krylov {
   // ELL when built, else CSR), FP32 vectors (benchmark phase).
   int spmvHot();
   void spmv_sell(const float *x, float *y, const int *done);
+  void resid32(const float *vals, const double *x, const double *b, double *r);
   // The preconditioner application of an Arnoldi step (the mixed path: the
   // FP32 basis column 0 into Z column 0; FP64 otherwise), reps of them
   // captured in one CUDA graph and replayed (after a warm replay) without
