@@ -237,7 +237,42 @@ int amg_build(const HostCSR &A0, const AMGParams &p, AMGHierarchy &H)
     }
     // Smoothed prolongator P = (I - omega D^-1 A) T, omega = 4 / (3 rho).
     const double omega = 4.0 / (3.0 * L.lmax);
-    HostCSR AT = spgemm(A, T);
+    // filterSmoothing: the prolongator is smoothed with the filtered operator
+    // (strong couplings kept, the weak ones lumped onto the diagonal), whose
+    // sparser stencil keeps the next level sparse
+    HostCSR AF;
+    if(p.filterSmoothing) {
+      std::vector<double> dg(A.n, 0.);
+      for(int64_t i = 0; i < A.n; ++i)
+        for(int64_t k = A.ia[i]; k < A.ia[i + 1]; ++k)
+          if(A.ja[k] == i) dg[i] = std::fabs(A.a[k]);
+      AF.n = A.n;
+      AF.m = A.m;
+      AF.ia.assign(A.n + 1, 0);
+      for(int64_t i = 0; i < A.n; ++i) {
+        double lump = 0.;
+        int64_t dpos = -1;
+        for(int64_t k = A.ia[i]; k < A.ia[i + 1]; ++k) {
+          const int32_t j = A.ja[k];
+          if(j == i) {
+            dpos = (int64_t)AF.ja.size();
+            AF.ja.push_back(j);
+            AF.a.push_back(A.a[k]);
+          } else if(std::fabs(A.a[k]) >= theta * std::sqrt(dg[i] * dg[j])) {
+            AF.ja.push_back(j);
+            AF.a.push_back(A.a[k]);
+          } else {
+            lump += A.a[k];
+          }
+        }
+        if(dpos >= 0) AF.a[dpos] += lump;
+        AF.ia[i + 1] = (int64_t)AF.ja.size();
+      }
+    }
+    const HostCSR &AS = p.filterSmoothing ? AF : A;
+    const std::vector<double> dinvS = p.filterSmoothing ? inv_diag(AF) : L.dinv;
+    const double omegaS = p.filterSmoothing ? 4.0 / (3.0 * spectral_radius(AF, dinvS)) : omega;
+    HostCSR AT = spgemm(AS, T);
     HostCSR P;
     P.n = A.n;
     P.m = na;
@@ -249,7 +284,7 @@ int amg_build(const HostCSR &A0, const AMGParams &p, AMGHierarchy &H)
       bool placed = false;
       for(int64_t k = AT.ia[i]; k < AT.ia[i + 1]; ++k) {
         const int32_t c = AT.ja[k];
-        double v = -omega * L.dinv[i] * AT.a[k];
+        double v = -omegaS * dinvS[i] * AT.a[k];
         if(!placed && c > tc) {
           P.ja.push_back(tc);
           P.a.push_back(tv);

@@ -752,14 +752,17 @@ int Krylov::setTransientShift(double c0, double mu)
     set_error("transient shift: preconditioner operators missing");
     return FE_INVALID_ARG;
   }
-  // Velocity multigrid on K + (c0 / mu) M (same pattern).
+  // Velocity multigrid on K + (c0 / mu) M (same pattern), the prolongators
+  // smoothed with the filtered operator when shifted.
   HostCSR L = M.lapH;
   const double alpha = c0 / mu;
   for(size_t k = 0; k < L.a.size(); ++k) L.a[k] += alpha * M.massH.a[k];
+  AMGParams vp = M.params;
+  vp.filterSmoothing = c0 > 0.;
   AMGHierarchy H;
-  FE_TRY(amg_build(L, M.params, H));
+  FE_TRY(amg_build(L, vp, H));
   auto amg = std::make_unique<AMGDevice>();
-  FE_TRY(amg->upload(H, M.params, M.fp32, s_));
+  FE_TRY(amg->upload(H, vp, M.fp32, s_));
   M.amg = std::move(amg);
   M.lapDiagSum = M.amg->finestDiagSum();
   // Pressure Laplacian multigrid (built once) and the Cahouet-Chabard weight.
