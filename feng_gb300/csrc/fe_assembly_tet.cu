@@ -681,18 +681,29 @@ __global__ void __launch_bounds__(RT_WARPS * 32) k_matrix_tet_rows(RowAsmTet ra,
           __syncwarp();
           if(lane < 30) {
             const int m = lane / 10, b = lane % 10;
+            // lanes b, b + 10, b + 20 hold the same column b: terms that do
+            // not depend on m are split among them and exchanged by shuffles
+            constexpr unsigned L30 = 0x3fffffffu;
             float A[3] = {0.f, 0.f, 0.f};
             if(fc.hasConv) {
-              // W = sum_c sum_r V0[r][c] T[r][a][c][b], Z_r = sum_c u_(c,m) T[r][a][b][c]
-              float W = 0.f, Z[3] = {0.f, 0.f, 0.f};
+              // W = sum_c sum_r V0[r][c] T[r][a][c][b] (lane m sums c = m, m + 3, ...),
+              // Z_r = sum_c u_(c,m) T[r][a][b][c]
+              float Wp = 0.f, Z[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+              for(int cc = 0; cc < 4; ++cc) {
+                const int c = m + 3 * cc;
+                if(c < 10) {
+#pragma unroll
+                  for(int q = 0; q < 3; ++q) Wp += sV0[warp][q * 10 + c] * Tt.t(q, a, c, b);
+                }
+              }
 #pragma unroll
               for(int c = 0; c < 10; ++c) {
-#pragma unroll
-                for(int q = 0; q < 3; ++q) W += sV0[warp][q * 10 + c] * Tt.t(q, a, c, b);
                 const float um = E[3 * c + m];
 #pragma unroll
                 for(int q = 0; q < 3; ++q) Z[q] += um * Tt.t(q, a, b, c);
               }
+              const float W = __shfl_sync(L30, Wp, b) + __shfl_sync(L30, Wp, b + 10) + __shfl_sync(L30, Wp, b + 20);
               const float cc = fconv * J;
 #pragma unroll
               for(int n = 0; n < 3; ++n) {
@@ -702,12 +713,18 @@ __global__ void __launch_bounds__(RT_WARPS * 32) k_matrix_tet_rows(RowAsmTet ra,
               }
             }
             if(fc.hasSigma) {
+              // row q = m of P formed here, rows q != m from lanes q * 10 + b
+              float Pm3[3];
+              {
+                const float k0 = Tt.k(m, 0, a, b), k1 = Tt.k(m, 1, a, b), k2 = Tt.k(m, 2, a, b);
+#pragma unroll
+                for(int l = 0; l < 3; ++l) Pm3[l] = k0 * G[0][l] + k1 * G[1][l] + k2 * G[2][l];
+              }
               float P[3][3];
 #pragma unroll
               for(int q = 0; q < 3; ++q)
 #pragma unroll
-                for(int l = 0; l < 3; ++l)
-                  P[q][l] = Tt.k(q, 0, a, b) * G[0][l] + Tt.k(q, 1, a, b) * G[1][l] + Tt.k(q, 2, a, b) * G[2][l];
+                for(int l = 0; l < 3; ++l) P[q][l] = __shfl_sync(L30, Pm3[l], q * 10 + b);
               float tr = 0.f;
 #pragma unroll
               for(int kk = 0; kk < 3; ++kk) tr += G[0][kk] * P[0][kk] + G[1][kk] * P[1][kk] + G[2][kk] * P[2][kk];
