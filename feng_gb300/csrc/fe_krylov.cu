@@ -744,17 +744,17 @@ __global__ void __launch_bounds__(RB, 4) k_gs_dots_all(int64_t n4, int m1, const
   if(c < nc) {
     const double *pc = partials + (int64_t)c * MAXRED;
     double v4[4] = {0., 0., 0., 0.};
-    for(int k0 = 0; s + T * k0 < nb; k0 += 16) {
+    for(int k0 = 0; s + T * k0 < nb; k0 += 24) {
       // straight-line loads (indices clamped into the array, the extra ones
-      // zeroed by selects), so that all 16 are in flight at once
-      double v[16];
+      // zeroed by selects), so that all 24 are in flight at once
+      double v[24];
 #pragma unroll
-      for(int k = 0; k < 16; ++k) {
+      for(int k = 0; k < 24; ++k) {
         const int b = s + T * (k0 + k);
         v[k] = __ldcg(pc + (b < nb ? b : 0));
       }
 #pragma unroll
-      for(int k = 0; k < 16; ++k) v4[k & 3] += s + T * (k0 + k) < nb ? v[k] : 0.;
+      for(int k = 0; k < 24; ++k) v4[k & 3] += s + T * (k0 + k) < nb ? v[k] : 0.;
     }
     part = (v4[0] + v4[1]) + (v4[2] + v4[3]);
   }
@@ -852,26 +852,33 @@ __global__ void __launch_bounds__(RB, 4) k_gs_upd(int64_t n4, int m1, float *__r
   __syncthreads();
   if(!last) return;
   __threadfence();
-  if(warp == 0) {
-    double s8[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
+  {
+    // every thread of the last block: partials t, t + RB, t + 2 RB, ... (one
+    // round of straight-line loads for up to 4 RB blocks), then the warps'
+    // sums in warp order
     const int nb = (int)gridDim.x;
-    for(int b0 = lane; b0 < nb; b0 += 256) {
-      double v[8];
+    double t = 0.;
+    for(int b0 = threadIdx.x; b0 < nb; b0 += 4 * RB) {
+      double v[4];
 #pragma unroll
-      for(int k = 0; k < 8; ++k) v[k] = __ldcg(partials + (b0 + 32 * k < nb ? b0 + 32 * k : 0));
+      for(int k = 0; k < 4; ++k) v[k] = __ldcg(partials + (b0 + RB * k < nb ? b0 + RB * k : 0));
 #pragma unroll
-      for(int k = 0; k < 8; ++k) s8[k] += b0 + 32 * k < nb ? v[k] : 0.;
+      for(int k = 0; k < 4; ++k) t += b0 + RB * k < nb ? v[k] : 0.;
     }
-    double sum = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
-    for(int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-    if(lane == 0) {
-      const double nrm = sqrt(sum);
-      st->result[0] = sum;
-      *Hnext = nrm;
-      st->finv = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
-      if(!second) st->reorth = sum < 1e-2 * st->result[2] ? 1 : 0;
-      st->counter = 0;
-    }
+    for(int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    __syncthreads();
+    if(lane == 0) wred[warp] = t;
+    __syncthreads();
+  }
+  if(threadIdx.x == 0) {
+    double sum = 0.;
+    for(int k = 0; k < RB / 32; ++k) sum += wred[k];
+    const double nrm = sqrt(sum);
+    st->result[0] = sum;
+    *Hnext = nrm;
+    st->finv = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
+    if(!second) st->reorth = sum < 1e-2 * st->result[2] ? 1 : 0;
+    st->counter = 0;
   }
 }
 
