@@ -87,6 +87,15 @@ namespace {
 
 constexpr int NPART = 512;
 
+// The Schur complement approximation S^-1 ~ -SCHUR_FACTOR (s / (vfac sigma
+// c_div)) M_p^-1: the viscous estimate (the velocity block ~ s K, so
+// mu ~ -s / (vfac sigma)) scaled up for what convection and the Newton terms
+// add to the velocity block.  Measured (FGMRES iterations; factor 1 / 3 / 6
+// / 10): Kovasznay 256^2 555 / 364 / 331 / 327 per solve, 512^2 884 (1) /
+// 489 (6) / 502 (8); cavity 384^2 64.0 / 50.6 / 49.3 per step (8: 52.6);
+// 48^3 cube 66.8 / 47.5 / 40.3 per step (8: 39.5).
+constexpr double SCHUR_FACTOR = 6.0;
+
 template <typename V>
 __global__ void k_dot_part(int64_t n, const V *__restrict__ a, const V *__restrict__ b, double *part)
 {
@@ -680,7 +689,7 @@ int Krylov::factor_mg(const double *values64, const float *values32)
     std::vector<double> sc(M.nP);
     std::vector<float> sc32(M.nP);
     for(int64_t k = 0; k < M.nP; ++k) {
-      sc[k] = -M.s / (M.vfac * M.sigma * M.divu * M.pMass[k]);
+      sc[k] = -SCHUR_FACTOR * M.s / (M.vfac * M.sigma * M.divu * M.pMass[k]);
       sc32[k] = (float)sc[k];
     }
     CKM(cudaMemcpyAsync(M.pScale64, sc.data(), sizeof(double) * M.nP, cudaMemcpyHostToDevice, s_));

@@ -19,7 +19,7 @@
  *     after the coarse correction, weight 1 / (0.7 rho);
  *   - the block upper-triangular preconditioner of Elman, Silvester and
  *     Wathen (Finite Elements and Fast Iterative Solvers, 2nd ed., ch. 9):
- *     z_p = S^-1 r_p with S^-1 ~ -(s / (1.5 sigma c_div)) M_p^-1 (lumped
+ *     z_p = S^-1 r_p with S^-1 ~ -6 (s / (1.5 sigma c_div)) M_p^-1 (lumped
  *     pressure mass) and the constant pressure mode deflated, then
  *     z_u = (s K)^-1 (r_u - G z_p) per velocity component by one V-cycle on
  *     the scalar P2 stiffness K, s = diag(A_uu) sum / diag(K) sum.
@@ -516,7 +516,8 @@ int fo_spmg_factor(fo_spmg *S, const double *a)
   if(!isfinite(sum) || sum == 0.) return -6;
   S->s = sum / fo_mg_diag_sum(S->mg);
   if(S->kind != 4) return 0;
-  for(int64_t k = 0; k < S->np; ++k) S->pscale[k] = -S->s / (1.5 * S->sigma * S->divu * S->pmass[k]);
+  /* the device preconditioner's scaled viscous estimate (factor 6) */
+  for(int64_t k = 0; k < S->np; ++k) S->pscale[k] = -6.0 * S->s / (1.5 * S->sigma * S->divu * S->pmass[k]);
   /* c^T S c = -(D^T c) . (s K)^-1 (G c), c = 1 on the pressure unknowns */
   const int64_t nn = S->nn;
   for(int64_t q = 0; q < 2 * nn; ++q) {
