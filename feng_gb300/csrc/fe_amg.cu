@@ -88,6 +88,39 @@ __device__ __forceinline__ void row_dot(int32_t beg, int32_t end, int sub, const
     for(int o = LANES / 2; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o, LANES);
 }
 
+// Lane sums acc[c] = sum_k (a[k] w[ja[k]]) x[ja[k]][c] over the entries
+// k = beg + sub, beg + sub + LANES, ... of a row (in that order; no
+// reduction across the lanes), walked as row_dot: the column indices and
+// values of UNR segments first, then their gathers.
+template <typename V, int LANES, int NV>
+__device__ __forceinline__ void row_dot_w(int32_t beg, int32_t end, int sub, const int32_t *__restrict__ ja,
+                                          const V *__restrict__ a, const V *__restrict__ w,
+                                          const V *__restrict__ x, V (&acc)[NV])
+{
+  constexpr int UNR = LANES >= 8 ? 4 : 2;
+#pragma unroll
+  for(int c = 0; c < NV; ++c) acc[c] = 0;
+  for(int32_t k0 = beg + sub; k0 < end; k0 += LANES * UNR) {
+    int32_t j[UNR];
+    V av[UNR];
+#pragma unroll
+    for(int u = 0; u < UNR; ++u) {
+      const int32_t k = k0 + u * LANES;
+      const bool ok = k < end;
+      j[u] = ok ? __ldcs(ja + k) : -1;
+      av[u] = ok ? __ldcs(a + k) : (V)0;
+    }
+#pragma unroll
+    for(int u = 0; u < UNR; ++u)
+      if(j[u] >= 0) {
+        const V ak = av[u] * w[j[u]];
+        const Vals<V, NV> xv = ldv<V, NV>(x, j[u]);
+#pragma unroll
+        for(int c = 0; c < NV; ++c) acc[c] += ak * xv.v[c];
+      }
+  }
+}
+
 // y = A x (MODE 0), y = b - A x (MODE 1), y += A x (MODE 2),
 // y = A (b .* x) with b a per-row scale of x (MODE 3), y = b + A x (MODE 4)
 template <typename V, int LANES, int MODE, int NV>
@@ -104,15 +137,7 @@ __global__ void __launch_bounds__(256) k_csr(int64_t n, const int32_t *__restric
   const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
   V acc[NV];
   if(MODE == 3) {
-#pragma unroll
-    for(int c = 0; c < NV; ++c) acc[c] = 0;
-    for(int32_t k = beg + sub; k < end; k += LANES) {
-      const int32_t j = ja[k];
-      const V ak = a[k] * b[j];
-      const Vals<V, NV> xv = ldv<V, NV>(x, j);
-#pragma unroll
-      for(int c = 0; c < NV; ++c) acc[c] += ak * xv.v[c];
-    }
+    row_dot_w<V, LANES, NV>(beg, end, sub, ja, a, b, x, acc);
 #pragma unroll
     for(int c = 0; c < NV; ++c)
 #pragma unroll
@@ -234,15 +259,7 @@ __global__ void __launch_bounds__(256) k_cheb_first(int64_t n, const int32_t *__
   const bool live = row < n;
   const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
   V acc[NV];
-#pragma unroll
-  for(int c = 0; c < NV; ++c) acc[c] = 0;
-  for(int32_t k = beg + sub; k < end; k += LANES) {
-    const int32_t j = __ldcs(ja + k);
-    const V ak = __ldcs(a + k) * dinv[j];
-    const Vals<V, NV> bv = ldv<V, NV>(b, j);
-#pragma unroll
-    for(int c = 0; c < NV; ++c) acc[c] += ak * bv.v[c];
-  }
+  row_dot_w<V, LANES, NV>(beg, end, sub, ja, a, dinv, b, acc);
 #pragma unroll
   for(int c = 0; c < NV; ++c)
 #pragma unroll
@@ -380,12 +397,24 @@ __global__ void __launch_bounds__(256) k_cheb_post_sell(int64_t n, const int32_t
                                                         const int32_t *__restrict__ sc, const V *__restrict__ sv,
                                                         const V *__restrict__ dinv, const V *__restrict__ b,
                                                         const V *__restrict__ y, V *__restrict__ x, V inv_theta,
-                                                        const int *__restrict__ skip, const int32_t *__restrict__ dofX,
-                                                        const int32_t *__restrict__ dofY,
-                                                        const double *__restrict__ scale, V *__restrict__ out)
+                                                        const int *__restrict__ skip, AMGDevice::OutMap om)
 {
   FE_PDL_ENTRY();
   if(skip && *skip) return;
+  if constexpr(OUT) {
+    const int64_t rowBlocks = (n + 255) / 256;
+    if((int64_t)blockIdx.x >= rowBlocks) {
+      // pressure rows of the folded saddle-point preconditioner
+      const int64_t k = ((int64_t)blockIdx.x - rowBlocks) * 256 + threadIdx.x;
+      if(k >= om.nP) return;
+      const double c = *om.cr, cSc = om.consts[1], cMc = om.consts[2];
+      const double shift = cMc > 0 ? c / cMc : 0., lift = cSc != 0. ? c / cSc : 0.;
+      const int32_t i = om.pRows[k];
+      const double rp = (double)((const V *)om.r)[i] - shift * om.pMass[k];
+      ((V *)om.z)[i] = (V)((double)((const V *)om.pScale)[k] * rp + lift);
+      return;
+    }
+  }
   const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if(row >= n) return;
   const int64_t sl = row >> 5;
@@ -400,13 +429,20 @@ __global__ void __launch_bounds__(256) k_cheb_post_sell(int64_t n, const int32_t
     for(int c = 0; c < NV; ++c) acc[c] += ak * yv.v[c];
   });
   const V dv = dinv[row];
+  V cf = 0;
+  if constexpr(OUT)
+    if(om.bgu) cf = (V)*om.cr;
 #pragma unroll
   for(int c = 0; c < NV; ++c) {
     const int64_t o = row * NV + c;
     const V ri = dv * (b[o] - acc[c]);
     const V xo = y[o] + ri * inv_theta;
-    if(OUT) out[c == 0 ? dofX[row] : dofY[row]] = xo * (V)*scale;
-    else x[o] = xo;
+    if constexpr(OUT) {
+      const V xf = om.bgu ? xo - cf * ((const V *)om.bgu)[o] : xo;
+      ((V *)om.z)[c == 0 ? om.dofX[row] : om.dofY[row]] = xf * (V)*om.scale;
+    } else {
+      x[o] = xo;
+    }
   }
 }
 
@@ -447,31 +483,39 @@ __global__ void k_cheb_last(int64_t m, const V *__restrict__ d, V *__restrict__ 
     x[i] += d[i];
 }
 
-// x = Minv b for the coarsest level (dense, row-major), one warp per row.
+// x = Minv b for the coarsest level (dense, row-major): one block of
+// DENSE_T threads per row, so that every load of the row is in flight at
+// once; warp sums, then the warps' sums in order (deterministic).
+constexpr int DENSE_T = 128;
 template <typename V, int NV>
-__global__ void k_dense(int64_t n, const V *__restrict__ M, const V *__restrict__ b, V *__restrict__ x,
-                        const int *__restrict__ skip)
+__global__ void __launch_bounds__(DENSE_T) k_dense(int64_t n, const V *__restrict__ M, const V *__restrict__ b,
+                                                   V *__restrict__ x, const int *__restrict__ skip)
 {
   FE_PDL_ENTRY();
   if(skip && *skip) return;
-  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
-  const int lane = threadIdx.x % 32;
-  const bool live = row < n;
+  __shared__ V red[DENSE_T / 32][NV];
+  const int64_t row = blockIdx.x;
   V acc[NV];
 #pragma unroll
   for(int c = 0; c < NV; ++c) acc[c] = 0;
-  if(live)
-    for(int64_t k = lane; k < n; k += 32) {
-      const V m = M[row * n + k];
+#pragma unroll 4
+  for(int64_t k = threadIdx.x; k < n; k += DENSE_T) {
+    const V m = M[row * n + k];
 #pragma unroll
-      for(int c = 0; c < NV; ++c) acc[c] += m * b[k * NV + c];
-    }
+    for(int c = 0; c < NV; ++c) acc[c] += m * b[k * NV + c];
+  }
 #pragma unroll
-  for(int c = 0; c < NV; ++c)
-    for(int o = 16; o > 0; o >>= 1) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], o);
-  if(live && lane == 0)
+  for(int c = 0; c < NV; ++c) {
+    for(int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+    if((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][c] = acc[c];
+  }
+  __syncthreads();
+  if(threadIdx.x < NV) {
+    V t = red[0][threadIdx.x];
 #pragma unroll
-    for(int c = 0; c < NV; ++c) x[row * NV + c] = acc[c];
+    for(int w = 1; w < DENSE_T / 32; ++w) t += red[w][threadIdx.x];
+    x[row * NV + threadIdx.x] = t;
+  }
 }
 
 template <typename V>
@@ -666,7 +710,7 @@ void AMGDevice::vcycle_t(int l, const V *b, V *x)
 {
   Lev &L = lv_[l];
   if(l == (int)lv_.size() - 1) {
-    ::feng::launch_k(k_dense<V, NV>, grid(L.n * 32), 256, 0, s_, L.n, (const V *)coarseInv_, b, x, skip_);
+    if(L.n > 0) ::feng::launch_k(k_dense<V, NV>, (int)L.n, DENSE_T, 0, s_, L.n, (const V *)coarseInv_, b, x, skip_);
     return;
   }
   Lev &C = lv_[l + 1];
@@ -694,12 +738,13 @@ void AMGDevice::vcycle_t(int l, const V *b, V *x)
     if(L.sellPtr) {
       const V *sv = (const V *)L.sellVal;
       if(l == 0 && NV == 2 && out_.z) {
-        ::feng::launch_k(k_cheb_post_sell<V, NV, true>, grid(L.n), 256, 0, s_, L.n, L.sellPtr, L.sellCol, sv, dinv, b, y, x, it, skip_,
-                                                                 out_.dofX, out_.dofY, out_.scale, (V *)out_.z);
+        const int extra = out_.bgu ? (int)((out_.nP + 255) / 256) : 0;
+        ::feng::launch_k(k_cheb_post_sell<V, NV, true>, grid(L.n) + extra, 256, 0, s_, L.n, L.sellPtr, L.sellCol, sv, dinv,
+                         b, y, x, it, skip_, out_);
         outWritten_ = true;
       } else {
         ::feng::launch_k(k_cheb_post_sell<V, NV, false>, grid(L.n), 256, 0, s_, L.n, L.sellPtr, L.sellCol, sv, dinv, b, y, x, it,
-                                                                  skip_, nullptr, nullptr, nullptr, nullptr);
+                         skip_, AMGDevice::OutMap());
       }
       return;
     }

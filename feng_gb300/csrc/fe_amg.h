@@ -82,7 +82,23 @@ class AMGDevice {
     const int32_t *dofX = nullptr, *dofY = nullptr;
     const double *scale = nullptr;
     void *z = nullptr;
+    // Optional pressure fold of the steady saddle-point preconditioner
+    // (bgu set): the velocity result is (x - c bgu) * scale, c = *cr and
+    // bgu interleaved like x, and extra blocks of the same launch write the
+    // nP pressure rows z[pRows[k]] = sc_k (r_i - c m_k / cMc) + c / cSc,
+    // i = pRows[k], sc = pScale (the vector type), m = pMass,
+    // cSc = consts[1], cMc = consts[2].
+    const double *cr = nullptr;
+    const void *bgu = nullptr;
+    int64_t nP = 0;
+    const int32_t *pRows = nullptr;
+    const void *pScale = nullptr;
+    const double *pMass = nullptr, *consts = nullptr;
+    const void *r = nullptr;
   };
+  // Whether the finest level runs on its sliced-ELL copy (then a paired
+  // V-cycle with an OutMap always writes through it).
+  bool fineSell() const { return !lv_.empty() && lv_[0].sellPtr != nullptr; }
   // Both components at once (x, b interleaved).  With om, the finest
   // post-smoothing pass writes the result through om when it can (then
   // returns true; x does not hold the result), otherwise x holds it.

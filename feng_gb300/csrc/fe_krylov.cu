@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "fe_common.h"
+#include "fe_df.h"
 #include "fe_launch.h"
 #include "fe_krylov.h"
 
@@ -336,52 +337,95 @@ __global__ void k_givens(GmresState *gs, int j)
   givens_warp(gs, j, threadIdx.x, sh, scs, ssn);
 }
 
-// y = R^-1 g with R the upper triangle of H (k x k): one block, R staged in
-// shared memory; row i's dot with the solved tail is a block reduction.
+// y = R^-1 g with R the upper triangle of H (k x k), by columns: the block
+// stages R in shared memory (all loads in flight at once), then one warp
+// sweeps c = k-1 .. 0: the lane holding row c divides, broadcasts y_c, and
+// every lane subtracts column c times y_c from its rows above c (lane l
+// holds rows l, l + 32, ...; fixed order, deterministic).
 __global__ void k_backsolve(GmresState *gs)
 {
   FE_PDL_ENTRY();
   // dynamic: the column-major upper triangle of the restart length m
   // (m (m + 1) / 2 doubles), sized at launch
   extern __shared__ double sR[];
-  __shared__ double sy[MAXM], sg[MAXM], red[32];
   const int k = gs->k;
   auto idx = [](int i, int c) { return c * (c + 1) / 2 + i; };  // i <= c
-  for(int c = threadIdx.x; c < k; c += blockDim.x) sg[c] = gs->g[c];
-  for(int c = 0; c < k; ++c)
-    for(int i = threadIdx.x; i <= c; i += blockDim.x) sR[idx(i, c)] = gs->H[(int64_t)c * (MAXM + 1) + i];
-  __syncthreads();
-  for(int i = k - 1; i >= 0; --i) {
-    double p = 0.;
-    for(int c = i + 1 + threadIdx.x; c < k; c += blockDim.x) p += sR[idx(i, c)] * sy[c];
-    for(int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
-    if((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = p;
-    __syncthreads();
-    if(threadIdx.x == 0) {
-      double s = sg[i];
-      for(int w = 0; w < (int)(blockDim.x >> 5); ++w) s -= red[w];
-      const double d = sR[idx(i, i)];
-      sy[i] = d != 0 ? s / d : 0.;
-    }
-    __syncthreads();
+  for(int e = threadIdx.x; e < k * k; e += blockDim.x) {
+    const int c = e / k, i = e - c * k;
+    if(i <= c) sR[idx(i, c)] = gs->H[(int64_t)c * (MAXM + 1) + i];
   }
-  for(int c = threadIdx.x; c < k; c += blockDim.x) gs->y[c] = sy[c];
+  __syncthreads();
+  if(threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  constexpr int RPL = MAXM / 32;  // rows per lane
+  double s[RPL];
+#pragma unroll
+  for(int t = 0; t < RPL; ++t) s[t] = lane + 32 * t < k ? gs->g[lane + 32 * t] : 0.;
+  for(int c = k - 1; c >= 0; --c) {
+    const int owner = c & 31, tc = c >> 5;
+    double sc = 0.;
+#pragma unroll
+    for(int t = 0; t < RPL; ++t)
+      if(t == tc) sc = s[t];
+    double yc = 0.;
+    if(lane == owner) {
+      const double d = sR[idx(c, c)];
+      yc = d != 0 ? sc / d : 0.;
+      gs->y[c] = yc;
+    }
+    yc = __shfl_sync(0xffffffffu, yc, owner);
+#pragma unroll
+    for(int t = 0; t < RPL; ++t) {
+      const int i = lane + 32 * t;
+      if(i < c) s[t] -= sR[idx(i, c)] * yc;
+    }
+  }
 }
 
+// x += Z y.  FP64 basis: FP64 products and sums.  FP32 basis (mixed path):
+// the products and the running sum in double-float on the FP32 pipes (the
+// FP64 pipe of the GB300 would bound the pass at ~50 us for 50 columns of
+// 588 k rows; double-float keeps it at the bytes), added to x in FP64.
 template <typename VZ>
 __global__ void k_xupdate(int64_t n, int64_t ld, const VZ *__restrict__ Z, const GmresState *gs,
                           double *__restrict__ x)
 {
   FE_PDL_ENTRY();
-  __shared__ double sy[MAXM];
   const int k = gs->k;
-  for(int c = threadIdx.x; c < k; c += blockDim.x) sy[c] = gs->y[c];
-  __syncthreads();
-  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-      i += (int64_t)gridDim.x * blockDim.x) {
-    double acc = x[i];
-    for(int c = 0; c < k; ++c) acc += sy[c] * (double)Z[(int64_t)c * ld + i];
-    x[i] = acc;
+  if constexpr(sizeof(VZ) == 8) {
+    __shared__ double sy[MAXM];
+    for(int c = threadIdx.x; c < k; c += blockDim.x) sy[c] = gs->y[c];
+    __syncthreads();
+    for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x) {
+      double acc = x[i];
+      for(int c = 0; c < k; ++c) acc += sy[c] * (double)Z[(int64_t)c * ld + i];
+      x[i] = acc;
+    }
+  } else {
+    __shared__ dfl sy[MAXM];
+    for(int c = threadIdx.x; c < k; c += blockDim.x) sy[c] = df_from(gs->y[c]);
+    __syncthreads();
+    constexpr int U = 8;
+    for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x) {
+      dfl acc = df_zero();
+      for(int c0 = 0; c0 < k; c0 += U) {
+        float z[U];
+#pragma unroll
+        for(int u = 0; u < U; ++u) z[u] = c0 + u < k ? (float)Z[(int64_t)(c0 + u) * ld + i] : 0.f;
+#pragma unroll
+        for(int u = 0; u < U; ++u)
+          if(c0 + u < k) {
+            const dfl y = sy[c0 + u];
+            const float p = __fmul_rn(z[u], y.hi);
+            float e = __fmaf_rn(z[u], y.hi, -p);
+            e = __fmaf_rn(z[u], y.lo, e);
+            acc = df_add(acc, df_fast2(p, e));
+          }
+      }
+      x[i] += df_to(acc);
+    }
   }
 }
 
@@ -1222,7 +1266,7 @@ struct Ws {
 #define Ws_INIT(k) {(RedState *)(k)->red_state_, (GmresState *)(k)->gmres_, (GmresState *)(k)->h_gmres_, (CGState *)(k)->cg_, (CGState *)(k)->h_cg_}
 Krylov::~Krylov()
 {
-  cudaFree(V_); cudaFree(Z_); cudaFree(Z32_); cudaFree(V32_); cudaFree(vc32_); cudaFree(v32_); cudaFree(w32_);
+  cudaFree(V_); cudaFree(Z_); cudaFree(Z32_); cudaFree(V32_); cudaFree(vc32_); cudaFree(xs2_); cudaFree(v32_); cudaFree(w32_);
   cudaFree(zeroFlag_);
   cudaFree(sellPtr_); cudaFree(sellCol_); cudaFree(sellSrc_); cudaFree(sellVal_);
   cudaFree(w_); cudaFree(r_); cudaFree(t_); cudaFree(p_); cudaFree(q_);
@@ -1289,12 +1333,12 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
         set_error("mixed-precision FGMRES supports restart lengths up to 64 (got %d)", m);
         return FE_INVALID_ARG;
       }
-      // Leading dimension a multiple of 64 floats; rows n..ld-1 stay zero.
       // whole row blocks of the basis (rows n..ld-1 stay zero)
       ld32_ = (n_ + VBLK - 1) / VBLK * VBLK;
       CK(cudaMalloc(&V32_, sizeof(float) * ld32_ * (m + 1)));
       CK(cudaMalloc(&Z32_, sizeof(float) * ld32_ * m));
       CK(cudaMalloc(&vc32_, sizeof(float) * ld32_));
+      CK(cudaMalloc(&xs2_, sizeof(float2) * ld32_));
       CK(cudaMemset(V32_, 0, sizeof(float) * ld32_ * (m + 1)));
       CK(cudaMemset(Z32_, 0, sizeof(float) * ld32_ * m));
       CK(cudaMemset(vc32_, 0, sizeof(float) * ld32_));
@@ -1607,6 +1651,72 @@ __global__ void __launch_bounds__(256) k_resid_sell(int64_t n, const int32_t *__
   y[row] = b[row] - acc;
 }
 
+// x split into two floats, x ~ hi + lo (the operand of k_resid_sell_df)
+__global__ void k_split_x(int64_t n, const double *__restrict__ x, float2 *__restrict__ xs)
+{
+  FE_PDL_ENTRY();
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const dfl d = df_from(x[i]);
+    xs[i] = make_float2(d.hi, d.lo);
+  }
+}
+
+// r = b - A x as k_resid_sell, the products a (x_hi + x_lo) and their sum in
+// double-float on the FP32 pipes (a x_hi exact by a fused multiply-add), the
+// result subtracted from b in FP64: ~2^-44 relative to sum |a x| against
+// FP64's 2^-53, far below the refinement's stops, and the FP64 pipe of the
+// GB300 (one FP64 product per entry would take ~27 us at 588 k rows) left
+// out.
+template <int UNR>
+__global__ void __launch_bounds__(256) k_resid_sell_df(int64_t n, const int32_t *__restrict__ sp,
+                                                       const int32_t *__restrict__ sc, const float *__restrict__ sv,
+                                                       const float2 *__restrict__ xs, const double *__restrict__ b,
+                                                       double *__restrict__ y)
+{
+  FE_PDL_ENTRY();
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if(row >= n) return;
+  const int64_t sl = row >> 5;
+  const int lane = (int)(row & 31);
+  const int32_t base = sp[sl], len = (sp[sl + 1] - base) >> 5;
+  dfl acc = df_zero();
+  int32_t c[UNR];
+  float a[UNR];
+#pragma unroll
+  for(int u = 0; u < UNR; ++u) {
+    const bool ok = u < len;
+    const int32_t e = base + (u << 5) + lane;
+    c[u] = ok ? __ldcs(sc + e) : -1;
+    a[u] = ok ? __ldcs(sv + e) : 0.f;
+  }
+  for(int32_t k = 0; k < len; k += UNR) {
+    int32_t cn[UNR];
+    float an[UNR];
+#pragma unroll
+    for(int u = 0; u < UNR; ++u) {
+      const bool ok = k + UNR + u < len;
+      const int32_t e = base + ((k + UNR + u) << 5) + lane;
+      cn[u] = ok ? __ldcs(sc + e) : -1;
+      an[u] = ok ? __ldcs(sv + e) : 0.f;
+    }
+#pragma unroll
+    for(int u = 0; u < UNR; ++u)
+      if(c[u] >= 0) {
+        const float2 xv = xs[c[u]];
+        const float p = __fmul_rn(a[u], xv.x);
+        float e = __fmaf_rn(a[u], xv.x, -p);
+        e = __fmaf_rn(a[u], xv.y, e);
+        acc = df_add(acc, df_fast2(p, e));
+      }
+#pragma unroll
+    for(int u = 0; u < UNR; ++u) {
+      c[u] = cn[u];
+      a[u] = an[u];
+    }
+  }
+  y[row] = b[row] - df_to(acc);
+}
+
 // sliced-ELL values from the CSR values (padding: 0)
 __global__ void k_sell_gather(int64_t m, const int32_t *__restrict__ src, const float *__restrict__ a,
                               float *__restrict__ out)
@@ -1831,7 +1941,11 @@ int Krylov::cycleGraph(bool mixed, const void *vals, const double *b, double *x,
 // copy when it is built (it holds the same values), else the CSR kernel.
 void Krylov::resid32(const float *vals, const double *x, const double *b, double *r)
 {
-  if(sellVal_)
+  if(sellVal_ && xs2_ && dfResid_) {
+    ::feng::launch_k(k_split_x, grid_for(n_, 256, 4096), 256, 0, s_, n_, x, (float2 *)xs2_);
+    ::feng::launch_k(k_resid_sell_df<8>, grid_for(n_, 256, 1 << 20), 256, 0, s_, n_, sellPtr_, sellCol_, sellVal_,
+                     (const float2 *)xs2_, b, r);
+  } else if(sellVal_)
     ::feng::launch_k(k_resid_sell<8>, grid_for(n_, 256, 1 << 20), 256, 0, s_, n_, sellPtr_, sellCol_, sellVal_, x, b,
                      r);
   else
@@ -2056,7 +2170,7 @@ void Krylov::launch_cycle(bool mixed, const void *vals, const double *b, double 
     ::feng::launch_k(k_givens, 1, 32, 0, s_, w.gs, j);
     if(poll && poll_done(&w.gs->done, j)) break;
   }
-  ::feng::launch_k(k_backsolve, 1, 128, backsolveSmem(opt.restart), s_, w.gs);
+  ::feng::launch_k(k_backsolve, 1, 256, backsolveSmem(opt.restart), s_, w.gs);
   ::feng::launch_k(k_xupdate<double>, gv, 256, 0, s_, n_, n_, Z_, w.gs, x);
   cudaMemcpyAsync(h_gmres_, w.gs, sizeof(GmresHead), cudaMemcpyDeviceToHost, s_);
 }
@@ -2124,7 +2238,7 @@ void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, i
     }
     if(poll && poll_done(&w.gs->done, j)) break;
   }
-  ::feng::launch_k(k_backsolve, 1, 128, backsolveSmem(opt.restart), s_, w.gs);
+  ::feng::launch_k(k_backsolve, 1, 256, backsolveSmem(opt.restart), s_, w.gs);
   ::feng::launch_k(k_xupdate<float>, gv, 256, 0, s_, n_, ld32_, Z32_, w.gs, x);
   cudaMemcpyAsync(h_gmres_, w.gs, sizeof(GmresHead), cudaMemcpyDeviceToHost, s_);
 }
@@ -2135,10 +2249,11 @@ int Krylov::run_cycle(bool mixed, const void *vals, const double *b, double *x, 
 {
   const int m = opt.restart;
   if(useGraphs_ && jmax == m) {
-    GraphKey key{mixed, vals, b, x};
+    GraphKey key{mixed, vals, b, x, mixed && dfResid_};
     cudaGraphExec_t exec = nullptr;
     for(auto &g : graphs_)
-      if(g.first.mixed == key.mixed && g.first.vals == key.vals && g.first.b == key.b && g.first.x == key.x)
+      if(g.first.mixed == key.mixed && g.first.vals == key.vals && g.first.b == key.b && g.first.x == key.x &&
+         g.first.dfResid == key.dfResid)
         exec = g.second;
     size_t nKernels = 0;
     if(!exec) {
@@ -2208,6 +2323,7 @@ int Krylov::solve_fgmres_mixed(const float *vals32, const double *b, double *x, 
   const GmresHead *hd = (const GmresHead *)h_gmres_;
   int total = 0;
   *htol_ = tolAbs;
+  dfResid_ = tolAbs >= 1e-9 * st.rnorm0;
   while(true) {
     FE_TRY(run_cycle(true, vals32, b, x, std::min(opt.restart, maxIt - total)));
     st.refinements++;

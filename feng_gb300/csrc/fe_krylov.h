@@ -150,6 +150,11 @@ class Krylov {
   float *V32_ = nullptr;  // (m+1) x n  Krylov basis of the mixed path, FP32, in row blocks of 1024
                           // rows (column c of row block k at (k (m+1) + c) 1024)
   float *vc32_ = nullptr;  // the newest basis vector, contiguous (the preconditioner's input)
+  void *xs2_ = nullptr;     // float2 split of the FP64 iterate (the mixed restart residual)
+  // The mixed restart residual in double-float (k_resid_sell_df) when the
+  // solve's tolerance is at least 1e-9 relative (its error, ~1e-13 of
+  // sum |a x| per row, stays far below the stop), else in FP64.
+  bool dfResid_ = false;
   // Sliced-ELL copy of the FP32 matrix for the Arnoldi SpMV of the mixed
   // path (slices of 32 rows padded to the longest row, entries column-major
   // in the slice; padding: the row's own column, value 0), refreshed from the
@@ -194,6 +199,7 @@ class Krylov {
     const void *vals;
     const double *b;
     double *x;
+    bool dfResid;
   };
   std::vector<std::pair<GraphKey, cudaGraphExec_t>> graphs_;
   std::vector<size_t> graphKernels_;  // kernel nodes of each graph

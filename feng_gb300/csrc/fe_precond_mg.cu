@@ -10,6 +10,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <cstring>
 #include <memory>
 
 #include "fe_amg.h"
@@ -71,6 +73,15 @@ struct Krylov::MG {
   double *part = nullptr;  // [2][1024] partial sums
   double *scal = nullptr;  // rz, pq
   unsigned *count = nullptr;  // blocks done of the fused pressure sum (k_psum)
+  // Pressure fold (steady, two components, one V-cycle): G with its columns
+  // scaled by the pressure scale (gScaled), the pressure index of each G
+  // entry (upColP), u_k = 1/cSc - sc_k m_k / cMc (uP) and bgu = V(G u) (the
+  // V-cycle of G u), so that z_u = (V(r_u - G (sc r_p)) - c bgu) / s without
+  // z_p; see apply_mg.
+  int32_t *upColP = nullptr;
+  void *gScaled = nullptr, *bgu = nullptr;
+  double *uP = nullptr;
+  bool fold = false;
   ~MG()
   {
     cudaFree(dofX); cudaFree(dofY); cudaFree(pRows); cudaFree(upIa); cudaFree(upPos); cudaFree(upCol);
@@ -79,6 +90,7 @@ struct Krylov::MG {
     cudaFree(part); cudaFree(scal); cudaFree(dnIa); cudaFree(dnPos); cudaFree(dnCol); cudaFree(slotOf);
     cudaFree(pMassDev); cudaFree(tP); cudaFree(consts); cudaFree(bxy); cudaFree(zxy); cudaFree(gVals);
     cudaFree(pr); cudaFree(pz); cudaFree(count); cudaFree(dofC);
+    cudaFree(upColP); cudaFree(gScaled); cudaFree(bgu); cudaFree(uP);
   }
   template <typename V> void solveK(const V *b, V *x, cudaStream_t st);
 };
@@ -220,21 +232,23 @@ namespace {
 
 int grid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 1 << 16)); }
 
+// partial sums of the entries a[pos[i]] (the finest velocity diagonal),
+// one per block; k_dot_fin adds them in block order
 template <typename VA>
-__global__ void k_diag_sum(int64_t n, const int32_t *__restrict__ pos, const VA *__restrict__ a,
-                           double *out)
+__global__ void k_diag_part(int64_t n, const int32_t *__restrict__ pos, const VA *__restrict__ a, double *part)
 {
   FE_PDL_ENTRY();
   __shared__ double sh[256];
   double s = 0.;
-  for(int64_t i = threadIdx.x; i < n; i += blockDim.x) s += (double)a[pos[i]];
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s += (double)a[pos[i]];
   sh[threadIdx.x] = s;
   __syncthreads();
   for(int o = 128; o > 0; o >>= 1) {
     if(threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
     __syncthreads();
   }
-  if(threadIdx.x == 0) *out = sh[0];
+  if(threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
 template <typename V>
@@ -287,16 +301,17 @@ __global__ void k_psum_part(int64_t nP, const int32_t *__restrict__ rows, const 
 
 // *out = sum of r over the pressure rows in one launch: the partial sums of
 // k_psum_part, then the last block to finish sums them as k_dot_fin does
-// (same order, same bits).
+// (same order, same bits).  psum_blocks: the body, run by vg blocks with
+// block index vb (the whole grid of k_psum, or a trailing range of blocks
+// of k_vel_rhs_fold).
 template <typename V>
-__global__ void k_psum(int64_t nP, const int32_t *__restrict__ rows, const V *__restrict__ r, double *part,
-                       unsigned *count, double *out)
+__device__ __forceinline__ void psum_blocks(int vb, int vg, int64_t nP, const int32_t *__restrict__ rows,
+                                            const V *__restrict__ r, double *part, unsigned *count, double *out)
 {
-  FE_PDL_ENTRY();
   __shared__ double sh[256];
   __shared__ bool last;
   double s = 0.;
-  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nP; k += (int64_t)gridDim.x * blockDim.x)
+  for(int64_t k = (int64_t)vb * blockDim.x + threadIdx.x; k < nP; k += (int64_t)vg * blockDim.x)
     s += (double)r[rows[k]];
   sh[threadIdx.x] = s;
   __syncthreads();
@@ -305,15 +320,15 @@ __global__ void k_psum(int64_t nP, const int32_t *__restrict__ rows, const V *__
     __syncthreads();
   }
   if(threadIdx.x == 0) {
-    part[blockIdx.x] = sh[0];
+    part[vb] = sh[0];
     __threadfence();
-    last = atomicAdd(count, 1u) == gridDim.x - 1;
+    last = atomicAdd(count, 1u) == (unsigned)vg - 1;
   }
   __syncthreads();
   if(!last) return;
   __threadfence();
   double t = 0.;
-  for(int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) t += __ldcg(part + i);
+  for(int i = threadIdx.x; i < vg; i += blockDim.x) t += __ldcg(part + i);
   sh[threadIdx.x] = t;
   __syncthreads();
   for(int o = 128; o > 0; o >>= 1) {
@@ -324,6 +339,14 @@ __global__ void k_psum(int64_t nP, const int32_t *__restrict__ rows, const V *__
     *out = sh[0];
     *count = 0;
   }
+}
+
+template <typename V>
+__global__ void k_psum(int64_t nP, const int32_t *__restrict__ rows, const V *__restrict__ r, double *part,
+                       unsigned *count, double *out)
+{
+  FE_PDL_ENTRY();
+  psum_blocks<V>(blockIdx.x, gridDim.x, nP, rows, r, part, count, out);
 }
 
 // partial sums of a double array
@@ -451,6 +474,50 @@ __global__ void k_vel_rhs_pair(int64_t nN, const int32_t *__restrict__ dofX, con
     V t = r[c == 0 ? dofX[k] : dofY[k]];
     for(int32_t e = upIa[q]; e < upIa[q + 1]; ++e) t -= (upPos ? a[upPos[e]] : a[e]) * z[upCol[e]];
     bxy[q] = t;
+  }
+}
+
+// Folded velocity right-hand side b0 = r_u - (G sc) r_p on the slots
+// (both components interleaved, one thread per slot), and in the trailing
+// gp blocks the pressure sum c = sum of r over the pressure rows (k_psum's
+// partials and order) into *cr.
+template <typename V>
+__global__ void k_vel_rhs_fold(int64_t nN, const int32_t *__restrict__ dofX, const int32_t *__restrict__ dofY,
+                               const int32_t *__restrict__ upIa, const int32_t *__restrict__ upCol,
+                               const V *__restrict__ gs, const V *__restrict__ r, V *__restrict__ bxy,
+                               int slotBlocks, int64_t nP, const int32_t *__restrict__ pRows, double *part,
+                               unsigned *count, double *cr, const int *__restrict__ skip)
+{
+  FE_PDL_ENTRY();
+  if(skip && *skip) return;
+  if((int)blockIdx.x >= slotBlocks) {
+    psum_blocks<V>((int)blockIdx.x - slotBlocks, (int)gridDim.x - slotBlocks, nP, pRows, r, part, count, cr);
+    return;
+  }
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if(q >= 2 * nN) return;
+  const int64_t k = q >> 1;
+  V t = r[(q & 1) == 0 ? dofX[k] : dofY[k]];
+  for(int32_t e = upIa[q]; e < upIa[q + 1]; ++e) t -= gs[e] * r[upCol[e]];
+  bxy[q] = t;
+}
+
+// Per Jacobian, for the pressure fold: gScaled[e] = G_e sc_k(e) and
+// gu[q] = sum_e G_e u_k(e) on slot q (FP64 sums).
+template <typename V, typename S>
+__global__ void k_fold_prep(int64_t nq, const int32_t *__restrict__ upIa, const int32_t *__restrict__ upColP,
+                            const V *__restrict__ g, const S *__restrict__ sc, const double *__restrict__ u,
+                            V *__restrict__ gScaled, V *__restrict__ gu)
+{
+  FE_PDL_ENTRY();
+  for(int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.;
+    for(int32_t e = upIa[q]; e < upIa[q + 1]; ++e) {
+      const int32_t kp = upColP[e];
+      gScaled[e] = (V)(g[e] * (V)sc[kp]);
+      s += (double)g[e] * u[kp];
+    }
+    gu[q] = (V)s;
   }
 }
 
@@ -588,8 +655,8 @@ int Krylov::setup_mg(const PrecondInfo &pi)
   const size_t vs = M.fp32 ? sizeof(float) : sizeof(double);
   for(void **v : {&M.bx, &M.by, &M.zx, &M.zy, &M.ir, &M.iz, &M.ip, &M.iq})
     CKM(cudaMalloc(v, vs * M.nNodes));
-  for(void **v : {&M.bxy, &M.zxy}) CKM(cudaMalloc(v, 3 * vs * M.nNodes));
-  CKM(cudaMalloc(&M.dsum, sizeof(double)));
+  for(void **v : {&M.bxy, &M.zxy, &M.bgu}) CKM(cudaMalloc(v, 3 * vs * M.nNodes));
+  CKM(cudaMalloc(&M.dsum, 2 * sizeof(double)));
   CKM(cudaMalloc(&M.part, sizeof(double) * NPART));
   CKM(cudaMalloc(&M.scal, sizeof(double) * 4));
   CKM(cudaMalloc(&M.consts, sizeof(double) * 4));
@@ -638,6 +705,15 @@ int Krylov::setup_mg(const PrecondInfo &pi)
     CKM(cudaMalloc(&M.gVals, sizeof(double) * std::max<int64_t>(1, M.nG)));
     FE_TRY(up(&M.upCol, col));
     FE_TRY(up(&M.pRows, pi.pRows));
+    {
+      // pressure index of each G entry's column (the pressure fold)
+      std::vector<int32_t> pIndex(n_, -1), colP(col.size());
+      for(int64_t k = 0; k < M.nP; ++k) pIndex[pi.pRows[k]] = (int32_t)k;
+      for(size_t e = 0; e < col.size(); ++e) colP[e] = pIndex[col[e]];
+      FE_TRY(up(&M.upColP, colP));
+      CKM(cudaMalloc(&M.gScaled, sizeof(double) * std::max<int64_t>(1, M.nG)));
+      CKM(cudaMalloc(&M.uP, sizeof(double) * std::max<int64_t>(1, M.nP)));
+    }
     // D block (pressure rows -> velocity columns) and the slot of each velocity DOF.
     std::vector<int32_t> slot(n_, -1);
     for(int64_t k = 0; k < M.nNodes; ++k)
@@ -667,11 +743,66 @@ int Krylov::factor_mg(const double *values64, const float *values32)
 {
   MG &M = *mg_;
   M.amg->setSkip(nullptr);
-  if(values64) ::feng::launch_k(k_diag_sum<double>, 1, 256, 0, s_, M.nNodes, M.diagX, values64, M.dsum);
-  else ::feng::launch_k(k_diag_sum<float>, 1, 256, 0, s_, M.nNodes, M.diagX, values32, M.dsum);
-  double sum = 0.;
-  CKM(cudaMemcpyAsync(&sum, M.dsum, sizeof(double), cudaMemcpyDeviceToHost, s_));
+  // Everything the scalars need is launched first and read back with one
+  // synchronisation: the diagonal sum (dsum[0]) and, for the saddle-point
+  // preconditioner, c^T S c's estimate (dsum[1]).
+  const int gd = (int)std::min<int64_t>(NPART, std::max<int64_t>(1, (M.nNodes + 255) / 256));
+  if(values64) ::feng::launch_k(k_diag_part<double>, gd, 256, 0, s_, M.nNodes, M.diagX, values64, M.part);
+  else ::feng::launch_k(k_diag_part<float>, gd, 256, 0, s_, M.nNodes, M.diagX, values32, M.part);
+  ::feng::launch_k(k_dot_fin, 1, 256, 0, s_, gd, M.part, M.dsum);
+  double sums[2] = {0., 0.};
+  if(M.kind == 4) {
+    // Contiguous copy of the G block's values for the apply kernels.
+    if(values64)
+      ::feng::launch_k(k_gather_vals<double>, grid(M.nG), 256, 0, s_, M.nG, M.upPos, values64, (double *)M.gVals);
+    else
+      ::feng::launch_k(k_gather_vals<float>, grid(M.nG), 256, 0, s_, M.nG, M.upPos, values32, (float *)M.gVals);
+    // Constant pressure mode c: with the pressure fixed at a single point the
+    // true Schur complement is nearly singular along c, far below the mass
+    // estimate.  c^T S c = -(D^T c) . A^-1 (G c) is estimated once per
+    // Jacobian with the velocity solve A^-1 ~ (s K)^-1 (the factor 1/s is
+    // applied on the host below): here t = D K^-1 G c.
+    if(M.nc == 3 || M.inner <= 0) {
+      // the components interleaved (slot nc k + c) through one V-cycle
+      const int64_t nq = (int64_t)M.nc * M.nNodes;
+      if(values64) {
+        ::feng::launch_k(k_gsum_nc<double>, grid(nq), 256, 0, s_, nq, M.upIa, M.upPos, values64, (double *)M.bxy);
+        if(M.nc == 3) M.amg->vcycle3_64((const double *)M.bxy, (double *)M.zxy);
+        else M.amg->vcycle2_64((const double *)M.bxy, (double *)M.zxy, nullptr);
+        ::feng::launch_k(k_dw_nc<double>, grid(M.nP), 256, 0, s_, M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values64,
+                         (const double *)M.zxy, M.tP);
+      } else {
+        ::feng::launch_k(k_gsum_nc<float>, grid(nq), 256, 0, s_, nq, M.upIa, M.upPos, values32, (float *)M.bxy);
+        if(M.nc == 3) M.amg->vcycle3_32((const float *)M.bxy, (float *)M.zxy);
+        else M.amg->vcycle2_32((const float *)M.bxy, (float *)M.zxy, nullptr);
+        ::feng::launch_k(k_dw_nc<float>, grid(M.nP), 256, 0, s_, M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values32,
+                         (const float *)M.zxy, M.tP);
+      }
+    } else {
+      const int g = grid(M.nNodes);
+      if(values64) {
+        ::feng::launch_k(k_gsum<double>, g, 256, 0, s_, M.nNodes, M.upIa, M.upPos, values64, (double *)M.bx, (double *)M.by);
+        M.solveK<double>((const double *)M.bx, (double *)M.zx, s_);
+        M.solveK<double>((const double *)M.by, (double *)M.zy, s_);
+        ::feng::launch_k(k_dw<double>, grid(M.nP), 256, 0, s_, M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values64,
+                         (const double *)M.zx, (const double *)M.zy, M.tP);
+      } else {
+        ::feng::launch_k(k_gsum<float>, g, 256, 0, s_, M.nNodes, M.upIa, M.upPos, values32, (float *)M.bx, (float *)M.by);
+        M.solveK<float>((const float *)M.bx, (float *)M.zx, s_);
+        M.solveK<float>((const float *)M.by, (float *)M.zy, s_);
+        ::feng::launch_k(k_dw<float>, grid(M.nP), 256, 0, s_, M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values32,
+                         (const float *)M.zx, (const float *)M.zy, M.tP);
+      }
+    }
+    const int gp = (int)std::min<int64_t>(NPART, std::max<int64_t>(1, (M.nP + 255) / 256));
+    ::feng::launch_k(k_tsum, gp, 256, 0, s_, M.nP, M.tP, M.part);
+    ::feng::launch_k(k_dot_fin, 1, 256, 0, s_, gp, M.part, M.dsum + 1);
+    CKM(cudaMemcpyAsync(sums, M.dsum, 2 * sizeof(double), cudaMemcpyDeviceToHost, s_));
+  } else {
+    CKM(cudaMemcpyAsync(sums, M.dsum, sizeof(double), cudaMemcpyDeviceToHost, s_));
+  }
   CKM(cudaStreamSynchronize(s_));
+  const double sum = sums[0];
   if(!(std::isfinite(sum)) || sum == 0.) {
     set_error("preconditioner scale: zero or non-finite diagonal");
     return FE_PC_FAILED;
@@ -681,57 +812,16 @@ int Krylov::factor_mg(const double *values64, const float *values32)
   // mu ~ -s / (1.5 sigma) and S^-1 ~ (mu / c_div) M_p^-1.
   M.s = sum / M.lapDiagSum;
   if(M.kind == 4) {
-    // Contiguous copy of the G block's values for the apply kernels.
-    if(values64)
-      ::feng::launch_k(k_gather_vals<double>, grid(M.nG), 256, 0, s_, M.nG, M.upPos, values64, (double *)M.gVals);
-    else
-      ::feng::launch_k(k_gather_vals<float>, grid(M.nG), 256, 0, s_, M.nG, M.upPos, values32, (float *)M.gVals);
     std::vector<double> sc(M.nP);
     std::vector<float> sc32(M.nP);
     for(int64_t k = 0; k < M.nP; ++k) {
       sc[k] = -SCHUR_FACTOR * M.s / (M.vfac * M.sigma * M.divu * M.pMass[k]);
       sc32[k] = (float)sc[k];
     }
+    // (pageable sources: staged before the calls return)
     CKM(cudaMemcpyAsync(M.pScale64, sc.data(), sizeof(double) * M.nP, cudaMemcpyHostToDevice, s_));
     CKM(cudaMemcpyAsync(M.pScale32, sc32.data(), sizeof(float) * M.nP, cudaMemcpyHostToDevice, s_));
-    // Constant pressure mode c: with the pressure fixed at a single point the
-    // true Schur complement is nearly singular along c, far below the mass
-    // estimate.  c^T S c = -(D^T c) . A^-1 (G c) is estimated once per
-    // Jacobian with the velocity solve A^-1 ~ (s K)^-1.
-    const int g = grid(M.nNodes);
-    double sum2 = 0.;
-    if(M.nc == 3) {
-      const int64_t nq = 3 * M.nNodes;
-      if(values64) {
-        ::feng::launch_k(k_gsum_nc<double>, grid(nq), 256, 0, s_, nq, M.upIa, M.upPos, values64, (double *)M.bxy);
-        M.amg->vcycle3_64((const double *)M.bxy, (double *)M.zxy);
-        ::feng::launch_k(k_dw_nc<double>, grid(M.nP), 256, 0, s_, M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values64,
-                                                   (const double *)M.zxy, M.tP);
-      } else {
-        ::feng::launch_k(k_gsum_nc<float>, grid(nq), 256, 0, s_, nq, M.upIa, M.upPos, values32, (float *)M.bxy);
-        M.amg->vcycle3_32((const float *)M.bxy, (float *)M.zxy);
-        ::feng::launch_k(k_dw_nc<float>, grid(M.nP), 256, 0, s_, M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values32,
-                                                  (const float *)M.zxy, M.tP);
-      }
-    } else if(values64) {
-      ::feng::launch_k(k_gsum<double>, g, 256, 0, s_, M.nNodes, M.upIa, M.upPos, values64, (double *)M.bx, (double *)M.by);
-      M.solveK<double>((const double *)M.bx, (double *)M.zx, s_);
-      M.solveK<double>((const double *)M.by, (double *)M.zy, s_);
-      ::feng::launch_k(k_dw<double>, grid(M.nP), 256, 0, s_, M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values64,
-                                                (const double *)M.zx, (const double *)M.zy, M.tP);
-    } else {
-      ::feng::launch_k(k_gsum<float>, g, 256, 0, s_, M.nNodes, M.upIa, M.upPos, values32, (float *)M.bx, (float *)M.by);
-      M.solveK<float>((const float *)M.bx, (float *)M.zx, s_);
-      M.solveK<float>((const float *)M.by, (float *)M.zy, s_);
-      ::feng::launch_k(k_dw<float>, grid(M.nP), 256, 0, s_, M.nP, M.dnIa, M.dnPos, M.dnCol, M.slotOf, values32,
-                                               (const float *)M.zx, (const float *)M.zy, M.tP);
-    }
-    const int gp = (int)std::min<int64_t>(NPART, std::max<int64_t>(1, (M.nP + 255) / 256));
-    ::feng::launch_k(k_tsum, gp, 256, 0, s_, M.nP, M.tP, M.part);
-    ::feng::launch_k(k_dot_fin, 1, 256, 0, s_, gp, M.part, M.dsum);
-    CKM(cudaMemcpyAsync(&sum2, M.dsum, sizeof(double), cudaMemcpyDeviceToHost, s_));
-    CKM(cudaStreamSynchronize(s_));
-    M.cSc = -sum2 / M.s;
+    M.cSc = -sums[1] / M.s;
     // Against the lumped-mass estimate c^T S c ~ -vfac sigma c_div c^T M c / s:
     // a negligible value means the pressure is determined only up to a
     // constant (no pressure DOF fixed); then the constant mode is only
@@ -739,13 +829,42 @@ int Krylov::factor_mg(const double *values64, const float *values32)
     const double massEst = std::fabs(M.vfac * M.sigma * M.divu * M.cMc / M.s);
     if(!std::isfinite(M.cSc) || std::fabs(M.cSc) <= 1e-8 * massEst) M.cSc = 0.;  // no deflation
   }
-  // Scalars read by the (graph-replayed) apply kernels.
+  // Scalars read by the (graph-replayed) apply kernels; the solve that
+  // follows runs on the same stream.
   M.hconst[0] = 1.0 / M.s;
   M.hconst[1] = M.cSc;
   M.hconst[2] = M.cMc;
   M.hconst[3] = M.cc;
   CKM(cudaMemcpyAsync(M.consts, M.hconst, sizeof(double) * 4, cudaMemcpyHostToDevice, s_));
-  CKM(cudaStreamSynchronize(s_));
+  // The pressure fold: the steady two-component preconditioner with one
+  // V-cycle on a sliced-ELL finest level (the fold's output goes through
+  // that level's post-smoothing pass).
+  static const bool foldOn = [] {
+    const char *e = std::getenv("FENG_PFOLD");
+    return !(e && std::strcmp(e, "0") == 0);
+  }();
+  M.fold = foldOn && M.kind == 4 && M.nc == 2 && M.inner <= 0 && !M.amgP && M.amg->fineSell();
+  if(M.fold) {
+    // u_k = 1/cSc - sc_k m_k / cMc: z_p = sc r_p + c u, c = the pressure sum
+    std::vector<double> u(M.nP);
+    const double iS = M.cSc != 0. ? 1.0 / M.cSc : 0., iM = M.cMc > 0 ? 1.0 / M.cMc : 0.;
+    for(int64_t k = 0; k < M.nP; ++k) {
+      const double sck = values64 ? -SCHUR_FACTOR * M.s / (M.vfac * M.sigma * M.divu * M.pMass[k])
+                                  : (double)(float)(-SCHUR_FACTOR * M.s / (M.vfac * M.sigma * M.divu * M.pMass[k]));
+      u[k] = iS - sck * M.pMass[k] * iM;
+    }
+    CKM(cudaMemcpyAsync(M.uP, u.data(), sizeof(double) * M.nP, cudaMemcpyHostToDevice, s_));
+    const int64_t nq = 2 * M.nNodes;
+    if(values64) {
+      ::feng::launch_k(k_fold_prep<double, double>, grid(nq), 256, 0, s_, nq, M.upIa, M.upColP, (const double *)M.gVals,
+                       M.pScale64, M.uP, (double *)M.gScaled, (double *)M.bxy);
+      M.amg->vcycle2_64((const double *)M.bxy, (double *)M.bgu, nullptr);
+    } else {
+      ::feng::launch_k(k_fold_prep<float, float>, grid(nq), 256, 0, s_, nq, M.upIa, M.upColP, (const float *)M.gVals,
+                       M.pScale32, M.uP, (float *)M.gScaled, (float *)M.bxy);
+      M.amg->vcycle2_32((const float *)M.bxy, (float *)M.bgu, nullptr);
+    }
+  }
   return FE_OK;
 }
 
@@ -838,6 +957,35 @@ void Krylov::apply_mg(const V *vals, const V *r, V *z, const int *skip)
     // z = (s K)^-1 r on the unknown rows (the nodes are the unknowns)
     ::feng::launch_k(k_vel_rhs<V>, grid(M.nNodes), 256, 0, s_, M.nNodes, M.dofX, M.dofX, nullptr, nullptr, nullptr,
                                                   vals, r, z, (V *)M.bx, (V *)M.by, skip);
+  } else if(M.fold) {
+    // z_p = sc r_p + c u and b = r_u - G z_p = b0 - c G u with
+    // b0 = r_u - (G sc) r_p, c = the pressure sum: the V-cycle is linear, so
+    // z_u = (V(b0) - c V(G u)) / s with V(G u) = bgu from the set-up.  One
+    // kernel forms b0 and c, the V-cycle's last pass writes z_u and z_p.
+    const int gp = (int)std::min<int64_t>(NPART, std::max<int64_t>(1, (M.nP + 255) / 256));
+    const int slotBlocks = (int)((2 * M.nNodes + 255) / 256);
+    double *cr = M.scal + 3;
+    ::feng::launch_k(k_vel_rhs_fold<V>, slotBlocks + gp, 256, 0, s_, M.nNodes, M.dofX, M.dofY, M.upIa, M.upCol,
+                     (const V *)M.gScaled, r, (V *)M.bxy, slotBlocks, M.nP, M.pRows, M.part, M.count, cr, skip);
+    AMGDevice::OutMap om;
+    om.dofX = M.dofX;
+    om.dofY = M.dofY;
+    om.scale = M.consts;
+    om.z = z;
+    om.cr = cr;
+    om.bgu = M.bgu;
+    om.nP = M.nP;
+    om.pRows = M.pRows;
+    if constexpr(sizeof(V) == 8) om.pScale = M.pScale64;
+    else om.pScale = M.pScale32;
+    om.pMass = M.pMassDev;
+    om.consts = M.consts;
+    om.r = r;
+    bool written;
+    if constexpr(sizeof(V) == 8) written = M.amg->vcycle2_64((const double *)M.bxy, (double *)M.zxy, &om);
+    else written = M.amg->vcycle2_32((const float *)M.bxy, (float *)M.zxy, &om);
+    if(!written) set_error("pressure fold: the finest post-smoothing pass did not write the result");
+    return;
   } else {
     const int gp = (int)std::min<int64_t>(NPART, std::max<int64_t>(1, (M.nP + 255) / 256));
     ::feng::launch_k(k_psum<V>, gp, 256, 0, s_, M.nP, M.pRows, r, M.part, M.count, M.scal + 3);
