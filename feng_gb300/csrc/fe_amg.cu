@@ -122,17 +122,15 @@ __device__ __forceinline__ void row_dot_w(int32_t beg, int32_t end, int sub, con
 }
 
 // y = A x (MODE 0), y = b - A x (MODE 1), y += A x (MODE 2),
-// y = A (b .* x) with b a per-row scale of x (MODE 3), y = b + A x (MODE 4)
+// y = A (b .* x) with b a per-row scale of x (MODE 3), y = b + A x (MODE 4);
+// csr_row: the LANES lanes of virtual thread t's row (row t / LANES).
 template <typename V, int LANES, int MODE, int NV>
-__global__ void __launch_bounds__(256) k_csr(int64_t n, const int32_t *__restrict__ ia,
-                                             const int32_t *__restrict__ ja, const V *__restrict__ a,
-                                             const V *__restrict__ x, const V *__restrict__ b,
-                                             V *__restrict__ y, const int *__restrict__ skip)
+__device__ __forceinline__ void csr_row(int64_t t, int64_t n, const int32_t *__restrict__ ia,
+                                        const int32_t *__restrict__ ja, const V *__restrict__ a,
+                                        const V *__restrict__ x, const V *__restrict__ b, V *__restrict__ y)
 {
-  FE_PDL_ENTRY();
-  if(skip && *skip) return;
-  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
-  const int sub = threadIdx.x % LANES;
+  const int64_t row = t / LANES;
+  const int sub = (int)(t % LANES);
   const bool live = row < n;
   const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
   V acc[NV];
@@ -155,6 +153,17 @@ __global__ void __launch_bounds__(256) k_csr(int64_t n, const int32_t *__restric
       else y[o] += acc[c];
     }
   }
+}
+
+template <typename V, int LANES, int MODE, int NV>
+__global__ void __launch_bounds__(256) k_csr(int64_t n, const int32_t *__restrict__ ia,
+                                             const int32_t *__restrict__ ja, const V *__restrict__ a,
+                                             const V *__restrict__ x, const V *__restrict__ b,
+                                             V *__restrict__ y, const int *__restrict__ skip)
+{
+  FE_PDL_ENTRY();
+  if(skip && *skip) return;
+  csr_row<V, LANES, MODE, NV>((int64_t)blockIdx.x * blockDim.x + threadIdx.x, n, ia, ja, a, x, b, y);
 }
 
 template <typename V, int MODE, int NV>
@@ -246,16 +255,14 @@ __global__ void __launch_bounds__(256) k_cheb_step(int64_t n, const int32_t *__r
 // (formed on the fly for the neighbours), x = d, r = D^-1 b - D^-1 A d,
 // dn = c1 d + c2 r.
 template <typename V, int LANES, int NV>
-__global__ void __launch_bounds__(256) k_cheb_first(int64_t n, const int32_t *__restrict__ ia,
-                                                    const int32_t *__restrict__ ja, const V *__restrict__ a,
-                                                    const V *__restrict__ dinv, const V *__restrict__ b,
-                                                    V *__restrict__ dn, V *__restrict__ r, V *__restrict__ x,
-                                                    V inv_theta, V c1, V c2, const int *__restrict__ skip)
+__device__ __forceinline__ void cheb_first_row(int64_t t, int64_t n, const int32_t *__restrict__ ia,
+                                               const int32_t *__restrict__ ja, const V *__restrict__ a,
+                                               const V *__restrict__ dinv, const V *__restrict__ b,
+                                               V *__restrict__ dn, V *__restrict__ r, V *__restrict__ x,
+                                               V inv_theta, V c1, V c2)
 {
-  FE_PDL_ENTRY();
-  if(skip && *skip) return;
-  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
-  const int sub = threadIdx.x % LANES;
+  const int64_t row = t / LANES;
+  const int sub = (int)(t % LANES);
   const bool live = row < n;
   const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
   V acc[NV];
@@ -280,24 +287,34 @@ __global__ void __launch_bounds__(256) k_cheb_first(int64_t n, const int32_t *__
   }
 }
 
+template <typename V, int LANES, int NV>
+__global__ void __launch_bounds__(256) k_cheb_first(int64_t n, const int32_t *__restrict__ ia,
+                                                    const int32_t *__restrict__ ja, const V *__restrict__ a,
+                                                    const V *__restrict__ dinv, const V *__restrict__ b,
+                                                    V *__restrict__ dn, V *__restrict__ r, V *__restrict__ x,
+                                                    V inv_theta, V c1, V c2, const int *__restrict__ skip)
+{
+  FE_PDL_ENTRY();
+  if(skip && *skip) return;
+  cheb_first_row<V, LANES, NV>((int64_t)blockIdx.x * blockDim.x + threadIdx.x, n, ia, ja, a, dinv, b, dn, r, x,
+                               inv_theta, c1, c2);
+}
+
 // Degree-1 post-smoothing from the prolongated y = x + P xc:
 // x = y + D^-1 (b - A y) / theta (x and y distinct).
 // OUT (the finest level of a paired V-cycle whose result goes straight to
 // the caller's vector): component c of row i is written, times *scale, to
 // out[dof[c][i]] instead of x.
 template <typename V, int LANES, int NV, bool OUT>
-__global__ void __launch_bounds__(256) k_cheb_post(int64_t n, const int32_t *__restrict__ ia,
-                                                   const int32_t *__restrict__ ja, const V *__restrict__ a,
-                                                   const V *__restrict__ dinv, const V *__restrict__ b,
-                                                   const V *__restrict__ y, V *__restrict__ x, V inv_theta,
-                                                   const int *__restrict__ skip, const int32_t *__restrict__ dofX,
-                                                   const int32_t *__restrict__ dofY, const double *__restrict__ scale,
-                                                   V *__restrict__ out)
+__device__ __forceinline__ void cheb_post_row(int64_t t, int64_t n, const int32_t *__restrict__ ia,
+                                              const int32_t *__restrict__ ja, const V *__restrict__ a,
+                                              const V *__restrict__ dinv, const V *__restrict__ b,
+                                              const V *__restrict__ y, V *__restrict__ x, V inv_theta,
+                                              const int32_t *__restrict__ dofX, const int32_t *__restrict__ dofY,
+                                              const double *__restrict__ scale, V *__restrict__ out)
 {
-  FE_PDL_ENTRY();
-  if(skip && *skip) return;
-  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
-  const int sub = threadIdx.x % LANES;
+  const int64_t row = t / LANES;
+  const int sub = (int)(t % LANES);
   const bool live = row < n;
   const int32_t beg = live ? ia[row] : 0, end = live ? ia[row + 1] : 0;
   V acc[NV];
@@ -313,6 +330,21 @@ __global__ void __launch_bounds__(256) k_cheb_post(int64_t n, const int32_t *__r
     if(OUT) out[sub == 0 ? dofX[row] : dofY[row]] = xo * (V)*scale;
     else x[o] = xo;
   }
+}
+
+template <typename V, int LANES, int NV, bool OUT>
+__global__ void __launch_bounds__(256) k_cheb_post(int64_t n, const int32_t *__restrict__ ia,
+                                                   const int32_t *__restrict__ ja, const V *__restrict__ a,
+                                                   const V *__restrict__ dinv, const V *__restrict__ b,
+                                                   const V *__restrict__ y, V *__restrict__ x, V inv_theta,
+                                                   const int *__restrict__ skip, const int32_t *__restrict__ dofX,
+                                                   const int32_t *__restrict__ dofY, const double *__restrict__ scale,
+                                                   V *__restrict__ out)
+{
+  FE_PDL_ENTRY();
+  if(skip && *skip) return;
+  cheb_post_row<V, LANES, NV, OUT>((int64_t)blockIdx.x * blockDim.x + threadIdx.x, n, ia, ja, a, dinv, b, y, x,
+                                   inv_theta, dofX, dofY, scale, out);
 }
 
 // Walks the len entries of row lane of a sliced-ELL slice (entry k at

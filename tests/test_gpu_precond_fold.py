@@ -52,3 +52,4 @@ def test_folded_preconditioner_matches_unfolded(precision, tmp_path):
     assert np.max(np.abs(ua - ub)) <= 1e-7 * np.max(np.abs(ub))
     if a["krylov"] >= 0 and b["krylov"] >= 0:
         assert abs(a["krylov"] - b["krylov"]) <= max(3, 0.05 * b["krylov"]), (a, b)
+
