@@ -433,11 +433,13 @@ __global__ void __launch_bounds__(256) k_cheb_post_sell(int64_t n, const int32_t
 {
   FE_PDL_ENTRY();
   if(skip && *skip) return;
+  int64_t blk = blockIdx.x;
   if constexpr(OUT) {
-    const int64_t rowBlocks = (n + 255) / 256;
-    if((int64_t)blockIdx.x >= rowBlocks) {
-      // pressure rows of the folded saddle-point preconditioner
-      const int64_t k = ((int64_t)blockIdx.x - rowBlocks) * 256 + threadIdx.x;
+    // the pressure rows of the folded saddle-point preconditioner in the
+    // leading blocks (scheduled first, overlapping the rows)
+    const int64_t pBlocks = om.bgu ? (om.nP + 255) / 256 : 0;
+    if(blk < pBlocks) {
+      const int64_t k = blk * 256 + threadIdx.x;
       if(k >= om.nP) return;
       const double c = *om.cr, cSc = om.consts[1], cMc = om.consts[2];
       const double shift = cMc > 0 ? c / cMc : 0., lift = cSc != 0. ? c / cSc : 0.;
@@ -446,8 +448,9 @@ __global__ void __launch_bounds__(256) k_cheb_post_sell(int64_t n, const int32_t
       ((V *)om.z)[i] = (V)((double)((const V *)om.pScale)[k] * rp + lift);
       return;
     }
+    blk -= pBlocks;
   }
-  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t row = blk * blockDim.x + threadIdx.x;
   if(row >= n) return;
   const int64_t sl = row >> 5;
   const int lane = (int)(row & 31);

@@ -478,9 +478,10 @@ __global__ void k_vel_rhs_pair(int64_t nN, const int32_t *__restrict__ dofX, con
 }
 
 // Folded velocity right-hand side b0 = r_u - (G sc) r_p on the slots
-// (both components interleaved, one thread per slot), and in the trailing
-// gp blocks the pressure sum c = sum of r over the pressure rows (k_psum's
-// partials and order) into *cr.
+// (both components interleaved, one thread per slot), and in the leading
+// gp blocks (scheduled first, so that the sum's last-block reduction
+// overlaps the slots) the pressure sum c = sum of r over the pressure rows
+// (k_psum's partials and order) into *cr.
 template <typename V>
 __global__ void k_vel_rhs_fold(int64_t nN, const int32_t *__restrict__ dofX, const int32_t *__restrict__ dofY,
                                const int32_t *__restrict__ upIa, const int32_t *__restrict__ upCol,
@@ -490,11 +491,12 @@ __global__ void k_vel_rhs_fold(int64_t nN, const int32_t *__restrict__ dofX, con
 {
   FE_PDL_ENTRY();
   if(skip && *skip) return;
-  if((int)blockIdx.x >= slotBlocks) {
-    psum_blocks<V>((int)blockIdx.x - slotBlocks, (int)gridDim.x - slotBlocks, nP, pRows, r, part, count, cr);
+  const int gp = (int)gridDim.x - slotBlocks;
+  if((int)blockIdx.x < gp) {
+    psum_blocks<V>((int)blockIdx.x, gp, nP, pRows, r, part, count, cr);
     return;
   }
-  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t q = (int64_t)((int)blockIdx.x - gp) * blockDim.x + threadIdx.x;
   if(q >= 2 * nN) return;
   const int64_t k = q >> 1;
   V t = r[(q & 1) == 0 ? dofX[k] : dofY[k]];
