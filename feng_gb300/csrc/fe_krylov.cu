@@ -302,14 +302,54 @@ __device__ void givens_warp(GmresState *gs, int j, int lane, double *sh, double 
     ssn[i] = gs->sn[i];
   }
   __syncwarp();
-  if(lane == 0) {
-    double hi = sh[0];
-    for(int i = 0; i < j; ++i) {
-      const double c = scs[i], s = ssn[i], hn = sh[i + 1];
-      sh[i] = c * hi + s * hn;
-      hi = -s * hi + c * hn;
+  // The chain t_0 = h_0, t_{i+1} = -s_i t_i + c_i h_{i+1}, h_i <- c_i t_i +
+  // s_i h_{i+1}, h_j <- t_j is an affine recurrence: lane l composes the
+  // maps t -> -s_i t + c_i h_{i+1} of its GCH consecutive rotations, a warp
+  // scan composes the lanes' maps (Hillis-Steele, five shuffle rounds), and
+  // each lane replays its rotations from its start value: ~25 dependent FP64
+  // operations instead of two per rotation in sequence.
+  {
+    constexpr int GCH = (MAXM + 31) / 32;
+    const int i0 = lane * GCH;
+    const double h0 = sh[0];
+    double cv[GCH], sv[GCH], hv[GCH];
+    double A = 1., B = 0.;  // the lane's map t -> A t + B
+#pragma unroll
+    for(int u = 0; u < GCH; ++u) {
+      const bool ok = i0 + u < j;
+      cv[u] = ok ? scs[i0 + u] : 1.;
+      sv[u] = ok ? ssn[i0 + u] : 0.;
+      hv[u] = ok ? sh[i0 + u + 1] : 0.;
+      if(ok) {
+        const double al = -sv[u], be = cv[u] * hv[u];
+        A = al * A;
+        B = al * B + be;
+      }
     }
-    sh[j] = hi;
+    // inclusive scan: (A, B) <- (A, B) o (lane - off's map)
+#pragma unroll
+    for(int off = 1; off < 32; off <<= 1) {
+      const double Ap = __shfl_up_sync(0xffffffffu, A, off), Bp = __shfl_up_sync(0xffffffffu, B, off);
+      if(lane >= off) {
+        B = A * Bp + B;
+        A = A * Ap;
+      }
+    }
+    // exclusive: the composition of the lanes before this one
+    double Ae = __shfl_up_sync(0xffffffffu, A, 1), Be = __shfl_up_sync(0xffffffffu, B, 1);
+    if(lane == 0) {
+      Ae = 1.;
+      Be = 0.;
+    }
+    __syncwarp();  // every read of sh before the writes below
+    double t = Ae * h0 + Be;
+#pragma unroll
+    for(int u = 0; u < GCH; ++u)
+      if(i0 + u < j) {
+        sh[i0 + u] = cv[u] * t + sv[u] * hv[u];
+        t = -sv[u] * t + cv[u] * hv[u];
+        if(i0 + u == j - 1) sh[j] = t;
+      }
   }
   __syncwarp();
   for(int i = lane; i < j; i += 32) h[i] = sh[i];
