@@ -504,6 +504,24 @@ __global__ void k_vel_rhs_fold(int64_t nN, const int32_t *__restrict__ dofX, con
   bxy[q] = t;
 }
 
+// Per Jacobian: the pressure scale sc_k = coef / (den m_k) in FP64 and
+// FP32 and, for the pressure fold (u non-null), u_k = iS - sc_k m_k iM with
+// sc_k as the apply kernels read it (FP32-rounded when fp32).
+__global__ void k_pressure_scale(int64_t nP, double coef, double den, const double *__restrict__ mass,
+                                 double *__restrict__ sc64, float *__restrict__ sc32, double *__restrict__ u,
+                                 double iS, double iM, int fp32)
+{
+  FE_PDL_ENTRY();
+  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nP; k += (int64_t)gridDim.x * blockDim.x) {
+    const double m = mass[k];
+    const double sc = coef / (den * m);
+    const float s32 = (float)sc;
+    sc64[k] = sc;
+    sc32[k] = s32;
+    if(u) u[k] = iS - (fp32 ? (double)s32 : sc) * m * iM;
+  }
+}
+
 // Per Jacobian, for the pressure fold: gScaled[e] = G_e sc_k(e) and
 // gu[q] = sum_e G_e u_k(e) on slot q (FP64 sums).
 template <typename V, typename S>
@@ -814,15 +832,6 @@ int Krylov::factor_mg(const double *values64, const float *values32)
   // mu ~ -s / (1.5 sigma) and S^-1 ~ (mu / c_div) M_p^-1.
   M.s = sum / M.lapDiagSum;
   if(M.kind == 4) {
-    std::vector<double> sc(M.nP);
-    std::vector<float> sc32(M.nP);
-    for(int64_t k = 0; k < M.nP; ++k) {
-      sc[k] = -SCHUR_FACTOR * M.s / (M.vfac * M.sigma * M.divu * M.pMass[k]);
-      sc32[k] = (float)sc[k];
-    }
-    // (pageable sources: staged before the calls return)
-    CKM(cudaMemcpyAsync(M.pScale64, sc.data(), sizeof(double) * M.nP, cudaMemcpyHostToDevice, s_));
-    CKM(cudaMemcpyAsync(M.pScale32, sc32.data(), sizeof(float) * M.nP, cudaMemcpyHostToDevice, s_));
     M.cSc = -sums[1] / M.s;
     // Against the lumped-mass estimate c^T S c ~ -vfac sigma c_div c^T M c / s:
     // a negligible value means the pressure is determined only up to a
@@ -846,16 +855,14 @@ int Krylov::factor_mg(const double *values64, const float *values32)
     return !(e && std::strcmp(e, "0") == 0);
   }();
   M.fold = foldOn && M.kind == 4 && M.nc == 2 && M.inner <= 0 && !M.amgP && M.amg->fineSell();
-  if(M.fold) {
-    // u_k = 1/cSc - sc_k m_k / cMc: z_p = sc r_p + c u, c = the pressure sum
-    std::vector<double> u(M.nP);
+  if(M.kind == 4) {
+    // the pressure scale (FP64 and FP32) and, for the fold, u on the device
+    const double coef = -SCHUR_FACTOR * M.s, den = M.vfac * M.sigma * M.divu;
     const double iS = M.cSc != 0. ? 1.0 / M.cSc : 0., iM = M.cMc > 0 ? 1.0 / M.cMc : 0.;
-    for(int64_t k = 0; k < M.nP; ++k) {
-      const double sck = values64 ? -SCHUR_FACTOR * M.s / (M.vfac * M.sigma * M.divu * M.pMass[k])
-                                  : (double)(float)(-SCHUR_FACTOR * M.s / (M.vfac * M.sigma * M.divu * M.pMass[k]));
-      u[k] = iS - sck * M.pMass[k] * iM;
-    }
-    CKM(cudaMemcpyAsync(M.uP, u.data(), sizeof(double) * M.nP, cudaMemcpyHostToDevice, s_));
+    ::feng::launch_k(k_pressure_scale, grid(M.nP), 256, 0, s_, M.nP, coef, den, M.pMassDev, M.pScale64, M.pScale32,
+                     M.fold ? M.uP : (double *)nullptr, iS, iM, values64 ? 0 : 1);
+  }
+  if(M.fold) {
     const int64_t nq = 2 * M.nNodes;
     if(values64) {
       ::feng::launch_k(k_fold_prep<double, double>, grid(nq), 256, 0, s_, nq, M.upIa, M.upColP, (const double *)M.gVals,
