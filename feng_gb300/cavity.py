@@ -97,11 +97,11 @@ def main(argv=None):
     args = ap.parse_args(argv)
     learn = dict(trainFrom=args.train_from, useFrom=args.use_from, trainIters=args.train_iters, lr=args.lr,
                  batch=args.batch) if args.guess == "learned" else {}
-    _, stats = run(args.n, args.re, args.dt, args.steps, args.guess, args.precision,
-                   solver=dict(gs_passes=args.gs_passes, restart=args.restart), **learn)
+    sys_, stats = run(args.n, args.re, args.dt, args.steps, args.guess, args.precision,
+                      solver=dict(gs_passes=args.gs_passes, restart=args.restart), **learn)
     print(json.dumps({"case": f"cavity_re{args.re:g}_{args.n}x{args.n}_dt{args.dt:g}", "guess": args.guess,
                       "precision": args.precision, "summary": summarize(stats, args.summary_from),
-                      "steps": stats}))
+                      "phase_ms_total": sys_.times(), "steps": stats}))
 
 
 if __name__ == "__main__":

@@ -1316,7 +1316,8 @@ Krylov::~Krylov()
   cudaFree(ilu_.ldiag); cudaFree(ilu_.srcPos); cudaFree(ilu_.vals); cudaFree(ilu_.status);
   cudaFree(ilu_.rowsL); cudaFree(ilu_.rowsU); cudaFree(ilu_.lvlL); cudaFree(ilu_.lvlU);
   cudaFree(red_state_); cudaFree(gmres_); cudaFree(cg_);
-  cudaFreeHost(h_gmres_); cudaFreeHost(h_cg_); cudaFreeHost(hflag_); cudaFreeHost(htol_);
+  cudaFreeHost(h_gmres_); cudaFreeHost(h_cg_); cudaFreeHost(hflag_); cudaFreeHost(htol_); cudaFreeHost(hdone_);
+  for(auto e : evs_) cudaEventDestroy(e);
   for(auto &g : graphs_) cudaGraphExecDestroy(g.second);
   delete mg_;
 }
@@ -1417,6 +1418,12 @@ int Krylov::setup(const DeviceCSR &A, const std::vector<int32_t> &blockOfRow, in
   CK(cudaMallocHost(&h_cg_, sizeof(CGState)));
   CK(cudaMallocHost(&hflag_, sizeof(int)));
   CK(cudaMallocHost(&htol_, sizeof(double)));
+  CK(cudaMallocHost(&hdone_, sizeof(int) * (MAXM + 1)));
+  {
+    // Arnoldi steps per part graph of a mixed cycle (0: one graph per cycle)
+    const char *e = std::getenv("FENG_GMRES_CHUNK");
+    chunk_ = e ? std::atoi(e) : 5;
+  }
 
   if(opt.precond == 3 || opt.precond == 4) {
     if(!pinfo) {
@@ -2223,17 +2230,27 @@ void Krylov::launch_cycle(bool mixed, const void *vals, const double *b, double 
 // and Givens rotations, FP64 solution update.
 void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, int jmax, bool poll)
 {
+  mixed_part(vals, b, x, 0, jmax, poll, true, true);
+}
+
+// Part of a mixed restart cycle: the prologue (restart residual, its norm,
+// v_0) when `pro`, the Arnoldi steps j0 <= j < j1, the epilogue
+// (back-substitution, x update, head copy) when `epi`.
+void Krylov::mixed_part(const float *vals, const double *b, double *x, int j0, int j1, bool poll, bool pro, bool epi)
+{
   Ws w = Ws_INIT(this);
   const int gv = grid_for(n_, 256, 2048);
+  const int m1 = opt.restart + 1;
+  if(pro) {
   resid32(vals, x, b, w_);
   cudaMemsetAsync(&w.gs->done, 0, sizeof(int), s_);
   cudaMemcpyAsync(&w.gs->tol, htol_, sizeof(double), cudaMemcpyHostToDevice, s_);
   ::feng::launch_k(k_norm_to, nParts_, RB, 0, s_, n_, w_, red_, w.st, &w.gs->done);
   ::feng::launch_k(k_gmres_init, 1, 1, 0, s_, w.gs, w.st);
-  const int m1 = opt.restart + 1;
   ::feng::launch_k(k_scale_r32, gv, 256, 0, s_, n_, w_, V32_, m1, vc32_, w.st, &w.gs->beta, &w.gs->done);
+  }
   const int g4 = grid_for(ld32_ / 4, 256, 4 * 152);
-  for(int j = 0; j < jmax; ++j) {
+  for(int j = j0; j < j1; ++j) {
     // v_j: the contiguous copy written with basis column j
     const float *vj = vc32_;
     float *zj = Z32_ + (int64_t)j * ld32_;
@@ -2278,6 +2295,7 @@ void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, i
     }
     if(poll && poll_done(&w.gs->done, j)) break;
   }
+  if(!epi) return;
   ::feng::launch_k(k_backsolve, 1, 256, backsolveSmem(opt.restart), s_, w.gs);
   ::feng::launch_k(k_xupdate<float>, gv, 256, 0, s_, n_, ld32_, Z32_, w.gs, x);
   cudaMemcpyAsync(h_gmres_, w.gs, sizeof(GmresHead), cudaMemcpyDeviceToHost, s_);
@@ -2285,15 +2303,101 @@ void Krylov::launch_cycle_mixed(const float *vals, const double *b, double *x, i
 
 // Runs one full restart cycle, from a CUDA graph when the cycle has its full
 // length (the graph is captured once per operand set and replayed).
+// A graph per part of the mixed cycle (part c: steps [cK, cK + K), the
+// prologue with part 0, then a copy of the done flag to pinned memory;
+// part P: the epilogue), looked up or captured.
+int Krylov::part_graph(const GraphKey &key, int part, int P, int K, const float *vals, const double *b, double *x,
+                       cudaGraphExec_t *out, size_t *nKernels)
+{
+  for(size_t i = 0; i < graphs_.size(); ++i) {
+    const GraphKey &g = graphs_[i].first;
+    if(g.mixed == key.mixed && g.vals == key.vals && g.b == key.b && g.x == key.x && g.dfResid == key.dfResid &&
+       g.part == part) {
+      *nKernels = graphKernels_[i];
+      *out = graphs_[i].second;
+      return FE_OK;
+    }
+  }
+  const int m = opt.restart;
+  cudaGraph_t graph;
+  cudaGraphExec_t exec = nullptr;
+  CK(cudaStreamBeginCapture(s_, cudaStreamCaptureModeThreadLocal));
+  ++g_capturing;
+  if(part == P) {
+    mixed_part(vals, b, x, 0, 0, false, false, true);
+  } else {
+    mixed_part(vals, b, x, part * K, std::min(m, part * K + K), false, part == 0, false);
+    Ws w = Ws_INIT(this);
+    cudaMemcpyAsync(hdone_ + part, &w.gs->done, sizeof(int), cudaMemcpyDeviceToHost, s_);
+  }
+  --g_capturing;
+  CK(cudaStreamEndCapture(s_, &graph));
+  CK(cudaGraphInstantiate(&exec, graph, 0));
+  size_t nn = 0, nk = 0;
+  CK(cudaGraphGetNodes(graph, nullptr, &nn));
+  std::vector<cudaGraphNode_t> nodes(nn);
+  CK(cudaGraphGetNodes(graph, nodes.data(), &nn));
+  for(auto nd : nodes) {
+    cudaGraphNodeType t;
+    CK(cudaGraphNodeGetType(nd, &t));
+    if(t == cudaGraphNodeTypeKernel) ++nk;
+  }
+  cudaGraphDestroy(graph);
+  GraphKey k2 = key;
+  k2.part = part;
+  graphs_.push_back({k2, exec});
+  graphKernels_.push_back(nk);
+  *nKernels = nk;
+  *out = exec;
+  return FE_OK;
+}
+
+// One full mixed restart cycle from part graphs of chunk_ Arnoldi steps:
+// part c + 1 is queued before the done flag of part c is read, so the GPU
+// always has work and a converged cycle stops within one part (instead of
+// replaying every remaining step's kernels, which return at once).
+int Krylov::run_cycle_chunked(const float *vals, const double *b, double *x)
+{
+  const int m = opt.restart, K = chunk_, P = (m + K - 1) / K;
+  GraphKey key{true, vals, b, x, dfResid_, -1};
+  if(evs_.size() < (size_t)P) {
+    for(size_t i = evs_.size(); i < (size_t)P; ++i) {
+      cudaEvent_t e;
+      CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      evs_.push_back(e);
+    }
+  }
+  size_t nk = 0;
+  for(int c = 0; c < P; ++c) {
+    cudaGraphExec_t ex = nullptr;
+    FE_TRY(part_graph(key, c, P, K, vals, b, x, &ex, &nk));
+    CK(cudaGraphLaunch(ex, s_));
+    g_launches.fetch_add((long long)nk, std::memory_order_relaxed);
+    CK(cudaEventRecord(evs_[c], s_));
+    if(c > 0) {
+      CK(cudaEventSynchronize(evs_[c - 1]));
+      if(hdone_[c - 1]) break;
+    }
+  }
+  cudaGraphExec_t ex = nullptr;
+  FE_TRY(part_graph(key, P, P, K, vals, b, x, &ex, &nk));
+  CK(cudaGraphLaunch(ex, s_));
+  g_launches.fetch_add((long long)nk, std::memory_order_relaxed);
+  CK(cudaStreamSynchronize(s_));
+  CK(cudaGetLastError());
+  return FE_OK;
+}
+
 int Krylov::run_cycle(bool mixed, const void *vals, const double *b, double *x, int jmax)
 {
   const int m = opt.restart;
+  if(useGraphs_ && jmax == m && mixed && chunk_ > 0 && chunk_ < m) return run_cycle_chunked((const float *)vals, b, x);
   if(useGraphs_ && jmax == m) {
-    GraphKey key{mixed, vals, b, x, mixed && dfResid_};
+    GraphKey key{mixed, vals, b, x, mixed && dfResid_, -1};
     cudaGraphExec_t exec = nullptr;
     for(auto &g : graphs_)
       if(g.first.mixed == key.mixed && g.first.vals == key.vals && g.first.b == key.b && g.first.x == key.x &&
-         g.first.dfResid == key.dfResid)
+         g.first.dfResid == key.dfResid && g.first.part == -1)
         exec = g.second;
     size_t nKernels = 0;
     if(!exec) {

@@ -193,6 +193,11 @@ class Krylov {
   bool poll_done(const int *dflag, int j);
   void launch_cycle(bool mixed, const void *vals, const double *b, double *x, int jmax, bool poll);
   void launch_cycle_mixed(const float *vals, const double *b, double *x, int jmax, bool poll);
+  void mixed_part(const float *vals, const double *b, double *x, int j0, int j1, bool poll, bool pro, bool epi);
+  int run_cycle_chunked(const float *vals, const double *b, double *x);
+  int chunk_ = 5;               // Arnoldi steps per part graph of a mixed cycle
+  int *hdone_ = nullptr;        // pinned: the done flag after each part
+  std::vector<cudaEvent_t> evs_;
   int run_cycle(bool mixed, const void *vals, const double *b, double *x, int jmax);
   struct GraphKey {
     bool mixed;
@@ -200,7 +205,10 @@ class Krylov {
     const double *b;
     double *x;
     bool dfResid;
+    int part;  // -1: the whole cycle; else a part of a chunked mixed cycle
   };
+  int part_graph(const GraphKey &key, int part, int P, int K, const float *vals, const double *b, double *x,
+                 cudaGraphExec_t *out, size_t *nKernels);
   std::vector<std::pair<GraphKey, cudaGraphExec_t>> graphs_;
   std::vector<size_t> graphKernels_;  // kernel nodes of each graph
 
