@@ -281,27 +281,9 @@ __global__ void k_pressure(int64_t nP, const int32_t *__restrict__ rows, const S
   }
 }
 
-// partial sums of r over the pressure rows
-template <typename V>
-__global__ void k_psum_part(int64_t nP, const int32_t *__restrict__ rows, const V *__restrict__ r, double *part)
-{
-  FE_PDL_ENTRY();
-  __shared__ double sh[256];
-  double s = 0.;
-  for(int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nP; k += (int64_t)gridDim.x * blockDim.x)
-    s += (double)r[rows[k]];
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  for(int o = 128; o > 0; o >>= 1) {
-    if(threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-    __syncthreads();
-  }
-  if(threadIdx.x == 0) part[blockIdx.x] = sh[0];
-}
-
-// *out = sum of r over the pressure rows in one launch: the partial sums of
-// k_psum_part, then the last block to finish sums them as k_dot_fin does
-// (same order, same bits).  psum_blocks: the body, run by vg blocks with
+// *out = sum of r over the pressure rows in one launch: one partial sum per
+// block, then the last block to finish sums them in block order as
+// k_dot_fin does (deterministic).  psum_blocks: the body, run by vg blocks with
 // block index vb (the whole grid of k_psum, or a trailing range of blocks
 // of k_vel_rhs_fold).
 template <typename V>
